@@ -1,0 +1,248 @@
+"""ctypes front end of the C oracle (oracle/tracefem_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
+the checker and by bench.py for the CPU baseline.  The product path never
+imports it.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libtf_oracle.so")
+
+OK = 0
+ERR_ZERO_NODE = 2
+ERR_ZERO_PATTERN = 3
+FORM_M, FORM_A, FORM_CN, FORM_LAPM = 0, 1, 2, 3
+NUM_FORMS = 4
+LS_SPHERE, LS_TORUS, LS_ELLIPSOID, LS_PLANE = 0, 1, 2, 3
+RHS_NONE, RHS_SPHERE_XYZ, RHS_CONST = 0, 1, 2
+
+
+def build(force=False):
+    """Compile the oracle with gcc (no contraction, so x86 and Arm agree)."""
+    src = os.path.join(HERE, "tracefem_oracle.c")
+    os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= max(
+        os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "tracefem_oracle.h"))
+    ):
+        return LIB_PATH
+    subprocess.check_call(
+        ["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", src, "-o", LIB_PATH, "-lm"]
+    )
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        i64, i32p, f64p, u8p, i64p = C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_uint8), C.POINTER(C.c_int64)
+        L.orc_brick_num_vertices.restype = i64
+        L.orc_brick_num_edges.restype = i64
+        L.orc_brick_num_tets.restype = i64
+        L.orc_ls_value.restype = C.c_double
+        L.orc_kahan_dot.restype = C.c_double
+        _lib = L
+    return _lib
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct)) if a is not None else None
+
+
+class Mesh:
+    def __init__(self, coords, tet_v, tet_e, edge_v):
+        self.coords, self.tet_v, self.tet_e, self.edge_v = coords, tet_v, tet_e, edge_v
+        self.nv = coords.shape[0]
+        self.nt = tet_v.shape[0]
+        self.ne = edge_v.shape[0]
+
+
+def brick(n, a=None, orig=None, e=None):
+    """BrickBuilderCL over [-a,a]^3 with n^3 cubes (or explicit orig / e1,e2,e3)."""
+    L = lib()
+    if isinstance(n, int):
+        n = (n, n, n)
+    if orig is None:
+        orig = np.array([-a, -a, -a], dtype=np.float64)
+        e = np.diag([2.0 * a] * 3)
+    orig = np.ascontiguousarray(orig, dtype=np.float64)
+    e = np.ascontiguousarray(e, dtype=np.float64)
+    nv = L.orc_brick_num_vertices(*n)
+    ne = L.orc_brick_num_edges(*n)
+    nt = L.orc_brick_num_tets(*n)
+    coords = np.empty((nv, 3), np.float64)
+    tet_v = np.empty((nt, 4), np.int32)
+    tet_e = np.empty((nt, 6), np.int32)
+    edge_v = np.empty((ne, 2), np.int32)
+    L.orc_brick(_p(orig, C.c_double), _p(e[0].copy(), C.c_double), _p(e[1].copy(), C.c_double),
+                _p(e[2].copy(), C.c_double), C.c_int(n[0]), C.c_int(n[1]), C.c_int(n[2]),
+                _p(coords, C.c_double), _p(tet_v, C.c_int32), _p(tet_e, C.c_int32), _p(edge_v, C.c_int32))
+    return Mesh(coords, tet_v, tet_e, edge_v)
+
+
+def levelset(mesh, kind, par, p2):
+    L = lib()
+    par = np.ascontiguousarray(par, dtype=np.float64)
+    lv = np.empty(mesh.nv, np.float64)
+    le = np.empty(mesh.ne, np.float64)
+    L.orc_levelset(C.c_int(kind), _p(par, C.c_double), C.c_int(int(p2)), C.c_int64(mesh.nv), C.c_int64(mesh.ne),
+                   _p(mesh.coords, C.c_double), _p(mesh.edge_v, C.c_int32), _p(lv, C.c_double), _p(le, C.c_double))
+    return lv, le
+
+
+def distribute_dofs(mesh, ls_vert, ls_edge, p2, dist=0.0):
+    L = lib()
+    na, nd = C.c_int64(), C.c_int64()
+    dv = np.empty(mesh.nv, np.int32)
+    de = np.empty(mesh.ne, np.int32)
+    act = np.empty(mesh.nt, np.uint8)
+    st = L.orc_distribute_dofs(C.c_int64(mesh.nt), _p(mesh.tet_v, C.c_int32), _p(mesh.tet_e, C.c_int32),
+                               C.c_int64(mesh.nv), C.c_int64(mesh.ne), _p(ls_vert, C.c_double),
+                               _p(ls_edge, C.c_double), C.c_int(int(p2)), C.c_double(dist), C.byref(na),
+                               C.byref(nd), _p(dv, C.c_int32), _p(de, C.c_int32), _p(act, C.c_uint8))
+    return st, na.value, nd.value, dv, (de if p2 else None), act
+
+
+def numb_on_interface_p1(mesh, ls_vert, ls_edge, omit_bound=-1.0):
+    L = lib()
+    na, nd = C.c_int64(), C.c_int64()
+    dv = np.empty(mesh.nv, np.int32)
+    st = L.orc_numb_on_interface_p1(C.c_int64(mesh.nt), _p(mesh.tet_v, C.c_int32), _p(mesh.tet_e, C.c_int32),
+                                    C.c_int64(mesh.nv), _p(mesh.coords, C.c_double), _p(ls_vert, C.c_double),
+                                    _p(ls_edge, C.c_double), C.c_double(omit_bound), C.byref(na), C.byref(nd),
+                                    _p(dv, C.c_int32))
+    return st, na.value, nd.value, dv
+
+
+class PatchT(C.Structure):
+    _fields_ = [("n_facets", C.c_int), ("n_verts", C.c_int), ("n_cut_verts", C.c_int),
+                ("facet", (C.c_int * 3) * 16), ("boundary", C.c_int * 16), ("bary", (C.c_double * 4) * 40)]
+
+
+def make_patch(ls10):
+    L = lib()
+    ls10 = np.ascontiguousarray(ls10, dtype=np.float64)
+    P = PatchT()
+    st = L.orc_make_patch(_p(ls10, C.c_double), C.byref(P))
+    facets = np.array([[P.facet[i][j] for j in range(3)] for i in range(P.n_facets)], dtype=np.int64).reshape(-1, 3)
+    bnd = np.array([P.boundary[i] for i in range(P.n_facets)], dtype=np.int64)
+    verts = np.array([[P.bary[i][j] for j in range(4)] for i in range(P.n_verts)]).reshape(-1, 4)
+    return st, facets, bnd, verts
+
+
+class AssembleOpts(C.Structure):
+    _fields_ = [("p2", C.c_int), ("forms", C.c_uint), ("rhs_kind", C.c_int), ("rhs_par", C.c_double * 8),
+                ("chi", C.POINTER(C.c_double)), ("degenerate", C.c_int)]
+
+
+def make_opts(p2, forms, rhs_kind=RHS_NONE, rhs_par=(), chi=None, degenerate=False):
+    o = AssembleOpts()
+    o.p2 = int(p2)
+    o.forms = sum(1 << f for f in forms)
+    o.rhs_kind = rhs_kind
+    for i, v in enumerate(rhs_par):
+        o.rhs_par[i] = v
+    o._chi_keep = chi
+    o.chi = _p(chi, C.c_double) if chi is not None else None
+    o.degenerate = int(degenerate)
+    return o
+
+
+def assemble(mesh, ls_vert, ls_edge, active, dof_vert, dof_edge, m, opts):
+    """Returns (status, rowptr, colind, {form: vals}, rhs)."""
+    L = lib()
+    rowptr = np.empty(m + 1, np.int64)
+    colind_p = C.POINTER(C.c_int32)()
+    nnz = C.c_int64()
+    vals_p = (C.POINTER(C.c_double) * NUM_FORMS)()
+    rhs = np.empty(m, np.float64)
+    st = L.orc_assemble(C.c_int64(mesh.nt), _p(mesh.tet_v, C.c_int32), _p(mesh.tet_e, C.c_int32),
+                        _p(mesh.coords, C.c_double), _p(ls_vert, C.c_double), _p(ls_edge, C.c_double),
+                        _p(active, C.c_uint8), _p(dof_vert, C.c_int32),
+                        _p(dof_edge, C.c_int32) if dof_edge is not None else None, C.c_int64(m), C.byref(opts),
+                        _p(rowptr, C.c_int64), C.byref(colind_p), C.byref(nnz), vals_p, _p(rhs, C.c_double))
+    if st != OK:
+        return st, None, None, None, None
+    libc = C.CDLL(None)
+    n = nnz.value
+    colind = np.ctypeslib.as_array(colind_p, shape=(max(n, 1),))[:n].copy()
+    libc.free(colind_p)
+    vals = {}
+    for f in range(NUM_FORMS):
+        if vals_p[f]:
+            vals[f] = np.ctypeslib.as_array(vals_p[f], shape=(max(n, 1),))[:n].copy()
+            libc.free(vals_p[f])
+    return st, rowptr, colind, vals, rhs
+
+
+def spmv(rowptr, colind, vals, x):
+    L = lib()
+    m = len(rowptr) - 1
+    y = np.empty(m, np.float64)
+    L.orc_spmv(C.c_int64(m), _p(rowptr, C.c_int64), _p(colind, C.c_int32), _p(vals, C.c_double),
+               _p(np.ascontiguousarray(x, dtype=np.float64), C.c_double), _p(y, C.c_double))
+    return y
+
+
+def pcg_jacobi(rowptr, colind, vals, b, x0=None, max_iter=100000, tol=1e-10, rel=True):
+    L = lib()
+    m = len(rowptr) - 1
+    x = np.zeros(m) if x0 is None else np.array(x0, dtype=np.float64)
+    it = C.c_int(max_iter)
+    t = C.c_double(tol)
+    st = L.orc_pcg_jacobi(C.c_int64(m), _p(rowptr, C.c_int64), _p(colind, C.c_int32), _p(vals, C.c_double),
+                          _p(np.ascontiguousarray(b, dtype=np.float64), C.c_double), _p(x, C.c_double),
+                          C.byref(it), C.byref(t), C.c_int(int(rel)))
+    return st, x, it.value, t.value
+
+
+def gmres_jacobi(rowptr, colind, vals, b, x0=None, restart=50, max_iter=100000, tol=1e-10, rel=True, method=0):
+    L = lib()
+    m = len(rowptr) - 1
+    x = np.zeros(m) if x0 is None else np.array(x0, dtype=np.float64)
+    it = C.c_int(max_iter)
+    t = C.c_double(tol)
+    st = L.orc_gmres_jacobi(C.c_int64(m), _p(rowptr, C.c_int64), _p(colind, C.c_int32), _p(vals, C.c_double),
+                            _p(np.ascontiguousarray(b, dtype=np.float64), C.c_double), _p(x, C.c_double),
+                            C.c_int(restart), C.byref(it), C.byref(t), C.c_int(int(rel)), C.c_int(method))
+    return st, x, it.value, t.value
+
+
+def ch_block(rowptr, colind, M, A, Cn, alpha, mob, rho, eps2, beta):
+    L = lib()
+    m = len(rowptr) - 1
+    nnz = len(colind)
+    brp = np.empty(2 * m + 1, np.int64)
+    bci = np.empty(4 * nnz, np.int32)
+    bv = np.empty(4 * nnz, np.float64)
+    L.orc_ch_block(C.c_int64(m), _p(rowptr, C.c_int64), _p(colind, C.c_int32), _p(M, C.c_double),
+                   _p(A, C.c_double), _p(Cn, C.c_double), C.c_double(alpha), C.c_double(mob), C.c_double(rho),
+                   C.c_double(eps2), C.c_double(beta), _p(brp, C.c_int64), _p(bci, C.c_int32), _p(bv, C.c_double))
+    return brp, bci, bv
+
+
+def set_threads(n):
+    lib().orc_set_threads(C.c_int(n))
+
+
+def local_forms(xv, ls10, opts):
+    """Element matrices of one tet: returns (status, {form: (nl, nl)}, rhs[nl], n_facets)."""
+    L = lib()
+    xv = np.ascontiguousarray(xv, dtype=np.float64)
+    ls10 = np.ascontiguousarray(ls10, dtype=np.float64)
+    out = np.zeros((NUM_FORMS, 100))
+    rhs = np.zeros(10)
+    nf = C.c_int()
+    st = L.orc_local_forms(_p(xv, C.c_double), _p(ls10, C.c_double), C.byref(opts), None,
+                           _p(out, C.c_double), _p(rhs, C.c_double), C.byref(nf))
+    nl = 10 if opts.p2 else 4
+    return st, {f: out[f, :nl * nl].reshape(nl, nl) for f in range(NUM_FORMS)}, rhs[:nl], nf.value

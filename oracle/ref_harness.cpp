@@ -1,0 +1,431 @@
+// Harness around the DROPS reference implementation -- TEST INFRASTRUCTURE.
+//
+// Compiled by oracle/build_ref.sh against the reference's own sources (read
+// in place, never copied) into oracle/_ref/ref_harness.  It drives the
+// reference's public API for the TraceFEM path and writes what it computes
+// to a small binary file (named arrays) that tests/golden/make_golden.py turns
+// into committed fixtures.  Nothing here is shipped or timed as the product.
+//
+//   ref_harness system  <p1|p2> <lsP1|lsP2> <shape> <n> <a> <solve:0|1> <out>
+//       BrickBuilderCL [-a,a]^3 with n^3 cubes (geom/builder.cpp:99-180),
+//       P2 level-set index via DistributeDOFs (surfphasesep.cpp:184-190),
+//       interface index DistributeDOFs (misc/problem.cpp:283-336),
+//       setupFESystem (surfactant/ifacetransp.cpp:615-622) for M, A, C_n (+F),
+//       optional PCGSolverCL<JACPcCL> on M + A + h C_n (num/krylovsolver.h:1805).
+//   ref_harness legacy_numb <case> <out>    CreateNumbOnInterface test cases
+//   ref_harness area <out>                  tests/principallattice.cpp:316-347
+//   ref_harness gmres <n> <a> <steps> <out> Cahn-Hilliard BDF1 steps, DROPS GMRES
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <functional>
+#include <iostream>
+#include <map>
+#include <memory>
+#include <random>
+#include <string>
+#include <utility>
+#include <valarray>
+#include <vector>
+#include <unordered_map>
+#include <list>
+#include <set>
+#include <sstream>
+#include <tuple>
+#include <array>
+
+// The P2 scalar Laplace-Beltrami and C_n forms are not members of
+// LocalAssembler; they are built from its own private builders below, which
+// is why this file is compiled with -fno-access-control.
+#include "geom/builder.h"
+#include "misc/problem.h"
+#include "num/krylovsolver.h"
+#include "num/precond.h"
+#include "surfactant/ifacetransp.h"
+
+using namespace DROPS;
+
+namespace {
+
+struct Writer {
+    FILE* f;
+    explicit Writer(const char* path) : f(std::fopen(path, "wb")) {
+        if (!f) throw std::runtime_error("cannot open output");
+        std::fwrite("TFG1", 1, 4, f);
+    }
+    ~Writer() { std::fclose(f); }
+    void put(const std::string& name, char type, const void* data, uint64_t n, size_t es) {
+        uint32_t l = (uint32_t)name.size();
+        std::fwrite(&l, 4, 1, f);
+        std::fwrite(name.data(), 1, l, f);
+        std::fwrite(&type, 1, 1, f);
+        std::fwrite(&n, 8, 1, f);
+        if (n) std::fwrite(data, es, n, f);
+    }
+    void d(const std::string& name, const std::vector<double>& v) { put(name, 'd', v.data(), v.size(), 8); }
+    void l(const std::string& name, const std::vector<int64_t>& v) { put(name, 'l', v.data(), v.size(), 8); }
+    void s(const std::string& name, double x) { d(name, std::vector<double>(1, x)); }
+    void i(const std::string& name, int64_t x) { l(name, std::vector<int64_t>(1, x)); }
+};
+
+double now() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// level sets (surfactant/Surface.hpp:71,130)
+double ls_value(const std::string& shape, const Point3DCL& x) {
+    if (shape == "sphere") return x.norm() - 1.0;
+    if (shape == "torus") {  // R = 1, r = 0.4, symmetry axis z
+        double rho = std::sqrt(x[0] * x[0] + x[1] * x[1]) - 1.0;
+        return std::sqrt(rho * rho + x[2] * x[2]) - 0.4;
+    }
+    throw std::invalid_argument("unknown shape");
+}
+
+void write_csr(Writer& w, const std::string& name, const MatrixCL& A) {
+    std::vector<int64_t> rp(A.num_rows() + 1), ci(A.num_nonzeros());
+    std::vector<double> v(A.num_nonzeros());
+    for (size_t r = 0; r <= A.num_rows(); ++r) rp[r] = (int64_t)A.raw_row()[r];
+    for (size_t k = 0; k < A.num_nonzeros(); ++k) {
+        ci[k] = (int64_t)A.raw_col()[k];
+        v[k] = A.raw_val()[k];
+    }
+    w.l(name + ".rowptr", rp);
+    w.l(name + ".colind", ci);
+    w.d(name + ".vals", v);
+}
+
+// Mesh as flat arrays: vertex order of the triangulation; per tet the 4 vertex
+// indices and, per local edge, its two vertex indices.
+struct Flat {
+    std::map<const VertexCL*, int64_t> vid;
+    std::vector<int64_t> tet_v, tet_ev;
+    std::vector<double> coords;
+};
+Flat flatten(MultiGridCL& mg) {
+    Flat F;
+    int64_t k = 0;
+    DROPS_FOR_TRIANG_VERTEX(mg, 0, it) {
+        F.vid[&*it] = k++;
+        for (int c = 0; c < 3; ++c) F.coords.push_back(it->GetCoord()[c]);
+    }
+    DROPS_FOR_TRIANG_TETRA(mg, 0, it) {
+        for (int i = 0; i < 4; ++i) F.tet_v.push_back(F.vid[it->GetVertex(i)]);
+        for (int e = 0; e < 6; ++e) {
+            F.tet_ev.push_back(F.vid[it->GetEdge(e)->GetVertex(0)]);
+            F.tet_ev.push_back(F.vid[it->GetEdge(e)->GetVertex(1)]);
+        }
+    }
+    return F;
+}
+
+// P2 forms built from LocalAssembler's own builders.
+LocalAssembler::mtx A_P2P2(LocalAssembler& a) {
+    if (a.qDomain.empty()) return a.createMtx(10, 0.);
+    a.require(a.qSurfGradP2[0], &LocalAssembler::buildSurfGradP2);
+    auto A = a.createMtx(10);
+    for (size_t i = 0; i < 10; ++i)
+        for (size_t j = i; j < 10; ++j) {
+            A[i][j] = quad_2D(dot(a.qSurfGradP2[j], a.qSurfGradP2[i]), a.qDomain);
+            A[j][i] = A[i][j];
+        }
+    return A;
+}
+LocalAssembler::mtx C_n_P2P2(LocalAssembler& a) {
+    a.require(a.q3DGradP2[0], &LocalAssembler::buildGradP2);
+    a.require(a.q3DNormal, &LocalAssembler::build3DNormal);
+    auto A = a.createMtx(10);
+    for (size_t i = 0; i < 10; ++i)
+        for (size_t j = i; j < 10; ++j) {
+            A[i][j] = quad(dot(a.q3DNormal, a.q3DGradP2[j]) * dot(a.q3DNormal, a.q3DGradP2[i]), a.absDet, a.q3Domain,
+                           AllTetraC);
+            A[j][i] = A[i][j];
+        }
+    return A;
+}
+LocalAssembler::vec F_P2(LocalAssembler& a) {
+    if (a.qDomain.empty()) return LocalAssembler::vec(10, 0.);
+    a.require(a.qHatP2[0], &LocalAssembler::buildHatP2);
+    a.require(a.qConcentrationF, &LocalAssembler::buildConcentrationF);
+    LocalAssembler::vec b(10);
+    for (size_t i = 0; i < 10; ++i) b[i] = quad_2D(a.qConcentrationF * a.qHatP2[i], a.qDomain);
+    return b;
+}
+
+int cmd_system(int argc, char** argv) {
+    if (argc < 9) throw std::invalid_argument("usage: system p1|p2 lsP1|lsP2 shape n a solve out");
+    const bool p2 = std::string(argv[2]) == "p2";
+    const bool lsp2 = std::string(argv[3]) == "lsP2";
+    const std::string shape = argv[4];
+    const int n = std::atoi(argv[5]);
+    const double a = std::atof(argv[6]);
+    const bool solve = std::atoi(argv[7]) != 0;
+    Writer w(argv[8]);
+
+    double t0 = now();
+    BrickBuilderCL brick(Point3DCL(-a), 2. * a * std_basis<3>(1), 2. * a * std_basis<3>(2), 2. * a * std_basis<3>(3), n, n,
+                         n);
+    MultiGridCL mg(brick);
+    Flat F = flatten(mg);
+    w.l("tet_v", F.tet_v);
+    w.l("tet_ev", F.tet_ev);
+    w.d("coords", F.coords);
+    w.s("time_mesh", now() - t0);
+
+    FESystem sys;
+    auto& levelSet = sys.params.levelSet;
+    IdxDescCL lsIdx(P2_FE);
+    lsIdx.DistributeDOFs(0, mg);
+    levelSet.SetIdx(&lsIdx);
+    const Uint li = lsIdx.GetIdx();
+    // vertex values, then edges: P2 nodal (LSInit) or P1-linear (LinearLSInit),
+    // surfactant/surfactant.cpp:733-758.
+    DROPS_FOR_TRIANG_VERTEX(mg, 0, it) levelSet.Data[it->Unknowns(li)] = ls_value(shape, it->GetCoord());
+    DROPS_FOR_TRIANG_EDGE(mg, 0, it) {
+        if (lsp2)
+            levelSet.Data[it->Unknowns(li)] =
+                ls_value(shape, 0.5 * (it->GetVertex(0)->GetCoord() + it->GetVertex(1)->GetCoord()));
+        else
+            levelSet.Data[it->Unknowns(li)] = 0.5 * (levelSet.Data[it->GetVertex(0)->Unknowns(li)] +
+                                                     levelSet.Data[it->GetVertex(1)->Unknowns(li)]);
+    }
+    {
+        std::vector<double> lv, le;
+        std::vector<int64_t> ev;
+        DROPS_FOR_TRIANG_VERTEX(mg, 0, it) lv.push_back(levelSet.Data[it->Unknowns(li)]);
+        DROPS_FOR_TRIANG_EDGE(mg, 0, it) {
+            le.push_back(levelSet.Data[it->Unknowns(li)]);
+            ev.push_back(F.vid[it->GetVertex(0)]);
+            ev.push_back(F.vid[it->GetVertex(1)]);
+        }
+        w.d("ls_vert", lv);
+        w.d("ls_edge", le);
+        w.l("edge_v", ev);
+    }
+
+    IdxDescCL ifIdx(p2 ? P2IF_FE : P1IF_FE);
+    t0 = now();
+    size_t n_active = ifIdx.DistributeDOFs(0, mg, &levelSet);
+    w.s("time_dofs", now() - t0);
+    w.i("n_active", (int64_t)n_active);
+    w.i("n_dofs", (int64_t)ifIdx.NumUnknowns());
+    {
+        std::vector<int64_t> l2g;
+        std::vector<int64_t> act;
+        int64_t k = 0;
+        DROPS_FOR_TRIANG_TETRA(mg, 0, it) {
+            auto I = ifIdx.Loc2Glo(*it);
+            if (!I.empty()) {
+                act.push_back(k);
+                for (auto x : I) l2g.push_back((int64_t)x);
+            }
+            ++k;
+        }
+        w.l("active_tets", act);
+        w.l("loc2glo", l2g);
+    }
+
+    const double h = 2. * a / n;
+    // rhs: f = 13 xyz at ext(x) on the unit sphere (Surface.hpp:46-52)
+    sys.params.surfCahnHilliardParams.f = [](Point3DCL const& x, double) {
+        Point3DCL y = x - (x.norm() - 1.0) * (x / x.norm());
+        return 13. * y[0] * y[1] * y[2];
+    };
+    MatrixCL Mm, Am, Cm;
+    VectorCL rhs;
+    t0 = now();
+    if (!p2) {
+        FEMatDescCL M(&ifIdx, &ifIdx, &LocalAssembler::M_P1P1), A(&ifIdx, &ifIdx, &LocalAssembler::A_P1P1),
+            C(&ifIdx, &ifIdx, &LocalAssembler::C_n_P1P1);
+        FEVecDescCL f(&ifIdx, &LocalAssembler::F_concentration_P1);
+        sys.matrices = {&M, &A, &C};
+        sys.vectors = {&f};
+        setupFESystem(mg, sys);
+        Mm = M.Data;
+        Am = A.Data;
+        Cm = C.Data;
+        rhs.resize(f.Data.size());
+        rhs = f.Data;
+    } else {
+        // FESystemAccumulator::visit restated for the P2 forms above
+        const size_t m = ifIdx.NumUnknowns();
+        MatrixBuilderCL bM(&Mm, m, m), bA(&Am, m, m), bC(&Cm, m, m);
+        rhs.resize(m, 0.);
+        DROPS_FOR_TRIANG_TETRA(mg, 0, it) {
+            auto I = ifIdx.Loc2Glo(*it);
+            if (I.empty()) continue;
+            LocalAssembler as(*it, sys.params);
+            auto fm = as.M_P2P2();
+            auto fa = A_P2P2(as);
+            auto fc = C_n_P2P2(as);
+            auto fb = F_P2(as);
+            for (size_t i = 0; i < 10; ++i) {
+                for (size_t j = 0; j < 10; ++j) {
+                    bM(I[i], I[j]) += fm[i][j];
+                    bA(I[i], I[j]) += fa[i][j];
+                    bC(I[i], I[j]) += fc[i][j];
+                }
+                rhs[I[i]] += fb[i];
+            }
+        }
+        bM.Build();
+        bA.Build();
+        bC.Build();
+    }
+    w.s("time_assemble", now() - t0);
+    write_csr(w, "M", Mm);
+    write_csr(w, "A", Am);
+    write_csr(w, "C", Cm);
+    w.d("rhs", std::vector<double>(std::begin(rhs), std::end(rhs)));
+
+    if (solve) {
+        MatrixCL S(1., Mm, 1., Am, h, Cm);  // LinComb ctor (num/spmat.h:712-715)
+        write_csr(w, "S", S);
+        VectorCL x(0., S.num_rows());
+        JACPcCL pc;
+        PCGSolverCL<JACPcCL> solver(pc, 100000, 1e-10, true);
+        t0 = now();
+        solver.Solve(S, x, rhs, ifIdx.GetEx());
+        w.s("time_solve", now() - t0);
+        w.i("iters", solver.GetIter());
+        w.s("resid", solver.GetResid());
+        w.d("x", std::vector<double>(std::begin(x), std::end(x)));
+    }
+    return 0;
+}
+
+double plane(const Point3DCL& p) { return p[0] - 0.41; }
+double plane2(const Point3DCL& p) { return p[0] - 0.4; }
+double sphere_2(const Point3DCL& p) { return (p - Point3DCL(0.5)).norm() - 0.31; }
+
+// tests/interfaceP1FE.cpp restated without LevelsetP2CL: P2 level set by
+// nodal interpolation, numbering by IdxDescCL::CreateNumbering (P1IF_FE).
+int cmd_legacy_numb(int argc, char** argv) {
+    if (argc < 4) throw std::invalid_argument("usage: legacy_numb case out");
+    const std::string cs = argv[2];
+    Writer w(argv[3]);
+    int nx = 10, ny = 1, nz = 1;
+    std::function<double(const Point3DCL&)> fn = plane;
+    if (cs == "plane2") fn = plane2;
+    if (cs == "sphere") { nx = ny = nz = 20; fn = sphere_2; }
+    BrickBuilderCL brick(std_basis<3>(0), std_basis<3>(1), std_basis<3>(2), std_basis<3>(3), nx, ny, nz);
+    MultiGridCL mg(brick);
+    Flat F = flatten(mg);
+    w.l("tet_v", F.tet_v);
+    w.l("tet_ev", F.tet_ev);
+    w.d("coords", F.coords);
+    IdxDescCL lsIdx(P2_FE);
+    lsIdx.DistributeDOFs(0, mg);
+    VecDescCL ls(&lsIdx);
+    const Uint li = lsIdx.GetIdx();
+    DROPS_FOR_TRIANG_VERTEX(mg, 0, it) ls.Data[it->Unknowns(li)] = fn(it->GetCoord());
+    DROPS_FOR_TRIANG_EDGE(mg, 0, it)
+        ls.Data[it->Unknowns(li)] = fn(0.5 * (it->GetVertex(0)->GetCoord() + it->GetVertex(1)->GetCoord()));
+    BndCondT bc[6] = {NoBC, NoBC, NoBC, NoBC, NoBC, NoBC};
+    BndDataCL<> lsbnd(6, bc);
+    IdxDescCL ifIdx(P1IF_FE);
+    int64_t status = 0, n_active = -1, n_dofs = -1;
+    try {
+        n_active = (int64_t)ifIdx.CreateNumbering(0, mg, &ls, &lsbnd);
+        n_dofs = (int64_t)ifIdx.NumUnknowns();
+    } catch (std::exception& e) {
+        status = 2;
+        std::cerr << "legacy_numb: " << e.what() << "\n";
+    } catch (DROPSErrCL& e) {
+        status = 3;
+    }
+    w.i("status", status);
+    w.i("n_active", n_active);
+    w.i("n_dofs", n_dofs);
+    if (status == 0) {
+        std::vector<int64_t> dv;
+        const Uint ii = ifIdx.GetIdx();
+        DROPS_FOR_TRIANG_VERTEX(mg, 0, it) dv.push_back(it->Unknowns.Exist(ii) ? (int64_t)it->Unknowns(ii) : -1);
+        w.l("dof_vert", dv);
+    }
+    return 0;
+}
+
+// tests/principallattice.cpp:316-347 (sphere r = 0.5 on [-1,1]^3, 8^3 cubes)
+int cmd_area(int argc, char** argv) {
+    if (argc < 3) throw std::invalid_argument("usage: area out");
+    Writer w(argv[2]);
+    BrickBuilderCL brick(Point3DCL(-1.), 2. * std_basis<3>(1), 2. * std_basis<3>(2), 2. * std_basis<3>(3), 8, 8, 8);
+    MultiGridCL mg(brick);
+    const PrincipalLatticeCL& lat = PrincipalLatticeCL::instance(2);
+    GridFunctionCL<> ls(lat.vertex_size());
+    SurfacePatchCL patch;
+    QuadDomain2DCL qdom;
+    double surf = 0.;
+    std::vector<double> per_tet;
+    std::vector<int64_t> nfac;
+    auto sph = [](const Point3DCL& p, double) { return p.norm() - 0.5; };
+    DROPS_FOR_TRIANG_TETRA(mg, 0, it) {
+        evaluate_on_vertexes(InstatScalarFunction(sph), *it, lat, 0., Addr(ls));
+        patch.make_patch<MergeCutPolicyCL>(lat, ls);
+        make_CompositeQuad5Domain2D(qdom, patch, *it);
+        GridFunctionCL<> integrand(1., qdom.vertex_size());
+        double s = quad_2D(integrand, qdom);
+        surf += s;
+        per_tet.push_back(s);
+        nfac.push_back(patch.facet_size());
+    }
+    w.s("surface", surf);
+    w.d("per_tet", per_tet);
+    w.l("n_facets", nfac);
+    Flat F = flatten(mg);
+    w.l("tet_v", F.tet_v);
+    w.l("tet_ev", F.tet_ev);
+    w.d("coords", F.coords);
+    // the patch topology of the first cut tets, for the patch parity test
+    std::vector<int64_t> facets, bnd, tet_of;
+    std::vector<double> verts;
+    std::vector<int64_t> nverts;
+    int64_t k = 0, dumped = 0;
+    DROPS_FOR_TRIANG_TETRA(mg, 0, it) {
+        evaluate_on_vertexes(InstatScalarFunction(sph), *it, lat, 0., Addr(ls));
+        patch.make_patch<MergeCutPolicyCL>(lat, ls);
+        if (!patch.empty() && dumped < 400) {
+            tet_of.push_back(k);
+            nverts.push_back(patch.vertex_size());
+            for (auto f = patch.facet_begin(); f != patch.facet_end(); ++f) {
+                for (int j = 0; j < 3; ++j) facets.push_back((*f)[j]);
+                bnd.push_back(patch.is_boundary_facet(f) ? 1 : 0);
+            }
+            for (auto v = patch.vertex_begin(); v != patch.vertex_end(); ++v)
+                for (int c = 0; c < 4; ++c) verts.push_back((*v)[c]);
+            std::vector<double> lsv(std::begin(ls), std::end(ls));
+            ++dumped;
+        }
+        ++k;
+    }
+    w.l("patch_tets", tet_of);
+    w.l("patch_nverts", nverts);
+    w.l("patch_facets", facets);
+    w.l("patch_boundary", bnd);
+    w.d("patch_verts", verts);
+    return 0;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    try {
+        if (argc < 2) throw std::invalid_argument("usage: ref_harness <cmd> ...");
+        std::string cmd = argv[1];
+        if (cmd == "system") return cmd_system(argc, argv);
+        if (cmd == "legacy_numb") return cmd_legacy_numb(argc, argv);
+        if (cmd == "area") return cmd_area(argc, argv);
+        throw std::invalid_argument("unknown command " + cmd);
+    } catch (std::exception& e) {
+        std::cerr << "ref_harness: " << e.what() << "\n";
+        return 1;
+    } catch (DROPSErrCL& e) {
+        e.handle();
+        return 1;
+    }
+}

@@ -1,0 +1,958 @@
+/*
+ * CPU oracle for the TraceFEM hot path of DROPS -- TEST INFRASTRUCTURE ONLY.
+ * See tracefem_oracle.h.  Compile with -ffp-contract=off so that x86 and Arm
+ * builds round identically.
+ */
+#include "tracefem_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static int g_threads = 0;
+void orc_set_threads(int n) { g_threads = n; }
+
+/* local edge -> local vertices (geom/topo.cpp VertOfEdgeAr, first 6 rows) */
+static const int EV[6][2] = {{0, 1}, {0, 2}, {1, 2}, {0, 3}, {1, 3}, {2, 3}};
+
+/* ======================================================================= */
+/* mesh                                                                      */
+/* ======================================================================= */
+/* The 7 edge directions of the Kuhn brick, as offsets (d3, d2, d1).       */
+static const int EDIR[7][3] = {{0, 0, 1}, {0, 1, 0}, {1, 0, 0}, {0, 1, 1}, {1, 0, 1}, {1, 1, 0}, {1, 1, 1}};
+
+int64_t orc_brick_num_vertices(int n1, int n2, int n3) { return (int64_t)(n1 + 1) * (n2 + 1) * (n3 + 1); }
+int64_t orc_brick_num_tets(int n1, int n2, int n3) { return (int64_t)6 * n1 * n2 * n3; }
+static int64_t edir_count(int t, int n1, int n2, int n3) {
+    return (int64_t)(n3 + 1 - EDIR[t][0]) * (n2 + 1 - EDIR[t][1]) * (n1 + 1 - EDIR[t][2]);
+}
+int64_t orc_brick_num_edges(int n1, int n2, int n3) {
+    int64_t s = 0;
+    for (int t = 0; t < 7; ++t) s += edir_count(t, n1, n2, n3);
+    return s;
+}
+
+/* Kuhn split of one cube into 6 tets, local vertex offsets (i3,i2,i1) in the
+ * order of BrickBuilderCL::build_ser_impl (geom/builder.cpp:151-176).      */
+static const int KUHN[6][4][3] = {
+    {{0, 0, 0}, {0, 0, 1}, {0, 1, 1}, {1, 1, 1}}, {{0, 0, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}},
+    {{0, 0, 0}, {0, 1, 0}, {0, 1, 1}, {1, 1, 1}}, {{0, 0, 0}, {0, 1, 0}, {1, 1, 0}, {1, 1, 1}},
+    {{0, 0, 0}, {1, 0, 0}, {1, 0, 1}, {1, 1, 1}}, {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {1, 1, 1}}};
+
+void orc_brick(const double orig[3], const double e1[3], const double e2[3], const double e3[3], int n1,
+               int n2, int n3, double* coords, int32_t* tet_v, int32_t* tet_e, int32_t* edge_v) {
+    double o1[3], o2[3], o3[3];
+    for (int c = 0; c < 3; ++c) {
+        o1[c] = (1.0 / (double)n1) * e1[c];
+        o2[c] = (1.0 / (double)n2) * e2[c];
+        o3[c] = (1.0 / (double)n3) * e3[c];
+    }
+    int64_t v = 0;
+    for (int i3 = 0; i3 <= n3; ++i3)
+        for (int i2 = 0; i2 <= n2; ++i2)
+            for (int i1 = 0; i1 <= n1; ++i1, ++v)
+                for (int c = 0; c < 3; ++c)
+                    coords[3 * v + c] = ((orig[c] + (double)i1 * o1[c]) + (double)i2 * o2[c]) + (double)i3 * o3[c];
+    int64_t eoff[8];
+    eoff[0] = 0;
+    for (int t = 0; t < 7; ++t) eoff[t + 1] = eoff[t] + edir_count(t, n1, n2, n3);
+    if (edge_v) {
+        for (int t = 0; t < 7; ++t) {
+            int64_t k = eoff[t];
+            for (int i3 = 0; i3 <= n3 - EDIR[t][0]; ++i3)
+                for (int i2 = 0; i2 <= n2 - EDIR[t][1]; ++i2)
+                    for (int i1 = 0; i1 <= n1 - EDIR[t][2]; ++i1, ++k) {
+                        int64_t a = ((int64_t)i3 * (n2 + 1) + i2) * (n1 + 1) + i1;
+                        int64_t b = ((int64_t)(i3 + EDIR[t][0]) * (n2 + 1) + i2 + EDIR[t][1]) * (n1 + 1) + i1 + EDIR[t][2];
+                        edge_v[2 * k] = (int32_t)a;
+                        edge_v[2 * k + 1] = (int32_t)b;
+                    }
+        }
+    }
+    int64_t tt = 0;
+    for (int i3 = 0; i3 < n3; ++i3)
+        for (int i2 = 0; i2 < n2; ++i2)
+            for (int i1 = 0; i1 < n1; ++i1)
+                for (int l = 0; l < 6; ++l, ++tt) {
+                    int p[4][3];
+                    for (int k = 0; k < 4; ++k) {
+                        p[k][0] = i3 + KUHN[l][k][0];
+                        p[k][1] = i2 + KUHN[l][k][1];
+                        p[k][2] = i1 + KUHN[l][k][2];
+                        tet_v[4 * tt + k] = (int32_t)(((int64_t)p[k][0] * (n2 + 1) + p[k][1]) * (n1 + 1) + p[k][2]);
+                    }
+                    if (tet_e) {
+                        for (int k = 0; k < 6; ++k) {
+                            const int* a = p[EV[k][0]];
+                            const int* b = p[EV[k][1]];
+                            int d[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+                            int t;
+                            for (t = 0; t < 7; ++t)
+                                if (EDIR[t][0] == d[0] && EDIR[t][1] == d[1] && EDIR[t][2] == d[2]) break;
+                            int64_t idx = eoff[t] + ((int64_t)a[0] * (n2 + 1 - EDIR[t][1]) + a[1]) * (n1 + 1 - EDIR[t][2]) + a[2];
+                            tet_e[6 * tt + k] = (int32_t)idx;
+                        }
+                    }
+                }
+}
+
+/* ======================================================================= */
+/* level sets                                                                */
+/* ======================================================================= */
+static double norm3(const double x[3]) { return sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]); }
+
+double orc_ls_value(int kind, const double* par, const double x[3]) {
+    switch (kind) {
+        case ORC_LS_SPHERE: { /* Sphere::dist (Surface.hpp:71), centred */
+            double y[3] = {x[0] - par[0], x[1] - par[1], x[2] - par[2]};
+            return norm3(y) - par[3];
+        }
+        case ORC_LS_TORUS: { /* Torus::dist (Surface.hpp:130) with r_min == r_max */
+            int ax = (int)par[2];
+            int a0 = (ax + 1) % 3, a1 = (ax + 2) % 3;
+            double rho = sqrt(x[a0] * x[a0] + x[a1] * x[a1]) - par[0];
+            return sqrt(rho * rho + x[ax] * x[ax]) - par[1];
+        }
+        case ORC_LS_ELLIPSOID: {
+            double d[3] = {x[0] - par[0], x[1] - par[1], x[2] - par[2]};
+            const double* R = par + 6;
+            double y[3];
+            for (int i = 0; i < 3; ++i) y[i] = (R[0 * 3 + i] * d[0] + R[1 * 3 + i] * d[1]) + R[2 * 3 + i] * d[2];
+            double z[3] = {y[0] / par[3], y[1] / par[4], y[2] / par[5]};
+            return norm3(z) - 1.0;
+        }
+        case ORC_LS_PLANE:
+            return ((par[0] * x[0] + par[1] * x[1]) + par[2] * x[2]) - par[3];
+    }
+    return NAN;
+}
+
+void orc_levelset(int kind, const double* par, int p2, int64_t nv, int64_t ne, const double* coords,
+                  const int32_t* edge_v, double* ls_vert, double* ls_edge) {
+    for (int64_t v = 0; v < nv; ++v) ls_vert[v] = orc_ls_value(kind, par, coords + 3 * v);
+    for (int64_t e = 0; e < ne; ++e) {
+        int32_t a = edge_v[2 * e], b = edge_v[2 * e + 1];
+        if (!p2) {
+            ls_edge[e] = 0.5 * (ls_vert[a] + ls_vert[b]);
+        } else {
+            double m[3];
+            for (int c = 0; c < 3; ++c) m[c] = 0.5 * (coords[3 * a + c] + coords[3 * b + c]);
+            ls_edge[e] = orc_ls_value(kind, par, m);
+        }
+    }
+}
+
+/* ======================================================================= */
+/* DOF numbering                                                             */
+/* ======================================================================= */
+static int sgn(double v) { return (v > 0.) - (v < 0.); }
+
+/* distance() (geom/subtriangulation.tpp:38-46): returns 0 for a cut tet,
+ * min |v| for a one-signed tet, -1 for an exact zero in a cut tet.        */
+static double tet_distance(const double* f, int n) {
+    int sum = 0;
+    for (int i = 0; i < n; ++i) sum += sgn(f[i]);
+    if (abs(sum) == n) {
+        double m = fabs(f[0]);
+        for (int i = 1; i < n; ++i)
+            if (fabs(f[i]) < m) m = fabs(f[i]);
+        return m;
+    }
+    for (int i = 0; i < n; ++i)
+        if (f[i] == 0.) return -1.;
+    return 0.;
+}
+
+static void gather_ls10(const int32_t* tv, const int32_t* te, const double* ls_vert, const double* ls_edge,
+                        double out[10]) {
+    for (int i = 0; i < 4; ++i) out[i] = ls_vert[tv[i]];
+    for (int i = 0; i < 6; ++i) out[4 + i] = ls_edge[te[i]];
+}
+
+int orc_distribute_dofs(int64_t nt, const int32_t* tet_v, const int32_t* tet_e, int64_t nv, int64_t ne,
+                        const double* ls_vert, const double* ls_edge, int p2, double dist, int64_t* n_active,
+                        int64_t* n_dofs, int32_t* dof_vert, int32_t* dof_edge, uint8_t* active) {
+    for (int64_t v = 0; v < nv; ++v) dof_vert[v] = -1;
+    if (p2)
+        for (int64_t e = 0; e < ne; ++e) dof_edge[e] = -1;
+    int64_t na = 0, block = 0;
+    for (int64_t t = 0; t < nt; ++t) {
+        double f[10];
+        gather_ls10(tet_v + 4 * t, tet_e + 6 * t, ls_vert, ls_edge, f);
+        double d = tet_distance(f, 10);
+        if (d < 0.) return ORC_ERR_ZERO_NODE;
+        active[t] = 0;
+        if (d <= dist) {
+            ++na;
+            active[t] = 1;
+            for (int i = 0; i < 4; ++i) {
+                int32_t* slot = &dof_vert[tet_v[4 * t + i]];
+                if (*slot < 0) *slot = (int32_t)block++;
+            }
+            if (p2)
+                for (int i = 0; i < 6; ++i) {
+                    int32_t* slot = &dof_edge[tet_e[6 * t + i]];
+                    if (*slot < 0) *slot = (int32_t)block++;
+                }
+        }
+    }
+    *n_active = na;
+    *n_dofs = block;
+    return ORC_OK;
+}
+
+/* ======================================================================= */
+/* principal lattice of order 2 and the surface patch                        */
+/* ======================================================================= */
+/* PrincipalLatticeCL (geom/principallattice.cpp:33-79) for n = 2.          */
+static int lat_index(int i, int j, int k) {
+    return (i > 0 ? ((i + 2) * (i + 1) * i) / 6 : 0) + (j > 0 ? ((j + 1) * j) / 2 : 0) + k;
+}
+static int in_ref(const int v[3], int n) { return n >= v[0] && v[0] >= v[1] && v[1] >= v[2]; }
+
+void orc_lattice2(double verts[10][4], int tets[8][4]) {
+    const int n = 2;
+    int nv = 0;
+    for (int x = 0; x <= n; ++x)
+        for (int y = 0; y <= x; ++y)
+            for (int z = 0; z <= y; ++z, ++nv) {
+                verts[nv][0] = (double)(n - x) / n;
+                verts[nv][1] = (double)(x - y) / n;
+                verts[nv][2] = (double)(y - z) / n;
+                verts[nv][3] = (double)z / n;
+            }
+    static const int perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+    int nt = 0;
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j <= i; ++j)
+            for (int k = 0; k <= j; ++k)
+                for (int l = 0; l < 6; ++l) {
+                    int t[4][3] = {{i, j, k}};
+                    int ok = 1;
+                    for (int s = 1; s < 4 && ok; ++s) {
+                        memcpy(t[s], t[s - 1], sizeof t[s]);
+                        ++t[s][perm[l][s - 1]];
+                        ok = in_ref(t[s], n);
+                    }
+                    if (!ok) continue;
+                    for (int s = 0; s < 4; ++s) tets[nt][s] = lat_index(t[s][0], t[s][1], t[s][2]);
+                    ++nt;
+                }
+}
+
+/* P2 local dof -> lattice vertex (geom/principallattice.cpp p2_dof_on_lattice_2) */
+static const int P2_ON_LAT[10] = {0, 4, 7, 9, 1, 2, 5, 3, 6, 8};
+
+int orc_make_patch(const double ls10[10], orc_patch_t* p) {
+    double LV[10][4];
+    int LT[8][4];
+    orc_lattice2(LV, LT);
+    double lat_ls[10];
+    for (int k = 0; k < 10; ++k) lat_ls[P2_ON_LAT[k]] = ls10[k];
+
+    /* MergeCut memo: lattice edge (lo,hi) -> cut vertex number */
+    int cut_key[ORC_MAX_PVERTS][2];
+    double cut_bary[ORC_MAX_PVERTS][4];
+    int n_cut = 0;
+    int copied[10];
+    for (int k = 0; k < 10; ++k) copied[k] = -1;
+    double zero_bary[10][4];
+    int n_zero = 0;
+    int zuse_f[3 * ORC_MAX_FACETS], zuse_j[3 * ORC_MAX_FACETS], n_zuse = 0;
+
+    p->n_facets = 0;
+    for (int s = 0; s < 8; ++s) {
+        double loc[4];
+        int sg[4], sum = 0;
+        for (int k = 0; k < 4; ++k) {
+            loc[k] = lat_ls[LT[s][k]];
+            sg[k] = sgn(loc[k]);
+            sum += sg[k];
+        }
+        /* SignTraitsCL<3>::assign / compute_cuts (geom/signtraits.h:112-139) */
+        int cut[4], n_root = 0, n_root_vert = 0;
+        if (sg[0] == 0 && sg[1] == 0 && sg[2] == 0 && sg[3] == 0) return ORC_ERR_ZERO_PATTERN;
+        if (abs(sum) != 4) {
+            for (int k = 0; k < 4; ++k)
+                if (sg[k] == 0) cut[n_root_vert++] = k;
+            n_root = n_root_vert;
+            for (int e = 0; e < 6; ++e)
+                if (sg[EV[e][0]] * sg[EV[e][1]] == -1) cut[n_root++] = e + 4;
+        }
+        /* RefPatchBuilderCL<3>::assign (geom/reftetracut.cpp:53-60) */
+        if (n_root < 3) continue;
+        int bnd = (n_root_vert == 3);
+        for (int f = 0; f + 2 < n_root; ++f) {
+            if (p->n_facets >= ORC_MAX_FACETS) return ORC_ERR_CAPACITY;
+            int fi = p->n_facets++;
+            p->boundary[fi] = bnd;
+            /* make_sub_facet (geom/subtriangulation.tpp:146-177) */
+            for (int j = 0; j < 3; ++j) {
+                int lv = cut[f + j];
+                if (lv < 4) {
+                    int lat = LT[s][lv];
+                    if (copied[lat] < 0) {
+                        copied[lat] = n_zero;
+                        memcpy(zero_bary[n_zero], LV[lat], sizeof zero_bary[0]);
+                        ++n_zero;
+                    }
+                    p->facet[fi][j] = copied[lat];
+                    zuse_f[n_zuse] = fi;
+                    zuse_j[n_zuse] = j;
+                    ++n_zuse;
+                } else {
+                    int v0 = EV[lv - 4][0], v1 = EV[lv - 4][1];
+                    int a = LT[s][v0], b = LT[s][v1];
+                    int lo = a < b ? a : b, hi = a < b ? b : a;
+                    int id = -1;
+                    for (int q = 0; q < n_cut; ++q)
+                        if (cut_key[q][0] == lo && cut_key[q][1] == hi) { id = q; break; }
+                    if (id < 0) {
+                        if (n_cut >= ORC_MAX_PVERTS) return ORC_ERR_CAPACITY;
+                        id = n_cut++;
+                        cut_key[id][0] = lo;
+                        cut_key[id][1] = hi;
+                        /* MergeCutPolicyCL::operator() (geom/subtriangulation.h:514-524) */
+                        double t = loc[v0] / (loc[v0] - loc[v1]);
+                        for (int c = 0; c < 4; ++c) cut_bary[id][c] = (1.0 - t) * LV[a][c] + t * LV[b][c];
+                    }
+                    p->facet[fi][j] = id;
+                }
+            }
+        }
+    }
+    for (int u = 0; u < n_zuse; ++u) p->facet[zuse_f[u]][zuse_j[u]] += n_cut;
+    if (n_cut + n_zero > ORC_MAX_PVERTS) return ORC_ERR_CAPACITY;
+    for (int q = 0; q < n_cut; ++q) memcpy(p->bary[q], cut_bary[q], sizeof p->bary[0]);
+    for (int q = 0; q < n_zero; ++q) memcpy(p->bary[n_cut + q], zero_bary[q], sizeof p->bary[0]);
+    p->n_cut_verts = n_cut;
+    p->n_verts = n_cut + n_zero;
+    return ORC_OK;
+}
+
+/* ======================================================================= */
+/* quadrature rules (num/discretize.cpp:153-294)                             */
+/* ======================================================================= */
+static double Q2D_NODE[7][3], Q2D_W[7], Q3D_NODE[15][4], Q3D_W[15];
+static int q_init = 0;
+static void init_quad(void) {
+    if (q_init) return;
+    const double s15 = sqrt(15.0);
+    /* Quad5_2DDataCL */
+    Q2D_NODE[0][0] = Q2D_NODE[0][1] = Q2D_NODE[0][2] = 1. / 3.;
+    double A1 = (6.0 - s15) / 21.0, B1 = (9.0 + 2.0 * s15) / 21.0;
+    double A2 = (6.0 + s15) / 21.0, B2 = (9.0 - 2.0 * s15) / 21.0;
+    double n2[6][3] = {{A1, A1, B1}, {A1, B1, A1}, {B1, A1, A1}, {A2, A2, B2}, {A2, B2, A2}, {B2, A2, A2}};
+    for (int i = 0; i < 6; ++i) memcpy(Q2D_NODE[i + 1], n2[i], sizeof n2[i]);
+    Q2D_W[0] = 9. / 80.;
+    for (int i = 1; i <= 3; ++i) Q2D_W[i] = (155. - s15) / 2400.;
+    for (int i = 4; i <= 6; ++i) Q2D_W[i] = (155. + s15) / 2400.;
+    /* Quad5DataCL */
+    for (int c = 0; c < 4; ++c) Q3D_NODE[0][c] = 0.25;
+    double a1 = (7.0 - s15) / 34.0, b1 = (13.0 + 3.0 * s15) / 34.0;
+    double a2 = (7.0 + s15) / 34.0, b2 = (13.0 - 3.0 * s15) / 34.0;
+    double a3 = (10.0 - 2.0 * s15) / 40.0, b3 = (10.0 + 2.0 * s15) / 40.0;
+    double n3[14][4] = {{a1, a1, a1, b1}, {a1, a1, b1, a1}, {a1, b1, a1, a1}, {b1, a1, a1, a1},
+                        {a2, a2, a2, b2}, {a2, a2, b2, a2}, {a2, b2, a2, a2}, {b2, a2, a2, a2},
+                        {a3, a3, b3, b3}, {a3, b3, a3, b3}, {a3, b3, b3, a3}, {b3, a3, a3, b3},
+                        {b3, a3, b3, a3}, {b3, b3, a3, a3}};
+    for (int i = 0; i < 14; ++i) memcpy(Q3D_NODE[i + 1], n3[i], sizeof n3[i]);
+    Q3D_W[0] = 0.01975308641975308641975308641975308641975;
+    for (int i = 1; i <= 4; ++i) Q3D_W[i] = 0.01198951396316977000173064248499538621936;
+    for (int i = 5; i <= 8; ++i) Q3D_W[i] = 0.01151136787104539754677023934921978132914;
+    for (int i = 9; i <= 14; ++i) Q3D_W[i] = 0.008818342151675485008818342151675485008818;
+    q_init = 1;
+}
+
+/* ======================================================================= */
+/* local forms: LocalAssembler (surfactant/ifacetransp.h:1013-1076,1242-1256, */
+/* 1522-1589)                                                               */
+/* ======================================================================= */
+/* GetTrafoTr (geom/multigrid.h:603-623): T = J^{-T}, det = det J */
+static void trafo(const double xv[4][3], double T[3][3], double* det) {
+    double M[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) M[j][i] = xv[i + 1][j] - xv[0][j];
+    double d = M[0][0] * (M[1][1] * M[2][2] - M[1][2] * M[2][1]) - M[0][1] * (M[1][0] * M[2][2] - M[1][2] * M[2][0]) +
+               M[0][2] * (M[1][0] * M[2][1] - M[1][1] * M[2][0]);
+    T[0][0] = (M[1][1] * M[2][2] - M[1][2] * M[2][1]) / d;
+    T[0][1] = (M[2][0] * M[1][2] - M[1][0] * M[2][2]) / d;
+    T[0][2] = (M[1][0] * M[2][1] - M[2][0] * M[1][1]) / d;
+    T[1][0] = (M[2][1] * M[0][2] - M[0][1] * M[2][2]) / d;
+    T[1][1] = (M[0][0] * M[2][2] - M[2][0] * M[0][2]) / d;
+    T[1][2] = (M[2][0] * M[0][1] - M[0][0] * M[2][1]) / d;
+    T[2][0] = (M[0][1] * M[1][2] - M[1][1] * M[0][2]) / d;
+    T[2][1] = (M[1][0] * M[0][2] - M[0][0] * M[1][2]) / d;
+    T[2][2] = (M[0][0] * M[1][1] - M[1][0] * M[0][1]) / d;
+    *det = d;
+}
+
+/* world gradients of the barycentric coordinates: grad lambda_i = T * gref_i */
+static void bary_grads(const double T[3][3], double g[4][3]) {
+    static const double gref[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int i = 0; i < 4; ++i)
+        for (int r = 0; r < 3; ++r) g[i][r] = T[r][0] * gref[i][0] + T[r][1] * gref[i][1] + T[r][2] * gref[i][2];
+}
+
+/* P2 basis values (FE_P2CL::H0..H9, num/fe.h:288-297) */
+static void p2_vals(const double b[4], double h[10]) {
+    for (int i = 0; i < 4; ++i) h[i] = b[i] * (2. * b[i] - 1.);
+    for (int e = 0; e < 6; ++e) h[4 + e] = 4. * b[EV[e][0]] * b[EV[e][1]];
+}
+/* world gradients of the P2 basis at barycentric point b */
+static void p2_grads(const double b[4], const double gl[4][3], double g[10][3]) {
+    for (int i = 0; i < 4; ++i)
+        for (int r = 0; r < 3; ++r) g[i][r] = (4. * b[i] - 1.) * gl[i][r];
+    for (int e = 0; e < 6; ++e) {
+        int a = EV[e][0], c = EV[e][1];
+        for (int r = 0; r < 3; ++r) g[4 + e][r] = 4. * (b[c] * gl[a][r] + b[a] * gl[c][r]);
+    }
+}
+static void unit_normal(const double ls10[10], const double g[10][3], double n[3]) {
+    double v[3] = {0, 0, 0};
+    for (int k = 0; k < 10; ++k)
+        for (int r = 0; r < 3; ++r) v[r] += ls10[k] * g[k][r];
+    double nn = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    for (int r = 0; r < 3; ++r) n[r] = v[r] / nn;
+}
+static double dot3(const double a[3], const double b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+static double rhs_value(const orc_assemble_opts* o, const double x[3]) {
+    if (o->rhs_kind == ORC_RHS_CONST) return o->rhs_par[0];
+    if (o->rhs_kind == ORC_RHS_SPHERE_XYZ) {
+        /* f(ext(x)), ext(x) = x - dist(x) * grad dist(x) (Surface.hpp:46-52) */
+        double d[3] = {x[0] - o->rhs_par[0], x[1] - o->rhs_par[1], x[2] - o->rhs_par[2]};
+        double nd = norm3(d);
+        double dist = nd - o->rhs_par[3];
+        double y[3];
+        for (int c = 0; c < 3; ++c) y[c] = x[c] - dist * (d[c] / nd);
+        return o->rhs_par[4] * y[0] * y[1] * y[2];
+    }
+    return 0.;
+}
+
+int orc_local_forms(const double xv[4][3], const double ls10[10], const orc_assemble_opts* o,
+                    const double* chi_loc, double out[ORC_NUM_MAT_FORMS][100], double rhs[10], int* n_facets) {
+    init_quad();
+    const int nl = o->p2 ? 10 : 4;
+    for (int f = 0; f < ORC_NUM_MAT_FORMS; ++f) memset(out[f], 0, sizeof(double) * 100);
+    if (rhs) memset(rhs, 0, sizeof(double) * 10);
+    orc_patch_t P;
+    int st = orc_make_patch(ls10, &P);
+    if (st) return st;
+    if (n_facets) *n_facets = P.n_facets;
+    double T[3][3], det;
+    trafo(xv, T, &det);
+    double absdet = fabs(det);
+    double gl[4][3];
+    bary_grads(T, gl);
+
+    /* surface quadrature: make_CompositeQuadDomainCodim1 (num/quadrature.tpp:265-314) */
+    for (int f = 0; f < P.n_facets; ++f) {
+        double w[3][3];
+        for (int j = 0; j < 3; ++j) {
+            const double* b = P.bary[P.facet[f][j]];
+            for (int c = 0; c < 3; ++c) w[j][c] = xv[0][c] * b[0] + xv[1][c] * b[1] + xv[2][c] * b[2] + xv[3][c] * b[3];
+        }
+        double u[3], v[3], cr[3];
+        for (int c = 0; c < 3; ++c) { u[c] = w[1][c] - w[0][c]; v[c] = w[2][c] - w[0][c]; }
+        cr[0] = u[1] * v[2] - u[2] * v[1];
+        cr[1] = u[2] * v[0] - u[0] * v[2];
+        cr[2] = u[0] * v[1] - u[1] * v[0];
+        double fdet = norm3(cr) * (P.boundary[f] ? 0.5 : 1.0);
+        for (int q = 0; q < 7; ++q) {
+            double b[4];
+            for (int c = 0; c < 4; ++c)
+                b[c] = P.bary[P.facet[f][0]][c] * Q2D_NODE[q][0] + P.bary[P.facet[f][1]][c] * Q2D_NODE[q][1] +
+                       P.bary[P.facet[f][2]][c] * Q2D_NODE[q][2];
+            double wq = fdet * Q2D_W[q];
+            double g2[10][3], n[3];
+            p2_grads(b, gl, g2);
+            unit_normal(ls10, g2, n);
+            double phi[10], grad[10][3], sg[10][3];
+            if (o->p2) {
+                p2_vals(b, phi);
+                memcpy(grad, g2, sizeof grad);
+            } else {
+                for (int i = 0; i < 4; ++i) { phi[i] = b[i]; memcpy(grad[i], gl[i], sizeof grad[i]); }
+            }
+            for (int i = 0; i < nl; ++i) {
+                double gn = dot3(grad[i], n);
+                for (int r = 0; r < 3; ++r) sg[i][r] = grad[i][r] - gn * n[r];
+            }
+            double mob = 1.0;
+            if (chi_loc && o->degenerate) {
+                double c = chi_loc[0] * b[0] + chi_loc[1] * b[1] + chi_loc[2] * b[2] + chi_loc[3] * b[3];
+                mob = c * (1. - c);
+                if (mob < 0.) mob = 0.;
+            }
+            for (int i = 0; i < nl; ++i)
+                for (int j = i; j < nl; ++j) {
+                    if (o->forms & (1u << ORC_FORM_M)) out[ORC_FORM_M][i * nl + j] += wq * (phi[j] * phi[i]);
+                    double a = dot3(sg[j], sg[i]);
+                    if (o->forms & (1u << ORC_FORM_A)) out[ORC_FORM_A][i * nl + j] += wq * a;
+                    if (o->forms & (1u << ORC_FORM_LAPM)) out[ORC_FORM_LAPM][i * nl + j] += wq * (mob * a);
+                }
+            if (rhs && o->rhs_kind != ORC_RHS_NONE) {
+                double x[3];
+                for (int c = 0; c < 3; ++c) x[c] = xv[0][c] * b[0] + xv[1][c] * b[1] + xv[2][c] * b[2] + xv[3][c] * b[3];
+                double fx = rhs_value(o, x);
+                for (int i = 0; i < nl; ++i) rhs[i] += wq * (fx * phi[i]);
+            }
+        }
+    }
+    /* volume stabilisation: C_n_P1P1 / diagonal block of C_n_vecP2vecP2 */
+    if (o->forms & (1u << ORC_FORM_CN)) {
+        double acc[100];
+        memset(acc, 0, sizeof acc);
+        for (int q = 0; q < 15; ++q) {
+            const double* b = Q3D_NODE[q];
+            double g2[10][3], n[3];
+            p2_grads(b, gl, g2);
+            unit_normal(ls10, g2, n);
+            double dn[10];
+            for (int i = 0; i < nl; ++i) dn[i] = o->p2 ? dot3(n, g2[i]) : dot3(n, gl[i]);
+            for (int i = 0; i < nl; ++i)
+                for (int j = i; j < nl; ++j) acc[i * nl + j] += Q3D_W[q] * (dn[j] * dn[i]);
+        }
+        for (int i = 0; i < nl; ++i)
+            for (int j = i; j < nl; ++j) out[ORC_FORM_CN][i * nl + j] = acc[i * nl + j] * absdet;
+    }
+    for (int f = 0; f < ORC_NUM_MAT_FORMS; ++f)
+        for (int i = 0; i < nl; ++i)
+            for (int j = 0; j < i; ++j) out[f][i * nl + j] = out[f][j * nl + i];
+    return ORC_OK;
+}
+
+/* ======================================================================= */
+/* assembly into CSR: FESystemAccumulator + SparseMatBuilderCL::Build         */
+/* ======================================================================= */
+static int cmp_i32(const void* a, const void* b) {
+    int32_t x = *(const int32_t*)a, y = *(const int32_t*)b;
+    return (x > y) - (x < y);
+}
+
+static int64_t find_col(const int32_t* cols, int64_t lo, int64_t hi, int32_t c) {
+    while (lo < hi) {
+        int64_t mid = (lo + hi) / 2;
+        if (cols[mid] < c) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+static void tet_dofs(const int32_t* tv, const int32_t* te, const int32_t* dof_vert, const int32_t* dof_edge,
+                     int p2, int32_t I[10]) {
+    for (int i = 0; i < 4; ++i) I[i] = dof_vert[tv[i]];
+    if (p2)
+        for (int i = 0; i < 6; ++i) I[4 + i] = dof_edge[te[i]];
+}
+
+int orc_assemble(int64_t nt, const int32_t* tet_v, const int32_t* tet_e, const double* coords,
+                 const double* ls_vert, const double* ls_edge, const uint8_t* active, const int32_t* dof_vert,
+                 const int32_t* dof_edge, int64_t m, const orc_assemble_opts* o, int64_t* rowptr,
+                 int32_t** colind_out, int64_t* nnz_out, double* vals[ORC_NUM_MAT_FORMS], double* rhs) {
+    const int nl = o->p2 ? 10 : 4;
+    /* pattern: count with duplicates, then sort/unique per row */
+    int64_t* cnt = (int64_t*)calloc((size_t)m + 1, sizeof(int64_t));
+    for (int64_t t = 0; t < nt; ++t) {
+        if (!active[t]) continue;
+        int32_t I[10];
+        tet_dofs(tet_v + 4 * t, tet_e + 6 * t, dof_vert, dof_edge, o->p2, I);
+        for (int i = 0; i < nl; ++i) {
+            if (I[i] < 0 || I[i] >= m) {
+                free(cnt);
+                return ORC_ERR_BAD_INPUT;
+            }
+            cnt[I[i] + 1] += nl;
+        }
+    }
+    for (int64_t r = 0; r < m; ++r) cnt[r + 1] += cnt[r];
+    int32_t* tmp = (int32_t*)malloc(sizeof(int32_t) * (size_t)(cnt[m] > 0 ? cnt[m] : 1));
+    int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * (size_t)(m + 1));
+    memcpy(fill, cnt, sizeof(int64_t) * (size_t)(m + 1));
+    for (int64_t t = 0; t < nt; ++t) {
+        if (!active[t]) continue;
+        int32_t I[10];
+        tet_dofs(tet_v + 4 * t, tet_e + 6 * t, dof_vert, dof_edge, o->p2, I);
+        for (int i = 0; i < nl; ++i)
+            for (int j = 0; j < nl; ++j) tmp[fill[I[i]]++] = I[j];
+    }
+    rowptr[0] = 0;
+    for (int64_t r = 0; r < m; ++r) {
+        int64_t b = cnt[r], e = cnt[r + 1];
+        qsort(tmp + b, (size_t)(e - b), sizeof(int32_t), cmp_i32);
+        int64_t u = 0;
+        for (int64_t k = b; k < e; ++k)
+            if (k == b || tmp[k] != tmp[k - 1]) ++u;
+        rowptr[r + 1] = rowptr[r] + u;
+    }
+    int64_t nnz = rowptr[m];
+    int32_t* colind = (int32_t*)malloc(sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1));
+    for (int64_t r = 0; r < m; ++r) {
+        int64_t b = cnt[r], e = cnt[r + 1], w = rowptr[r];
+        for (int64_t k = b; k < e; ++k)
+            if (k == b || tmp[k] != tmp[k - 1]) colind[w++] = tmp[k];
+    }
+    free(tmp);
+    free(fill);
+    free(cnt);
+    for (int f = 0; f < ORC_NUM_MAT_FORMS; ++f) {
+        vals[f] = NULL;
+        if (o->forms & (1u << f)) vals[f] = (double*)calloc((size_t)(nnz > 0 ? nnz : 1), sizeof(double));
+    }
+    if (rhs)
+        for (int64_t r = 0; r < m; ++r) rhs[r] = 0.;
+    /* values: element loop in triangulation order (serial accumulate) */
+    for (int64_t t = 0; t < nt; ++t) {
+        if (!active[t]) continue;
+        int32_t I[10];
+        tet_dofs(tet_v + 4 * t, tet_e + 6 * t, dof_vert, dof_edge, o->p2, I);
+        double xv[4][3], ls10[10];
+        for (int i = 0; i < 4; ++i) memcpy(xv[i], coords + 3 * tet_v[4 * t + i], sizeof xv[i]);
+        gather_ls10(tet_v + 4 * t, tet_e + 6 * t, ls_vert, ls_edge, ls10);
+        double chi_loc[4], loc[ORC_NUM_MAT_FORMS][100], b[10];
+        if (o->chi)
+            for (int i = 0; i < 4; ++i) chi_loc[i] = o->chi[I[i]];
+        int st = orc_local_forms(xv, ls10, o, o->chi ? chi_loc : NULL, loc, b, NULL);
+        if (st) {
+            free(colind);
+            for (int f = 0; f < ORC_NUM_MAT_FORMS; ++f) { free(vals[f]); vals[f] = NULL; }
+            return st;
+        }
+        for (int i = 0; i < nl; ++i) {
+            int32_t r = I[i];
+            for (int j = 0; j < nl; ++j) {
+                int64_t pos = find_col(colind, rowptr[r], rowptr[r + 1], I[j]);
+                for (int f = 0; f < ORC_NUM_MAT_FORMS; ++f)
+                    if (vals[f]) vals[f][pos] += loc[f][i * nl + j];
+            }
+            if (rhs && o->rhs_kind != ORC_RHS_NONE) rhs[r] += b[i];
+        }
+    }
+    *colind_out = colind;
+    *nnz_out = nnz;
+    return ORC_OK;
+}
+
+/* ======================================================================= */
+/* legacy numbering CreateNumbOnInterfaceVertex (misc/problem.cpp:443-505)   */
+/* ======================================================================= */
+int orc_numb_on_interface_p1(int64_t nt, const int32_t* tet_v, const int32_t* tet_e, int64_t nv,
+                             const double* coords, const double* ls_vert, const double* ls_edge, double omit_bound,
+                             int64_t* n_active, int64_t* n_dofs, int32_t* dof_vert) {
+    static const double Q2N[4][3] = {{1., 0., 0.}, {0., 1., 0.}, {0., 0., 1.}, {1. / 3., 1. / 3., 1. / 3.}};
+    static const double Q2W[4] = {1. / 24., 1. / 24., 1. / 24., 0.375};
+    for (int64_t v = 0; v < nv; ++v) dof_vert[v] = -1;
+    int64_t counter = 0, na = 0;
+    for (int64_t t = 0; t < nt; ++t) {
+        double ls10[10], lat[10];
+        gather_ls10(tet_v + 4 * t, tet_e + 6 * t, ls_vert, ls_edge, ls10);
+        for (int k = 0; k < 10; ++k) lat[P2_ON_LAT[k]] = ls10[k];
+        double d = tet_distance(lat, 10);
+        if (d < 0.) return ORC_ERR_ZERO_NODE;
+        if (d != 0.) continue;
+        double xv[4][3];
+        for (int i = 0; i < 4; ++i) memcpy(xv[i], coords + 3 * tet_v[4 * t + i], sizeof xv[i]);
+        double T[3][3], det;
+        trafo(xv, T, &det);
+        double vol = fabs(det) / 6.;
+        double limit = omit_bound < 0. ? 0. : omit_bound * pow(vol * 6, 4. / 3.);
+        orc_patch_t P;
+        int st = orc_make_patch(ls10, &P);
+        if (st) return st;
+        if (P.n_facets == 0) continue;
+        int act = 0;
+        for (int i = 0; i < 4; ++i) {
+            int32_t* slot = &dof_vert[tet_v[4 * t + i]];
+            if (*slot >= 0) { act = 1; continue; }
+            /* coefficients of lambda_i^2 as a P2 function: 1 at vertex i, 1/4 on its edges */
+            double c[10] = {0};
+            c[i] = 1.;
+            for (int e = 0; e < 6; ++e)
+                if (EV[e][0] == i || EV[e][1] == i) c[4 + e] = 0.25;
+            double s = 0.;
+            for (int f = 0; f < P.n_facets; ++f) {
+                double w[3][3];
+                for (int j = 0; j < 3; ++j) {
+                    const double* b = P.bary[P.facet[f][j]];
+                    for (int cc = 0; cc < 3; ++cc)
+                        w[j][cc] = xv[0][cc] * b[0] + xv[1][cc] * b[1] + xv[2][cc] * b[2] + xv[3][cc] * b[3];
+                }
+                double u[3], v[3], cr[3];
+                for (int cc = 0; cc < 3; ++cc) { u[cc] = w[1][cc] - w[0][cc]; v[cc] = w[2][cc] - w[0][cc]; }
+                cr[0] = u[1] * v[2] - u[2] * v[1];
+                cr[1] = u[2] * v[0] - u[0] * v[2];
+                cr[2] = u[0] * v[1] - u[1] * v[0];
+                double fdet = norm3(cr) * (P.boundary[f] ? 0.5 : 1.0);
+                for (int q = 0; q < 4; ++q) {
+                    double b[4], h[10];
+                    for (int cc = 0; cc < 4; ++cc)
+                        b[cc] = P.bary[P.facet[f][0]][cc] * Q2N[q][0] + P.bary[P.facet[f][1]][cc] * Q2N[q][1] +
+                                P.bary[P.facet[f][2]][cc] * Q2N[q][2];
+                    p2_vals(b, h);
+                    double val = 0.;
+                    for (int k = 0; k < 10; ++k) val += c[k] * h[k];
+                    s += (fdet * Q2W[q]) * val;
+                }
+            }
+            if (s > limit) {
+                *slot = (int32_t)counter++;
+                act = 1;
+            }
+        }
+        na += act;
+    }
+    *n_active = na;
+    *n_dofs = counter;
+    return ORC_OK;
+}
+
+/* ======================================================================= */
+/* sparse linear algebra and Krylov solvers                                  */
+/* ======================================================================= */
+void orc_spmv(int64_t m, const int64_t* rowptr, const int32_t* colind, const double* vals, const double* x,
+              double* y) {
+#ifdef _OPENMP
+    int nth = g_threads > 0 ? g_threads : omp_get_max_threads();
+#pragma omp parallel for num_threads(nth) schedule(static)
+#endif
+    for (int64_t r = 0; r < m; ++r) {
+        double s = 0.;
+        for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) s += vals[k] * x[colind[k]];
+        y[r] = s;
+    }
+}
+
+/* KahanInnerProd (num/spmat.h:318-330) */
+double orc_kahan_dot(int64_t n, const double* x, const double* y) {
+    double sum = 0., c = 0., t, yy;
+    for (int64_t i = 0; i < n; ++i) {
+        yy = x[i] * y[i] - c;
+        t = sum + yy;
+        c = (t - sum) - yy;
+        sum = t;
+    }
+    return sum;
+}
+static double plain_dot(int64_t n, const double* x, const double* y) {
+    double s = 0.;
+    for (int64_t i = 0; i < n; ++i) s += x[i] * y[i];
+    return s;
+}
+
+/* diagonal found by a row scan (SolveGSstep<PB_JAC0>, num/precond.h:153-169) */
+static void jacobi_diag(int64_t m, const int64_t* rowptr, const int32_t* colind, const double* vals, double* d) {
+    for (int64_t r = 0; r < m; ++r) {
+        int64_t k = rowptr[r];
+        while (k < rowptr[r + 1] && colind[k] != r) ++k;
+        d[r] = k < rowptr[r + 1] ? vals[k] : 0.;
+    }
+}
+
+int orc_pcg_jacobi(int64_t m, const int64_t* rowptr, const int32_t* colind, const double* vals, const double* b,
+                   double* x, int* max_iter, double* tol, int rel) {
+    double* d = (double*)malloc(sizeof(double) * (size_t)m * 6);
+    double *p = d + m, *z = p + m, *q = z + m, *r = q + m, *tmp = r + m;
+    jacobi_diag(m, rowptr, colind, vals, d);
+    orc_spmv(m, rowptr, colind, vals, x, tmp);
+    for (int64_t i = 0; i < m; ++i) r[i] = b[i] - tmp[i];
+    double resid = sqrt(orc_kahan_dot(m, r, r));
+    double normb = sqrt(orc_kahan_dot(m, b, b));
+    if (normb == 0.0 || !rel) normb = 1.0;
+    resid = resid / normb;
+    if (resid <= *tol) {
+        *tol = resid;
+        *max_iter = 0;
+        free(d);
+        return ORC_OK;
+    }
+    for (int64_t i = 0; i < m; ++i) z[i] = 1.0 * r[i] / d[i];
+    double rho = orc_kahan_dot(m, z, r), rho_1;
+    memcpy(p, z, sizeof(double) * (size_t)m);
+    for (int it = 1; it <= *max_iter; ++it) {
+        orc_spmv(m, rowptr, colind, vals, p, q);
+        double lambda = orc_kahan_dot(m, q, p);
+        double alpha = rho / lambda;
+        for (int64_t i = 0; i < m; ++i) x[i] += alpha * p[i];
+        for (int64_t i = 0; i < m; ++i) r[i] += (-alpha) * q[i];
+        resid = sqrt(orc_kahan_dot(m, r, r)) / normb;
+        if (resid <= *tol) {
+            *tol = resid;
+            *max_iter = it;
+            free(d);
+            return ORC_OK;
+        }
+        for (int64_t i = 0; i < m; ++i) z[i] = 1.0 * r[i] / d[i];
+        rho_1 = rho;
+        rho = orc_kahan_dot(m, z, r);
+        double beta = rho / rho_1;
+        for (int64_t i = 0; i < m; ++i) p[i] = z[i] + beta * p[i];
+    }
+    *tol = resid;
+    free(d);
+    return ORC_ERR_NOT_CONVERGED;
+}
+
+int orc_gmres_jacobi(int64_t m, const int64_t* rowptr, const int32_t* colind, const double* vals, const double* b,
+                     double* x, int restart, int* max_iter, double* tol, int rel, int method) {
+    int mm = restart <= *max_iter ? restart : *max_iter;
+    double* d = (double*)malloc(sizeof(double) * (size_t)m * (size_t)(mm + 4));
+    double *w = d + m, *r = w + m, *t = r + m, *V = t + m;
+    double* H = (double*)calloc((size_t)mm * mm, sizeof(double));
+    double* s = (double*)calloc((size_t)mm, sizeof(double));
+    double* cs = (double*)calloc((size_t)mm, sizeof(double));
+    double* sn = (double*)calloc((size_t)mm, sizeof(double));
+    double* y = (double*)calloc((size_t)mm, sizeof(double));
+#define HH(i, j) H[(size_t)(i) * mm + (j)]
+    jacobi_diag(m, rowptr, colind, vals, d);
+    double beta, normb, resid;
+    orc_spmv(m, rowptr, colind, vals, x, t);
+    if (method == 0) {
+        for (int64_t i = 0; i < m; ++i) r[i] = b[i] - t[i];
+        beta = sqrt(plain_dot(m, r, r));
+        normb = sqrt(plain_dot(m, b, b));
+    } else {
+        for (int64_t i = 0; i < m; ++i) r[i] = (b[i] - t[i]) / d[i];
+        beta = sqrt(plain_dot(m, r, r));
+        for (int64_t i = 0; i < m; ++i) w[i] = b[i] / d[i];
+        normb = sqrt(plain_dot(m, w, w));
+    }
+    if (normb == 0.0 || !rel) normb = 1.0;
+    resid = beta / normb;
+    int ret = ORC_ERR_NOT_CONVERGED;
+    if (resid <= *tol) {
+        *tol = resid;
+        *max_iter = 0;
+        ret = ORC_OK;
+        goto done;
+    }
+    int j = 1;
+    while (j <= *max_iter) {
+        for (int64_t k = 0; k < m; ++k) V[k] = r[k] * (1.0 / beta);
+        for (int k = 0; k < mm; ++k) s[k] = 0.;
+        s[0] = beta;
+        int i;
+        for (i = 0; i < mm - 1 && j <= *max_iter; ++i, ++j) {
+            double* vi = V + (size_t)i * m;
+            if (method == 0) {
+                for (int64_t k = 0; k < m; ++k) t[k] = vi[k] / d[k];
+                orc_spmv(m, rowptr, colind, vals, t, w);
+            } else {
+                orc_spmv(m, rowptr, colind, vals, vi, t);
+                for (int64_t k = 0; k < m; ++k) w[k] = t[k] / d[k];
+            }
+            for (int k = 0; k <= i; ++k) {
+                double* vk = V + (size_t)k * m;
+                HH(k, i) = plain_dot(m, w, vk);
+                for (int64_t q = 0; q < m; ++q) w[q] -= HH(k, i) * vk[q];
+            }
+            HH(i + 1, i) = sqrt(plain_dot(m, w, w));
+            double* vn = V + (size_t)(i + 1) * m;
+            for (int64_t q = 0; q < m; ++q) vn[q] = w[q] * (1.0 / HH(i + 1, i));
+            for (int k = 0; k < i; ++k) {
+                double tmp = cs[k] * HH(k, i) + sn[k] * HH(k + 1, i);
+                HH(k + 1, i) = -sn[k] * HH(k, i) + cs[k] * HH(k + 1, i);
+                HH(k, i) = tmp;
+            }
+            /* GMRES_GeneratePlaneRotation / ApplyPlaneRotation (num/krylovsolver.h:263-282) */
+            {
+                double dx = HH(i, i), dy = HH(i + 1, i);
+                if (dy == 0.0) { cs[i] = 1.0; sn[i] = 0.0; }
+                else { double rr = sqrt(dx * dx + dy * dy); cs[i] = dx / rr; sn[i] = dy / rr; }
+                double tmp = cs[i] * HH(i, i) + sn[i] * HH(i + 1, i);
+                HH(i + 1, i) = -sn[i] * HH(i, i) + cs[i] * HH(i + 1, i);
+                HH(i, i) = tmp;
+                tmp = cs[i] * s[i] + sn[i] * s[i + 1];
+                s[i + 1] = -sn[i] * s[i] + cs[i] * s[i + 1];
+                s[i] = tmp;
+            }
+            resid = fabs(s[i + 1]) / normb;
+            if (resid <= *tol) {
+                int kk = i;
+                for (int q = 0; q <= kk; ++q) y[q] = s[q];
+                for (int q = kk; q >= 0; --q) {
+                    y[q] /= HH(q, q);
+                    for (int p = q - 1; p >= 0; --p) y[p] -= HH(p, q) * y[q];
+                }
+                if (method == 0) {
+                    for (int64_t k = 0; k < m; ++k) w[k] = 0.;
+                    for (int q = 0; q <= kk; ++q)
+                        for (int64_t k = 0; k < m; ++k) w[k] += y[q] * V[(size_t)q * m + k];
+                    for (int64_t k = 0; k < m; ++k) x[k] += w[k] / d[k];
+                } else {
+                    for (int q = 0; q <= kk; ++q)
+                        for (int64_t k = 0; k < m; ++k) x[k] += y[q] * V[(size_t)q * m + k];
+                }
+                *tol = resid;
+                *max_iter = j;
+                ret = ORC_OK;
+                goto done;
+            }
+        }
+        {
+            int kk = i - 1;
+            for (int q = 0; q <= kk; ++q) y[q] = s[q];
+            for (int q = kk; q >= 0; --q) {
+                y[q] /= HH(q, q);
+                for (int p = q - 1; p >= 0; --p) y[p] -= HH(p, q) * y[q];
+            }
+            if (method == 0) {
+                for (int64_t k = 0; k < m; ++k) w[k] = 0.;
+                for (int q = 0; q <= kk; ++q)
+                    for (int64_t k = 0; k < m; ++k) w[k] += y[q] * V[(size_t)q * m + k];
+                for (int64_t k = 0; k < m; ++k) x[k] += w[k] / d[k];
+                orc_spmv(m, rowptr, colind, vals, x, t);
+                for (int64_t k = 0; k < m; ++k) r[k] = b[k] - t[k];
+            } else {
+                for (int q = 0; q <= kk; ++q)
+                    for (int64_t k = 0; k < m; ++k) x[k] += y[q] * V[(size_t)q * m + k];
+                orc_spmv(m, rowptr, colind, vals, x, t);
+                for (int64_t k = 0; k < m; ++k) r[k] = (b[k] - t[k]) / d[k];
+            }
+        }
+        beta = sqrt(plain_dot(m, r, r));
+        resid = beta / normb;
+        if (resid <= *tol) {
+            *tol = resid;
+            *max_iter = j;
+            ret = ORC_OK;
+            goto done;
+        }
+    }
+    *tol = resid;
+done:
+#undef HH
+    free(d);
+    free(H);
+    free(s);
+    free(cs);
+    free(sn);
+    free(y);
+    return ret;
+}
+
+int orc_ch_block(int64_t m, const int64_t* rowptr, const int32_t* colind, const double* M, const double* A,
+                 const double* C, double alpha, double mob, double rho, double eps2, double beta, int64_t* browptr,
+                 int32_t* bcolind, double* bvals) {
+    /* row r of the top blocks: [alpha*M | mob*A + rho*C]; bottom: [eps2*A + beta*M + eps2*rho*C | -M] */
+    int64_t w = 0;
+    browptr[0] = 0;
+    for (int half = 0; half < 2; ++half)
+        for (int64_t r = 0; r < m; ++r) {
+            for (int blk = 0; blk < 2; ++blk)
+                for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+                    double v;
+                    if (half == 0) v = blk == 0 ? alpha * M[k] : mob * A[k] + rho * C[k];
+                    else v = blk == 0 ? (eps2 * A[k] + beta * M[k]) + (eps2 * rho) * C[k] : -1. * M[k];
+                    bcolind[w] = (int32_t)(colind[k] + blk * m);
+                    bvals[w] = v;
+                    ++w;
+                }
+            browptr[half * m + r + 1] = w;
+        }
+    return ORC_OK;
+}

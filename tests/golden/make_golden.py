@@ -1,0 +1,105 @@
+"""Regenerates the golden fixtures in this folder from the DROPS reference itself.
+
+Runs oracle/_ref/ref_harness (built from the reference sources by
+oracle/build_ref.sh) on small cases of the TraceFEM path and stores what the
+reference computed as compressed .npz files.  Level-set values on edges are
+re-indexed from the reference's edge order to this library's brick edge
+numbering by the edge's two vertex indices (vertex order is identical).  Large
+integer arrays that are only checked for bit-exactness are stored as SHA-256
+digests.
+
+    python tests/golden/make_golden.py            (needs the reference sources)
+"""
+import hashlib
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, HERE)
+from oracle import pyoracle as O  # noqa: E402
+from tfg import read_tfg  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def run(*args):
+    with tempfile.TemporaryDirectory() as d:
+        out = os.path.join(d, "out.bin")
+        subprocess.check_call([HARNESS, *args, out], cwd=d, stdout=subprocess.DEVNULL)
+        return read_tfg(out)
+
+
+def edge_map(mesh, ref_edge_v):
+    key = {tuple(sorted(p)): i for i, p in enumerate(mesh.edge_v.tolist())}
+    return np.array([key[tuple(sorted(p))] for p in ref_edge_v.reshape(-1, 2).tolist()], dtype=np.int64)
+
+
+def system_case(name, fe, ls, shape, n, a, solve):
+    d = run("system", fe, ls, shape, str(n), repr(a), "1" if solve else "0")
+    mesh = O.brick(n, a=a)
+    emap = edge_map(mesh, d["edge_v"])
+    ls_edge = np.empty(mesh.ne)
+    ls_edge[emap] = d["ls_edge"]
+    tev = np.sort(d["tet_ev"].reshape(-1, 6, 2), axis=2)
+    out = dict(
+        n=n, a=a, p2=int(fe == "p2"), ls_p2=int(ls == "lsP2"), shape=shape,
+        coords_sha=sha(d["coords"]), tet_v_sha=sha(d["tet_v"].astype(np.int64)),
+        tet_edge_pairs_sha=sha(tev.astype(np.int64)),
+        ls_vert=d["ls_vert"], ls_edge=ls_edge,
+        n_active=int(d["n_active"][0]), n_dofs=int(d["n_dofs"][0]),
+        active_tets=d["active_tets"].astype(np.int32), loc2glo=d["loc2glo"].astype(np.int32),
+        rowptr=d["M.rowptr"], colind=d["M.colind"].astype(np.int32),
+        M=d["M.vals"], A=d["A.vals"], C=d["C.vals"], rhs=d["rhs"],
+        ref_time_dofs=d["time_dofs"][0], ref_time_assemble=d["time_assemble"][0],
+    )
+    if solve:
+        assert np.array_equal(d["S.rowptr"], d["M.rowptr"]) and np.array_equal(d["S.colind"], d["M.colind"])
+        out.update(S=d["S.vals"], x=d["x"], iters=int(d["iters"][0]), resid=float(d["resid"][0]),
+                   ref_time_solve=d["time_solve"][0])
+    np.savez_compressed(os.path.join(HERE, name), **out)
+    print(name, "active", out["n_active"], "dofs", out["n_dofs"], "nnz", len(out["colind"]))
+
+
+def area_case():
+    d = run("area")
+    np.savez_compressed(
+        os.path.join(HERE, "area_sphere05_n8.npz"), surface=d["surface"][0], per_tet=d["per_tet"],
+        n_facets=d["n_facets"].astype(np.int32), patch_tets=d["patch_tets"].astype(np.int32),
+        patch_nverts=d["patch_nverts"].astype(np.int32), patch_facets=d["patch_facets"].astype(np.int32),
+        patch_boundary=d["patch_boundary"].astype(np.int32), patch_verts=d["patch_verts"],
+        tet_v_sha=sha(d["tet_v"].astype(np.int64)), coords_sha=sha(d["coords"]))
+    print("area", d["surface"][0])
+
+
+def legacy_case():
+    out = {}
+    for c in ("plane", "plane2", "sphere"):
+        d = run("legacy_numb", c)
+        out[c + "_status"] = int(d["status"][0])
+        out[c + "_n_dofs"] = int(d["n_dofs"][0])
+        out[c + "_n_active"] = int(d["n_active"][0])
+        if "dof_vert" in d:
+            out[c + "_dof_vert"] = d["dof_vert"].astype(np.int32)
+    np.savez_compressed(os.path.join(HERE, "legacy_numbering.npz"), **out)
+    print("legacy", {k: v for k, v in out.items() if not k.endswith("dof_vert")})
+
+
+if __name__ == "__main__":
+    if not os.path.exists(HARNESS):
+        subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
+    system_case("c1_sphere_p1_n16.npz", "p1", "lsP1", "sphere", 16, 5.0 / 3.0, True)
+    system_case("sphere_p2_n8.npz", "p2", "lsP2", "sphere", 8, 5.0 / 3.0, True)
+    system_case("torus_p1_n16.npz", "p1", "lsP1", "torus", 16, 1.6, True)
+    system_case("torus_p2_n10.npz", "p2", "lsP2", "torus", 10, 1.6, False)
+    area_case()
+    legacy_case()

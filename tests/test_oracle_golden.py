@@ -1,0 +1,127 @@
+"""The C oracle against golden vectors produced by the DROPS reference itself.
+
+Fixtures come from tests/golden/make_golden.py, which runs the reference's own
+BrickBuilderCL, DistributeDOFs, setupFESystem and PCGSolverCL<JACPcCL>.  These
+tests pin the oracle before it is used as the checker of the CUDA path.
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+from tests.helpers import loc2glo, mat_close, sha, sol_close
+
+SYSTEMS = [
+    ("c1_sphere_p1_n16.npz", O.LS_SPHERE, [0, 0, 0, 1.0]),
+    ("sphere_p2_n8.npz", O.LS_SPHERE, [0, 0, 0, 1.0]),
+    ("torus_p1_n16.npz", O.LS_TORUS, [1.0, 0.4, 2]),
+    ("torus_p2_n10.npz", O.LS_TORUS, [1.0, 0.4, 2]),
+]
+
+
+@pytest.mark.parametrize("name,kind,par", SYSTEMS)
+def test_mesh_levelset_dofs_bitexact(golden, name, kind, par):
+    g = golden(name)
+    mesh = O.brick(int(g["n"]), a=float(g["a"]))
+    assert sha(mesh.coords.ravel()) == str(g["coords_sha"])
+    assert sha(mesh.tet_v.astype(np.int64).ravel()) == str(g["tet_v_sha"])
+    pairs = np.sort(mesh.edge_v[mesh.tet_e], axis=2).astype(np.int64)
+    assert sha(pairs.ravel()) == str(g["tet_edge_pairs_sha"])
+    lv, le = O.levelset(mesh, kind, par, p2=bool(g["ls_p2"]))
+    assert np.array_equal(lv, g["ls_vert"]) and np.array_equal(le, g["ls_edge"])
+    p2 = bool(g["p2"])
+    st, na, nd, dv, de, act = O.distribute_dofs(mesh, lv, le, p2)
+    assert st == O.OK and na == int(g["n_active"]) and nd == int(g["n_dofs"])
+    assert np.array_equal(np.nonzero(act)[0], g["active_tets"])
+    assert np.array_equal(loc2glo(mesh, act, dv, de, p2), g["loc2glo"])
+
+
+@pytest.mark.parametrize("name,kind,par", SYSTEMS)
+def test_assembly_matches_reference(golden, name, kind, par):
+    g = golden(name)
+    p2 = bool(g["p2"])
+    mesh = O.brick(int(g["n"]), a=float(g["a"]))
+    lv, le = O.levelset(mesh, kind, par, p2=bool(g["ls_p2"]))
+    st, na, nd, dv, de, act = O.distribute_dofs(mesh, lv, le, p2)
+    opts = O.make_opts(p2, [O.FORM_M, O.FORM_A, O.FORM_CN], O.RHS_SPHERE_XYZ, [0, 0, 0, 1.0, 13.0])
+    st, rp, ci, vals, rhs = O.assemble(mesh, lv, le, act, dv, de, nd, opts)
+    assert st == O.OK
+    assert np.array_equal(rp, g["rowptr"]) and np.array_equal(ci, g["colind"])
+    for f, key in ((O.FORM_M, "M"), (O.FORM_A, "A"), (O.FORM_CN, "C")):
+        ok, err = mat_close(vals[f], g[key])
+        assert ok, (key, err)
+    ok, err = mat_close(rhs, g["rhs"])
+    assert ok, err
+
+
+@pytest.mark.parametrize("name", ["c1_sphere_p1_n16.npz", "sphere_p2_n8.npz", "torus_p1_n16.npz"])
+def test_pcg_jacobi_matches_reference(golden, name):
+    g = golden(name)
+    rp, ci = g["rowptr"], g["colind"]
+    st, x, it, res = O.pcg_jacobi(rp, ci, g["S"], g["rhs"], tol=1e-10)
+    assert st == O.OK and res <= 1e-10
+    assert abs(it - int(g["iters"])) <= 1
+    ok, err = sol_close(x, g["x"])
+    assert ok, err
+
+
+def test_lincomb_matches_reference(golden):
+    g = golden("c1_sphere_p1_n16.npz")
+    h = 2 * float(g["a"]) / int(g["n"])
+    ok, err = mat_close(g["M"] + g["A"] + h * g["C"], g["S"])
+    assert ok, err
+
+
+def test_surface_area_golden(golden):
+    """tests/principallattice.cpp:316-347: area 3.0909 (rel 1e-4), per-tet areas and patches."""
+    g = golden("area_sphere05_n8.npz")
+    assert abs(float(g["surface"]) - 3.0909) / 3.0909 < 1e-4
+    mesh = O.brick(8, a=1.0)
+    assert sha(mesh.coords.ravel()) == str(g["coords_sha"])
+    lv, le = O.levelset(mesh, O.LS_SPHERE, [0, 0, 0, 0.5], p2=True)
+    # the reference test visits every tet (vertices with phi == 0 included);
+    # the P1 hat functions sum to one, so the mass entries of a tet sum to its area
+    opts = O.make_opts(False, [O.FORM_M])
+    per_tet = np.zeros(mesh.nt)
+    for t in range(mesh.nt):
+        ls10 = np.concatenate([lv[mesh.tet_v[t]], le[mesh.tet_e[t]]])
+        st, forms, _, nf = O.local_forms(mesh.coords[mesh.tet_v[t]], ls10, opts)
+        assert st == O.OK and nf == int(g["n_facets"][t])
+        per_tet[t] = forms[O.FORM_M].sum()
+    assert np.abs(per_tet - g["per_tet"]).max() <= 1e-14
+    assert abs(per_tet.sum() - float(g["surface"])) <= 1e-12
+    fo = vo = 0
+    for i, t in enumerate(g["patch_tets"]):
+        ls10 = np.concatenate([lv[mesh.tet_v[t]], le[mesh.tet_e[t]]])
+        st, f, b, v = O.make_patch(ls10)
+        k = int(g["n_facets"][t])
+        nv = int(g["patch_nverts"][i])
+        assert st == O.OK
+        assert np.array_equal(f, g["patch_facets"][3 * fo:3 * (fo + k)].reshape(-1, 3))
+        assert np.array_equal(b, g["patch_boundary"][fo:fo + k])
+        assert np.array_equal(v, g["patch_verts"][4 * vo:4 * (vo + nv)].reshape(-1, 4))
+        fo += k
+        vo += nv
+
+
+def test_legacy_numbering_golden(golden):
+    """tests/interfaceP1FE.cpp: 8 (plane), 1156 (sphere); a plane through
+    vertices makes distance() throw in the reference as shipped."""
+    g = golden("legacy_numbering.npz")
+    cases = {
+        "plane": ((10, 1, 1), [1, 0, 0, 0.41]),
+        "plane2": ((10, 1, 1), [1, 0, 0, 0.4]),
+        "sphere": ((20, 20, 20), None),
+    }
+    for c, (n, par) in cases.items():
+        mesh = O.brick(n, orig=np.zeros(3), e=np.eye(3))
+        if par is None:
+            lv, le = O.levelset(mesh, O.LS_SPHERE, [0.5, 0.5, 0.5, 0.31], p2=True)
+        else:
+            lv, le = O.levelset(mesh, O.LS_PLANE, par, p2=True)
+        st, na, nd, dv = O.numb_on_interface_p1(mesh, lv, le)
+        if int(g[c + "_status"]) != 0:
+            assert st == O.ERR_ZERO_NODE
+            continue
+        assert st == O.OK and nd == int(g[c + "_n_dofs"]) and na == int(g[c + "_n_active"])
+        assert np.array_equal(dv, g[c + "_dof_vert"])
+    assert int(g["sphere_n_dofs"]) == 1156 and int(g["plane_n_dofs"]) == 8
