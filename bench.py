@@ -1,0 +1,354 @@
+"""Benchmark of the TraceFEM path (DROPS) on GB300.
+
+Workload (one "step"): the P2 surface-Poisson problem on the sphere |x| = 1 in
+[-5/3, 5/3]^3 split into 96^3 Kuhn cubes (5,308,416 tets), P2 level set by
+nodal interpolation, f = 13 xyz at ext(x):
+    IdxDescCL::DistributeDOFs (P2IF) -> setupFESystem {M, A, C_n, F}
+    -> LinComb M + A + h C_n -> Jacobi-PCG to relative residual 1e-10
+(FP32 PCG sweeps inside FP64 iterative refinement).  The level set is the
+input; everything downstream of it is recomputed every step.
+
+value: cut tets per second through the whole step, inputs resident in HBM.
+e2e:   the same through the C ABI from pinned host buffers: level-set upload
+       (H2D), the step, solution download (D2H) inside the timed region.
+L2 is flushed (2x L2 bytes written) before every timed step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm on the host cores: the C
+restatement in oracle/ (the DROPS sources do not exist on the GPU host), same
+workload, FP64 Jacobi-PCG as in the reference, all host threads.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_CUBES = 96
+HALF = 5.0 / 3.0
+H = 2 * HALF / N_CUBES
+SPHERE = [0.0, 0.0, 0.0, 1.0]
+RHS = [0.0, 0.0, 0.0, 1.0, 13.0]
+TOL = 1e-10
+METRIC = "cut tets/s through DistributeDOFs + setupFESystem + Jacobi-PCG to rel. residual 1e-10 (P2 TraceFEM)"
+CONFIG = {
+    "workload": "surface Poisson, P2 TraceFEM, sphere r=1 in [-5/3,5/3]^3, 96^3 Kuhn cubes (5,308,416 tets), "
+                "P2 level set, f=13xyz(ext x), A=M+A_LB+h*C_n, Jacobi-PCG rel 1e-10, FP32 inner / FP64 refinement",
+    "mesh": "96^3 x 6 tets", "fe": "P2IF", "solver": "PCG+Jacobi, mixed FP32/FP64 IR", "tol": TOL,
+    "l2": "flushed before every timed step (2x L2 size written)", "parallelism": "replicas",
+}
+
+
+# ---------------------------------------------------------------------------
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=ws)
+        return rank, ws, dist
+    return 0, 1, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def all_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def all_sum(dist, v):
+    if dist is None:
+        return v
+    import torch
+
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples (200 ms) while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.3)
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) >= 9:
+                    rows.append(p)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+def pcg_bytes(m, nnz, iters, fp32):
+    """Algorithmic bytes of the persistent PCG per iteration: CSR values and
+    column indices once, row pointers once, vectors: z and p gathered (counted
+    once), p_new and q written, x, r, p_new, q, diag read and x, r, z written."""
+    vb = 4 if fp32 else 8
+    return iters * ((vb + 4) * nnz + 4 * (m + 1) + 12 * vb * m)
+
+
+def run_ours(args, rank, ws, dist):
+    import drops_gb300 as tf
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    ctx = tf.TraceFEM(dev)
+    ctx.brick_cube(N_CUBES, HALF)
+    ctx.levelset_analytic(tf.LS_SPHERE, SPHERE, p2=True)
+    nv, ne, nt = ctx.mesh_info()
+    lv_dev, le_dev = ctx.levelset_download()
+    pin_v, pin_e = tf.PinnedArray(nv), tf.PinnedArray(ne)
+    pin_v.array[:] = lv_dev
+    pin_e.array[:] = le_dev
+
+    forms = [tf.FORM_M, tf.FORM_A, tf.FORM_CN]
+    state = {}
+
+    def step(precision=tf.PREC_MIXED):
+        na, m = ctx.distribute_dofs(tf.P2IF)
+        nnz = ctx.setup_fe_system(forms, tf.RHS_SPHERE_XYZ, RHS)
+        ctx.lincomb(forms, [1.0, 1.0, H])
+        ctx.vec_fill(tf.VEC_X, m, 0.0)
+        st, it, res = ctx.pcg_jacobi(tf.MAT_SYS, tf.VEC_RHS, tf.VEC_X, tol=TOL, precision=precision)
+        if st != tf.OK or res > TOL:
+            raise RuntimeError(f"solve failed: status {st}, residual {res}")
+        state.update(na=na, m=m, nnz=nnz, it=it, res=res)
+        return na
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    barrier(dist)
+
+    # ---- device-resident timed region --------------------------------------
+    ctx.timing(True)
+    ctx.timing_reset()
+    launches0 = ctx.launch_count()
+    step_ms, cut = [], 0
+    with Clocks(dev) as clk:
+        for _ in range(args.steps):
+            ctx.flush_l2()
+            barrier(dist)
+            ctx.marker(0)
+            cut += step()
+            ctx.marker(1)
+            step_ms.append(ctx.elapsed_ms(0, 1))
+    launches = ctx.launch_count() - launches0 - args.steps  # the flushes are memsets, not kernels
+    ktimes = {name: ctx.timing_get(k) for k, name in enumerate(tf.KERNEL_NAMES)}
+    ctx.timing(False)
+    clocks = clk.summary()
+    total_ms = all_max(dist, sum(step_ms))
+    total_cut = all_sum(dist, cut)
+    value = total_cut / (total_ms / 1e3)
+
+    # ---- end to end through the C ABI from pinned host buffers -------------
+    pin_x = tf.PinnedArray(state["m"])
+    e2e_ms, e2e_cut = [], 0
+    for _ in range(args.steps):
+        ctx.flush_l2()
+        barrier(dist)
+        ctx.marker(2)
+        ctx.levelset_upload(pin_v.array, pin_e.array)
+        e2e_cut += step()
+        if pin_x.array.size != state["m"]:
+            pin_x.free()
+            pin_x = tf.PinnedArray(state["m"])
+        ctx.vec_download(tf.VEC_X, out=pin_x.array)
+        ctx.marker(3)
+        e2e_ms.append(ctx.elapsed_ms(2, 3))
+    e2e_total = all_max(dist, sum(e2e_ms))
+    e2e_value = all_sum(dist, e2e_cut) / (e2e_total / 1e3)
+
+    # ---- mixed vs plain FP64 solve time on the same system ----------------
+    solve = {}
+    for prec, name in ((tf.PREC_FP64, "fp64"), (tf.PREC_MIXED, "mixed")):
+        ctx.vec_fill(tf.VEC_X, state["m"], 0.0)
+        ctx.flush_l2()
+        ctx.marker(4)
+        st, it, res = ctx.pcg_jacobi(tf.MAT_SYS, tf.VEC_RHS, tf.VEC_X, tol=TOL, precision=prec)
+        ctx.marker(5)
+        solve[name] = {"ms": ctx.elapsed_ms(4, 5), "iters": it, "resid": res}
+
+    # ---- roofline of the dominant kernel ------------------------------------
+    dom = max(ktimes, key=lambda k: ktimes[k][0])
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    ms_d, n_d = ktimes[dom]
+    na, m, nnz = state["na"], state["m"], state["nnz"]
+    if dom == "pcg":
+        per_launch = pcg_bytes(m, nnz, state["it"], fp32=True)
+        note = "FP32 inner PCG iterations of one solve: (4+4)*nnz + 4*(m+1) + 48*m bytes per iteration"
+    elif dom == "assemble":
+        per_launch = na * (10 * 8 + 3 * 55 * 8 + 10 * 8)
+        note = "per cut tet: 10 level-set values read, 3 packed 10x10 element matrices + load vector written"
+    else:
+        per_launch = 0
+        note = "no byte model for this kernel"
+    achieved = per_launch / ((ms_d / max(n_d, 1)) / 1e3) / 1e9 if ms_d > 0 else 0.0
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                "frac": round(achieved / hbm_peak, 4), "traffic": None, "peak_source": peak_src,
+                "bytes_model": note, "launch_ms": round(ms_d / max(n_d, 1), 4)}
+
+    out = {
+        "metric": METRIC, "value": round(value, 1), "unit": "cut_tets/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic (analytic level set)",
+        "config": CONFIG,
+        "e2e": {"value": round(e2e_value, 1), "unit": "cut_tets/s", "h2d_bytes_per_step": 8 * (nv + ne),
+                "d2h_bytes_per_step": 8 * state["m"], "ms_per_step": round(e2e_total / args.steps, 3)},
+        "gpu_launches": int(launches),
+        "roofline": roofline,
+        "clocks": clocks,
+        "problem": {"tets": nt, "cut_tets": na, "dofs": m, "nnz": nnz, "pcg_iters_inner": state["it"]},
+        "solve_ms": solve,
+        "kernel_ms": {k: round(v[0] / args.steps, 4) for k, v in ktimes.items() if v[1]},
+    }
+    ctx.close()
+    pin_v.free()
+    pin_e.free()
+    pin_x.free()
+    return out
+
+
+# ---------------------------------------------------------------------------
+def cpu_workload(threads):
+    """The same step with the oracle (C restatement of the reference) on the host."""
+    from oracle import pyoracle as O
+
+    O.set_threads(threads)
+    mesh = O.brick(N_CUBES, a=HALF)
+    lv, le = O.levelset(mesh, O.LS_SPHERE, SPHERE, True)
+    opts = O.make_opts(True, [O.FORM_M, O.FORM_A, O.FORM_CN], O.RHS_SPHERE_XYZ, RHS)
+
+    def step():
+        t0 = time.perf_counter()
+        st, na, m, dv, de, act = O.distribute_dofs(mesh, lv, le, True)
+        st, rp, ci, vals, rhs = O.assemble(mesh, lv, le, act, dv, de, m, opts)
+        S = vals[O.FORM_M] + vals[O.FORM_A] + H * vals[O.FORM_CN]
+        st, x, it, res = O.pcg_jacobi(rp, ci, S, rhs, tol=TOL)
+        return na, time.perf_counter() - t0, it
+
+    return step
+
+
+def run_reference(args, rank, ws, dist):
+    if rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    step = cpu_workload(threads)
+    for _ in range(args.warmup):
+        step()
+    tot_t, tot_cut = 0.0, 0
+    for _ in range(args.steps):
+        na, dt, it = step()
+        tot_t += dt
+        tot_cut += na
+    value = tot_cut / tot_t
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": "cut_tets/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * tot_t / args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (analytic level set)", "config": CONFIG,
+        "cpu_baseline": {"value": round(value, 1), "unit": "cut_tets/s", "cores": threads, "kind": "port",
+                         "sample": "the full workload per step (FP64 Jacobi-PCG as in the reference); "
+                                   "C restatement of the reference in oracle/, SpMV on all host threads"},
+        "e2e": {"value": round(value, 1), "unit": "cut_tets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, ws, dist = dist_init()
+    if args.impl == "reference":
+        out = run_reference(args, rank, ws, dist)
+        if rank == 0:
+            print(json.dumps(out))
+        return
+    from drops_gb300 import build
+
+    if rank == 0:
+        build.build()
+    barrier(dist)
+    out = run_ours(args, rank, ws, dist)
+    if rank == 0:
+        if ws == 1 and not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            step = cpu_workload(threads)
+            na, dt, it = step()
+            out["cpu_baseline"] = {"value": round(na / dt, 1), "unit": "cut_tets/s", "cores": threads, "kind": "port",
+                                   "sample": f"one full step of the same workload ({dt:.1f} s, FP64 PCG {it} iterations)"}
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,310 @@
+"""drops_gb300: the TraceFEM path of DROPS on GB300 (sm_103a).
+
+The compute path is libtracefem.so (CUDA, built by drops_gb300/build.py) with
+the C ABI declared in include/tracefem.h.  This module is a thin ctypes front
+end over that ABI, named after the reference's interface:
+
+    ctx = TraceFEM()
+    ctx.brick(orig, e1, e2, e3, n1, n2, n3)          # BrickBuilderCL
+    ctx.levelset_analytic(LS_SPHERE, [0, 0, 0, 1])     # LSInit / LinearLSInit
+    n_active, n = ctx.distribute_dofs(P1IF)            # IdxDescCL::DistributeDOFs
+    nnz = ctx.setup_fe_system([FORM_M, FORM_A, FORM_CN], RHS_SPHERE_XYZ, [...])
+    ctx.lincomb([FORM_M, FORM_A, FORM_CN], [1, 1, h])  # MatrixCL LinComb ctor
+    it, res = ctx.pcg_jacobi(MAT_SYS, VEC_RHS, VEC_X, tol=1e-10)   # PCGSolverCL<JACPcCL>
+
+There is no CPU fallback: if the library is missing or no suitable GPU is
+present, constructing a context raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libtracefem.so")
+
+# status codes
+OK, ERR_CUDA, ERR_ZERO_NODE, ERR_ZERO_PATTERN, ERR_BAD_INPUT, ERR_NOT_CONVERGED, ERR_CAPACITY, ERR_WATCHDOG, ERR_NO_DEVICE = range(9)
+P1IF, P2IF = 1, 2
+FORM_M, FORM_A, FORM_CN, FORM_LAPM = 0, 1, 2, 3
+MAT_SYS, MAT_BLOCK, MAT_USER = 4, 5, 6
+VEC_RHS, VEC_X, VEC_B, VEC_CHI, VEC_T0, VEC_T1, VEC_T2, VEC_T3 = range(8)
+LS_SPHERE, LS_TORUS, LS_ELLIPSOID, LS_PLANE = range(4)
+RHS_NONE, RHS_SPHERE_XYZ, RHS_CONST = range(3)
+PREC_FP64, PREC_MIXED = 0, 1
+K_CLASSIFY, K_NUMBER, K_ASSEMBLE, K_PATTERN, K_SCATTER, K_SPMV, K_PCG, K_GMRES, K_LEVELSET = range(9)
+KERNEL_NAMES = ["classify", "number", "assemble", "pattern", "scatter", "spmv", "pcg", "gmres", "levelset"]
+
+# every symbol include/tracefem.h declares
+EXPORTS = [
+    "tf_create", "tf_destroy", "tf_last_error", "tf_status_string", "tf_stream", "tf_mesh_brick", "tf_mesh_upload",
+    "tf_mesh_info", "tf_mesh_download", "tf_levelset_upload", "tf_levelset_analytic", "tf_levelset_download",
+    "tf_distribute_dofs", "tf_create_numb_on_interface_p1", "tf_dofs_download", "tf_setup_fe_system",
+    "tf_matrix_info", "tf_matrix_download", "tf_matrix_upload", "tf_lincomb", "tf_ch_block", "tf_vec_upload",
+    "tf_vec_download", "tf_vec_size", "tf_vec_fill", "tf_spmv", "tf_pcg_jacobi", "tf_gmres_jacobi", "tf_timing_enable",
+    "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2",
+    "tf_host_alloc", "tf_host_free",
+]
+
+
+class TraceFEMError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"[{status}] {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Loads libtracefem.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with drops_gb300.build.build() (nvcc, sm_103a)")
+    L = C.CDLL(path)
+    L.tf_last_error.restype = C.c_char_p
+    L.tf_status_string.restype = C.c_char_p
+    L.tf_stream.restype = C.c_void_p
+    L.tf_launch_count.restype = C.c_int64
+    L.tf_host_alloc.restype = C.c_void_p
+    L.tf_host_alloc.argtypes = [C.c_size_t]
+    L.tf_host_free.argtypes = [C.c_void_p]
+    _lib = L
+    return L
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32)) if a is not None else None
+
+
+def _lp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int64)) if a is not None else None
+
+
+class TraceFEM:
+    """One device context (tf_context)."""
+
+    def __init__(self, device=0):
+        self.L = load_library()
+        h = C.c_void_p()
+        st = self.L.tf_create(C.byref(h), C.c_int(device))
+        if st != OK:
+            raise TraceFEMError(st, self.L.tf_status_string(st).decode() + " (no sm_103a-capable GPU / driver)")
+        self.h = h
+        self.fe = None
+        self.m = 0
+
+    def close(self):
+        if self.h:
+            self.L.tf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st):
+        if st != OK:
+            raise TraceFEMError(st, self.L.tf_last_error(self.h).decode())
+
+    def call(self, name, *args):
+        """Raw call; returns the status without raising."""
+        return getattr(self.L, name)(self.h, *args)
+
+    # ---- mesh -----------------------------------------------------------
+    def brick(self, orig, e1, e2, e3, n1, n2, n3):
+        v = [np.ascontiguousarray(x, dtype=np.float64) for x in (orig, e1, e2, e3)]
+        self._check(self.L.tf_mesh_brick(self.h, *[_dp(x) for x in v], C.c_int(n1), C.c_int(n2), C.c_int(n3)))
+        self._keep = v
+
+    def brick_cube(self, n, a):
+        """[-a,a]^3 with n^3 cubes."""
+        self.brick([-a, -a, -a], [2 * a, 0, 0], [0, 2 * a, 0], [0, 0, 2 * a], n, n, n)
+
+    def mesh_upload(self, coords, tet_v, tet_e, edge_v):
+        coords = np.ascontiguousarray(coords, dtype=np.float64)
+        tet_v = np.ascontiguousarray(tet_v, dtype=np.int32)
+        tet_e = np.ascontiguousarray(tet_e, dtype=np.int32)
+        edge_v = np.ascontiguousarray(edge_v, dtype=np.int32)
+        self._check(self.L.tf_mesh_upload(self.h, C.c_int64(coords.size // 3), _dp(coords), C.c_int64(tet_v.size // 4),
+                                          _ip(tet_v), _ip(tet_e), C.c_int64(edge_v.size // 2), _ip(edge_v)))
+
+    def mesh_info(self):
+        nv, ne, nt = C.c_int64(), C.c_int64(), C.c_int64()
+        self._check(self.L.tf_mesh_info(self.h, C.byref(nv), C.byref(ne), C.byref(nt)))
+        return nv.value, ne.value, nt.value
+
+    def mesh_download(self):
+        nv, ne, nt = self.mesh_info()
+        coords = np.empty((nv, 3))
+        tv = np.empty((nt, 4), np.int32)
+        te = np.empty((nt, 6), np.int32)
+        ev = np.empty((ne, 2), np.int32)
+        self._check(self.L.tf_mesh_download(self.h, _dp(coords), _ip(tv), _ip(te), _ip(ev)))
+        return coords, tv, te, ev
+
+    # ---- level set ---------------------------------------------------------
+    def levelset_upload(self, ls_vert, ls_edge=None):
+        ls_vert = np.ascontiguousarray(ls_vert, dtype=np.float64)
+        ls_edge = None if ls_edge is None else np.ascontiguousarray(ls_edge, dtype=np.float64)
+        self._check(self.L.tf_levelset_upload(self.h, _dp(ls_vert), _dp(ls_edge)))
+
+    def levelset_analytic(self, kind, par, p2=False):
+        par = np.ascontiguousarray(par, dtype=np.float64)
+        self._check(self.L.tf_levelset_analytic(self.h, C.c_int(kind), _dp(par), C.c_int(par.size), C.c_int(int(p2))))
+
+    def levelset_download(self):
+        nv, ne, nt = self.mesh_info()
+        lv, le = np.empty(nv), np.empty(ne)
+        self._check(self.L.tf_levelset_download(self.h, _dp(lv), _dp(le)))
+        return lv, le
+
+    # ---- DOFs ----------------------------------------------------------------
+    def distribute_dofs(self, fe, dist=0.0):
+        na, nd = C.c_int64(), C.c_int64()
+        self._check(self.L.tf_distribute_dofs(self.h, C.c_int(fe), C.c_double(dist), C.byref(na), C.byref(nd)))
+        self.fe, self.n_active, self.m = fe, na.value, nd.value
+        return na.value, nd.value
+
+    def create_numb_on_interface_p1(self, omit_bound=-1.0):
+        na, nd = C.c_int64(), C.c_int64()
+        self._check(self.L.tf_create_numb_on_interface_p1(self.h, C.c_double(omit_bound), C.byref(na), C.byref(nd)))
+        self.fe, self.n_active, self.m = P1IF, na.value, nd.value
+        return na.value, nd.value
+
+    def dofs(self):
+        nv, ne, nt = self.mesh_info()
+        nl = 10 if self.fe == P2IF else 4
+        dv = np.empty(nv, np.int32)
+        de = np.empty(ne, np.int32) if self.fe == P2IF else None
+        act = np.empty(max(self.n_active, 1), np.int32)
+        l2g = np.empty(max(self.n_active * nl, 1), np.int32)
+        self._check(self.L.tf_dofs_download(self.h, _ip(dv), _ip(de), _ip(act), _ip(l2g)))
+        return dv, de, act[: self.n_active], l2g[: self.n_active * nl]
+
+    # ---- assembly ----------------------------------------------------------------
+    def setup_fe_system(self, forms, rhs_kind=RHS_NONE, rhs_par=()):
+        mask = sum(1 << f for f in forms)
+        par = np.ascontiguousarray(rhs_par if len(rhs_par) else [0.0], dtype=np.float64)
+        nnz = C.c_int64()
+        self._check(self.L.tf_setup_fe_system(self.h, C.c_uint(mask), C.c_int(rhs_kind), _dp(par),
+                                              C.c_int(len(rhs_par)), C.byref(nnz)))
+        return nnz.value
+
+    def matrix(self, mat):
+        m, nnz = C.c_int64(), C.c_int64()
+        self._check(self.L.tf_matrix_info(self.h, C.c_int(mat), C.byref(m), C.byref(nnz)))
+        rp = np.empty(m.value + 1, np.int64)
+        ci = np.empty(max(nnz.value, 1), np.int64)
+        v = np.empty(max(nnz.value, 1))
+        self._check(self.L.tf_matrix_download(self.h, C.c_int(mat), _lp(rp), _lp(ci), _dp(v)))
+        return rp, ci[: nnz.value], v[: nnz.value]
+
+    def matrix_upload(self, rowptr, colind, vals):
+        rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+        colind = np.ascontiguousarray(colind, dtype=np.int64)
+        vals = np.ascontiguousarray(vals, dtype=np.float64)
+        self._check(self.L.tf_matrix_upload(self.h, C.c_int64(rowptr.size - 1), _lp(rowptr), _lp(colind), _dp(vals)))
+
+    def lincomb(self, forms, coeffs):
+        f = np.ascontiguousarray(forms, dtype=np.int32)
+        c = np.ascontiguousarray(coeffs, dtype=np.float64)
+        self._check(self.L.tf_lincomb(self.h, C.c_int(f.size), f.ctypes.data_as(C.POINTER(C.c_int)), _dp(c)))
+
+    def ch_block(self, alpha, mob, rho, eps2, beta, use_lapm=False):
+        self._check(self.L.tf_ch_block(self.h, C.c_double(alpha), C.c_double(mob), C.c_double(rho), C.c_double(eps2),
+                                       C.c_double(beta), C.c_int(int(use_lapm))))
+
+    # ---- vectors and solvers --------------------------------------------------------
+    def vec_upload(self, vec, data):
+        data = np.ascontiguousarray(data, dtype=np.float64)
+        self._check(self.L.tf_vec_upload(self.h, C.c_int(vec), C.c_int64(data.size), _dp(data)))
+
+    def vec_download(self, vec, out=None):
+        n = C.c_int64()
+        self._check(self.L.tf_vec_size(self.h, C.c_int(vec), C.byref(n)))
+        if out is None:
+            out = np.empty(n.value)
+        self._check(self.L.tf_vec_download(self.h, C.c_int(vec), _dp(out), C.c_int64(n.value)))
+        return out
+
+    def vec_fill(self, vec, n, value=0.0):
+        self._check(self.L.tf_vec_fill(self.h, C.c_int(vec), C.c_int64(n), C.c_double(value)))
+
+    def spmv(self, mat, vec_x, vec_y):
+        self._check(self.L.tf_spmv(self.h, C.c_int(mat), C.c_int(vec_x), C.c_int(vec_y)))
+
+    def pcg_jacobi(self, mat, vec_b, vec_x, tol=1e-10, max_iter=100000, rel=True, precision=PREC_FP64, check=True):
+        it, t = C.c_int(max_iter), C.c_double(tol)
+        st = self.L.tf_pcg_jacobi(self.h, C.c_int(mat), C.c_int(vec_b), C.c_int(vec_x), C.c_int(precision),
+                                  C.byref(it), C.byref(t), C.c_int(int(rel)))
+        if check and st not in (OK, ERR_NOT_CONVERGED):
+            self._check(st)
+        return st, it.value, t.value
+
+    def gmres_jacobi(self, mat, vec_b, vec_x, restart=50, tol=1e-10, max_iter=100000, rel=True, method=0,
+                     precision=PREC_FP64, check=True):
+        it, t = C.c_int(max_iter), C.c_double(tol)
+        st = self.L.tf_gmres_jacobi(self.h, C.c_int(mat), C.c_int(vec_b), C.c_int(vec_x), C.c_int(restart),
+                                    C.c_int(method), C.c_int(precision), C.byref(it), C.byref(t), C.c_int(int(rel)))
+        if check and st not in (OK, ERR_NOT_CONVERGED):
+            self._check(st)
+        return st, it.value, t.value
+
+    # ---- instrumentation ------------------------------------------------------------------
+    def timing(self, on=True):
+        self._check(self.L.tf_timing_enable(self.h, C.c_int(int(on))))
+
+    def timing_reset(self):
+        self._check(self.L.tf_timing_reset(self.h))
+
+    def timing_get(self, kernel):
+        ms, n = C.c_double(), C.c_int64()
+        self._check(self.L.tf_timing_get(self.h, C.c_int(kernel), C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def launch_count(self):
+        return int(self.L.tf_launch_count(self.h))
+
+    def marker(self, slot):
+        self._check(self.L.tf_marker_record(self.h, C.c_int(slot)))
+
+    def elapsed_ms(self, a, b):
+        ms = C.c_double()
+        self._check(self.L.tf_marker_elapsed(self.h, C.c_int(a), C.c_int(b), C.byref(ms)))
+        return ms.value
+
+    def flush_l2(self):
+        self._check(self.L.tf_flush_l2(self.h))
+
+
+class PinnedArray:
+    """A numpy view of page-locked host memory (tf_host_alloc)."""
+
+    def __init__(self, n, dtype=np.float64):
+        L = load_library()
+        dt = np.dtype(dtype)
+        self.nbytes = max(int(n) * dt.itemsize, 1)
+        self.ptr = L.tf_host_alloc(self.nbytes)
+        if not self.ptr:
+            raise MemoryError("tf_host_alloc failed")
+        self.array = np.ctypeslib.as_array((C.c_byte * self.nbytes).from_address(self.ptr)).view(dt)[: int(n)]
+
+    def free(self):
+        if self.ptr:
+            load_library().tf_host_free(C.c_void_p(self.ptr))
+            self.ptr = None

@@ -1,0 +1,828 @@
+// Surface patches, quadrature and local forms; CSR pattern; segmented scatter.
+//
+// One warp assembles one cut tet (grid-stride over the active tets):
+//   patch   lanes 0..7 take the 8 sub-tets of the order-2 principal lattice
+//           (PrincipalLatticeCL, geom/principallattice.cpp:33-79), classify
+//           their sign pattern through the 81-entry facet table
+//           (RefPatchBuilderCL<3>::assign, geom/reftetracut.cpp:53-60) and
+//           place their facets with a warp scan -- facet order is the
+//           reference's (sub-tet order, table order);
+//   points  lanes take the 7 Quad5_2D nodes of the facets (num/discretize.cpp:
+//           263-294, weights |det| (x1/2 on lattice faces), num/quadrature.tpp:
+//           265-314), 32 points per round, and stage weight, basis values and
+//           surface gradients (I - n n^T) grad(phi) in shared memory, with
+//           n = grad(phi_h)/|grad(phi_h)| of the P2 level set
+//           (LocalAssembler::buildNormal, surfactant/ifacetransp.h:1066-1072);
+//   forms   lanes own entries (i <= j) of the symmetric element matrices and
+//           sum over the staged points (quad_2D, num/quadrature.tpp:31-108);
+//           C_n uses the 15-point Quad5 rule on the tet times |det J|.
+// Element matrices go to a packed buffer; the CSR values are then formed by a
+// segmented sum over contributions sorted by (row, column, tet), i.e. in the
+// reference's triangulation-order accumulation, without atomics.
+#include <climits>
+
+#include "tf_internal.cuh"
+
+namespace tf {
+
+// ---------------------------------------------------------------------------
+// constant tables (built on the host at first use)
+// ---------------------------------------------------------------------------
+struct Tables {
+    double lat_v[10][4];    // lattice vertices (barycentric)
+    int lat_t[8][4];        // lattice sub-tets
+    int can_a[8][6];        // cut-edge orientation of the first sub-tet holding the edge
+    int can_b[8][6];
+    int ledge[8][6];        // lattice edge id 0..24
+    signed char pat_nf[81]; // facets per sign pattern (-1: all-zero pattern)
+    signed char pat_bnd[81];
+    signed char pat_f[81][2][3];  // ext ids: 0..3 vertex, 4..9 edge + 4
+    double q2_node[7][3], q2_w[7];
+    double q3_node[15][4], q3_w[15];
+    double qq2_node[4][3], qq2_w[4];  // Quad2_2D (legacy numbering)
+    int sym_i[55], sym_j[55];  // packed upper triangle, NL = 10
+    int sym4_i[10], sym4_j[10];  // NL = 4
+};
+__constant__ Tables cT;
+static bool g_tables_ready[64] = {false};
+
+__constant__ int cP2OnLat[10] = {0, 4, 7, 9, 1, 2, 5, 3, 6, 8};  // p2_dof_on_lattice_2
+
+static void build_tables(Tables& T) {
+    // lattice of order 2 (PrincipalLatticeCL ctor and create_tetras)
+    const int n = 2;
+    int nv = 0;
+    for (int x = 0; x <= n; ++x)
+        for (int y = 0; y <= x; ++y)
+            for (int z = 0; z <= y; ++z, ++nv) {
+                T.lat_v[nv][0] = (double)(n - x) / n;
+                T.lat_v[nv][1] = (double)(x - y) / n;
+                T.lat_v[nv][2] = (double)(y - z) / n;
+                T.lat_v[nv][3] = (double)z / n;
+            }
+    auto vidx = [](int i, int j, int k) {
+        return (i > 0 ? ((i + 2) * (i + 1) * i) / 6 : 0) + (j > 0 ? ((j + 1) * j) / 2 : 0) + k;
+    };
+    static const int perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+    int nt = 0;
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j <= i; ++j)
+            for (int k = 0; k <= j; ++k)
+                for (int l = 0; l < 6; ++l) {
+                    int t[4][3] = {{i, j, k}};
+                    bool ok = true;
+                    for (int s = 1; s < 4 && ok; ++s) {
+                        for (int q = 0; q < 3; ++q) t[s][q] = t[s - 1][q];
+                        ++t[s][perm[l][s - 1]];
+                        ok = n >= t[s][0] && t[s][0] >= t[s][1] && t[s][1] >= t[s][2];
+                    }
+                    if (!ok) continue;
+                    for (int s = 0; s < 4; ++s) T.lat_t[nt][s] = vidx(t[s][0], t[s][1], t[s][2]);
+                    ++nt;
+                }
+    // canonical cut-edge orientation and lattice edge ids
+    int seen_a[64], seen_b[64], nseen = 0;
+    for (int s = 0; s < 8; ++s)
+        for (int e = 0; e < 6; ++e) {
+            const int a = T.lat_t[s][ev0(e)], b = T.lat_t[s][ev1(e)];
+            const int lo = a < b ? a : b, hi = a < b ? b : a;
+            int id = -1;
+            for (int q = 0; q < nseen; ++q)
+                if ((seen_a[q] < seen_b[q] ? seen_a[q] : seen_b[q]) == lo &&
+                    (seen_a[q] < seen_b[q] ? seen_b[q] : seen_a[q]) == hi)
+                    id = q;
+            if (id < 0) {
+                id = nseen++;
+                seen_a[id] = a;
+                seen_b[id] = b;
+            }
+            T.can_a[s][e] = seen_a[id];
+            T.can_b[s][e] = seen_b[id];
+            T.ledge[s][e] = id;
+        }
+    // sign-pattern facet table (SignTraitsCL<3>::compute_cuts + RefPatchBuilderCL<3>::assign)
+    for (int p = 0; p < 81; ++p) {
+        int sg[4], q = p, sum = 0;
+        for (int k = 0; k < 4; ++k) {
+            sg[k] = (q % 3) - 1;
+            q /= 3;
+            sum += sg[k];
+        }
+        // index = sum (s_k + 1) 3^k
+        T.pat_nf[p] = 0;
+        T.pat_bnd[p] = 0;
+        if (sg[0] == 0 && sg[1] == 0 && sg[2] == 0 && sg[3] == 0) {
+            T.pat_nf[p] = -1;
+            continue;
+        }
+        int cut[4], nr = 0, nrv = 0;
+        if (sum != 4 && sum != -4) {
+            for (int k = 0; k < 4; ++k)
+                if (sg[k] == 0) cut[nrv++] = k;
+            nr = nrv;
+            for (int e = 0; e < 6; ++e)
+                if (sg[ev0(e)] * sg[ev1(e)] == -1) cut[nr++] = e + 4;
+        }
+        if (nr < 3) continue;
+        T.pat_nf[p] = (signed char)(nr - 2);
+        T.pat_bnd[p] = nrv == 3;
+        for (int f = 0; f + 2 < nr; ++f)
+            for (int j = 0; j < 3; ++j) T.pat_f[p][f][j] = (signed char)cut[f + j];
+    }
+    // quadrature rules (Quad5_2DDataCL, Quad5DataCL, Quad2_2DDataCL)
+    const double s15 = std::sqrt(15.0);
+    const double A1 = (6.0 - s15) / 21.0, B1 = (9.0 + 2.0 * s15) / 21.0;
+    const double A2 = (6.0 + s15) / 21.0, B2 = (9.0 - 2.0 * s15) / 21.0;
+    const double n2[7][3] = {{1. / 3., 1. / 3., 1. / 3.}, {A1, A1, B1}, {A1, B1, A1}, {B1, A1, A1},
+                             {A2, A2, B2}, {A2, B2, A2}, {B2, A2, A2}};
+    for (int i = 0; i < 7; ++i)
+        for (int j = 0; j < 3; ++j) T.q2_node[i][j] = n2[i][j];
+    T.q2_w[0] = 9. / 80.;
+    for (int i = 1; i <= 3; ++i) T.q2_w[i] = (155. - s15) / 2400.;
+    for (int i = 4; i <= 6; ++i) T.q2_w[i] = (155. + s15) / 2400.;
+    const double a1 = (7.0 - s15) / 34.0, b1 = (13.0 + 3.0 * s15) / 34.0;
+    const double a2 = (7.0 + s15) / 34.0, b2 = (13.0 - 3.0 * s15) / 34.0;
+    const double a3 = (10.0 - 2.0 * s15) / 40.0, b3 = (10.0 + 2.0 * s15) / 40.0;
+    const double n3[15][4] = {{0.25, 0.25, 0.25, 0.25}, {a1, a1, a1, b1}, {a1, a1, b1, a1}, {a1, b1, a1, a1},
+                              {b1, a1, a1, a1},         {a2, a2, a2, b2}, {a2, a2, b2, a2}, {a2, b2, a2, a2},
+                              {b2, a2, a2, a2},         {a3, a3, b3, b3}, {a3, b3, a3, b3}, {a3, b3, b3, a3},
+                              {b3, a3, a3, b3},         {b3, a3, b3, a3}, {b3, b3, a3, a3}};
+    for (int i = 0; i < 15; ++i)
+        for (int j = 0; j < 4; ++j) T.q3_node[i][j] = n3[i][j];
+    T.q3_w[0] = 0.01975308641975308641975308641975308641975;
+    for (int i = 1; i <= 4; ++i) T.q3_w[i] = 0.01198951396316977000173064248499538621936;
+    for (int i = 5; i <= 8; ++i) T.q3_w[i] = 0.01151136787104539754677023934921978132914;
+    for (int i = 9; i <= 14; ++i) T.q3_w[i] = 0.008818342151675485008818342151675485008818;
+    const double qq[4][3] = {{1., 0., 0.}, {0., 1., 0.}, {0., 0., 1.}, {1. / 3., 1. / 3., 1. / 3.}};
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 3; ++j) T.qq2_node[i][j] = qq[i][j];
+    T.qq2_w[0] = T.qq2_w[1] = T.qq2_w[2] = 1. / 24.;
+    T.qq2_w[3] = 0.375;
+    int k = 0;
+    for (int i = 0; i < 10; ++i)
+        for (int j = i; j < 10; ++j, ++k) {
+            T.sym_i[k] = i;
+            T.sym_j[k] = j;
+        }
+    k = 0;
+    for (int i = 0; i < 4; ++i)
+        for (int j = i; j < 4; ++j, ++k) {
+            T.sym4_i[k] = i;
+            T.sym4_j[k] = j;
+        }
+}
+
+int ensure_tables(Context* c) {
+    if (c->device >= 0 && c->device < 64 && g_tables_ready[c->device]) return TF_OK;
+    Tables T;
+    build_tables(T);
+    TF_CUDA(c, cudaMemcpyToSymbol(cT, &T, sizeof(Tables)));
+    if (c->device >= 0 && c->device < 64) g_tables_ready[c->device] = true;
+    return TF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// per-tet geometry shared by the kernels
+// ---------------------------------------------------------------------------
+struct TetGeom {
+    double X[4][3];   // vertex coordinates
+    double gl[4][3];  // world gradients of the barycentric coordinates (T * ref grads)
+    double G[4][3];   // gradient of the P2 level set at the 4 vertices (linear field)
+    double absdet;    // |det J|
+};
+
+// GetTrafoTr (geom/multigrid.h:603-623), P1 gradients and the vertex values
+// of grad(phi_h) for the P2 level set ls10 (4 vertex + 6 edge values).
+__device__ inline void tet_geometry(TetGeom& g, const double ls10[10]) {
+    double M[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) M[j][i] = g.X[i + 1][j] - g.X[0][j];
+    const double d = M[0][0] * (M[1][1] * M[2][2] - M[1][2] * M[2][1]) - M[0][1] * (M[1][0] * M[2][2] - M[1][2] * M[2][0]) +
+                     M[0][2] * (M[1][0] * M[2][1] - M[1][1] * M[2][0]);
+    double T[3][3];
+    T[0][0] = (M[1][1] * M[2][2] - M[1][2] * M[2][1]) / d;
+    T[0][1] = (M[2][0] * M[1][2] - M[1][0] * M[2][2]) / d;
+    T[0][2] = (M[1][0] * M[2][1] - M[2][0] * M[1][1]) / d;
+    T[1][0] = (M[2][1] * M[0][2] - M[0][1] * M[2][2]) / d;
+    T[1][1] = (M[0][0] * M[2][2] - M[2][0] * M[0][2]) / d;
+    T[1][2] = (M[2][0] * M[0][1] - M[0][0] * M[2][1]) / d;
+    T[2][0] = (M[0][1] * M[1][2] - M[1][1] * M[0][2]) / d;
+    T[2][1] = (M[1][0] * M[0][2] - M[0][0] * M[1][2]) / d;
+    T[2][2] = (M[0][0] * M[1][1] - M[1][0] * M[0][1]) / d;
+    g.absdet = fabs(d);
+    for (int r = 0; r < 3; ++r) {
+        g.gl[0][r] = -T[r][0] - T[r][1] - T[r][2];
+        g.gl[1][r] = T[r][0];
+        g.gl[2][r] = T[r][1];
+        g.gl[3][r] = T[r][2];
+    }
+    // grad H_i(e_v) = (4 delta_iv - 1) gl_i ; grad H_ab(e_v) = 4 (delta_bv gl_a + delta_av gl_b)
+    for (int v = 0; v < 4; ++v)
+        for (int r = 0; r < 3; ++r) {
+            double s = 0.;
+            for (int i = 0; i < 4; ++i) s += ls10[i] * ((i == v ? 3. : -1.) * g.gl[i][r]);
+            for (int e = 0; e < 6; ++e) {
+                const int a = ev0(e), b = ev1(e);
+                if (b == v) s += ls10[4 + e] * (4. * g.gl[a][r]);
+                if (a == v) s += ls10[4 + e] * (4. * g.gl[b][r]);
+            }
+            g.G[v][r] = s;
+        }
+}
+
+__device__ inline void unit_normal(const TetGeom& g, const double b[4], double n[3]) {
+    double v[3];
+    for (int r = 0; r < 3; ++r) v[r] = b[0] * g.G[0][r] + b[1] * g.G[1][r] + b[2] * g.G[2][r] + b[3] * g.G[3][r];
+    const double inv = 1.0 / sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    n[0] = v[0] * inv;
+    n[1] = v[1] * inv;
+    n[2] = v[2] * inv;
+}
+
+template <bool P2>
+__device__ inline void basis(const TetGeom& g, const double b[4], double* phi, double (*grad)[3]) {
+    if constexpr (!P2) {
+        for (int i = 0; i < 4; ++i) {
+            phi[i] = b[i];
+            for (int r = 0; r < 3; ++r) grad[i][r] = g.gl[i][r];
+        }
+    } else {
+        for (int i = 0; i < 4; ++i) {
+            phi[i] = b[i] * (2. * b[i] - 1.);
+            const double f = 4. * b[i] - 1.;
+            for (int r = 0; r < 3; ++r) grad[i][r] = f * g.gl[i][r];
+        }
+        for (int e = 0; e < 6; ++e) {
+            const int a = ev0(e), c = ev1(e);
+            phi[4 + e] = 4. * b[a] * b[c];
+            for (int r = 0; r < 3; ++r) grad[4 + e][r] = 4. * (b[c] * g.gl[a][r] + b[a] * g.gl[c][r]);
+        }
+    }
+}
+
+struct RhsPar {
+    int kind;
+    double p[8];
+};
+__device__ inline double rhs_value(const RhsPar& R, const double x[3]) {
+    if (R.kind == TF_RHS_CONST) return R.p[0];
+    if (R.kind == TF_RHS_SPHERE_XYZ) {
+        const double d0 = x[0] - R.p[0], d1 = x[1] - R.p[1], d2 = x[2] - R.p[2];
+        const double nd = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+        const double dist = nd - R.p[3];
+        const double y0 = x[0] - dist * (d0 / nd), y1 = x[1] - dist * (d1 / nd), y2 = x[2] - dist * (d2 / nd);
+        return R.p[4] * y0 * y1 * y2;
+    }
+    return 0.;
+}
+
+__device__ inline void set_status(int* st, int code, int64_t where) {
+    if (atomicCAS(st, 0, code) == 0) st[1] = (int)where;
+}
+
+
+__device__ inline void sym_entry(int nl, int k, int& i, int& j) {
+    if (nl == 10) {
+        i = cT.sym_i[k];
+        j = cT.sym_j[k];
+    } else {
+        i = cT.sym4_i[k];
+        j = cT.sym4_j[k];
+    }
+}
+__host__ __device__ inline int sym_index(int nl, int i, int j) {
+    if (i > j) {
+        const int t = i;
+        i = j;
+        j = t;
+    }
+    return i * nl - (i * (i - 1)) / 2 + (j - i);
+}
+
+// ---------------------------------------------------------------------------
+// the warp's patch: facets of the 8 lattice sub-tets (sub-tet order)
+// ---------------------------------------------------------------------------
+struct PatchSmem {
+    double fb[16][3][4];  // facet vertices, barycentric
+    double fw[16];        // |det| of the facet, x1/2 on lattice faces
+    int bnd[16];
+    int nf;
+};
+
+// cut point of a lattice edge: ConvexComb(ls_a/(ls_a - ls_b), v_a, v_b)
+// (MergeCutPolicyCL::operator(), geom/subtriangulation.h:514-524), rounded
+// like the reference (no contraction).
+__device__ inline void cut_point(const double* lat, int a, int b, double out[4]) {
+    const double t = __ddiv_rn(lat[a], __dsub_rn(lat[a], lat[b]));
+    const double s = __dsub_rn(1.0, t);
+    for (int c = 0; c < 4; ++c) out[c] = __dadd_rn(__dmul_rn(s, cT.lat_v[a][c]), __dmul_rn(t, cT.lat_v[b][c]));
+}
+
+// All lanes call; lanes 0..7 own one sub-tet each.  Returns the facet count.
+__device__ int warp_patch(const double ls10[10], const double X[4][3], PatchSmem& P, int lane, int* status,
+                          int64_t tet) {
+    double lat[10];
+    for (int k = 0; k < 10; ++k) lat[cP2OnLat[k]] = ls10[k];
+    int nf = 0, pat = 0;
+    if (lane < 8) {
+        for (int k = 0; k < 4; ++k) {
+            const double v = lat[cT.lat_t[lane][k]];
+            pat += ((v > 0.) - (v < 0.) + 1) * (k == 0 ? 1 : k == 1 ? 3 : k == 2 ? 9 : 27);
+        }
+        nf = cT.pat_nf[pat];
+        if (nf < 0) {
+            set_status(status, TF_ERR_ZERO_PATTERN, tet);
+            nf = 0;
+        }
+    }
+    int incl = nf;
+    for (int o = 1; o < 8; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 7);
+    if (lane < 8) {
+        const int off = incl - nf;
+        const int bnd = cT.pat_bnd[pat];
+        for (int f = 0; f < nf; ++f) {
+            double w[3][3];
+            for (int j = 0; j < 3; ++j) {
+                const int ext = cT.pat_f[pat][f][j];
+                double b[4];
+                if (ext < 4) {
+                    const int L = cT.lat_t[lane][ext];
+                    for (int c = 0; c < 4; ++c) b[c] = cT.lat_v[L][c];
+                } else {
+                    cut_point(lat, cT.can_a[lane][ext - 4], cT.can_b[lane][ext - 4], b);
+                }
+                for (int c = 0; c < 4; ++c) P.fb[off + f][j][c] = b[c];
+                for (int r = 0; r < 3; ++r) w[j][r] = X[0][r] * b[0] + X[1][r] * b[1] + X[2][r] * b[2] + X[3][r] * b[3];
+            }
+            double u[3], v[3];
+            for (int r = 0; r < 3; ++r) {
+                u[r] = w[1][r] - w[0][r];
+                v[r] = w[2][r] - w[0][r];
+            }
+            const double c0 = u[1] * v[2] - u[2] * v[1], c1 = u[2] * v[0] - u[0] * v[2], c2 = u[0] * v[1] - u[1] * v[0];
+            P.fw[off + f] = sqrt(c0 * c0 + c1 * c1 + c2 * c2) * (bnd ? 0.5 : 1.0);
+            P.bnd[off + f] = bnd;
+        }
+    }
+    if (lane == 0) P.nf = total;
+    __syncwarp();
+    return total;
+}
+
+// ---------------------------------------------------------------------------
+// assembly kernel: warp per active tet
+// ---------------------------------------------------------------------------
+constexpr int kAsmWarps = 4;
+
+template <int NL>
+struct AsmSmem {
+    TetGeom g;
+    double ls10[10];
+    PatchSmem P;
+    double w[32];
+    double phi[32][NL];   // also n.grad(phi) for the volume rule
+    double sg[32][NL][3];
+    double mob[32];
+    double fx[32];
+};
+
+struct AsmArgs {
+    MeshView M;
+    const double* lsv;
+    const double* lse;
+    int64_t n_active;
+    const int32_t* active;
+    const int32_t* l2g;
+    unsigned forms;
+    RhsPar rhs;
+    const double* chi;  // P1 DOF vector for LaplaceM (NULL: mobility 1)
+    int degenerate;
+    double* elem;       // [form][n_active][nsym]
+    double* elem_rhs;   // [n_active][NL]
+    int* status;
+};
+
+template <int NL>
+__global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
+    constexpr bool P2 = NL == 10;
+    constexpr int NSYM = NL * (NL + 1) / 2;
+    constexpr int EPL = (NSYM + 31) / 32;  // entries per lane
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    AsmSmem<NL>& S = reinterpret_cast<AsmSmem<NL>*>(smem_raw)[wib];
+    const bool wantM = A.forms & (1u << TF_FORM_M), wantA = A.forms & (1u << TF_FORM_A);
+    const bool wantC = A.forms & (1u << TF_FORM_CN), wantL = A.forms & (1u << TF_FORM_LAPM);
+    const bool wantF = A.rhs.kind != TF_RHS_NONE;
+    const int64_t nwarps = (int64_t)gridDim.x * kAsmWarps;
+
+    for (int64_t r = (int64_t)blockIdx.x * kAsmWarps + wib; r < A.n_active; r += nwarps) {
+        const int32_t t = A.active[r];
+        int32_t v[4], e[6];
+        mesh_tet(A.M, t, v, e);
+        if (lane < 4) {
+            double x[3];
+            mesh_coord(A.M, v[lane], x);
+            for (int c = 0; c < 3; ++c) S.g.X[lane][c] = x[c];
+            S.ls10[lane] = A.lsv[v[lane]];
+        } else if (lane < 10) {
+            S.ls10[lane] = A.lse[e[lane - 4]];
+        }
+        __syncwarp();
+        if (lane == 0) tet_geometry(S.g, S.ls10);
+        double ls10[10];
+        for (int k = 0; k < 10; ++k) ls10[k] = S.ls10[k];
+        __syncwarp();
+        const int nf = warp_patch(ls10, S.g.X, S.P, lane, A.status, t);
+        double chi_loc[4] = {0, 0, 0, 0};
+        if (wantL && A.chi && A.degenerate)
+            for (int k = 0; k < 4; ++k) chi_loc[k] = A.chi[A.l2g[r * NL + k]];
+
+        double accM[EPL], accA[EPL], accL[EPL], accC[EPL];
+        for (int q = 0; q < EPL; ++q) accM[q] = accA[q] = accL[q] = accC[q] = 0.;
+        double accF = 0.;
+        const int npts = 7 * nf;
+        for (int base = 0; base < npts; base += 32) {
+            const int p = base + lane;
+            if (p < npts) {
+                const int f = p / 7, q = p - 7 * (p / 7);
+                double b[4];
+                for (int c = 0; c < 4; ++c)
+                    b[c] = S.P.fb[f][0][c] * cT.q2_node[q][0] + S.P.fb[f][1][c] * cT.q2_node[q][1] +
+                           S.P.fb[f][2][c] * cT.q2_node[q][2];
+                const double w = S.P.fw[f] * cT.q2_w[q];
+                double n[3];
+                unit_normal(S.g, b, n);
+                double phi[NL], grad[NL][3];
+                basis<P2>(S.g, b, phi, grad);
+                S.w[lane] = w;
+                for (int i = 0; i < NL; ++i) {
+                    S.phi[lane][i] = phi[i];
+                    const double gn = grad[i][0] * n[0] + grad[i][1] * n[1] + grad[i][2] * n[2];
+                    for (int c = 0; c < 3; ++c) S.sg[lane][i][c] = grad[i][c] - gn * n[c];
+                }
+                if (wantL) {
+                    double m = 1.0;
+                    if (A.chi && A.degenerate) {
+                        const double ch = chi_loc[0] * b[0] + chi_loc[1] * b[1] + chi_loc[2] * b[2] + chi_loc[3] * b[3];
+                        m = ch * (1. - ch);
+                        if (m < 0.) m = 0.;
+                    }
+                    S.mob[lane] = m;
+                }
+                if (wantF) {
+                    double x[3];
+                    for (int c = 0; c < 3; ++c)
+                        x[c] = S.g.X[0][c] * b[0] + S.g.X[1][c] * b[1] + S.g.X[2][c] * b[2] + S.g.X[3][c] * b[3];
+                    S.fx[lane] = rhs_value(A.rhs, x);
+                }
+            }
+            __syncwarp();
+            const int cnt = min(32, npts - base);
+            for (int q = 0; q < EPL; ++q) {
+                const int k = lane + 32 * q;
+                if (k >= NSYM) break;
+                int i, j;
+                sym_entry(NL, k, i, j);
+                double sm = accM[q], sa = accA[q], sl = accL[q];
+                for (int pp = 0; pp < cnt; ++pp) {
+                    const double w = S.w[pp];
+                    if (wantM) sm += w * (S.phi[pp][j] * S.phi[pp][i]);
+                    if (wantA || wantL) {
+                        const double d = S.sg[pp][j][0] * S.sg[pp][i][0] + S.sg[pp][j][1] * S.sg[pp][i][1] +
+                                         S.sg[pp][j][2] * S.sg[pp][i][2];
+                        sa += w * d;
+                        if (wantL) sl += w * (S.mob[pp] * d);
+                    }
+                }
+                accM[q] = sm;
+                accA[q] = sa;
+                accL[q] = sl;
+            }
+            if (wantF && lane < NL)
+                for (int pp = 0; pp < cnt; ++pp) accF += S.w[pp] * (S.fx[pp] * S.phi[pp][lane]);
+            __syncwarp();
+        }
+        if (wantC) {
+            // normal-gradient volume stabilisation on the 15-point Quad5 rule
+            if (lane < 15) {
+                double b[4];
+                for (int c = 0; c < 4; ++c) b[c] = cT.q3_node[lane][c];
+                double n[3];
+                unit_normal(S.g, b, n);
+                double phi[NL], grad[NL][3];
+                basis<P2>(S.g, b, phi, grad);
+                for (int i = 0; i < NL; ++i) S.phi[lane][i] = n[0] * grad[i][0] + n[1] * grad[i][1] + n[2] * grad[i][2];
+            }
+            __syncwarp();
+            for (int q = 0; q < EPL; ++q) {
+                const int k = lane + 32 * q;
+                if (k >= NSYM) break;
+                int i, j;
+                sym_entry(NL, k, i, j);
+                double sc = 0.;
+                for (int pp = 0; pp < 15; ++pp) sc += cT.q3_w[pp] * (S.phi[pp][j] * S.phi[pp][i]);
+                accC[q] = sc * S.g.absdet;
+            }
+            __syncwarp();
+        }
+        // write the packed element matrices
+        for (int q = 0; q < EPL; ++q) {
+            const int k = lane + 32 * q;
+            if (k >= NSYM) break;
+            if (wantM) A.elem[((int64_t)TF_FORM_M * A.n_active + r) * NSYM + k] = accM[q];
+            if (wantA) A.elem[((int64_t)TF_FORM_A * A.n_active + r) * NSYM + k] = accA[q];
+            if (wantC) A.elem[((int64_t)TF_FORM_CN * A.n_active + r) * NSYM + k] = accC[q];
+            if (wantL) A.elem[((int64_t)TF_FORM_LAPM * A.n_active + r) * NSYM + k] = accL[q];
+        }
+        if (wantF && lane < NL) A.elem_rhs[r * NL + lane] = accF;
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// CSR pattern: contributions bucketed by row, sorted by (column, contribution)
+// ---------------------------------------------------------------------------
+constexpr int kRowCap = 1024;  // contributions per row handled by one warp
+
+__global__ void k_row_counts(int64_t n_active, int nl, const int32_t* __restrict__ l2g, int32_t* __restrict__ cnt) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n_active * nl;
+         q += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&cnt[l2g[q]], nl);
+}
+
+__global__ void k_bucket(int64_t n_active, int nl, const int32_t* __restrict__ l2g, const int32_t* __restrict__ start,
+                         int32_t* __restrict__ cursor, uint64_t* __restrict__ contrib) {
+    const int nl2 = nl * nl;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n_active * nl2;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = c / nl2;
+        const int ij = (int)(c - r * nl2);
+        const int i = ij / nl, j = ij - (ij / nl) * nl;
+        const int32_t row = l2g[r * nl + i], col = l2g[r * nl + j];
+        const int32_t pos = start[row] + atomicAdd(&cursor[row], 1);
+        contrib[pos] = ((uint64_t)(uint32_t)col << 32) | (uint64_t)(uint32_t)c;
+    }
+}
+
+// warp per row: bitonic sort of the row's keys in shared memory, unique count
+__global__ void k_row_sort(int64_t m, const int32_t* __restrict__ start, uint64_t* __restrict__ contrib,
+                           int32_t* __restrict__ ucnt, int* __restrict__ status) {
+    __shared__ uint64_t buf[4][kRowCap];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint64_t* b = buf[wib];
+    for (int64_t row = (int64_t)blockIdx.x * 4 + wib; row < m; row += (int64_t)gridDim.x * 4) {
+        const int32_t s = start[row], n = start[row + 1] - start[row];
+        if (n > kRowCap) {
+            if (lane == 0) set_status(status, TF_ERR_CAPACITY, row);
+            continue;
+        }
+        int np = 1;
+        while (np < n) np <<= 1;
+        for (int k = lane; k < np; k += 32) b[k] = k < n ? contrib[s + k] : ~0ull;
+        __syncwarp();
+        for (int size = 2; size <= np; size <<= 1)
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int k = lane; k < np; k += 32) {
+                    const int partner = k ^ stride;
+                    if (partner > k) {
+                        const bool up = (k & size) == 0;
+                        const uint64_t a = b[k], c = b[partner];
+                        if ((a > c) == up) {
+                            b[k] = c;
+                            b[partner] = a;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        int u = 0;
+        for (int k = lane; k < n; k += 32) {
+            contrib[s + k] = b[k];
+            u += (k == 0) || ((b[k] >> 32) != (b[k - 1] >> 32));
+        }
+        for (int o = 16; o > 0; o >>= 1) u += __shfl_xor_sync(0xffffffffu, u, o);
+        if (lane == 0) ucnt[row] = u;
+        __syncwarp();
+    }
+}
+
+// warp per row: column indices, segment starts, diagonal slot
+__global__ void k_row_emit(int64_t m, const int32_t* __restrict__ start, const uint64_t* __restrict__ contrib,
+                           const int32_t* __restrict__ rowptr, int32_t* __restrict__ colind,
+                           int32_t* __restrict__ seg_start, int32_t* __restrict__ diag_slot) {
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    for (int64_t row = (int64_t)blockIdx.x * 4 + wib; row < m; row += (int64_t)gridDim.x * 4) {
+        const int32_t s = start[row], n = start[row + 1] - start[row];
+        int32_t carry = rowptr[row];
+        for (int k0 = 0; k0 < n; k0 += 32) {
+            const int k = k0 + lane;
+            int head = 0;
+            uint32_t col = 0;
+            if (k < n) {
+                col = (uint32_t)(contrib[s + k] >> 32);
+                head = (k == 0) || (col != (uint32_t)(contrib[s + k - 1] >> 32));
+            }
+            const unsigned mask = __ballot_sync(0xffffffffu, head);
+            if (head) {
+                const int32_t slot = carry + __popc(mask & ((1u << lane) - 1));
+                colind[slot] = (int32_t)col;
+                seg_start[slot] = s + k;
+                if ((int64_t)col == row) diag_slot[row] = slot;
+            }
+            carry += __popc(mask);
+        }
+    }
+}
+
+// segmented sums: vals[f][slot] = sum over the slot's contributions (tet order)
+template <int NL>
+__global__ void k_scatter(int64_t nnz, const int32_t* __restrict__ seg_start, const uint64_t* __restrict__ contrib,
+                          int64_t n_active, const double* __restrict__ elem, unsigned forms, double* v0, double* v1,
+                          double* v2, double* v3) {
+    constexpr int NSYM = NL * (NL + 1) / 2;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz; k += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t s = seg_start[k], e = seg_start[k + 1];
+        double a0 = 0., a1 = 0., a2 = 0., a3 = 0.;
+        for (int32_t p = s; p < e; ++p) {
+            const uint32_t c = (uint32_t)contrib[p];
+            const uint32_t r = c / (NL * NL);
+            const int ij = (int)(c - r * (NL * NL));
+            const int64_t idx = (int64_t)r * NSYM + sym_index(NL, ij / NL, ij % NL);
+            if (forms & 1u) a0 += elem[idx];
+            if (forms & 2u) a1 += elem[(int64_t)TF_FORM_A * n_active * NSYM + idx];
+            if (forms & 4u) a2 += elem[(int64_t)TF_FORM_CN * n_active * NSYM + idx];
+            if (forms & 8u) a3 += elem[(int64_t)TF_FORM_LAPM * n_active * NSYM + idx];
+        }
+        if (forms & 1u) v0[k] = a0;
+        if (forms & 2u) v1[k] = a1;
+        if (forms & 4u) v2[k] = a2;
+        if (forms & 8u) v3[k] = a3;
+    }
+}
+
+// load vector: the diagonal slot of a row lists exactly its (tet, i) pairs
+template <int NL>
+__global__ void k_scatter_rhs(int64_t m, const int32_t* __restrict__ diag_slot, const int32_t* __restrict__ seg_start,
+                              const uint64_t* __restrict__ contrib, const double* __restrict__ elem_rhs,
+                              double* __restrict__ rhs) {
+    for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < m; row += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t k = diag_slot[row];
+        double a = 0.;
+        for (int32_t p = seg_start[k]; p < seg_start[k + 1]; ++p) {
+            const uint32_t c = (uint32_t)contrib[p];
+            const uint32_t r = c / (NL * NL);
+            const int i = (int)(c - r * (NL * NL)) / NL;
+            a += elem_rhs[(int64_t)r * NL + i];
+        }
+        rhs[row] = a;
+    }
+}
+
+static int build_pattern(Context* c) {
+    const int nl = c->fe == TF_P2IF ? 10 : 4;
+    const int64_t na = c->n_active, m = c->n_dofs;
+    const int64_t ncontrib = na * nl * nl;
+    if (ncontrib >= INT32_MAX) return set_err(c, TF_ERR_CAPACITY, "pattern: too many contributions for 32-bit offsets");
+    TimedLaunch tl(c, TF_K_PATTERN);
+    TF_TRY(ensure(c, c->row_cursor, (size_t)m + 1));
+    TF_CUDA(c, cudaMemsetAsync(c->row_cursor.p, 0, sizeof(int32_t) * (size_t)(m + 1), c->stream));
+    k_row_counts<<<grid_for(c, na * nl), kBlock, 0, c->stream>>>(na, nl, c->loc2glo.p, c->row_cursor.p);
+    ++c->launches;
+    TF_TRY(ensure(c, c->rowptr, (size_t)m + 1));
+    int64_t total = 0;
+    // bucket starts -> rowptr buffer (temporarily)
+    TF_TRY(exclusive_scan_i32_to_i32(c, c->row_cursor.p, c->rowptr.p, m, &total));
+    TF_CUDA(c, cudaMemsetAsync(c->row_cursor.p, 0, sizeof(int32_t) * (size_t)(m + 1), c->stream));
+    TF_TRY(ensure(c, c->contrib, (size_t)ncontrib + 1));
+    k_bucket<<<grid_for(c, ncontrib), kBlock, 0, c->stream>>>(na, nl, c->loc2glo.p, c->rowptr.p, c->row_cursor.p,
+                                                              c->contrib.p);
+    ++c->launches;
+    TF_CUDA(c, cudaMemsetAsync(c->status.p, 0, 4 * sizeof(int), c->stream));
+    // unique counts into row_cursor
+    k_row_sort<<<grid_for(c, m, 128, 16), 128, 0, c->stream>>>(m, c->rowptr.p, c->contrib.p, c->row_cursor.p,
+                                                                 c->status.p);
+    ++c->launches;
+    TF_CUDA(c, cudaGetLastError());
+    int st = 0;
+    TF_TRY(sync_status(c, &st));
+    if (st) return set_err(c, st, "pattern: a matrix row has more than 1024 element contributions");
+    // keep bucket starts in seg_start's tail? copy them to a separate array
+    DBuf<int32_t> bstart;
+    TF_TRY(ensure(c, bstart, (size_t)m + 1));
+    TF_CUDA(c, cudaMemcpyAsync(bstart.p, c->rowptr.p, sizeof(int32_t) * (size_t)(m + 1), cudaMemcpyDeviceToDevice,
+                               c->stream));
+    int64_t nnz = 0;
+    TF_TRY(exclusive_scan_i32_to_i32(c, c->row_cursor.p, c->rowptr.p, m, &nnz));
+    TF_TRY(ensure(c, c->colind, (size_t)(nnz > 0 ? nnz : 1)));
+    TF_TRY(ensure(c, c->seg_start, (size_t)nnz + 1));
+    TF_TRY(ensure(c, c->diag_slot, (size_t)(m > 0 ? m : 1)));
+    k_row_emit<<<grid_for(c, m, 128, 16), 128, 0, c->stream>>>(m, bstart.p, c->contrib.p, c->rowptr.p, c->colind.p,
+                                                                 c->seg_start.p, c->diag_slot.p);
+    ++c->launches;
+    int32_t tot32 = (int32_t)ncontrib;
+    TF_CUDA(c, cudaMemcpyAsync(c->seg_start.p + nnz, &tot32, sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    release(bstart);
+    TF_CUDA(c, cudaGetLastError());
+    for (int f = 0; f < TF_NUM_FORMS; ++f) {
+        CSR& A = c->mats[f];
+        A.m = m;
+        A.nnz = nnz;
+        A.rowptr = c->rowptr.p;
+        A.colind = c->colind.p;
+        ++A.version;
+    }
+    c->pattern_dof_version = c->dof_version;
+    return TF_OK;
+}
+
+int setup_fe_system(Context* c, unsigned forms, int rhs_kind, const double* rhs_par, int npar) {
+    if (!c->fe) return set_err(c, TF_ERR_BAD_INPUT, "setup_fe_system: distribute DOFs first");
+    if (forms == 0 && rhs_kind == TF_RHS_NONE) return TF_OK;
+    if (forms & ~0xFu) return set_err(c, TF_ERR_BAD_INPUT, "setup_fe_system: unknown form bits");
+    const bool p2 = c->fe == TF_P2IF;
+    if (p2 && (forms & (1u << TF_FORM_LAPM)))
+        return set_err(c, TF_ERR_BAD_INPUT, "setup_fe_system: LaplaceM is a P1 form");
+    TF_TRY(ensure_tables(c));
+    const int nl = p2 ? 10 : 4, nsym = nl * (nl + 1) / 2;
+    const int64_t na = c->n_active, m = c->n_dofs;
+    if (c->pattern_dof_version != c->dof_version) TF_TRY(build_pattern(c));
+    RhsPar R{};
+    R.kind = rhs_kind;
+    for (int i = 0; i < npar && i < 8; ++i) R.p[i] = rhs_par[i];
+    if (rhs_kind == TF_RHS_SPHERE_XYZ && npar < 5) return set_err(c, TF_ERR_BAD_INPUT, "rhs: 5 parameters needed");
+    if (rhs_kind == TF_RHS_CONST && npar < 1) return set_err(c, TF_ERR_BAD_INPUT, "rhs: 1 parameter needed");
+    TF_TRY(ensure(c, c->elem, (size_t)TF_NUM_FORMS * (size_t)(na > 0 ? na : 1) * nsym));
+    TF_TRY(ensure(c, c->elem_rhs, (size_t)(na > 0 ? na : 1) * nl));
+    const double* chi = nullptr;
+    if (forms & (1u << TF_FORM_LAPM)) {
+        if (c->vecs[TF_VEC_CHI].n == (size_t)m && m > 0) chi = c->vecs[TF_VEC_CHI].p;
+    }
+    AsmArgs A{c->mesh, c->ls_vert.p, c->ls_edge.p, na, c->active.p, c->loc2glo.p, forms, R, chi, chi ? 1 : 0,
+              c->elem.p, c->elem_rhs.p, c->status.p};
+    TF_CUDA(c, cudaMemsetAsync(c->status.p, 0, 4 * sizeof(int), c->stream));
+    if (na > 0) {
+        TimedLaunch tl(c, TF_K_ASSEMBLE);
+        const int blocks = grid_for(c, (na + kAsmWarps - 1) / kAsmWarps, 1, 8);
+        if (p2) {
+            const size_t sm = sizeof(AsmSmem<10>) * kAsmWarps;
+            TF_CUDA(c, cudaFuncSetAttribute(k_assemble<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            k_assemble<10><<<blocks, 32 * kAsmWarps, sm, c->stream>>>(A);
+        } else {
+            const size_t sm = sizeof(AsmSmem<4>) * kAsmWarps;
+            TF_CUDA(c, cudaFuncSetAttribute(k_assemble<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            k_assemble<4><<<blocks, 32 * kAsmWarps, sm, c->stream>>>(A);
+        }
+        ++c->launches;
+        TF_CUDA(c, cudaGetLastError());
+    }
+    int st = 0;
+    TF_TRY(sync_status(c, &st));
+    if (st == TF_ERR_ZERO_PATTERN)
+        return set_err(c, st, "RefPatchCL::instance: found a full body in the zero level set, grid is too coarse");
+    if (st) return set_err(c, st, "assembly failed");
+    // values
+    double* v[4] = {nullptr, nullptr, nullptr, nullptr};
+    const int64_t nnz = c->mats[0].nnz;
+    for (int f = 0; f < TF_NUM_FORMS; ++f) {
+        if (!(forms & (1u << f))) continue;
+        TF_TRY(ensure(c, c->mat_vals[f], (size_t)(nnz > 0 ? nnz : 1)));
+        c->mats[f].vals = c->mat_vals[f].p;
+        ++c->mats[f].version;
+        v[f] = c->mats[f].vals;
+    }
+    if (nnz > 0) {
+        TimedLaunch tl(c, TF_K_SCATTER);
+        if (p2)
+            k_scatter<10><<<grid_for(c, nnz), kBlock, 0, c->stream>>>(nnz, c->seg_start.p, c->contrib.p, na, c->elem.p,
+                                                                       forms, v[0], v[1], v[2], v[3]);
+        else
+            k_scatter<4><<<grid_for(c, nnz), kBlock, 0, c->stream>>>(nnz, c->seg_start.p, c->contrib.p, na, c->elem.p,
+                                                                      forms, v[0], v[1], v[2], v[3]);
+        ++c->launches;
+        if (rhs_kind != TF_RHS_NONE) {
+            TF_TRY(ensure(c, c->vecs[TF_VEC_RHS], (size_t)m));
+            if (p2)
+                k_scatter_rhs<10><<<grid_for(c, m), kBlock, 0, c->stream>>>(m, c->diag_slot.p, c->seg_start.p, c->contrib.p,
+                                                                             c->elem_rhs.p, c->vecs[TF_VEC_RHS].p);
+            else
+                k_scatter_rhs<4><<<grid_for(c, m), kBlock, 0, c->stream>>>(m, c->diag_slot.p, c->seg_start.p, c->contrib.p,
+                                                                            c->elem_rhs.p, c->vecs[TF_VEC_RHS].p);
+            ++c->launches;
+        }
+        TF_CUDA(c, cudaGetLastError());
+    }
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TF_OK;
+}
+
+int numb_on_interface_p1(Context* c, double omit_bound) {
+    (void)omit_bound;
+    return set_err(c, TF_ERR_BAD_INPUT, "legacy numbering: not available in this build");
+}
+
+}  // namespace tf

@@ -1,0 +1,533 @@
+// extern "C" entry points of libtracefem (include/tracefem.h).
+#include <cstring>
+
+#include "tf_internal.cuh"
+
+using tf::Context;
+
+struct tf_context {
+    Context c;
+};
+
+#define CTX_CHECK(ctx)                       \
+    do {                                     \
+        if (!(ctx)) return TF_ERR_BAD_INPUT; \
+    } while (0)
+
+static int vec_need(Context* c, int vec) {
+    if (vec < 0 || vec >= TF_NUM_VECS) return tf::set_err(c, TF_ERR_BAD_INPUT, "bad vector handle");
+    return TF_OK;
+}
+static int mat_need(Context* c, int mat) {
+    if (mat < 0 || mat >= TF_NUM_MATS) return tf::set_err(c, TF_ERR_BAD_INPUT, "bad matrix handle");
+    if (!c->mats[mat].vals) return tf::set_err(c, TF_ERR_BAD_INPUT, "matrix handle holds no matrix");
+    return TF_OK;
+}
+
+extern "C" {
+
+const char* tf_status_string(int s) {
+    switch (s) {
+        case TF_OK: return "ok";
+        case TF_ERR_CUDA: return "CUDA runtime error";
+        case TF_ERR_ZERO_NODE: return "level set exactly zero at a node of a cut tet";
+        case TF_ERR_ZERO_PATTERN: return "all-zero sign pattern on a lattice sub-tet";
+        case TF_ERR_BAD_INPUT: return "bad input";
+        case TF_ERR_NOT_CONVERGED: return "solver did not converge";
+        case TF_ERR_CAPACITY: return "capacity exceeded";
+        case TF_ERR_WATCHDOG: return "device wait watchdog fired";
+        case TF_ERR_NO_DEVICE: return "no usable CUDA device";
+    }
+    return "unknown status";
+}
+
+int tf_create(tf_context** out, int device) {
+    if (!out) return TF_ERR_BAD_INPUT;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0) return TF_ERR_NO_DEVICE;
+    if (cudaSetDevice(device) != cudaSuccess) return TF_ERR_NO_DEVICE;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return TF_ERR_NO_DEVICE;
+    if (prop.major * 10 + prop.minor < 100) return TF_ERR_NO_DEVICE;  // built for sm_103a only
+    tf_context* t = new tf_context();
+    Context* c = &t->c;
+    c->device = device;
+    c->num_sms = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
+        cudaMallocHost((void**)&c->h_status, 4 * sizeof(int)) != cudaSuccess ||
+        tf::ensure(c, c->status, 4) != TF_OK) {
+        delete t;
+        return TF_ERR_CUDA;
+    }
+    cudaMemset(c->status.p, 0, 4 * sizeof(int));
+    // the module must hold code for this device: a first kernel launch tells
+    if (tf::ensure_tables(c) != TF_OK || cudaDeviceSynchronize() != cudaSuccess) {
+        delete t;
+        return TF_ERR_NO_DEVICE;
+    }
+    *out = t;
+    return TF_OK;
+}
+
+int tf_destroy(tf_context* t) {
+    if (!t) return TF_OK;
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    tf::release(c->coords);
+    tf::release(c->tet_v);
+    tf::release(c->tet_e);
+    tf::release(c->edge_v);
+    tf::release(c->ls_vert);
+    tf::release(c->ls_edge);
+    tf::release(c->dof_vert);
+    tf::release(c->dof_edge);
+    tf::release(c->active);
+    tf::release(c->loc2glo);
+    tf::release(c->flags);
+    tf::release(c->keys_v);
+    tf::release(c->keys_e);
+    tf::release(c->owner);
+    tf::release(c->rowptr);
+    tf::release(c->colind);
+    tf::release(c->seg_start);
+    tf::release(c->row_cursor);
+    tf::release(c->diag_slot);
+    tf::release(c->contrib);
+    tf::release(c->elem);
+    tf::release(c->elem_rhs);
+    for (int i = 0; i < TF_NUM_MATS; ++i) {
+        tf::release(c->mat_vals[i]);
+        tf::release(c->mat_vals32[i]);
+        tf::release(c->mat_diag[i]);
+    }
+    tf::release(c->block_rowptr);
+    tf::release(c->block_colind);
+    tf::release(c->user_rowptr);
+    tf::release(c->user_colind);
+    for (int i = 0; i < TF_NUM_VECS; ++i) tf::release(c->vecs[i]);
+    tf::release(c->scratch);
+    tf::release(c->scan_tmp);
+    tf::release(c->status);
+    tf::release_solver_workspace(c);
+    tf::release(c->flush_buf);
+    for (auto& e : c->markers)
+        if (e) cudaEventDestroy(e);
+    if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete t;
+    return TF_OK;
+}
+
+const char* tf_last_error(const tf_context* t) { return t ? t->c.err.c_str() : "no context"; }
+void* tf_stream(tf_context* t) { return t ? (void*)t->c.stream : nullptr; }
+
+int tf_mesh_brick(tf_context* t, const double orig[3], const double e1[3], const double e2[3], const double e3[3], int n1,
+                  int n2, int n3) {
+    CTX_CHECK(t);
+    if (!orig || !e1 || !e2 || !e3) return tf::set_err(&t->c, TF_ERR_BAD_INPUT, "brick: null vector");
+    cudaSetDevice(t->c.device);
+    return tf::mesh_set_brick(&t->c, orig, e1, e2, e3, n1, n2, n3);
+}
+
+int tf_mesh_upload(tf_context* t, int64_t nv, const double* coords, int64_t nt, const int32_t* tet_v,
+                   const int32_t* tet_e, int64_t ne, const int32_t* edge_v) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (nv <= 0 || nt <= 0 || ne <= 0 || !coords || !tet_v || !tet_e || !edge_v)
+        return tf::set_err(c, TF_ERR_BAD_INPUT, "mesh_upload: sizes and arrays required");
+    if (nv > INT32_MAX || ne > INT32_MAX) return tf::set_err(c, TF_ERR_CAPACITY, "mesh_upload: 32-bit ids");
+    for (int64_t i = 0; i < 4 * nt; ++i)
+        if (tet_v[i] < 0 || tet_v[i] >= nv) return tf::set_err(c, TF_ERR_BAD_INPUT, "mesh_upload: tet vertex out of range");
+    for (int64_t i = 0; i < 6 * nt; ++i)
+        if (tet_e[i] < 0 || tet_e[i] >= ne) return tf::set_err(c, TF_ERR_BAD_INPUT, "mesh_upload: tet edge out of range");
+    for (int64_t i = 0; i < 2 * ne; ++i)
+        if (edge_v[i] < 0 || edge_v[i] >= nv) return tf::set_err(c, TF_ERR_BAD_INPUT, "mesh_upload: edge vertex out of range");
+    TF_TRY(tf::ensure(c, c->coords, (size_t)(3 * nv)));
+    TF_TRY(tf::ensure(c, c->tet_v, (size_t)(4 * nt)));
+    TF_TRY(tf::ensure(c, c->tet_e, (size_t)(6 * nt)));
+    TF_TRY(tf::ensure(c, c->edge_v, (size_t)(2 * ne)));
+    TF_CUDA(c, cudaMemcpyAsync(c->coords.p, coords, sizeof(double) * 3 * nv, cudaMemcpyHostToDevice, c->stream));
+    TF_CUDA(c, cudaMemcpyAsync(c->tet_v.p, tet_v, sizeof(int32_t) * 4 * nt, cudaMemcpyHostToDevice, c->stream));
+    TF_CUDA(c, cudaMemcpyAsync(c->tet_e.p, tet_e, sizeof(int32_t) * 6 * nt, cudaMemcpyHostToDevice, c->stream));
+    TF_CUDA(c, cudaMemcpyAsync(c->edge_v.p, edge_v, sizeof(int32_t) * 2 * ne, cudaMemcpyHostToDevice, c->stream));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    tf::MeshView& M = c->mesh;
+    M = tf::MeshView{};
+    M.explicit_mesh = 1;
+    M.nv = nv;
+    M.ne = ne;
+    M.nt = nt;
+    M.coords = c->coords.p;
+    M.tet_v = c->tet_v.p;
+    M.tet_e = c->tet_e.p;
+    M.edge_v = c->edge_v.p;
+    c->has_mesh = true;
+    c->has_ls = false;
+    c->fe = 0;
+    return TF_OK;
+}
+
+int tf_mesh_info(tf_context* t, int64_t* nv, int64_t* ne, int64_t* nt) {
+    CTX_CHECK(t);
+    if (!t->c.has_mesh) return tf::set_err(&t->c, TF_ERR_BAD_INPUT, "no mesh");
+    if (nv) *nv = t->c.mesh.nv;
+    if (ne) *ne = t->c.mesh.ne;
+    if (nt) *nt = t->c.mesh.nt;
+    return TF_OK;
+}
+
+int tf_mesh_download(tf_context* t, double* coords, int32_t* tet_v, int32_t* tet_e, int32_t* edge_v) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (!c->has_mesh) return tf::set_err(c, TF_ERR_BAD_INPUT, "no mesh");
+    const tf::MeshView& M = c->mesh;
+    double* dc = nullptr;
+    int32_t *dv = nullptr, *de = nullptr, *dev = nullptr;
+    if (coords) TF_CUDA(c, cudaMalloc((void**)&dc, sizeof(double) * 3 * M.nv));
+    if (tet_v) TF_CUDA(c, cudaMalloc((void**)&dv, sizeof(int32_t) * 4 * M.nt));
+    if (tet_e) TF_CUDA(c, cudaMalloc((void**)&de, sizeof(int32_t) * 6 * M.nt));
+    if (edge_v) TF_CUDA(c, cudaMalloc((void**)&dev, sizeof(int32_t) * 2 * M.ne));
+    int st = tf::mesh_materialise(c, dc, dv, de, dev);
+    if (st == TF_OK) {
+        if (coords) cudaMemcpyAsync(coords, dc, sizeof(double) * 3 * M.nv, cudaMemcpyDeviceToHost, c->stream);
+        if (tet_v) cudaMemcpyAsync(tet_v, dv, sizeof(int32_t) * 4 * M.nt, cudaMemcpyDeviceToHost, c->stream);
+        if (tet_e) cudaMemcpyAsync(tet_e, de, sizeof(int32_t) * 6 * M.nt, cudaMemcpyDeviceToHost, c->stream);
+        if (edge_v) cudaMemcpyAsync(edge_v, dev, sizeof(int32_t) * 2 * M.ne, cudaMemcpyDeviceToHost, c->stream);
+        if (cudaStreamSynchronize(c->stream) != cudaSuccess) st = tf::set_err(c, TF_ERR_CUDA, "mesh_download");
+    }
+    cudaFree(dc);
+    cudaFree(dv);
+    cudaFree(de);
+    cudaFree(dev);
+    return st;
+}
+
+int tf_levelset_upload(tf_context* t, const double* ls_vert, const double* ls_edge) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (!c->has_mesh || !ls_vert) return tf::set_err(c, TF_ERR_BAD_INPUT, "levelset_upload: mesh and values required");
+    TF_TRY(tf::ensure(c, c->ls_vert, (size_t)c->mesh.nv));
+    TF_TRY(tf::ensure(c, c->ls_edge, (size_t)c->mesh.ne));
+    TF_CUDA(c, cudaMemcpyAsync(c->ls_vert.p, ls_vert, sizeof(double) * c->mesh.nv, cudaMemcpyHostToDevice, c->stream));
+    if (ls_edge) {
+        TF_CUDA(c, cudaMemcpyAsync(c->ls_edge.p, ls_edge, sizeof(double) * c->mesh.ne, cudaMemcpyHostToDevice, c->stream));
+    } else {
+        TF_TRY(tf::levelset_p1_edges(c));
+    }
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->has_ls = true;
+    ++c->ls_version;
+    c->fe = 0;
+    return TF_OK;
+}
+
+int tf_levelset_analytic(tf_context* t, int kind, const double* par, int npar, int p2) {
+    CTX_CHECK(t);
+    cudaSetDevice(t->c.device);
+    TF_TRY(tf::levelset_analytic(&t->c, kind, par, npar, p2));
+    TF_CUDA(&t->c, cudaStreamSynchronize(t->c.stream));
+    return TF_OK;
+}
+
+int tf_levelset_download(tf_context* t, double* ls_vert, double* ls_edge) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (!c->has_ls) return tf::set_err(c, TF_ERR_BAD_INPUT, "no level set");
+    if (ls_vert) TF_CUDA(c, cudaMemcpyAsync(ls_vert, c->ls_vert.p, sizeof(double) * c->mesh.nv, cudaMemcpyDeviceToHost, c->stream));
+    if (ls_edge) TF_CUDA(c, cudaMemcpyAsync(ls_edge, c->ls_edge.p, sizeof(double) * c->mesh.ne, cudaMemcpyDeviceToHost, c->stream));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TF_OK;
+}
+
+int tf_distribute_dofs(tf_context* t, int fe, double dist, int64_t* n_active, int64_t* n_dofs) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    TF_TRY(tf::distribute_dofs(c, fe, dist));
+    if (n_active) *n_active = c->n_active;
+    if (n_dofs) *n_dofs = c->n_dofs;
+    return TF_OK;
+}
+
+int tf_create_numb_on_interface_p1(tf_context* t, double omit_bound, int64_t* n_active, int64_t* n_dofs) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    TF_TRY(tf::numb_on_interface_p1(c, omit_bound));
+    if (n_active) *n_active = c->n_active;
+    if (n_dofs) *n_dofs = c->n_dofs;
+    return TF_OK;
+}
+
+int tf_dofs_download(tf_context* t, int32_t* dof_vert, int32_t* dof_edge, int32_t* active_tets, int32_t* loc2glo) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (!c->fe) return tf::set_err(c, TF_ERR_BAD_INPUT, "no DOF numbering");
+    const int nl = c->fe == TF_P2IF ? 10 : 4;
+    if (dof_vert) TF_CUDA(c, cudaMemcpyAsync(dof_vert, c->dof_vert.p, sizeof(int32_t) * c->mesh.nv, cudaMemcpyDeviceToHost, c->stream));
+    if (dof_edge) {
+        if (c->fe != TF_P2IF) return tf::set_err(c, TF_ERR_BAD_INPUT, "edge DOFs exist for P2 only");
+        TF_CUDA(c, cudaMemcpyAsync(dof_edge, c->dof_edge.p, sizeof(int32_t) * c->mesh.ne, cudaMemcpyDeviceToHost, c->stream));
+    }
+    if (active_tets && c->n_active)
+        TF_CUDA(c, cudaMemcpyAsync(active_tets, c->active.p, sizeof(int32_t) * c->n_active, cudaMemcpyDeviceToHost, c->stream));
+    if (loc2glo && c->n_active)
+        TF_CUDA(c, cudaMemcpyAsync(loc2glo, c->loc2glo.p, sizeof(int32_t) * c->n_active * nl, cudaMemcpyDeviceToHost, c->stream));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TF_OK;
+}
+
+int tf_setup_fe_system(tf_context* t, unsigned forms, int rhs_kind, const double* rhs_par, int npar, int64_t* nnz) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    TF_TRY(tf::setup_fe_system(c, forms, rhs_kind, rhs_par, npar));
+    if (nnz) *nnz = c->mats[0].nnz;
+    return TF_OK;
+}
+
+int tf_matrix_info(tf_context* t, int mat, int64_t* rows, int64_t* nnz) {
+    CTX_CHECK(t);
+    TF_TRY(mat_need(&t->c, mat));
+    if (rows) *rows = t->c.mats[mat].m;
+    if (nnz) *nnz = t->c.mats[mat].nnz;
+    return TF_OK;
+}
+
+int tf_matrix_download(tf_context* t, int mat, int64_t* rowptr, int64_t* colind, double* vals) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    TF_TRY(mat_need(c, mat));
+    const tf::CSR& A = c->mats[mat];
+    std::vector<int32_t> tmp;
+    if (rowptr) {
+        tmp.resize((size_t)A.m + 1);
+        TF_CUDA(c, cudaMemcpy(tmp.data(), A.rowptr, sizeof(int32_t) * (A.m + 1), cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i <= A.m; ++i) rowptr[i] = tmp[i];
+    }
+    if (colind) {
+        tmp.resize((size_t)A.nnz);
+        TF_CUDA(c, cudaMemcpy(tmp.data(), A.colind, sizeof(int32_t) * A.nnz, cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < A.nnz; ++i) colind[i] = tmp[i];
+    }
+    if (vals) TF_CUDA(c, cudaMemcpy(vals, A.vals, sizeof(double) * A.nnz, cudaMemcpyDeviceToHost));
+    return TF_OK;
+}
+
+int tf_matrix_upload(tf_context* t, int64_t m, const int64_t* rowptr, const int64_t* colind, const double* vals) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (m <= 0 || !rowptr || !colind || !vals) return tf::set_err(c, TF_ERR_BAD_INPUT, "matrix_upload: arrays required");
+    const int64_t nnz = rowptr[m];
+    if (nnz < 0 || nnz >= INT32_MAX || m >= INT32_MAX) return tf::set_err(c, TF_ERR_CAPACITY, "matrix_upload: 32-bit indices");
+    std::vector<int32_t> rp((size_t)m + 1), ci((size_t)(nnz > 0 ? nnz : 1));
+    for (int64_t i = 0; i <= m; ++i) {
+        if (rowptr[i] < 0 || rowptr[i] > nnz || (i > 0 && rowptr[i] < rowptr[i - 1]))
+            return tf::set_err(c, TF_ERR_BAD_INPUT, "matrix_upload: rowptr not monotone");
+        rp[i] = (int32_t)rowptr[i];
+    }
+    for (int64_t k = 0; k < nnz; ++k) {
+        if (colind[k] < 0 || colind[k] >= m) return tf::set_err(c, TF_ERR_BAD_INPUT, "matrix_upload: column out of range");
+        ci[k] = (int32_t)colind[k];
+    }
+    TF_TRY(tf::ensure(c, c->user_rowptr, (size_t)m + 1));
+    TF_TRY(tf::ensure(c, c->user_colind, (size_t)(nnz > 0 ? nnz : 1)));
+    TF_TRY(tf::ensure(c, c->mat_vals[TF_MAT_USER], (size_t)(nnz > 0 ? nnz : 1)));
+    TF_CUDA(c, cudaMemcpy(c->user_rowptr.p, rp.data(), sizeof(int32_t) * (m + 1), cudaMemcpyHostToDevice));
+    TF_CUDA(c, cudaMemcpy(c->user_colind.p, ci.data(), sizeof(int32_t) * nnz, cudaMemcpyHostToDevice));
+    TF_CUDA(c, cudaMemcpy(c->mat_vals[TF_MAT_USER].p, vals, sizeof(double) * nnz, cudaMemcpyHostToDevice));
+    tf::CSR& U = c->mats[TF_MAT_USER];
+    U.m = m;
+    U.nnz = nnz;
+    U.rowptr = c->user_rowptr.p;
+    U.colind = c->user_colind.p;
+    U.vals = c->mat_vals[TF_MAT_USER].p;
+    ++U.version;
+    return TF_OK;
+}
+
+int tf_lincomb(tf_context* t, int nterms, const int* forms, const double* coeffs) {
+    CTX_CHECK(t);
+    cudaSetDevice(t->c.device);
+    TF_TRY(tf::lincomb(&t->c, nterms, forms, coeffs));
+    TF_CUDA(&t->c, cudaStreamSynchronize(t->c.stream));
+    return TF_OK;
+}
+
+int tf_ch_block(tf_context* t, double alpha, double mob, double rho, double eps2, double beta, int use_lapm) {
+    CTX_CHECK(t);
+    cudaSetDevice(t->c.device);
+    TF_TRY(tf::ch_block(&t->c, alpha, mob, rho, eps2, beta, use_lapm));
+    TF_CUDA(&t->c, cudaStreamSynchronize(t->c.stream));
+    return TF_OK;
+}
+
+int tf_vec_upload(tf_context* t, int vec, int64_t n, const double* host) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    TF_TRY(vec_need(c, vec));
+    if (n < 0 || (n > 0 && !host)) return tf::set_err(c, TF_ERR_BAD_INPUT, "vec_upload: data required");
+    TF_TRY(tf::ensure(c, c->vecs[vec], (size_t)n));
+    if (n) TF_CUDA(c, cudaMemcpyAsync(c->vecs[vec].p, host, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TF_OK;
+}
+
+int tf_vec_download(tf_context* t, int vec, double* host, int64_t n) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    TF_TRY(vec_need(c, vec));
+    if ((size_t)n != c->vecs[vec].n || (n > 0 && !host)) return tf::set_err(c, TF_ERR_BAD_INPUT, "vec_download: size mismatch");
+    if (n) TF_CUDA(c, cudaMemcpyAsync(host, c->vecs[vec].p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TF_OK;
+}
+
+int tf_vec_size(tf_context* t, int vec, int64_t* n) {
+    CTX_CHECK(t);
+    TF_TRY(vec_need(&t->c, vec));
+    if (n) *n = (int64_t)t->c.vecs[vec].n;
+    return TF_OK;
+}
+
+int tf_vec_fill(tf_context* t, int vec, int64_t n, double value) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    TF_TRY(vec_need(c, vec));
+    if (n < 0) return tf::set_err(c, TF_ERR_BAD_INPUT, "vec_fill: n < 0");
+    TF_TRY(tf::ensure(c, c->vecs[vec], (size_t)n));
+    TF_TRY(tf::fill_f64(c, c->vecs[vec].p, n, value));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TF_OK;
+}
+
+int tf_spmv(tf_context* t, int mat, int vec_x, int vec_y) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    TF_TRY(mat_need(c, mat));
+    TF_TRY(vec_need(c, vec_x));
+    TF_TRY(vec_need(c, vec_y));
+    const tf::CSR& A = c->mats[mat];
+    if ((int64_t)c->vecs[vec_x].n != A.m) return tf::set_err(c, TF_ERR_BAD_INPUT, "spmv: x has the wrong size");
+    TF_TRY(tf::ensure(c, c->vecs[vec_y], (size_t)A.m));
+    TF_TRY(tf::spmv(c, A, c->vecs[vec_x].p, c->vecs[vec_y].p));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TF_OK;
+}
+
+static int solver_vectors(Context* c, int mat, int vec_b, int vec_x) {
+    TF_TRY(mat_need(c, mat));
+    TF_TRY(vec_need(c, vec_b));
+    TF_TRY(vec_need(c, vec_x));
+    if (vec_b == vec_x) return tf::set_err(c, TF_ERR_BAD_INPUT, "solver: b and x must differ");
+    const int64_t m = c->mats[mat].m;
+    if ((int64_t)c->vecs[vec_b].n != m) return tf::set_err(c, TF_ERR_BAD_INPUT, "solver: b has the wrong size");
+    if ((int64_t)c->vecs[vec_x].n != m) {
+        // no initial guess given: start from zero like VectorCL(0., n)
+        TF_TRY(tf::ensure(c, c->vecs[vec_x], (size_t)m));
+        TF_CUDA(c, cudaMemsetAsync(c->vecs[vec_x].p, 0, sizeof(double) * m, c->stream));
+    }
+    return TF_OK;
+}
+
+int tf_pcg_jacobi(tf_context* t, int mat, int vec_b, int vec_x, int precision, int* max_iter, double* tol, int rel) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (!max_iter || !tol || *max_iter < 0) return tf::set_err(c, TF_ERR_BAD_INPUT, "pcg: max_iter and tol required");
+    if (precision != TF_PREC_FP64 && precision != TF_PREC_MIXED) return tf::set_err(c, TF_ERR_BAD_INPUT, "pcg: bad precision");
+    TF_TRY(solver_vectors(c, mat, vec_b, vec_x));
+    return tf::pcg_jacobi(c, c->mats[mat], c->vecs[vec_b].p, c->vecs[vec_x].p, precision, max_iter, tol, rel);
+}
+
+int tf_gmres_jacobi(tf_context* t, int mat, int vec_b, int vec_x, int restart, int method, int precision, int* max_iter,
+                    double* tol, int rel) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (!max_iter || !tol || *max_iter < 0 || restart < 2) return tf::set_err(c, TF_ERR_BAD_INPUT, "gmres: bad arguments");
+    if (method != 0 && method != 1) return tf::set_err(c, TF_ERR_BAD_INPUT, "gmres: method is 0 (right) or 1 (left)");
+    TF_TRY(solver_vectors(c, mat, vec_b, vec_x));
+    return tf::gmres_jacobi(c, c->mats[mat], c->vecs[vec_b].p, c->vecs[vec_x].p, restart, method, precision, max_iter,
+                            tol, rel);
+}
+
+int tf_timing_enable(tf_context* t, int on) {
+    CTX_CHECK(t);
+    t->c.timing = on != 0;
+    return TF_OK;
+}
+int tf_timing_get(tf_context* t, int kernel, double* total_ms, int64_t* launches) {
+    CTX_CHECK(t);
+    if (kernel < 0 || kernel >= TF_NUM_KERNELS) return tf::set_err(&t->c, TF_ERR_BAD_INPUT, "bad kernel id");
+    if (total_ms) *total_ms = t->c.timers[kernel].total_ms;
+    if (launches) *launches = t->c.timers[kernel].launches;
+    return TF_OK;
+}
+int tf_timing_reset(tf_context* t) {
+    CTX_CHECK(t);
+    for (auto& k : t->c.timers) k = tf::KernelTimer{};
+    return TF_OK;
+}
+int64_t tf_launch_count(tf_context* t) { return t ? t->c.launches : 0; }
+
+int tf_marker_record(tf_context* t, int slot) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    if (slot < 0 || slot >= 8) return tf::set_err(c, TF_ERR_BAD_INPUT, "marker slot 0..7");
+    if (!c->markers[slot]) TF_CUDA(c, cudaEventCreate(&c->markers[slot]));
+    TF_CUDA(c, cudaEventRecord(c->markers[slot], c->stream));
+    return TF_OK;
+}
+
+int tf_marker_elapsed(tf_context* t, int a, int b, double* ms) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    if (a < 0 || a >= 8 || b < 0 || b >= 8 || !c->markers[a] || !c->markers[b] || !ms)
+        return tf::set_err(c, TF_ERR_BAD_INPUT, "marker_elapsed: record both markers first");
+    TF_CUDA(c, cudaEventSynchronize(c->markers[b]));
+    float f = 0.f;
+    TF_CUDA(c, cudaEventElapsedTime(&f, c->markers[a], c->markers[b]));
+    *ms = f;
+    return TF_OK;
+}
+
+int tf_flush_l2(tf_context* t) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    int l2 = 0;
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c->device);
+    const size_t bytes = 2 * (size_t)(l2 > 0 ? l2 : (128 << 20));
+    TF_TRY(tf::ensure(c, c->flush_buf, bytes));
+    TF_CUDA(c, cudaMemsetAsync(c->flush_buf.p, (int)(c->launches & 0xff), bytes, c->stream));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TF_OK;
+}
+
+void* tf_host_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+    return p;
+}
+void tf_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

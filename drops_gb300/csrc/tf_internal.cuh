@@ -1,0 +1,279 @@
+// Internal declarations shared by the CUDA translation units of libtracefem.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/tracefem.h"
+
+namespace tf {
+
+// ---------------------------------------------------------------------------
+// tet-local topology (geom/topo.cpp VertOfEdgeAr, first 6 rows)
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int ev0(int e) { return e < 3 ? (e < 2 ? 0 : 1) : (e == 3 ? 0 : (e == 4 ? 1 : 2)); }
+__host__ __device__ constexpr int ev1(int e) { return e == 0 ? 1 : (e == 1 || e == 2 ? 2 : 3); }
+
+// ---------------------------------------------------------------------------
+// Mesh view: implicit Kuhn brick or explicit arrays.
+// Brick edge numbering: 7 direction classes (d3,d2,d1) in the order
+// 001,010,100,011,101,110,111; inside a class edges are numbered by the
+// brick index of their lower vertex.
+// ---------------------------------------------------------------------------
+struct MeshView {
+    int explicit_mesh;
+    int64_t nv, ne, nt;
+    // brick
+    int n1, n2, n3;
+    double orig[3], o1[3], o2[3], o3[3];
+    int64_t eoff[8];
+    // explicit arrays (device)
+    const double* coords;
+    const int32_t* tet_v;
+    const int32_t* tet_e;
+    const int32_t* edge_v;
+};
+
+__host__ __device__ inline int edir_class(int d3, int d2, int d1) {
+    // offsets (d3,d2,d1) -> class index
+    const int code = d3 * 4 + d2 * 2 + d1;  // 1,2,4,3,5,6,7
+    switch (code) {
+        case 1: return 0;
+        case 2: return 1;
+        case 4: return 2;
+        case 3: return 3;
+        case 5: return 4;
+        case 6: return 5;
+        default: return 6;
+    }
+}
+
+// Kuhn split (geom/builder.cpp:151-176): vertex offsets (i3,i2,i1) per tet type
+__host__ __device__ inline void kuhn_offset(int l, int k, int& d3, int& d2, int& d1) {
+    // k = 0: (0,0,0); k = 3: (1,1,1)
+    if (k == 0) { d3 = d2 = d1 = 0; return; }
+    if (k == 3) { d3 = d2 = d1 = 1; return; }
+    // first step axis and second step axis per tet type, (i3,i2,i1) = axis 0,1,2
+    // l=0: +i1, +i2   l=1: +i1, +i3   l=2: +i2, +i1   l=3: +i2, +i3   l=4: +i3, +i1   l=5: +i3, +i2
+    const int first[6] = {2, 2, 1, 1, 0, 0};
+    const int second[6] = {1, 0, 2, 0, 2, 1};
+    int d[3] = {0, 0, 0};
+    d[first[l]] = 1;
+    if (k == 2) d[second[l]] = 1;
+    d3 = d[0]; d2 = d[1]; d1 = d[2];
+}
+
+__host__ __device__ inline void mesh_tet(const MeshView& M, int64_t t, int32_t v[4], int32_t e[6]) {
+    if (M.explicit_mesh) {
+        for (int k = 0; k < 4; ++k) v[k] = M.tet_v[4 * t + k];
+        if (e)
+            for (int k = 0; k < 6; ++k) e[k] = M.tet_e[6 * t + k];
+        return;
+    }
+    const int64_t cube = t / 6;
+    const int l = (int)(t - cube * 6);
+    const int i1 = (int)(cube % M.n1);
+    const int64_t r = cube / M.n1;
+    const int i2 = (int)(r % M.n2);
+    const int i3 = (int)(r / M.n2);
+    int p[4][3];
+    for (int k = 0; k < 4; ++k) {
+        int d3, d2, d1;
+        kuhn_offset(l, k, d3, d2, d1);
+        p[k][0] = i3 + d3; p[k][1] = i2 + d2; p[k][2] = i1 + d1;
+        v[k] = (int32_t)(((int64_t)p[k][0] * (M.n2 + 1) + p[k][1]) * (M.n1 + 1) + p[k][2]);
+    }
+    if (e) {
+        for (int k = 0; k < 6; ++k) {
+            const int* a = p[ev0(k)];
+            const int* b = p[ev1(k)];
+            const int d3 = b[0] - a[0], d2 = b[1] - a[1], d1 = b[2] - a[2];
+            const int c = edir_class(d3, d2, d1);
+            e[k] = (int32_t)(M.eoff[c] + ((int64_t)a[0] * (M.n2 + 1 - d2) + a[1]) * (M.n1 + 1 - d1) + a[2]);
+        }
+    }
+}
+
+// Vertex coordinates; for the brick, ((orig + i1*o1) + i2*o2) + i3*o3 per
+// component with round-to-nearest products and sums (no contraction), as in
+// BrickBuilderCL::build_ser_impl.
+__device__ inline void mesh_coord(const MeshView& M, int32_t v, double x[3]) {
+    if (M.explicit_mesh) {
+        x[0] = M.coords[3 * (int64_t)v];
+        x[1] = M.coords[3 * (int64_t)v + 1];
+        x[2] = M.coords[3 * (int64_t)v + 2];
+        return;
+    }
+    const int i1 = v % (M.n1 + 1);
+    const int r = v / (M.n1 + 1);
+    const int i2 = r % (M.n2 + 1);
+    const int i3 = r / (M.n2 + 1);
+    for (int c = 0; c < 3; ++c)
+        x[c] = __dadd_rn(__dadd_rn(__dadd_rn(M.orig[c], __dmul_rn((double)i1, M.o1[c])), __dmul_rn((double)i2, M.o2[c])),
+                         __dmul_rn((double)i3, M.o3[c]));
+}
+
+// ---------------------------------------------------------------------------
+// device buffers
+// ---------------------------------------------------------------------------
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;    // elements
+    size_t cap = 0;  // capacity
+};
+
+struct CSR {
+    int64_t m = 0, nnz = 0;
+    int32_t* rowptr = nullptr;  // m+1 (device)
+    int32_t* colind = nullptr;  // nnz
+    double* vals = nullptr;     // nnz
+    float* vals32 = nullptr;    // nnz (mixed precision copy, on demand)
+    double* diag = nullptr;     // m (Jacobi)
+    bool own_pattern = false;
+    int64_t version = 0;        // bumps whenever values change
+    int64_t vals32_version = -1, diag_version = -1;
+};
+
+struct KernelTimer {
+    double total_ms = 0;
+    int64_t launches = 0;
+};
+
+struct Context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int num_sms = 0;
+    // mesh
+    MeshView mesh{};
+    bool has_mesh = false;
+    DBuf<double> coords;
+    DBuf<int32_t> tet_v, tet_e, edge_v;
+    // level set
+    DBuf<double> ls_vert, ls_edge;
+    bool has_ls = false;
+    int64_t ls_version = 0;
+    // DOFs
+    int fe = 0;  // TF_P1IF / TF_P2IF, 0 = none
+    int64_t n_active = 0, n_dofs = 0;
+    int64_t dof_version = 0;
+    DBuf<int32_t> dof_vert, dof_edge, active, loc2glo;
+    DBuf<uint8_t> flags;
+    DBuf<int32_t> keys_v, keys_e, owner;
+    // pattern
+    int64_t pattern_dof_version = -1;
+    DBuf<int32_t> rowptr, colind, seg_start, row_cursor, diag_slot;
+    DBuf<uint64_t> contrib;  // sorted (col << 32 | contribution) per row
+    DBuf<double> elem;       // packed element matrices [form][tet][nsym]
+    DBuf<double> elem_rhs;   // [tet][nl]
+    CSR mats[TF_NUM_MATS];
+    DBuf<double> mat_vals[TF_NUM_MATS];
+    DBuf<int32_t> block_rowptr, block_colind, user_rowptr, user_colind;
+    DBuf<float> mat_vals32[TF_NUM_MATS];
+    DBuf<double> mat_diag[TF_NUM_MATS];
+    DBuf<double> vecs[TF_NUM_VECS];
+    // Krylov workspaces
+    DBuf<double> kry64, kry_part, kry_resid;
+    DBuf<float> kry32;
+    DBuf<unsigned> kry_bar;
+    DBuf<int> kry_iters;
+    // scratch
+    DBuf<unsigned char> scratch;
+    DBuf<int64_t> scan_tmp;
+    DBuf<int> status;  // device status word(s)
+    int* h_status = nullptr;  // pinned
+    // timing
+    bool timing = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t markers[8] = {};
+    DBuf<unsigned char> flush_buf;
+    KernelTimer timers[TF_NUM_KERNELS];
+    int64_t launches = 0;
+};
+
+// ---------------------------------------------------------------------------
+// error handling helpers (host)
+// ---------------------------------------------------------------------------
+int set_err(Context* c, int code, const std::string& msg);
+#define TF_CUDA(ctx, call)                                                                          \
+    do {                                                                                            \
+        cudaError_t e__ = (call);                                                                   \
+        if (e__ != cudaSuccess)                                                                     \
+            return ::tf::set_err((ctx), TF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e__)); \
+    } while (0)
+#define TF_TRY(expr)             \
+    do {                         \
+        int s__ = (expr);        \
+        if (s__ != TF_OK) return s__; \
+    } while (0)
+
+template <class T>
+int ensure(Context* c, DBuf<T>& b, size_t n) {
+    if (b.cap < n) {
+        if (b.p) cudaFree(b.p);
+        b.p = nullptr;
+        b.cap = 0;
+        size_t bytes = (n > 0 ? n : 1) * sizeof(T);
+        cudaError_t e = cudaMalloc((void**)&b.p, bytes);
+        if (e != cudaSuccess) return set_err(c, TF_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        b.cap = n > 0 ? n : 1;
+    }
+    b.n = n;
+    return TF_OK;
+}
+template <class T>
+void release(DBuf<T>& b) {
+    if (b.p) cudaFree(b.p);
+    b = DBuf<T>();
+}
+
+// kernel timing around one launch (events on the context stream)
+struct TimedLaunch {
+    Context* c;
+    int k;
+    TimedLaunch(Context* ctx, int kernel);
+    ~TimedLaunch();
+};
+
+// device-wide exclusive scan of int32 counts -> int64 offsets (out[n] = total)
+int exclusive_scan_i32(Context* c, const int32_t* in, int64_t* out, int64_t n);
+int exclusive_scan_i32_to_i32(Context* c, const int32_t* in, int32_t* out, int64_t n, int64_t* total);
+int sync_status(Context* c, int* status_out);
+int fill_f64(Context* c, double* p, int64_t n, double v);
+
+// sub-module entry points (host)
+int mesh_materialise(Context* c, double* coords, int32_t* tet_v, int32_t* tet_e, int32_t* edge_v);
+int ensure_tables(Context* c);
+int patch_dump(Context* c, int64_t first, int64_t count, int32_t* nf, int32_t* facets, int32_t* bnd, int32_t* nverts,
+               double* verts);
+int mesh_set_brick(Context* c, const double orig[3], const double e1[3], const double e2[3], const double e3[3],
+                   int n1, int n2, int n3);
+int levelset_analytic(Context* c, int kind, const double* par, int npar, int p2);
+int levelset_p1_edges(Context* c);
+int distribute_dofs(Context* c, int fe, double dist);
+int numb_on_interface_p1(Context* c, double omit_bound);
+int setup_fe_system(Context* c, unsigned forms, int rhs_kind, const double* rhs_par, int npar);
+int lincomb(Context* c, int nterms, const int* forms, const double* coeffs);
+int ch_block(Context* c, double alpha, double mob, double rho, double eps2, double beta, int use_lapm);
+int spmv(Context* c, const CSR& A, const double* x, double* y);
+int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, int* max_iter, double* tol, int rel);
+int gmres_jacobi(Context* c, CSR& A, const double* b, double* x, int restart, int method, int precision,
+                 int* max_iter, double* tol, int rel);
+int ensure_diag(Context* c, CSR& A);
+void release_solver_workspace(Context* c);
+int ensure_vals32(Context* c, CSR& A);
+
+constexpr int kBlock = 256;
+inline int grid_for(Context* c, int64_t n, int block = kBlock, int per_sm = 8) {
+    int64_t g = (n + block - 1) / block;
+    int64_t cap = (int64_t)c->num_sms * per_sm;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+}  // namespace tf

@@ -1,0 +1,226 @@
+/*
+ * tracefem.h -- C ABI of the GB300 (sm_103a) TraceFEM path.
+ *
+ * Drop-in boundary for the TraceFEM surface-PDE path of DROPS: interface DOF
+ * numbering, surface-patch quadrature assembly of the local forms into CSR
+ * matrices, and the Jacobi-preconditioned PCG / GMRES solves.  Every entry
+ * point takes plain pointers and sizes; all device memory is owned by the
+ * context.  Host arrays passed in are copied; host arrays passed out are
+ * filled by the call.  One context per host thread; calls on one context are
+ * ordered on the context's stream and return after their results are ready.
+ *
+ * Numbering conventions (identical to the reference's):
+ *   - tet local vertices 0..3, local edges 0..5 = (0,1),(0,2),(1,2),(0,3),(1,3),(2,3)
+ *     (geom/topo.cpp VertOfEdgeAr);
+ *   - a P2 level set is given by one value per vertex and one per edge
+ *     (the P2 VecDescCL of the reference, split by simplex);
+ *   - local DOF order of a P2 tet: 4 vertices, then 6 edges (IdxDescCL::Loc2Glo,
+ *     misc/problem.h:314-331).
+ *
+ * Every function returns TF_OK (0) or one of the TF_ERR_* codes below; the
+ * message of the last failure is available from tf_last_error().
+ */
+#ifndef TRACEFEM_H
+#define TRACEFEM_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define TF_OK 0
+#define TF_ERR_CUDA 1          /* a CUDA runtime call failed                                     */
+#define TF_ERR_ZERO_NODE 2     /* level set exactly 0 at a node of a cut tet: distance() throws  */
+                               /* std::invalid_argument (geom/subtriangulation.tpp:43-44)        */
+#define TF_ERR_ZERO_PATTERN 3  /* all-zero sign pattern on a lattice sub-tet: RefPatchCL::instance */
+                               /* throws DROPSErrCL (geom/reftetracut.h:152-153)                  */
+#define TF_ERR_BAD_INPUT 4     /* null/inconsistent arguments, call out of order                 */
+#define TF_ERR_NOT_CONVERGED 5 /* Krylov solve hit max_iter: the reference returns false         */
+#define TF_ERR_CAPACITY 6      /* a fixed per-row / per-tet capacity was exceeded                */
+#define TF_ERR_WATCHDOG 7      /* a device-side wait gave up (bounded spin); context stays usable */
+#define TF_ERR_NO_DEVICE 8     /* no CUDA device, or the library was not built for it            */
+
+/* ---- finite elements, forms, level sets -------------------------------- */
+#define TF_P1IF 1 /* P1IF_FE (misc/problem.h:73) */
+#define TF_P2IF 2 /* P2IF_FE (misc/problem.h:75) */
+
+/* matrix handles: the bilinear forms of LocalAssembler (surfactant/ifacetransp.h) */
+#define TF_FORM_M 0      /* M_P1P1 :1568 / M_P2P2 :1579                                  */
+#define TF_FORM_A 1      /* A_P1P1 :1522 / P2 surface-gradient Laplace-Beltrami           */
+#define TF_FORM_CN 2     /* C_n_P1P1 :1545 / diagonal blocks of C_n_vecP2vecP2 :1458      */
+#define TF_FORM_LAPM 3   /* LaplaceM_P1P1 :1533 (mobility chi(1-chi), cut off at 0)       */
+#define TF_NUM_FORMS 4
+#define TF_MAT_SYS 4     /* linear combination of forms (tf_lincomb), same pattern       */
+#define TF_MAT_BLOCK 5   /* 2x2 Cahn-Hilliard block matrix (tf_ch_block), 2m rows        */
+#define TF_MAT_USER 6    /* matrix uploaded with tf_matrix_upload                         */
+#define TF_NUM_MATS 7
+
+/* vector handles (device vectors owned by the context) */
+#define TF_VEC_RHS 0 /* assembled load vector (F_concentration_P1 :1610 or its P2 analogue) */
+#define TF_VEC_X 1
+#define TF_VEC_B 2
+#define TF_VEC_CHI 3 /* P1 concentration used by TF_FORM_LAPM                              */
+#define TF_VEC_T0 4
+#define TF_VEC_T1 5
+#define TF_VEC_T2 6
+#define TF_VEC_T3 7
+#define TF_NUM_VECS 8
+
+/* analytic level sets (surfactant/Surface.hpp) */
+#define TF_LS_SPHERE 0    /* par: cx,cy,cz,r         phi = |x-c| - r            (Sphere::dist :71)  */
+#define TF_LS_TORUS 1     /* par: R,r,axis           phi = |(rho-R, x_axis)| - r (Torus::dist :130)  */
+#define TF_LS_ELLIPSOID 2 /* par: cx,cy,cz,a,b,c,Q[9] phi = |diag(1/a,1/b,1/c) Q^T (x-c)| - 1          */
+#define TF_LS_PLANE 3     /* par: nx,ny,nz,d         phi = n.x - d                                   */
+
+/* load-vector integrands f(x) for TF_VEC_RHS */
+#define TF_RHS_NONE 0
+#define TF_RHS_SPHERE_XYZ 1 /* par: cx,cy,cz,r,c: f = c*y0*y1*y2, y = ext(x) on the sphere (Surface::ext) */
+#define TF_RHS_CONST 2      /* par: c */
+
+#define TF_PREC_FP64 0  /* every Krylov operation in FP64                               */
+#define TF_PREC_MIXED 1 /* FP32 inner Krylov iterations inside FP64 iterative refinement */
+
+typedef struct tf_context tf_context;
+
+/* ---- context ------------------------------------------------------------ */
+/* Creates a context on CUDA device `device`.  Replaces nothing in the
+ * reference (which has no device state); it owns all device memory.        */
+int tf_create(tf_context** ctx, int device);
+int tf_destroy(tf_context* ctx);
+const char* tf_last_error(const tf_context* ctx);
+const char* tf_status_string(int status);
+/* The context's CUDA stream (a cudaStream_t), for callers that time or order
+ * their own work against the library's.                                      */
+void* tf_stream(tf_context* ctx);
+
+/* ---- mesh: one triangulation level of MultiGridCL ------------------------- */
+/* BrickBuilderCL(orig, e1, e2, e3, n1, n2, n3) (geom/builder.cpp:99-180): the
+ * mesh is kept implicit on the device (vertex / tet / edge numbers follow from
+ * the brick indices); vertex coordinates and tet order are the reference's,
+ * bit for bit.  Edges are numbered by direction class, see tf_mesh_download. */
+int tf_mesh_brick(tf_context* ctx, const double orig[3], const double e1[3], const double e2[3],
+                  const double e3[3], int n1, int n2, int n3);
+/* A general tetrahedral mesh given as flat arrays (what a MultiGridCL level
+ * flattens to): coords[3*nv], tet_v[4*nt], tet_e[6*nt] (edge ids, local edge
+ * order above), edge_v[2*ne].  Copied to the device.                         */
+int tf_mesh_upload(tf_context* ctx, int64_t nv, const double* coords, int64_t nt, const int32_t* tet_v,
+                   const int32_t* tet_e, int64_t ne, const int32_t* edge_v);
+int tf_mesh_info(tf_context* ctx, int64_t* nv, int64_t* ne, int64_t* nt);
+/* Materialises the mesh arrays on the host (any pointer may be NULL). */
+int tf_mesh_download(tf_context* ctx, double* coords, int32_t* tet_v, int32_t* tet_e, int32_t* edge_v);
+
+/* ---- level set: the P2 VecDescCL LocalAssemblerParams::levelSet ------------ */
+/* Host values per vertex and per edge.  ls_edge == NULL gives the
+ * P1-interpolated level set, edge = 0.5*(a+b) (LinearLSInit,
+ * surfactant/surfactant.cpp:733-745).                                          */
+int tf_levelset_upload(tf_context* ctx, const double* ls_vert, const double* ls_edge);
+/* Analytic level set evaluated on the device at the vertices and, for p2 != 0,
+ * at the edge midpoints 0.5*(x0+x1) (LSInit / VecDescCL::Interpolate); p2 == 0
+ * gives edge = 0.5*(a+b).  Values equal the host evaluation bit for bit.       */
+int tf_levelset_analytic(tf_context* ctx, int kind, const double* par, int npar, int p2);
+int tf_levelset_download(tf_context* ctx, double* ls_vert, double* ls_edge);
+
+/* ---- interface DOFs -------------------------------------------------------- */
+/* IdxDescCL::DistributeDOFs(level, mg, &levelSet, dist) (misc/problem.cpp:283-336):
+ * a tet is active iff distance(its 10 level-set values) <= dist; DOFs are
+ * numbered in first-touch order over active tets in triangulation order,
+ * vertices 0..3 then (P2) edges 0..5.  Returns the number of active tets like
+ * the reference; TF_ERR_ZERO_NODE where distance() throws.                    */
+int tf_distribute_dofs(tf_context* ctx, int fe, double dist, int64_t* n_active, int64_t* n_dofs);
+/* IdxDescCL::CreateNumbering for P1IF_FE -> CreateNumbOnInterfaceVertex
+ * (misc/problem.cpp:443-505, legacy path): a vertex is a DOF iff the Quad2
+ * integral of lambda_i^2 over the patch exceeds omit_bound*(6|T|)^(4/3).      */
+int tf_create_numb_on_interface_p1(tf_context* ctx, double omit_bound, int64_t* n_active, int64_t* n_dofs);
+/* dof_vert[nv], dof_edge[ne] (-1 = no DOF), active_tets[n_active], loc2glo[n_active*nloc]
+ * (IdxDescCL::Loc2Glo per active tet); any pointer may be NULL.                 */
+int tf_dofs_download(tf_context* ctx, int32_t* dof_vert, int32_t* dof_edge, int32_t* active_tets,
+                     int32_t* loc2glo);
+
+/* ---- assembly ---------------------------------------------------------------- */
+/* setupFESystem(mg, FESystem&) (surfactant/ifacetransp.cpp:566-622): for every
+ * active tet, the patch of the level set on the order-2 principal lattice
+ * (SPatchCL::make_patch<MergeCutPolicyCL>, geom/subtriangulation.tpp:191-228),
+ * Quad5_2D on every facet (make_CompositeQuad5Domain2D, num/quadrature.tpp:265-332)
+ * and Quad5 on the tet; the local forms of `forms` (bit mask over TF_FORM_*)
+ * and, when rhs_kind != TF_RHS_NONE, the load vector into TF_VEC_RHS.  The CSR
+ * pattern is the union of the active-tet blocks, rows sorted by column
+ * (SparseMatBuilderCL::Build, num/spmat.h:620-678); values are summed in
+ * triangulation order.  The pattern is kept and reused while the DOF
+ * numbering is unchanged.                                                       */
+int tf_setup_fe_system(tf_context* ctx, unsigned forms, int rhs_kind, const double* rhs_par, int npar,
+                       int64_t* nnz);
+/* Pattern and values of a matrix handle (rowptr[m+1] as size_t-compatible
+ * int64, colind[nnz], vals[nnz]; any pointer may be NULL).                      */
+int tf_matrix_info(tf_context* ctx, int mat, int64_t* rows, int64_t* nnz);
+int tf_matrix_download(tf_context* ctx, int mat, int64_t* rowptr, int64_t* colind, double* vals);
+/* A host CSR matrix (MatrixCL: size_t row/col, double values) as TF_MAT_USER. */
+int tf_matrix_upload(tf_context* ctx, int64_t m, const int64_t* rowptr, const int64_t* colind,
+                     const double* vals);
+/* MatrixCL LinComb ctor (num/spmat.h:712-715) on the shared pattern:
+ * TF_MAT_SYS = sum_k coeffs[k] * forms[k].                                      */
+int tf_lincomb(tf_context* ctx, int nterms, const int* forms, const double* coeffs);
+/* The Cahn-Hilliard block matrix of surfphasesep/surfphasesep.cpp:431-434 as
+ * TF_MAT_BLOCK: [[alpha M, mob A + rho C], [eps2 A + beta M + eps2 rho C, -M]],
+ * A = TF_FORM_LAPM when use_lapm else TF_FORM_A.                              */
+int tf_ch_block(tf_context* ctx, double alpha, double mob, double rho, double eps2, double beta, int use_lapm);
+
+/* ---- vectors ----------------------------------------------------------------- */
+int tf_vec_upload(tf_context* ctx, int vec, int64_t n, const double* host);
+int tf_vec_download(tf_context* ctx, int vec, double* host, int64_t n);
+int tf_vec_size(tf_context* ctx, int vec, int64_t* n);
+/* Sets vector `vec` to n copies of `value` on the device (e.g. a zero initial guess). */
+int tf_vec_fill(tf_context* ctx, int vec, int64_t n, double value);
+/* y = A x on device vectors (y_Ax, num/spmat.h:1684-1709). */
+int tf_spmv(tf_context* ctx, int mat, int vec_x, int vec_y);
+
+/* ---- solvers ------------------------------------------------------------------- */
+/* PCGSolverCL<JACPcCL>(pc, max_iter, tol, rel).Solve(A, x, b) (num/krylovsolver.h:
+ * 107-189, 1805-1836; Jacobi SolveGSstep<PB_JAC0>, num/precond.h:153-169):
+ * x (vec_x) is the initial guess and the result; max_iter and tol are in/out
+ * (used iterations / reached residual).  TF_PREC_MIXED runs FP32 PCG sweeps
+ * inside FP64 iterative refinement with the same stopping test on the FP64
+ * residual.  Returns TF_ERR_NOT_CONVERGED where the reference returns false.  */
+int tf_pcg_jacobi(tf_context* ctx, int mat, int vec_b, int vec_x, int precision, int* max_iter, double* tol,
+                  int rel);
+/* GMResSolverCL / GMRES (num/krylovsolver.h:320-463, 1924-1975): restarted
+ * GMRES(restart) with modified Gram-Schmidt and Givens rotations, Jacobi
+ * preconditioning of the diagonal (for TF_MAT_BLOCK: of both diagonal blocks),
+ * method 0 = right, 1 = left preconditioning.                                 */
+int tf_gmres_jacobi(tf_context* ctx, int mat, int vec_b, int vec_x, int restart, int method, int precision,
+                    int* max_iter, double* tol, int rel);
+
+/* ---- instrumentation -------------------------------------------------------------- */
+/* Per-kernel device time, recorded with CUDA events on the context's stream
+ * while enabled; kernel ids are the TF_K_* below.                                  */
+#define TF_K_CLASSIFY 0
+#define TF_K_NUMBER 1
+#define TF_K_ASSEMBLE 2
+#define TF_K_PATTERN 3
+#define TF_K_SCATTER 4
+#define TF_K_SPMV 5
+#define TF_K_PCG 6
+#define TF_K_GMRES 7
+#define TF_K_LEVELSET 8
+#define TF_NUM_KERNELS 9
+int tf_timing_enable(tf_context* ctx, int on);
+int tf_timing_get(tf_context* ctx, int kernel, double* total_ms, int64_t* launches);
+int tf_timing_reset(tf_context* ctx);
+/* number of kernels this library launched on the context since creation */
+int64_t tf_launch_count(tf_context* ctx);
+/* CUDA events on the context's stream: record marker `slot` (0..7) and read
+ * the elapsed device time between two recorded markers.                     */
+int tf_marker_record(tf_context* ctx, int slot);
+int tf_marker_elapsed(tf_context* ctx, int slot_a, int slot_b, double* ms);
+/* Overwrites a scratch buffer of twice the L2 size on the context's stream,
+ * so that the next call starts with a cold L2.                               */
+int tf_flush_l2(tf_context* ctx);
+/* Page-locked host memory for callers that stage inputs/outputs (NULL on failure). */
+void* tf_host_alloc(size_t bytes);
+void tf_host_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
