@@ -41,7 +41,7 @@ EXPORTS = [
     "tf_mesh_info", "tf_mesh_download", "tf_levelset_upload", "tf_levelset_analytic", "tf_levelset_download",
     "tf_distribute_dofs", "tf_create_numb_on_interface_p1", "tf_dofs_download", "tf_setup_fe_system",
     "tf_matrix_info", "tf_matrix_download", "tf_matrix_upload", "tf_lincomb", "tf_ch_block", "tf_vec_upload",
-    "tf_vec_download", "tf_vec_size", "tf_vec_fill", "tf_spmv", "tf_pcg_jacobi", "tf_gmres_jacobi", "tf_timing_enable",
+    "tf_vec_download", "tf_vec_size", "tf_vec_fill", "tf_spmv", "tf_pcg_jacobi", "tf_gmres_jacobi", "tf_ch_steps", "tf_timing_enable",
     "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2",
     "tf_host_alloc", "tf_host_free",
 ]
@@ -264,6 +264,19 @@ class TraceFEM:
         if check and st not in (OK, ERR_NOT_CONVERGED):
             self._check(st)
         return st, it.value, t.value
+
+    def ch_steps(self, nsteps, dt, mobility, eps, beta_s, xi, rho_vol, restart=50, tol=1e-10, max_iter=100000,
+                 warm=True, check=True):
+        """Cahn-Hilliard BDF1 steps (tf_ch_steps); returns (status, iterations[], residuals[])."""
+        its = np.zeros(max(nsteps, 1), np.int32)
+        res = np.zeros(max(nsteps, 1))
+        st = self.L.tf_ch_steps(self.h, C.c_int(nsteps), C.c_double(dt), C.c_double(mobility), C.c_double(eps),
+                                C.c_double(beta_s), C.c_double(xi), C.c_double(rho_vol), C.c_int(restart),
+                                C.c_double(tol), C.c_int(max_iter), C.c_int(int(warm)),
+                                its.ctypes.data_as(C.POINTER(C.c_int)), _dp(res))
+        if check and st != OK:
+            self._check(st)
+        return st, its[:nsteps], res[:nsteps]
 
     # ---- instrumentation ------------------------------------------------------------------
     def timing(self, on=True):

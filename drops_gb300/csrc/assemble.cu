@@ -728,12 +728,14 @@ static int build_pattern(Context* c) {
     TF_CUDA(c, cudaStreamSynchronize(c->stream));
     release(bstart);
     TF_CUDA(c, cudaGetLastError());
+    const int64_t gen = ++c->pattern_counter;
     for (int f = 0; f < TF_NUM_FORMS; ++f) {
         CSR& A = c->mats[f];
         A.m = m;
         A.nnz = nnz;
         A.rowptr = c->rowptr.p;
         A.colind = c->colind.p;
+        A.pattern_gen = gen;
         ++A.version;
     }
     c->pattern_dof_version = c->dof_version;
@@ -742,6 +744,8 @@ static int build_pattern(Context* c) {
 
 int setup_fe_system(Context* c, unsigned forms, int rhs_kind, const double* rhs_par, int npar) {
     if (!c->fe) return set_err(c, TF_ERR_BAD_INPUT, "setup_fe_system: distribute DOFs first");
+    if (c->legacy_numbering)
+        return set_err(c, TF_ERR_BAD_INPUT, "setup_fe_system: needs a DistributeDOFs numbering, not the legacy one");
     if (forms == 0 && rhs_kind == TF_RHS_NONE) return TF_OK;
     if (forms & ~0xFu) return set_err(c, TF_ERR_BAD_INPUT, "setup_fe_system: unknown form bits");
     const bool p2 = c->fe == TF_P2IF;
@@ -820,9 +824,178 @@ int setup_fe_system(Context* c, unsigned forms, int rhs_kind, const double* rhs_
     return TF_OK;
 }
 
+__global__ void k_fill_i32_asm(int32_t* p, int64_t n, int32_t v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+__global__ void k_mark_owned_asm(int64_t n, const int32_t* __restrict__ keys, int32_t* __restrict__ owned) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (keys[i] != INT_MAX) owned[keys[i]] = 1;
+}
+__global__ void k_assign_asm(int64_t n, const int32_t* __restrict__ keys, const int32_t* __restrict__ rank,
+                             int32_t* __restrict__ dof) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dof[i] = keys[i] != INT_MAX ? rank[keys[i]] : -1;
+}
+
+// ---------------------------------------------------------------------------
+// legacy numbering: CreateNumbOnInterfaceVertex (misc/problem.cpp:443-505)
+// A vertex gets its number at the first tet (triangulation order) whose patch
+// carries a Quad2 integral of lambda_i^2 above omit_bound * (6|T|)^{4/3};
+// the key t*4 + i of that first qualifying (tet, vertex) orders the numbers.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(32 * kAsmWarps) k_legacy_touch(MeshView M, const double* __restrict__ lsv,
+                                                                const double* __restrict__ lse, int64_t n_cand,
+                                                                const int32_t* __restrict__ cand, double omit_bound,
+                                                                int32_t* __restrict__ keys, uint8_t* __restrict__ nonempty,
+                                                                int* status) {
+    __shared__ PatchSmem Ps[kAsmWarps];
+    __shared__ double Xs[kAsmWarps][4][3];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    PatchSmem& P = Ps[wib];
+    for (int64_t r = (int64_t)blockIdx.x * kAsmWarps + wib; r < n_cand; r += (int64_t)gridDim.x * kAsmWarps) {
+        const int32_t t = cand[r];
+        int32_t v[4], e[6];
+        mesh_tet(M, t, v, e);
+        double ls10[10];
+        for (int k = 0; k < 4; ++k) ls10[k] = lsv[v[k]];
+        for (int k = 0; k < 6; ++k) ls10[4 + k] = lse[e[k]];
+        if (lane < 4) {
+            double x[3];
+            mesh_coord(M, v[lane], x);
+            for (int c2 = 0; c2 < 3; ++c2) Xs[wib][lane][c2] = x[c2];
+        }
+        __syncwarp();
+        double X[4][3];
+        for (int k = 0; k < 4; ++k)
+            for (int c2 = 0; c2 < 3; ++c2) X[k][c2] = Xs[wib][k][c2];
+        const int nf = warp_patch(ls10, X, P, lane, status, t);
+        if (lane == 0) nonempty[r] = nf > 0;
+        if (nf == 0) {
+            __syncwarp();
+            continue;
+        }
+        // 6|T| = |det J|
+        double M3[3][3];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) M3[j][i] = X[i + 1][j] - X[0][j];
+        const double det = M3[0][0] * (M3[1][1] * M3[2][2] - M3[1][2] * M3[2][1]) -
+                           M3[0][1] * (M3[1][0] * M3[2][2] - M3[1][2] * M3[2][0]) +
+                           M3[0][2] * (M3[1][0] * M3[2][1] - M3[1][1] * M3[2][0]);
+        const double limit = omit_bound < 0. ? 0. : omit_bound * pow(fabs(det), 4. / 3.);
+        double acc[4] = {0, 0, 0, 0};
+        for (int p = lane; p < 4 * nf; p += 32) {
+            const int f = p >> 2, q = p & 3;
+            double b[4];
+            for (int c2 = 0; c2 < 4; ++c2)
+                b[c2] = P.fb[f][0][c2] * cT.qq2_node[q][0] + P.fb[f][1][c2] * cT.qq2_node[q][1] +
+                        P.fb[f][2][c2] * cT.qq2_node[q][2];
+            const double w = P.fw[f] * cT.qq2_w[q];
+            double h[10];
+            for (int i = 0; i < 4; ++i) h[i] = b[i] * (2. * b[i] - 1.);
+            for (int k = 0; k < 6; ++k) h[4 + k] = 4. * b[ev0(k)] * b[ev1(k)];
+            for (int i = 0; i < 4; ++i) {
+                // lambda_i^2 as a P2 function: 1 at vertex i, 1/4 on the edges at i
+                double val = 0.;
+                for (int k = 0; k < 10; ++k) {
+                    const double ck = k < 4 ? (k == i ? 1. : 0.) : ((ev0(k - 4) == i || ev1(k - 4) == i) ? 0.25 : 0.);
+                    val += ck * h[k];
+                }
+                acc[i] += w * val;
+            }
+        }
+        for (int i = 0; i < 4; ++i)
+            for (int o = 16; o > 0; o >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], o);
+        if (lane < 4 && acc[lane] > limit) atomicMin(&keys[v[lane]], (int32_t)(t * 4 + lane));
+        __syncwarp();
+    }
+}
+
+__global__ void k_legacy_active(MeshView M, int64_t n_cand, const int32_t* __restrict__ cand,
+                                const uint8_t* __restrict__ nonempty, const int32_t* __restrict__ keys,
+                                int32_t* __restrict__ act_flag) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_cand; r += (int64_t)gridDim.x * blockDim.x) {
+        int a = 0;
+        if (nonempty[r]) {
+            const int32_t t = cand[r];
+            int32_t v[4];
+            mesh_tet(M, t, v, nullptr);
+            for (int i = 0; i < 4; ++i) {
+                const int32_t k = keys[v[i]];
+                if (k != INT_MAX && k / 4 <= t) a = 1;
+            }
+        }
+        act_flag[r] = a;
+    }
+}
+
+int compact_active(Context* c, int64_t* n_active);
+
 int numb_on_interface_p1(Context* c, double omit_bound) {
-    (void)omit_bound;
-    return set_err(c, TF_ERR_BAD_INPUT, "legacy numbering: not available in this build");
+    if (!c->has_mesh || !c->has_ls) return set_err(c, TF_ERR_BAD_INPUT, "numbering: mesh and level set required");
+    TF_TRY(ensure_tables(c));
+    const MeshView& M = c->mesh;
+    if (M.nt * 4 >= INT_MAX) return set_err(c, TF_ERR_CAPACITY, "numbering: too many tets for 32-bit keys");
+    c->fe = 0;
+    // cut tets (distance == 0 on the lattice values) -> candidate list
+    TF_TRY(distribute_dofs(c, TF_P1IF, 0.0));
+    const int64_t n_cand = c->n_active;
+    DBuf<int32_t> cand;
+    DBuf<uint8_t> nonempty;
+    TF_TRY(ensure(c, cand, (size_t)(n_cand > 0 ? n_cand : 1)));
+    TF_TRY(ensure(c, nonempty, (size_t)(n_cand > 0 ? n_cand : 1)));
+    TF_CUDA(c, cudaMemcpyAsync(cand.p, c->active.p, sizeof(int32_t) * n_cand, cudaMemcpyDeviceToDevice, c->stream));
+    TF_TRY(ensure(c, c->keys_v, (size_t)M.nv));
+    TF_TRY(ensure(c, c->dof_vert, (size_t)M.nv));
+    k_fill_i32_asm<<<grid_for(c, M.nv), kBlock, 0, c->stream>>>(c->keys_v.p, M.nv, INT_MAX);
+    ++c->launches;
+    TF_CUDA(c, cudaMemsetAsync(c->status.p, 0, 4 * sizeof(int), c->stream));
+    if (n_cand > 0) {
+        k_legacy_touch<<<grid_for(c, (n_cand + kAsmWarps - 1) / kAsmWarps, 1, 8), 32 * kAsmWarps, 0, c->stream>>>(
+            M, c->ls_vert.p, c->ls_edge.p, n_cand, cand.p, omit_bound, c->keys_v.p, nonempty.p, c->status.p);
+        ++c->launches;
+    }
+    int st = 0;
+    TF_TRY(sync_status(c, &st));
+    if (st) {
+        release(cand);
+        release(nonempty);
+        return set_err(c, st, "legacy numbering: all-zero sign pattern on a lattice sub-tet");
+    }
+    // ranks over the key space t*4+i
+    const int64_t nkeys = M.nt * 4;
+    TF_TRY(ensure(c, c->owner, (size_t)nkeys + 1));
+    TF_CUDA(c, cudaMemsetAsync(c->owner.p, 0, sizeof(int32_t) * (size_t)(nkeys + 1), c->stream));
+    k_mark_owned_asm<<<grid_for(c, M.nv), kBlock, 0, c->stream>>>(M.nv, c->keys_v.p, c->owner.p);
+    ++c->launches;
+    DBuf<int32_t> rank;
+    TF_TRY(ensure(c, rank, (size_t)nkeys + 1));
+    int64_t ndofs = 0;
+    TF_TRY(exclusive_scan_i32_to_i32(c, c->owner.p, rank.p, nkeys, &ndofs));
+    k_assign_asm<<<grid_for(c, M.nv), kBlock, 0, c->stream>>>(M.nv, c->keys_v.p, rank.p, c->dof_vert.p);
+    ++c->launches;
+    // active tets: a cut tet with a non-empty patch that touches a numbered vertex
+    TF_TRY(ensure(c, c->scratch, (size_t)M.nt * sizeof(int32_t)));
+    TF_CUDA(c, cudaMemsetAsync(c->scratch.p, 0, sizeof(int32_t) * (size_t)M.nt, c->stream));
+    DBuf<int32_t> flag;
+    TF_TRY(ensure(c, flag, (size_t)(n_cand > 0 ? n_cand : 1)));
+    if (n_cand > 0) {
+        k_legacy_active<<<grid_for(c, n_cand), kBlock, 0, c->stream>>>(M, n_cand, cand.p, nonempty.p, c->keys_v.p, flag.p);
+        ++c->launches;
+    }
+    int64_t na = 0;
+    TF_TRY(exclusive_scan_i32_to_i32(c, flag.p, rank.p, n_cand, &na));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    TF_CUDA(c, cudaGetLastError());
+    release(cand);
+    release(nonempty);
+    release(rank);
+    release(flag);
+    c->n_active = na;
+    c->n_dofs = ndofs;
+    c->fe = TF_P1IF;
+    c->legacy_numbering = true;
+    ++c->dof_version;
+    return TF_OK;
 }
 
 }  // namespace tf

@@ -102,6 +102,11 @@ int tf_destroy(tf_context* t) {
         tf::release(c->mat_vals[i]);
         tf::release(c->mat_vals32[i]);
         tf::release(c->mat_diag[i]);
+        tf::release(c->sell_ptr[i]);
+        tf::release(c->sell_col[i]);
+        tf::release(c->sell_src[i]);
+        tf::release(c->sell_v64[i]);
+        tf::release(c->sell_v32[i]);
     }
     tf::release(c->block_rowptr);
     tf::release(c->block_colind);
@@ -354,6 +359,7 @@ int tf_matrix_upload(tf_context* t, int64_t m, const int64_t* rowptr, const int6
     U.rowptr = c->user_rowptr.p;
     U.colind = c->user_colind.p;
     U.vals = c->mat_vals[TF_MAT_USER].p;
+    U.pattern_gen = ++c->pattern_counter;
     ++U.version;
     return TF_OK;
 }
@@ -466,6 +472,15 @@ int tf_gmres_jacobi(tf_context* t, int mat, int vec_b, int vec_x, int restart, i
     TF_TRY(solver_vectors(c, mat, vec_b, vec_x));
     return tf::gmres_jacobi(c, c->mats[mat], c->vecs[vec_b].p, c->vecs[vec_x].p, restart, method, precision, max_iter,
                             tol, rel);
+}
+
+int tf_ch_steps(tf_context* t, int nsteps, double dt, double mobility, double eps, double beta_s, double xi,
+                double rho_vol, int restart, double tol, int max_iter, int warm, int* iters, double* resids) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (restart < 2 || max_iter < 1 || tol <= 0.) return tf::set_err(c, TF_ERR_BAD_INPUT, "ch_steps: bad solver arguments");
+    return tf::ch_steps(c, nsteps, dt, mobility, eps, beta_s, xi, rho_vol, restart, tol, max_iter, warm, iters, resids);
 }
 
 int tf_timing_enable(tf_context* t, int on) {

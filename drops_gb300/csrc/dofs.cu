@@ -167,6 +167,7 @@ int distribute_dofs(Context* c, int fe, double dist) {
     if (fe != TF_P1IF && fe != TF_P2IF) return set_err(c, TF_ERR_BAD_INPUT, "distribute_dofs: fe must be TF_P1IF or TF_P2IF");
     const MeshView& M = c->mesh;
     c->fe = 0;
+    c->legacy_numbering = false;
     TF_TRY(ensure(c, c->scratch, (size_t)M.nt * sizeof(int32_t)));
     TF_CUDA(c, cudaMemsetAsync(c->status.p, 0, 4 * sizeof(int), c->stream));
     {

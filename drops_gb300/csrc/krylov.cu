@@ -140,61 +140,158 @@ __device__ void grid_reduce(const double* part, double (&out)[NV]) {
 }
 
 // ---------------------------------------------------------------------------
-// SpMV (y_Ax, num/spmat.h:1684-1709): G lanes per row
+// SELL-32 layout and SpMV (y_Ax, num/spmat.h:1684-1709)
 // ---------------------------------------------------------------------------
-// Rows are handed out per warp (32/G rows at a time) so that every lane of a
-// warp runs the same number of iterations and reaches every shuffle.
-template <class T, int G>
-__device__ __forceinline__ double row_dot(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
-                                          const T* __restrict__ vals, const T* x, int64_t row, int64_t m, int sub) {
-    int32_t s = 0, e = 0;
-    if (row < m) {
-        s = __ldg(rowptr + row);
-        e = __ldg(rowptr + row + 1);
-    }
-    double acc = 0.;
-    for (int32_t k = s + sub; k < e; k += G) acc += (double)__ldg(vals + k) * (double)__ldcg(x + __ldg(colind + k));
-    for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
-    return acc;
-}
-
-#define TF_ROW_LOOP(G, m, row, sub)                                                         \
-    const int sub = threadIdx.x & ((G)-1);                                                  \
-    const int64_t warp__ = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;          \
-    const int64_t nwarp__ = ((int64_t)gridDim.x * blockDim.x) >> 5;                         \
-    for (int64_t base__ = warp__ * (32 / (G)); base__ < (m); base__ += nwarp__ * (32 / (G))) \
-        for (int64_t row = base__ + (threadIdx.x & 31) / (G), once__ = 0; once__ < 1; ++once__)
-
-template <class T, int G>
-__global__ void k_spmv(int64_t m, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
-                       const T* __restrict__ vals, const T* __restrict__ x, T* __restrict__ y) {
-    TF_ROW_LOOP(G, m, row, sub) {
-        const double a = row_dot<T, G>(rowptr, colind, vals, x, row, m, sub);
-        if (sub == 0 && row < m) y[row] = (T)a;
+__global__ void k_sell_width(int64_t m, int64_t nslices, const int32_t* __restrict__ rowptr, int32_t* __restrict__ w) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t s = warp; s < nslices; s += nwarp) {
+        const int64_t row = s * 32 + lane;
+        int len = row < m ? rowptr[row + 1] - rowptr[row] : 0;
+        len = __reduce_max_sync(0xffffffffu, len);
+        if (lane == 0) w[s] = 32 * len;
     }
 }
 
-static int pick_group(int64_t m, int64_t nnz) {
-    const double avg = m > 0 ? (double)nnz / (double)m : 1.0;
-    return avg <= 6 ? 4 : avg <= 12 ? 8 : avg <= 24 ? 16 : 32;
+__global__ void k_sell_fill(int64_t m, int64_t nslices, const int32_t* __restrict__ rowptr,
+                            const int32_t* __restrict__ colind, const int32_t* __restrict__ ptr,
+                            int32_t* __restrict__ col, int32_t* __restrict__ src) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t s = warp; s < nslices; s += nwarp) {
+        const int64_t row = s * 32 + lane;
+        const int32_t p0 = ptr[s], w = (ptr[s + 1] - p0) >> 5;
+        int32_t rs = 0, len = 0;
+        if (row < m) {
+            rs = rowptr[row];
+            len = rowptr[row + 1] - rs;
+        }
+        const int32_t pad_col = row < m ? (int32_t)row : 0;
+        for (int32_t k = 0; k < w; ++k) {
+            const int32_t pos = p0 + k * 32 + lane;
+            if (k < len) {
+                col[pos] = colind[rs + k];
+                src[pos] = rs + k;
+            } else {
+                col[pos] = pad_col;
+                src[pos] = -1;
+            }
+        }
+    }
 }
 
 template <class T>
-static void launch_spmv(Context* c, const CSR& A, const T* vals, const T* x, T* y) {
-    const int G = pick_group(A.m, A.nnz);
-    const int blocks = grid_for(c, (A.m * G + kBlock - 1) / kBlock * kBlock, kBlock, 8);
-    switch (G) {
-        case 4: k_spmv<T, 4><<<blocks, kBlock, 0, c->stream>>>(A.m, A.rowptr, A.colind, vals, x, y); break;
-        case 8: k_spmv<T, 8><<<blocks, kBlock, 0, c->stream>>>(A.m, A.rowptr, A.colind, vals, x, y); break;
-        case 16: k_spmv<T, 16><<<blocks, kBlock, 0, c->stream>>>(A.m, A.rowptr, A.colind, vals, x, y); break;
-        default: k_spmv<T, 32><<<blocks, kBlock, 0, c->stream>>>(A.m, A.rowptr, A.colind, vals, x, y); break;
+__global__ void k_sell_vals(int64_t npad, const int32_t* __restrict__ src, const double* __restrict__ vals,
+                            T* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npad; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t k = src[i];
+        out[i] = k >= 0 ? (T)vals[k] : (T)0;
     }
-    ++c->launches;
 }
 
-int spmv(Context* c, const CSR& A, const double* x, double* y) {
+static int mat_index(Context* c, const CSR& A) {
+    for (int i = 0; i < TF_NUM_MATS; ++i)
+        if (&c->mats[i] == &A) return i;
+    return 0;
+}
+
+int ensure_sell(Context* c, CSR& A, bool fp32) {
+    const int id = mat_index(c, A);
+    Sell& S = A.sell;
+    if (S.pattern_gen != A.pattern_gen || !S.ptr) {
+        const int64_t ns = (A.m + 31) / 32;
+        TF_TRY(ensure(c, c->sell_ptr[id], (size_t)ns + 1));
+        TF_TRY(ensure(c, c->scratch, sizeof(int32_t) * (size_t)(ns + 1)));
+        int32_t* w = (int32_t*)c->scratch.p;
+        k_sell_width<<<grid_for(c, ns * 32), kBlock, 0, c->stream>>>(A.m, ns, A.rowptr, w);
+        ++c->launches;
+        int64_t npad = 0;
+        TF_TRY(exclusive_scan_i32_to_i32(c, w, c->sell_ptr[id].p, ns, &npad));
+        TF_TRY(ensure(c, c->sell_col[id], (size_t)(npad > 0 ? npad : 1)));
+        TF_TRY(ensure(c, c->sell_src[id], (size_t)(npad > 0 ? npad : 1)));
+        k_sell_fill<<<grid_for(c, ns * 32), kBlock, 0, c->stream>>>(A.m, ns, A.rowptr, A.colind, c->sell_ptr[id].p,
+                                                                     c->sell_col[id].p, c->sell_src[id].p);
+        ++c->launches;
+        TF_CUDA(c, cudaGetLastError());
+        S.nslices = ns;
+        S.npad = npad;
+        S.ptr = c->sell_ptr[id].p;
+        S.col = c->sell_col[id].p;
+        S.src = c->sell_src[id].p;
+        S.pattern_gen = A.pattern_gen;
+        S.v64_version = S.v32_version = -1;
+    }
+    if (fp32) {
+        if (S.v32_version != A.version || !S.v32) {
+            TF_TRY(ensure(c, c->sell_v32[id], (size_t)(S.npad > 0 ? S.npad : 1)));
+            S.v32 = c->sell_v32[id].p;
+            k_sell_vals<float><<<grid_for(c, S.npad), kBlock, 0, c->stream>>>(S.npad, S.src, A.vals, S.v32);
+            ++c->launches;
+            S.v32_version = A.version;
+        }
+    } else if (S.v64_version != A.version || !S.v64) {
+        TF_TRY(ensure(c, c->sell_v64[id], (size_t)(S.npad > 0 ? S.npad : 1)));
+        S.v64 = c->sell_v64[id].p;
+        k_sell_vals<double><<<grid_for(c, S.npad), kBlock, 0, c->stream>>>(S.npad, S.src, A.vals, S.v64);
+        ++c->launches;
+        S.v64_version = A.version;
+    }
+    TF_CUDA(c, cudaGetLastError());
+    return TF_OK;
+}
+
+// Row 32s+lane of a SELL-32 matrix times the vector given by xload(col);
+// four columns are loaded before they are used, so each lane keeps several
+// independent gathers in flight.  Terms are summed in CSR order.
+template <class T, class XL>
+__device__ __forceinline__ double sell_row(const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                                           const T* __restrict__ val, int64_t s, int lane, XL xload) {
+    const int32_t p0 = __ldg(ptr + s);
+    const int32_t w = (__ldg(ptr + s + 1) - p0) >> 5;
+    const int32_t* cp = col + p0 + lane;
+    const T* vp = val + p0 + lane;
+    double acc = 0.;
+    int32_t k = 0;
+    for (; k + 4 <= w; k += 4) {
+        const int32_t c0 = __ldg(cp + 32 * k), c1 = __ldg(cp + 32 * (k + 1)), c2 = __ldg(cp + 32 * (k + 2)),
+                      c3 = __ldg(cp + 32 * (k + 3));
+        const double v0 = (double)__ldg(vp + 32 * k), v1 = (double)__ldg(vp + 32 * (k + 1)),
+                     v2 = (double)__ldg(vp + 32 * (k + 2)), v3 = (double)__ldg(vp + 32 * (k + 3));
+        const double x0 = xload(c0), x1 = xload(c1), x2 = xload(c2), x3 = xload(c3);
+        acc += v0 * x0;
+        acc += v1 * x1;
+        acc += v2 * x2;
+        acc += v3 * x3;
+    }
+    for (; k < w; ++k) acc += (double)__ldg(vp + 32 * k) * xload(__ldg(cp + 32 * k));
+    return acc;
+}
+
+#define TF_SLICE_LOOP(nslices, s)                                                    \
+    const int64_t warp__ = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;   \
+    const int64_t nwarp__ = ((int64_t)gridDim.x * blockDim.x) >> 5;                  \
+    for (int64_t s = warp__; s < (nslices); s += nwarp__)
+
+template <class T>
+__global__ void k_spmv(int64_t m, int64_t nslices, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                       const T* __restrict__ val, const T* __restrict__ x, T* __restrict__ y) {
+    const int lane = threadIdx.x & 31;
+    TF_SLICE_LOOP(nslices, s) {
+        const double a = sell_row<T>(ptr, col, val, s, lane, [&](int32_t j) { return (double)__ldcg(x + j); });
+        const int64_t row = s * 32 + lane;
+        if (row < m) y[row] = (T)a;
+    }
+}
+
+int spmv(Context* c, const CSR& Ac, const double* x, double* y) {
+    CSR& A = const_cast<CSR&>(Ac);
+    TF_TRY(ensure_sell(c, A, false));
     TimedLaunch tl(c, TF_K_SPMV);
-    launch_spmv<double>(c, A, A.vals, x, y);
+    k_spmv<double><<<grid_for(c, A.sell.nslices * 32), kBlock, 0, c->stream>>>(A.m, A.sell.nslices, A.sell.ptr,
+                                                                               A.sell.col, A.sell.v64, x, y);
+    ++c->launches;
     TF_CUDA(c, cudaGetLastError());
     return TF_OK;
 }
@@ -216,12 +313,6 @@ __global__ void k_to_f32(int64_t n, const double* __restrict__ a, float* __restr
         b[i] = (float)a[i];
 }
 
-static int mat_index(Context* c, const CSR& A) {
-    for (int i = 0; i < TF_NUM_MATS; ++i)
-        if (&c->mats[i] == &A) return i;
-    return 0;
-}
-
 int ensure_diag(Context* c, CSR& A) {
     if (A.diag_version == A.version && A.diag) return TF_OK;
     const int id = mat_index(c, A);
@@ -234,17 +325,7 @@ int ensure_diag(Context* c, CSR& A) {
     return TF_OK;
 }
 
-int ensure_vals32(Context* c, CSR& A) {
-    if (A.vals32_version == A.version && A.vals32) return TF_OK;
-    const int id = mat_index(c, A);
-    TF_TRY(ensure(c, c->mat_vals32[id], (size_t)(A.nnz > 0 ? A.nnz : 1)));
-    A.vals32 = c->mat_vals32[id].p;
-    k_to_f32<<<grid_for(c, A.nnz), kBlock, 0, c->stream>>>(A.nnz, A.vals, A.vals32);
-    ++c->launches;
-    TF_CUDA(c, cudaGetLastError());
-    A.vals32_version = A.version;
-    return TF_OK;
-}
+int ensure_vals32(Context* c, CSR& A) { return ensure_sell(c, A, true); }
 
 // ---------------------------------------------------------------------------
 // linear combination on the shared pattern, CH block matrix
@@ -286,6 +367,7 @@ int lincomb(Context* c, int nterms, const int* forms, const double* coeffs) {
     S.nnz = F.nnz;
     S.rowptr = F.rowptr;
     S.colind = F.colind;
+    S.pattern_gen = F.pattern_gen;
     S.vals = c->mat_vals[TF_MAT_SYS].p;
     k_lincomb2<<<grid_for(c, S.nnz), kBlock, 0, c->stream>>>(S.nnz, nterms, a, S.vals);
     ++c->launches;
@@ -331,6 +413,10 @@ int ch_block(Context* c, double alpha, double mob, double rho, double eps2, doub
     TF_TRY(ensure(c, c->block_rowptr, (size_t)(2 * m + 1)));
     TF_TRY(ensure(c, c->block_colind, (size_t)(4 * nnz > 0 ? 4 * nnz : 1)));
     TF_TRY(ensure(c, c->mat_vals[TF_MAT_BLOCK], (size_t)(4 * nnz > 0 ? 4 * nnz : 1)));
+    if (c->block_src_gen != M.pattern_gen || B.m != 2 * m) {
+        B.pattern_gen = ++c->pattern_counter;
+        c->block_src_gen = M.pattern_gen;
+    }
     B.m = 2 * m;
     B.nnz = 4 * nnz;
     B.rowptr = c->block_rowptr.p;
@@ -350,10 +436,10 @@ int ch_block(Context* c, double alpha, double mob, double rho, double eps2, doub
 // ---------------------------------------------------------------------------
 template <class T>
 struct PcgArgs {
-    int64_t m;
-    const int32_t* rowptr;
-    const int32_t* colind;
-    const T* vals;
+    int64_t m, nslices;
+    const int32_t* ptr;
+    const int32_t* col;
+    const T* val;
     const T* diag;
     const T* b;
     T* x;
@@ -371,17 +457,23 @@ struct PcgArgs {
     double* out_resid;
 };
 
-template <class T, int G>
-__global__ void __launch_bounds__(256) k_pcg(PcgArgs<T> a) {
+constexpr int kKryThreads = 256;
+
+template <class T>
+__global__ void __launch_bounds__(kKryThreads, 4) k_pcg(PcgArgs<T> a) {
+    const int lane = threadIdx.x & 31;
     double* partA = a.part;
     double* partB = a.part + (size_t)gridDim.x * 3 * 2;
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
 
     // r = b - A x ; z = r / d ; p0 = z ; partials <r,r>, <b,b>, <z,r>
     {
         DD v[3] = {{0, 0}, {0, 0}, {0, 0}};
-        TF_ROW_LOOP(G, a.m, row, sub) {
-            const double ax = row_dot<T, G>(a.rowptr, a.colind, a.vals, a.x, row, a.m, sub);
-            if (sub == 0 && row < a.m) {
+        const T* x = a.x;
+        TF_SLICE_LOOP(a.nslices, s) {
+            const double ax = sell_row<T>(a.ptr, a.col, a.val, s, lane, [&](int32_t j) { return (double)__ldcg(x + j); });
+            const int64_t row = s * 32 + lane;
+            if (row < a.m) {
                 const double bi = (double)a.b[row];
                 const T ri = (T)(bi - ax);
                 const T zi = (T)((double)ri / (double)a.diag[row]);
@@ -410,28 +502,21 @@ __global__ void __launch_bounds__(256) k_pcg(PcgArgs<T> a) {
         return;
     }
     double beta = 0.;
-    T* pc = a.p0;  // current direction (previous one when beta != 0)
+    T* pc = a.p0;  // previous direction (beta = 0 in the first iteration)
     T* pn = a.p1;
     for (int it = 1; it <= a.max_iter; ++it) {
-        // phase A: p_new = z + beta p_cur ; q = A p_new ; <q, p_new>
+        // phase A: p_new = z + beta p_old ; q = A p_new ; <q, p_new>
         {
             DD v[1] = {{0, 0}};
             const T* z = a.z;
-            TF_ROW_LOOP(G, a.m, row, sub) {
-                int32_t s = 0, e = 0;
+            const T* po = pc;
+            TF_SLICE_LOOP(a.nslices, s) {
+                const double acc = sell_row<T>(a.ptr, a.col, a.val, s, lane, [&](int32_t j) {
+                    return (double)(T)((double)__ldcg(z + j) + beta * (double)__ldcg(po + j));
+                });
+                const int64_t row = s * 32 + lane;
                 if (row < a.m) {
-                    s = __ldg(a.rowptr + row);
-                    e = __ldg(a.rowptr + row + 1);
-                }
-                double acc = 0.;
-                for (int32_t k = s + sub; k < e; k += G) {
-                    const int32_t j = __ldg(a.colind + k);
-                    const double pj = (double)__ldcg(z + j) + beta * (double)__ldcg(pc + j);
-                    acc += (double)__ldg(a.vals + k) * (double)(T)pj;
-                }
-                for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
-                if (sub == 0 && row < a.m) {
-                    const T pi = (T)((double)__ldcg(z + row) + beta * (double)__ldcg(pc + row));
+                    const T pi = (T)((double)__ldcg(z + row) + beta * (double)__ldcg(po + row));
                     const T qi = (T)acc;
                     pn[row] = pi;
                     a.q[row] = qi;
@@ -447,7 +532,7 @@ __global__ void __launch_bounds__(256) k_pcg(PcgArgs<T> a) {
         // phase B: x += alpha p ; r -= alpha q ; z = r / d ; <r,r>, <z,r>
         {
             DD v[2] = {{0, 0}, {0, 0}};
-            for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.m; i += (int64_t)gridDim.x * blockDim.x) {
+            for (int64_t i = tid; i < a.m; i += nth) {
                 const double pi = (double)__ldcg(pn + i);
                 a.x[i] = (T)((double)a.x[i] + alpha * pi);
                 const T ri = (T)((double)a.r[i] + (-alpha) * (double)__ldcg(a.q + i));
@@ -488,24 +573,23 @@ void release_solver_workspace(Context* c) {
     release(c->kry_iters);
 }
 
+// blocks of a cooperative launch: all co-resident, at most one row slice per warp
+static int coop_blocks(Context* c, const void* fn, int64_t nslices, int* out) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kKryThreads, 0) != cudaSuccess || per_sm < 1)
+        return set_err(c, TF_ERR_CUDA, "occupancy query failed");
+    const int64_t want = (nslices * 32 + kKryThreads - 1) / kKryThreads;
+    int64_t b = std::min<int64_t>(want, (int64_t)per_sm * c->num_sms);
+    *out = (int)(b < 1 ? 1 : b);
+    return TF_OK;
+}
+
 template <class T>
-static int run_pcg_kernel(Context* c, const CSR& A, const T* vals, const T* diag, const T* b, T* x, T* work, int max_iter,
+static int run_pcg_kernel(Context* c, const CSR& A, const T* val, const T* diag, const T* b, T* x, T* work, int max_iter,
                           double tol, int rel, int* iters_out, double* resid_out) {
-    const int G = pick_group(A.m, A.nnz);
-    int dev_blocks_per_sm = 0;
-    cudaError_t e;
-    void* fn;
-    switch (G) {
-        case 4: fn = (void*)k_pcg<T, 4>; break;
-        case 8: fn = (void*)k_pcg<T, 8>; break;
-        case 16: fn = (void*)k_pcg<T, 16>; break;
-        default: fn = (void*)k_pcg<T, 32>; break;
-    }
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&dev_blocks_per_sm, fn, 256, 0);
-    if (e != cudaSuccess || dev_blocks_per_sm < 1) return set_err(c, TF_ERR_CUDA, "pcg: occupancy query failed");
-    int64_t want = (A.m * G + 255) / 256;
-    int blocks = (int)std::min<int64_t>(want, (int64_t)dev_blocks_per_sm * c->num_sms);
-    if (blocks < 1) blocks = 1;
+    const void* fn = (const void*)k_pcg<T>;
+    int blocks = 0;
+    TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks));
     TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 3 * 2 * 2));
     TF_TRY(ensure(c, c->kry_bar, 2));
     TF_TRY(ensure(c, c->kry_iters, 1));
@@ -514,9 +598,10 @@ static int run_pcg_kernel(Context* c, const CSR& A, const T* vals, const T* diag
     TF_CUDA(c, cudaMemsetAsync(c->status.p, 0, 4 * sizeof(int), c->stream));
     PcgArgs<T> a;
     a.m = A.m;
-    a.rowptr = A.rowptr;
-    a.colind = A.colind;
-    a.vals = vals;
+    a.nslices = A.sell.nslices;
+    a.ptr = A.sell.ptr;
+    a.col = A.sell.col;
+    a.val = val;
     a.diag = diag;
     a.b = b;
     a.x = x;
@@ -533,7 +618,7 @@ static int run_pcg_kernel(Context* c, const CSR& A, const T* vals, const T* diag
     a.out_iter = c->kry_iters.p;
     a.out_resid = c->kry_resid.p;
     void* args[] = {&a};
-    TF_CUDA(c, cudaLaunchCooperativeKernel(fn, blocks, 256, args, 0, c->stream));
+    TF_CUDA(c, cudaLaunchCooperativeKernel(fn, blocks, kKryThreads, args, 0, c->stream));
     ++c->launches;
     int it = 0;
     double res = 0;
@@ -547,15 +632,16 @@ static int run_pcg_kernel(Context* c, const CSR& A, const T* vals, const T* diag
     return TF_OK;
 }
 
-// residual r = b - A x (FP64) with <r,r> partials, then norms on the host
-__global__ void k_residual(int64_t m, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
-                           const double* __restrict__ vals, const double* __restrict__ b, const double* __restrict__ x,
+// residual r = b - A x (FP64) with <r,r>, <b,b> partials
+__global__ void k_residual(int64_t m, int64_t nslices, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                           const double* __restrict__ val, const double* __restrict__ b, const double* __restrict__ x,
                            double* __restrict__ r, double* __restrict__ part) {
-    constexpr int G = 8;
+    const int lane = threadIdx.x & 31;
     DD v[2] = {{0, 0}, {0, 0}};
-    TF_ROW_LOOP(G, m, row, sub) {
-        const double ax = row_dot<double, G>(rowptr, colind, vals, x, row, m, sub);
-        if (sub == 0 && row < m) {
+    TF_SLICE_LOOP(nslices, s) {
+        const double ax = sell_row<double>(ptr, col, val, s, lane, [&](int32_t j) { return __ldcg(x + j); });
+        const int64_t row = s * 32 + lane;
+        if (row < m) {
             const double ri = b[row] - ax;
             r[row] = ri;
             two_sum_add(v[0], ri * ri);
@@ -596,20 +682,21 @@ __global__ void k_axpy_f32(int64_t n, double s, const float* __restrict__ d, dou
 int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, int* max_iter, double* tol, int rel) {
     if (!A.vals || A.m <= 0) return set_err(c, TF_ERR_BAD_INPUT, "pcg: empty matrix");
     TF_TRY(ensure_diag(c, A));
+    TF_TRY(ensure_sell(c, A, precision == TF_PREC_MIXED));
     const int64_t m = A.m;
     TimedLaunch tl(c, TF_K_PCG);
     if (precision == TF_PREC_FP64) {
         TF_TRY(ensure(c, c->kry64, (size_t)(5 * m)));
         int it = 0;
         double res = 0.;
-        TF_TRY(run_pcg_kernel<double>(c, A, A.vals, A.diag, b, x, c->kry64.p, *max_iter, *tol, rel, &it, &res));
+        TF_TRY(run_pcg_kernel<double>(c, A, A.sell.v64, A.diag, b, x, c->kry64.p, *max_iter, *tol, rel, &it, &res));
         const bool ok = it >= 0;
         *max_iter = ok ? it : -it;
         *tol = res;
         return ok ? TF_OK : set_err(c, TF_ERR_NOT_CONVERGED, "pcg: no convergence within max_iter");
     }
     // mixed precision: FP32 PCG sweeps inside FP64 iterative refinement
-    TF_TRY(ensure_vals32(c, A));
+    TF_TRY(ensure_sell(c, A, false));  // FP64 copy for the outer residual
     TF_TRY(ensure(c, c->kry32, (size_t)(8 * m)));
     TF_TRY(ensure(c, c->kry64, (size_t)(5 * m)));
     float* d32 = c->kry32.p;  // diag, rhs, x, work(5m)
@@ -619,15 +706,16 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
     k_to_f32<<<grid_for(c, m), kBlock, 0, c->stream>>>(m, A.diag, d32);
     ++c->launches;
     double* r64 = c->kry64.p;
-    double* part = c->kry64.p + m;  // needs <= 4 m doubles of room
-    const int rblocks = (int)std::min<int64_t>((m * 8 + kBlock - 1) / kBlock, (int64_t)c->num_sms * 8);
+    double* part = c->kry64.p + m;
+    const int rblocks = (int)std::min<int64_t>((A.sell.nslices * 32 + kBlock - 1) / kBlock, (int64_t)c->num_sms * 8);
     if ((int64_t)rblocks * 4 + 2 > 4 * m) return set_err(c, TF_ERR_CAPACITY, "pcg: matrix too small for mixed precision");
     double* sums = part + (size_t)rblocks * 4;
     int total_inner = 0;
     double res = 0.;
     const int max_outer = 60;
     for (int outer = 0; outer <= max_outer; ++outer) {
-        k_residual<<<rblocks, kBlock, 0, c->stream>>>(m, A.rowptr, A.colind, A.vals, b, x, r64, part);
+        k_residual<<<rblocks, kBlock, 0, c->stream>>>(m, A.sell.nslices, A.sell.ptr, A.sell.col, A.sell.v64, b, x, r64,
+                                                     part);
         k_reduce_partials<<<1, 256, 0, c->stream>>>(rblocks, part, sums);
         c->launches += 2;
         double h[2];
@@ -651,7 +739,7 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
         if (inner_tol > 0.1) inner_tol = 0.1;
         int it = 0;
         double ires = 0.;
-        TF_TRY(run_pcg_kernel<float>(c, A, A.vals32, d32, b32, x32, w32, *max_iter - total_inner, inner_tol, 1, &it,
+        TF_TRY(run_pcg_kernel<float>(c, A, A.sell.v32, d32, b32, x32, w32, *max_iter - total_inner, inner_tol, 1, &it,
                                      &ires));
         total_inner += it >= 0 ? it : -it;
         k_axpy_f32<<<grid_for(c, m), kBlock, 0, c->stream>>>(m, rn, x32, x);
@@ -663,10 +751,350 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
     return set_err(c, TF_ERR_NOT_CONVERGED, "pcg (mixed): no convergence within max_iter");
 }
 
+// ---------------------------------------------------------------------------
+// persistent restarted GMRES (num/krylovsolver.h:320-463)
+//
+// One cooperative kernel runs the whole solve.  Basis vectors are stored
+// unnormalised with a scale factor (v_k = sc_k * V_k), so v_{i+1} = w / h_{i+1,i}
+// needs no extra pass.  Modified Gram-Schmidt keeps the reference's order:
+// one grid barrier per projection.  The Hessenberg matrix, the Givens
+// rotations and the right-hand side s live in shared memory of every block and
+// are updated redundantly (bit-identical in all blocks).
+// ---------------------------------------------------------------------------
+constexpr int kMaxRestart = 64;
+
+struct GmresArgs {
+    int64_t m, nslices;
+    const int32_t* ptr;
+    const int32_t* col;
+    const double* val;
+    const double* diag;
+    const double* b;
+    double* x;
+    double* V;     // [R][m] unnormalised basis
+    double* part;  // [2][nblocks][2][2]
+    GridSync gs;
+    int R;         // restart
+    int left;      // 1: left preconditioning, 0: right
+    const double* binv;  // nodal 2x2 block-Jacobi inverses [m/2][4] (NULL: point Jacobi)
+    double* Z;           // work vector for the block preconditioner
+    int max_iter;
+    double tol;
+    int rel;
+    int* out_iter;
+    double* out_resid;
+};
+
+__global__ void __launch_bounds__(kKryThreads, 4) k_gmres(GmresArgs a) {
+    const int lane = threadIdx.x & 31;
+    __shared__ double H[kMaxRestart][kMaxRestart];
+    __shared__ double cs[kMaxRestart], sn[kMaxRestart], s[kMaxRestart + 1], y[kMaxRestart], sc[kMaxRestart];
+    const int64_t m = a.m;
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
+    double* partA = a.part;
+    double* partB = a.part + (size_t)gridDim.x * 2 * 2;
+    int flip = 0;
+    auto P = [&]() { flip ^= 1; return flip ? partB : partA; };
+
+    // r0 = b - A x (right) or M^{-1}(b - A x) (left) into V_0; <r,r>, |b| or |M^{-1} b|
+    {
+        double* pp = P();
+        DD v[2] = {{0, 0}, {0, 0}};
+        const double* x0 = a.x;
+        TF_SLICE_LOOP(a.nslices, sl) {
+            const double ax = sell_row<double>(a.ptr, a.col, a.val, sl, lane, [&](int32_t j) { return __ldcg(x0 + j); });
+            const int64_t row = sl * 32 + lane;
+            if (row < m) {
+                double r = a.b[row] - ax, bb = a.b[row];
+                if (a.left) {
+                    r = r / a.diag[row];
+                    bb = bb / a.diag[row];
+                }
+                a.V[row] = r;
+                two_sum_add(v[0], r * r);
+                two_sum_add(v[1], bb * bb);
+            }
+        }
+        block_partials<2>(v, pp);
+        if (!grid_barrier(a.gs)) return;
+        double t[2];
+        grid_reduce<2>(pp, t);
+        double beta = sqrt(t[0]);
+        double normb = sqrt(t[1]);
+        if (normb == 0.0 || !a.rel) normb = 1.0;
+        double resid = beta / normb;
+        if (resid <= a.tol) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                *a.out_iter = 0;
+                *a.out_resid = resid;
+            }
+            return;
+        }
+        int j = 1;
+        while (j <= a.max_iter) {
+            if (threadIdx.x == 0) {
+                sc[0] = 1.0 / beta;
+                s[0] = beta;
+                for (int k = 1; k <= a.R; ++k) s[k] = 0.;
+            }
+            __syncthreads();
+            int i;
+            bool done = false;
+            for (i = 0; i < a.R - 1 && j <= a.max_iter; ++i, ++j) {
+                const double* Vi = a.V + (size_t)i * m;
+                double* W = a.V + (size_t)(i + 1) * m;
+                const double sci = sc[i], sc0 = sc[0];
+                // block Jacobi (right): Z = P^{-1} v_i node by node, then w = A Z
+                if (a.binv) {
+                    const int64_t half = m / 2;
+                    for (int64_t e = tid; e < half; e += nth) {
+                        const double va = sci * __ldcg(Vi + e), vb = sci * __ldcg(Vi + e + half);
+                        const double* q4 = a.binv + 4 * e;
+                        a.Z[e] = q4[0] * va + q4[1] * vb;
+                        a.Z[e + half] = q4[2] * va + q4[3] * vb;
+                    }
+                    if (!grid_barrier(a.gs)) return;
+                }
+                // w = A M^{-1} v_i (right) or M^{-1} A v_i (left); <w, v_0>
+                {
+                    double* pq = P();
+                    DD v1[1] = {{0, 0}};
+                    const bool left = a.left;
+                    const double* dg = a.diag;
+                    const double* Zp = a.binv ? a.Z : nullptr;
+                    TF_SLICE_LOOP(a.nslices, s2) {
+                        double acc = sell_row<double>(a.ptr, a.col, a.val, s2, lane, [&](int32_t j) {
+                            if (Zp) return __ldcg(Zp + j);
+                            const double vj = sci * __ldcg(Vi + j);
+                            return left ? vj : vj / __ldg(dg + j);
+                        });
+                        const int64_t row = s2 * 32 + lane;
+                        if (row < m) {
+                            if (a.left) acc = acc / a.diag[row];
+                            W[row] = acc;
+                            two_sum_add(v1[0], acc * (sc0 * __ldcg(a.V + row)));
+                        }
+                    }
+                    block_partials<1>(v1, pq);
+                    if (!grid_barrier(a.gs)) return;
+                    double h[1];
+                    grid_reduce<1>(pq, h);
+                    if (threadIdx.x == 0) H[0][i] = h[0];
+                    __syncthreads();
+                }
+                // modified Gram-Schmidt: w -= h_k v_k, then <w, v_{k+1}> (or <w,w>)
+                for (int k = 0; k <= i; ++k) {
+                    double* pq = P();
+                    const double hk = H[k][i] * sc[k];
+                    const double* Vk = a.V + (size_t)k * m;
+                    const double* Vn = k < i ? a.V + (size_t)(k + 1) * m : nullptr;
+                    const double scn = k < i ? sc[k + 1] : 0.;
+                    DD v1[1] = {{0, 0}};
+                    for (int64_t e = tid; e < m; e += nth) {
+                        const double w = __ldcg(W + e) - hk * __ldcg(Vk + e);
+                        W[e] = w;
+                        two_sum_add(v1[0], k < i ? w * (scn * __ldcg(Vn + e)) : w * w);
+                    }
+                    block_partials<1>(v1, pq);
+                    if (!grid_barrier(a.gs)) return;
+                    double h[1];
+                    grid_reduce<1>(pq, h);
+                    if (threadIdx.x == 0) {
+                        if (k < i) H[k + 1][i] = h[0];
+                        else H[i + 1][i] = sqrt(h[0]);
+                    }
+                    __syncthreads();
+                }
+                if (threadIdx.x == 0) {
+                    sc[i + 1] = 1.0 / H[i + 1][i];
+                    for (int k = 0; k < i; ++k) {
+                        const double t0 = cs[k] * H[k][i] + sn[k] * H[k + 1][i];
+                        H[k + 1][i] = -sn[k] * H[k][i] + cs[k] * H[k + 1][i];
+                        H[k][i] = t0;
+                    }
+                    const double dx = H[i][i], dy = H[i + 1][i];
+                    if (dy == 0.0) {
+                        cs[i] = 1.0;
+                        sn[i] = 0.0;
+                    } else {
+                        const double r = sqrt(dx * dx + dy * dy);
+                        cs[i] = dx / r;
+                        sn[i] = dy / r;
+                    }
+                    double t0 = cs[i] * H[i][i] + sn[i] * H[i + 1][i];
+                    H[i + 1][i] = -sn[i] * H[i][i] + cs[i] * H[i + 1][i];
+                    H[i][i] = t0;
+                    t0 = cs[i] * s[i] + sn[i] * s[i + 1];
+                    s[i + 1] = -sn[i] * s[i] + cs[i] * s[i + 1];
+                    s[i] = t0;
+                }
+                __syncthreads();
+                resid = fabs(s[i + 1]) / normb;
+                if (resid <= a.tol) {
+                    done = true;
+                    break;
+                }
+            }
+            // x += V y (left) or x += M^{-1} V y (right) with k = i (converged) or i - 1
+            const int kk = done ? i : i - 1;
+            if (threadIdx.x == 0) {
+                for (int q = 0; q <= kk; ++q) y[q] = s[q];
+                for (int q = kk; q >= 0; --q) {
+                    y[q] /= H[q][q];
+                    for (int p = q - 1; p >= 0; --p) y[p] -= H[p][q] * y[q];
+                }
+            }
+            __syncthreads();
+            if (a.binv) {
+                const int64_t half = m / 2;
+                for (int64_t e = tid; e < half; e += nth) {
+                    double za = 0., zb = 0.;
+                    for (int q = 0; q <= kk; ++q) {
+                        za += y[q] * (sc[q] * __ldcg(a.V + (size_t)q * m + e));
+                        zb += y[q] * (sc[q] * __ldcg(a.V + (size_t)q * m + e + half));
+                    }
+                    const double* q4 = a.binv + 4 * e;
+                    a.x[e] = a.x[e] + (q4[0] * za + q4[1] * zb);
+                    a.x[e + half] = a.x[e + half] + (q4[2] * za + q4[3] * zb);
+                }
+            } else {
+                for (int64_t e = tid; e < m; e += nth) {
+                    double z = 0.;
+                    for (int q = 0; q <= kk; ++q) z += y[q] * (sc[q] * __ldcg(a.V + (size_t)q * m + e));
+                    if (!a.left) z = z / a.diag[e];
+                    a.x[e] = a.x[e] + z;
+                }
+            }
+            if (done) {
+                if (blockIdx.x == 0 && threadIdx.x == 0) {
+                    *a.out_iter = j;
+                    *a.out_resid = resid;
+                }
+                return;
+            }
+            if (!grid_barrier(a.gs)) return;
+            // new residual into V_0
+            {
+                double* pq = P();
+                DD v1[1] = {{0, 0}};
+                const double* x1 = a.x;
+                TF_SLICE_LOOP(a.nslices, s3) {
+                    const double ax = sell_row<double>(a.ptr, a.col, a.val, s3, lane, [&](int32_t j) { return __ldcg(x1 + j); });
+                    const int64_t row = s3 * 32 + lane;
+                    if (row < m) {
+                        double r = a.b[row] - ax;
+                        if (a.left) r = r / a.diag[row];
+                        a.V[row] = r;
+                        two_sum_add(v1[0], r * r);
+                    }
+                }
+                block_partials<1>(v1, pq);
+                if (!grid_barrier(a.gs)) return;
+                double t1[1];
+                grid_reduce<1>(pq, t1);
+                beta = sqrt(t1[0]);
+                resid = beta / normb;
+                if (resid <= a.tol) {
+                    if (blockIdx.x == 0 && threadIdx.x == 0) {
+                        *a.out_iter = j;
+                        *a.out_resid = resid;
+                    }
+                    return;
+                }
+            }
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            *a.out_iter = -(j - 1);
+            *a.out_resid = resid;
+        }
+    }
+}
+
+// nodal 2x2 block-Jacobi inverses of a 2x2 block system (rows i and i + m/2)
+__global__ void k_block_inv(int64_t half, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
+                            const double* __restrict__ vals, double* __restrict__ inv) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < half; i += (int64_t)gridDim.x * blockDim.x) {
+        double a11 = 0, a12 = 0, a21 = 0, a22 = 0;
+        for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+            if (colind[k] == i) a11 = vals[k];
+            if (colind[k] == i + half) a12 = vals[k];
+        }
+        for (int32_t k = rowptr[i + half]; k < rowptr[i + half + 1]; ++k) {
+            if (colind[k] == i) a21 = vals[k];
+            if (colind[k] == i + half) a22 = vals[k];
+        }
+        const double det = a11 * a22 - a12 * a21;
+        inv[4 * i] = a22 / det;
+        inv[4 * i + 1] = -a12 / det;
+        inv[4 * i + 2] = -a21 / det;
+        inv[4 * i + 3] = a11 / det;
+    }
+}
+
 int gmres_jacobi(Context* c, CSR& A, const double* b, double* x, int restart, int method, int precision, int* max_iter,
                  double* tol, int rel) {
-    (void)A; (void)b; (void)x; (void)restart; (void)method; (void)precision; (void)max_iter; (void)tol; (void)rel;
-    return set_err(c, TF_ERR_BAD_INPUT, "gmres: not available in this build");
+    if (!A.vals || A.m <= 0) return set_err(c, TF_ERR_BAD_INPUT, "gmres: empty matrix");
+    const bool block = &A == &c->mats[TF_MAT_BLOCK];
+    if (block && method == 1)
+        return set_err(c, TF_ERR_BAD_INPUT, "gmres: the block-Jacobi preconditioner is applied from the right (method 0)");
+    if (restart > kMaxRestart) return set_err(c, TF_ERR_CAPACITY, "gmres: restart > 64");
+    if (precision != TF_PREC_FP64) return set_err(c, TF_ERR_BAD_INPUT, "gmres: FP64 only");
+    TF_TRY(ensure_diag(c, A));
+    TF_TRY(ensure_sell(c, A, false));
+    const int64_t m = A.m;
+    const int R = restart <= *max_iter ? restart : (*max_iter > 1 ? *max_iter : 2);
+    TimedLaunch tl(c, TF_K_GMRES);
+    TF_TRY(ensure(c, c->kry64, (size_t)(R + 1) * m + (block ? 2 * m : 0)));
+    double* binv = nullptr;
+    if (block) {
+        binv = c->kry64.p + (size_t)(R + 1) * m;
+        k_block_inv<<<grid_for(c, m / 2), kBlock, 0, c->stream>>>(m / 2, A.rowptr, A.colind, A.vals, binv);
+        ++c->launches;
+        TF_CUDA(c, cudaGetLastError());
+    }
+    const void* fn = (const void*)k_gmres;
+    int blocks = 0;
+    TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks));
+    TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 2 * 2 * 2));
+    TF_TRY(ensure(c, c->kry_bar, 2));
+    TF_TRY(ensure(c, c->kry_iters, 1));
+    TF_TRY(ensure(c, c->kry_resid, 1));
+    TF_CUDA(c, cudaMemsetAsync(c->kry_bar.p, 0, 2 * sizeof(unsigned), c->stream));
+    TF_CUDA(c, cudaMemsetAsync(c->status.p, 0, 4 * sizeof(int), c->stream));
+    GmresArgs g;
+    g.m = m;
+    g.nslices = A.sell.nslices;
+    g.ptr = A.sell.ptr;
+    g.col = A.sell.col;
+    g.val = A.sell.v64;
+    g.diag = A.diag;
+    g.b = b;
+    g.x = x;
+    g.V = c->kry64.p;
+    g.part = c->kry_part.p;
+    g.gs = GridSync{c->kry_bar.p, c->kry_bar.p + 1, c->status.p};
+    g.R = R;
+    g.left = method == 1;
+    g.binv = binv;
+    g.Z = c->kry64.p + (size_t)R * m;
+    g.max_iter = *max_iter;
+    g.tol = *tol;
+    g.rel = rel;
+    g.out_iter = c->kry_iters.p;
+    g.out_resid = c->kry_resid.p;
+    void* args[] = {&g};
+    TF_CUDA(c, cudaLaunchCooperativeKernel(fn, blocks, kKryThreads, args, 0, c->stream));
+    ++c->launches;
+    int it = 0;
+    double res = 0;
+    TF_CUDA(c, cudaMemcpyAsync(&it, c->kry_iters.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    TF_CUDA(c, cudaMemcpyAsync(&res, c->kry_resid.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    int st = 0;
+    TF_TRY(sync_status(c, &st));
+    if (st) return set_err(c, st, "gmres: grid barrier watchdog fired");
+    *max_iter = it >= 0 ? it : -it;
+    *tol = res;
+    return it >= 0 ? TF_OK : set_err(c, TF_ERR_NOT_CONVERGED, "gmres: no convergence within max_iter");
 }
 
 }  // namespace tf

@@ -126,8 +126,23 @@ struct DBuf {
     size_t cap = 0;  // capacity
 };
 
+// Sliced ELLPACK copy of a CSR matrix for the Krylov kernels: slices of 32
+// consecutive rows, each padded to its longest row and stored column-major so
+// that lane l of a warp streams row 32s+l with coalesced loads.
+struct Sell {
+    int64_t nslices = 0, npad = 0;
+    int32_t* ptr = nullptr;  // nslices+1 offsets (elements)
+    int32_t* col = nullptr;  // npad
+    int32_t* src = nullptr;  // npad: CSR index or -1 for padding
+    double* v64 = nullptr;
+    float* v32 = nullptr;
+    int64_t pattern_gen = -1, v64_version = -1, v32_version = -1;
+};
+
 struct CSR {
     int64_t m = 0, nnz = 0;
+    int64_t pattern_gen = 0;    // bumps whenever the pattern changes
+    Sell sell;
     int32_t* rowptr = nullptr;  // m+1 (device)
     int32_t* colind = nullptr;  // nnz
     double* vals = nullptr;     // nnz
@@ -161,6 +176,7 @@ struct Context {
     int fe = 0;  // TF_P1IF / TF_P2IF, 0 = none
     int64_t n_active = 0, n_dofs = 0;
     int64_t dof_version = 0;
+    bool legacy_numbering = false;
     DBuf<int32_t> dof_vert, dof_edge, active, loc2glo;
     DBuf<uint8_t> flags;
     DBuf<int32_t> keys_v, keys_e, owner;
@@ -193,6 +209,10 @@ struct Context {
     DBuf<unsigned char> flush_buf;
     KernelTimer timers[TF_NUM_KERNELS];
     int64_t launches = 0;
+    int64_t pattern_counter = 0, block_src_gen = -1;
+    DBuf<int32_t> sell_ptr[TF_NUM_MATS], sell_col[TF_NUM_MATS], sell_src[TF_NUM_MATS];
+    DBuf<double> sell_v64[TF_NUM_MATS];
+    DBuf<float> sell_v32[TF_NUM_MATS];
 };
 
 // ---------------------------------------------------------------------------
@@ -264,8 +284,11 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
 int gmres_jacobi(Context* c, CSR& A, const double* b, double* x, int restart, int method, int precision,
                  int* max_iter, double* tol, int rel);
 int ensure_diag(Context* c, CSR& A);
+int ch_steps(Context* c, int nsteps, double dt, double mob, double eps, double beta_s, double xi, double rho_vol,
+             int restart, double tol, int max_iter, int warm, int* iters, double* resids);
 void release_solver_workspace(Context* c);
 int ensure_vals32(Context* c, CSR& A);
+int ensure_sell(Context* c, CSR& A, bool fp32);
 
 constexpr int kBlock = 256;
 inline int grid_for(Context* c, int64_t n, int block = kBlock, int per_sm = 8) {

@@ -191,6 +191,22 @@ int tf_pcg_jacobi(tf_context* ctx, int mat, int vec_b, int vec_x, int precision,
 int tf_gmres_jacobi(tf_context* ctx, int mat, int vec_b, int vec_x, int restart, int method, int precision,
                     int* max_iter, double* tol, int rel);
 
+/* ---- Cahn-Hilliard time stepping ------------------------------------------------- */
+/* `nsteps` implicit (BDF1) steps of the surface Cahn-Hilliard system of
+ * surfphasesep/surfphasesep.cpp:397-440 (constant mobility, no wind):
+ *   F_chi = f + (1/dt) M chi,  F_omega = beta_s M chi - M f0'(chi),
+ *   f0'(c) = xi 2c(1-c)(1-2c) (surfphasesep.cpp:140-150),
+ * block matrix [[M/dt, mob A + rho C], [eps^2 A + beta_s M + eps^2 rho C, -M]]
+ * (TF_MAT_BLOCK), GMRES(restart) with nodal 2x2 block-Jacobi applied from the
+ * right, relative residual tol.  Needs TF_FORM_M/A/CN assembled; f is
+ * TF_VEC_RHS when it holds m values, else 0.  TF_VEC_X holds [chi; omega]
+ * (2m) on entry and exit; warm != 0 starts every solve from the previous state
+ * (the reference's UsePreviousFrameAsInitialGuess), warm == 0 from zero.
+ * iters[nsteps], resids[nsteps] (may be NULL) receive each solve's GMRES
+ * iteration count and relative residual; TF_VEC_CHI receives the final chi. */
+int tf_ch_steps(tf_context* ctx, int nsteps, double dt, double mobility, double eps, double beta_s, double xi,
+                double rho_vol, int restart, double tol, int max_iter, int warm, int* iters, double* resids);
+
 /* ---- instrumentation -------------------------------------------------------------- */
 /* Per-kernel device time, recorded with CUDA events on the context's stream
  * while enabled; kernel ids are the TF_K_* below.                                  */

@@ -205,15 +205,16 @@ def pcg_jacobi(rowptr, colind, vals, b, x0=None, max_iter=100000, tol=1e-10, rel
     return st, x, it.value, t.value
 
 
-def gmres_jacobi(rowptr, colind, vals, b, x0=None, restart=50, max_iter=100000, tol=1e-10, rel=True, method=0):
+def gmres_jacobi(rowptr, colind, vals, b, x0=None, restart=50, max_iter=100000, tol=1e-10, rel=True, method=0,
+                 block=False):
     L = lib()
     m = len(rowptr) - 1
     x = np.zeros(m) if x0 is None else np.array(x0, dtype=np.float64)
     it = C.c_int(max_iter)
     t = C.c_double(tol)
-    st = L.orc_gmres_jacobi(C.c_int64(m), _p(rowptr, C.c_int64), _p(colind, C.c_int32), _p(vals, C.c_double),
-                            _p(np.ascontiguousarray(b, dtype=np.float64), C.c_double), _p(x, C.c_double),
-                            C.c_int(restart), C.byref(it), C.byref(t), C.c_int(int(rel)), C.c_int(method))
+    st = L.orc_gmres(C.c_int64(m), _p(rowptr, C.c_int64), _p(colind, C.c_int32), _p(vals, C.c_double),
+                     _p(np.ascontiguousarray(b, dtype=np.float64), C.c_double), _p(x, C.c_double),
+                     C.c_int(restart), C.byref(it), C.byref(t), C.c_int(int(rel)), C.c_int(method), C.c_int(int(block)))
     return st, x, it.value, t.value
 
 

@@ -797,11 +797,50 @@ int orc_pcg_jacobi(int64_t m, const int64_t* rowptr, const int32_t* colind, cons
     return ORC_ERR_NOT_CONVERGED;
 }
 
+/* Nodal 2x2 block Jacobi for a 2x2 block system of size 2*h: the inverse of
+ * [[a(i,i), a(i,i+h)], [a(i+h,i), a(i+h,i+h)]] applied to (v_i, v_{i+h}).   */
+static void block_inv(int64_t m, const int64_t* rowptr, const int32_t* colind, const double* vals, double* inv) {
+    const int64_t h = m / 2;
+    for (int64_t i = 0; i < h; ++i) {
+        double a11 = 0, a12 = 0, a21 = 0, a22 = 0;
+        for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+            if (colind[k] == i) a11 = vals[k];
+            if (colind[k] == i + h) a12 = vals[k];
+        }
+        for (int64_t k = rowptr[i + h]; k < rowptr[i + h + 1]; ++k) {
+            if (colind[k] == i) a21 = vals[k];
+            if (colind[k] == i + h) a22 = vals[k];
+        }
+        const double det = a11 * a22 - a12 * a21;
+        inv[4 * i] = a22 / det;
+        inv[4 * i + 1] = -a12 / det;
+        inv[4 * i + 2] = -a21 / det;
+        inv[4 * i + 3] = a11 / det;
+    }
+}
+static void prec_apply(int64_t m, int block, const double* d, const double* inv, const double* v, double* out) {
+    if (!block) {
+        for (int64_t i = 0; i < m; ++i) out[i] = v[i] / d[i];
+        return;
+    }
+    const int64_t h = m / 2;
+    for (int64_t i = 0; i < h; ++i) {
+        const double a = v[i], c = v[i + h];
+        out[i] = inv[4 * i] * a + inv[4 * i + 1] * c;
+        out[i + h] = inv[4 * i + 2] * a + inv[4 * i + 3] * c;
+    }
+}
+
 int orc_gmres_jacobi(int64_t m, const int64_t* rowptr, const int32_t* colind, const double* vals, const double* b,
                      double* x, int restart, int* max_iter, double* tol, int rel, int method) {
+    return orc_gmres(m, rowptr, colind, vals, b, x, restart, max_iter, tol, rel, method, 0);
+}
+
+int orc_gmres(int64_t m, const int64_t* rowptr, const int32_t* colind, const double* vals, const double* b,
+              double* x, int restart, int* max_iter, double* tol, int rel, int method, int block) {
     int mm = restart <= *max_iter ? restart : *max_iter;
-    double* d = (double*)malloc(sizeof(double) * (size_t)m * (size_t)(mm + 4));
-    double *w = d + m, *r = w + m, *t = r + m, *V = t + m;
+    double* d = (double*)malloc(sizeof(double) * (size_t)m * (size_t)(mm + 7));
+    double *w = d + m, *r = w + m, *t = r + m, *u = t + m, *inv = u + m, *V = inv + 2 * m;
     double* H = (double*)calloc((size_t)mm * mm, sizeof(double));
     double* s = (double*)calloc((size_t)mm, sizeof(double));
     double* cs = (double*)calloc((size_t)mm, sizeof(double));
@@ -809,6 +848,7 @@ int orc_gmres_jacobi(int64_t m, const int64_t* rowptr, const int32_t* colind, co
     double* y = (double*)calloc((size_t)mm, sizeof(double));
 #define HH(i, j) H[(size_t)(i) * mm + (j)]
     jacobi_diag(m, rowptr, colind, vals, d);
+    if (block) block_inv(m, rowptr, colind, vals, inv);
     double beta, normb, resid;
     orc_spmv(m, rowptr, colind, vals, x, t);
     if (method == 0) {
@@ -816,9 +856,10 @@ int orc_gmres_jacobi(int64_t m, const int64_t* rowptr, const int32_t* colind, co
         beta = sqrt(plain_dot(m, r, r));
         normb = sqrt(plain_dot(m, b, b));
     } else {
-        for (int64_t i = 0; i < m; ++i) r[i] = (b[i] - t[i]) / d[i];
+        for (int64_t i = 0; i < m; ++i) u[i] = b[i] - t[i];
+        prec_apply(m, block, d, inv, u, r);
         beta = sqrt(plain_dot(m, r, r));
-        for (int64_t i = 0; i < m; ++i) w[i] = b[i] / d[i];
+        prec_apply(m, block, d, inv, b, w);
         normb = sqrt(plain_dot(m, w, w));
     }
     if (normb == 0.0 || !rel) normb = 1.0;
@@ -839,11 +880,11 @@ int orc_gmres_jacobi(int64_t m, const int64_t* rowptr, const int32_t* colind, co
         for (i = 0; i < mm - 1 && j <= *max_iter; ++i, ++j) {
             double* vi = V + (size_t)i * m;
             if (method == 0) {
-                for (int64_t k = 0; k < m; ++k) t[k] = vi[k] / d[k];
+                prec_apply(m, block, d, inv, vi, t);
                 orc_spmv(m, rowptr, colind, vals, t, w);
             } else {
                 orc_spmv(m, rowptr, colind, vals, vi, t);
-                for (int64_t k = 0; k < m; ++k) w[k] = t[k] / d[k];
+                prec_apply(m, block, d, inv, t, w);
             }
             for (int k = 0; k <= i; ++k) {
                 double* vk = V + (size_t)k * m;
@@ -882,7 +923,8 @@ int orc_gmres_jacobi(int64_t m, const int64_t* rowptr, const int32_t* colind, co
                     for (int64_t k = 0; k < m; ++k) w[k] = 0.;
                     for (int q = 0; q <= kk; ++q)
                         for (int64_t k = 0; k < m; ++k) w[k] += y[q] * V[(size_t)q * m + k];
-                    for (int64_t k = 0; k < m; ++k) x[k] += w[k] / d[k];
+                    prec_apply(m, block, d, inv, w, u);
+                    for (int64_t k = 0; k < m; ++k) x[k] += u[k];
                 } else {
                     for (int q = 0; q <= kk; ++q)
                         for (int64_t k = 0; k < m; ++k) x[k] += y[q] * V[(size_t)q * m + k];
@@ -904,14 +946,16 @@ int orc_gmres_jacobi(int64_t m, const int64_t* rowptr, const int32_t* colind, co
                 for (int64_t k = 0; k < m; ++k) w[k] = 0.;
                 for (int q = 0; q <= kk; ++q)
                     for (int64_t k = 0; k < m; ++k) w[k] += y[q] * V[(size_t)q * m + k];
-                for (int64_t k = 0; k < m; ++k) x[k] += w[k] / d[k];
+                prec_apply(m, block, d, inv, w, u);
+                for (int64_t k = 0; k < m; ++k) x[k] += u[k];
                 orc_spmv(m, rowptr, colind, vals, x, t);
                 for (int64_t k = 0; k < m; ++k) r[k] = b[k] - t[k];
             } else {
                 for (int q = 0; q <= kk; ++q)
                     for (int64_t k = 0; k < m; ++k) x[k] += y[q] * V[(size_t)q * m + k];
                 orc_spmv(m, rowptr, colind, vals, x, t);
-                for (int64_t k = 0; k < m; ++k) r[k] = (b[k] - t[k]) / d[k];
+                for (int64_t k = 0; k < m; ++k) u[k] = b[k] - t[k];
+                prec_apply(m, block, d, inv, u, r);
             }
         }
         beta = sqrt(plain_dot(m, r, r));

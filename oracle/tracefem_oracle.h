@@ -122,6 +122,9 @@ int orc_pcg_jacobi(int64_t m, const int64_t* rowptr, const int32_t* colind, cons
 int orc_gmres_jacobi(int64_t m, const int64_t* rowptr, const int32_t* colind, const double* vals,
                      const double* b, double* x, int restart, int* max_iter, double* tol, int rel,
                      int method);
+/* block != 0: nodal 2x2 block Jacobi on a 2x2 block system (rows i and i+m/2) */
+int orc_gmres(int64_t m, const int64_t* rowptr, const int32_t* colind, const double* vals, const double* b,
+              double* x, int restart, int* max_iter, double* tol, int rel, int method, int block);
 
 /* Cahn-Hilliard 2x2 block system (surfphasesep/surfphasesep.cpp:431-434):
  * [[a*M, mob*A + rho*C], [eps2*A + beta*M + eps2*rho*C, -M]] with the shared

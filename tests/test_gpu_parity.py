@@ -201,3 +201,104 @@ def test_p2_against_oracle_mid_size(ctx):
         assert ok, err
     ok, err = mat_close(ctx.vec_download(tf.VEC_RHS), rhs)
     assert ok, err
+
+
+@pytest.mark.parametrize("method", [0, 1])
+def test_gmres_parity(ctx, golden, method):
+    """GMRES(m) with Jacobi, right (0) and left (1) preconditioning, vs the oracle's restatement."""
+    g = golden("c1_sphere_p1_n16.npz")
+    ctx.matrix_upload(g["rowptr"], g["colind"], g["S"])
+    ctx.vec_upload(tf.VEC_B, g["rhs"])
+    ctx.vec_fill(tf.VEC_X, len(g["rhs"]), 0.0)
+    st, it, res = ctx.gmres_jacobi(tf.MAT_USER, tf.VEC_B, tf.VEC_X, restart=20, tol=1e-10, method=method)
+    ost, ox, oit, ores = O.gmres_jacobi(g["rowptr"], g["colind"], g["S"], g["rhs"], restart=20, tol=1e-10,
+                                        method=method)
+    assert st == tf.OK and ost == O.OK
+    assert abs(it - oit) <= 2, (it, oit)
+    ok, err = sol_close(ctx.vec_download(tf.VEC_X), g["x"])
+    assert ok, err
+
+
+def test_ch_block_gmres(ctx, golden):
+    """One implicit Cahn-Hilliard step: block matrix (surfphasesep.cpp:431-434) + GMRES(50)."""
+    g = golden("torus_p1_n16.npz")
+    om, p2, na, nd = setup_case(ctx, g, O.LS_TORUS, [1.0, 0.4, 2])
+    ctx.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN])
+    dt, eps, h = 1e-3, 0.02, 2 * float(g["a"]) / int(g["n"])
+    alpha, rho, beta = 1.0 / dt, h, 0.0
+    ctx.ch_block(alpha, 1.0, rho, eps * eps, beta)
+    rp, ci, B = ctx.matrix(tf.MAT_BLOCK)
+    brp, bci, bv = O.ch_block(g["rowptr"], g["colind"], g["M"], g["A"], g["C"], alpha, 1.0, rho, eps * eps, beta)
+    assert np.array_equal(rp, brp) and np.array_equal(ci, bci)
+    ok, err = mat_close(B, bv)
+    assert ok, err
+    rng = np.random.default_rng(7)
+    chi = 0.5 + rng.uniform(-0.01, 0.01, nd)
+    Mchi = O.spmv(g["rowptr"], g["colind"], g["M"], chi)
+    fp = 2 * chi * (1 - chi) * (1 - 2 * chi)
+    rhs = np.concatenate([alpha * Mchi, beta * Mchi - O.spmv(g["rowptr"], g["colind"], g["M"], fp)])
+    ctx.vec_upload(tf.VEC_B, rhs)
+    ctx.vec_fill(tf.VEC_X, 2 * nd, 0.0)
+    st, it, res = ctx.gmres_jacobi(tf.MAT_BLOCK, tf.VEC_B, tf.VEC_X, restart=50, tol=1e-10, max_iter=20000)
+    ost, ox, oit, ores = O.gmres_jacobi(brp, bci, bv, rhs, restart=50, tol=1e-10, max_iter=20000, block=True)
+    assert st == tf.OK and ost == O.OK, (st, ost, it, oit)
+    assert abs(it - oit) <= max(5, oit // 50), (it, oit)
+    x = ctx.vec_download(tf.VEC_X)
+    ok, err = sol_close(x, ox)
+    assert ok, err
+
+
+def test_legacy_numbering(ctx, golden):
+    """CreateNumbOnInterfaceVertex: 8 unknowns (plane), 1156 (sphere r=0.31 on 20^3), error at a vertex plane."""
+    g = golden("legacy_numbering.npz")
+    brick(ctx, (10, 1, 1), orig=np.zeros(3), e=np.eye(3))
+    ctx.levelset_analytic(tf.LS_PLANE, [1, 0, 0, 0.41], True)
+    na, nd = ctx.create_numb_on_interface_p1()
+    assert nd == int(g["plane_n_dofs"]) == 8 and na == int(g["plane_n_active"])
+    assert np.array_equal(ctx.dofs()[0], g["plane_dof_vert"])
+    ctx.levelset_analytic(tf.LS_PLANE, [1, 0, 0, 0.4], True)
+    with pytest.raises(tf.TraceFEMError) as ei:
+        ctx.create_numb_on_interface_p1()
+    assert ei.value.status == tf.ERR_ZERO_NODE
+    brick(ctx, (20, 20, 20), orig=np.zeros(3), e=np.eye(3))
+    ctx.levelset_analytic(tf.LS_SPHERE, [0.5, 0.5, 0.5, 0.31], True)
+    na, nd = ctx.create_numb_on_interface_p1()
+    assert nd == int(g["sphere_n_dofs"]) == 1156 and na == int(g["sphere_n_active"])
+    assert np.array_equal(ctx.dofs()[0], g["sphere_dof_vert"])
+
+
+def oracle_ch_steps(g, nsteps, dt, eps, rho, beta, xi, chi0, restart=50, tol=1e-10, warm=True):
+    """surfphasesep BDF1 steps restated on the oracle (CPU)."""
+    rp, ci, M = g["rowptr"], g["colind"], g["M"]
+    brp, bci, bv = O.ch_block(rp, ci, M, g["A"], g["C"], 1.0 / dt, 1.0, rho, eps * eps, beta)
+    m = len(rp) - 1
+    X = np.concatenate([chi0, np.zeros(m)])
+    its = []
+    for _ in range(nsteps):
+        chi = X[:m]
+        Mc = O.spmv(rp, ci, M, chi)
+        Mf = O.spmv(rp, ci, M, xi * 2 * chi * (1 - chi) * (1 - 2 * chi))
+        b = np.concatenate([Mc / dt, beta * Mc - Mf])
+        st, X, it, res = O.gmres_jacobi(brp, bci, bv, b, x0=X if warm else None, restart=restart, tol=tol,
+                                        max_iter=50000, block=True)
+        assert st == O.OK
+        its.append(it)
+    return X, its
+
+
+def test_ch_steps_parity(ctx, golden):
+    """Three warm-started CH steps on the torus (P1, n=16): state within 1e-8, iterations close."""
+    g = golden("torus_p1_n16.npz")
+    om, p2, na, nd = setup_case(ctx, g, O.LS_TORUS, [1.0, 0.4, 2])
+    ctx.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN])
+    dt, eps, h, beta, xi = 1e-3, 0.02, 2 * float(g["a"]) / int(g["n"]), 0.0, 1.0
+    rng = np.random.default_rng(11)
+    chi0 = 0.5 + rng.uniform(-0.01, 0.01, nd)
+    ctx.vec_upload(tf.VEC_X, np.concatenate([chi0, np.zeros(nd)]))
+    st, its, res = ctx.ch_steps(3, dt, 1.0, eps, beta, xi, h, restart=50, tol=1e-10)
+    assert st == tf.OK and np.all(res <= 1e-10)
+    X = ctx.vec_download(tf.VEC_X)
+    OX, oits = oracle_ch_steps(g, 3, dt, eps, h, beta, xi, chi0)
+    assert np.linalg.norm(X[:nd] - OX[:nd]) <= 1e-8 * np.linalg.norm(OX[:nd])
+    for a, b in zip(its, oits):
+        assert abs(int(a) - b) <= max(5, b // 50), (its, oits)
