@@ -36,7 +36,6 @@ sys.path.insert(0, ROOT)
 
 N_CUBES = 96
 HALF = 5.0 / 3.0
-H = 2 * HALF / N_CUBES
 SPHERE = [0.0, 0.0, 0.0, 1.0]
 RHS = [0.0, 0.0, 0.0, 1.0, 13.0]
 TOL = 1e-10
@@ -149,9 +148,12 @@ def pcg_bytes(m, nnz, iters, fp32):
 def run_ours(args, rank, ws, dist):
     import drops_gb300 as tf
 
+    N = args.size
+    H = 2 * HALF / N
+
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     ctx = tf.TraceFEM(dev)
-    ctx.brick_cube(N_CUBES, HALF)
+    ctx.brick_cube(N, HALF)
     ctx.levelset_analytic(tf.LS_SPHERE, SPHERE, p2=True)
     nv, ne, nt = ctx.mesh_info()
     lv_dev, le_dev = ctx.levelset_download()
@@ -190,7 +192,7 @@ def run_ours(args, rank, ws, dist):
             cut += step()
             ctx.marker(1)
             step_ms.append(ctx.elapsed_ms(0, 1))
-    launches = ctx.launch_count() - launches0 - args.steps  # the flushes are memsets, not kernels
+    launches = ctx.launch_count() - launches0  # L2 flushes are memsets, not counted
     ktimes = {name: ctx.timing_get(k) for k, name in enumerate(tf.KERNEL_NAMES)}
     ctx.timing(False)
     clocks = clk.summary()
@@ -273,12 +275,13 @@ def run_ours(args, rank, ws, dist):
 
 
 # ---------------------------------------------------------------------------
-def cpu_workload(threads):
+def cpu_workload(threads, N=N_CUBES):
     """The same step with the oracle (C restatement of the reference) on the host."""
     from oracle import pyoracle as O
 
     O.set_threads(threads)
-    mesh = O.brick(N_CUBES, a=HALF)
+    H = 2 * HALF / N
+    mesh = O.brick(N, a=HALF)
     lv, le = O.levelset(mesh, O.LS_SPHERE, SPHERE, True)
     opts = O.make_opts(True, [O.FORM_M, O.FORM_A, O.FORM_CN], O.RHS_SPHERE_XYZ, RHS)
 
@@ -297,7 +300,7 @@ def run_reference(args, rank, ws, dist):
     if rank != 0:
         return None
     threads = os.cpu_count() or 1
-    step = cpu_workload(threads)
+    step = cpu_workload(threads, args.size)
     for _ in range(args.warmup):
         step()
     tot_t, tot_cut = 0.0, 0
@@ -325,6 +328,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--size", type=int, default=N_CUBES, help="cubes per direction (96 = the benchmark workload; "
+                    "smaller sizes are for profiling captures)")
     args = ap.parse_args()
     rank, ws, dist = dist_init()
     if args.impl == "reference":
@@ -338,10 +343,12 @@ def main():
         build.build()
     barrier(dist)
     out = run_ours(args, rank, ws, dist)
+    if args.size != N_CUBES:
+        out["config"] = dict(out["config"], workload=f"PROFILING SIZE {args.size}^3 (not the benchmark workload)")
     if rank == 0:
         if ws == 1 and not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
-            step = cpu_workload(threads)
+            step = cpu_workload(threads, args.size)
             na, dt, it = step()
             out["cpu_baseline"] = {"value": round(na / dt, 1), "unit": "cut_tets/s", "cores": threads, "kind": "port",
                                    "sample": f"one full step of the same workload ({dt:.1f} s, FP64 PCG {it} iterations)"}
