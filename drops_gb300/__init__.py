@@ -39,7 +39,7 @@ KERNEL_NAMES = ["classify", "number", "assemble", "pattern", "scatter", "spmv", 
 EXPORTS = [
     "tf_create", "tf_destroy", "tf_last_error", "tf_status_string", "tf_stream", "tf_mesh_brick", "tf_mesh_upload",
     "tf_mesh_info", "tf_mesh_download", "tf_levelset_upload", "tf_levelset_analytic", "tf_levelset_download",
-    "tf_distribute_dofs", "tf_create_numb_on_interface_p1", "tf_dofs_download", "tf_setup_fe_system",
+    "tf_distribute_dofs", "tf_create_numb_on_interface_p1", "tf_dofs_download", "tf_patches_download", "tf_setup_fe_system",
     "tf_matrix_info", "tf_matrix_download", "tf_matrix_upload", "tf_lincomb", "tf_ch_block", "tf_vec_upload",
     "tf_vec_download", "tf_vec_size", "tf_vec_fill", "tf_spmv", "tf_pcg_jacobi", "tf_gmres_jacobi", "tf_ch_steps", "tf_timing_enable",
     "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2",
@@ -195,6 +195,19 @@ class TraceFEM:
         l2g = np.empty(max(self.n_active * nl, 1), np.int32)
         self._check(self.L.tf_dofs_download(self.h, _ip(dv), _ip(de), _ip(act), _ip(l2g)))
         return dv, de, act[: self.n_active], l2g[: self.n_active * nl]
+
+    def patches(self, first=0, count=None):
+        """make_patch topology of active tets [first, first+count): list of (facets, boundary, verts)."""
+        if count is None:
+            count = self.n_active - first
+        nf = np.zeros(count, np.int32)
+        fac = np.zeros((count, 16, 3), np.int32)
+        bnd = np.zeros((count, 16), np.int32)
+        nv = np.zeros(count, np.int32)
+        ver = np.zeros((count, 40, 4))
+        self._check(self.L.tf_patches_download(self.h, C.c_int64(first), C.c_int64(count), _ip(nf), _ip(fac), _ip(bnd),
+                                               _ip(nv), _dp(ver)))
+        return [(fac[i, :nf[i]], bnd[i, :nf[i]], ver[i, :nv[i]]) for i in range(count)]
 
     # ---- assembly ----------------------------------------------------------------
     def setup_fe_system(self, forms, rhs_kind=RHS_NONE, rhs_par=()):

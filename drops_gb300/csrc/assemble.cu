@@ -838,6 +838,115 @@ __global__ void k_assign_asm(int64_t n, const int32_t* __restrict__ keys, const 
 }
 
 // ---------------------------------------------------------------------------
+// patch topology in the reference's own numbering (for parity checks):
+// SPatchCL<3>::make_patch<MergeCutPolicyCL> (geom/subtriangulation.tpp:191-228)
+// replayed per tet -- cut vertices numbered in discovery order, copied zero
+// vertices after them, facets in sub-tet order.
+// ---------------------------------------------------------------------------
+__global__ void k_patch_dump(MeshView M, const double* __restrict__ lsv, const double* __restrict__ lse,
+                             const int32_t* __restrict__ tets, int64_t count, int32_t* __restrict__ nf_out,
+                             int32_t* __restrict__ facets, int32_t* __restrict__ bnd_out, int32_t* __restrict__ nv_out,
+                             double* __restrict__ verts, int* status) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < count; r += (int64_t)gridDim.x * blockDim.x) {
+        int32_t v[4], e[6];
+        mesh_tet(M, tets[r], v, e);
+        double ls10[10], lat[10];
+        for (int k = 0; k < 4; ++k) ls10[k] = lsv[v[k]];
+        for (int k = 0; k < 6; ++k) ls10[4 + k] = lse[e[k]];
+        for (int k = 0; k < 10; ++k) lat[cP2OnLat[k]] = ls10[k];
+        int cut_a[32], cut_b[32], ncut = 0;
+        int copied[10];
+        for (int k = 0; k < 10; ++k) copied[k] = -1;
+        int zero_lat[10], nzero = 0;
+        int zf[48], zj[48], nz = 0;
+        int nf = 0;
+        int32_t* F = facets + r * 48;
+        for (int s = 0; s < 8; ++s) {
+            int pat = 0;
+            for (int k = 0; k < 4; ++k) {
+                const double x = lat[cT.lat_t[s][k]];
+                pat += ((x > 0.) - (x < 0.) + 1) * (k == 0 ? 1 : k == 1 ? 3 : k == 2 ? 9 : 27);
+            }
+            const int n = cT.pat_nf[pat];
+            if (n < 0) {
+                set_status(status, TF_ERR_ZERO_PATTERN, tets[r]);
+                break;
+            }
+            for (int f = 0; f < n; ++f, ++nf) {
+                bnd_out[r * 16 + nf] = cT.pat_bnd[pat];
+                for (int j = 0; j < 3; ++j) {
+                    const int ext = cT.pat_f[pat][f][j];
+                    if (ext < 4) {
+                        const int L = cT.lat_t[s][ext];
+                        if (copied[L] < 0) {
+                            copied[L] = nzero;
+                            zero_lat[nzero++] = L;
+                        }
+                        F[3 * nf + j] = copied[L];
+                        zf[nz] = nf;
+                        zj[nz] = j;
+                        ++nz;
+                    } else {
+                        const int a = cT.can_a[s][ext - 4], b = cT.can_b[s][ext - 4];
+                        int id = -1;
+                        for (int q = 0; q < ncut; ++q)
+                            if (cut_a[q] == a && cut_b[q] == b) id = q;
+                        if (id < 0) {
+                            id = ncut++;
+                            cut_a[id] = a;
+                            cut_b[id] = b;
+                        }
+                        F[3 * nf + j] = id;
+                    }
+                }
+            }
+        }
+        for (int u = 0; u < nz; ++u) F[3 * zf[u] + zj[u]] += ncut;
+        nf_out[r] = nf;
+        nv_out[r] = ncut + nzero;
+        double* V = verts + r * 40 * 4;
+        for (int q = 0; q < ncut; ++q) cut_point(lat, cut_a[q], cut_b[q], V + 4 * q);
+        for (int q = 0; q < nzero; ++q)
+            for (int c2 = 0; c2 < 4; ++c2) V[4 * (ncut + q) + c2] = cT.lat_v[zero_lat[q]][c2];
+    }
+}
+
+int patch_dump(Context* c, int64_t first, int64_t count, int32_t* nf, int32_t* facets, int32_t* bnd, int32_t* nverts,
+               double* verts) {
+    if (!c->fe) return set_err(c, TF_ERR_BAD_INPUT, "patches: distribute DOFs first");
+    if (first < 0 || count < 0 || first + count > c->n_active) return set_err(c, TF_ERR_BAD_INPUT, "patches: range outside the active tets");
+    TF_TRY(ensure_tables(c));
+    if (count == 0) return TF_OK;
+    DBuf<int32_t> i32;
+    DBuf<double> f64;
+    TF_TRY(ensure(c, i32, (size_t)count * (1 + 48 + 16 + 1)));
+    TF_TRY(ensure(c, f64, (size_t)count * 160));
+    int32_t* dnf = i32.p;
+    int32_t* dfac = dnf + count;
+    int32_t* dbnd = dfac + count * 48;
+    int32_t* dnv = dbnd + count * 16;
+    TF_CUDA(c, cudaMemsetAsync(i32.p, 0, sizeof(int32_t) * (size_t)count * 66, c->stream));
+    TF_CUDA(c, cudaMemsetAsync(c->status.p, 0, 4 * sizeof(int), c->stream));
+    k_patch_dump<<<grid_for(c, count), 128, 0, c->stream>>>(c->mesh, c->ls_vert.p, c->ls_edge.p, c->active.p + first, count,
+                                                            dnf, dfac, dbnd, dnv, f64.p, c->status.p);
+    ++c->launches;
+    TF_CUDA(c, cudaGetLastError());
+    int st = 0;
+    TF_TRY(sync_status(c, &st));
+    if (st == 0) {
+        if (nf) TF_CUDA(c, cudaMemcpy(nf, dnf, sizeof(int32_t) * count, cudaMemcpyDeviceToHost));
+        if (facets) TF_CUDA(c, cudaMemcpy(facets, dfac, sizeof(int32_t) * count * 48, cudaMemcpyDeviceToHost));
+        if (bnd) TF_CUDA(c, cudaMemcpy(bnd, dbnd, sizeof(int32_t) * count * 16, cudaMemcpyDeviceToHost));
+        if (nverts) TF_CUDA(c, cudaMemcpy(nverts, dnv, sizeof(int32_t) * count, cudaMemcpyDeviceToHost));
+        if (verts) TF_CUDA(c, cudaMemcpy(verts, f64.p, sizeof(double) * count * 160, cudaMemcpyDeviceToHost));
+    }
+    release(i32);
+    release(f64);
+    if (st) return set_err(c, st, "RefPatchCL::instance: found a full body in the zero level set");
+    return TF_OK;
+}
+
+// ---------------------------------------------------------------------------
 // legacy numbering: CreateNumbOnInterfaceVertex (misc/problem.cpp:443-505)
 // A vertex gets its number at the first tet (triangulation order) whose patch
 // carries a Quad2 integral of lambda_i^2 above omit_bound * (6|T|)^{4/3};

@@ -105,6 +105,7 @@ int tf_destroy(tf_context* t) {
         tf::release(c->sell_ptr[i]);
         tf::release(c->sell_col[i]);
         tf::release(c->sell_src[i]);
+        tf::release(c->sell_perm[i]);
         tf::release(c->sell_v64[i]);
         tf::release(c->sell_v32[i]);
     }
@@ -290,6 +291,13 @@ int tf_dofs_download(tf_context* t, int32_t* dof_vert, int32_t* dof_edge, int32_
         TF_CUDA(c, cudaMemcpyAsync(loc2glo, c->loc2glo.p, sizeof(int32_t) * c->n_active * nl, cudaMemcpyDeviceToHost, c->stream));
     TF_CUDA(c, cudaStreamSynchronize(c->stream));
     return TF_OK;
+}
+
+int tf_patches_download(tf_context* t, int64_t first, int64_t count, int32_t* nf, int32_t* facets, int32_t* boundary,
+                        int32_t* nverts, double* verts) {
+    CTX_CHECK(t);
+    cudaSetDevice(t->c.device);
+    return tf::patch_dump(&t->c, first, count, nf, facets, boundary, nverts, verts);
 }
 
 int tf_setup_fe_system(tf_context* t, unsigned forms, int rhs_kind, const double* rhs_par, int npar, int64_t* nnz) {

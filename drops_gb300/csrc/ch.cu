@@ -12,7 +12,8 @@ namespace tf {
 int ensure_sell(Context* c, CSR& A, bool fp32);
 
 // one pass over the rows of M (SELL-32): M chi and M f0'(chi) together
-__global__ void k_ch_rhs(int64_t m, int64_t nslices, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+__global__ void k_ch_rhs(int64_t m, int64_t nslices, const int32_t* __restrict__ perm, const int32_t* __restrict__ ptr,
+                         const int32_t* __restrict__ col,
                          const double* __restrict__ val, const double* __restrict__ x, const double* __restrict__ f,
                          double alpha, double beta, double xi, double* __restrict__ rhs, double* __restrict__ chi_out) {
     const int lane = threadIdx.x & 31;
@@ -28,8 +29,8 @@ __global__ void k_ch_rhs(int64_t m, int64_t nslices, const int32_t* __restrict__
             mc += v * cj;
             mf += v * (xi * 2. * cj * (1. - cj) * (1. - 2. * cj));
         }
-        const int64_t row = s * 32 + lane;
-        if (row < m) {
+        const int32_t row = perm[s * 32 + lane];
+        if (row >= 0) {
             rhs[row] = (f ? f[row] : 0.) + alpha * mc;
             rhs[row + m] = beta * mc - mf;
             chi_out[row] = x[row];
@@ -55,7 +56,7 @@ int ch_steps(Context* c, int nsteps, double dt, double mob, double eps, double b
     for (int step = 0; step < nsteps; ++step) {
         double* X = c->vecs[TF_VEC_X].p;
         k_ch_rhs<<<grid_for(c, M.sell.nslices * 32), kBlock, 0, c->stream>>>(
-            m, M.sell.nslices, M.sell.ptr, M.sell.col, M.sell.v64, X, f, 1.0 / dt, beta_s, xi, c->vecs[TF_VEC_B].p,
+            m, M.sell.nslices, M.sell.perm, M.sell.ptr, M.sell.col, M.sell.v64, X, f, 1.0 / dt, beta_s, xi, c->vecs[TF_VEC_B].p,
             c->vecs[TF_VEC_CHI].p);
         ++c->launches;
         TF_CUDA(c, cudaGetLastError());

@@ -2,52 +2,26 @@
 // Cahn-Hilliard block matrix, persistent Jacobi-PCG (FP64 and FP32), mixed-
 // precision iterative refinement and restarted GMRES.
 //
+// GB300 note: FP64 arithmetic runs at a small fraction of the FP32 rate, so
+// these kernels spend FP64 operations only where the result needs them (the
+// FP64 SpMV of the FP64 solvers, their vector updates and reductions).  The
+// FP32 inner solver of the mixed-precision path does all of its arithmetic in
+// FP32; only per-warp partial sums are widened to FP64.
+//
 // The PCG of num/krylovsolver.h:107-189 runs as ONE cooperative kernel: every
 // block owns a slice of rows, a grid barrier separates the two phases of an
 // iteration (q = A p with <q,p>;  x,r,z updates with <r,r>,<z,r>), and the
 // search-direction update p = z + beta p is fused into the next SpMV (double
-// buffered).  Dot products are compensated (TwoSum) and reduced over blocks in
-// a fixed order, so every block computes bit-identical scalars and all blocks
-// take the same convergence decision.  Every barrier wait is bounded: a block
-// that waits too long raises TF_ERR_WATCHDOG and the kernel returns.
-#include <cooperative_groups.h>
-
+// buffered).  Dot products are reduced over warps, blocks and then over all
+// blocks in one fixed order, so every block computes bit-identical scalars and
+// all blocks take the same convergence decision.  Every barrier wait is
+// bounded: a block that waits too long raises TF_ERR_WATCHDOG and the kernel
+// returns.
 #include <cmath>
 
 #include "tf_internal.cuh"
 
 namespace tf {
-
-// ---------------------------------------------------------------------------
-// compensated summation
-// ---------------------------------------------------------------------------
-struct DD {
-    double s, c;
-};
-__device__ __forceinline__ void two_sum_add(DD& a, double b) {
-    const double s = a.s + b;
-    const double bp = s - a.s;
-    const double err = (a.s - (s - bp)) + (b - bp);
-    a.s = s;
-    a.c += err;
-}
-__device__ __forceinline__ DD dd_add(DD a, DD b) {
-    DD r = a;
-    two_sum_add(r, b.s);
-    r.c += b.c;
-    return r;
-}
-__device__ __forceinline__ DD warp_dd_sum(DD v) {
-    for (int o = 16; o > 0; o >>= 1) {
-        DD w;
-        w.s = __shfl_xor_sync(0xffffffffu, v.s, o);
-        w.c = __shfl_xor_sync(0xffffffffu, v.c, o);
-        // order-independent pairing: combine the lower lane's value first
-        const int lane = threadIdx.x & 31;
-        v = (lane & o) ? dd_add(w, v) : dd_add(v, w);
-    }
-    return v;
-}
 
 // ---------------------------------------------------------------------------
 // grid barrier with a bounded wait
@@ -60,7 +34,6 @@ struct GridSync {
 constexpr long long kSpinLimit = 20000000;  // ~1-2 s with the backoff below
 
 __device__ __forceinline__ bool grid_barrier(const GridSync& g) {
-    __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned* vgen = g.gen;
@@ -77,98 +50,131 @@ __device__ __forceinline__ bool grid_barrier(const GridSync& g) {
                     atomicCAS(g.status, 0, TF_ERR_WATCHDOG);
                     break;
                 }
-                if (spins > 64) __nanosleep(64);
+                if (spins > 256) __nanosleep(32);
             }
         }
         __threadfence();
     }
     __syncthreads();
-    return *((volatile int*)g.status) == 0;
+    __shared__ int st;
+    if (threadIdx.x == 0) st = *((volatile int*)g.status);
+    __syncthreads();
+    return st == 0;
 }
 
 // ---------------------------------------------------------------------------
-// block-level reductions into per-block partials, and their global reduction
+// reductions: warp xor-trees (every lane ends with the same sum), one FP64
+// partial per block, and a fixed-order sum of all partials in every block
 // ---------------------------------------------------------------------------
-template <int NV>
-__device__ void block_partials(DD (&v)[NV], double* part /* [nblocks][NV][2] */) {
-    __shared__ DD red[NV][32];
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int NV, class T>
+__device__ void block_partials(T (&v)[NV], double* part /* [nblocks][NV] */) {
+    __shared__ double red[NV][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int k = 0; k < NV; ++k) {
-        DD x = warp_dd_sum(v[k]);
-        if (lane == 0) red[k][w] = x;
+        const T x = warp_sum(v[k]);
+        if (lane == 0) red[k][w] = (double)x;
     }
     __syncthreads();
-    if (w == 0) {
+    if (w == 0)
         for (int k = 0; k < NV; ++k) {
-            DD x = lane < nw ? red[k][lane] : DD{0., 0.};
-            x = warp_dd_sum(x);
-            if (lane == 0) {
-                part[((size_t)blockIdx.x * NV + k) * 2] = x.s;
-                part[((size_t)blockIdx.x * NV + k) * 2 + 1] = x.c;
-            }
+            double x = lane < nw ? red[k][lane] : 0.;
+            x = warp_sum(x);
+            if (lane == 0) part[(size_t)blockIdx.x * NV + k] = x;
         }
-    }
     __syncthreads();
 }
 
-// every block reduces all partials in the same fixed order
 template <int NV>
 __device__ void grid_reduce(const double* part, double (&out)[NV]) {
-    __shared__ DD red[NV][32];
+    __shared__ double red[NV][32];
     __shared__ double res[NV];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int k = 0; k < NV; ++k) {
-        DD x{0., 0.};
-        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
-            DD y{__ldcg(part + ((size_t)b * NV + k) * 2), __ldcg(part + ((size_t)b * NV + k) * 2 + 1)};
-            x = dd_add(x, y);
-        }
-        x = warp_dd_sum(x);
+        double x = 0.;
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) x += __ldcg(part + (size_t)b * NV + k);
+        x = warp_sum(x);
         if (lane == 0) red[k][w] = x;
     }
     __syncthreads();
-    if (w == 0) {
+    if (w == 0)
         for (int k = 0; k < NV; ++k) {
-            DD x = lane < nw ? red[k][lane] : DD{0., 0.};
-            x = warp_dd_sum(x);
-            if (lane == 0) res[k] = x.s + x.c;
+            double x = lane < nw ? red[k][lane] : 0.;
+            x = warp_sum(x);
+            if (lane == 0) res[k] = x;
         }
-    }
     __syncthreads();
     for (int k = 0; k < NV; ++k) out[k] = res[k];
     __syncthreads();
 }
 
 // ---------------------------------------------------------------------------
-// SELL-32 layout and SpMV (y_Ax, num/spmat.h:1684-1709)
+// SELL-32-sigma layout and SpMV (y_Ax, num/spmat.h:1684-1709)
 // ---------------------------------------------------------------------------
-__global__ void k_sell_width(int64_t m, int64_t nslices, const int32_t* __restrict__ rowptr, int32_t* __restrict__ w) {
+constexpr int kSigma = 512;  // rows sorted by length inside windows of 512
+
+// one block of kSigma threads per window: bitonic sort of (descending length, row)
+__global__ void __launch_bounds__(kSigma) k_sell_sort(int64_t m, const int32_t* __restrict__ rowptr,
+                                                      int32_t* __restrict__ perm) {
+    __shared__ uint64_t key[kSigma];
+    const int t = threadIdx.x;
+    const int64_t row = (int64_t)blockIdx.x * kSigma + t;
+    if (row < m) {
+        const uint32_t len = (uint32_t)(rowptr[row + 1] - rowptr[row]);
+        key[t] = ((uint64_t)(0x7fffffffu - len) << 32) | (uint64_t)(uint32_t)row;
+    } else {
+        key[t] = ~0ull;
+    }
+    __syncthreads();
+    for (int size = 2; size <= kSigma; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            const int partner = t ^ stride;
+            if (partner > t) {
+                const bool up = (t & size) == 0;
+                const uint64_t a = key[t], b = key[partner];
+                if ((a > b) == up) {
+                    key[t] = b;
+                    key[partner] = a;
+                }
+            }
+            __syncthreads();
+        }
+    perm[(int64_t)blockIdx.x * kSigma + t] = key[t] == ~0ull ? -1 : (int32_t)(key[t] & 0xffffffffu);
+}
+
+__global__ void k_sell_width(int64_t nslices, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ perm,
+                             int32_t* __restrict__ w) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t s = warp; s < nslices; s += nwarp) {
-        const int64_t row = s * 32 + lane;
-        int len = row < m ? rowptr[row + 1] - rowptr[row] : 0;
+        const int32_t row = perm[s * 32 + lane];
+        int len = row >= 0 ? rowptr[row + 1] - rowptr[row] : 0;
         len = __reduce_max_sync(0xffffffffu, len);
         if (lane == 0) w[s] = 32 * len;
     }
 }
 
-__global__ void k_sell_fill(int64_t m, int64_t nslices, const int32_t* __restrict__ rowptr,
-                            const int32_t* __restrict__ colind, const int32_t* __restrict__ ptr,
+__global__ void k_sell_fill(int64_t nslices, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
+                            const int32_t* __restrict__ perm, const int32_t* __restrict__ ptr,
                             int32_t* __restrict__ col, int32_t* __restrict__ src) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t s = warp; s < nslices; s += nwarp) {
-        const int64_t row = s * 32 + lane;
+        const int32_t row = perm[s * 32 + lane];
         const int32_t p0 = ptr[s], w = (ptr[s + 1] - p0) >> 5;
         int32_t rs = 0, len = 0;
-        if (row < m) {
+        if (row >= 0) {
             rs = rowptr[row];
             len = rowptr[row + 1] - rs;
         }
-        const int32_t pad_col = row < m ? (int32_t)row : 0;
+        const int32_t pad_col = row >= 0 ? row : 0;
         for (int32_t k = 0; k < w; ++k) {
             const int32_t pos = p0 + k * 32 + lane;
             if (k < len) {
@@ -201,22 +207,27 @@ int ensure_sell(Context* c, CSR& A, bool fp32) {
     const int id = mat_index(c, A);
     Sell& S = A.sell;
     if (S.pattern_gen != A.pattern_gen || !S.ptr) {
-        const int64_t ns = (A.m + 31) / 32;
+        const int64_t nwin = (A.m + kSigma - 1) / kSigma;
+        const int64_t ns = nwin * (kSigma / 32);
+        TF_TRY(ensure(c, c->sell_perm[id], (size_t)(ns * 32)));
         TF_TRY(ensure(c, c->sell_ptr[id], (size_t)ns + 1));
         TF_TRY(ensure(c, c->scratch, sizeof(int32_t) * (size_t)(ns + 1)));
         int32_t* w = (int32_t*)c->scratch.p;
-        k_sell_width<<<grid_for(c, ns * 32), kBlock, 0, c->stream>>>(A.m, ns, A.rowptr, w);
-        ++c->launches;
+        k_sell_sort<<<(unsigned)nwin, kSigma, 0, c->stream>>>(A.m, A.rowptr, c->sell_perm[id].p);
+        k_sell_width<<<grid_for(c, ns * 32), kBlock, 0, c->stream>>>(ns, A.rowptr, c->sell_perm[id].p, w);
+        c->launches += 2;
         int64_t npad = 0;
         TF_TRY(exclusive_scan_i32_to_i32(c, w, c->sell_ptr[id].p, ns, &npad));
         TF_TRY(ensure(c, c->sell_col[id], (size_t)(npad > 0 ? npad : 1)));
         TF_TRY(ensure(c, c->sell_src[id], (size_t)(npad > 0 ? npad : 1)));
-        k_sell_fill<<<grid_for(c, ns * 32), kBlock, 0, c->stream>>>(A.m, ns, A.rowptr, A.colind, c->sell_ptr[id].p,
-                                                                     c->sell_col[id].p, c->sell_src[id].p);
+        k_sell_fill<<<grid_for(c, ns * 32), kBlock, 0, c->stream>>>(ns, A.rowptr, A.colind, c->sell_perm[id].p,
+                                                                     c->sell_ptr[id].p, c->sell_col[id].p,
+                                                                     c->sell_src[id].p);
         ++c->launches;
         TF_CUDA(c, cudaGetLastError());
         S.nslices = ns;
         S.npad = npad;
+        S.perm = c->sell_perm[id].p;
         S.ptr = c->sell_ptr[id].p;
         S.col = c->sell_col[id].p;
         S.src = c->sell_src[id].p;
@@ -242,30 +253,30 @@ int ensure_sell(Context* c, CSR& A, bool fp32) {
     return TF_OK;
 }
 
-// Row 32s+lane of a SELL-32 matrix times the vector given by xload(col);
-// four columns are loaded before they are used, so each lane keeps several
-// independent gathers in flight.  Terms are summed in CSR order.
+// Slot row of a SELL matrix times the vector given by xload(col), accumulated
+// in T; four columns are loaded before they are used, so each lane keeps
+// several independent gathers in flight.  Terms are summed in CSR order.
 template <class T, class XL>
-__device__ __forceinline__ double sell_row(const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
-                                           const T* __restrict__ val, int64_t s, int lane, XL xload) {
+__device__ __forceinline__ T sell_row(const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                                      const T* __restrict__ val, int64_t s, int lane, XL xload) {
     const int32_t p0 = __ldg(ptr + s);
     const int32_t w = (__ldg(ptr + s + 1) - p0) >> 5;
     const int32_t* cp = col + p0 + lane;
     const T* vp = val + p0 + lane;
-    double acc = 0.;
+    T acc = T(0);
     int32_t k = 0;
     for (; k + 4 <= w; k += 4) {
         const int32_t c0 = __ldg(cp + 32 * k), c1 = __ldg(cp + 32 * (k + 1)), c2 = __ldg(cp + 32 * (k + 2)),
                       c3 = __ldg(cp + 32 * (k + 3));
-        const double v0 = (double)__ldg(vp + 32 * k), v1 = (double)__ldg(vp + 32 * (k + 1)),
-                     v2 = (double)__ldg(vp + 32 * (k + 2)), v3 = (double)__ldg(vp + 32 * (k + 3));
-        const double x0 = xload(c0), x1 = xload(c1), x2 = xload(c2), x3 = xload(c3);
+        const T v0 = __ldg(vp + 32 * k), v1 = __ldg(vp + 32 * (k + 1)), v2 = __ldg(vp + 32 * (k + 2)),
+                v3 = __ldg(vp + 32 * (k + 3));
+        const T x0 = xload(c0), x1 = xload(c1), x2 = xload(c2), x3 = xload(c3);
         acc += v0 * x0;
         acc += v1 * x1;
         acc += v2 * x2;
         acc += v3 * x3;
     }
-    for (; k < w; ++k) acc += (double)__ldg(vp + 32 * k) * xload(__ldg(cp + 32 * k));
+    for (; k < w; ++k) acc += __ldg(vp + 32 * k) * xload(__ldg(cp + 32 * k));
     return acc;
 }
 
@@ -275,13 +286,14 @@ __device__ __forceinline__ double sell_row(const int32_t* __restrict__ ptr, cons
     for (int64_t s = warp__; s < (nslices); s += nwarp__)
 
 template <class T>
-__global__ void k_spmv(int64_t m, int64_t nslices, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
-                       const T* __restrict__ val, const T* __restrict__ x, T* __restrict__ y) {
+__global__ void k_spmv(int64_t nslices, const int32_t* __restrict__ perm, const int32_t* __restrict__ ptr,
+                       const int32_t* __restrict__ col, const T* __restrict__ val, const T* __restrict__ x,
+                       T* __restrict__ y) {
     const int lane = threadIdx.x & 31;
     TF_SLICE_LOOP(nslices, s) {
-        const double a = sell_row<T>(ptr, col, val, s, lane, [&](int32_t j) { return (double)__ldcg(x + j); });
-        const int64_t row = s * 32 + lane;
-        if (row < m) y[row] = (T)a;
+        const T a = sell_row<T>(ptr, col, val, s, lane, [&](int32_t j) { return __ldcg(x + j); });
+        const int32_t row = perm[s * 32 + lane];
+        if (row >= 0) y[row] = a;
     }
 }
 
@@ -289,7 +301,7 @@ int spmv(Context* c, const CSR& Ac, const double* x, double* y) {
     CSR& A = const_cast<CSR&>(Ac);
     TF_TRY(ensure_sell(c, A, false));
     TimedLaunch tl(c, TF_K_SPMV);
-    k_spmv<double><<<grid_for(c, A.sell.nslices * 32), kBlock, 0, c->stream>>>(A.m, A.sell.nslices, A.sell.ptr,
+    k_spmv<double><<<grid_for(c, A.sell.nslices * 32), kBlock, 0, c->stream>>>(A.sell.nslices, A.sell.perm, A.sell.ptr,
                                                                                A.sell.col, A.sell.v64, x, y);
     ++c->launches;
     TF_CUDA(c, cudaGetLastError());
@@ -437,6 +449,7 @@ int ch_block(Context* c, double alpha, double mob, double rho, double eps2, doub
 template <class T>
 struct PcgArgs {
     int64_t m, nslices;
+    const int32_t* perm;
     const int32_t* ptr;
     const int32_t* col;
     const T* val;
@@ -448,7 +461,7 @@ struct PcgArgs {
     T* p0;
     T* p1;
     T* q;
-    double* part;  // [2][nblocks][3][2]
+    double* part;  // [2][nblocks][3]
     GridSync gs;
     int max_iter;
     double tol;
@@ -463,26 +476,26 @@ template <class T>
 __global__ void __launch_bounds__(kKryThreads, 4) k_pcg(PcgArgs<T> a) {
     const int lane = threadIdx.x & 31;
     double* partA = a.part;
-    double* partB = a.part + (size_t)gridDim.x * 3 * 2;
+    double* partB = a.part + (size_t)gridDim.x * 3;
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
 
     // r = b - A x ; z = r / d ; p0 = z ; partials <r,r>, <b,b>, <z,r>
     {
-        DD v[3] = {{0, 0}, {0, 0}, {0, 0}};
+        T v[3] = {T(0), T(0), T(0)};
         const T* x = a.x;
         TF_SLICE_LOOP(a.nslices, s) {
-            const double ax = sell_row<T>(a.ptr, a.col, a.val, s, lane, [&](int32_t j) { return (double)__ldcg(x + j); });
-            const int64_t row = s * 32 + lane;
-            if (row < a.m) {
-                const double bi = (double)a.b[row];
-                const T ri = (T)(bi - ax);
-                const T zi = (T)((double)ri / (double)a.diag[row]);
+            const T ax = sell_row<T>(a.ptr, a.col, a.val, s, lane, [&](int32_t j) { return __ldcg(x + j); });
+            const int32_t row = __ldg(a.perm + s * 32 + lane);
+            if (row >= 0) {
+                const T bi = a.b[row];
+                const T ri = bi - ax;
+                const T zi = ri / a.diag[row];
                 a.r[row] = ri;
                 a.z[row] = zi;
                 a.p0[row] = zi;
-                two_sum_add(v[0], (double)ri * (double)ri);
-                two_sum_add(v[1], bi * bi);
-                two_sum_add(v[2], (double)zi * (double)ri);
+                v[0] += ri * ri;
+                v[1] += bi * bi;
+                v[2] += zi * ri;
             }
         }
         block_partials<3>(v, partA);
@@ -501,26 +514,24 @@ __global__ void __launch_bounds__(kKryThreads, 4) k_pcg(PcgArgs<T> a) {
         }
         return;
     }
-    double beta = 0.;
+    T beta = T(0);
     T* pc = a.p0;  // previous direction (beta = 0 in the first iteration)
     T* pn = a.p1;
     for (int it = 1; it <= a.max_iter; ++it) {
         // phase A: p_new = z + beta p_old ; q = A p_new ; <q, p_new>
         {
-            DD v[1] = {{0, 0}};
+            T v[1] = {T(0)};
             const T* z = a.z;
             const T* po = pc;
             TF_SLICE_LOOP(a.nslices, s) {
-                const double acc = sell_row<T>(a.ptr, a.col, a.val, s, lane, [&](int32_t j) {
-                    return (double)(T)((double)__ldcg(z + j) + beta * (double)__ldcg(po + j));
-                });
-                const int64_t row = s * 32 + lane;
-                if (row < a.m) {
-                    const T pi = (T)((double)__ldcg(z + row) + beta * (double)__ldcg(po + row));
-                    const T qi = (T)acc;
+                const T acc = sell_row<T>(a.ptr, a.col, a.val, s, lane,
+                                          [&](int32_t j) { return __ldcg(z + j) + beta * __ldcg(po + j); });
+                const int32_t row = __ldg(a.perm + s * 32 + lane);
+                if (row >= 0) {
+                    const T pi = __ldcg(z + row) + beta * __ldcg(po + row);
                     pn[row] = pi;
-                    a.q[row] = qi;
-                    two_sum_add(v[0], (double)qi * (double)pi);
+                    a.q[row] = acc;
+                    v[0] += acc * pi;
                 }
             }
             block_partials<1>(v, partA);
@@ -528,19 +539,18 @@ __global__ void __launch_bounds__(kKryThreads, 4) k_pcg(PcgArgs<T> a) {
         if (!grid_barrier(a.gs)) return;
         double lam[1];
         grid_reduce<1>(partA, lam);
-        const double alpha = rho / lam[0];
+        const T alpha = (T)(rho / lam[0]);
         // phase B: x += alpha p ; r -= alpha q ; z = r / d ; <r,r>, <z,r>
         {
-            DD v[2] = {{0, 0}, {0, 0}};
+            T v[2] = {T(0), T(0)};
             for (int64_t i = tid; i < a.m; i += nth) {
-                const double pi = (double)__ldcg(pn + i);
-                a.x[i] = (T)((double)a.x[i] + alpha * pi);
-                const T ri = (T)((double)a.r[i] + (-alpha) * (double)__ldcg(a.q + i));
-                const T zi = (T)((double)ri / (double)a.diag[i]);
+                a.x[i] += alpha * __ldcg(pn + i);
+                const T ri = a.r[i] - alpha * __ldcg(a.q + i);
+                const T zi = ri / a.diag[i];
                 a.r[i] = ri;
                 a.z[i] = zi;
-                two_sum_add(v[0], (double)ri * (double)ri);
-                two_sum_add(v[1], (double)zi * (double)ri);
+                v[0] += ri * ri;
+                v[1] += zi * ri;
             }
             block_partials<2>(v, partB);
         }
@@ -557,7 +567,7 @@ __global__ void __launch_bounds__(kKryThreads, 4) k_pcg(PcgArgs<T> a) {
         }
         const double rho1 = rho;
         rho = s2[1];
-        beta = rho / rho1;
+        beta = (T)(rho / rho1);
         T* tmp = pc;
         pc = pn;
         pn = tmp;
@@ -590,7 +600,7 @@ static int run_pcg_kernel(Context* c, const CSR& A, const T* val, const T* diag,
     const void* fn = (const void*)k_pcg<T>;
     int blocks = 0;
     TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks));
-    TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 3 * 2 * 2));
+    TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 3 * 2));
     TF_TRY(ensure(c, c->kry_bar, 2));
     TF_TRY(ensure(c, c->kry_iters, 1));
     TF_TRY(ensure(c, c->kry_resid, 1));
@@ -599,6 +609,7 @@ static int run_pcg_kernel(Context* c, const CSR& A, const T* val, const T* diag,
     PcgArgs<T> a;
     a.m = A.m;
     a.nslices = A.sell.nslices;
+    a.perm = A.sell.perm;
     a.ptr = A.sell.ptr;
     a.col = A.sell.col;
     a.val = val;
@@ -633,39 +644,41 @@ static int run_pcg_kernel(Context* c, const CSR& A, const T* val, const T* diag,
 }
 
 // residual r = b - A x (FP64) with <r,r>, <b,b> partials
-__global__ void k_residual(int64_t m, int64_t nslices, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
-                           const double* __restrict__ val, const double* __restrict__ b, const double* __restrict__ x,
-                           double* __restrict__ r, double* __restrict__ part) {
+__global__ void k_residual(int64_t nslices, const int32_t* __restrict__ perm, const int32_t* __restrict__ ptr,
+                           const int32_t* __restrict__ col, const double* __restrict__ val, const double* __restrict__ b,
+                           const double* __restrict__ x, double* __restrict__ r, double* __restrict__ part) {
     const int lane = threadIdx.x & 31;
-    DD v[2] = {{0, 0}, {0, 0}};
+    double v[2] = {0., 0.};
     TF_SLICE_LOOP(nslices, s) {
         const double ax = sell_row<double>(ptr, col, val, s, lane, [&](int32_t j) { return __ldcg(x + j); });
-        const int64_t row = s * 32 + lane;
-        if (row < m) {
+        const int32_t row = perm[s * 32 + lane];
+        if (row >= 0) {
             const double ri = b[row] - ax;
             r[row] = ri;
-            two_sum_add(v[0], ri * ri);
-            two_sum_add(v[1], b[row] * b[row]);
+            v[0] += ri * ri;
+            v[1] += b[row] * b[row];
         }
     }
     block_partials<2>(v, part);
 }
 __global__ void k_reduce_partials(int nblocks, const double* __restrict__ part, double* __restrict__ out) {
-    // one block; same fixed order as grid_reduce
-    __shared__ DD red[2][32];
+    double o[2];
+    // one block; the same fixed order as grid_reduce
+    __shared__ double red[2][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int k = 0; k < 2; ++k) {
-        DD x{0., 0.};
-        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) x = dd_add(x, DD{part[(b * 2 + k) * 2], part[(b * 2 + k) * 2 + 1]});
-        x = warp_dd_sum(x);
+        double x = 0.;
+        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) x += part[b * 2 + k];
+        x = warp_sum(x);
         if (lane == 0) red[k][w] = x;
     }
     __syncthreads();
     if (w == 0)
         for (int k = 0; k < 2; ++k) {
-            DD x = lane < nw ? red[k][lane] : DD{0., 0.};
-            x = warp_dd_sum(x);
-            if (lane == 0) out[k] = x.s + x.c;
+            double x = lane < nw ? red[k][lane] : 0.;
+            x = warp_sum(x);
+            o[k] = x;
+            if (lane == 0) out[k] = o[k];
         }
 }
 __global__ void k_scale_to_f32(int64_t n, const double* __restrict__ a, double s, float* __restrict__ b, float* __restrict__ x0) {
@@ -708,14 +721,14 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
     double* r64 = c->kry64.p;
     double* part = c->kry64.p + m;
     const int rblocks = (int)std::min<int64_t>((A.sell.nslices * 32 + kBlock - 1) / kBlock, (int64_t)c->num_sms * 8);
-    if ((int64_t)rblocks * 4 + 2 > 4 * m) return set_err(c, TF_ERR_CAPACITY, "pcg: matrix too small for mixed precision");
-    double* sums = part + (size_t)rblocks * 4;
+    if ((int64_t)rblocks * 2 + 2 > 4 * m) return set_err(c, TF_ERR_CAPACITY, "pcg: matrix too small for mixed precision");
+    double* sums = part + (size_t)rblocks * 2;
     int total_inner = 0;
     double res = 0.;
     const int max_outer = 60;
     for (int outer = 0; outer <= max_outer; ++outer) {
-        k_residual<<<rblocks, kBlock, 0, c->stream>>>(m, A.sell.nslices, A.sell.ptr, A.sell.col, A.sell.v64, b, x, r64,
-                                                     part);
+        k_residual<<<rblocks, kBlock, 0, c->stream>>>(A.sell.nslices, A.sell.perm, A.sell.ptr, A.sell.col, A.sell.v64, b,
+                                                     x, r64, part);
         k_reduce_partials<<<1, 256, 0, c->stream>>>(rblocks, part, sums);
         c->launches += 2;
         double h[2];
@@ -765,6 +778,7 @@ constexpr int kMaxRestart = 64;
 
 struct GmresArgs {
     int64_t m, nslices;
+    const int32_t* perm;
     const int32_t* ptr;
     const int32_t* col;
     const double* val;
@@ -772,7 +786,7 @@ struct GmresArgs {
     const double* b;
     double* x;
     double* V;     // [R][m] unnormalised basis
-    double* part;  // [2][nblocks][2][2]
+    double* part;  // [2][nblocks][2]
     GridSync gs;
     int R;         // restart
     int left;      // 1: left preconditioning, 0: right
@@ -792,27 +806,27 @@ __global__ void __launch_bounds__(kKryThreads, 4) k_gmres(GmresArgs a) {
     const int64_t m = a.m;
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
     double* partA = a.part;
-    double* partB = a.part + (size_t)gridDim.x * 2 * 2;
+    double* partB = a.part + (size_t)gridDim.x * 2;
     int flip = 0;
     auto P = [&]() { flip ^= 1; return flip ? partB : partA; };
 
     // r0 = b - A x (right) or M^{-1}(b - A x) (left) into V_0; <r,r>, |b| or |M^{-1} b|
     {
         double* pp = P();
-        DD v[2] = {{0, 0}, {0, 0}};
+        double v[2] = {0., 0.};
         const double* x0 = a.x;
         TF_SLICE_LOOP(a.nslices, sl) {
             const double ax = sell_row<double>(a.ptr, a.col, a.val, sl, lane, [&](int32_t j) { return __ldcg(x0 + j); });
-            const int64_t row = sl * 32 + lane;
-            if (row < m) {
+            const int32_t row = __ldg(a.perm + sl * 32 + lane);
+            if (row >= 0) {
                 double r = a.b[row] - ax, bb = a.b[row];
                 if (a.left) {
                     r = r / a.diag[row];
                     bb = bb / a.diag[row];
                 }
                 a.V[row] = r;
-                two_sum_add(v[0], r * r);
-                two_sum_add(v[1], bb * bb);
+                v[0] += r * r;
+                v[1] += bb * bb;
             }
         }
         block_partials<2>(v, pp);
@@ -858,7 +872,7 @@ __global__ void __launch_bounds__(kKryThreads, 4) k_gmres(GmresArgs a) {
                 // w = A M^{-1} v_i (right) or M^{-1} A v_i (left); <w, v_0>
                 {
                     double* pq = P();
-                    DD v1[1] = {{0, 0}};
+                    double v1[1] = {0.};
                     const bool left = a.left;
                     const double* dg = a.diag;
                     const double* Zp = a.binv ? a.Z : nullptr;
@@ -868,11 +882,11 @@ __global__ void __launch_bounds__(kKryThreads, 4) k_gmres(GmresArgs a) {
                             const double vj = sci * __ldcg(Vi + j);
                             return left ? vj : vj / __ldg(dg + j);
                         });
-                        const int64_t row = s2 * 32 + lane;
-                        if (row < m) {
+                        const int32_t row = __ldg(a.perm + s2 * 32 + lane);
+                        if (row >= 0) {
                             if (a.left) acc = acc / a.diag[row];
                             W[row] = acc;
-                            two_sum_add(v1[0], acc * (sc0 * __ldcg(a.V + row)));
+                            v1[0] += acc * (sc0 * __ldcg(a.V + row));
                         }
                     }
                     block_partials<1>(v1, pq);
@@ -889,11 +903,11 @@ __global__ void __launch_bounds__(kKryThreads, 4) k_gmres(GmresArgs a) {
                     const double* Vk = a.V + (size_t)k * m;
                     const double* Vn = k < i ? a.V + (size_t)(k + 1) * m : nullptr;
                     const double scn = k < i ? sc[k + 1] : 0.;
-                    DD v1[1] = {{0, 0}};
+                    double v1[1] = {0.};
                     for (int64_t e = tid; e < m; e += nth) {
                         const double w = __ldcg(W + e) - hk * __ldcg(Vk + e);
                         W[e] = w;
-                        two_sum_add(v1[0], k < i ? w * (scn * __ldcg(Vn + e)) : w * w);
+                        v1[0] += k < i ? w * (scn * __ldcg(Vn + e)) : w * w;
                     }
                     block_partials<1>(v1, pq);
                     if (!grid_barrier(a.gs)) return;
@@ -976,16 +990,16 @@ __global__ void __launch_bounds__(kKryThreads, 4) k_gmres(GmresArgs a) {
             // new residual into V_0
             {
                 double* pq = P();
-                DD v1[1] = {{0, 0}};
+                double v1[1] = {0.};
                 const double* x1 = a.x;
                 TF_SLICE_LOOP(a.nslices, s3) {
                     const double ax = sell_row<double>(a.ptr, a.col, a.val, s3, lane, [&](int32_t j) { return __ldcg(x1 + j); });
-                    const int64_t row = s3 * 32 + lane;
-                    if (row < m) {
+                    const int32_t row = __ldg(a.perm + s3 * 32 + lane);
+                    if (row >= 0) {
                         double r = a.b[row] - ax;
                         if (a.left) r = r / a.diag[row];
                         a.V[row] = r;
-                        two_sum_add(v1[0], r * r);
+                        v1[0] += r * r;
                     }
                 }
                 block_partials<1>(v1, pq);
@@ -1055,7 +1069,7 @@ int gmres_jacobi(Context* c, CSR& A, const double* b, double* x, int restart, in
     const void* fn = (const void*)k_gmres;
     int blocks = 0;
     TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks));
-    TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 2 * 2 * 2));
+    TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 2 * 2));
     TF_TRY(ensure(c, c->kry_bar, 2));
     TF_TRY(ensure(c, c->kry_iters, 1));
     TF_TRY(ensure(c, c->kry_resid, 1));
@@ -1064,6 +1078,7 @@ int gmres_jacobi(Context* c, CSR& A, const double* b, double* x, int restart, in
     GmresArgs g;
     g.m = m;
     g.nslices = A.sell.nslices;
+    g.perm = A.sell.perm;
     g.ptr = A.sell.ptr;
     g.col = A.sell.col;
     g.val = A.sell.v64;

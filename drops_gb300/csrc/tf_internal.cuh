@@ -126,11 +126,13 @@ struct DBuf {
     size_t cap = 0;  // capacity
 };
 
-// Sliced ELLPACK copy of a CSR matrix for the Krylov kernels: slices of 32
-// consecutive rows, each padded to its longest row and stored column-major so
-// that lane l of a warp streams row 32s+l with coalesced loads.
+// Sliced ELLPACK (SELL-32-sigma) copy of a CSR matrix for the Krylov kernels:
+// rows are sorted by length inside windows of 512 rows, cut into slices of 32,
+// each slice padded to its longest row and stored column-major, so that lane l
+// of a warp streams row perm[32s+l] with coalesced loads and little padding.
 struct Sell {
     int64_t nslices = 0, npad = 0;
+    int32_t* perm = nullptr; // nslices*32: row of each slot (-1: none)
     int32_t* ptr = nullptr;  // nslices+1 offsets (elements)
     int32_t* col = nullptr;  // npad
     int32_t* src = nullptr;  // npad: CSR index or -1 for padding
@@ -210,7 +212,7 @@ struct Context {
     KernelTimer timers[TF_NUM_KERNELS];
     int64_t launches = 0;
     int64_t pattern_counter = 0, block_src_gen = -1;
-    DBuf<int32_t> sell_ptr[TF_NUM_MATS], sell_col[TF_NUM_MATS], sell_src[TF_NUM_MATS];
+    DBuf<int32_t> sell_ptr[TF_NUM_MATS], sell_col[TF_NUM_MATS], sell_src[TF_NUM_MATS], sell_perm[TF_NUM_MATS];
     DBuf<double> sell_v64[TF_NUM_MATS];
     DBuf<float> sell_v32[TF_NUM_MATS];
 };
