@@ -196,16 +196,16 @@ class TraceFEM:
         self._check(self.L.tf_dofs_download(self.h, _ip(dv), _ip(de), _ip(act), _ip(l2g)))
         return dv, de, act[: self.n_active], l2g[: self.n_active * nl]
 
-    def patches(self, first=0, count=None):
-        """make_patch topology of active tets [first, first+count): list of (facets, boundary, verts)."""
-        if count is None:
-            count = self.n_active - first
+    def patches(self, tets):
+        """make_patch topology of the given tets: list of (facets, boundary, verts)."""
+        tets = np.ascontiguousarray(tets, dtype=np.int32)
+        count = tets.size
         nf = np.zeros(count, np.int32)
         fac = np.zeros((count, 16, 3), np.int32)
         bnd = np.zeros((count, 16), np.int32)
         nv = np.zeros(count, np.int32)
         ver = np.zeros((count, 40, 4))
-        self._check(self.L.tf_patches_download(self.h, C.c_int64(first), C.c_int64(count), _ip(nf), _ip(fac), _ip(bnd),
+        self._check(self.L.tf_patches_download(self.h, _ip(tets), C.c_int64(count), _ip(nf), _ip(fac), _ip(bnd),
                                                _ip(nv), _dp(ver)))
         return [(fac[i, :nf[i]], bnd[i, :nf[i]], ver[i, :nv[i]]) for i in range(count)]
 

@@ -911,23 +911,27 @@ __global__ void k_patch_dump(MeshView M, const double* __restrict__ lsv, const d
     }
 }
 
-int patch_dump(Context* c, int64_t first, int64_t count, int32_t* nf, int32_t* facets, int32_t* bnd, int32_t* nverts,
-               double* verts) {
-    if (!c->fe) return set_err(c, TF_ERR_BAD_INPUT, "patches: distribute DOFs first");
-    if (first < 0 || count < 0 || first + count > c->n_active) return set_err(c, TF_ERR_BAD_INPUT, "patches: range outside the active tets");
+int patch_dump(Context* c, const int32_t* tets, int64_t count, int32_t* nf, int32_t* facets, int32_t* bnd,
+               int32_t* nverts, double* verts) {
+    if (!c->has_mesh || !c->has_ls) return set_err(c, TF_ERR_BAD_INPUT, "patches: mesh and level set required");
+    if (count < 0 || (count > 0 && !tets)) return set_err(c, TF_ERR_BAD_INPUT, "patches: tet ids required");
+    for (int64_t i = 0; i < count; ++i)
+        if (tets[i] < 0 || tets[i] >= c->mesh.nt) return set_err(c, TF_ERR_BAD_INPUT, "patches: tet id out of range");
     TF_TRY(ensure_tables(c));
     if (count == 0) return TF_OK;
     DBuf<int32_t> i32;
     DBuf<double> f64;
-    TF_TRY(ensure(c, i32, (size_t)count * (1 + 48 + 16 + 1)));
+    TF_TRY(ensure(c, i32, (size_t)count * (1 + 48 + 16 + 1 + 1)));
     TF_TRY(ensure(c, f64, (size_t)count * 160));
+    int32_t* dtet = i32.p + count * 66;
+    TF_CUDA(c, cudaMemcpy(dtet, tets, sizeof(int32_t) * count, cudaMemcpyHostToDevice));
     int32_t* dnf = i32.p;
     int32_t* dfac = dnf + count;
     int32_t* dbnd = dfac + count * 48;
     int32_t* dnv = dbnd + count * 16;
     TF_CUDA(c, cudaMemsetAsync(i32.p, 0, sizeof(int32_t) * (size_t)count * 66, c->stream));
     TF_CUDA(c, cudaMemsetAsync(c->status.p, 0, 4 * sizeof(int), c->stream));
-    k_patch_dump<<<grid_for(c, count), 128, 0, c->stream>>>(c->mesh, c->ls_vert.p, c->ls_edge.p, c->active.p + first, count,
+    k_patch_dump<<<grid_for(c, count), 128, 0, c->stream>>>(c->mesh, c->ls_vert.p, c->ls_edge.p, dtet, count,
                                                             dnf, dfac, dbnd, dnv, f64.p, c->status.p);
     ++c->launches;
     TF_CUDA(c, cudaGetLastError());

@@ -293,11 +293,11 @@ int tf_dofs_download(tf_context* t, int32_t* dof_vert, int32_t* dof_edge, int32_
     return TF_OK;
 }
 
-int tf_patches_download(tf_context* t, int64_t first, int64_t count, int32_t* nf, int32_t* facets, int32_t* boundary,
-                        int32_t* nverts, double* verts) {
+int tf_patches_download(tf_context* t, const int32_t* tets, int64_t count, int32_t* nf, int32_t* facets,
+                        int32_t* boundary, int32_t* nverts, double* verts) {
     CTX_CHECK(t);
     cudaSetDevice(t->c.device);
-    return tf::patch_dump(&t->c, first, count, nf, facets, boundary, nverts, verts);
+    return tf::patch_dump(&t->c, tets, count, nf, facets, boundary, nverts, verts);
 }
 
 int tf_setup_fe_system(tf_context* t, unsigned forms, int rhs_kind, const double* rhs_par, int npar, int64_t* nnz) {

@@ -270,8 +270,8 @@ int fill_f64(Context* c, double* p, int64_t n, double v);
 // sub-module entry points (host)
 int mesh_materialise(Context* c, double* coords, int32_t* tet_v, int32_t* tet_e, int32_t* edge_v);
 int ensure_tables(Context* c);
-int patch_dump(Context* c, int64_t first, int64_t count, int32_t* nf, int32_t* facets, int32_t* bnd, int32_t* nverts,
-               double* verts);
+int patch_dump(Context* c, const int32_t* tets, int64_t count, int32_t* nf, int32_t* facets, int32_t* bnd,
+               int32_t* nverts, double* verts);
 int mesh_set_brick(Context* c, const double orig[3], const double e1[3], const double e2[3], const double e3[3],
                    int n1, int n2, int n3);
 int levelset_analytic(Context* c, int kind, const double* par, int npar, int p2);

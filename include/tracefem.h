@@ -138,13 +138,13 @@ int tf_create_numb_on_interface_p1(tf_context* ctx, double omit_bound, int64_t* 
 int tf_dofs_download(tf_context* ctx, int32_t* dof_vert, int32_t* dof_edge, int32_t* active_tets,
                      int32_t* loc2glo);
 
-/* Surface patches of active tets [first, first+count) exactly as
- * SPatchCL<3>::make_patch<MergeCutPolicyCL> builds them
+/* Surface patches of the tets tets[0..count) (tet ids, host array) exactly as
+ * SPatchCL<3>::make_patch<MergeCutPolicyCL> builds them from the level set
  * (geom/subtriangulation.tpp:191-228): per tet the facet count nf[count],
  * facets[count*16*3] (vertex numbers: edge cuts in discovery order, then the
  * copied zero vertices), boundary[count*16] (is_boundary_facet),
  * nverts[count] and verts[count*40*4] (barycentric coordinates).            */
-int tf_patches_download(tf_context* ctx, int64_t first, int64_t count, int32_t* nf, int32_t* facets,
+int tf_patches_download(tf_context* ctx, const int32_t* tets, int64_t count, int32_t* nf, int32_t* facets,
                         int32_t* boundary, int32_t* nverts, double* verts);
 
 /* ---- assembly ---------------------------------------------------------------- */

@@ -302,3 +302,21 @@ def test_ch_steps_parity(ctx, golden):
     assert np.linalg.norm(X[:nd] - OX[:nd]) <= 1e-8 * np.linalg.norm(OX[:nd])
     for a, b in zip(its, oits):
         assert abs(int(a) - b) <= max(5, b // 50), (its, oits)
+
+
+def test_patch_topology_bitexact(ctx, golden):
+    """make_patch facets, boundary flags and vertices of the reference's area test
+    (sphere r=0.5 on [-1,1]^3, 8^3 cubes, vertices on the sphere included) bit for bit."""
+    g = golden("area_sphere05_n8.npz")
+    brick(ctx, 8, 1.0)
+    ctx.levelset_analytic(tf.LS_SPHERE, [0, 0, 0, 0.5], True)
+    pats = ctx.patches(g["patch_tets"])
+    fo = vo = 0
+    for i, t in enumerate(g["patch_tets"]):
+        f, b, v = pats[i]
+        k, nv = int(g["n_facets"][t]), int(g["patch_nverts"][i])
+        assert np.array_equal(f, g["patch_facets"][3 * fo:3 * (fo + k)].reshape(-1, 3))
+        assert np.array_equal(b, g["patch_boundary"][fo:fo + k])
+        assert np.array_equal(v, g["patch_verts"][4 * vo:4 * (vo + nv)].reshape(-1, 4))
+        fo += k
+        vo += nv
