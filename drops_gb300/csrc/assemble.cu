@@ -230,13 +230,75 @@ __device__ inline void tet_geometry(TetGeom& g, const double ls10[10]) {
         }
 }
 
+// 1/sqrt(s) to FP64 accuracy: FP32 seed and two Newton steps
+// y <- y (3/2 - s/2 y^2) (relative error ~1e-16); FP64 division and square
+// root are long instruction sequences on the FP64 pipe, this is ~10 operations.
+__device__ inline double rsqrt_fp64(double s) {
+    if (!(s > 1e-30 && s < 1e30)) return 1.0 / sqrt(s);
+    double y = (double)rsqrtf((float)s);
+    const double h = 0.5 * s;
+    y = y * (1.5 - h * y * y);
+    y = y * (1.5 - h * y * y);
+    return y;
+}
+
 __device__ inline void unit_normal(const TetGeom& g, const double b[4], double n[3]) {
     double v[3];
     for (int r = 0; r < 3; ++r) v[r] = b[0] * g.G[0][r] + b[1] * g.G[1][r] + b[2] * g.G[2][r] + b[3] * g.G[3][r];
-    const double inv = 1.0 / sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    const double inv = rsqrt_fp64(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
     n[0] = v[0] * inv;
     n[1] = v[1] * inv;
     n[2] = v[2] * inv;
+}
+
+// Surface gradients (I - n n^T) grad(phi_i) and values phi_i at barycentric b.
+// grad(phi_i) = sum_v c_iv(b) grad(lambda_v) with at most two terms (P2:
+// vertex i: (4 b_i - 1) grad(lambda_i); edge (a,c): 4 b_c grad(lambda_a) +
+// 4 b_a grad(lambda_c)), so the projection is applied to the four
+// grad(lambda_v) once and combined afterwards.
+template <bool P2>
+__device__ inline void surf_basis(const TetGeom& g, const double b[4], const double n[3], double* phi,
+                                  double (*sg)[3]) {
+    double pg[4][3];
+    for (int v = 0; v < 4; ++v) {
+        const double ng = n[0] * g.gl[v][0] + n[1] * g.gl[v][1] + n[2] * g.gl[v][2];
+        for (int r = 0; r < 3; ++r) pg[v][r] = g.gl[v][r] - ng * n[r];
+    }
+    if constexpr (!P2) {
+        for (int i = 0; i < 4; ++i) {
+            phi[i] = b[i];
+            for (int r = 0; r < 3; ++r) sg[i][r] = pg[i][r];
+        }
+    } else {
+        double q[4];
+        for (int i = 0; i < 4; ++i) {
+            q[i] = 4. * b[i];
+            phi[i] = b[i] * (2. * b[i] - 1.);
+            const double f = q[i] - 1.;
+            for (int r = 0; r < 3; ++r) sg[i][r] = f * pg[i][r];
+        }
+        for (int e = 0; e < 6; ++e) {
+            const int a = ev0(e), c = ev1(e);
+            phi[4 + e] = q[a] * b[c];
+            for (int r = 0; r < 3; ++r) sg[4 + e][r] = q[c] * pg[a][r] + q[a] * pg[c][r];
+        }
+    }
+}
+
+// n . grad(phi_i) at barycentric b (volume stabilisation)
+template <bool P2>
+__device__ inline void normal_derivs(const TetGeom& g, const double b[4], const double n[3], double* dn) {
+    double ng[4];
+    for (int v = 0; v < 4; ++v) ng[v] = n[0] * g.gl[v][0] + n[1] * g.gl[v][1] + n[2] * g.gl[v][2];
+    if constexpr (!P2) {
+        for (int i = 0; i < 4; ++i) dn[i] = ng[i];
+    } else {
+        for (int i = 0; i < 4; ++i) dn[i] = (4. * b[i] - 1.) * ng[i];
+        for (int e = 0; e < 6; ++e) {
+            const int a = ev0(e), c = ev1(e);
+            dn[4 + e] = 4. * (b[c] * ng[a] + b[a] * ng[c]);
+        }
+    }
 }
 
 template <bool P2>
@@ -268,9 +330,11 @@ __device__ inline double rhs_value(const RhsPar& R, const double x[3]) {
     if (R.kind == TF_RHS_CONST) return R.p[0];
     if (R.kind == TF_RHS_SPHERE_XYZ) {
         const double d0 = x[0] - R.p[0], d1 = x[1] - R.p[1], d2 = x[2] - R.p[2];
-        const double nd = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
-        const double dist = nd - R.p[3];
-        const double y0 = x[0] - dist * (d0 / nd), y1 = x[1] - dist * (d1 / nd), y2 = x[2] - dist * (d2 / nd);
+        const double n2 = d0 * d0 + d1 * d1 + d2 * d2;
+        const double inv = rsqrt_fp64(n2);
+        const double dist = n2 * inv - R.p[3];
+        const double s = dist * inv;
+        const double y0 = x[0] - s * d0, y1 = x[1] - s * d1, y2 = x[2] - s * d2;
         return R.p[4] * y0 * y1 * y2;
     }
     return 0.;
@@ -454,15 +518,16 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
                     b[c] = S.P.fb[f][0][c] * cT.q2_node[q][0] + S.P.fb[f][1][c] * cT.q2_node[q][1] +
                            S.P.fb[f][2][c] * cT.q2_node[q][2];
                 const double w = S.P.fw[f] * cT.q2_w[q];
+                // values are stored times sqrt(w): sum_p w u_i u_j = sum_p (sqrt(w) u_i)(sqrt(w) u_j)
+                const double sw = w > 0. ? w * rsqrt_fp64(w) : 0.;
                 double n[3];
                 unit_normal(S.g, b, n);
-                double phi[NL], grad[NL][3];
-                basis<P2>(S.g, b, phi, grad);
-                S.w[lane] = w;
+                double phi[NL], sg[NL][3];
+                surf_basis<P2>(S.g, b, n, phi, sg);
+                S.w[lane] = sw;
                 for (int i = 0; i < NL; ++i) {
-                    S.phi[lane][i] = phi[i];
-                    const double gn = grad[i][0] * n[0] + grad[i][1] * n[1] + grad[i][2] * n[2];
-                    for (int c = 0; c < 3; ++c) S.sg[lane][i][c] = grad[i][c] - gn * n[c];
+                    S.phi[lane][i] = sw * phi[i];
+                    for (int c = 0; c < 3; ++c) S.sg[lane][i][c] = sw * sg[i][c];
                 }
                 if (wantL) {
                     double m = 1.0;
@@ -489,13 +554,12 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
                 sym_entry(NL, k, i, j);
                 double sm = accM[q], sa = accA[q], sl = accL[q];
                 for (int pp = 0; pp < cnt; ++pp) {
-                    const double w = S.w[pp];
-                    if (wantM) sm += w * (S.phi[pp][j] * S.phi[pp][i]);
+                    if (wantM) sm += S.phi[pp][j] * S.phi[pp][i];
                     if (wantA || wantL) {
                         const double d = S.sg[pp][j][0] * S.sg[pp][i][0] + S.sg[pp][j][1] * S.sg[pp][i][1] +
                                          S.sg[pp][j][2] * S.sg[pp][i][2];
-                        sa += w * d;
-                        if (wantL) sl += w * (S.mob[pp] * d);
+                        sa += d;
+                        if (wantL) sl += S.mob[pp] * d;
                     }
                 }
                 accM[q] = sm;
@@ -503,7 +567,7 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
                 accL[q] = sl;
             }
             if (wantF && lane < NL)
-                for (int pp = 0; pp < cnt; ++pp) accF += S.w[pp] * (S.fx[pp] * S.phi[pp][lane]);
+                for (int pp = 0; pp < cnt; ++pp) accF += (S.w[pp] * S.fx[pp]) * S.phi[pp][lane];
             __syncwarp();
         }
         if (wantC) {
@@ -513,9 +577,9 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
                 for (int c = 0; c < 4; ++c) b[c] = cT.q3_node[lane][c];
                 double n[3];
                 unit_normal(S.g, b, n);
-                double phi[NL], grad[NL][3];
-                basis<P2>(S.g, b, phi, grad);
-                for (int i = 0; i < NL; ++i) S.phi[lane][i] = n[0] * grad[i][0] + n[1] * grad[i][1] + n[2] * grad[i][2];
+                double dn[NL];
+                normal_derivs<P2>(S.g, b, n, dn);
+                for (int i = 0; i < NL; ++i) S.phi[lane][i] = dn[i];
             }
             __syncwarp();
             for (int q = 0; q < EPL; ++q) {

@@ -254,29 +254,47 @@ int ensure_sell(Context* c, CSR& A, bool fp32) {
 }
 
 // Slot row of a SELL matrix times the vector given by xload(col), accumulated
-// in T; four columns are loaded before they are used, so each lane keeps
-// several independent gathers in flight.  Terms are summed in CSR order.
+// in T.  The row is walked in blocks of eight: the column indices and values
+// of the next block are loaded while the gathers of the current block are in
+// flight, so a lane keeps up to 16 independent loads outstanding.  Terms are
+// summed in CSR order.
 template <class T, class XL>
 __device__ __forceinline__ T sell_row(const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
                                       const T* __restrict__ val, int64_t s, int lane, XL xload) {
+    constexpr int U = 8;
     const int32_t p0 = __ldg(ptr + s);
     const int32_t w = (__ldg(ptr + s + 1) - p0) >> 5;
     const int32_t* cp = col + p0 + lane;
     const T* vp = val + p0 + lane;
     T acc = T(0);
-    int32_t k = 0;
-    for (; k + 4 <= w; k += 4) {
-        const int32_t c0 = __ldg(cp + 32 * k), c1 = __ldg(cp + 32 * (k + 1)), c2 = __ldg(cp + 32 * (k + 2)),
-                      c3 = __ldg(cp + 32 * (k + 3));
-        const T v0 = __ldg(vp + 32 * k), v1 = __ldg(vp + 32 * (k + 1)), v2 = __ldg(vp + 32 * (k + 2)),
-                v3 = __ldg(vp + 32 * (k + 3));
-        const T x0 = xload(c0), x1 = xload(c1), x2 = xload(c2), x3 = xload(c3);
-        acc += v0 * x0;
-        acc += v1 * x1;
-        acc += v2 * x2;
-        acc += v3 * x3;
+    int32_t cn[U];
+    T vn[U];
+    const int32_t wu = w - w % U;
+    if (wu > 0) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            cn[u] = __ldg(cp + 32 * u);
+            vn[u] = __ldg(vp + 32 * u);
+        }
     }
-    for (; k < w; ++k) acc += __ldg(vp + 32 * k) * xload(__ldg(cp + 32 * k));
+    for (int32_t k = 0; k < wu; k += U) {
+        T xv[U], vv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            xv[u] = xload(cn[u]);
+            vv[u] = vn[u];
+        }
+        if (k + U < wu) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                cn[u] = __ldg(cp + 32 * (k + U + u));
+                vn[u] = __ldg(vp + 32 * (k + U + u));
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) acc += vv[u] * xv[u];
+    }
+    for (int32_t k = wu; k < w; ++k) acc += __ldg(vp + 32 * k) * xload(__ldg(cp + 32 * k));
     return acc;
 }
 
@@ -473,7 +491,7 @@ struct PcgArgs {
 constexpr int kKryThreads = 256;
 
 template <class T>
-__global__ void __launch_bounds__(kKryThreads, 4) k_pcg(PcgArgs<T> a) {
+__global__ void __launch_bounds__(kKryThreads, sizeof(T) == 4 ? 4 : 3) k_pcg(PcgArgs<T> a) {
     const int lane = threadIdx.x & 31;
     double* partA = a.part;
     double* partB = a.part + (size_t)gridDim.x * 3;
@@ -799,7 +817,7 @@ struct GmresArgs {
     double* out_resid;
 };
 
-__global__ void __launch_bounds__(kKryThreads, 4) k_gmres(GmresArgs a) {
+__global__ void __launch_bounds__(kKryThreads, 2) k_gmres(GmresArgs a) {
     const int lane = threadIdx.x & 31;
     __shared__ double H[kMaxRestart][kMaxRestart];
     __shared__ double cs[kMaxRestart], sn[kMaxRestart], s[kMaxRestart + 1], y[kMaxRestart], sc[kMaxRestart];
