@@ -1,4 +1,5 @@
 // extern "C" entry points of libtracefem (include/tracefem.h).
+#include <cstdlib>
 #include <cstring>
 
 #include "tf_internal.cuh"
@@ -54,6 +55,8 @@ int tf_create(tf_context** out, int device) {
     Context* c = &t->c;
     c->device = device;
     c->num_sms = prop.multiProcessorCount;
+    // launch-shape knob for the persistent Krylov kernels (resident blocks per SM)
+    if (const char* e = std::getenv("TF_KRY_BLOCKS_PER_SM")) c->kry_blocks_per_sm = std::atoi(e);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
         cudaMallocHost((void**)&c->h_status, 4 * sizeof(int)) != cudaSuccess ||

@@ -113,6 +113,66 @@ __device__ void grid_reduce(const double* part, double (&out)[NV]) {
     __syncthreads();
 }
 
+// Barrier and reduction in one: every block has written its NV partials; the
+// last block to arrive sums all of them in a fixed order (so the result does
+// not depend on which block is last), publishes the NV sums, and releases the
+// others.  Cost: one reduction of nblocks values instead of one per block.
+template <int NV>
+__device__ bool grid_sync_reduce(const GridSync& g, const double* part, double* result, double (&out)[NV]) {
+    __shared__ int last;
+    __shared__ double red[NV][32];
+    __shared__ int st;
+    __syncthreads();
+    unsigned my = 0;
+    if (threadIdx.x == 0) {
+        volatile unsigned* vgen = g.gen;
+        my = *vgen;
+        __threadfence();
+        last = atomicAdd(g.count, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last) {
+        __threadfence();
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int k = 0; k < NV; ++k) {
+            double x = 0.;
+            for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) x += __ldcg(part + (size_t)b * NV + k);
+            x = warp_sum(x);
+            if (lane == 0) red[k][w] = x;
+        }
+        __syncthreads();
+        if (w == 0)
+            for (int k = 0; k < NV; ++k) {
+                double x = lane < nw ? red[k][lane] : 0.;
+                x = warp_sum(x);
+                if (lane == 0) result[k] = x;
+            }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            *g.count = 0;
+            __threadfence();
+            atomicAdd(g.gen, 1u);
+        }
+    } else if (threadIdx.x == 0) {
+        volatile unsigned* vgen = g.gen;
+        long long spins = 0;
+        while (*vgen == my) {
+            if (++spins > kSpinLimit) {
+                atomicCAS(g.status, 0, TF_ERR_WATCHDOG);
+                break;
+            }
+            if (spins > 256) __nanosleep(32);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) st = *((volatile int*)g.status);
+    __syncthreads();
+    if (st != 0) return false;
+    for (int k = 0; k < NV; ++k) out[k] = __ldcg(result + k);
+    return true;
+}
+
 // ---------------------------------------------------------------------------
 // SELL-32-sigma layout and SpMV (y_Ax, num/spmat.h:1684-1709)
 // ---------------------------------------------------------------------------
@@ -466,6 +526,7 @@ int ch_block(Context* c, double alpha, double mob, double rho, double eps2, doub
 // ---------------------------------------------------------------------------
 template <class T>
 struct PcgArgs {
+    double* result;  // reduced sums published by grid_sync_reduce
     int64_t m, nslices;
     const int32_t* perm;
     const int32_t* ptr;
@@ -518,9 +579,8 @@ __global__ void __launch_bounds__(kKryThreads, sizeof(T) == 4 ? 4 : 3) k_pcg(Pcg
         }
         block_partials<3>(v, partA);
     }
-    if (!grid_barrier(a.gs)) return;
     double s0[3];
-    grid_reduce<3>(partA, s0);
+    if (!grid_sync_reduce<3>(a.gs, partA, a.result, s0)) return;
     double normb = sqrt(s0[1]);
     if (normb == 0.0 || !a.rel) normb = 1.0;
     double resid = sqrt(s0[0]) / normb;
@@ -554,9 +614,8 @@ __global__ void __launch_bounds__(kKryThreads, sizeof(T) == 4 ? 4 : 3) k_pcg(Pcg
             }
             block_partials<1>(v, partA);
         }
-        if (!grid_barrier(a.gs)) return;
         double lam[1];
-        grid_reduce<1>(partA, lam);
+        if (!grid_sync_reduce<1>(a.gs, partA, a.result + 4, lam)) return;
         const T alpha = (T)(rho / lam[0]);
         // phase B: x += alpha p ; r -= alpha q ; z = r / d ; <r,r>, <z,r>
         {
@@ -572,9 +631,8 @@ __global__ void __launch_bounds__(kKryThreads, sizeof(T) == 4 ? 4 : 3) k_pcg(Pcg
             }
             block_partials<2>(v, partB);
         }
-        if (!grid_barrier(a.gs)) return;
         double s2[2];
-        grid_reduce<2>(partB, s2);
+        if (!grid_sync_reduce<2>(a.gs, partB, a.result + 8, s2)) return;
         resid = sqrt(s2[0]) / normb;
         if (resid <= a.tol || it == a.max_iter) {
             if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -587,6 +645,165 @@ __global__ void __launch_bounds__(kKryThreads, sizeof(T) == 4 ? 4 : 3) k_pcg(Pcg
         rho = s2[1];
         beta = (T)(rho / rho1);
         T* tmp = pc;
+        pc = pn;
+        pn = tmp;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// mixed-precision PCG: FP32 iterations with FP64 reliable updates
+//
+// The search directions, the recursive residual and every SpMV of the
+// iteration are FP32 (A in FP32, 8 bytes per non-zero instead of 12, FP32
+// arithmetic); the iterate x is accumulated in FP64.  Whenever the FP32
+// residual has dropped by a factor kRelUpdate since the last refinement, or
+// claims convergence, the true residual b - A x is recomputed in FP64 (FP64
+// SpMV) and replaces the FP32 one: one step of FP64 iterative refinement that
+// keeps the Krylov recurrence instead of restarting it, so the iteration count
+// stays close to the FP64 solver's.  Convergence is decided on the FP64
+// residual only.
+// ---------------------------------------------------------------------------
+constexpr double kRelUpdate = 0.1;
+
+struct PcgMixedArgs {
+    double* result;
+    int64_t m, nslices;
+    const int32_t* perm;
+    const int32_t* ptr;
+    const int32_t* col;
+    const float* val32;
+    const double* val64;
+    const float* diag;
+    const double* b;
+    double* x;
+    float* r;
+    float* z;
+    float* p0;
+    float* p1;
+    float* q;
+    double* part;  // [3][nblocks][3]
+    GridSync gs;
+    int max_iter;
+    double tol;
+    int rel;
+    int* out_iter;
+    double* out_resid;
+    int* out_updates;
+};
+
+__global__ void __launch_bounds__(kKryThreads, 3) k_pcg_mixed(PcgMixedArgs a) {
+    const int lane = threadIdx.x & 31;
+    double* partA = a.part;
+    double* partB = a.part + (size_t)gridDim.x * 3;
+    double* partC = a.part + (size_t)gridDim.x * 6;
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
+
+    // r = b - A x in FP64, then FP32 copies: r, z = r / d; <r,r>, <b,b>, <z,r> in FP64
+    auto true_residual = [&](double* part, bool with_b, bool set_p) {
+        double v[3] = {0., 0., 0.};
+        const double* x = a.x;
+        TF_SLICE_LOOP(a.nslices, s) {
+            const double ax = sell_row<double>(a.ptr, a.col, a.val64, s, lane, [&](int32_t j) { return __ldcg(x + j); });
+            const int32_t row = __ldg(a.perm + s * 32 + lane);
+            if (row >= 0) {
+                const double bi = a.b[row];
+                const double ri = bi - ax;
+                const float r32 = (float)ri;
+                const float z32 = r32 / a.diag[row];
+                a.r[row] = r32;
+                a.z[row] = z32;
+                if (set_p) a.p0[row] = z32;
+                v[0] += ri * ri;
+                if (with_b) v[1] += bi * bi;
+                v[2] += (double)(z32 * r32);
+            }
+        }
+        block_partials<3>(v, part);
+    };
+
+    true_residual(partC, true, true);
+    double s0[3];
+    if (!grid_sync_reduce<3>(a.gs, partC, a.result, s0)) return;
+    double normb = sqrt(s0[1]);
+    if (normb == 0.0 || !a.rel) normb = 1.0;
+    double resid = sqrt(s0[0]) / normb;
+    double rho = s0[2];
+    double r_last = sqrt(s0[0]);
+    int updates = 1;
+    if (resid <= a.tol) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            *a.out_iter = 0;
+            *a.out_resid = resid;
+            *a.out_updates = updates;
+        }
+        return;
+    }
+    float beta = 0.f;
+    float* pc = a.p0;
+    float* pn = a.p1;
+    for (int it = 1; it <= a.max_iter; ++it) {
+        // phase A (FP32): p_new = z + beta p_old ; q = A p_new ; <q, p_new>
+        {
+            float v[1] = {0.f};
+            const float* z = a.z;
+            const float* po = pc;
+            TF_SLICE_LOOP(a.nslices, s) {
+                const float acc = sell_row<float>(a.ptr, a.col, a.val32, s, lane,
+                                                  [&](int32_t j) { return __ldcg(z + j) + beta * __ldcg(po + j); });
+                const int32_t row = __ldg(a.perm + s * 32 + lane);
+                if (row >= 0) {
+                    const float pi = __ldcg(z + row) + beta * __ldcg(po + row);
+                    pn[row] = pi;
+                    a.q[row] = acc;
+                    v[0] += acc * pi;
+                }
+            }
+            block_partials<1>(v, partA);
+        }
+        double lam[1];
+        if (!grid_sync_reduce<1>(a.gs, partA, a.result + 4, lam)) return;
+        const double alpha = rho / lam[0];
+        const float alpha32 = (float)alpha;
+        // phase B: x += alpha p (FP64) ; r -= alpha q ; z = r / d (FP32) ; <r,r>, <z,r>
+        {
+            float v[2] = {0.f, 0.f};
+            for (int64_t i = tid; i < a.m; i += nth) {
+                const float pi = __ldcg(pn + i);
+                a.x[i] += alpha * (double)pi;
+                const float ri = a.r[i] - alpha32 * __ldcg(a.q + i);
+                const float zi = ri / a.diag[i];
+                a.r[i] = ri;
+                a.z[i] = zi;
+                v[0] += ri * ri;
+                v[1] += zi * ri;
+            }
+            block_partials<2>(v, partB);
+        }
+        double s2[2];
+        if (!grid_sync_reduce<2>(a.gs, partB, a.result + 8, s2)) return;
+        const double rn32 = sqrt(s2[0]);
+        double rho_new = s2[1];
+        if (rn32 <= kRelUpdate * r_last || rn32 / normb <= a.tol || it == a.max_iter) {
+            // reliable update: FP64 residual replaces the FP32 one
+            true_residual(partC, false, false);
+            double s3[3];
+            if (!grid_sync_reduce<3>(a.gs, partC, a.result + 12, s3)) return;
+            ++updates;
+            r_last = sqrt(s3[0]);
+            resid = r_last / normb;
+            rho_new = s3[2];
+            if (resid <= a.tol || it == a.max_iter) {
+                if (blockIdx.x == 0 && threadIdx.x == 0) {
+                    *a.out_iter = resid <= a.tol ? it : -it;
+                    *a.out_resid = resid;
+                    *a.out_updates = updates;
+                }
+                return;
+            }
+        }
+        beta = (float)(rho_new / rho);
+        rho = rho_new;
+        float* tmp = pc;
         pc = pn;
         pn = tmp;
     }
@@ -606,6 +823,7 @@ static int coop_blocks(Context* c, const void* fn, int64_t nslices, int* out) {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kKryThreads, 0) != cudaSuccess || per_sm < 1)
         return set_err(c, TF_ERR_CUDA, "occupancy query failed");
+    if (c->kry_blocks_per_sm > 0 && c->kry_blocks_per_sm < per_sm) per_sm = c->kry_blocks_per_sm;
     const int64_t want = (nslices * 32 + kKryThreads - 1) / kKryThreads;
     int64_t b = std::min<int64_t>(want, (int64_t)per_sm * c->num_sms);
     *out = (int)(b < 1 ? 1 : b);
@@ -618,7 +836,7 @@ static int run_pcg_kernel(Context* c, const CSR& A, const T* val, const T* diag,
     const void* fn = (const void*)k_pcg<T>;
     int blocks = 0;
     TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks));
-    TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 3 * 2));
+    TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 3 * 2 + 16));
     TF_TRY(ensure(c, c->kry_bar, 2));
     TF_TRY(ensure(c, c->kry_iters, 1));
     TF_TRY(ensure(c, c->kry_resid, 1));
@@ -640,6 +858,7 @@ static int run_pcg_kernel(Context* c, const CSR& A, const T* val, const T* diag,
     a.p1 = work + 3 * A.m;
     a.q = work + 4 * A.m;
     a.part = c->kry_part.p;
+    a.result = c->kry_part.p + (size_t)blocks * 3 * 2;
     a.gs = GridSync{c->kry_bar.p, c->kry_bar.p + 1, c->status.p};
     a.max_iter = max_iter;
     a.tol = tol;
@@ -661,55 +880,6 @@ static int run_pcg_kernel(Context* c, const CSR& A, const T* val, const T* diag,
     return TF_OK;
 }
 
-// residual r = b - A x (FP64) with <r,r>, <b,b> partials
-__global__ void k_residual(int64_t nslices, const int32_t* __restrict__ perm, const int32_t* __restrict__ ptr,
-                           const int32_t* __restrict__ col, const double* __restrict__ val, const double* __restrict__ b,
-                           const double* __restrict__ x, double* __restrict__ r, double* __restrict__ part) {
-    const int lane = threadIdx.x & 31;
-    double v[2] = {0., 0.};
-    TF_SLICE_LOOP(nslices, s) {
-        const double ax = sell_row<double>(ptr, col, val, s, lane, [&](int32_t j) { return __ldcg(x + j); });
-        const int32_t row = perm[s * 32 + lane];
-        if (row >= 0) {
-            const double ri = b[row] - ax;
-            r[row] = ri;
-            v[0] += ri * ri;
-            v[1] += b[row] * b[row];
-        }
-    }
-    block_partials<2>(v, part);
-}
-__global__ void k_reduce_partials(int nblocks, const double* __restrict__ part, double* __restrict__ out) {
-    double o[2];
-    // one block; the same fixed order as grid_reduce
-    __shared__ double red[2][32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int k = 0; k < 2; ++k) {
-        double x = 0.;
-        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) x += part[b * 2 + k];
-        x = warp_sum(x);
-        if (lane == 0) red[k][w] = x;
-    }
-    __syncthreads();
-    if (w == 0)
-        for (int k = 0; k < 2; ++k) {
-            double x = lane < nw ? red[k][lane] : 0.;
-            x = warp_sum(x);
-            o[k] = x;
-            if (lane == 0) out[k] = o[k];
-        }
-}
-__global__ void k_scale_to_f32(int64_t n, const double* __restrict__ a, double s, float* __restrict__ b, float* __restrict__ x0) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        b[i] = (float)(a[i] * s);
-        x0[i] = 0.f;
-    }
-}
-__global__ void k_axpy_f32(int64_t n, double s, const float* __restrict__ d, double* __restrict__ x) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        x[i] += s * (double)d[i];
-}
-
 int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, int* max_iter, double* tol, int rel) {
     if (!A.vals || A.m <= 0) return set_err(c, TF_ERR_BAD_INPUT, "pcg: empty matrix");
     TF_TRY(ensure_diag(c, A));
@@ -726,60 +896,60 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
         *tol = res;
         return ok ? TF_OK : set_err(c, TF_ERR_NOT_CONVERGED, "pcg: no convergence within max_iter");
     }
-    // mixed precision: FP32 PCG sweeps inside FP64 iterative refinement
-    TF_TRY(ensure_sell(c, A, false));  // FP64 copy for the outer residual
-    TF_TRY(ensure(c, c->kry32, (size_t)(8 * m)));
-    TF_TRY(ensure(c, c->kry64, (size_t)(5 * m)));
-    float* d32 = c->kry32.p;  // diag, rhs, x, work(5m)
-    float* b32 = d32 + m;
-    float* x32 = b32 + m;
-    float* w32 = x32 + m;
+    // mixed precision: FP32 iterations, FP64 iterate and reliable updates
+    TF_TRY(ensure_sell(c, A, false));  // FP64 copy for the refinement residuals
+    TF_TRY(ensure(c, c->kry32, (size_t)(6 * m)));
+    float* d32 = c->kry32.p;
     k_to_f32<<<grid_for(c, m), kBlock, 0, c->stream>>>(m, A.diag, d32);
     ++c->launches;
-    double* r64 = c->kry64.p;
-    double* part = c->kry64.p + m;
-    const int rblocks = (int)std::min<int64_t>((A.sell.nslices * 32 + kBlock - 1) / kBlock, (int64_t)c->num_sms * 8);
-    if ((int64_t)rblocks * 2 + 2 > 4 * m) return set_err(c, TF_ERR_CAPACITY, "pcg: matrix too small for mixed precision");
-    double* sums = part + (size_t)rblocks * 2;
-    int total_inner = 0;
-    double res = 0.;
-    const int max_outer = 60;
-    for (int outer = 0; outer <= max_outer; ++outer) {
-        k_residual<<<rblocks, kBlock, 0, c->stream>>>(A.sell.nslices, A.sell.perm, A.sell.ptr, A.sell.col, A.sell.v64, b,
-                                                     x, r64, part);
-        k_reduce_partials<<<1, 256, 0, c->stream>>>(rblocks, part, sums);
-        c->launches += 2;
-        double h[2];
-        TF_CUDA(c, cudaMemcpyAsync(h, sums, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-        TF_CUDA(c, cudaStreamSynchronize(c->stream));
-        double normb = std::sqrt(h[1]);
-        if (normb == 0.0 || !rel) normb = 1.0;
-        const double rn = std::sqrt(h[0]);
-        res = rn / normb;
-        if (res <= *tol) {
-            *max_iter = total_inner;
-            *tol = res;
-            return TF_OK;
-        }
-        if (total_inner >= *max_iter || outer == max_outer) break;
-        // inner FP32 PCG on A d = r / |r|
-        k_scale_to_f32<<<grid_for(c, m), kBlock, 0, c->stream>>>(m, r64, 1.0 / rn, b32, x32);
-        ++c->launches;
-        double inner_tol = 0.25 * (*tol) / res;
-        if (inner_tol < 2e-6) inner_tol = 2e-6;
-        if (inner_tol > 0.1) inner_tol = 0.1;
-        int it = 0;
-        double ires = 0.;
-        TF_TRY(run_pcg_kernel<float>(c, A, A.sell.v32, d32, b32, x32, w32, *max_iter - total_inner, inner_tol, 1, &it,
-                                     &ires));
-        total_inner += it >= 0 ? it : -it;
-        k_axpy_f32<<<grid_for(c, m), kBlock, 0, c->stream>>>(m, rn, x32, x);
-        ++c->launches;
-        TF_CUDA(c, cudaGetLastError());
-    }
-    *max_iter = total_inner;
+    const void* fn = (const void*)k_pcg_mixed;
+    int blocks = 0;
+    TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks));
+    TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 3 * 3 + 16));
+    TF_TRY(ensure(c, c->kry_bar, 2));
+    TF_TRY(ensure(c, c->kry_iters, 2));
+    TF_TRY(ensure(c, c->kry_resid, 1));
+    TF_CUDA(c, cudaMemsetAsync(c->kry_bar.p, 0, 2 * sizeof(unsigned), c->stream));
+    TF_CUDA(c, cudaMemsetAsync(c->status.p, 0, 4 * sizeof(int), c->stream));
+    PcgMixedArgs g;
+    g.m = m;
+    g.nslices = A.sell.nslices;
+    g.perm = A.sell.perm;
+    g.ptr = A.sell.ptr;
+    g.col = A.sell.col;
+    g.val32 = A.sell.v32;
+    g.val64 = A.sell.v64;
+    g.diag = d32;
+    g.b = b;
+    g.x = x;
+    g.r = d32 + m;
+    g.z = d32 + 2 * m;
+    g.p0 = d32 + 3 * m;
+    g.p1 = d32 + 4 * m;
+    g.q = d32 + 5 * m;
+    g.part = c->kry_part.p;
+    g.result = c->kry_part.p + (size_t)blocks * 3 * 3;
+    g.gs = GridSync{c->kry_bar.p, c->kry_bar.p + 1, c->status.p};
+    g.max_iter = *max_iter;
+    g.tol = *tol;
+    g.rel = rel;
+    g.out_iter = c->kry_iters.p;
+    g.out_resid = c->kry_resid.p;
+    g.out_updates = c->kry_iters.p + 1;
+    void* args[] = {&g};
+    TF_CUDA(c, cudaLaunchCooperativeKernel(fn, blocks, kKryThreads, args, 0, c->stream));
+    ++c->launches;
+    int it[2] = {0, 0};
+    double res = 0;
+    TF_CUDA(c, cudaMemcpyAsync(it, c->kry_iters.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    TF_CUDA(c, cudaMemcpyAsync(&res, c->kry_resid.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    int st = 0;
+    TF_TRY(sync_status(c, &st));
+    if (st) return set_err(c, st, "pcg (mixed): grid barrier watchdog fired");
+    c->last_refinements = it[1];
+    *max_iter = it[0] >= 0 ? it[0] : -it[0];
     *tol = res;
-    return set_err(c, TF_ERR_NOT_CONVERGED, "pcg (mixed): no convergence within max_iter");
+    return it[0] >= 0 ? TF_OK : set_err(c, TF_ERR_NOT_CONVERGED, "pcg (mixed): no convergence within max_iter");
 }
 
 // ---------------------------------------------------------------------------
@@ -795,6 +965,7 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
 constexpr int kMaxRestart = 64;
 
 struct GmresArgs {
+    double* result;
     int64_t m, nslices;
     const int32_t* perm;
     const int32_t* ptr;
@@ -848,9 +1019,8 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres(GmresArgs a) {
             }
         }
         block_partials<2>(v, pp);
-        if (!grid_barrier(a.gs)) return;
         double t[2];
-        grid_reduce<2>(pp, t);
+        if (!grid_sync_reduce<2>(a.gs, pp, a.result, t)) return;
         double beta = sqrt(t[0]);
         double normb = sqrt(t[1]);
         if (normb == 0.0 || !a.rel) normb = 1.0;
@@ -908,9 +1078,8 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres(GmresArgs a) {
                         }
                     }
                     block_partials<1>(v1, pq);
-                    if (!grid_barrier(a.gs)) return;
                     double h[1];
-                    grid_reduce<1>(pq, h);
+                    if (!grid_sync_reduce<1>(a.gs, pq, a.result + 2 + flip, h)) return;
                     if (threadIdx.x == 0) H[0][i] = h[0];
                     __syncthreads();
                 }
@@ -928,9 +1097,8 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres(GmresArgs a) {
                         v1[0] += k < i ? w * (scn * __ldcg(Vn + e)) : w * w;
                     }
                     block_partials<1>(v1, pq);
-                    if (!grid_barrier(a.gs)) return;
                     double h[1];
-                    grid_reduce<1>(pq, h);
+                    if (!grid_sync_reduce<1>(a.gs, pq, a.result + 2 + flip, h)) return;
                     if (threadIdx.x == 0) {
                         if (k < i) H[k + 1][i] = h[0];
                         else H[i + 1][i] = sqrt(h[0]);
@@ -1021,9 +1189,8 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres(GmresArgs a) {
                     }
                 }
                 block_partials<1>(v1, pq);
-                if (!grid_barrier(a.gs)) return;
                 double t1[1];
-                grid_reduce<1>(pq, t1);
+                if (!grid_sync_reduce<1>(a.gs, pq, a.result + 2 + flip, t1)) return;
                 beta = sqrt(t1[0]);
                 resid = beta / normb;
                 if (resid <= a.tol) {
@@ -1087,7 +1254,7 @@ int gmres_jacobi(Context* c, CSR& A, const double* b, double* x, int restart, in
     const void* fn = (const void*)k_gmres;
     int blocks = 0;
     TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks));
-    TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 2 * 2));
+    TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 2 * 2 + 8));
     TF_TRY(ensure(c, c->kry_bar, 2));
     TF_TRY(ensure(c, c->kry_iters, 1));
     TF_TRY(ensure(c, c->kry_resid, 1));
@@ -1105,6 +1272,7 @@ int gmres_jacobi(Context* c, CSR& A, const double* b, double* x, int restart, in
     g.x = x;
     g.V = c->kry64.p;
     g.part = c->kry_part.p;
+    g.result = c->kry_part.p + (size_t)blocks * 2 * 2;
     g.gs = GridSync{c->kry_bar.p, c->kry_bar.p + 1, c->status.p};
     g.R = R;
     g.left = method == 1;

@@ -211,6 +211,8 @@ struct Context {
     DBuf<unsigned char> flush_buf;
     KernelTimer timers[TF_NUM_KERNELS];
     int64_t launches = 0;
+    int last_refinements = 0;  // FP64 residual replacements of the last mixed solve
+    int kry_blocks_per_sm = 0; // cap on resident Krylov blocks per SM (0: occupancy limit)
     int64_t pattern_counter = 0, block_src_gen = -1;
     DBuf<int32_t> sell_ptr[TF_NUM_MATS], sell_col[TF_NUM_MATS], sell_src[TF_NUM_MATS], sell_perm[TF_NUM_MATS];
     DBuf<double> sell_v64[TF_NUM_MATS];
