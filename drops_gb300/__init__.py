@@ -41,7 +41,7 @@ EXPORTS = [
     "tf_mesh_info", "tf_mesh_download", "tf_levelset_upload", "tf_levelset_analytic", "tf_levelset_download",
     "tf_distribute_dofs", "tf_create_numb_on_interface_p1", "tf_dofs_download", "tf_patches_download", "tf_setup_fe_system",
     "tf_matrix_info", "tf_matrix_download", "tf_matrix_upload", "tf_lincomb", "tf_ch_block", "tf_vec_upload",
-    "tf_vec_download", "tf_vec_size", "tf_vec_fill", "tf_spmv", "tf_pcg_jacobi", "tf_gmres_jacobi", "tf_ch_steps", "tf_timing_enable",
+    "tf_vec_download", "tf_vec_size", "tf_vec_fill", "tf_spmv", "tf_pcg_jacobi", "tf_gmres_jacobi", "tf_pcg_jacobi_noalloc", "tf_ch_steps", "tf_timing_enable",
     "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2",
     "tf_host_alloc", "tf_host_free",
 ]

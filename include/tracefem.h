@@ -200,6 +200,28 @@ int tf_pcg_jacobi(tf_context* ctx, int mat, int vec_b, int vec_x, int precision,
 int tf_gmres_jacobi(tf_context* ctx, int mat, int vec_b, int vec_x, int restart, int method, int precision,
                     int* max_iter, double* tol, int rel);
 
+/* ---- allocation-free PCG -------------------------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory: applications that manage every GPU byte through their own pool and
+ * forbid third-party cudaMalloc, real-time loops that must not pay the
+ * implicit device synchronisation of cudaMalloc/cudaFree.  Jacobi-PCG as
+ * tf_pcg_jacobi (FP64), but without a context: rowptr[m+1], colind[nnz]
+ * (int32), vals[nnz], b[m] and x[m] (initial guess in, solution out) are
+ * DEVICE pointers owned by the
+ * caller; max_iter and tol are host in/out values as in tf_pcg_jacobi; stream
+ * is a cudaStream_t or NULL.  All other memory the solve needs lives in one
+ * fixed device array of the library (6*TF_NOALLOC_MAX_ROWS doubles plus a few
+ * hundred KB, about 13 MB), which every GPU that loads the library holds until
+ * the process exits.  The call allocates nothing.  m > TF_NOALLOC_MAX_ROWS
+ * returns TF_ERR_CAPACITY.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) and must come before any stream
+ * capture on that device.  Every call reuses the same array: calls that
+ * overlap on the GPU (two streams, two host threads) race on it and must be
+ * serialised by the caller.                                                    */
+#define TF_NOALLOC_MAX_ROWS 262144
+int tf_pcg_jacobi_noalloc(int64_t m, const int32_t* rowptr, const int32_t* colind, const double* vals,
+                          const double* b, double* x, int* max_iter, double* tol, int rel, void* stream);
+
 /* ---- Cahn-Hilliard time stepping ------------------------------------------------- */
 /* `nsteps` implicit (BDF1) steps of the surface Cahn-Hilliard system of
  * surfphasesep/surfphasesep.cpp:397-440 (constant mobility, no wind):
