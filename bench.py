@@ -13,7 +13,11 @@ e2e:   the same through the C ABI from pinned host buffers: level-set upload
        (H2D), the step, solution download (D2H) inside the timed region.
 L2 is flushed (2x L2 bytes written) before every timed step.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload poisson|batch]
+
+--workload batch: 256 independent P1 ellipsoid problems of uneven size (n^3
+cubes, n ~ U{16..64}) through the same calls, solved by one persistent
+batched PCG launch (CUDA graph, autotuned lanes per row).
 
 --impl reference times the reference algorithm on the host cores: the C
 restatement in oracle/ (the DROPS sources do not exist on the GPU host), same
@@ -228,6 +232,19 @@ def run_ours(args, rank, ws, dist):
         ctx.marker(5)
         solve[name] = {"ms": ctx.elapsed_ms(4, 5), "iters": it, "resid": res}
 
+    # ---- standalone FP64 SpMV (y_Ax) on the system matrix, cold L2 ---------
+    spmv_ms = []
+    for _ in range(10):
+        ctx.flush_l2()
+        ctx.marker(6)
+        ctx.spmv(tf.MAT_SYS, tf.VEC_X, tf.VEC_T0)
+        ctx.marker(7)
+        spmv_ms.append(ctx.elapsed_ms(6, 7))
+    spmv_t = statistics.median(spmv_ms)
+    spmv_bytes = 12 * state["nnz"] + 4 * (state["m"] + 1) + 16 * state["m"]
+    spmv = {"ms": round(spmv_t, 4), "bytes": spmv_bytes, "achieved_gbs": round(spmv_bytes / (spmv_t / 1e3) / 1e9, 1),
+            "bytes_model": "12*nnz + 4*(m+1) + 16*m (FP64 values + int32 columns, row pointers, x read, y written)"}
+
     # ---- roofline of the dominant kernel ------------------------------------
     dom = max(ktimes, key=lambda k: ktimes[k][0])
     peaks = {}
@@ -237,6 +254,7 @@ def run_ours(args, rank, ws, dist):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    spmv["frac"] = round(spmv["achieved_gbs"] / hbm_peak, 4)
     ms_d, n_d = ktimes[dom]
     na, m, nnz = state["na"], state["m"], state["nnz"]
     if dom == "pcg":
@@ -265,6 +283,7 @@ def run_ours(args, rank, ws, dist):
         "clocks": clocks,
         "problem": {"tets": nt, "cut_tets": na, "dofs": m, "nnz": nnz, "pcg_iters_inner": state["it"]},
         "solve_ms": solve,
+        "spmv_fp64_cold": spmv,
         "kernel_ms": {k: round(v[0] / args.steps, 4) for k, v in ktimes.items() if v[1]},
     }
     ctx.close()
@@ -272,6 +291,177 @@ def run_ours(args, rank, ws, dist):
     pin_e.free()
     pin_x.free()
     return out
+
+
+# ---------------------------------------------------------------------------
+BATCH_COUNT, BATCH_NMIN, BATCH_NMAX = 256, 16, 64
+BATCH_METRIC = "cut tets/s through DistributeDOFs + setupFESystem + batched Jacobi-PCG to rel. residual 1e-10 " \
+               "(256 independent P1 ellipsoid problems, one persistent solve launch)"
+BATCH_CONFIG = {
+    "workload": "256 independent surface Poisson problems, P1 TraceFEM, ellipsoids (semi-axes U[0.6,1.4], "
+                "Haar rotations, centres in the 0.1-ball, seed 1000+i) on [-5/3,5/3]^3 with n^3 Kuhn cubes, "
+                "n ~ U{16..64}; A_i = M + A_LB + h_i C_n, f = 13xyz(x/|x|); batched Jacobi-PCG rel 1e-10, "
+                "FP32 inner / FP64 reliable updates, CUDA-graph launch, autotuned lanes per row",
+    "instances": BATCH_COUNT, "fe": "P1IF", "tol": TOL,
+    "l2": "flushed before every timed step (2x L2 size written)", "parallelism": "replicas",
+}
+
+
+def batch_spec(args):
+    from drops_gb300.workloads import ellipsoid_batch
+
+    return ellipsoid_batch(args.batch_count, args.batch_nmin, args.batch_nmax, seed=1000)
+
+
+def run_batch(args, rank, ws, dist):
+    import drops_gb300 as tf
+
+    W = batch_spec(args)
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    ctx = tf.TraceFEM(dev)
+    ctx.brick_batch(W["n"], W["orig"], W["axes"])
+    ctx.levelset_analytic_batch(tf.LS_ELLIPSOID, W["par"], p2=False)
+    nv, ne, nt = ctx.mesh_info()
+    lv_dev, le_dev = ctx.levelset_download()
+    pin_v, pin_e = tf.PinnedArray(nv), tf.PinnedArray(ne)
+    pin_v.array[:] = lv_dev
+    pin_e.array[:] = le_dev
+    forms = [tf.FORM_M, tf.FORM_A, tf.FORM_CN]
+    coef = np.stack([np.ones(len(W["h"])), np.ones(len(W["h"])), W["h"]], axis=1)
+    state = {}
+
+    def step(precision=tf.PREC_MIXED):
+        na, m = ctx.distribute_dofs(tf.P1IF)
+        nnz = ctx.setup_fe_system(forms, tf.RHS_SPHERE_XYZ, RHS)
+        ctx.batch_lincomb(forms, coef)
+        ctx.vec_fill(tf.VEC_X, m, 0.0)
+        st, its, res = ctx.batch_pcg_jacobi(tf.MAT_SYS, tf.VEC_RHS, tf.VEC_X, tol=TOL, precision=precision)
+        if st != tf.OK or np.any(res > TOL):
+            raise RuntimeError(f"batched solve failed: status {st}, worst residual {res.max()}")
+        state.update(na=na, m=m, nnz=nnz, its=its.copy())
+        return na
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    lanes, threads = ctx.batch_tune(tf.MAT_SYS, tf.VEC_RHS, tf.PREC_MIXED)
+    barrier(dist)
+    ctx.timing(True)
+    ctx.timing_reset()
+    launches0 = ctx.launch_count()
+    step_ms, cut = [], 0
+    with Clocks(dev) as clk:
+        for _ in range(args.steps):
+            ctx.flush_l2()
+            barrier(dist)
+            ctx.marker(0)
+            cut += step()
+            ctx.marker(1)
+            step_ms.append(ctx.elapsed_ms(0, 1))
+    launches = ctx.launch_count() - launches0
+    ktimes = {name: ctx.timing_get(k) for k, name in enumerate(tf.KERNEL_NAMES)}
+    ctx.timing(False)
+    clocks = clk.summary()
+    total_ms = all_max(dist, sum(step_ms))
+    value = all_sum(dist, cut) / (total_ms / 1e3)
+
+    pin_x = tf.PinnedArray(state["m"])
+    e2e_ms, e2e_cut = [], 0
+    for _ in range(args.steps):
+        ctx.flush_l2()
+        barrier(dist)
+        ctx.marker(2)
+        ctx.levelset_upload(pin_v.array, pin_e.array)
+        e2e_cut += step()
+        ctx.vec_download(tf.VEC_X, out=pin_x.array)
+        ctx.marker(3)
+        e2e_ms.append(ctx.elapsed_ms(2, 3))
+    e2e_total = all_max(dist, sum(e2e_ms))
+    e2e_value = all_sum(dist, e2e_cut) / (e2e_total / 1e3)
+
+    # solve only: FP64 vs mixed, graph replay vs direct launch
+    solve = {}
+    for prec, name, graph in ((tf.PREC_FP64, "fp64", True), (tf.PREC_MIXED, "mixed", True),
+                              (tf.PREC_MIXED, "mixed_no_graph", False)):
+        ctx.batch_config(lanes, threads, use_graph=graph)
+        ts = []
+        for rep in range(3):
+            ctx.vec_fill(tf.VEC_X, state["m"], 0.0)
+            ctx.flush_l2()
+            ctx.marker(4)
+            st, its, res = ctx.batch_pcg_jacobi(tf.MAT_SYS, tf.VEC_RHS, tf.VEC_X, tol=TOL, precision=prec)
+            ctx.marker(5)
+            ts.append(ctx.elapsed_ms(4, 5))
+        solve[name] = {"ms": round(min(ts[1:]), 4), "iters_max": int(its.max()), "iters_sum": int(its.sum()),
+                       "resid_max": float(res.max())}
+    tets, cutr, rows, nnzr = ctx.batch_info()
+    sizes = {"tets": int(nt), "cut_tets": int(state["na"]), "dofs": int(state["m"]), "nnz": int(state["nnz"]),
+             "rows_min": int(np.diff(rows).min()), "rows_max": int(np.diff(rows).max())}
+
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    dom = max(ktimes, key=lambda k: ktimes[k][0])
+    ms_d, n_d = ktimes[dom]
+    na, m, nnz = state["na"], state["m"], state["nnz"]
+    if dom == "assemble":
+        per_launch = na * (4 * 8 + 3 * 10 * 8 + 4 * 8)
+        note = "per cut tet: 4 level-set values read, 3 packed 4x4 element matrices + load vector written"
+    elif dom == "batch":
+        per_launch = sum(((4 + 4) * (nnzr[i + 1] - nnzr[i]) + 4 * (rows[i + 1] - rows[i] + 1) +
+                          48 * (rows[i + 1] - rows[i])) * int(state["its"][i]) for i in range(len(state["its"])))
+        note = "FP32 inner PCG iterations of every instance: (4+4)*nnz_i + 4*(m_i+1) + 48*m_i bytes per iteration"
+    else:
+        per_launch = 0
+        note = "no byte model for this kernel"
+    achieved = per_launch / ((ms_d / max(n_d, 1)) / 1e3) / 1e9 if ms_d > 0 else 0.0
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                "frac": round(achieved / hbm_peak, 4), "traffic": None,
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "bytes_model": note,
+                "launch_ms": round(ms_d / max(n_d, 1), 4)}
+    out = {
+        "metric": BATCH_METRIC, "value": round(value, 1), "unit": "cut_tets/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic (analytic level sets)",
+        "config": BATCH_CONFIG,
+        "e2e": {"value": round(e2e_value, 1), "unit": "cut_tets/s", "h2d_bytes_per_step": 8 * (nv + ne),
+                "d2h_bytes_per_step": 8 * state["m"], "ms_per_step": round(e2e_total / args.steps, 3)},
+        "gpu_launches": int(launches), "roofline": roofline, "clocks": clocks, "problem": sizes,
+        "autotuned": {"lanes_per_row": lanes, "threads": threads}, "solve_ms": solve,
+        "kernel_ms": {k: round(v[0] / args.steps, 4) for k, v in ktimes.items() if v[1]},
+    }
+    ctx.close()
+    pin_v.free()
+    pin_e.free()
+    pin_x.free()
+    return out
+
+
+def batch_cpu_sample(args, threads, budget_s=20.0):
+    """Oracle (C restatement of the reference) on the batch instances, in order, until budget_s has passed."""
+    from oracle import pyoracle as O
+
+    O.set_threads(threads)
+    W = batch_spec(args)
+    opts = O.make_opts(False, [O.FORM_M, O.FORM_A, O.FORM_CN], O.RHS_SPHERE_XYZ, RHS)
+    tot_t, tot_cut, done = 0.0, 0, 0
+    for i in range(len(W["h"])):
+        n = tuple(int(k) for k in W["n"][i])
+        mesh = O.brick(n, orig=W["orig"][i], e=W["axes"][i])
+        lv, le = O.levelset(mesh, O.LS_ELLIPSOID, W["par"][i], False)
+        t0 = time.perf_counter()
+        st, na, m, dv, de, act = O.distribute_dofs(mesh, lv, le, False)
+        st, rp, ci, vals, rhs = O.assemble(mesh, lv, le, act, dv, None, m, opts)
+        S = vals[O.FORM_M] + vals[O.FORM_A] + W["h"][i] * vals[O.FORM_CN]
+        O.pcg_jacobi(rp, ci, S, rhs, tol=TOL)
+        tot_t += time.perf_counter() - t0
+        tot_cut += na
+        done += 1
+        if tot_t > budget_s:
+            break
+    return tot_cut / tot_t, f"first {done} of {len(W['h'])} instances, in order ({tot_t:.1f} s, FP64 PCG)"
 
 
 # ---------------------------------------------------------------------------
@@ -300,6 +490,17 @@ def run_reference(args, rank, ws, dist):
     if rank != 0:
         return None
     threads = os.cpu_count() or 1
+    if args.workload == "batch":
+        vals = [batch_cpu_sample(args, threads, budget_s=10.0) for _ in range(max(args.steps, 1))]
+        value = statistics.median(v[0] for v in vals)
+        return {
+            "impl": "reference", "metric": BATCH_METRIC, "value": round(value, 1), "unit": "cut_tets/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": 0, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic level sets)", "config": BATCH_CONFIG,
+            "cpu_baseline": {"value": round(value, 1), "unit": "cut_tets/s", "cores": threads, "kind": "port",
+                             "sample": vals[0][1] + "; C restatement of the reference in oracle/"},
+            "e2e": {"value": round(value, 1), "unit": "cut_tets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
     step = cpu_workload(threads, args.size)
     for _ in range(args.warmup):
         step()
@@ -330,6 +531,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--size", type=int, default=N_CUBES, help="cubes per direction (96 = the benchmark workload; "
                     "smaller sizes are for profiling captures)")
+    ap.add_argument("--workload", default="poisson", choices=["poisson", "batch"],
+                    help="poisson: the P2 96^3 sphere problem (headline); batch: 256 independent P1 ellipsoids")
+    ap.add_argument("--batch-count", type=int, default=BATCH_COUNT)
+    ap.add_argument("--batch-nmin", type=int, default=BATCH_NMIN)
+    ap.add_argument("--batch-nmax", type=int, default=BATCH_NMAX)
     args = ap.parse_args()
     rank, ws, dist = dist_init()
     if args.impl == "reference":
@@ -342,6 +548,20 @@ def main():
     if rank == 0:
         build.build()
     barrier(dist)
+    if args.workload == "batch":
+        out = run_batch(args, rank, ws, dist)
+        if (args.batch_count, args.batch_nmin, args.batch_nmax) != (BATCH_COUNT, BATCH_NMIN, BATCH_NMAX):
+            out["config"] = dict(out["config"], workload=f"PROFILING SIZE {args.batch_count} instances, "
+                                 f"n in [{args.batch_nmin},{args.batch_nmax}] (not the benchmark workload)")
+        if rank == 0:
+            if ws == 1 and not args.no_cpu_baseline:
+                v, sample = batch_cpu_sample(args, os.cpu_count() or 1)
+                out["cpu_baseline"] = {"value": round(v, 1), "unit": "cut_tets/s", "cores": os.cpu_count() or 1,
+                                       "kind": "port", "sample": sample}
+            print(json.dumps(out))
+        if dist is not None:
+            dist.destroy_process_group()
+        return
     out = run_ours(args, rank, ws, dist)
     if args.size != N_CUBES:
         out["config"] = dict(out["config"], workload=f"PROFILING SIZE {args.size}^3 (not the benchmark workload)")

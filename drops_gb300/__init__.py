@@ -32,8 +32,8 @@ VEC_RHS, VEC_X, VEC_B, VEC_CHI, VEC_T0, VEC_T1, VEC_T2, VEC_T3 = range(8)
 LS_SPHERE, LS_TORUS, LS_ELLIPSOID, LS_PLANE = range(4)
 RHS_NONE, RHS_SPHERE_XYZ, RHS_CONST = range(3)
 PREC_FP64, PREC_MIXED = 0, 1
-K_CLASSIFY, K_NUMBER, K_ASSEMBLE, K_PATTERN, K_SCATTER, K_SPMV, K_PCG, K_GMRES, K_LEVELSET = range(9)
-KERNEL_NAMES = ["classify", "number", "assemble", "pattern", "scatter", "spmv", "pcg", "gmres", "levelset"]
+K_CLASSIFY, K_NUMBER, K_ASSEMBLE, K_PATTERN, K_SCATTER, K_SPMV, K_PCG, K_GMRES, K_LEVELSET, K_BATCH = range(10)
+KERNEL_NAMES = ["classify", "number", "assemble", "pattern", "scatter", "spmv", "pcg", "gmres", "levelset", "batch"]
 
 # every symbol include/tracefem.h declares
 EXPORTS = [
@@ -41,7 +41,9 @@ EXPORTS = [
     "tf_mesh_info", "tf_mesh_download", "tf_levelset_upload", "tf_levelset_analytic", "tf_levelset_download",
     "tf_distribute_dofs", "tf_create_numb_on_interface_p1", "tf_dofs_download", "tf_patches_download", "tf_setup_fe_system",
     "tf_matrix_info", "tf_matrix_download", "tf_matrix_upload", "tf_lincomb", "tf_ch_block", "tf_vec_upload",
-    "tf_vec_download", "tf_vec_size", "tf_vec_fill", "tf_spmv", "tf_pcg_jacobi", "tf_gmres_jacobi", "tf_pcg_jacobi_noalloc", "tf_ch_steps", "tf_timing_enable",
+    "tf_vec_download", "tf_vec_size", "tf_vec_fill", "tf_spmv", "tf_pcg_jacobi", "tf_gmres_jacobi", "tf_pcg_jacobi_noalloc", "tf_ch_steps",
+    "tf_mesh_brick_batch", "tf_levelset_analytic_batch", "tf_batch_info", "tf_batch_lincomb", "tf_batch_pcg_jacobi",
+    "tf_batch_tune", "tf_batch_config", "tf_timing_enable",
     "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2",
     "tf_host_alloc", "tf_host_free",
 ]
@@ -99,6 +101,7 @@ class TraceFEM:
         self.h = h
         self.fe = None
         self.m = 0
+        self.batch_count = 0
 
     def close(self):
         if self.h:
@@ -135,6 +138,48 @@ class TraceFEM:
         """[-a,a]^3 with n^3 cubes."""
         self.brick([-a, -a, -a], [2 * a, 0, 0], [0, 2 * a, 0], [0, 0, 2 * a], n, n, n)
 
+    def brick_batch(self, n, orig, axes):
+        """count independent bricks: n[count,3] cubes, orig[count,3], axes[count,3,3] (rows e1, e2, e3)."""
+        n = np.ascontiguousarray(n, dtype=np.int32).reshape(-1, 3)
+        orig = np.ascontiguousarray(orig, dtype=np.float64).reshape(-1, 3)
+        axes = np.ascontiguousarray(axes, dtype=np.float64).reshape(-1, 9)
+        self.batch_count = n.shape[0]
+        self._check(self.L.tf_mesh_brick_batch(self.h, C.c_int(n.shape[0]), _ip(n), _dp(orig), _dp(axes)))
+
+    def batch_info(self, nnz=True):
+        """Per-instance starts (count+1 each): tets, cut tets, rows, nnz."""
+        k = self.batch_count + 1
+        t, c, r, z = (np.zeros(k, np.int64) for _ in range(4))
+        p = lambda a: a.ctypes.data_as(C.POINTER(C.c_int64))
+        self._check(self.L.tf_batch_info(self.h, p(t), p(c), p(r), p(z) if nnz else None))
+        return t, c, r, (z if nnz else None)
+
+    def batch_lincomb(self, forms, coeffs):
+        """TF_MAT_SYS = sum_k coeffs[i, k] forms[k] on the rows of instance i."""
+        f = np.ascontiguousarray(forms, dtype=np.int32)
+        co = np.ascontiguousarray(coeffs, dtype=np.float64).reshape(self.batch_count, f.size)
+        self._check(self.L.tf_batch_lincomb(self.h, C.c_int(f.size), _ip(f), _dp(co)))
+
+    def batch_pcg_jacobi(self, mat, vec_b, vec_x, tol=1e-10, max_iter=100000, rel=True, precision=PREC_FP64,
+                         check=True):
+        """One persistent launch over all instances; returns (status, iterations[count], residuals[count])."""
+        its = np.zeros(self.batch_count, np.int32)
+        res = np.zeros(self.batch_count)
+        st = self.L.tf_batch_pcg_jacobi(self.h, C.c_int(mat), C.c_int(vec_b), C.c_int(vec_x), C.c_int(precision),
+                                        C.c_int(max_iter), C.c_double(tol), C.c_int(int(rel)), _ip(its), _dp(res))
+        if check and st not in (OK, ERR_NOT_CONVERGED):
+            self._check(st)
+        return st, its, res
+
+    def batch_tune(self, mat, vec_b, precision=PREC_FP64):
+        lanes, threads = C.c_int(), C.c_int()
+        self._check(self.L.tf_batch_tune(self.h, C.c_int(mat), C.c_int(vec_b), C.c_int(precision), C.byref(lanes),
+                                         C.byref(threads)))
+        return lanes.value, threads.value
+
+    def batch_config(self, lanes=0, threads=0, use_graph=True):
+        self._check(self.L.tf_batch_config(self.h, C.c_int(lanes), C.c_int(threads), C.c_int(int(use_graph))))
+
     def mesh_upload(self, coords, tet_v, tet_e, edge_v):
         coords = np.ascontiguousarray(coords, dtype=np.float64)
         tet_v = np.ascontiguousarray(tet_v, dtype=np.int32)
@@ -166,6 +211,12 @@ class TraceFEM:
     def levelset_analytic(self, kind, par, p2=False):
         par = np.ascontiguousarray(par, dtype=np.float64)
         self._check(self.L.tf_levelset_analytic(self.h, C.c_int(kind), _dp(par), C.c_int(par.size), C.c_int(int(p2))))
+
+    def levelset_analytic_batch(self, kind, par, p2=False):
+        """par[count, npar]: one parameter set per batch instance."""
+        par = np.ascontiguousarray(par, dtype=np.float64).reshape(self.batch_count, -1)
+        self._check(self.L.tf_levelset_analytic_batch(self.h, C.c_int(kind), _dp(par), C.c_int(par.shape[1]),
+                                                      C.c_int(int(p2))))
 
     def levelset_download(self):
         nv, ne, nt = self.mesh_info()

@@ -121,6 +121,17 @@ int tf_destroy(tf_context* t) {
     tf::release(c->scan_tmp);
     tf::release(c->status);
     tf::release_solver_workspace(c);
+    tf::release_batch(c);
+    tf::release(c->batch_tab);
+    tf::release(c->batch_start);
+    tf::release(c->batch_ls);
+    tf::release(c->batch_rows);
+    tf::release(c->batch_coef);
+    tf::release(c->batch_resid);
+    tf::release(c->batch_xtmp);
+    tf::release(c->batch_queue);
+    tf::release(c->batch_iters);
+    tf::release(c->batch_order);
     tf::release(c->flush_buf);
     for (auto& e : c->markers)
         if (e) cudaEventDestroy(e);
@@ -169,6 +180,7 @@ int tf_mesh_upload(tf_context* t, int64_t nv, const double* coords, int64_t nt, 
     tf::MeshView& M = c->mesh;
     M = tf::MeshView{};
     M.explicit_mesh = 1;
+    c->batch_count = 0;
     M.nv = nv;
     M.ne = ne;
     M.nt = nt;
@@ -241,7 +253,7 @@ int tf_levelset_upload(tf_context* t, const double* ls_vert, const double* ls_ed
 int tf_levelset_analytic(tf_context* t, int kind, const double* par, int npar, int p2) {
     CTX_CHECK(t);
     cudaSetDevice(t->c.device);
-    TF_TRY(tf::levelset_analytic(&t->c, kind, par, npar, p2));
+    TF_TRY(tf::levelset_analytic(&t->c, kind, par, npar, p2, 0));
     TF_CUDA(&t->c, cudaStreamSynchronize(t->c.stream));
     return TF_OK;
 }
@@ -483,6 +495,79 @@ int tf_gmres_jacobi(tf_context* t, int mat, int vec_b, int vec_x, int restart, i
     TF_TRY(solver_vectors(c, mat, vec_b, vec_x));
     return tf::gmres_jacobi(c, c->mats[mat], c->vecs[vec_b].p, c->vecs[vec_x].p, restart, method, precision, max_iter,
                             tol, rel);
+}
+
+int tf_mesh_brick_batch(tf_context* t, int count, const int32_t* n, const double* orig, const double* axes) {
+    CTX_CHECK(t);
+    cudaSetDevice(t->c.device);
+    if (count > tf::kMaxBatchInstances) return tf::set_err(&t->c, TF_ERR_CAPACITY, "brick batch: too many instances");
+    return tf::mesh_set_brick_batch(&t->c, count, n, orig, axes);
+}
+
+int tf_levelset_analytic_batch(tf_context* t, int kind, const double* par, int npar, int p2) {
+    CTX_CHECK(t);
+    cudaSetDevice(t->c.device);
+    if (t->c.batch_count < 1) return tf::set_err(&t->c, TF_ERR_BAD_INPUT, "levelset batch: not a batch mesh");
+    TF_TRY(tf::levelset_analytic(&t->c, kind, par, npar, p2, t->c.batch_count));
+    TF_CUDA(&t->c, cudaStreamSynchronize(t->c.stream));
+    return TF_OK;
+}
+
+int tf_batch_info(tf_context* t, int64_t* tets, int64_t* cut, int64_t* rows, int64_t* nnz) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    const int n = c->batch_count;
+    if (n < 1) return tf::set_err(c, TF_ERR_BAD_INPUT, "batch_info: not a batch mesh");
+    if (tets) std::memcpy(tets, c->h_batch_tstart.data(), sizeof(int64_t) * (n + 1));
+    if (!cut && !rows && !nnz) return TF_OK;
+    TF_TRY(tf::batch_ranges(c));
+    if (cut) std::memcpy(cut, c->h_batch_cut.data(), sizeof(int64_t) * (n + 1));
+    if (rows) std::memcpy(rows, c->h_batch_rows.data(), sizeof(int64_t) * (n + 1));
+    if (nnz) {
+        if (c->pattern_dof_version != c->dof_version || !c->rowptr.p)
+            return tf::set_err(c, TF_ERR_BAD_INPUT, "batch_info: nnz needs tf_setup_fe_system first");
+        std::vector<int32_t> rp(n + 1);
+        for (int i = 0; i <= n; ++i)
+            TF_CUDA(c, cudaMemcpyAsync(&rp[i], c->rowptr.p + c->h_batch_rows[i], sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                       c->stream));
+        TF_CUDA(c, cudaStreamSynchronize(c->stream));
+        for (int i = 0; i <= n; ++i) nnz[i] = rp[i];
+    }
+    return TF_OK;
+}
+
+int tf_batch_lincomb(tf_context* t, int nterms, const int* forms, const double* coeffs) {
+    CTX_CHECK(t);
+    cudaSetDevice(t->c.device);
+    return tf::batch_lincomb(&t->c, nterms, forms, coeffs);
+}
+
+int tf_batch_pcg_jacobi(tf_context* t, int mat, int vec_b, int vec_x, int precision, int max_iter, double tol, int rel,
+                        int* iters, double* resids) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    TF_TRY(solver_vectors(c, mat, vec_b, vec_x));
+    return tf::batch_pcg(c, c->mats[mat], c->vecs[vec_b].p, c->vecs[vec_x].p, precision, max_iter, tol, rel, iters,
+                         resids);
+}
+
+int tf_batch_tune(tf_context* t, int mat, int vec_b, int precision, int* lanes, int* threads) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (precision != TF_PREC_FP64 && precision != TF_PREC_MIXED) return tf::set_err(c, TF_ERR_BAD_INPUT, "batch_tune: precision");
+    TF_TRY(mat_need(c, mat));
+    TF_TRY(vec_need(c, vec_b));
+    if ((int64_t)c->vecs[vec_b].n != c->mats[mat].m) return tf::set_err(c, TF_ERR_BAD_INPUT, "batch_tune: b has the wrong size");
+    return tf::batch_tune(c, c->mats[mat], c->vecs[vec_b].p, precision == TF_PREC_MIXED, lanes, threads);
+}
+
+int tf_batch_config(tf_context* t, int lanes, int threads, int use_graph) {
+    CTX_CHECK(t);
+    cudaSetDevice(t->c.device);
+    return tf::batch_config(&t->c, lanes, threads, use_graph);
 }
 
 int tf_ch_steps(tf_context* t, int nsteps, double dt, double mobility, double eps, double beta_s, double xi,

@@ -23,19 +23,46 @@ __host__ __device__ constexpr int ev1(int e) { return e == 0 ? 1 : (e == 1 || e 
 // 001,010,100,011,101,110,111; inside a class edges are numbered by the
 // brick index of their lower vertex.
 // ---------------------------------------------------------------------------
-struct MeshView {
-    int explicit_mesh;
-    int64_t nv, ne, nt;
-    // brick
+// One Kuhn brick: n1 x n2 x n3 cubes of 6 tets (geom/builder.cpp:99-180).
+struct Brick {
     int n1, n2, n3;
     double orig[3], o1[3], o2[3], o3[3];
-    int64_t eoff[8];
+    int64_t eoff[8];  // first edge of each direction class; eoff[7] = edges
+};
+
+// Row of the instance table of a batch: the brick and where its vertices,
+// edges and tets start in the concatenated numbering.
+struct BatchBrick {
+    Brick b;
+    int64_t v0, e0, t0;
+};
+
+struct MeshView {
+    int explicit_mesh;
+    int nbatch;  // > 0: concatenation of nbatch bricks, instance after instance
+    int64_t nv, ne, nt;
+    Brick b;     // the brick when nbatch == 0
+    // batch tables (device): instances, and nbatch+1 start offsets for the searches
+    const BatchBrick* batch;
+    const int64_t* tstart;
+    const int64_t* vstart;
+    const int64_t* estart;
     // explicit arrays (device)
     const double* coords;
     const int32_t* tet_v;
     const int32_t* tet_e;
     const int32_t* edge_v;
 };
+
+// instance owning index x: the largest i with start[i] <= x (start[0] = 0)
+__host__ __device__ inline int batch_find(const int64_t* start, int n, int64_t x) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= x) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
 
 __host__ __device__ inline int edir_class(int d3, int d2, int d1) {
     // offsets (d3,d2,d1) -> class index
@@ -66,25 +93,19 @@ __host__ __device__ inline void kuhn_offset(int l, int k, int& d3, int& d2, int&
     d3 = d[0]; d2 = d[1]; d1 = d[2];
 }
 
-__host__ __device__ inline void mesh_tet(const MeshView& M, int64_t t, int32_t v[4], int32_t e[6]) {
-    if (M.explicit_mesh) {
-        for (int k = 0; k < 4; ++k) v[k] = M.tet_v[4 * t + k];
-        if (e)
-            for (int k = 0; k < 6; ++k) e[k] = M.tet_e[6 * t + k];
-        return;
-    }
+__host__ __device__ inline void brick_tet(const Brick& B, int64_t t, int64_t v0, int64_t e0, int32_t v[4], int32_t e[6]) {
     const int64_t cube = t / 6;
     const int l = (int)(t - cube * 6);
-    const int i1 = (int)(cube % M.n1);
-    const int64_t r = cube / M.n1;
-    const int i2 = (int)(r % M.n2);
-    const int i3 = (int)(r / M.n2);
+    const int i1 = (int)(cube % B.n1);
+    const int64_t r = cube / B.n1;
+    const int i2 = (int)(r % B.n2);
+    const int i3 = (int)(r / B.n2);
     int p[4][3];
     for (int k = 0; k < 4; ++k) {
         int d3, d2, d1;
         kuhn_offset(l, k, d3, d2, d1);
         p[k][0] = i3 + d3; p[k][1] = i2 + d2; p[k][2] = i1 + d1;
-        v[k] = (int32_t)(((int64_t)p[k][0] * (M.n2 + 1) + p[k][1]) * (M.n1 + 1) + p[k][2]);
+        v[k] = (int32_t)(v0 + ((int64_t)p[k][0] * (B.n2 + 1) + p[k][1]) * (B.n1 + 1) + p[k][2]);
     }
     if (e) {
         for (int k = 0; k < 6; ++k) {
@@ -92,14 +113,39 @@ __host__ __device__ inline void mesh_tet(const MeshView& M, int64_t t, int32_t v
             const int* b = p[ev1(k)];
             const int d3 = b[0] - a[0], d2 = b[1] - a[1], d1 = b[2] - a[2];
             const int c = edir_class(d3, d2, d1);
-            e[k] = (int32_t)(M.eoff[c] + ((int64_t)a[0] * (M.n2 + 1 - d2) + a[1]) * (M.n1 + 1 - d1) + a[2]);
+            e[k] = (int32_t)(e0 + B.eoff[c] + ((int64_t)a[0] * (B.n2 + 1 - d2) + a[1]) * (B.n1 + 1 - d1) + a[2]);
         }
     }
 }
 
-// Vertex coordinates; for the brick, ((orig + i1*o1) + i2*o2) + i3*o3 per
+__device__ inline void mesh_tet(const MeshView& M, int64_t t, int32_t v[4], int32_t e[6]) {
+    if (M.explicit_mesh) {
+        for (int k = 0; k < 4; ++k) v[k] = M.tet_v[4 * t + k];
+        if (e)
+            for (int k = 0; k < 6; ++k) e[k] = M.tet_e[6 * t + k];
+        return;
+    }
+    if (M.nbatch) {
+        const BatchBrick& I = M.batch[batch_find(M.tstart, M.nbatch, t)];
+        brick_tet(I.b, t - I.t0, I.v0, I.e0, v, e);
+        return;
+    }
+    brick_tet(M.b, t, 0, 0, v, e);
+}
+
+// Vertex coordinates; for a brick, ((orig + i1*o1) + i2*o2) + i3*o3 per
 // component with round-to-nearest products and sums (no contraction), as in
 // BrickBuilderCL::build_ser_impl.
+__device__ inline void brick_coord(const Brick& B, int64_t v, double x[3]) {
+    const int i1 = (int)(v % (B.n1 + 1));
+    const int64_t r = v / (B.n1 + 1);
+    const int i2 = (int)(r % (B.n2 + 1));
+    const int i3 = (int)(r / (B.n2 + 1));
+    for (int c = 0; c < 3; ++c)
+        x[c] = __dadd_rn(__dadd_rn(__dadd_rn(B.orig[c], __dmul_rn((double)i1, B.o1[c])), __dmul_rn((double)i2, B.o2[c])),
+                         __dmul_rn((double)i3, B.o3[c]));
+}
+
 __device__ inline void mesh_coord(const MeshView& M, int32_t v, double x[3]) {
     if (M.explicit_mesh) {
         x[0] = M.coords[3 * (int64_t)v];
@@ -107,13 +153,12 @@ __device__ inline void mesh_coord(const MeshView& M, int32_t v, double x[3]) {
         x[2] = M.coords[3 * (int64_t)v + 2];
         return;
     }
-    const int i1 = v % (M.n1 + 1);
-    const int r = v / (M.n1 + 1);
-    const int i2 = r % (M.n2 + 1);
-    const int i3 = r / (M.n2 + 1);
-    for (int c = 0; c < 3; ++c)
-        x[c] = __dadd_rn(__dadd_rn(__dadd_rn(M.orig[c], __dmul_rn((double)i1, M.o1[c])), __dmul_rn((double)i2, M.o2[c])),
-                         __dmul_rn((double)i3, M.o3[c]));
+    if (M.nbatch) {
+        const BatchBrick& I = M.batch[batch_find(M.vstart, M.nbatch, v)];
+        brick_coord(I.b, v - I.v0, x);
+        return;
+    }
+    brick_coord(M.b, v, x);
 }
 
 // ---------------------------------------------------------------------------
@@ -217,7 +262,31 @@ struct Context {
     DBuf<int32_t> sell_ptr[TF_NUM_MATS], sell_col[TF_NUM_MATS], sell_src[TF_NUM_MATS], sell_perm[TF_NUM_MATS];
     DBuf<double> sell_v64[TF_NUM_MATS];
     DBuf<float> sell_v32[TF_NUM_MATS];
+    // batch of bricks (tf_mesh_brick_batch); 0 = single mesh
+    int batch_count = 0;
+    DBuf<BatchBrick> batch_tab;
+    DBuf<int64_t> batch_start;        // tet, vertex, edge starts (3 x (count+1))
+    DBuf<unsigned char> batch_ls;     // per-instance level-set parameters
+    std::vector<int64_t> h_batch_tstart, h_batch_vstart, h_batch_estart;
+    // per-instance ranges after numbering: cut tets and rows (count+1 each)
+    int64_t batch_dof_version = -1;
+    std::vector<int64_t> h_batch_cut, h_batch_rows;
+    DBuf<int64_t> batch_rows;         // device: row starts, then cut-tet starts (2 x (count+1))
+    // batched PCG
+    DBuf<double> batch_coef, batch_resid, batch_xtmp;
+    DBuf<int> batch_queue, batch_iters;
+    DBuf<int32_t> batch_order;
+    std::vector<int64_t> h_batch_nnz;
+    int64_t batch_order_gen = -1, batch_tuned_gen = -1;
+    bool batch_tuned_mixed = false, batch_use_graph = true;
+    int batch_lanes = 0, batch_threads = 0;             // autotuned
+    int batch_fixed_lanes = 0, batch_fixed_threads = 0; // set by tf_batch_config (0: autotune)
+    double* h_batch_out = nullptr;                      // pinned: iterations, then residuals
+    cudaGraphExec_t batch_exec = nullptr;
+    std::vector<int64_t> batch_graph_key;
 };
+
+constexpr int kMaxBatchInstances = 65536;
 
 // ---------------------------------------------------------------------------
 // error handling helpers (host)
@@ -276,7 +345,8 @@ int patch_dump(Context* c, const int32_t* tets, int64_t count, int32_t* nf, int3
                int32_t* nverts, double* verts);
 int mesh_set_brick(Context* c, const double orig[3], const double e1[3], const double e2[3], const double e3[3],
                    int n1, int n2, int n3);
-int levelset_analytic(Context* c, int kind, const double* par, int npar, int p2);
+int levelset_analytic(Context* c, int kind, const double* par, int npar, int p2, int count);
+int mesh_set_brick_batch(Context* c, int count, const int32_t* n, const double* orig, const double* axes);
 int levelset_p1_edges(Context* c);
 int distribute_dofs(Context* c, int fe, double dist);
 int numb_on_interface_p1(Context* c, double omit_bound);
@@ -291,6 +361,13 @@ int ensure_diag(Context* c, CSR& A);
 int ch_steps(Context* c, int nsteps, double dt, double mob, double eps, double beta_s, double xi, double rho_vol,
              int restart, double tol, int max_iter, int warm, int* iters, double* resids);
 void release_solver_workspace(Context* c);
+int batch_ranges(Context* c);
+int batch_lincomb(Context* c, int nterms, const int* forms, const double* coeffs);
+int batch_tune(Context* c, CSR& A, const double* b, bool mixed, int* lanes_out, int* threads_out);
+int batch_pcg(Context* c, CSR& A, const double* b, double* x, int precision, int max_iter, double tol, int rel,
+              int* iters, double* resids);
+int batch_config(Context* c, int lanes, int threads, int use_graph);
+void release_batch(Context* c);
 int ensure_vals32(Context* c, CSR& A);
 int ensure_sell(Context* c, CSR& A, bool fp32);
 

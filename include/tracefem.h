@@ -200,6 +200,46 @@ int tf_pcg_jacobi(tf_context* ctx, int mat, int vec_b, int vec_x, int precision,
 int tf_gmres_jacobi(tf_context* ctx, int mat, int vec_b, int vec_x, int restart, int method, int precision,
                     int* max_iter, double* tol, int rel);
 
+/* ---- batches of independent problems ----------------------------------------------- */
+/* The reference solves one surface problem per MultiGridCL; these calls run
+ * `count` independent problems of uneven size as one: instance i is the brick
+ * n[3i..3i+2] cubes spanned by axes[9i..9i+8] (e1, e2, e3) from orig[3i..3i+2]
+ * (BrickBuilderCL, geom/builder.cpp:99-180), numbered after instance i-1.
+ * tf_distribute_dofs, tf_setup_fe_system and the per-form calls then work on
+ * the whole batch: each instance gets exactly the DOF numbering, CSR rows and
+ * entries it would get alone, shifted by the rows of the instances before it
+ * (the matrices are block diagonal).                                           */
+int tf_mesh_brick_batch(tf_context* ctx, int count, const int32_t* n, const double* orig, const double* axes);
+/* Level set per instance: par holds count consecutive sets of npar values of
+ * the TF_LS_* kind (LSInit / LinearLSInit, surfactant/surfactant.cpp:733-758). */
+int tf_levelset_analytic_batch(tf_context* ctx, int kind, const double* par, int npar, int p2);
+/* Per-instance ranges after tf_distribute_dofs (each array count+1 long, NULL
+ * to skip): tets, cut (active) tets, rows (DOFs); nnz needs the pattern of
+ * tf_setup_fe_system.                                                          */
+int tf_batch_info(tf_context* ctx, int64_t* tets, int64_t* cut, int64_t* rows, int64_t* nnz);
+/* TF_MAT_SYS = sum_k coeffs[i*nterms + k] * forms[k] on the rows of instance i
+ * (the per-problem LinComb of num/spmat.h:712-715, e.g. M + A + h_i C_n).      */
+int tf_batch_lincomb(tf_context* ctx, int nterms, const int* forms, const double* coeffs);
+/* Jacobi-PCG (num/krylovsolver.h:107-189) on every instance at once, one
+ * persistent launch: CTAs take instances from a queue, largest first, and
+ * each solves its instance to relative residual tol (rel != 0) within
+ * max_iter iterations, x (vec_x) being the initial guess and the result.
+ * TF_PREC_MIXED: FP32 iterations with FP64 iterate and FP64 residual
+ * replacement.  iters[count] and resids[count] (may be NULL) receive each
+ * instance's iterations and reached residual; TF_ERR_NOT_CONVERGED when any
+ * instance missed tol.  Unless tf_batch_config fixed them, the lanes per row
+ * and CTA size come from tf_batch_tune, run on the first solve of a pattern,
+ * and the launch sequence is captured once as a CUDA graph and replayed while
+ * matrix, vectors and parameters stay the same.                                */
+int tf_batch_pcg_jacobi(tf_context* ctx, int mat, int vec_b, int vec_x, int precision, int max_iter, double tol,
+                        int rel, int* iters, double* resids);
+/* Autotuner: times every (lanes per row in {2,4,8,16}, CTA size in
+ * {128,256,512,1024}) candidate on this batch and keeps the fastest.           */
+int tf_batch_tune(tf_context* ctx, int mat, int vec_b, int precision, int* lanes, int* threads);
+/* lanes = 0: autotune; else fixed lanes per row and CTA size.  use_graph = 0
+ * launches the solve directly instead of replaying a CUDA graph.               */
+int tf_batch_config(tf_context* ctx, int lanes, int threads, int use_graph);
+
 /* ---- allocation-free PCG -------------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory: applications that manage every GPU byte through their own pool and
@@ -250,7 +290,8 @@ int tf_ch_steps(tf_context* ctx, int nsteps, double dt, double mobility, double 
 #define TF_K_PCG 6
 #define TF_K_GMRES 7
 #define TF_K_LEVELSET 8
-#define TF_NUM_KERNELS 9
+#define TF_K_BATCH 9
+#define TF_NUM_KERNELS 10
 int tf_timing_enable(tf_context* ctx, int on);
 int tf_timing_get(tf_context* ctx, int kernel, double* total_ms, int64_t* launches);
 int tf_timing_reset(tf_context* ctx);
