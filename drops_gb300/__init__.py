@@ -32,6 +32,7 @@ VEC_RHS, VEC_X, VEC_B, VEC_CHI, VEC_T0, VEC_T1, VEC_T2, VEC_T3 = range(8)
 LS_SPHERE, LS_TORUS, LS_ELLIPSOID, LS_PLANE = range(4)
 RHS_NONE, RHS_SPHERE_XYZ, RHS_CONST = range(3)
 PREC_FP64, PREC_MIXED = 0, 1
+MLP_IN, MLP_WEIGHTS = 80, 16640
 K_CLASSIFY, K_NUMBER, K_ASSEMBLE, K_PATTERN, K_SCATTER, K_SPMV, K_PCG, K_GMRES, K_LEVELSET, K_BATCH = range(10)
 KERNEL_NAMES = ["classify", "number", "assemble", "pattern", "scatter", "spmv", "pcg", "gmres", "levelset", "batch"]
 
@@ -43,7 +44,8 @@ EXPORTS = [
     "tf_matrix_info", "tf_matrix_download", "tf_matrix_upload", "tf_lincomb", "tf_ch_block", "tf_vec_upload",
     "tf_vec_download", "tf_vec_size", "tf_vec_fill", "tf_spmv", "tf_pcg_jacobi", "tf_gmres_jacobi", "tf_pcg_jacobi_noalloc", "tf_ch_steps",
     "tf_mesh_brick_batch", "tf_levelset_analytic_batch", "tf_batch_info", "tf_batch_lincomb", "tf_batch_pcg_jacobi",
-    "tf_batch_tune", "tf_batch_config", "tf_timing_enable",
+    "tf_batch_tune", "tf_batch_config", "tf_mlp_init", "tf_mlp_get_weights", "tf_mlp_set_weights", "tf_mlp_forward",
+    "tf_mlp_gradient", "tf_mlp_train", "tf_ch_features", "tf_ch_steps_learned", "tf_timing_enable",
     "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2",
     "tf_host_alloc", "tf_host_free",
 ]
@@ -328,6 +330,75 @@ class TraceFEM:
         if check and st not in (OK, ERR_NOT_CONVERGED):
             self._check(st)
         return st, it.value, t.value
+
+    # ---- learned warm start -------------------------------------------------
+    def mlp_init(self, seed=1234):
+        self._check(self.L.tf_mlp_init(self.h, C.c_uint64(seed)))
+
+    def mlp_weights(self, w=None):
+        """Returns the FP32 weights (MLP_WEIGHTS floats); sets them first when w is given."""
+        if w is not None:
+            w = np.ascontiguousarray(w, dtype=np.float32)
+            self._check(self.L.tf_mlp_set_weights(self.h, w.ctypes.data_as(C.POINTER(C.c_float))))
+        out = np.empty(MLP_WEIGHTS, np.float32)
+        self._check(self.L.tf_mlp_get_weights(self.h, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    @staticmethod
+    def _u16(a):
+        return np.ascontiguousarray(a, dtype=np.uint16).ctypes.data_as(C.POINTER(C.c_uint16))
+
+    def mlp_forward(self, X):
+        """X: (n, 80) BF16 bit patterns (uint16); returns (n, 2) float32."""
+        X = np.ascontiguousarray(X, dtype=np.uint16)
+        n = X.shape[0]
+        out = np.empty((n, 2), np.float32)
+        self._check(self.L.tf_mlp_forward(self.h, X.ctypes.data_as(C.POINTER(C.c_uint16)), C.c_int64(n),
+                                          out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def mlp_gradient(self, X, Y):
+        X = np.ascontiguousarray(X, dtype=np.uint16)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        g = np.empty(MLP_WEIGHTS, np.float32)
+        loss = C.c_double()
+        self._check(self.L.tf_mlp_gradient(self.h, X.ctypes.data_as(C.POINTER(C.c_uint16)),
+                                           Y.ctypes.data_as(C.POINTER(C.c_float)), C.c_int64(X.shape[0]),
+                                           g.ctypes.data_as(C.POINTER(C.c_float)), C.byref(loss)))
+        return g, loss.value
+
+    def mlp_train(self, X, Y, epochs=1, minibatch_tiles=16, lr=1e-3):
+        X = np.ascontiguousarray(X, dtype=np.uint16)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        loss = C.c_double()
+        self._check(self.L.tf_mlp_train(self.h, X.ctypes.data_as(C.POINTER(C.c_uint16)),
+                                        Y.ctypes.data_as(C.POINTER(C.c_float)), C.c_int64(X.shape[0]), C.c_int(epochs),
+                                        C.c_int(minibatch_tiles), C.c_float(lr), C.byref(loss)))
+        return loss.value
+
+    def ch_features(self, vec_cur, vec_old, vec_next=-1):
+        m = self.m
+        X = np.empty((m, MLP_IN), np.uint16)
+        Y = np.empty((m, 2), np.float32)
+        self._check(self.L.tf_ch_features(self.h, C.c_int(vec_cur), C.c_int(vec_old), C.c_int(vec_next),
+                                          X.ctypes.data_as(C.POINTER(C.c_uint16)),
+                                          Y.ctypes.data_as(C.POINTER(C.c_float))))
+        return X, (Y if vec_next >= 0 else None)
+
+    def ch_steps_learned(self, nsteps, dt, mobility, eps, beta_s, xi, rho_vol, restart=50, tol=1e-10,
+                         max_iter=100000, learned=True, train_steps=100, epochs=2, minibatch_tiles=16, lr=1e-3,
+                         check=True):
+        """Cahn-Hilliard steps with the learned warm start; returns (status, iterations[], residuals[], used[])."""
+        k = max(nsteps, 1)
+        its, res, used = np.zeros(k, np.int32), np.zeros(k), np.zeros(k, np.int32)
+        st = self.L.tf_ch_steps_learned(self.h, C.c_int(nsteps), C.c_double(dt), C.c_double(mobility),
+                                        C.c_double(eps), C.c_double(beta_s), C.c_double(xi), C.c_double(rho_vol),
+                                        C.c_int(restart), C.c_double(tol), C.c_int(max_iter), C.c_int(int(learned)),
+                                        C.c_int(train_steps), C.c_int(epochs), C.c_int(minibatch_tiles),
+                                        C.c_float(lr), _ip(its), _dp(res), _ip(used))
+        if check:
+            self._check(st)
+        return st, its[:nsteps], res[:nsteps], used[:nsteps]
 
     def ch_steps(self, nsteps, dt, mobility, eps, beta_s, xi, rho_vol, restart=50, tol=1e-10, max_iter=100000,
                  warm=True, check=True):

@@ -425,6 +425,21 @@ static int ensure_csr_f32(Context* c, CSR& A) {
     return TF_OK;
 }
 
+__global__ void k_batch_nnz(int count, const int64_t* __restrict__ rows, const int32_t* __restrict__ rowptr,
+                            int64_t* __restrict__ nnz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) nnz[i] = (int64_t)rowptr[rows[i + 1]] - rowptr[rows[i]];
+}
+
+// Structure of the batch for caching the queue order and the tuned launch
+// shape: rebuilding the same problems gives the same key.
+static std::vector<int64_t> batch_key(Context* c, const std::vector<int64_t>& nnz, bool mixed) {
+    std::vector<int64_t> k(c->h_batch_rows);
+    k.insert(k.end(), nnz.begin(), nnz.end());
+    k.push_back(mixed);
+    return k;
+}
+
 static int batch_workspace(Context* c, CSR& A, bool mixed) {
     const int n = c->batch_count;
     TF_TRY(ensure(c, c->batch_queue, 1));
@@ -443,20 +458,22 @@ static int batch_workspace(Context* c, CSR& A, bool mixed) {
     }
     // largest instances first (longest-processing-time order for the queue)
     if (c->batch_order_gen != A.pattern_gen) {
-        std::vector<int32_t> rp(n + 1);
+        TF_TRY(ensure(c, c->batch_nnz, (size_t)n));
+        k_batch_nnz<<<(n + 127) / 128, 128, 0, c->stream>>>(n, c->batch_rows.p, A.rowptr, c->batch_nnz.p);
+        ++c->launches;
+        TF_CUDA(c, cudaGetLastError());
         std::vector<int64_t> nnz(n);
-        for (int i = 0; i <= n; ++i) {
-            const int64_t r = c->h_batch_rows[i];
-            TF_CUDA(c, cudaMemcpyAsync(&rp[i], A.rowptr + r, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+        TF_CUDA(c, cudaMemcpyAsync(nnz.data(), c->batch_nnz.p, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, c->stream));
+        TF_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (nnz != c->h_batch_nnz) {
+            std::vector<int32_t> ord(n);
+            std::iota(ord.begin(), ord.end(), 0);
+            std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return nnz[x] > nnz[y]; });
+            TF_CUDA(c, cudaMemcpyAsync(c->batch_order.p, ord.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice,
+                                       c->stream));
+            TF_CUDA(c, cudaStreamSynchronize(c->stream));
+            c->h_batch_nnz = nnz;
         }
-        TF_CUDA(c, cudaStreamSynchronize(c->stream));
-        for (int i = 0; i < n; ++i) nnz[i] = (int64_t)rp[i + 1] - rp[i];
-        std::vector<int32_t> ord(n);
-        std::iota(ord.begin(), ord.end(), 0);
-        std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return nnz[x] > nnz[y]; });
-        c->h_batch_nnz = nnz;
-        TF_CUDA(c, cudaMemcpyAsync(c->batch_order.p, ord.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, c->stream));
-        TF_CUDA(c, cudaStreamSynchronize(c->stream));
         c->batch_order_gen = A.pattern_gen;
     }
     return TF_OK;
@@ -529,8 +546,7 @@ int batch_tune(Context* c, CSR& A, const double* b, bool mixed, int* lanes_out, 
     TF_TRY(st);
     c->batch_lanes = bl;
     c->batch_threads = bt;
-    c->batch_tuned_gen = A.pattern_gen;
-    c->batch_tuned_mixed = mixed;
+    c->batch_tuned_key = batch_key(c, c->h_batch_nnz, mixed);
     if (lanes_out) *lanes_out = bl;
     if (threads_out) *threads_out = bt;
     return TF_OK;
@@ -552,8 +568,7 @@ int batch_pcg(Context* c, CSR& A, const double* b, double* x, int precision, int
     const int n = c->batch_count;
     if (n > kMaxBatchInstances) return set_err(c, TF_ERR_CAPACITY, "batch_pcg: too many instances");
     TF_TRY(batch_workspace(c, A, mixed));
-    if (c->batch_fixed_lanes == 0 &&
-        (c->batch_tuned_gen != A.pattern_gen || c->batch_tuned_mixed != mixed || c->batch_lanes == 0))
+    if (c->batch_fixed_lanes == 0 && (c->batch_lanes == 0 || c->batch_tuned_key != batch_key(c, c->h_batch_nnz, mixed)))
         TF_TRY(batch_tune(c, A, b, mixed, nullptr, nullptr));
     const int G = c->batch_fixed_lanes ? c->batch_fixed_lanes : c->batch_lanes;
     const int T = c->batch_fixed_lanes ? c->batch_fixed_threads : c->batch_threads;
@@ -617,7 +632,10 @@ int batch_config(Context* c, int lanes, int threads, int use_graph) {
         return set_err(c, TF_ERR_BAD_INPUT, "batch_config: lanes in {2,4,8,16}, threads a multiple of 32 in [64,1024]");
     c->batch_fixed_lanes = lanes;
     c->batch_fixed_threads = lanes ? threads : 0;
-    if (!lanes) c->batch_lanes = 0;  // re-tune on the next solve
+    if (!lanes) {  // re-tune on the next solve
+        c->batch_lanes = 0;
+        c->batch_tuned_key.clear();
+    }
     c->batch_use_graph = use_graph != 0;
     drop_batch_graph(c);
     return TF_OK;

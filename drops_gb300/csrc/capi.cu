@@ -55,7 +55,10 @@ int tf_create(tf_context** out, int device) {
     Context* c = &t->c;
     c->device = device;
     c->num_sms = prop.multiProcessorCount;
-    // launch-shape knob for the persistent Krylov kernels (resident blocks per SM)
+    // launch shape of the persistent Krylov kernels: resident blocks per SM.
+    // Two measured fastest on GB300 (fewer blocks make the grid barrier
+    // cheaper, more hide gather latency); TF_KRY_BLOCKS_PER_SM overrides.
+    c->kry_blocks_per_sm = 2;
     if (const char* e = std::getenv("TF_KRY_BLOCKS_PER_SM")) c->kry_blocks_per_sm = std::atoi(e);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
@@ -132,6 +135,24 @@ int tf_destroy(tf_context* t) {
     tf::release(c->batch_queue);
     tf::release(c->batch_iters);
     tf::release(c->batch_order);
+    tf::release(c->batch_nnz);
+    tf::release(c->mlp_w);
+    tf::release(c->mlp_m1);
+    tf::release(c->mlp_m2);
+    tf::release(c->mlp_grad);
+    tf::release(c->mlp_lossacc);
+    tf::release(c->mlp_w16);
+    tf::release(c->mlp_xio);
+    tf::release(c->mlp_yio);
+    tf::release(c->mlp_pio);
+    tf::release(c->ch_part);
+    tf::release(c->ch_scales);
+    tf::release(c->ch_hist);
+    tf::release(c->ch_xyz);
+    tf::release(c->ch_nrm);
+    tf::release(c->ch_Y);
+    tf::release(c->ch_pred);
+    tf::release(c->ch_X);
     tf::release(c->flush_buf);
     for (auto& e : c->markers)
         if (e) cudaEventDestroy(e);
@@ -568,6 +589,127 @@ int tf_batch_config(tf_context* t, int lanes, int threads, int use_graph) {
     CTX_CHECK(t);
     cudaSetDevice(t->c.device);
     return tf::batch_config(&t->c, lanes, threads, use_graph);
+}
+
+int tf_mlp_init(tf_context* t, uint64_t seed) {
+    CTX_CHECK(t);
+    cudaSetDevice(t->c.device);
+    return tf::mlp_init(&t->c, seed);
+}
+
+int tf_mlp_get_weights(tf_context* t, float* w) {
+    CTX_CHECK(t);
+    if (!w) return tf::set_err(&t->c, TF_ERR_BAD_INPUT, "mlp: null buffer");
+    cudaSetDevice(t->c.device);
+    return tf::mlp_get_weights(&t->c, w);
+}
+
+int tf_mlp_set_weights(tf_context* t, const float* w) {
+    CTX_CHECK(t);
+    if (!w) return tf::set_err(&t->c, TF_ERR_BAD_INPUT, "mlp: null buffer");
+    cudaSetDevice(t->c.device);
+    return tf::mlp_set_weights(&t->c, w);
+}
+
+static int mlp_upload(Context* c, const uint16_t* X, const float* Y, int64_t n) {
+    if (n <= 0 || !X) return tf::set_err(c, TF_ERR_BAD_INPUT, "mlp: n > 0 and inputs required");
+    TF_TRY(tf::ensure(c, c->mlp_xio, (size_t)(TF_MLP_IN * n)));
+    TF_CUDA(c, cudaMemcpyAsync(c->mlp_xio.p, X, sizeof(uint16_t) * TF_MLP_IN * n, cudaMemcpyHostToDevice, c->stream));
+    if (Y) {
+        TF_TRY(tf::ensure(c, c->mlp_yio, (size_t)(2 * n)));
+        TF_CUDA(c, cudaMemcpyAsync(c->mlp_yio.p, Y, sizeof(float) * 2 * n, cudaMemcpyHostToDevice, c->stream));
+    }
+    return TF_OK;
+}
+
+int tf_mlp_forward(tf_context* t, const uint16_t* X, int64_t n, float* pred) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (!pred) return tf::set_err(c, TF_ERR_BAD_INPUT, "mlp: null output");
+    TF_TRY(mlp_upload(c, X, nullptr, n));
+    TF_TRY(tf::ensure(c, c->mlp_pio, (size_t)(2 * n)));
+    TF_TRY(tf::mlp_forward_dev(c, c->mlp_xio.p, n, c->mlp_pio.p));
+    TF_CUDA(c, cudaMemcpyAsync(pred, c->mlp_pio.p, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, c->stream));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TF_OK;
+}
+
+int tf_mlp_gradient(tf_context* t, const uint16_t* X, const float* Y, int64_t n, float* grad, double* loss) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (!Y || !grad) return tf::set_err(c, TF_ERR_BAD_INPUT, "mlp: targets and gradient buffer required");
+    TF_TRY(mlp_upload(c, X, Y, n));
+    TF_TRY(tf::ensure(c, c->mlp_pio, (size_t)TF_MLP_WEIGHTS));
+    TF_TRY(tf::mlp_epoch_dev(c, c->mlp_xio.p, c->mlp_yio.p, n, 0, 0.f, c->mlp_pio.p, loss));
+    TF_CUDA(c, cudaMemcpyAsync(grad, c->mlp_pio.p, sizeof(float) * TF_MLP_WEIGHTS, cudaMemcpyDeviceToHost, c->stream));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TF_OK;
+}
+
+int tf_mlp_train(tf_context* t, const uint16_t* X, const float* Y, int64_t n, int epochs, int minibatch_tiles, float lr,
+                 double* loss) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (!Y || epochs < 1 || minibatch_tiles < 1 || !(lr > 0.f))
+        return tf::set_err(c, TF_ERR_BAD_INPUT, "mlp_train: targets, epochs >= 1, minibatch_tiles >= 1, lr > 0");
+    TF_TRY(mlp_upload(c, X, Y, n));
+    for (int e = 0; e < epochs; ++e)
+        TF_TRY(tf::mlp_epoch_dev(c, c->mlp_xio.p, c->mlp_yio.p, n, minibatch_tiles, lr, nullptr,
+                                 e + 1 == epochs ? loss : nullptr));
+    return TF_OK;
+}
+
+int tf_ch_features(tf_context* t, int vec_cur, int vec_old, int vec_next, uint16_t* X, float* Y) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    const int64_t m = c->mats[TF_FORM_M].m;
+    if (!c->mats[TF_FORM_M].vals || !X) return tf::set_err(c, TF_ERR_BAD_INPUT, "ch_features: TF_FORM_M and X required");
+    TF_TRY(vec_need(c, vec_cur));
+    TF_TRY(vec_need(c, vec_old));
+    if ((int64_t)c->vecs[vec_cur].n != 2 * m || (int64_t)c->vecs[vec_old].n != 2 * m)
+        return tf::set_err(c, TF_ERR_BAD_INPUT, "ch_features: states hold [chi; omega] (2m)");
+    const double* nx = nullptr;
+    if (vec_next >= 0) {
+        TF_TRY(vec_need(c, vec_next));
+        if ((int64_t)c->vecs[vec_next].n != 2 * m || !Y) return tf::set_err(c, TF_ERR_BAD_INPUT, "ch_features: next state / Y");
+        nx = c->vecs[vec_next].p;
+    }
+    TF_TRY(tf::ch_features_dev(c, c->vecs[vec_cur].p, c->vecs[vec_old].p, nx));
+    TF_CUDA(c, cudaMemcpyAsync(X, c->ch_X.p, sizeof(uint16_t) * TF_MLP_IN * m, cudaMemcpyDeviceToHost, c->stream));
+    if (nx) TF_CUDA(c, cudaMemcpyAsync(Y, c->ch_Y.p, sizeof(float) * 2 * m, cudaMemcpyDeviceToHost, c->stream));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TF_OK;
+}
+
+int tf_ch_steps_learned(tf_context* t, int nsteps, double dt, double mobility, double eps, double beta_s, double xi,
+                        double rho_vol, int restart, double tol, int max_iter, int learned, int train_steps, int epochs,
+                        int minibatch_tiles, float lr, int* iters, double* resids, int* used) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (restart < 2 || max_iter < 1 || tol <= 0. || epochs < 0 || minibatch_tiles < 1 || lr < 0.f)
+        return tf::set_err(c, TF_ERR_BAD_INPUT, "ch_steps_learned: bad arguments");
+    tf::ChLearnParams P;
+    P.nsteps = nsteps;
+    P.dt = dt;
+    P.mob = mobility;
+    P.eps = eps;
+    P.beta_s = beta_s;
+    P.xi = xi;
+    P.rho_vol = rho_vol;
+    P.restart = restart;
+    P.tol = tol;
+    P.max_iter = max_iter;
+    P.learned = learned;
+    P.train_steps = learned ? train_steps : 0;
+    P.epochs = epochs;
+    P.mb_tiles = minibatch_tiles;
+    P.lr = lr;
+    return tf::ch_steps_learned(c, P, iters, resids, used);
 }
 
 int tf_ch_steps(tf_context* t, int nsteps, double dt, double mobility, double eps, double beta_s, double xi,

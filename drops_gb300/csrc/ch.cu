@@ -38,6 +38,22 @@ __global__ void k_ch_rhs(int64_t m, int64_t nslices, const int32_t* __restrict__
     }
 }
 
+// right-hand side of one step from the state X = [chi; omega] into TF_VEC_B, chi into TF_VEC_CHI
+int ch_rhs(Context* c, const double* X, double dt, double beta_s, double xi) {
+    CSR& M = c->mats[TF_FORM_M];
+    const int64_t m = M.m;
+    const double* f = (int64_t)c->vecs[TF_VEC_RHS].n == m ? c->vecs[TF_VEC_RHS].p : nullptr;
+    TF_TRY(ensure_sell(c, M, false));
+    TF_TRY(ensure(c, c->vecs[TF_VEC_B], (size_t)(2 * m)));
+    TF_TRY(ensure(c, c->vecs[TF_VEC_CHI], (size_t)m));
+    k_ch_rhs<<<grid_for(c, M.sell.nslices * 32), kBlock, 0, c->stream>>>(
+        m, M.sell.nslices, M.sell.perm, M.sell.ptr, M.sell.col, M.sell.v64, X, f, 1.0 / dt, beta_s, xi,
+        c->vecs[TF_VEC_B].p, c->vecs[TF_VEC_CHI].p);
+    ++c->launches;
+    TF_CUDA(c, cudaGetLastError());
+    return TF_OK;
+}
+
 int ch_steps(Context* c, int nsteps, double dt, double mob, double eps, double beta_s, double xi, double rho_vol,
              int restart, double tol, int max_iter, int warm, int* iters, double* resids) {
     CSR& M = c->mats[TF_FORM_M];
@@ -46,20 +62,10 @@ int ch_steps(Context* c, int nsteps, double dt, double mob, double eps, double b
     if (dt <= 0. || nsteps < 0) return set_err(c, TF_ERR_BAD_INPUT, "ch_steps: dt > 0, nsteps >= 0");
     const int64_t m = M.m;
     if ((int64_t)c->vecs[TF_VEC_X].n != 2 * m) return set_err(c, TF_ERR_BAD_INPUT, "ch_steps: TF_VEC_X must hold [chi; omega] (2m)");
-    const double* f = nullptr;
-    if ((int64_t)c->vecs[TF_VEC_RHS].n == m) f = c->vecs[TF_VEC_RHS].p;
     TF_TRY(ch_block(c, 1.0 / dt, mob, rho_vol, eps * eps, beta_s, 0));
-    TF_TRY(ensure_sell(c, M, false));
-    TF_TRY(ensure(c, c->vecs[TF_VEC_B], (size_t)(2 * m)));
-    TF_TRY(ensure(c, c->vecs[TF_VEC_CHI], (size_t)m));
-    TF_TRY(ensure(c, c->vecs[TF_VEC_T0], (size_t)(2 * m)));
     for (int step = 0; step < nsteps; ++step) {
         double* X = c->vecs[TF_VEC_X].p;
-        k_ch_rhs<<<grid_for(c, M.sell.nslices * 32), kBlock, 0, c->stream>>>(
-            m, M.sell.nslices, M.sell.perm, M.sell.ptr, M.sell.col, M.sell.v64, X, f, 1.0 / dt, beta_s, xi, c->vecs[TF_VEC_B].p,
-            c->vecs[TF_VEC_CHI].p);
-        ++c->launches;
-        TF_CUDA(c, cudaGetLastError());
+        TF_TRY(ch_rhs(c, X, dt, beta_s, xi));
         if (!warm) TF_CUDA(c, cudaMemsetAsync(X, 0, sizeof(double) * 2 * m, c->stream));
         int it = max_iter;
         double res = tol;
@@ -70,6 +76,7 @@ int ch_steps(Context* c, int nsteps, double dt, double mob, double eps, double b
         if (st != TF_OK) return st;
     }
     // chi of the final state
+    TF_TRY(ensure(c, c->vecs[TF_VEC_CHI], (size_t)m));
     TF_CUDA(c, cudaMemcpyAsync(c->vecs[TF_VEC_CHI].p, c->vecs[TF_VEC_X].p, sizeof(double) * m, cudaMemcpyDeviceToDevice,
                                c->stream));
     TF_CUDA(c, cudaStreamSynchronize(c->stream));

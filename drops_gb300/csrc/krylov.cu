@@ -314,10 +314,12 @@ int ensure_sell(Context* c, CSR& A, bool fp32) {
 }
 
 // Slot row of a SELL matrix times the vector given by xload(col), accumulated
-// in T.  The row is walked in blocks of eight: the column indices and values
-// of the next block are loaded while the gathers of the current block are in
-// flight, so a lane keeps up to 16 independent loads outstanding.  Terms are
-// summed in CSR order.
+// in T.  The row is walked in blocks of eight, the last block masked (the
+// slice width is the same for all 32 lanes, so the mask is warp-uniform): the
+// column indices and values of the next block are loaded while the gathers of
+// the current block are in flight, so a lane keeps up to 16 independent loads
+// outstanding and a row of w entries costs ceil(w/8) gather latencies.  Terms
+// are summed in CSR order; masked terms add +0.
 template <class T, class XL>
 __device__ __forceinline__ T sell_row(const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
                                       const T* __restrict__ val, int64_t s, int lane, XL xload) {
@@ -329,32 +331,31 @@ __device__ __forceinline__ T sell_row(const int32_t* __restrict__ ptr, const int
     T acc = T(0);
     int32_t cn[U];
     T vn[U];
-    const int32_t wu = w - w % U;
-    if (wu > 0) {
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            cn[u] = __ldg(cp + 32 * u);
-            vn[u] = __ldg(vp + 32 * u);
-        }
+    for (int u = 0; u < U; ++u) {
+        const bool in = u < w;
+        cn[u] = in ? __ldg(cp + 32 * u) : -1;
+        vn[u] = in ? __ldg(vp + 32 * u) : T(0);
     }
-    for (int32_t k = 0; k < wu; k += U) {
+    for (int32_t k = 0; k < w; k += U) {
         T xv[U], vv[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            xv[u] = xload(cn[u]);
+            xv[u] = cn[u] >= 0 ? xload(cn[u]) : T(0);
             vv[u] = vn[u];
         }
-        if (k + U < wu) {
+        const int32_t kn = k + U;
+        if (kn < w) {
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                cn[u] = __ldg(cp + 32 * (k + U + u));
-                vn[u] = __ldg(vp + 32 * (k + U + u));
+                const bool in = kn + u < w;
+                cn[u] = in ? __ldg(cp + 32 * (kn + u)) : -1;
+                vn[u] = in ? __ldg(vp + 32 * (kn + u)) : T(0);
             }
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) acc += vv[u] * xv[u];
     }
-    for (int32_t k = wu; k < w; ++k) acc += __ldg(vp + 32 * k) * xload(__ldg(cp + 32 * k));
     return acc;
 }
 

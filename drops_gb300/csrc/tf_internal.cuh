@@ -1,5 +1,6 @@
 // Internal declarations shared by the CUDA translation units of libtracefem.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -277,13 +278,41 @@ struct Context {
     DBuf<int> batch_queue, batch_iters;
     DBuf<int32_t> batch_order;
     std::vector<int64_t> h_batch_nnz;
-    int64_t batch_order_gen = -1, batch_tuned_gen = -1;
-    bool batch_tuned_mixed = false, batch_use_graph = true;
+    int64_t batch_order_gen = -1;
+    std::vector<int64_t> batch_tuned_key;              // batch structure the tuned shape belongs to
+    DBuf<int64_t> batch_nnz;
+    bool batch_use_graph = true;
     int batch_lanes = 0, batch_threads = 0;             // autotuned
     int batch_fixed_lanes = 0, batch_fixed_threads = 0; // set by tf_batch_config (0: autotune)
     double* h_batch_out = nullptr;                      // pinned: iterations, then residuals
     cudaGraphExec_t batch_exec = nullptr;
     std::vector<int64_t> batch_graph_key;
+    // learned warm start (per-DOF MLP)
+    DBuf<float> mlp_w, mlp_m1, mlp_m2, mlp_grad, mlp_lossacc;
+    DBuf<__nv_bfloat16> mlp_w16, mlp_xio;
+    DBuf<float> mlp_yio, mlp_pio;
+    int64_t mlp_step = 0;
+    // learned Cahn-Hilliard warm start
+    DBuf<double> ch_part, ch_scales, ch_hist;
+    DBuf<float> ch_xyz, ch_nrm, ch_Y, ch_pred;
+    DBuf<__nv_bfloat16> ch_X;
+    int64_t ch_geom_version = -1;
+    double ch_train_loss = 0.;
+};
+
+struct ChLearnParams {
+    int nsteps = 0;
+    double dt = 0., mob = 1., eps = 0., beta_s = 0., xi = 0., rho_vol = 0.;
+    int restart = 50;
+    double tol = 1e-10;
+    int max_iter = 100000;
+    int precision = TF_PREC_FP64;
+    int learned = 1;        // 0: previous-step guess only (the reference's warm start)
+    int train_steps = 100;  // online training during the first steps
+    int epochs = 2;
+    int mb_tiles = 16;      // tiles of 128 DOFs per mini-batch
+    float lr = 1e-3f;
+    int min_trained = 3;    // training steps before the first learned guess
 };
 
 constexpr int kMaxBatchInstances = 65536;
@@ -368,6 +397,16 @@ int batch_pcg(Context* c, CSR& A, const double* b, double* x, int precision, int
               int* iters, double* resids);
 int batch_config(Context* c, int lanes, int threads, int use_graph);
 void release_batch(Context* c);
+int mlp_init(Context* c, uint64_t seed);
+int mlp_set_weights(Context* c, const float* w);
+int mlp_get_weights(Context* c, float* w);
+int mlp_forward_dev(Context* c, const __nv_bfloat16* X, int64_t n, float* pred);
+int ch_rhs(Context* c, const double* X, double dt, double beta_s, double xi);
+int ch_geometry(Context* c);
+int ch_features_dev(Context* c, const double* xn, const double* xp, const double* xnext);
+int ch_steps_learned(Context* c, const ChLearnParams& P, int* iters, double* resids, int* used);
+int mlp_epoch_dev(Context* c, const __nv_bfloat16* X, const float* Y, int64_t n, int mb_tiles, float lr, float* gsum,
+                  double* loss);
 int ensure_vals32(Context* c, CSR& A);
 int ensure_sell(Context* c, CSR& A, bool fp32);
 

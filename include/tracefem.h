@@ -240,6 +240,33 @@ int tf_batch_tune(tf_context* ctx, int mat, int vec_b, int precision, int* lanes
  * launches the solve directly instead of replaying a CUDA graph.               */
 int tf_batch_config(tf_context* ctx, int lanes, int threads, int use_graph);
 
+/* ---- learned warm start: per-DOF MLP on the tensor cores ------------------------- */
+/* No counterpart in the reference (it starts each Cahn-Hilliard solve from the
+ * previous state).  A per-DOF MLP, 80 BF16 inputs -> 64 -> 64 -> 64 -> 2 with
+ * tanh, FP32 accumulation, run and trained by tcgen05 kernels.  Weights are
+ * TF_MLP_WEIGHTS floats: four row-major [out][80] matrices (64, 64, 64 and 16
+ * rows; the last layer's rows 2..15 are zero) whose bias is the column of the
+ * constant-1 input (70 in the first layer, 64 in the others).  Inputs X are
+ * n x 80 BF16 values (raw 16-bit patterns), targets and outputs n x 2 floats;
+ * all buffers of these calls are host memory.                                  */
+#define TF_MLP_IN 80
+#define TF_MLP_WEIGHTS 16640
+int tf_mlp_init(tf_context* ctx, uint64_t seed);
+int tf_mlp_get_weights(tf_context* ctx, float* w);
+int tf_mlp_set_weights(tf_context* ctx, const float* w);
+int tf_mlp_forward(tf_context* ctx, const uint16_t* X, int64_t n, float* pred);
+/* Gradient of the mean squared error over all n samples and both outputs,
+ * weights unchanged; loss receives that mean.                                  */
+int tf_mlp_gradient(tf_context* ctx, const uint16_t* X, const float* Y, int64_t n, float* grad, double* loss);
+/* `epochs` passes of Adam (beta 0.9/0.999) over mini-batches of
+ * minibatch_tiles x 128 samples; loss receives the last pass's mean error.     */
+int tf_mlp_train(tf_context* ctx, const uint16_t* X, const float* Y, int64_t n, int epochs, int minibatch_tiles,
+                 float lr, double* loss);
+/* Inputs (and targets when vec_next >= 0) of every DOF for states cur = x_n
+ * and old = x_{n-1} (vectors [chi; omega] of 2m values), as the learned
+ * Cahn-Hilliard loop builds them; needs the P1 numbering and TF_FORM_M.       */
+int tf_ch_features(tf_context* ctx, int vec_cur, int vec_old, int vec_next, uint16_t* X, float* Y);
+
 /* ---- allocation-free PCG -------------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory: applications that manage every GPU byte through their own pool and
@@ -277,6 +304,18 @@ int tf_pcg_jacobi_noalloc(int64_t m, const int32_t* rowptr, const int32_t* colin
  * iteration count and relative residual; TF_VEC_CHI receives the final chi. */
 int tf_ch_steps(tf_context* ctx, int nsteps, double dt, double mobility, double eps, double beta_s, double xi,
                 double rho_vol, int restart, double tol, int max_iter, int warm, int* iters, double* resids);
+/* tf_ch_steps with the learned warm start: the MLP (tf_mlp_init first, or a
+ * default initialisation) is trained online with `epochs` Adam passes
+ * (minibatch_tiles x 128 DOFs, rate lr) on the increment of each of the first
+ * train_steps steps; from its third training step on, the guess of a step is
+ * x_n + predicted increment when that guess has the smaller FP64 residual,
+ * else the previous state, and a step whose learned solve needed more GMRES
+ * iterations than the last plain solve makes the next step use the previous
+ * state.  learned = 0 gives the plain previous-state warm start.  used[nsteps]
+ * (may be NULL) flags the steps that started from the learned guess.          */
+int tf_ch_steps_learned(tf_context* ctx, int nsteps, double dt, double mobility, double eps, double beta_s, double xi,
+                        double rho_vol, int restart, double tol, int max_iter, int learned, int train_steps,
+                        int epochs, int minibatch_tiles, float lr, int* iters, double* resids, int* used);
 
 /* ---- instrumentation -------------------------------------------------------------- */
 /* Per-kernel device time, recorded with CUDA events on the context's stream

@@ -24,14 +24,14 @@ RHS_NONE, RHS_SPHERE_XYZ, RHS_CONST = 0, 1, 2
 
 def build(force=False):
     """Compile the oracle with gcc (no contraction, so x86 and Arm agree)."""
-    src = os.path.join(HERE, "tracefem_oracle.c")
+    srcs = [os.path.join(HERE, f) for f in ("tracefem_oracle.c", "mlp_oracle.c")]
     os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
     if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= max(
-        os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "tracefem_oracle.h"))
+        [os.path.getmtime(s) for s in srcs] + [os.path.getmtime(os.path.join(HERE, "tracefem_oracle.h"))]
     ):
         return LIB_PATH
     subprocess.check_call(
-        ["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", src, "-o", LIB_PATH, "-lm"]
+        ["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", *srcs, "-o", LIB_PATH, "-lm"]
     )
     return LIB_PATH
 
@@ -50,6 +50,7 @@ def lib():
         L.orc_brick_num_tets.restype = i64
         L.orc_ls_value.restype = C.c_double
         L.orc_kahan_dot.restype = C.c_double
+        L.orc_mlp_gradient.restype = C.c_double
         _lib = L
     return _lib
 
@@ -247,3 +248,39 @@ def local_forms(xv, ls10, opts):
                            _p(out, C.c_double), _p(rhs, C.c_double), C.byref(nf))
     nl = 10 if opts.p2 else 4
     return st, {f: out[f, :nl * nl].reshape(nl, nl) for f in range(NUM_FORMS)}, rhs[:nl], nf.value
+
+
+# ---- per-DOF MLP of the learned warm start ---------------------------------
+MLP_IN, MLP_WEIGHTS = 80, 16640
+
+
+def bf16_bits(a):
+    """float32 array -> BF16 bit patterns (uint16), round to nearest even."""
+    u = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) >> 16
+    return u.astype(np.uint16)
+
+
+def bf16_value(bits):
+    return (np.asarray(bits, dtype=np.uint16).astype(np.uint32) << 16).view(np.float32)
+
+
+def mlp_forward(w, X, exact=False):
+    L = lib()
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.uint16)
+    n = X.shape[0]
+    out = np.empty((n, 2), np.float32)
+    L.orc_mlp_forward(_p(w, C.c_float), _p(X, C.c_uint16), C.c_int64(n), C.c_int(int(exact)), _p(out, C.c_float))
+    return out
+
+
+def mlp_gradient(w, X, Y, exact=False):
+    L = lib()
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.uint16)
+    Y = np.ascontiguousarray(Y, dtype=np.float32)
+    g = np.empty(MLP_WEIGHTS, np.float32)
+    loss = L.orc_mlp_gradient(_p(w, C.c_float), _p(X, C.c_uint16), _p(Y, C.c_float), C.c_int64(X.shape[0]),
+                              C.c_int(int(exact)), _p(g, C.c_float))
+    return g, loss
