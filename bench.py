@@ -465,6 +465,115 @@ def batch_cpu_sample(args, threads, budget_s=20.0):
 
 
 # ---------------------------------------------------------------------------
+CH_N, CH_HALF, CH_DT, CH_EPS, CH_STEPS = 128, 1.6, 1e-3, 0.02, 200
+CH_METRIC = "Cahn-Hilliard GMRES(50) solve time to rel. residual 1e-10 per time step, mixed precision + learned " \
+            "warm start vs plain FP64 (P1 TraceFEM, torus)"
+CH_CONFIG = {
+    "workload": "surface Cahn-Hilliard on the torus R=1, r=0.4 in [-1.6,1.6]^3 with 128^3 Kuhn cubes (12,582,912 "
+                "tets), P1, 2x2 block system, BDF1 dt=1e-3, mobility 1, eps=0.02, c0=0.5+U(+-0.01) (seed 2024), "
+                "GMRES(50) with nodal block-Jacobi to rel 1e-10; learned warm start trained online on steps 1-100",
+    "fe": "P1IF", "tol": TOL, "restart": 50, "parallelism": "replicas",
+}
+
+
+def run_ch(args, rank, ws, dist):
+    import drops_gb300 as tf
+
+    n = args.ch_n
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    ctx = tf.TraceFEM(dev)
+    ctx.brick_cube(n, CH_HALF)
+    ctx.levelset_analytic(tf.LS_TORUS, [1.0, 0.4, 2], False)
+    na, nd = ctx.distribute_dofs(tf.P1IF)
+    nnz = ctx.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN])
+    h = 2 * CH_HALF / n
+    rng = np.random.default_rng(2024)
+    x0 = np.concatenate([0.5 + rng.uniform(-0.01, 0.01, nd), np.zeros(nd)])
+    pin0, pinx = tf.PinnedArray(2 * nd), tf.PinnedArray(2 * nd)
+    pin0.array[:] = x0
+    steps = args.ch_steps
+    # learned: 0 previous state (the reference's warm start), 2 linear extrapolation, 1 MLP correction of it
+    variants = [("fp64_mgs_plain", tf.PREC_FP64, tf.ORTH_MGS, 0), ("fp64_cgs2_plain", tf.PREC_FP64, tf.ORTH_CGS2, 0),
+                ("mixed_plain", tf.PREC_MIXED, tf.ORTH_MGS, 0), ("mixed_extrapolated", tf.PREC_MIXED, tf.ORTH_MGS, 2),
+                ("mixed_learned", tf.PREC_MIXED, tf.ORTH_MGS, 1)]
+    if args.ch_quick:
+        variants = [variants[0], variants[4]]
+    runs = {}
+    launches0 = ctx.launch_count()
+    with Clocks(dev) as clk:
+        for name, prec, orth, learned in variants:
+            ctx.gmres_options(orth)
+            ctx.mlp_init(1234)
+            ctx.flush_l2()
+            barrier(dist)
+            ctx.marker(0)
+            ctx.vec_upload(tf.VEC_X, pin0.array)
+            st, its, res, used = ctx.ch_steps_learned(steps, CH_DT, 1.0, CH_EPS, 0.0, 1.0, h, restart=50, tol=TOL,
+                                                      max_iter=100000, precision=prec, learned=learned,
+                                                      train_steps=100, epochs=2, minibatch_tiles=16, lr=1e-3)
+            ctx.vec_download(tf.VEC_X, out=pinx.array)
+            ctx.marker(1)
+            ms = all_max(dist, ctx.elapsed_ms(0, 1))
+            if st != tf.OK or np.any(res > TOL):
+                raise RuntimeError(f"{name}: status {st}, worst residual {res.max()}")
+            runs[name] = {"ms": round(ms, 2), "ms_per_step": round(ms / steps, 3), "gmres_iters": int(its.sum()),
+                          "iters_per_step": round(float(its.mean()), 1), "learned_steps": int(used.sum()),
+                          "final_chi_mean": float(pinx.array[:nd].mean())}
+    ctx.gmres_options(tf.ORTH_MGS)
+    launches = ctx.launch_count() - launches0
+    clocks = clk.summary()
+    base, best = runs["fp64_mgs_plain"], runs["mixed_learned"]
+    value = steps / (best["ms"] / 1e3)
+    out = {
+        "metric": CH_METRIC, "value": round(value, 2), "unit": "time_steps/s", "n_gpus": ws, "steps": steps,
+        "warmup": 0, "ms_per_step": best["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64+f32+bf16", "data": "synthetic (analytic level set, seeded noise)",
+        "config": dict(CH_CONFIG, steps=steps, n=n),
+        "speedup_vs_plain_fp64": round(base["ms"] / best["ms"], 3),
+        "e2e": {"value": round(value, 2), "unit": "time_steps/s", "h2d_bytes_per_step": round(16 * nd / steps, 1),
+                "d2h_bytes_per_step": round(16 * nd / steps, 1),
+                "note": "each run uploads the initial state and downloads the final state (pinned host buffers)"},
+        "gpu_launches": int(launches), "clocks": clocks,
+        "problem": {"cut_tets": na, "dofs_per_field": nd, "block_rows": 2 * nd, "nnz_per_block": nnz},
+        "runs": runs,
+    }
+    ctx.close()
+    pin0.free()
+    pinx.free()
+    return out
+
+
+def ch_cpu_sample(args, threads, budget_s=20.0):
+    """Oracle GMRES(50) with block Jacobi on the same CH steps (FP64, previous-state guess) until budget_s."""
+    from oracle import pyoracle as O
+
+    O.set_threads(threads)
+    n = args.ch_n
+    mesh = O.brick(n, a=CH_HALF)
+    lv, le = O.levelset(mesh, O.LS_TORUS, [1.0, 0.4, 2], False)
+    st, na, m, dv, de, act = O.distribute_dofs(mesh, lv, le, False)
+    opts = O.make_opts(False, [O.FORM_M, O.FORM_A, O.FORM_CN])
+    st, rp, ci, vals, rhs = O.assemble(mesh, lv, le, act, dv, None, m, opts)
+    h = 2 * CH_HALF / n
+    alpha = 1.0 / CH_DT
+    brp, bci, bv = O.ch_block(rp, ci, vals[O.FORM_M], vals[O.FORM_A], vals[O.FORM_CN], alpha, 1.0, h,
+                              CH_EPS * CH_EPS, 0.0)
+    rng = np.random.default_rng(2024)
+    x = np.concatenate([0.5 + rng.uniform(-0.01, 0.01, m), np.zeros(m)])
+    t_tot, k = 0.0, 0
+    while t_tot < budget_s and k < args.ch_steps:
+        chi = x[:m]
+        Mchi = O.spmv(rp, ci, vals[O.FORM_M], chi)
+        fp = 2 * chi * (1 - chi) * (1 - 2 * chi)
+        b = np.concatenate([alpha * Mchi, -O.spmv(rp, ci, vals[O.FORM_M], fp)])
+        t0 = time.perf_counter()
+        st, x, it, res = O.gmres_jacobi(brp, bci, bv, b, x0=x, restart=50, tol=TOL, max_iter=100000, block=True)
+        t_tot += time.perf_counter() - t0
+        k += 1
+    return k / t_tot, f"first {k} of {args.ch_steps} time steps, GMRES(50) solves only ({t_tot:.1f} s)"
+
+
+# ---------------------------------------------------------------------------
 def cpu_workload(threads, N=N_CUBES):
     """The same step with the oracle (C restatement of the reference) on the host."""
     from oracle import pyoracle as O
@@ -531,8 +640,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--size", type=int, default=N_CUBES, help="cubes per direction (96 = the benchmark workload; "
                     "smaller sizes are for profiling captures)")
-    ap.add_argument("--workload", default="poisson", choices=["poisson", "batch"],
-                    help="poisson: the P2 96^3 sphere problem (headline); batch: 256 independent P1 ellipsoids")
+    ap.add_argument("--workload", default="poisson", choices=["poisson", "batch", "ch"],
+                    help="poisson: the P2 96^3 sphere problem (headline); batch: 256 independent P1 ellipsoids; "
+                         "ch: Cahn-Hilliard steps on the torus, plain FP64 vs mixed + learned warm start")
+    ap.add_argument("--ch-n", type=int, default=CH_N)
+    ap.add_argument("--ch-steps", type=int, default=CH_STEPS)
+    ap.add_argument("--ch-quick", action="store_true", help="only the plain FP64 and the mixed + learned runs")
     ap.add_argument("--batch-count", type=int, default=BATCH_COUNT)
     ap.add_argument("--batch-nmin", type=int, default=BATCH_NMIN)
     ap.add_argument("--batch-nmax", type=int, default=BATCH_NMAX)
@@ -548,6 +661,17 @@ def main():
     if rank == 0:
         build.build()
     barrier(dist)
+    if args.workload == "ch":
+        out = run_ch(args, rank, ws, dist)
+        if rank == 0:
+            if ws == 1 and not args.no_cpu_baseline:
+                v, sample = ch_cpu_sample(args, os.cpu_count() or 1)
+                out["cpu_baseline"] = {"value": round(v, 3), "unit": "time_steps/s", "cores": os.cpu_count() or 1,
+                                       "kind": "port", "sample": sample}
+            print(json.dumps(out))
+        if dist is not None:
+            dist.destroy_process_group()
+        return
     if args.workload == "batch":
         out = run_batch(args, rank, ws, dist)
         if (args.batch_count, args.batch_nmin, args.batch_nmax) != (BATCH_COUNT, BATCH_NMIN, BATCH_NMAX):

@@ -32,6 +32,7 @@ VEC_RHS, VEC_X, VEC_B, VEC_CHI, VEC_T0, VEC_T1, VEC_T2, VEC_T3 = range(8)
 LS_SPHERE, LS_TORUS, LS_ELLIPSOID, LS_PLANE = range(4)
 RHS_NONE, RHS_SPHERE_XYZ, RHS_CONST = range(3)
 PREC_FP64, PREC_MIXED = 0, 1
+ORTH_MGS, ORTH_CGS2 = 0, 1
 MLP_IN, MLP_WEIGHTS = 80, 16640
 K_CLASSIFY, K_NUMBER, K_ASSEMBLE, K_PATTERN, K_SCATTER, K_SPMV, K_PCG, K_GMRES, K_LEVELSET, K_BATCH = range(10)
 KERNEL_NAMES = ["classify", "number", "assemble", "pattern", "scatter", "spmv", "pcg", "gmres", "levelset", "batch"]
@@ -45,7 +46,7 @@ EXPORTS = [
     "tf_vec_download", "tf_vec_size", "tf_vec_fill", "tf_spmv", "tf_pcg_jacobi", "tf_gmres_jacobi", "tf_pcg_jacobi_noalloc", "tf_ch_steps",
     "tf_mesh_brick_batch", "tf_levelset_analytic_batch", "tf_batch_info", "tf_batch_lincomb", "tf_batch_pcg_jacobi",
     "tf_batch_tune", "tf_batch_config", "tf_mlp_init", "tf_mlp_get_weights", "tf_mlp_set_weights", "tf_mlp_forward",
-    "tf_mlp_gradient", "tf_mlp_train", "tf_ch_features", "tf_ch_steps_learned", "tf_timing_enable",
+    "tf_mlp_gradient", "tf_mlp_train", "tf_ch_features", "tf_ch_steps_learned", "tf_gmres_options", "tf_timing_enable",
     "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2",
     "tf_host_alloc", "tf_host_free",
 ]
@@ -385,15 +386,19 @@ class TraceFEM:
                                           Y.ctypes.data_as(C.POINTER(C.c_float))))
         return X, (Y if vec_next >= 0 else None)
 
+    def gmres_options(self, orth=ORTH_MGS):
+        self._check(self.L.tf_gmres_options(self.h, C.c_int(orth)))
+
     def ch_steps_learned(self, nsteps, dt, mobility, eps, beta_s, xi, rho_vol, restart=50, tol=1e-10,
-                         max_iter=100000, learned=True, train_steps=100, epochs=2, minibatch_tiles=16, lr=1e-3,
-                         check=True):
+                         max_iter=100000, precision=PREC_FP64, learned=True, train_steps=100, epochs=2,
+                         minibatch_tiles=16, lr=1e-3, check=True):
         """Cahn-Hilliard steps with the learned warm start; returns (status, iterations[], residuals[], used[])."""
         k = max(nsteps, 1)
         its, res, used = np.zeros(k, np.int32), np.zeros(k), np.zeros(k, np.int32)
         st = self.L.tf_ch_steps_learned(self.h, C.c_int(nsteps), C.c_double(dt), C.c_double(mobility),
                                         C.c_double(eps), C.c_double(beta_s), C.c_double(xi), C.c_double(rho_vol),
-                                        C.c_int(restart), C.c_double(tol), C.c_int(max_iter), C.c_int(int(learned)),
+                                        C.c_int(restart), C.c_double(tol), C.c_int(max_iter), C.c_int(precision),
+                                        C.c_int(int(learned)),  # 0 plain, 1 MLP, 2 extrapolation
                                         C.c_int(train_steps), C.c_int(epochs), C.c_int(minibatch_tiles),
                                         C.c_float(lr), _ip(its), _dp(res), _ip(used))
         if check:

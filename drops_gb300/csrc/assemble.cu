@@ -34,6 +34,7 @@ struct Tables {
     int can_a[8][6];        // cut-edge orientation of the first sub-tet holding the edge
     int can_b[8][6];
     int ledge[8][6];        // lattice edge id 0..24
+    int edge_a[25], edge_b[25];  // canonical endpoints of every lattice edge
     signed char pat_nf[81]; // facets per sign pattern (-1: all-zero pattern)
     signed char pat_bnd[81];
     signed char pat_f[81][2][3];  // ext ids: 0..3 vertex, 4..9 edge + 4
@@ -100,6 +101,10 @@ static void build_tables(Tables& T) {
             T.can_b[s][e] = seen_b[id];
             T.ledge[s][e] = id;
         }
+    for (int q = 0; q < 25; ++q) {
+        T.edge_a[q] = seen_a[q];
+        T.edge_b[q] = seen_b[q];
+    }
     // sign-pattern facet table (SignTraitsCL<3>::compute_cuts + RefPatchBuilderCL<3>::assign)
     for (int p = 0; p < 81; ++p) {
         int sg[4], q = p, sum = 0;
@@ -193,41 +198,45 @@ struct TetGeom {
 
 // GetTrafoTr (geom/multigrid.h:603-623), P1 gradients and the vertex values
 // of grad(phi_h) for the P2 level set ls10 (4 vertex + 6 edge values).
-__device__ inline void tet_geometry(TetGeom& g, const double ls10[10]) {
-    double M[3][3];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) M[j][i] = g.X[i + 1][j] - g.X[0][j];
-    const double d = M[0][0] * (M[1][1] * M[2][2] - M[1][2] * M[2][1]) - M[0][1] * (M[1][0] * M[2][2] - M[1][2] * M[2][0]) +
-                     M[0][2] * (M[1][0] * M[2][1] - M[1][1] * M[2][0]);
-    double T[3][3];
-    T[0][0] = (M[1][1] * M[2][2] - M[1][2] * M[2][1]) / d;
-    T[0][1] = (M[2][0] * M[1][2] - M[1][0] * M[2][2]) / d;
-    T[0][2] = (M[1][0] * M[2][1] - M[2][0] * M[1][1]) / d;
-    T[1][0] = (M[2][1] * M[0][2] - M[0][1] * M[2][2]) / d;
-    T[1][1] = (M[0][0] * M[2][2] - M[2][0] * M[0][2]) / d;
-    T[1][2] = (M[2][0] * M[0][1] - M[0][0] * M[2][1]) / d;
-    T[2][0] = (M[0][1] * M[1][2] - M[1][1] * M[0][2]) / d;
-    T[2][1] = (M[1][0] * M[0][2] - M[0][0] * M[1][2]) / d;
-    T[2][2] = (M[0][0] * M[1][1] - M[1][0] * M[0][1]) / d;
-    g.absdet = fabs(d);
-    for (int r = 0; r < 3; ++r) {
-        g.gl[0][r] = -T[r][0] - T[r][1] - T[r][2];
-        g.gl[1][r] = T[r][0];
-        g.gl[2][r] = T[r][1];
-        g.gl[3][r] = T[r][2];
+// Tet geometry (GetTrafoTr, geom/multigrid.h:627-650) on the warp.  Lanes
+// 0..8 form the edge matrix M (M[r][c] = X[c+1][r] - X[0][r]) and its
+// cofactors, the warp takes one reciprocal of det M, and lanes 0..11 form the
+// barycentric gradients gl (T = cof(M) / det) and the gradient coefficients G
+// of the P2 level set.  On GB300 an FP64 instruction costs the same with one
+// active lane as with 32, so spreading the work over lanes divides its cost.
+__device__ inline void warp_tet_geometry(TetGeom& g, const double* ls10, double* Ms, double* Cs, int lane) {
+    if (lane < 9) {
+        const int r = lane / 3, c = lane % 3;
+        Ms[lane] = g.X[c + 1][r] - g.X[0][r];
     }
+    __syncwarp();
+    if (lane < 9) {
+        const int r = lane / 3, c = lane % 3;
+        const int r1 = (r + 1) % 3, r2 = (r + 2) % 3, c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+        Cs[lane] = Ms[3 * r1 + c1] * Ms[3 * r2 + c2] - Ms[3 * r1 + c2] * Ms[3 * r2 + c1];
+    }
+    __syncwarp();
+    const double d = Ms[0] * Cs[0] + Ms[1] * Cs[1] + Ms[2] * Cs[2];
+    const double inv = 1.0 / d;
+    if (lane < 12) {
+        const int v = lane / 3, r = lane % 3;
+        g.gl[v][r] = v == 0 ? (-(Cs[3 * r] * inv) - Cs[3 * r + 1] * inv) - Cs[3 * r + 2] * inv : Cs[3 * r + v - 1] * inv;
+    }
+    if (lane == 0) g.absdet = fabs(d);
+    __syncwarp();
     // grad H_i(e_v) = (4 delta_iv - 1) gl_i ; grad H_ab(e_v) = 4 (delta_bv gl_a + delta_av gl_b)
-    for (int v = 0; v < 4; ++v)
-        for (int r = 0; r < 3; ++r) {
-            double s = 0.;
-            for (int i = 0; i < 4; ++i) s += ls10[i] * ((i == v ? 3. : -1.) * g.gl[i][r]);
-            for (int e = 0; e < 6; ++e) {
-                const int a = ev0(e), b = ev1(e);
-                if (b == v) s += ls10[4 + e] * (4. * g.gl[a][r]);
-                if (a == v) s += ls10[4 + e] * (4. * g.gl[b][r]);
-            }
-            g.G[v][r] = s;
+    if (lane < 12) {
+        const int v = lane / 3, r = lane % 3;
+        double s = 0.;
+        for (int i = 0; i < 4; ++i) s += ls10[i] * ((i == v ? 3. : -1.) * g.gl[i][r]);
+        for (int e = 0; e < 6; ++e) {
+            const int a = ev0(e), b = ev1(e);
+            if (b == v) s += ls10[4 + e] * (4. * g.gl[a][r]);
+            if (a == v) s += ls10[4 + e] * (4. * g.gl[b][r]);
         }
+        g.G[v][r] = s;
+    }
+    __syncwarp();
 }
 
 // 1/sqrt(s) to FP64 accuracy: FP32 seed and two Newton steps
@@ -371,6 +380,8 @@ struct PatchSmem {
     double fw[16];        // |det| of the facet, x1/2 on lattice faces
     int bnd[16];
     int nf;
+    double cut[25][4];    // cut point of each lattice edge (where the edge is cut)
+    int fsub[16], floc[16], fpat[16];  // owning sub-tet, facet index in its pattern, pattern
 };
 
 // cut point of a lattice edge: ConvexComb(ls_a/(ls_a - ls_b), v_a, v_b)
@@ -382,11 +393,24 @@ __device__ inline void cut_point(const double* lat, int a, int b, double out[4])
     for (int c = 0; c < 4; ++c) out[c] = __dadd_rn(__dmul_rn(s, cT.lat_v[a][c]), __dmul_rn(t, cT.lat_v[b][c]));
 }
 
-// All lanes call; lanes 0..7 own one sub-tet each.  Returns the facet count.
+// All lanes call.  Lanes 0..24 compute the cut point of one lattice edge each
+// (every edge once, with its canonical orientation, so all sub-tets sharing
+// an edge see the same point, as MergeCutPolicyCL's memo gives); lanes 0..7
+// classify one sub-tet each and list its facets; then one lane per facet
+// forms the facet's vertices and |det|.  Returns the facet count.
 __device__ int warp_patch(const double ls10[10], const double X[4][3], PatchSmem& P, int lane, int* status,
                           int64_t tet) {
     double lat[10];
     for (int k = 0; k < 10; ++k) lat[cP2OnLat[k]] = ls10[k];
+    if (lane < 25) {
+        const int a = cT.edge_a[lane], b = cT.edge_b[lane];
+        const double va = lat[a], vb = lat[b];
+        if ((va > 0. && vb < 0.) || (va < 0. && vb > 0.)) {
+            double cp[4];
+            cut_point(lat, a, b, cp);
+            for (int c = 0; c < 4; ++c) P.cut[lane][c] = cp[c];
+        }
+    }
     int nf = 0, pat = 0;
     if (lane < 8) {
         for (int k = 0; k < 4; ++k) {
@@ -405,32 +429,39 @@ __device__ int warp_patch(const double ls10[10], const double X[4][3], PatchSmem
         if (lane >= o) incl += y;
     }
     const int total = __shfl_sync(0xffffffffu, incl, 7);
-    if (lane < 8) {
-        const int off = incl - nf;
-        const int bnd = cT.pat_bnd[pat];
+    if (lane < 8)
         for (int f = 0; f < nf; ++f) {
-            double w[3][3];
-            for (int j = 0; j < 3; ++j) {
-                const int ext = cT.pat_f[pat][f][j];
-                double b[4];
-                if (ext < 4) {
-                    const int L = cT.lat_t[lane][ext];
-                    for (int c = 0; c < 4; ++c) b[c] = cT.lat_v[L][c];
-                } else {
-                    cut_point(lat, cT.can_a[lane][ext - 4], cT.can_b[lane][ext - 4], b);
-                }
-                for (int c = 0; c < 4; ++c) P.fb[off + f][j][c] = b[c];
-                for (int r = 0; r < 3; ++r) w[j][r] = X[0][r] * b[0] + X[1][r] * b[1] + X[2][r] * b[2] + X[3][r] * b[3];
-            }
-            double u[3], v[3];
-            for (int r = 0; r < 3; ++r) {
-                u[r] = w[1][r] - w[0][r];
-                v[r] = w[2][r] - w[0][r];
-            }
-            const double c0 = u[1] * v[2] - u[2] * v[1], c1 = u[2] * v[0] - u[0] * v[2], c2 = u[0] * v[1] - u[1] * v[0];
-            P.fw[off + f] = sqrt(c0 * c0 + c1 * c1 + c2 * c2) * (bnd ? 0.5 : 1.0);
-            P.bnd[off + f] = bnd;
+            const int k = incl - nf + f;
+            P.fsub[k] = lane;
+            P.floc[k] = f;
+            P.fpat[k] = pat;
         }
+    __syncwarp();
+    if (lane < total) {
+        const int sub = P.fsub[lane], f = P.floc[lane], fp = P.fpat[lane];
+        double w[3][3];
+        for (int j = 0; j < 3; ++j) {
+            const int ext = cT.pat_f[fp][f][j];
+            double b[4];
+            if (ext < 4) {
+                const int L = cT.lat_t[sub][ext];
+                for (int c = 0; c < 4; ++c) b[c] = cT.lat_v[L][c];
+            } else {
+                const int id = cT.ledge[sub][ext - 4];
+                for (int c = 0; c < 4; ++c) b[c] = P.cut[id][c];
+            }
+            for (int c = 0; c < 4; ++c) P.fb[lane][j][c] = b[c];
+            for (int r = 0; r < 3; ++r) w[j][r] = X[0][r] * b[0] + X[1][r] * b[1] + X[2][r] * b[2] + X[3][r] * b[3];
+        }
+        double u[3], v[3];
+        for (int r = 0; r < 3; ++r) {
+            u[r] = w[1][r] - w[0][r];
+            v[r] = w[2][r] - w[0][r];
+        }
+        const double c0 = u[1] * v[2] - u[2] * v[1], c1 = u[2] * v[0] - u[0] * v[2], c2 = u[0] * v[1] - u[1] * v[0];
+        const int bnd = cT.pat_bnd[fp];
+        P.fw[lane] = sqrt(c0 * c0 + c1 * c1 + c2 * c2) * (bnd ? 0.5 : 1.0);
+        P.bnd[lane] = bnd;
     }
     if (lane == 0) P.nf = total;
     __syncwarp();
@@ -445,6 +476,7 @@ constexpr int kAsmWarps = 4;
 template <int NL>
 struct AsmSmem {
     TetGeom g;
+    double gM[9], gC[9];  // edge matrix and cofactors
     double ls10[10];
     PatchSmem P;
     double w[32];
@@ -496,7 +528,7 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
             S.ls10[lane] = A.lse[e[lane - 4]];
         }
         __syncwarp();
-        if (lane == 0) tet_geometry(S.g, S.ls10);
+        warp_tet_geometry(S.g, S.ls10, S.gM, S.gC, lane);
         double ls10[10];
         for (int k = 0; k < 10; ++k) ls10[k] = S.ls10[k];
         __syncwarp();

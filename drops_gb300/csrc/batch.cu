@@ -131,11 +131,12 @@ int batch_lincomb(Context* c, int nterms, const int* forms, const double* coeffs
 constexpr int kMaxBatchThreads = 1024;
 
 // Sum NV values over the CTA in a fixed order (warp tree, then warp 0 over the
-// warp partials in FP64); every thread receives the sums.  sh holds
-// 32*4 + 4 doubles; the result slots sit above every partial slot, so a
-// following call cannot overwrite them while slow threads still read them.
-template <int NV, class V>
-__device__ __forceinline__ void cta_sum(const V (&v)[NV], double (&out)[NV], double* sh) {
+// warp partials in FP64) and hand the sums to f, which thread 0 alone runs:
+// FP64 arithmetic issues at a small fraction of the FP32 rate on GB300, so
+// the scalar recurrences of the solver run once per CTA, not once per thread,
+// and reach the other threads through shared memory.  sh holds 32*4 doubles.
+template <int NV, class V, class F>
+__device__ __forceinline__ void cta_sum(const V (&v)[NV], double* sh, F f) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
@@ -146,17 +147,17 @@ __device__ __forceinline__ void cta_sum(const V (&v)[NV], double (&out)[NV], dou
     }
     __syncthreads();
     if (warp == 0) {
+        double out[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
             double s = lane < nw ? sh[k * 32 + lane] : 0.0;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0) sh[128 + k] = s;
+            out[k] = s;
         }
+        if (lane == 0) f(out);
     }
     __syncthreads();
-#pragma unroll
-    for (int k = 0; k < NV; ++k) out[k] = sh[128 + k];
 }
 
 // <row of A, x> by a group of G lanes (aligned inside the warp); every lane of
@@ -196,6 +197,14 @@ struct BatchPcgArgs {
 
 constexpr double kBatchRelUpdate = 0.1;
 
+// scalar state of one instance's solve, owned by thread 0, read by all
+struct BatchScalars {
+    double rho, r_last, normb, resid, alpha;
+    float alpha32, beta_f;
+    double beta_d;
+    int done, converged, true_res;
+};
+
 // One instance, rows [r0, r1), solved by the whole CTA.
 //   V = double: PCG with Jacobi in FP64, stopping on the recursive residual
 //               like the reference;
@@ -203,7 +212,7 @@ constexpr double kBatchRelUpdate = 0.1;
 //               residual replaces the FP32 one whenever the latter dropped by
 //               kBatchRelUpdate or claims convergence (reliable updates).
 template <int G, class V>
-__device__ void batch_pcg_instance(const BatchPcgArgs& a, int inst, double* sh) {
+__device__ void batch_pcg_instance(const BatchPcgArgs& a, int inst, double* sh, BatchScalars& sc) {
     constexpr bool kMixed = sizeof(V) == 4;
     const int64_t r0 = a.rows[inst], r1 = a.rows[inst + 1];
     const int64_t m = a.m;
@@ -217,6 +226,8 @@ __device__ void batch_pcg_instance(const BatchPcgArgs& a, int inst, double* sh) 
     const int nt = blockDim.x;
     const int slot = threadIdx.x / G, sub = threadIdx.x % G;
     const int per_pass = nt / G;
+    const double tol = a.tol;
+    const int max_iter = a.max_iter;
 
     // Jacobi diagonal (SolveGSstep<PB_JAC0> locates it by a row scan)
     for (int64_t i = r0 + threadIdx.x; i < r1; i += nt) {
@@ -227,8 +238,8 @@ __device__ void batch_pcg_instance(const BatchPcgArgs& a, int inst, double* sh) 
     }
     __syncthreads();
 
-    // r = b - A x (FP64), z = r / d, p = z; sums <r,r>, <b,b>, <z,r>
-    auto true_residual = [&](bool first, double (&s)[3]) {
+    // r = b - A x (FP64), z = r / d (p = z the first time); sums <r,r>, <b,b>, <z,r>
+    auto true_residual = [&](bool first) {
         double v[3] = {0., 0., 0.};
         for (int64_t base = r0; base < r1; base += per_pass) {
             const int64_t row = base + slot;
@@ -248,25 +259,41 @@ __device__ void batch_pcg_instance(const BatchPcgArgs& a, int inst, double* sh) 
                 v[2] += (double)(zv * rv);
             }
         }
-        cta_sum<3, double>(v, s, sh);
+        if (first) {
+            cta_sum<3, double>(v, sh, [&](const double* s) {
+                double nb = sqrt(s[1]);
+                if (nb == 0.0 || !a.rel) nb = 1.0;
+                sc.normb = nb;
+                sc.r_last = sqrt(s[0]);
+                sc.resid = sc.r_last / nb;
+                sc.rho = s[2];
+                sc.converged = sc.resid <= tol;
+                sc.done = sc.converged || max_iter <= 0;
+                sc.beta_f = 0.f;
+                sc.beta_d = 0.;
+            });
+        } else {  // reliable update: the FP64 residual replaces the FP32 one
+            cta_sum<3, double>(v, sh, [&](const double* s) {
+                sc.r_last = sqrt(s[0]);
+                sc.resid = sc.r_last / sc.normb;
+                sc.converged = sc.resid <= tol;
+                const double rho_new = s[2];
+                sc.beta_d = rho_new / sc.rho;
+                sc.beta_f = (float)sc.beta_d;
+                sc.rho = rho_new;
+            });
+        }
     };
 
-    double s0[3];
-    true_residual(true, s0);
-    double normb = sqrt(s0[1]);
-    if (normb == 0.0 || !a.rel) normb = 1.0;
-    double resid = sqrt(s0[0]) / normb;
-    double rho = s0[2];
-    double r_last = sqrt(s0[0]);
-    int it_done = 0;
-    bool converged = resid <= a.tol;
-    V beta = V(0);
+    true_residual(true);
     V* pc = pa;
     V* pn = pb;
+    int it = 0;
     // first iteration uses p = z: with beta = 0, p_new = z + 0 * p_old = z
-    for (int it = 1; !converged && it <= a.max_iter; ++it) {
+    while (!sc.done) {
+        ++it;
+        const V beta = kMixed ? (V)sc.beta_f : (V)sc.beta_d;
         // phase A: p_new = z + beta p_old (on the fly), q = A p_new, <q, p_new>
-        double lam[1];
         {
             V v[1] = {V(0)};
             for (int64_t base = r0; base < r1; base += per_pass) {
@@ -281,13 +308,15 @@ __device__ void batch_pcg_instance(const BatchPcgArgs& a, int inst, double* sh) 
                     v[0] += acc * pi;
                 }
             }
-            cta_sum<1, V>(v, lam, sh);
+            cta_sum<1, V>(v, sh, [&](const double* s) {
+                sc.alpha = sc.rho / s[0];
+                sc.alpha32 = (float)sc.alpha;
+            });
         }
-        const double alpha = rho / lam[0];
-        const V alphav = (V)alpha;
         // phase B: x += alpha p, r -= alpha q, z = r / d; <r,r>, <z,r>
-        double s2[2];
         {
+            const double alpha = sc.alpha;
+            const V alphav = kMixed ? (V)sc.alpha32 : (V)alpha;
             V v[2] = {V(0), V(0)};
             for (int64_t i = r0 + threadIdx.x; i < r1; i += nt) {
                 const V pi = pn[i];
@@ -299,40 +328,45 @@ __device__ void batch_pcg_instance(const BatchPcgArgs& a, int inst, double* sh) 
                 v[0] += ri * ri;
                 v[1] += zi * ri;
             }
-            cta_sum<2, V>(v, s2, sh);
+            cta_sum<2, V>(v, sh, [&](const double* s) {
+                const double rn = sqrt(s[0]);
+                if (kMixed) {
+                    sc.true_res = rn <= kBatchRelUpdate * sc.r_last || rn / sc.normb <= tol || it == max_iter;
+                    if (!sc.true_res) {
+                        sc.beta_d = s[1] / sc.rho;
+                        sc.beta_f = (float)sc.beta_d;
+                        sc.rho = s[1];
+                    }
+                } else {
+                    sc.true_res = 0;
+                    sc.resid = rn / sc.normb;
+                    sc.converged = sc.resid <= tol;
+                    sc.beta_d = s[1] / sc.rho;
+                    sc.rho = s[1];
+                    sc.done = sc.converged || it == max_iter;
+                }
+            });
         }
-        double rho_new = s2[1];
-        const double rn = sqrt(s2[0]);
-        it_done = it;
-        if (kMixed) {
-            if (rn <= kBatchRelUpdate * r_last || rn / normb <= a.tol || it == a.max_iter) {
-                double s3[3];
-                true_residual(false, s3);
-                r_last = sqrt(s3[0]);
-                rho_new = s3[2];
-                resid = r_last / normb;
-                converged = resid <= a.tol;
-            }
-        } else {
-            resid = rn / normb;
-            converged = resid <= a.tol;
+        if (kMixed && sc.true_res) {
+            true_residual(false);
+            if (threadIdx.x == 0) sc.done = sc.converged || it == max_iter;
+            __syncthreads();
         }
-        beta = (V)(rho_new / rho);
-        rho = rho_new;
         V* tmp = pc;
         pc = pn;
         pn = tmp;
     }
     if (threadIdx.x == 0) {
-        a.out_iter[inst] = converged ? it_done : -1 - it_done;
-        a.out_resid[inst] = resid;
+        a.out_iter[inst] = sc.converged ? it : -1 - it;
+        a.out_resid[inst] = sc.resid;
     }
-    __syncthreads();  // the next instance reuses sh and may share cache lines
+    __syncthreads();  // the next instance reuses sh and sc
 }
 
 template <int G, class V>
 __global__ void __launch_bounds__(kMaxBatchThreads) k_batch_pcg(BatchPcgArgs a) {
-    __shared__ double sh[132];
+    __shared__ double sh[128];
+    __shared__ BatchScalars sc;
     __shared__ int next;
     for (;;) {
         if (threadIdx.x == 0) next = atomicAdd(a.queue, 1);
@@ -340,7 +374,7 @@ __global__ void __launch_bounds__(kMaxBatchThreads) k_batch_pcg(BatchPcgArgs a) 
         const int k = next;
         __syncthreads();
         if (k >= a.count) return;
-        batch_pcg_instance<G, V>(a, a.order[k], sh);
+        batch_pcg_instance<G, V>(a, a.order[k], sh, sc);
     }
 }
 

@@ -153,6 +153,11 @@ int tf_destroy(tf_context* t) {
     tf::release(c->ch_Y);
     tf::release(c->ch_pred);
     tf::release(c->ch_X);
+    tf::release(c->gm2_b32);
+    tf::release(c->gm2_v32);
+    tf::release(c->gm2_b64);
+    tf::release(c->gm2_v64);
+    tf::release(c->gm2_binv);
     tf::release(c->flush_buf);
     for (auto& e : c->markers)
         if (e) cudaEventDestroy(e);
@@ -685,13 +690,22 @@ int tf_ch_features(tf_context* t, int vec_cur, int vec_old, int vec_next, uint16
     return TF_OK;
 }
 
+int tf_gmres_options(tf_context* t, int orth) {
+    CTX_CHECK(t);
+    if (orth != TF_ORTH_MGS && orth != TF_ORTH_CGS2) return tf::set_err(&t->c, TF_ERR_BAD_INPUT, "gmres_options: orth");
+    t->c.gmres_orth = orth;
+    return TF_OK;
+}
+
 int tf_ch_steps_learned(tf_context* t, int nsteps, double dt, double mobility, double eps, double beta_s, double xi,
-                        double rho_vol, int restart, double tol, int max_iter, int learned, int train_steps, int epochs,
-                        int minibatch_tiles, float lr, int* iters, double* resids, int* used) {
+                        double rho_vol, int restart, double tol, int max_iter, int precision, int learned,
+                        int train_steps, int epochs, int minibatch_tiles, float lr, int* iters, double* resids,
+                        int* used) {
     CTX_CHECK(t);
     Context* c = &t->c;
     cudaSetDevice(c->device);
-    if (restart < 2 || max_iter < 1 || tol <= 0. || epochs < 0 || minibatch_tiles < 1 || lr < 0.f)
+    if (restart < 2 || max_iter < 1 || tol <= 0. || epochs < 0 || minibatch_tiles < 1 || lr < 0.f ||
+        (precision != TF_PREC_FP64 && precision != TF_PREC_MIXED) || learned < 0 || learned > 2)
         return tf::set_err(c, TF_ERR_BAD_INPUT, "ch_steps_learned: bad arguments");
     tf::ChLearnParams P;
     P.nsteps = nsteps;
@@ -704,8 +718,9 @@ int tf_ch_steps_learned(tf_context* t, int nsteps, double dt, double mobility, d
     P.restart = restart;
     P.tol = tol;
     P.max_iter = max_iter;
+    P.precision = precision;
     P.learned = learned;
-    P.train_steps = learned ? train_steps : 0;
+    P.train_steps = learned == 1 ? train_steps : 0;
     P.epochs = epochs;
     P.mb_tiles = minibatch_tiles;
     P.lr = lr;

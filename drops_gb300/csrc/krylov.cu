@@ -19,159 +19,9 @@
 // returns.
 #include <cmath>
 
-#include "tf_internal.cuh"
+#include "krylov_dev.cuh"
 
 namespace tf {
-
-// ---------------------------------------------------------------------------
-// grid barrier with a bounded wait
-// ---------------------------------------------------------------------------
-struct GridSync {
-    unsigned* count;
-    unsigned* gen;
-    int* status;
-};
-constexpr long long kSpinLimit = 20000000;  // ~1-2 s with the backoff below
-
-__device__ __forceinline__ bool grid_barrier(const GridSync& g) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned* vgen = g.gen;
-        const unsigned my = *vgen;
-        __threadfence();
-        if (atomicAdd(g.count, 1u) == gridDim.x - 1) {
-            *g.count = 0;
-            __threadfence();
-            atomicAdd(g.gen, 1u);
-        } else {
-            long long spins = 0;
-            while (*vgen == my) {
-                if (++spins > kSpinLimit) {
-                    atomicCAS(g.status, 0, TF_ERR_WATCHDOG);
-                    break;
-                }
-                if (spins > 256) __nanosleep(32);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    __shared__ int st;
-    if (threadIdx.x == 0) st = *((volatile int*)g.status);
-    __syncthreads();
-    return st == 0;
-}
-
-// ---------------------------------------------------------------------------
-// reductions: warp xor-trees (every lane ends with the same sum), one FP64
-// partial per block, and a fixed-order sum of all partials in every block
-// ---------------------------------------------------------------------------
-template <class T>
-__device__ __forceinline__ T warp_sum(T v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-template <int NV, class T>
-__device__ void block_partials(T (&v)[NV], double* part /* [nblocks][NV] */) {
-    __shared__ double red[NV][32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int k = 0; k < NV; ++k) {
-        const T x = warp_sum(v[k]);
-        if (lane == 0) red[k][w] = (double)x;
-    }
-    __syncthreads();
-    if (w == 0)
-        for (int k = 0; k < NV; ++k) {
-            double x = lane < nw ? red[k][lane] : 0.;
-            x = warp_sum(x);
-            if (lane == 0) part[(size_t)blockIdx.x * NV + k] = x;
-        }
-    __syncthreads();
-}
-
-template <int NV>
-__device__ void grid_reduce(const double* part, double (&out)[NV]) {
-    __shared__ double red[NV][32];
-    __shared__ double res[NV];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int k = 0; k < NV; ++k) {
-        double x = 0.;
-        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) x += __ldcg(part + (size_t)b * NV + k);
-        x = warp_sum(x);
-        if (lane == 0) red[k][w] = x;
-    }
-    __syncthreads();
-    if (w == 0)
-        for (int k = 0; k < NV; ++k) {
-            double x = lane < nw ? red[k][lane] : 0.;
-            x = warp_sum(x);
-            if (lane == 0) res[k] = x;
-        }
-    __syncthreads();
-    for (int k = 0; k < NV; ++k) out[k] = res[k];
-    __syncthreads();
-}
-
-// Barrier and reduction in one: every block has written its NV partials; the
-// last block to arrive sums all of them in a fixed order (so the result does
-// not depend on which block is last), publishes the NV sums, and releases the
-// others.  Cost: one reduction of nblocks values instead of one per block.
-template <int NV>
-__device__ bool grid_sync_reduce(const GridSync& g, const double* part, double* result, double (&out)[NV]) {
-    __shared__ int last;
-    __shared__ double red[NV][32];
-    __shared__ int st;
-    __syncthreads();
-    unsigned my = 0;
-    if (threadIdx.x == 0) {
-        volatile unsigned* vgen = g.gen;
-        my = *vgen;
-        __threadfence();
-        last = atomicAdd(g.count, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (last) {
-        __threadfence();
-        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-        for (int k = 0; k < NV; ++k) {
-            double x = 0.;
-            for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) x += __ldcg(part + (size_t)b * NV + k);
-            x = warp_sum(x);
-            if (lane == 0) red[k][w] = x;
-        }
-        __syncthreads();
-        if (w == 0)
-            for (int k = 0; k < NV; ++k) {
-                double x = lane < nw ? red[k][lane] : 0.;
-                x = warp_sum(x);
-                if (lane == 0) result[k] = x;
-            }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            *g.count = 0;
-            __threadfence();
-            atomicAdd(g.gen, 1u);
-        }
-    } else if (threadIdx.x == 0) {
-        volatile unsigned* vgen = g.gen;
-        long long spins = 0;
-        while (*vgen == my) {
-            if (++spins > kSpinLimit) {
-                atomicCAS(g.status, 0, TF_ERR_WATCHDOG);
-                break;
-            }
-            if (spins > 256) __nanosleep(32);
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) st = *((volatile int*)g.status);
-    __syncthreads();
-    if (st != 0) return false;
-    for (int k = 0; k < NV; ++k) out[k] = __ldcg(result + k);
-    return true;
-}
 
 // ---------------------------------------------------------------------------
 // SELL-32-sigma layout and SpMV (y_Ax, num/spmat.h:1684-1709)
@@ -313,56 +163,6 @@ int ensure_sell(Context* c, CSR& A, bool fp32) {
     return TF_OK;
 }
 
-// Slot row of a SELL matrix times the vector given by xload(col), accumulated
-// in T.  The row is walked in blocks of eight, the last block masked (the
-// slice width is the same for all 32 lanes, so the mask is warp-uniform): the
-// column indices and values of the next block are loaded while the gathers of
-// the current block are in flight, so a lane keeps up to 16 independent loads
-// outstanding and a row of w entries costs ceil(w/8) gather latencies.  Terms
-// are summed in CSR order; masked terms add +0.
-template <class T, class XL>
-__device__ __forceinline__ T sell_row(const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
-                                      const T* __restrict__ val, int64_t s, int lane, XL xload) {
-    constexpr int U = 8;
-    const int32_t p0 = __ldg(ptr + s);
-    const int32_t w = (__ldg(ptr + s + 1) - p0) >> 5;
-    const int32_t* cp = col + p0 + lane;
-    const T* vp = val + p0 + lane;
-    T acc = T(0);
-    int32_t cn[U];
-    T vn[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-        const bool in = u < w;
-        cn[u] = in ? __ldg(cp + 32 * u) : -1;
-        vn[u] = in ? __ldg(vp + 32 * u) : T(0);
-    }
-    for (int32_t k = 0; k < w; k += U) {
-        T xv[U], vv[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            xv[u] = cn[u] >= 0 ? xload(cn[u]) : T(0);
-            vv[u] = vn[u];
-        }
-        const int32_t kn = k + U;
-        if (kn < w) {
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const bool in = kn + u < w;
-                cn[u] = in ? __ldg(cp + 32 * (kn + u)) : -1;
-                vn[u] = in ? __ldg(vp + 32 * (kn + u)) : T(0);
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) acc += vv[u] * xv[u];
-    }
-    return acc;
-}
-
-#define TF_SLICE_LOOP(nslices, s)                                                    \
-    const int64_t warp__ = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;   \
-    const int64_t nwarp__ = ((int64_t)gridDim.x * blockDim.x) >> 5;                  \
-    for (int64_t s = warp__; s < (nslices); s += nwarp__)
 
 template <class T>
 __global__ void k_spmv(int64_t nslices, const int32_t* __restrict__ perm, const int32_t* __restrict__ ptr,
@@ -370,7 +170,7 @@ __global__ void k_spmv(int64_t nslices, const int32_t* __restrict__ perm, const 
                        T* __restrict__ y) {
     const int lane = threadIdx.x & 31;
     TF_SLICE_LOOP(nslices, s) {
-        const T a = sell_row<T>(ptr, col, val, s, lane, [&](int32_t j) { return __ldcg(x + j); });
+        const T a = sell_row<T>(ptr, col, val, s, lane, [&](int32_t j) { return __ldg(x + j); });
         const int32_t row = perm[s * 32 + lane];
         if (row >= 0) y[row] = a;
     }
@@ -527,7 +327,7 @@ int ch_block(Context* c, double alpha, double mob, double rho, double eps2, doub
 // ---------------------------------------------------------------------------
 template <class T>
 struct PcgArgs {
-    double* result;  // reduced sums published by grid_sync_reduce
+    KryScal* sc;     // scalar state (global)
     int64_t m, nslices;
     const int32_t* perm;
     const int32_t* ptr;
@@ -550,21 +350,23 @@ struct PcgArgs {
     double* out_resid;
 };
 
-constexpr int kKryThreads = 256;
 
 template <class T>
 __global__ void __launch_bounds__(kKryThreads, sizeof(T) == 4 ? 4 : 3) k_pcg(PcgArgs<T> a) {
+    __shared__ KryScal sc;
     const int lane = threadIdx.x & 31;
     double* partA = a.part;
     double* partB = a.part + (size_t)gridDim.x * 3;
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
+    const double tol = a.tol;
+    const int max_iter = a.max_iter, rel = a.rel;
 
     // r = b - A x ; z = r / d ; p0 = z ; partials <r,r>, <b,b>, <z,r>
     {
         T v[3] = {T(0), T(0), T(0)};
         const T* x = a.x;
         TF_SLICE_LOOP(a.nslices, s) {
-            const T ax = sell_row<T>(a.ptr, a.col, a.val, s, lane, [&](int32_t j) { return __ldcg(x + j); });
+            const T ax = sell_row<T>(a.ptr, a.col, a.val, s, lane, [&](int32_t j) { return kld(x + j); });
             const int32_t row = __ldg(a.perm + s * 32 + lane);
             if (row >= 0) {
                 const T bi = a.b[row];
@@ -580,23 +382,22 @@ __global__ void __launch_bounds__(kKryThreads, sizeof(T) == 4 ? 4 : 3) k_pcg(Pcg
         }
         block_partials<3>(v, partA);
     }
-    double s0[3];
-    if (!grid_sync_reduce<3>(a.gs, partA, a.result, s0)) return;
-    double normb = sqrt(s0[1]);
-    if (normb == 0.0 || !a.rel) normb = 1.0;
-    double resid = sqrt(s0[0]) / normb;
-    double rho = s0[2];
-    if (resid <= a.tol) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            *a.out_iter = 0;
-            *a.out_resid = resid;
-        }
+    if (!grid_step<3>(a.gs, partA, a.sc, sc, [&](const double* s, KryScal& g) {
+            double nb = sqrt(s[1]);
+            if (nb == 0.0 || !rel) nb = 1.0;
+            g.normb = nb;
+            g.resid = sqrt(s[0]) / nb;
+            g.rho = s[2];
+            g.beta = 0.;
+            g.it = 0;
+            g.converged = g.resid <= tol;
+            g.done = g.converged || max_iter <= 0;
+        }))
         return;
-    }
-    T beta = T(0);
     T* pc = a.p0;  // previous direction (beta = 0 in the first iteration)
     T* pn = a.p1;
-    for (int it = 1; it <= a.max_iter; ++it) {
+    while (!sc.done) {
+        const T beta = (T)sc.beta;
         // phase A: p_new = z + beta p_old ; q = A p_new ; <q, p_new>
         {
             T v[1] = {T(0)};
@@ -604,10 +405,10 @@ __global__ void __launch_bounds__(kKryThreads, sizeof(T) == 4 ? 4 : 3) k_pcg(Pcg
             const T* po = pc;
             TF_SLICE_LOOP(a.nslices, s) {
                 const T acc = sell_row<T>(a.ptr, a.col, a.val, s, lane,
-                                          [&](int32_t j) { return __ldcg(z + j) + beta * __ldcg(po + j); });
+                                          [&](int32_t j) { return kld(z + j) + beta * kld(po + j); });
                 const int32_t row = __ldg(a.perm + s * 32 + lane);
                 if (row >= 0) {
-                    const T pi = __ldcg(z + row) + beta * __ldcg(po + row);
+                    const T pi = kld(z + row) + beta * kld(po + row);
                     pn[row] = pi;
                     a.q[row] = acc;
                     v[0] += acc * pi;
@@ -615,15 +416,14 @@ __global__ void __launch_bounds__(kKryThreads, sizeof(T) == 4 ? 4 : 3) k_pcg(Pcg
             }
             block_partials<1>(v, partA);
         }
-        double lam[1];
-        if (!grid_sync_reduce<1>(a.gs, partA, a.result + 4, lam)) return;
-        const T alpha = (T)(rho / lam[0]);
+        if (!grid_step<1>(a.gs, partA, a.sc, sc, [&](const double* s, KryScal& g) { g.alpha = g.rho / s[0]; })) return;
+        const T alpha = (T)sc.alpha;
         // phase B: x += alpha p ; r -= alpha q ; z = r / d ; <r,r>, <z,r>
         {
             T v[2] = {T(0), T(0)};
             for (int64_t i = tid; i < a.m; i += nth) {
-                a.x[i] += alpha * __ldcg(pn + i);
-                const T ri = a.r[i] - alpha * __ldcg(a.q + i);
+                a.x[i] += alpha * kld(pn + i);
+                const T ri = a.r[i] - alpha * kld(a.q + i);
                 const T zi = ri / a.diag[i];
                 a.r[i] = ri;
                 a.z[i] = zi;
@@ -632,22 +432,22 @@ __global__ void __launch_bounds__(kKryThreads, sizeof(T) == 4 ? 4 : 3) k_pcg(Pcg
             }
             block_partials<2>(v, partB);
         }
-        double s2[2];
-        if (!grid_sync_reduce<2>(a.gs, partB, a.result + 8, s2)) return;
-        resid = sqrt(s2[0]) / normb;
-        if (resid <= a.tol || it == a.max_iter) {
-            if (blockIdx.x == 0 && threadIdx.x == 0) {
-                *a.out_iter = resid <= a.tol ? it : -it;
-                *a.out_resid = resid;
-            }
+        if (!grid_step<2>(a.gs, partB, a.sc, sc, [&](const double* s, KryScal& g) {
+                g.it += 1;
+                g.resid = sqrt(s[0]) / g.normb;
+                g.converged = g.resid <= tol;
+                g.done = g.converged || g.it >= max_iter;
+                g.beta = s[1] / g.rho;
+                g.rho = s[1];
+            }))
             return;
-        }
-        const double rho1 = rho;
-        rho = s2[1];
-        beta = (T)(rho / rho1);
         T* tmp = pc;
         pc = pn;
         pn = tmp;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *a.out_iter = sc.converged ? (int)sc.it : -1 - (int)sc.it;
+        *a.out_resid = sc.resid;
     }
 }
 
@@ -667,7 +467,7 @@ __global__ void __launch_bounds__(kKryThreads, sizeof(T) == 4 ? 4 : 3) k_pcg(Pcg
 constexpr double kRelUpdate = 0.1;
 
 struct PcgMixedArgs {
-    double* result;
+    KryScal* sc;
     int64_t m, nslices;
     const int32_t* perm;
     const int32_t* ptr;
@@ -693,18 +493,21 @@ struct PcgMixedArgs {
 };
 
 __global__ void __launch_bounds__(kKryThreads, 3) k_pcg_mixed(PcgMixedArgs a) {
+    __shared__ KryScal sc;
     const int lane = threadIdx.x & 31;
     double* partA = a.part;
     double* partB = a.part + (size_t)gridDim.x * 3;
     double* partC = a.part + (size_t)gridDim.x * 6;
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
+    const double tol = a.tol;
+    const int max_iter = a.max_iter, rel = a.rel;
 
     // r = b - A x in FP64, then FP32 copies: r, z = r / d; <r,r>, <b,b>, <z,r> in FP64
-    auto true_residual = [&](double* part, bool with_b, bool set_p) {
+    auto true_residual = [&](bool first) {
         double v[3] = {0., 0., 0.};
         const double* x = a.x;
         TF_SLICE_LOOP(a.nslices, s) {
-            const double ax = sell_row<double>(a.ptr, a.col, a.val64, s, lane, [&](int32_t j) { return __ldcg(x + j); });
+            const double ax = sell_row<double>(a.ptr, a.col, a.val64, s, lane, [&](int32_t j) { return kld(x + j); });
             const int32_t row = __ldg(a.perm + s * 32 + lane);
             if (row >= 0) {
                 const double bi = a.b[row];
@@ -713,36 +516,35 @@ __global__ void __launch_bounds__(kKryThreads, 3) k_pcg_mixed(PcgMixedArgs a) {
                 const float z32 = r32 / a.diag[row];
                 a.r[row] = r32;
                 a.z[row] = z32;
-                if (set_p) a.p0[row] = z32;
+                if (first) a.p0[row] = z32;
                 v[0] += ri * ri;
-                if (with_b) v[1] += bi * bi;
+                if (first) v[1] += bi * bi;
                 v[2] += (double)(z32 * r32);
             }
         }
-        block_partials<3>(v, part);
+        block_partials<3>(v, partC);
     };
 
-    true_residual(partC, true, true);
-    double s0[3];
-    if (!grid_sync_reduce<3>(a.gs, partC, a.result, s0)) return;
-    double normb = sqrt(s0[1]);
-    if (normb == 0.0 || !a.rel) normb = 1.0;
-    double resid = sqrt(s0[0]) / normb;
-    double rho = s0[2];
-    double r_last = sqrt(s0[0]);
-    int updates = 1;
-    if (resid <= a.tol) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            *a.out_iter = 0;
-            *a.out_resid = resid;
-            *a.out_updates = updates;
-        }
+    true_residual(true);
+    if (!grid_step<3>(a.gs, partC, a.sc, sc, [&](const double* s, KryScal& g) {
+            double nb = sqrt(s[1]);
+            if (nb == 0.0 || !rel) nb = 1.0;
+            g.normb = nb;
+            g.r_last = sqrt(s[0]);
+            g.resid = g.r_last / nb;
+            g.rho = s[2];
+            g.beta = 0.;
+            g.it = 0;
+            g.updates = 1;
+            g.true_res = 0;
+            g.converged = g.resid <= tol;
+            g.done = g.converged || max_iter <= 0;
+        }))
         return;
-    }
-    float beta = 0.f;
     float* pc = a.p0;
     float* pn = a.p1;
-    for (int it = 1; it <= a.max_iter; ++it) {
+    while (!sc.done) {
+        const float beta = (float)sc.beta;
         // phase A (FP32): p_new = z + beta p_old ; q = A p_new ; <q, p_new>
         {
             float v[1] = {0.f};
@@ -750,10 +552,10 @@ __global__ void __launch_bounds__(kKryThreads, 3) k_pcg_mixed(PcgMixedArgs a) {
             const float* po = pc;
             TF_SLICE_LOOP(a.nslices, s) {
                 const float acc = sell_row<float>(a.ptr, a.col, a.val32, s, lane,
-                                                  [&](int32_t j) { return __ldcg(z + j) + beta * __ldcg(po + j); });
+                                                  [&](int32_t j) { return kld(z + j) + beta * kld(po + j); });
                 const int32_t row = __ldg(a.perm + s * 32 + lane);
                 if (row >= 0) {
-                    const float pi = __ldcg(z + row) + beta * __ldcg(po + row);
+                    const float pi = kld(z + row) + beta * kld(po + row);
                     pn[row] = pi;
                     a.q[row] = acc;
                     v[0] += acc * pi;
@@ -761,17 +563,16 @@ __global__ void __launch_bounds__(kKryThreads, 3) k_pcg_mixed(PcgMixedArgs a) {
             }
             block_partials<1>(v, partA);
         }
-        double lam[1];
-        if (!grid_sync_reduce<1>(a.gs, partA, a.result + 4, lam)) return;
-        const double alpha = rho / lam[0];
+        if (!grid_step<1>(a.gs, partA, a.sc, sc, [&](const double* s, KryScal& g) { g.alpha = g.rho / s[0]; })) return;
+        const double alpha = sc.alpha;
         const float alpha32 = (float)alpha;
         // phase B: x += alpha p (FP64) ; r -= alpha q ; z = r / d (FP32) ; <r,r>, <z,r>
         {
             float v[2] = {0.f, 0.f};
             for (int64_t i = tid; i < a.m; i += nth) {
-                const float pi = __ldcg(pn + i);
+                const float pi = kld(pn + i);
                 a.x[i] += alpha * (double)pi;
-                const float ri = a.r[i] - alpha32 * __ldcg(a.q + i);
+                const float ri = a.r[i] - alpha32 * kld(a.q + i);
                 const float zi = ri / a.diag[i];
                 a.r[i] = ri;
                 a.z[i] = zi;
@@ -780,33 +581,38 @@ __global__ void __launch_bounds__(kKryThreads, 3) k_pcg_mixed(PcgMixedArgs a) {
             }
             block_partials<2>(v, partB);
         }
-        double s2[2];
-        if (!grid_sync_reduce<2>(a.gs, partB, a.result + 8, s2)) return;
-        const double rn32 = sqrt(s2[0]);
-        double rho_new = s2[1];
-        if (rn32 <= kRelUpdate * r_last || rn32 / normb <= a.tol || it == a.max_iter) {
-            // reliable update: FP64 residual replaces the FP32 one
-            true_residual(partC, false, false);
-            double s3[3];
-            if (!grid_sync_reduce<3>(a.gs, partC, a.result + 12, s3)) return;
-            ++updates;
-            r_last = sqrt(s3[0]);
-            resid = r_last / normb;
-            rho_new = s3[2];
-            if (resid <= a.tol || it == a.max_iter) {
-                if (blockIdx.x == 0 && threadIdx.x == 0) {
-                    *a.out_iter = resid <= a.tol ? it : -it;
-                    *a.out_resid = resid;
-                    *a.out_updates = updates;
+        if (!grid_step<2>(a.gs, partB, a.sc, sc, [&](const double* s, KryScal& g) {
+                g.it += 1;
+                const double rn = sqrt(s[0]);
+                g.true_res = rn <= kRelUpdate * g.r_last || rn / g.normb <= tol || g.it >= max_iter;
+                if (!g.true_res) {
+                    g.beta = s[1] / g.rho;
+                    g.rho = s[1];
                 }
+            }))
+            return;
+        if (sc.true_res) {
+            // reliable update: the FP64 residual replaces the FP32 one
+            true_residual(false);
+            if (!grid_step<3>(a.gs, partC, a.sc, sc, [&](const double* s, KryScal& g) {
+                    g.updates += 1;
+                    g.r_last = sqrt(s[0]);
+                    g.resid = g.r_last / g.normb;
+                    g.converged = g.resid <= tol;
+                    g.done = g.converged || g.it >= max_iter;
+                    g.beta = s[2] / g.rho;
+                    g.rho = s[2];
+                }))
                 return;
-            }
         }
-        beta = (float)(rho_new / rho);
-        rho = rho_new;
         float* tmp = pc;
         pc = pn;
         pn = tmp;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *a.out_iter = sc.converged ? (int)sc.it : -1 - (int)sc.it;
+        *a.out_resid = sc.resid;
+        *a.out_updates = (int)sc.updates;
     }
 }
 
@@ -820,7 +626,7 @@ void release_solver_workspace(Context* c) {
 }
 
 // blocks of a cooperative launch: all co-resident, at most one row slice per warp
-static int coop_blocks(Context* c, const void* fn, int64_t nslices, int* out) {
+int coop_blocks(Context* c, const void* fn, int64_t nslices, int* out) {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kKryThreads, 0) != cudaSuccess || per_sm < 1)
         return set_err(c, TF_ERR_CUDA, "occupancy query failed");
@@ -837,7 +643,7 @@ static int run_pcg_kernel(Context* c, const CSR& A, const T* val, const T* diag,
     const void* fn = (const void*)k_pcg<T>;
     int blocks = 0;
     TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks));
-    TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 3 * 2 + 16));
+    TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 3 * 2 + 16 + kScalWords));
     TF_TRY(ensure(c, c->kry_bar, 2));
     TF_TRY(ensure(c, c->kry_iters, 1));
     TF_TRY(ensure(c, c->kry_resid, 1));
@@ -859,7 +665,7 @@ static int run_pcg_kernel(Context* c, const CSR& A, const T* val, const T* diag,
     a.p1 = work + 3 * A.m;
     a.q = work + 4 * A.m;
     a.part = c->kry_part.p;
-    a.result = c->kry_part.p + (size_t)blocks * 3 * 2;
+    a.sc = reinterpret_cast<KryScal*>(c->kry_part.p + (size_t)blocks * 3 * 2 + 16);
     a.gs = GridSync{c->kry_bar.p, c->kry_bar.p + 1, c->status.p};
     a.max_iter = max_iter;
     a.tol = tol;
@@ -893,7 +699,7 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
         double res = 0.;
         TF_TRY(run_pcg_kernel<double>(c, A, A.sell.v64, A.diag, b, x, c->kry64.p, *max_iter, *tol, rel, &it, &res));
         const bool ok = it >= 0;
-        *max_iter = ok ? it : -it;
+        *max_iter = ok ? it : -1 - it;
         *tol = res;
         return ok ? TF_OK : set_err(c, TF_ERR_NOT_CONVERGED, "pcg: no convergence within max_iter");
     }
@@ -906,7 +712,7 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
     const void* fn = (const void*)k_pcg_mixed;
     int blocks = 0;
     TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks));
-    TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 3 * 3 + 16));
+    TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 3 * 3 + 16 + kScalWords));
     TF_TRY(ensure(c, c->kry_bar, 2));
     TF_TRY(ensure(c, c->kry_iters, 2));
     TF_TRY(ensure(c, c->kry_resid, 1));
@@ -929,7 +735,7 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
     g.p1 = d32 + 4 * m;
     g.q = d32 + 5 * m;
     g.part = c->kry_part.p;
-    g.result = c->kry_part.p + (size_t)blocks * 3 * 3;
+    g.sc = reinterpret_cast<KryScal*>(c->kry_part.p + (size_t)blocks * 3 * 3 + 16);
     g.gs = GridSync{c->kry_bar.p, c->kry_bar.p + 1, c->status.p};
     g.max_iter = *max_iter;
     g.tol = *tol;
@@ -948,7 +754,7 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
     TF_TRY(sync_status(c, &st));
     if (st) return set_err(c, st, "pcg (mixed): grid barrier watchdog fired");
     c->last_refinements = it[1];
-    *max_iter = it[0] >= 0 ? it[0] : -it[0];
+    *max_iter = it[0] >= 0 ? it[0] : -1 - it[0];
     *tol = res;
     return it[0] >= 0 ? TF_OK : set_err(c, TF_ERR_NOT_CONVERGED, "pcg (mixed): no convergence within max_iter");
 }
@@ -1006,7 +812,7 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres(GmresArgs a) {
         double v[2] = {0., 0.};
         const double* x0 = a.x;
         TF_SLICE_LOOP(a.nslices, sl) {
-            const double ax = sell_row<double>(a.ptr, a.col, a.val, sl, lane, [&](int32_t j) { return __ldcg(x0 + j); });
+            const double ax = sell_row<double>(a.ptr, a.col, a.val, sl, lane, [&](int32_t j) { return kld(x0 + j); });
             const int32_t row = __ldg(a.perm + sl * 32 + lane);
             if (row >= 0) {
                 double r = a.b[row] - ax, bb = a.b[row];
@@ -1051,7 +857,7 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres(GmresArgs a) {
                 if (a.binv) {
                     const int64_t half = m / 2;
                     for (int64_t e = tid; e < half; e += nth) {
-                        const double va = sci * __ldcg(Vi + e), vb = sci * __ldcg(Vi + e + half);
+                        const double va = sci * kld(Vi + e), vb = sci * kld(Vi + e + half);
                         const double* q4 = a.binv + 4 * e;
                         a.Z[e] = q4[0] * va + q4[1] * vb;
                         a.Z[e + half] = q4[2] * va + q4[3] * vb;
@@ -1067,15 +873,15 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres(GmresArgs a) {
                     const double* Zp = a.binv ? a.Z : nullptr;
                     TF_SLICE_LOOP(a.nslices, s2) {
                         double acc = sell_row<double>(a.ptr, a.col, a.val, s2, lane, [&](int32_t j) {
-                            if (Zp) return __ldcg(Zp + j);
-                            const double vj = sci * __ldcg(Vi + j);
+                            if (Zp) return kld(Zp + j);
+                            const double vj = sci * kld(Vi + j);
                             return left ? vj : vj / __ldg(dg + j);
                         });
                         const int32_t row = __ldg(a.perm + s2 * 32 + lane);
                         if (row >= 0) {
                             if (a.left) acc = acc / a.diag[row];
                             W[row] = acc;
-                            v1[0] += acc * (sc0 * __ldcg(a.V + row));
+                            v1[0] += acc * (sc0 * kld(a.V + row));
                         }
                     }
                     block_partials<1>(v1, pq);
@@ -1093,9 +899,9 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres(GmresArgs a) {
                     const double scn = k < i ? sc[k + 1] : 0.;
                     double v1[1] = {0.};
                     for (int64_t e = tid; e < m; e += nth) {
-                        const double w = __ldcg(W + e) - hk * __ldcg(Vk + e);
+                        const double w = kld(W + e) - hk * kld(Vk + e);
                         W[e] = w;
-                        v1[0] += k < i ? w * (scn * __ldcg(Vn + e)) : w * w;
+                        v1[0] += k < i ? w * (scn * kld(Vn + e)) : w * w;
                     }
                     block_partials<1>(v1, pq);
                     double h[1];
@@ -1151,8 +957,8 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres(GmresArgs a) {
                 for (int64_t e = tid; e < half; e += nth) {
                     double za = 0., zb = 0.;
                     for (int q = 0; q <= kk; ++q) {
-                        za += y[q] * (sc[q] * __ldcg(a.V + (size_t)q * m + e));
-                        zb += y[q] * (sc[q] * __ldcg(a.V + (size_t)q * m + e + half));
+                        za += y[q] * (sc[q] * kld(a.V + (size_t)q * m + e));
+                        zb += y[q] * (sc[q] * kld(a.V + (size_t)q * m + e + half));
                     }
                     const double* q4 = a.binv + 4 * e;
                     a.x[e] = a.x[e] + (q4[0] * za + q4[1] * zb);
@@ -1161,7 +967,7 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres(GmresArgs a) {
             } else {
                 for (int64_t e = tid; e < m; e += nth) {
                     double z = 0.;
-                    for (int q = 0; q <= kk; ++q) z += y[q] * (sc[q] * __ldcg(a.V + (size_t)q * m + e));
+                    for (int q = 0; q <= kk; ++q) z += y[q] * (sc[q] * kld(a.V + (size_t)q * m + e));
                     if (!a.left) z = z / a.diag[e];
                     a.x[e] = a.x[e] + z;
                 }
@@ -1180,7 +986,7 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres(GmresArgs a) {
                 double v1[1] = {0.};
                 const double* x1 = a.x;
                 TF_SLICE_LOOP(a.nslices, s3) {
-                    const double ax = sell_row<double>(a.ptr, a.col, a.val, s3, lane, [&](int32_t j) { return __ldcg(x1 + j); });
+                    const double ax = sell_row<double>(a.ptr, a.col, a.val, s3, lane, [&](int32_t j) { return kld(x1 + j); });
                     const int32_t row = __ldg(a.perm + s3 * 32 + lane);
                     if (row >= 0) {
                         double r = a.b[row] - ax;
@@ -1237,8 +1043,12 @@ int gmres_jacobi(Context* c, CSR& A, const double* b, double* x, int restart, in
     const bool block = &A == &c->mats[TF_MAT_BLOCK];
     if (block && method == 1)
         return set_err(c, TF_ERR_BAD_INPUT, "gmres: the block-Jacobi preconditioner is applied from the right (method 0)");
+    if (precision == TF_PREC_MIXED || (precision == TF_PREC_FP64 && c->gmres_orth == TF_ORTH_CGS2)) {
+        if (method != 0) return set_err(c, TF_ERR_BAD_INPUT, "gmres (CGS2 / mixed): right preconditioning only");
+        return gmres2(c, A, b, x, restart, precision == TF_PREC_MIXED, max_iter, tol, rel);
+    }
     if (restart > kMaxRestart) return set_err(c, TF_ERR_CAPACITY, "gmres: restart > 64");
-    if (precision != TF_PREC_FP64) return set_err(c, TF_ERR_BAD_INPUT, "gmres: FP64 only");
+    if (precision != TF_PREC_FP64) return set_err(c, TF_ERR_BAD_INPUT, "gmres: precision");
     TF_TRY(ensure_diag(c, A));
     TF_TRY(ensure_sell(c, A, false));
     const int64_t m = A.m;

@@ -15,8 +15,10 @@
 // at that DOF; then the DOF's coordinates, the unit normal of the level set
 // in the tet that first touched the DOF, the constant 1 (bias), zeros.
 // s_chi, s_omega are the RMS increments of the last step and S_omega the RMS
-// of omega_n, so the targets (chi_{n+1} - chi_n) / s_chi and
-// (omega_{n+1} - omega_n) / s_omega are of order one.
+// of omega_n.  The network corrects linear extrapolation: its targets are
+// ((chi_{n+1} - chi_n) - (chi_n - chi_{n-1})) / s_chi and the same for omega,
+// and the guess is x_n + (x_n - x_{n-1}) + s * prediction, so an untrained
+// network (prediction ~ 0) already gives the extrapolated state.
 //
 // Guard: the learned guess is used only when its FP64 residual is smaller
 // than the previous-step guess's, and after a step whose learned solve took
@@ -132,18 +134,19 @@ __global__ void k_ch_features(int64_t m, const int32_t* __restrict__ rowptr, con
         const uint4* src = reinterpret_cast<const uint4*>(f);
         for (int q = 0; q < kFeat / 8; ++q) dst[q] = src[q];
         if (Y && xnext) {
-            Y[2 * i] = (float)((xnext[i] - xn[i]) / s_c);
-            Y[2 * i + 1] = (float)((xnext[m + i] - xn[m + i]) / s_w);
+            Y[2 * i] = (float)(((xnext[i] - xn[i]) - (xn[i] - xp[i])) / s_c);
+            Y[2 * i + 1] = (float)(((xnext[m + i] - xn[m + i]) - (xn[m + i] - xp[m + i])) / s_w);
         }
     }
 }
 
-// guess = x_n + (s_chi, s_omega) * prediction
-__global__ void k_ch_apply(int64_t m, const double* __restrict__ xn, const float* __restrict__ pred,
-                           const double* __restrict__ sc, double* __restrict__ guess) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
-        guess[i] = xn[i] + sc[0] * (double)pred[2 * i];
-        guess[m + i] = xn[m + i] + sc[1] * (double)pred[2 * i + 1];
+// guess = x_n + (x_n - x_{n-1}) + (s_chi, s_omega) * prediction (pred == nullptr: extrapolation only)
+__global__ void k_ch_apply(int64_t m, const double* __restrict__ xn, const double* __restrict__ xp,
+                           const float* __restrict__ pred, const double* __restrict__ sc, double* __restrict__ guess) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 2 * m; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t d = i < m ? i : i - m;
+        const double corr = pred ? sc[i < m ? 0 : 1] * (double)pred[2 * d + (i < m ? 0 : 1)] : 0.;
+        guess[i] = (xn[i] + (xn[i] - xp[i])) + corr;
     }
 }
 
@@ -245,9 +248,11 @@ int ch_steps_learned(Context* c, const ChLearnParams& P, int* iters, double* res
         const bool have_hist = step > 0;
         bool use = false;
         if (have_hist) TF_TRY(ch_features_dev(c, X, x_old, nullptr));
-        if (have_hist && P.learned && trained >= P.min_trained && !fallback_next) {
-            TF_TRY(mlp_forward_dev(c, c->ch_X.p, m, c->ch_pred.p));
-            k_ch_apply<<<grid_for(c, m), kBlock, 0, c->stream>>>(m, X, c->ch_pred.p, c->ch_scales.p, guess);
+        const bool mlp_ready = P.learned == 2 || (P.learned == 1 && trained >= P.min_trained);
+        if (have_hist && mlp_ready && !fallback_next) {
+            if (P.learned == 1) TF_TRY(mlp_forward_dev(c, c->ch_X.p, m, c->ch_pred.p));
+            k_ch_apply<<<grid_for(c, 2 * m), kBlock, 0, c->stream>>>(m, X, x_old, P.learned == 1 ? c->ch_pred.p : nullptr,
+                                                                     c->ch_scales.p, guess);
             ++c->launches;
             TF_CUDA(c, cudaGetLastError());
             double r_plain = 0., r_learn = 0.;
@@ -271,7 +276,7 @@ int ch_steps_learned(Context* c, const ChLearnParams& P, int* iters, double* res
             plain_ref = it;
         }
         // online training on this step's increment
-        if (have_hist && step < P.train_steps) {
+        if (have_hist && P.learned == 1 && step < P.train_steps) {
             TF_TRY(ch_features_dev(c, x_prev, x_old, X));
             double loss = 0.;
             for (int e = 0; e < P.epochs; ++e)

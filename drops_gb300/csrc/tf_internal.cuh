@@ -298,6 +298,11 @@ struct Context {
     DBuf<__nv_bfloat16> ch_X;
     int64_t ch_geom_version = -1;
     double ch_train_loss = 0.;
+    // CGS2 GMRES: B = A P^{-1} in SELL order, block inverses, bases
+    DBuf<float> gm2_b32, gm2_v32;
+    DBuf<double> gm2_b64, gm2_v64, gm2_binv;
+    int64_t gm2_src_version[2] = {-1, -1}, gm2_src_gen[2] = {-1, -1};
+    int gmres_orth = TF_ORTH_MGS;
 };
 
 struct ChLearnParams {
@@ -306,8 +311,8 @@ struct ChLearnParams {
     int restart = 50;
     double tol = 1e-10;
     int max_iter = 100000;
-    int precision = TF_PREC_FP64;
-    int learned = 1;        // 0: previous-step guess only (the reference's warm start)
+    int precision = TF_PREC_FP64;  // TF_PREC_MIXED: FP32 Arnoldi cycles in FP64 refinement
+    int learned = 1;        // 0: previous-step guess (the reference's warm start), 1: MLP, 2: extrapolation only
     int train_steps = 100;  // online training during the first steps
     int epochs = 2;
     int mb_tiles = 16;      // tiles of 128 DOFs per mini-batch
@@ -387,6 +392,8 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
 int gmres_jacobi(Context* c, CSR& A, const double* b, double* x, int restart, int method, int precision,
                  int* max_iter, double* tol, int rel);
 int ensure_diag(Context* c, CSR& A);
+int coop_blocks(Context* c, const void* fn, int64_t nslices, int* out);
+int gmres2(Context* c, CSR& A, const double* b, double* x, int restart, bool mixed, int* max_iter, double* tol, int rel);
 int ch_steps(Context* c, int nsteps, double dt, double mob, double eps, double beta_s, double xi, double rho_vol,
              int restart, double tol, int max_iter, int warm, int* iters, double* resids);
 void release_solver_workspace(Context* c);

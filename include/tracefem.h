@@ -199,6 +199,15 @@ int tf_pcg_jacobi(tf_context* ctx, int mat, int vec_b, int vec_x, int precision,
  * method 0 = right, 1 = left preconditioning.                                 */
 int tf_gmres_jacobi(tf_context* ctx, int mat, int vec_b, int vec_x, int restart, int method, int precision,
                     int* max_iter, double* tol, int rel);
+/* Orthogonalisation of tf_gmres_jacobi in FP64: TF_ORTH_MGS (default) is the
+ * reference's modified Gram-Schmidt, one grid barrier per projection;
+ * TF_ORTH_CGS2 is classical Gram-Schmidt with one reorthogonalisation, three
+ * grid barriers per Arnoldi step, right preconditioning only.  TF_PREC_MIXED
+ * always uses CGS2 with FP32 Arnoldi cycles, each restart being one step of
+ * FP64 iterative refinement (true residual and update of x in FP64).          */
+#define TF_ORTH_MGS 0
+#define TF_ORTH_CGS2 1
+int tf_gmres_options(tf_context* ctx, int orth);
 
 /* ---- batches of independent problems ----------------------------------------------- */
 /* The reference solves one surface problem per MultiGridCL; these calls run
@@ -311,11 +320,17 @@ int tf_ch_steps(tf_context* ctx, int nsteps, double dt, double mobility, double 
  * x_n + predicted increment when that guess has the smaller FP64 residual,
  * else the previous state, and a step whose learned solve needed more GMRES
  * iterations than the last plain solve makes the next step use the previous
- * state.  learned = 0 gives the plain previous-state warm start.  used[nsteps]
+ * state.  The network predicts the deviation from linear extrapolation, so
+ * the guess is x_n + (x_n - x_{n-1}) + predicted correction.  learned = 0
+ * gives the plain previous-state warm start, learned = 2 linear extrapolation
+ * without the network (same residual guard).  precision as
+ * in tf_gmres_jacobi (the orthogonalisation of tf_gmres_options applies to
+ * TF_PREC_FP64).  used[nsteps]
  * (may be NULL) flags the steps that started from the learned guess.          */
 int tf_ch_steps_learned(tf_context* ctx, int nsteps, double dt, double mobility, double eps, double beta_s, double xi,
-                        double rho_vol, int restart, double tol, int max_iter, int learned, int train_steps,
-                        int epochs, int minibatch_tiles, float lr, int* iters, double* resids, int* used);
+                        double rho_vol, int restart, double tol, int max_iter, int precision, int learned,
+                        int train_steps, int epochs, int minibatch_tiles, float lr, int* iters, double* resids,
+                        int* used);
 
 /* ---- instrumentation -------------------------------------------------------------- */
 /* Per-kernel device time, recorded with CUDA events on the context's stream
