@@ -579,13 +579,17 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
             }
             __syncwarp();
             const int cnt = min(32, npts - base);
+            // P1: 10 entries x 3 point groups on 30 lanes, F: 4 rows x 8 groups
+            // (groups combined after the last chunk); P2: 55 entries on 2 x 32 lanes
+            constexpr int kGroups = NL == 4 ? 3 : 1;
+            const int grp = NL == 4 ? lane / 10 : 0;
             for (int q = 0; q < EPL; ++q) {
-                const int k = lane + 32 * q;
-                if (k >= NSYM) break;
+                const int k = NL == 4 ? lane % 10 : lane + 32 * q;
+                if (k >= NSYM || grp >= kGroups) break;
                 int i, j;
                 sym_entry(NL, k, i, j);
                 double sm = accM[q], sa = accA[q], sl = accL[q];
-                for (int pp = 0; pp < cnt; ++pp) {
+                for (int pp = grp; pp < cnt; pp += kGroups) {
                     if (wantM) sm += S.phi[pp][j] * S.phi[pp][i];
                     if (wantA || wantL) {
                         const double d = S.sg[pp][j][0] * S.sg[pp][i][0] + S.sg[pp][j][1] * S.sg[pp][i][1] +
@@ -598,9 +602,25 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
                 accA[q] = sa;
                 accL[q] = sl;
             }
-            if (wantF && lane < NL)
+            if constexpr (NL == 4) {
+                if (wantF)
+                    for (int pp = lane >> 2; pp < cnt; pp += 8) accF += (S.w[pp] * S.fx[pp]) * S.phi[pp][lane & 3];
+            } else if (wantF && lane < NL) {
                 for (int pp = 0; pp < cnt; ++pp) accF += (S.w[pp] * S.fx[pp]) * S.phi[pp][lane];
+            }
             __syncwarp();
+        }
+        if constexpr (NL == 4) {
+            // combine the point groups in a fixed order: entries (g0 + g1) + g2, F tree over 8 groups
+            const double m1 = __shfl_down_sync(0xffffffffu, accM[0], 10), m2 = __shfl_down_sync(0xffffffffu, accM[0], 20);
+            const double a1 = __shfl_down_sync(0xffffffffu, accA[0], 10), a2 = __shfl_down_sync(0xffffffffu, accA[0], 20);
+            const double l1 = __shfl_down_sync(0xffffffffu, accL[0], 10), l2 = __shfl_down_sync(0xffffffffu, accL[0], 20);
+            accM[0] = (accM[0] + m1) + m2;
+            accA[0] = (accA[0] + a1) + a2;
+            accL[0] = (accL[0] + l1) + l2;
+            accF += __shfl_down_sync(0xffffffffu, accF, 16);
+            accF += __shfl_down_sync(0xffffffffu, accF, 8);
+            accF += __shfl_down_sync(0xffffffffu, accF, 4);
         }
         if (wantC) {
             // normal-gradient volume stabilisation on the 15-point Quad5 rule
@@ -614,14 +634,25 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
                 for (int i = 0; i < NL; ++i) S.phi[lane][i] = dn[i];
             }
             __syncwarp();
-            for (int q = 0; q < EPL; ++q) {
-                const int k = lane + 32 * q;
-                if (k >= NSYM) break;
-                int i, j;
-                sym_entry(NL, k, i, j);
+            if constexpr (NL == 4) {
                 double sc = 0.;
-                for (int pp = 0; pp < 15; ++pp) sc += cT.q3_w[pp] * (S.phi[pp][j] * S.phi[pp][i]);
-                accC[q] = sc * S.g.absdet;
+                if (lane < 30) {
+                    int i, j;
+                    sym_entry(NL, lane % 10, i, j);
+                    for (int pp = lane / 10; pp < 15; pp += 3) sc += cT.q3_w[pp] * (S.phi[pp][j] * S.phi[pp][i]);
+                }
+                const double s1 = __shfl_down_sync(0xffffffffu, sc, 10), s2 = __shfl_down_sync(0xffffffffu, sc, 20);
+                accC[0] = ((sc + s1) + s2) * S.g.absdet;
+            } else {
+                for (int q = 0; q < EPL; ++q) {
+                    const int k = lane + 32 * q;
+                    if (k >= NSYM) break;
+                    int i, j;
+                    sym_entry(NL, k, i, j);
+                    double sc = 0.;
+                    for (int pp = 0; pp < 15; ++pp) sc += cT.q3_w[pp] * (S.phi[pp][j] * S.phi[pp][i]);
+                    accC[q] = sc * S.g.absdet;
+                }
             }
             __syncwarp();
         }

@@ -60,6 +60,7 @@ int tf_create(tf_context** out, int device) {
     // cheaper, more hide gather latency); TF_KRY_BLOCKS_PER_SM overrides.
     c->kry_blocks_per_sm = 2;
     if (const char* e = std::getenv("TF_KRY_BLOCKS_PER_SM")) c->kry_blocks_per_sm = std::atoi(e);
+    if (const char* e = std::getenv("TF_KRY_THREADS")) c->kry_threads = std::atoi(e);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
         cudaMallocHost((void**)&c->h_status, 4 * sizeof(int)) != cudaSuccess ||

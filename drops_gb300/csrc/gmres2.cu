@@ -54,44 +54,47 @@ struct Gm2Args {
     int* out_cycles;
 };
 
-// Grid step over n partial sums per block (n <= kGm2Stride), partials and
-// sums in S: the last block sums the partials in a fixed order and thread 0
-// runs f(sums, state).  The Arnoldi dots of the FP32 cycles reduce in FP32
-// all the way (S = float): FP64 instructions tie up the FP64 pipe whatever
-// the number of active lanes, and the basis itself is FP32.
+// Grid step with a fixed master block.  Every block has written n partial
+// sums (type S) for this step; block 0 waits until all others have arrived,
+// sums the partials in a fixed order, and its thread 0 runs f(sums, state) on
+// block 0's shared-memory copy of the state (the Hessenberg matrix and the
+// Givens rotations live in block 0's shared memory too, so the serial scalar
+// work never waits on global-memory latency), publishes the state, and
+// releases the others, which copy it.  The Arnoldi dots of the FP32 cycles
+// reduce in FP32 all the way (S = float): FP64 instructions tie up the FP64
+// pipe whatever the number of active lanes, and the basis itself is FP32.
 template <class S, class F>
 __device__ bool gm2_step(const GridSync& g, const S* part, int n, Gm2Scal* gsc, Gm2Scal& ssc, F f) {
-    __shared__ int last;
     __shared__ int st;
     __shared__ S sums[kGm2Stride];
     __syncthreads();
-    unsigned my = 0;
-    if (threadIdx.x == 0) {
-        volatile unsigned* vgen = g.gen;
-        my = *vgen;
-        __threadfence();
-        last = atomicAdd(g.count, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (last) {
-        __threadfence();
-        for (int k = threadIdx.x; k < n; k += blockDim.x) {
-            S x = S(0);
-            for (unsigned b = 0; b < gridDim.x; ++b) x += __ldcg(part + (size_t)b * kGm2Stride + k);
-            sums[k] = x;
+    if (blockIdx.x != 0) {
+        if (threadIdx.x == 0) {
+            volatile unsigned* vgen = g.gen;
+            const unsigned my = *vgen;
+            __threadfence();
+            atomicAdd(g.count, 1u);
+            long long spins = 0;
+            while (*vgen == my) {
+                if (++spins > kSpinLimit) {
+                    atomicCAS(g.status, 0, TF_ERR_WATCHDOG);
+                    break;
+                }
+                if (spins > 256) __nanosleep(32);
+            }
+            __threadfence();
+            st = *((volatile int*)g.status);
+            const unsigned long long* src = reinterpret_cast<const unsigned long long*>(gsc);
+            unsigned long long* dst = reinterpret_cast<unsigned long long*>(&ssc);
+            for (int k = 0; k < (int)(sizeof(Gm2Scal) / 8); ++k) dst[k] = __ldcg(src + k);
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            f(sums, *gsc);
-            __threadfence();
-            *g.count = 0;
-            __threadfence();
-            atomicAdd(g.gen, 1u);
-        }
-    } else if (threadIdx.x == 0) {
-        volatile unsigned* vgen = g.gen;
+        return st == 0;
+    }
+    if (threadIdx.x == 0) {
+        volatile unsigned* vcount = g.count;
         long long spins = 0;
-        while (*vgen == my) {
+        while (*vcount != gridDim.x - 1) {
             if (++spins > kSpinLimit) {
                 atomicCAS(g.status, 0, TF_ERR_WATCHDOG);
                 break;
@@ -99,15 +102,46 @@ __device__ bool gm2_step(const GridSync& g, const S* part, int n, Gm2Scal* gsc, 
             if (spins > 256) __nanosleep(32);
         }
         __threadfence();
-    }
-    if (threadIdx.x == 0) {
         st = *((volatile int*)g.status);
-        const unsigned long long* src = reinterpret_cast<const unsigned long long*>(gsc);
-        unsigned long long* dst = reinterpret_cast<unsigned long long*>(&ssc);
-        for (int k = 0; k < (int)(sizeof(Gm2Scal) / 8); ++k) dst[k] = __ldcg(src + k);
     }
     __syncthreads();
-    return st == 0;
+    if (st != 0) return false;
+    // warp w sums the values k = w, w + 8, ...; its lanes split the blocks
+    // (independent loads in flight), then a fixed warp tree per value
+    {
+        constexpr int kPerWarp = (kGm2Stride + kGm2Warps - 1) / kGm2Warps;
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        S acc[kPerWarp];
+#pragma unroll
+        for (int q = 0; q < kPerWarp; ++q) acc[q] = S(0);
+        for (unsigned b = lane; b < gridDim.x; b += 32) {
+            const S* pb = part + (size_t)b * kGm2Stride;
+#pragma unroll
+            for (int q = 0; q < kPerWarp; ++q) {
+                const int k = warp + q * kGm2Warps;
+                if (k < n) acc[q] += __ldcg(pb + k);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kPerWarp; ++q) {
+            const S v = warp_sum(acc[q]);
+            const int k = warp + q * kGm2Warps;
+            if (lane == 0 && k < n) sums[k] = v;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        f(sums, ssc);
+        const unsigned long long* src = reinterpret_cast<const unsigned long long*>(&ssc);
+        unsigned long long* dst = reinterpret_cast<unsigned long long*>(gsc);
+        for (int k = 0; k < (int)(sizeof(Gm2Scal) / 8); ++k) dst[k] = src[k];
+        __threadfence();
+        *g.count = 0;
+        __threadfence();
+        atomicAdd(g.gen, 1u);
+    }
+    __syncthreads();
+    return true;
 }
 
 // warp partials (wred[k][warp]) -> block partials part[block][k]
@@ -125,6 +159,9 @@ template <class V>
 __global__ void __launch_bounds__(kKryThreads, 2) k_gmres2(Gm2Args<V> a) {
     __shared__ Gm2Scal sc;
     __shared__ V wred[kGm2Stride][kGm2Warps];   // Arnoldi dots, in V
+    // least-squares state, used by block 0 (the master of every grid step)
+    __shared__ V H[(kGm2MaxR + 1) * kGm2MaxR];  // H[k][i] at H[i * (R + 1) + k]
+    __shared__ V cs[kGm2MaxR], sn[kGm2MaxR], s[kGm2MaxR + 1], ys[kGm2MaxR];
     __shared__ double wres[2][kGm2Warps];       // FP64 true residual
     double* const part64 = a.part;
     V* const partV = reinterpret_cast<V*>(a.part);
@@ -132,11 +169,9 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres2(Gm2Args<V> a) {
     const int64_t m = a.m;
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
     const int R = a.R;
-    V* const H = a.small;                // H[k][i] at H[i * (R + 1) + k]
-    V* const cs = H + (size_t)(R + 1) * R;
-    V* const sn = cs + R;
-    V* const s = sn + R;
-    V* const y = s + R + 1;
+    // published by the master for every block: solution of the least-squares
+    // problem, basis scales, projection coefficients
+    V* const y = a.small;
     V* const scl = y + R;
     V* const coef = scl + R + 1;
     const double tol = a.tol, inner_floor = a.inner_floor;
@@ -300,9 +335,10 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres2(Gm2Args<V> a) {
                                 // y = H^{-1} s on the leading (i+1) x (i+1) triangle
                                 for (int q = i; q >= 0; --q) {
                                     V acc = s[q];
-                                    for (int p2 = q + 1; p2 <= i; ++p2) acc -= H[(size_t)p2 * (R + 1) + q] * y[p2];
-                                    y[q] = acc / H[(size_t)q * (R + 1) + q];
+                                    for (int p2 = q + 1; p2 <= i; ++p2) acc -= H[(size_t)p2 * (R + 1) + q] * ys[p2];
+                                    ys[q] = acc / H[(size_t)q * (R + 1) + q];
                                 }
+                                for (int q = 0; q <= i; ++q) y[q] = ys[q];
                                 g.cycle_end = 1;
                             }
                             g.i = i + 1;
@@ -424,7 +460,7 @@ static int run_gmres2(Context* c, CSR& A, const double* b, double* x, int R, int
     }
     const void* fn = (const void*)k_gmres2<V>;
     int blocks = 0;
-    TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks));
+    TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks, kKryThreads));
     // H (R+1) x R, cs R, sn R, s R+1, y R, scl R+1, coef R+1
     const size_t small = (size_t)(R + 1) * R + 6 * (size_t)R + 3;
     DBuf<V>& basis = *reinterpret_cast<DBuf<V>*>(sizeof(V) == 4 ? (void*)&c->gm2_v32 : (void*)&c->gm2_v64);

@@ -492,7 +492,8 @@ struct PcgMixedArgs {
     int* out_updates;
 };
 
-__global__ void __launch_bounds__(kKryThreads, 3) k_pcg_mixed(PcgMixedArgs a) {
+template <int NT>
+__global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_mixed(PcgMixedArgs a) {
     __shared__ KryScal sc;
     const int lane = threadIdx.x & 31;
     double* partA = a.part;
@@ -626,12 +627,12 @@ void release_solver_workspace(Context* c) {
 }
 
 // blocks of a cooperative launch: all co-resident, at most one row slice per warp
-int coop_blocks(Context* c, const void* fn, int64_t nslices, int* out) {
+int coop_blocks(Context* c, const void* fn, int64_t nslices, int* out, int threads) {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kKryThreads, 0) != cudaSuccess || per_sm < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess || per_sm < 1)
         return set_err(c, TF_ERR_CUDA, "occupancy query failed");
     if (c->kry_blocks_per_sm > 0 && c->kry_blocks_per_sm < per_sm) per_sm = c->kry_blocks_per_sm;
-    const int64_t want = (nslices * 32 + kKryThreads - 1) / kKryThreads;
+    const int64_t want = (nslices * 32 + threads - 1) / threads;
     int64_t b = std::min<int64_t>(want, (int64_t)per_sm * c->num_sms);
     *out = (int)(b < 1 ? 1 : b);
     return TF_OK;
@@ -642,7 +643,7 @@ static int run_pcg_kernel(Context* c, const CSR& A, const T* val, const T* diag,
                           double tol, int rel, int* iters_out, double* resid_out) {
     const void* fn = (const void*)k_pcg<T>;
     int blocks = 0;
-    TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks));
+    TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks, kKryThreads));
     TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 3 * 2 + 16 + kScalWords));
     TF_TRY(ensure(c, c->kry_bar, 2));
     TF_TRY(ensure(c, c->kry_iters, 1));
@@ -709,9 +710,11 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
     float* d32 = c->kry32.p;
     k_to_f32<<<grid_for(c, m), kBlock, 0, c->stream>>>(m, A.diag, d32);
     ++c->launches;
-    const void* fn = (const void*)k_pcg_mixed;
+    // 512-thread blocks (one per SM): half the blocks arrive at each grid barrier
+    const int nt = c->kry_threads == 512 ? 512 : 256;
+    const void* fn = nt == 512 ? (const void*)k_pcg_mixed<512> : (const void*)k_pcg_mixed<256>;
     int blocks = 0;
-    TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks));
+    TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks, nt));
     TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 3 * 3 + 16 + kScalWords));
     TF_TRY(ensure(c, c->kry_bar, 2));
     TF_TRY(ensure(c, c->kry_iters, 2));
@@ -744,7 +747,7 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
     g.out_resid = c->kry_resid.p;
     g.out_updates = c->kry_iters.p + 1;
     void* args[] = {&g};
-    TF_CUDA(c, cudaLaunchCooperativeKernel(fn, blocks, kKryThreads, args, 0, c->stream));
+    TF_CUDA(c, cudaLaunchCooperativeKernel(fn, blocks, nt, args, 0, c->stream));
     ++c->launches;
     int it[2] = {0, 0};
     double res = 0;
@@ -1064,7 +1067,7 @@ int gmres_jacobi(Context* c, CSR& A, const double* b, double* x, int restart, in
     }
     const void* fn = (const void*)k_gmres;
     int blocks = 0;
-    TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks));
+    TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks, kKryThreads));
     TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 2 * 2 + 8));
     TF_TRY(ensure(c, c->kry_bar, 2));
     TF_TRY(ensure(c, c->kry_iters, 1));

@@ -259,6 +259,7 @@ struct Context {
     int64_t launches = 0;
     int last_refinements = 0;  // FP64 residual replacements of the last mixed solve
     int kry_blocks_per_sm = 0; // cap on resident Krylov blocks per SM (0: occupancy limit)
+    int kry_threads = 256;     // block size of the mixed-precision PCG (256 or 512)
     int64_t pattern_counter = 0, block_src_gen = -1;
     DBuf<int32_t> sell_ptr[TF_NUM_MATS], sell_col[TF_NUM_MATS], sell_src[TF_NUM_MATS], sell_perm[TF_NUM_MATS];
     DBuf<double> sell_v64[TF_NUM_MATS];
@@ -392,7 +393,7 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
 int gmres_jacobi(Context* c, CSR& A, const double* b, double* x, int restart, int method, int precision,
                  int* max_iter, double* tol, int rel);
 int ensure_diag(Context* c, CSR& A);
-int coop_blocks(Context* c, const void* fn, int64_t nslices, int* out);
+int coop_blocks(Context* c, const void* fn, int64_t nslices, int* out, int threads);
 int gmres2(Context* c, CSR& A, const double* b, double* x, int restart, bool mixed, int* max_iter, double* tol, int rel);
 int ch_steps(Context* c, int nsteps, double dt, double mob, double eps, double beta_s, double xi, double rho_vol,
              int restart, double tol, int max_iter, int warm, int* iters, double* resids);

@@ -13,6 +13,9 @@
 //       setupFESystem (surfactant/ifacetransp.cpp:615-622) for M, A, C_n (+F),
 //       optional PCGSolverCL<JACPcCL> on M + A + h C_n (num/krylovsolver.h:1805).
 //   ref_harness legacy_numb <case> <out>    CreateNumbOnInterface test cases
+//   ref_harness legacy_forms <n> <a> <out>  SetupInterfaceMassP1 / SetupLBP1 / SetupInterfaceRhsP1
+//       (surfactant/ifacetransp.cpp:367-380, 499-512, 532-563) on the unit sphere,
+//       P2 level set, CreateNumbering(P1IF_FE)
 //   ref_harness area <out>                  tests/principallattice.cpp:316-347
 //   ref_harness gmres <n> <a> <steps> <out> Cahn-Hilliard BDF1 steps, DROPS GMRES
 #include <algorithm>
@@ -350,6 +353,63 @@ int cmd_legacy_numb(int argc, char** argv) {
     return 0;
 }
 
+double legacy_f(const Point3DCL& p, double) { return 1.0 + p[0] * p[1] - 0.5 * p[2]; }
+
+// The older surfactant.cpp path: legacy numbering and the legacy P1 forms.
+int cmd_legacy_forms(int argc, char** argv) {
+    if (argc < 5) throw std::invalid_argument("usage: legacy_forms n a out");
+    const int n = std::atoi(argv[2]);
+    const double a = std::atof(argv[3]);
+    Writer w(argv[4]);
+    BrickBuilderCL brick(Point3DCL(-a), 2. * a * std_basis<3>(1), 2. * a * std_basis<3>(2), 2. * a * std_basis<3>(3), n,
+                         n, n);
+    MultiGridCL mg(brick);
+    Flat F = flatten(mg);
+    w.l("tet_v", F.tet_v);
+    w.l("tet_ev", F.tet_ev);
+    w.d("coords", F.coords);
+    IdxDescCL lsIdx(P2_FE);
+    lsIdx.DistributeDOFs(0, mg);
+    VecDescCL ls(&lsIdx);
+    const Uint li = lsIdx.GetIdx();
+    DROPS_FOR_TRIANG_VERTEX(mg, 0, it) ls.Data[it->Unknowns(li)] = it->GetCoord().norm() - 1.0;
+    DROPS_FOR_TRIANG_EDGE(mg, 0, it)
+        ls.Data[it->Unknowns(li)] = (0.5 * (it->GetVertex(0)->GetCoord() + it->GetVertex(1)->GetCoord())).norm() - 1.0;
+    BndCondT bc[6] = {NoBC, NoBC, NoBC, NoBC, NoBC, NoBC};
+    BndDataCL<> lsbnd(6, bc);
+    IdxDescCL ifIdx(P1IF_FE);
+    const int64_t n_active = (int64_t)ifIdx.CreateNumbering(0, mg, &ls, &lsbnd);
+    w.i("n_active", n_active);
+    w.i("n_dofs", (int64_t)ifIdx.NumUnknowns());
+    std::vector<int64_t> dv;
+    const Uint ii = ifIdx.GetIdx();
+    DROPS_FOR_TRIANG_VERTEX(mg, 0, it) dv.push_back(it->Unknowns.Exist(ii) ? (int64_t)it->Unknowns(ii) : -1);
+    w.l("dof_vert", dv);
+    std::vector<double> lsv, lse;
+    DROPS_FOR_TRIANG_VERTEX(mg, 0, it) lsv.push_back(ls.Data[it->Unknowns(li)]);
+    w.d("ls_vert", lsv);
+    std::vector<int64_t> ev;
+    DROPS_FOR_TRIANG_EDGE(mg, 0, it) {
+        lse.push_back(ls.Data[it->Unknowns(li)]);
+        ev.push_back(F.vid[it->GetVertex(0)]);
+        ev.push_back(F.vid[it->GetVertex(1)]);
+    }
+    w.d("ls_edge", lse);
+    w.l("edge_v", ev);
+    const double alpha = 0.7, D = 1.3;
+    w.s("alpha", alpha);
+    w.s("D", D);
+    MatDescCL M(&ifIdx, &ifIdx), A(&ifIdx, &ifIdx);
+    SetupInterfaceMassP1(mg, &M, ls, lsbnd, alpha);
+    SetupLBP1(mg, &A, ls, lsbnd, D);
+    write_csr(w, "M", M.Data);
+    write_csr(w, "A", A.Data);
+    VecDescCL rhs(&ifIdx);
+    SetupInterfaceRhsP1(mg, &rhs, ls, lsbnd, legacy_f, 0.);
+    w.d("rhs", std::vector<double>(std::begin(rhs.Data), std::end(rhs.Data)));
+    return 0;
+}
+
 // tests/principallattice.cpp:316-347 (sphere r = 0.5 on [-1,1]^3, 8^3 cubes)
 int cmd_area(int argc, char** argv) {
     if (argc < 3) throw std::invalid_argument("usage: area out");
@@ -419,6 +479,7 @@ int main(int argc, char** argv) {
         std::string cmd = argv[1];
         if (cmd == "system") return cmd_system(argc, argv);
         if (cmd == "legacy_numb") return cmd_legacy_numb(argc, argv);
+        if (cmd == "legacy_forms") return cmd_legacy_forms(argc, argv);
         if (cmd == "area") return cmd_area(argc, argv);
         throw std::invalid_argument("unknown command " + cmd);
     } catch (std::exception& e) {
