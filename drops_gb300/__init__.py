@@ -41,7 +41,7 @@ KERNEL_NAMES = ["classify", "number", "assemble", "pattern", "scatter", "spmv", 
 EXPORTS = [
     "tf_create", "tf_destroy", "tf_last_error", "tf_status_string", "tf_stream", "tf_mesh_brick", "tf_mesh_upload",
     "tf_mesh_info", "tf_mesh_download", "tf_levelset_upload", "tf_levelset_analytic", "tf_levelset_download",
-    "tf_distribute_dofs", "tf_create_numb_on_interface_p1", "tf_dofs_download", "tf_patches_download", "tf_setup_fe_system",
+    "tf_distribute_dofs", "tf_create_numb_on_interface_p1", "tf_dofs_download", "tf_dofs_info", "tf_setup_interface_p1_legacy", "tf_patches_download", "tf_setup_fe_system",
     "tf_matrix_info", "tf_matrix_download", "tf_matrix_upload", "tf_lincomb", "tf_ch_block", "tf_vec_upload",
     "tf_vec_download", "tf_vec_size", "tf_vec_fill", "tf_spmv", "tf_pcg_jacobi", "tf_gmres_jacobi", "tf_pcg_jacobi_noalloc", "tf_ch_steps",
     "tf_mesh_brick_batch", "tf_levelset_analytic_batch", "tf_batch_info", "tf_batch_lincomb", "tf_batch_pcg_jacobi",
@@ -243,6 +243,9 @@ class TraceFEM:
     def dofs(self):
         nv, ne, nt = self.mesh_info()
         nl = 10 if self.fe == P2IF else 4
+        ntl = C.c_int64()
+        self._check(self.L.tf_dofs_info(self.h, C.byref(ntl), None, None))
+        self.n_active = ntl.value
         dv = np.empty(nv, np.int32)
         de = np.empty(ne, np.int32) if self.fe == P2IF else None
         act = np.empty(max(self.n_active, 1), np.int32)
@@ -270,6 +273,17 @@ class TraceFEM:
         nnz = C.c_int64()
         self._check(self.L.tf_setup_fe_system(self.h, C.c_uint(mask), C.c_int(rhs_kind), _dp(par),
                                               C.c_int(len(rhs_par)), C.byref(nnz)))
+        return nnz.value
+
+    def setup_interface_p1_legacy(self, alpha, D, fpar=None):
+        """SetupInterfaceMassP1 (alpha), SetupLBP1 (D) and, with fpar (10 coefficients of the quadratic
+        f), SetupInterfaceRhsP1 on the legacy P1 numbering; returns nnz."""
+        par = None if fpar is None else np.ascontiguousarray(fpar, dtype=np.float64)
+        if par is not None and par.size != 10:
+            raise ValueError("fpar holds the 10 coefficients of a quadratic")
+        nnz = C.c_int64()
+        self._check(self.L.tf_setup_interface_p1_legacy(self.h, C.c_double(alpha), C.c_double(D),
+                                                        None if par is None else _dp(par), C.byref(nnz)))
         return nnz.value
 
     def matrix(self, mat):

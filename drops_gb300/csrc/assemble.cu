@@ -35,6 +35,7 @@ struct Tables {
     int can_b[8][6];
     int ledge[8][6];        // lattice edge id 0..24
     int edge_a[25], edge_b[25];  // canonical endpoints of every lattice edge
+    int reg_child[8][4];         // regular children in P2-DoF numbering (ChildDataAr, geom/topo.cpp:333-341)
     signed char pat_nf[81]; // facets per sign pattern (-1: all-zero pattern)
     signed char pat_bnd[81];
     signed char pat_f[81][2][3];  // ext ids: 0..3 vertex, 4..9 edge + 4
@@ -105,6 +106,10 @@ static void build_tables(Tables& T) {
         T.edge_a[q] = seen_a[q];
         T.edge_b[q] = seen_b[q];
     }
+    static const int reg[8][4] = {{0, 4, 5, 7}, {4, 1, 6, 8}, {4, 5, 6, 8}, {4, 5, 7, 8},
+                                  {5, 6, 2, 9}, {5, 6, 8, 9}, {5, 7, 8, 9}, {7, 8, 9, 3}};
+    for (int c = 0; c < 8; ++c)
+        for (int k = 0; k < 4; ++k) T.reg_child[c][k] = reg[c][k];
     // sign-pattern facet table (SignTraitsCL<3>::compute_cuts + RefPatchBuilderCL<3>::assign)
     for (int p = 0; p < 81; ++p) {
         int sg[4], q = p, sum = 0;
@@ -675,14 +680,24 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
 // ---------------------------------------------------------------------------
 constexpr int kRowCap = 1024;  // contributions per row handled by one warp
 
-__global__ void k_row_counts(int64_t n_active, int nl, const int32_t* __restrict__ l2g, int32_t* __restrict__ cnt) {
+// Contributions of the active tets to every row.  Entries of unnumbered DOFs
+// (-1, legacy numbering) and tets with mask[r] == 0 are left out, as the
+// reference's MatrixBuilderCL only receives numbered pairs of visited tets.
+__global__ void k_row_counts(int64_t n_active, int nl, const int32_t* __restrict__ l2g, const uint8_t* __restrict__ mask,
+                             int32_t* __restrict__ cnt) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n_active * nl;
-         q += (int64_t)gridDim.x * blockDim.x)
-        atomicAdd(&cnt[l2g[q]], nl);
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = q / nl;
+        const int32_t row = l2g[q];
+        if (row < 0 || (mask && !mask[r])) continue;
+        int nc = 0;
+        for (int j = 0; j < nl; ++j) nc += l2g[r * nl + j] >= 0;
+        atomicAdd(&cnt[row], nc);
+    }
 }
 
-__global__ void k_bucket(int64_t n_active, int nl, const int32_t* __restrict__ l2g, const int32_t* __restrict__ start,
-                         int32_t* __restrict__ cursor, uint64_t* __restrict__ contrib) {
+__global__ void k_bucket(int64_t n_active, int nl, const int32_t* __restrict__ l2g, const uint8_t* __restrict__ mask,
+                         const int32_t* __restrict__ start, int32_t* __restrict__ cursor, uint64_t* __restrict__ contrib) {
     const int nl2 = nl * nl;
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n_active * nl2;
          c += (int64_t)gridDim.x * blockDim.x) {
@@ -690,6 +705,7 @@ __global__ void k_bucket(int64_t n_active, int nl, const int32_t* __restrict__ l
         const int ij = (int)(c - r * nl2);
         const int i = ij / nl, j = ij - (ij / nl) * nl;
         const int32_t row = l2g[r * nl + i], col = l2g[r * nl + j];
+        if (row < 0 || col < 0 || (mask && !mask[r])) continue;
         const int32_t pos = start[row] + atomicAdd(&cursor[row], 1);
         contrib[pos] = ((uint64_t)(uint32_t)col << 32) | (uint64_t)(uint32_t)c;
     }
@@ -799,6 +815,7 @@ __global__ void k_scatter_rhs(int64_t m, const int32_t* __restrict__ diag_slot, 
     for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < m; row += (int64_t)gridDim.x * blockDim.x) {
         const int32_t k = diag_slot[row];
         double a = 0.;
+        if (k >= 0)
         for (int32_t p = seg_start[k]; p < seg_start[k + 1]; ++p) {
             const uint32_t c = (uint32_t)contrib[p];
             const uint32_t r = c / (NL * NL);
@@ -809,7 +826,7 @@ __global__ void k_scatter_rhs(int64_t m, const int32_t* __restrict__ diag_slot, 
     }
 }
 
-static int build_pattern(Context* c) {
+static int build_pattern(Context* c, const uint8_t* mask = nullptr) {
     const int nl = c->fe == TF_P2IF ? 10 : 4;
     const int64_t na = c->n_active, m = c->n_dofs;
     const int64_t ncontrib = na * nl * nl;
@@ -817,7 +834,7 @@ static int build_pattern(Context* c) {
     TimedLaunch tl(c, TF_K_PATTERN);
     TF_TRY(ensure(c, c->row_cursor, (size_t)m + 1));
     TF_CUDA(c, cudaMemsetAsync(c->row_cursor.p, 0, sizeof(int32_t) * (size_t)(m + 1), c->stream));
-    k_row_counts<<<grid_for(c, na * nl), kBlock, 0, c->stream>>>(na, nl, c->loc2glo.p, c->row_cursor.p);
+    k_row_counts<<<grid_for(c, na * nl), kBlock, 0, c->stream>>>(na, nl, c->loc2glo.p, mask, c->row_cursor.p);
     ++c->launches;
     TF_TRY(ensure(c, c->rowptr, (size_t)m + 1));
     int64_t total = 0;
@@ -825,7 +842,7 @@ static int build_pattern(Context* c) {
     TF_TRY(exclusive_scan_i32_to_i32(c, c->row_cursor.p, c->rowptr.p, m, &total));
     TF_CUDA(c, cudaMemsetAsync(c->row_cursor.p, 0, sizeof(int32_t) * (size_t)(m + 1), c->stream));
     TF_TRY(ensure(c, c->contrib, (size_t)ncontrib + 1));
-    k_bucket<<<grid_for(c, ncontrib), kBlock, 0, c->stream>>>(na, nl, c->loc2glo.p, c->rowptr.p, c->row_cursor.p,
+    k_bucket<<<grid_for(c, ncontrib), kBlock, 0, c->stream>>>(na, nl, c->loc2glo.p, mask, c->rowptr.p, c->row_cursor.p,
                                                               c->contrib.p);
     ++c->launches;
     TF_CUDA(c, cudaMemsetAsync(c->status.p, 0, 4 * sizeof(int), c->stream));
@@ -847,10 +864,11 @@ static int build_pattern(Context* c) {
     TF_TRY(ensure(c, c->colind, (size_t)(nnz > 0 ? nnz : 1)));
     TF_TRY(ensure(c, c->seg_start, (size_t)nnz + 1));
     TF_TRY(ensure(c, c->diag_slot, (size_t)(m > 0 ? m : 1)));
+    TF_CUDA(c, cudaMemsetAsync(c->diag_slot.p, 0xff, sizeof(int32_t) * (size_t)(m > 0 ? m : 1), c->stream));
     k_row_emit<<<grid_for(c, m, 128, 16), 128, 0, c->stream>>>(m, bstart.p, c->contrib.p, c->rowptr.p, c->colind.p,
                                                                  c->seg_start.p, c->diag_slot.p);
     ++c->launches;
-    int32_t tot32 = (int32_t)ncontrib;
+    int32_t tot32 = (int32_t)total;  // contributions actually bucketed
     TF_CUDA(c, cudaMemcpyAsync(c->seg_start.p + nnz, &tot32, sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
     TF_CUDA(c, cudaStreamSynchronize(c->stream));
     release(bstart);
@@ -865,7 +883,7 @@ static int build_pattern(Context* c) {
         A.pattern_gen = gen;
         ++A.version;
     }
-    c->pattern_dof_version = c->dof_version;
+    c->pattern_dof_version = mask ? -1 : c->dof_version;  // a masked pattern is not the DistributeDOFs one
     return TF_OK;
 }
 
@@ -948,6 +966,327 @@ int setup_fe_system(Context* c, unsigned forms, int rhs_kind, const double* rhs_
         TF_CUDA(c, cudaGetLastError());
     }
     TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// legacy P1 interface forms of the surfactant.cpp path
+// ---------------------------------------------------------------------------
+// InterfacePatchCL::Sign (num/interfacePatch.h:75): |phi| < 2 eps counts as 0
+__device__ inline int legacy_sign(double phi) {
+    return fabs(phi) < 4.440892098500626e-16 ? 0 : (phi > 0. ? 1 : -1);
+}
+
+__device__ inline double rhs_quadratic(const double* p, const double x[3]) {
+    return ((p[0] + p[1] * x[0] + p[2] * x[1] + p[3] * x[2]) + (p[4] * x[0] * x[0] + p[5] * x[1] * x[1] + p[6] * x[2] * x[2])) +
+           (p[7] * x[0] * x[1] + p[8] * x[0] * x[2] + p[9] * x[1] * x[2]);
+}
+
+// Planar pieces of regular child ch: InterfacePatchCL::ComputeVerticesOfCut
+// (num/interfacePatch.cpp:137-199) with linear edge roots, then
+// InterfaceTriangleCL::ComputeForChild (:478-512): triangle (P,Q,R) with
+// |det|, for four points also (Q,R,S) with |det| (a + b - 1) from the least-
+// squares fit S - P = a (Q - P) + b (R - P); halved when the patch is a face
+// shared by two children.  Returns the triangle count, -1 for a 3-D zero set.
+__device__ int legacy_child_triangles(const double X[4][3], const double ls10[10], int ch, double tri[2][3][4],
+                                      double det[2]) {
+    const int* cv = cT.reg_child[ch];
+    int ns[3] = {0, 0, 0}, sg[4];
+    for (int k = 0; k < 4; ++k) {
+        sg[k] = legacy_sign(ls10[cv[k]]);
+        ++ns[sg[k] + 1];
+    }
+    if (ns[0] * ns[2] == 0 && ns[1] < 3) return 0;
+    if (ns[1] == 4) return -1;
+    auto bdof = [&](int v, double b[4]) {
+        for (int c = 0; c < 4; ++c) b[c] = 0.;
+        if (v < 4) b[v] = 1.;
+        else { b[ev0(v - 4)] = 0.5; b[ev1(v - 4)] = 0.5; }
+    };
+    auto cdof = [&](int v, double x[3]) {
+        if (v < 4) for (int c = 0; c < 3; ++c) x[c] = X[v][c];
+        else for (int c = 0; c < 3; ++c) x[c] = 0.5 * (X[ev0(v - 4)][c] + X[ev1(v - 4)][c]);
+    };
+    double bary[4][4], pqrs[4][3];
+    int np = 0;
+    for (int k = 0; k < 4; ++k)
+        if (sg[k] == 0) {
+            bdof(cv[k], bary[np]);
+            cdof(cv[k], pqrs[np]);
+            ++np;
+        }
+    for (int e = 0; e < 6; ++e) {
+        const int k0 = ev0(e), k1 = ev1(e);
+        if (sg[k0] * sg[k1] < 0) {
+            const int v0 = cv[k0], v1 = cv[k1];
+            const double lam = ls10[v0] / (ls10[v0] - ls10[v1]);
+            double b0[4], b1[4], x0[3], x1[3];
+            bdof(v0, b0);
+            bdof(v1, b1);
+            cdof(v0, x0);
+            cdof(v1, x1);
+            for (int c = 0; c < 4; ++c) bary[np][c] = (1. - lam) * b0[c] + lam * b1[c];
+            for (int c = 0; c < 3; ++c) pqrs[np][c] = (1. - lam) * x0[c] + lam * x1[c];
+            ++np;
+        }
+    }
+    for (int f = 0; f < 4; ++f) {  // cut lying on a face of the parent
+        int on = 0;
+        for (int i = 0; i < np; ++i) on += bary[i][f] < 1e-9;
+        if (on == np) return 0;
+    }
+    if (np < 3) return 0;
+    double u[3], v[3];
+    for (int c = 0; c < 3; ++c) {
+        u[c] = pqrs[1][c] - pqrs[0][c];
+        v[c] = pqrs[2][c] - pqrs[0][c];
+    }
+    const double c0 = u[1] * v[2] - u[2] * v[1], c1 = u[2] * v[0] - u[0] * v[2], c2 = u[0] * v[1] - u[1] * v[0];
+    double d = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+    if (ns[1] >= 3) d /= 2.;
+    for (int j = 0; j < 3; ++j)
+        for (int c = 0; c < 4; ++c) tri[0][j][c] = bary[j][c];
+    det[0] = d;
+    if (np < 4) return 1;
+    double w[3];
+    for (int c = 0; c < 3; ++c) w[c] = pqrs[3][c] - pqrs[0][c];
+    const double uu = u[0] * u[0] + u[1] * u[1] + u[2] * u[2], uv = u[0] * v[0] + u[1] * v[1] + u[2] * v[2];
+    const double vv = v[0] * v[0] + v[1] * v[1] + v[2] * v[2], uw = u[0] * w[0] + u[1] * w[1] + u[2] * w[2];
+    const double vw = v[0] * w[0] + v[1] * w[1] + v[2] * w[2];
+    const double dd = uu * vv - uv * uv;
+    const double aa = (uw * vv - vw * uv) / dd, bb = (vw * uu - uw * uv) / dd;
+    for (int j = 0; j < 3; ++j)
+        for (int c = 0; c < 4; ++c) tri[1][j][c] = bary[j + 1][c];
+    det[1] = d * (aa + bb - 1.);
+    return 2;
+}
+
+struct LegacySmem {
+    TetGeom g;
+    double gM[9], gC[9];
+    double ls10[10];
+    PatchSmem P;
+};
+
+struct LegacyArgs {
+    MeshView M;
+    const double* lsv;
+    const double* lse;
+    int64_t n;               // tets in the list
+    const int32_t* tets;
+    double alpha, D;
+    int want_rhs;
+    double fp[10];
+    double* elem;            // [form][n][10]
+    double* elem_rhs;        // [n][4]
+    uint8_t* nonempty;       // [n]
+    int* status;
+};
+
+// warp per tet: LocalInterfaceMassP1CL (Quad2_2D composite rule on the
+// lattice-2 patch; diagonal unscaled, off-diagonal x alpha,
+// surfactant/ifacetransp.h:881-906), LocalLaplaceBeltramiP1CL (facet
+// normals, D/2 sum |det_f| without halving on lattice faces, :1657-1695) on
+// one lane per facet, and the SetupInterfaceRhsP1 contributions
+// (surfactant/ifacetransp.cpp:515-563) on one lane per regular child;
+// lane sums combined by a fixed shuffle tree.
+__global__ void __launch_bounds__(32 * kAsmWarps) k_assemble_legacy(LegacyArgs A) {
+    __shared__ LegacySmem smem[kAsmWarps];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    LegacySmem& S = smem[wib];
+    const int64_t nwarps = (int64_t)gridDim.x * kAsmWarps;
+    for (int64_t r = (int64_t)blockIdx.x * kAsmWarps + wib; r < A.n; r += nwarps) {
+        const int32_t t = A.tets[r];
+        int32_t v[4], e[6];
+        mesh_tet(A.M, t, v, e);
+        if (lane < 4) {
+            double x[3];
+            mesh_coord(A.M, v[lane], x);
+            for (int c = 0; c < 3; ++c) S.g.X[lane][c] = x[c];
+            S.ls10[lane] = A.lsv[v[lane]];
+        } else if (lane < 10) {
+            S.ls10[lane] = A.lse[e[lane - 4]];
+        }
+        __syncwarp();
+        warp_tet_geometry(S.g, S.ls10, S.gM, S.gC, lane);
+        double ls10[10];
+        for (int k = 0; k < 10; ++k) ls10[k] = S.ls10[k];
+        const int nf = warp_patch(ls10, S.g.X, S.P, lane, A.status, t);
+        double mq[10], lq[10], rq[4];
+        for (int k = 0; k < 10; ++k) mq[k] = lq[k] = 0.;
+        for (int k = 0; k < 4; ++k) rq[k] = 0.;
+        if (lane < nf) {
+            double w[3][3];
+            for (int j = 0; j < 3; ++j)
+                for (int c = 0; c < 3; ++c)
+                    w[j][c] = S.g.X[0][c] * S.P.fb[lane][j][0] + S.g.X[1][c] * S.P.fb[lane][j][1] +
+                              S.g.X[2][c] * S.P.fb[lane][j][2] + S.g.X[3][c] * S.P.fb[lane][j][3];
+            double u[3], vv[3];
+            for (int c = 0; c < 3; ++c) {
+                u[c] = w[1][c] - w[0][c];
+                vv[c] = w[2][c] - w[0][c];
+            }
+            const double cr[3] = {u[1] * vv[2] - u[2] * vv[1], u[2] * vv[0] - u[0] * vv[2], u[0] * vv[1] - u[1] * vv[0]};
+            const double ad = sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+            const double wq = ad * (S.P.bnd[lane] ? 0.5 : 1.);
+            for (int q = 0; q < 4; ++q) {
+                double b[4];
+                for (int c = 0; c < 4; ++c)
+                    b[c] = S.P.fb[lane][0][c] * cT.qq2_node[q][0] + S.P.fb[lane][1][c] * cT.qq2_node[q][1] +
+                           S.P.fb[lane][2][c] * cT.qq2_node[q][2];
+                const double wt = wq * cT.qq2_w[q];
+                for (int k = 0; k < 10; ++k) mq[k] += wt * (b[cT.sym4_i[k]] * b[cT.sym4_j[k]]);
+            }
+            if (ad > 0.) {
+                const double n[3] = {cr[0] / ad, cr[1] / ad, cr[2] / ad};
+                double pq[4][3];
+                for (int i = 0; i < 4; ++i) {
+                    const double gn = S.g.gl[i][0] * n[0] + S.g.gl[i][1] * n[1] + S.g.gl[i][2] * n[2];
+                    for (int c = 0; c < 3; ++c) pq[i][c] = S.g.gl[i][c] - gn * n[c];
+                }
+                for (int k = 0; k < 10; ++k) {
+                    const int i = cT.sym4_i[k], j = cT.sym4_j[k];
+                    lq[k] += (pq[i][0] * pq[j][0] + pq[i][1] * pq[j][1] + pq[i][2] * pq[j][2]) * ad;
+                }
+            }
+        }
+        if (A.want_rhs && lane < 8) {
+            const int s0 = legacy_sign(ls10[0]);
+            bool inter = false;
+            for (int k = 1; k < 10; ++k) inter |= legacy_sign(ls10[k]) != s0;
+            if (inter) {
+                double tri[2][3][4], det[2];
+                const int ntr = legacy_child_triangles(S.g.X, ls10, lane, tri, det);
+                if (ntr < 0) set_status(A.status, TF_ERR_ZERO_PATTERN, t);
+                for (int tt = 0; tt < ntr; ++tt)
+                    for (int q = 0; q < 7; ++q) {
+                        double b[4], x[3];
+                        for (int c = 0; c < 4; ++c)
+                            b[c] = tri[tt][0][c] * cT.q2_node[q][0] + tri[tt][1][c] * cT.q2_node[q][1] +
+                                   tri[tt][2][c] * cT.q2_node[q][2];
+                        for (int c = 0; c < 3; ++c)
+                            x[c] = S.g.X[0][c] * b[0] + S.g.X[1][c] * b[1] + S.g.X[2][c] * b[2] + S.g.X[3][c] * b[3];
+                        const double fx = rhs_quadratic(A.fp, x);
+                        for (int i = 0; i < 4; ++i) rq[i] += (det[tt] * cT.q2_w[q]) * (fx * b[i]);
+                    }
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            for (int k = 0; k < 10; ++k) {
+                mq[k] += __shfl_xor_sync(0xffffffffu, mq[k], o);
+                lq[k] += __shfl_xor_sync(0xffffffffu, lq[k], o);
+            }
+            for (int k = 0; k < 4; ++k) rq[k] += __shfl_xor_sync(0xffffffffu, rq[k], o);
+        }
+        if (lane < 10) {
+            const int k = lane;
+            const bool diag = cT.sym4_i[k] == cT.sym4_j[k];
+            double mv = 0., lv = 0.;
+            for (int kk = 0; kk < 10; ++kk)
+                if (kk == k) {
+                    mv = mq[kk];
+                    lv = lq[kk];
+                }
+            A.elem[((int64_t)TF_FORM_M * A.n + r) * 10 + k] = diag ? mv : A.alpha * mv;
+            A.elem[((int64_t)TF_FORM_A * A.n + r) * 10 + k] = (A.D * 0.5) * lv;
+        }
+        if (lane < 4) {
+            double rv = 0.;
+            for (int i = 0; i < 4; ++i)
+                if (i == lane) rv = rq[i];
+            A.elem_rhs[r * 4 + lane] = rv;
+        }
+        if (lane == 0) {
+            A.nonempty[r] = nf > 0;
+            // a rhs piece on a tet whose patch is empty (values within 2 eps
+            // of zero) has no slot in the pattern: counted for a fix-up pass
+            if (nf == 0 && (rq[0] != 0. || rq[1] != 0. || rq[2] != 0. || rq[3] != 0.)) atomicAdd(A.status + 2, 1);
+        }
+        __syncwarp();
+    }
+}
+
+// rhs pieces of tets outside the masked pattern, added in tet order by one
+// thread (runs only when the assembly counted such tets)
+__global__ void k_legacy_rhs_stray(int64_t n, const uint8_t* __restrict__ nonempty, const int32_t* __restrict__ l2g,
+                                   const double* __restrict__ elem_rhs, double* __restrict__ rhs) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (int64_t r = 0; r < n; ++r) {
+        if (nonempty[r]) continue;
+        for (int i = 0; i < 4; ++i) {
+            const int32_t d = l2g[4 * r + i];
+            if (d >= 0) rhs[d] += elem_rhs[4 * r + i];
+        }
+    }
+}
+
+int setup_legacy_p1(Context* c, double alpha, double D, const double* fpar, int64_t* nnz_out) {
+    if (c->fe != TF_P1IF) return set_err(c, TF_ERR_BAD_INPUT, "legacy forms: a P1 interface numbering is required");
+    TF_TRY(ensure_tables(c));
+    const int64_t na = c->n_active, m = c->n_dofs;
+    TF_TRY(ensure(c, c->elem, (size_t)TF_NUM_FORMS * (size_t)(na > 0 ? na : 1) * 10));
+    TF_TRY(ensure(c, c->elem_rhs, (size_t)(na > 0 ? na : 1) * 4));
+    TF_TRY(ensure(c, c->legacy_mask, (size_t)(na > 0 ? na : 1)));
+    LegacyArgs A{};
+    A.M = c->mesh;
+    A.lsv = c->ls_vert.p;
+    A.lse = c->ls_edge.p;
+    A.n = na;
+    A.tets = c->active.p;
+    A.alpha = alpha;
+    A.D = D;
+    A.want_rhs = fpar != nullptr;
+    for (int i = 0; i < 10; ++i) A.fp[i] = fpar ? fpar[i] : 0.;
+    A.elem = c->elem.p;
+    A.elem_rhs = c->elem_rhs.p;
+    A.nonempty = c->legacy_mask.p;
+    A.status = c->status.p;
+    TF_CUDA(c, cudaMemsetAsync(c->status.p, 0, 4 * sizeof(int), c->stream));
+    if (na > 0) {
+        TimedLaunch tl(c, TF_K_ASSEMBLE);
+        k_assemble_legacy<<<grid_for(c, (na + kAsmWarps - 1) / kAsmWarps, 1, 8), 32 * kAsmWarps, 0, c->stream>>>(A);
+        ++c->launches;
+        TF_CUDA(c, cudaGetLastError());
+    }
+    int st = 0;
+    TF_TRY(sync_status(c, &st));
+    if (st == TF_ERR_ZERO_PATTERN)
+        return set_err(c, st, "legacy forms: zero level set of positive volume on a lattice sub-tet or child");
+    if (st) return set_err(c, st, "legacy forms failed");
+    const int stray = c->h_status[2];
+    TF_TRY(build_pattern(c, c->legacy_mask.p));
+    const int64_t nnz = c->mats[0].nnz;
+    double* v[4] = {nullptr, nullptr, nullptr, nullptr};
+    for (int f : {TF_FORM_M, TF_FORM_A}) {
+        TF_TRY(ensure(c, c->mat_vals[f], (size_t)(nnz > 0 ? nnz : 1)));
+        c->mats[f].vals = c->mat_vals[f].p;
+        ++c->mats[f].version;
+        v[f] = c->mats[f].vals;
+    }
+    for (int f : {TF_FORM_CN, TF_FORM_LAPM}) c->mats[f].vals = nullptr;  // not part of this pattern
+    if (nnz > 0) {
+        TimedLaunch tl(c, TF_K_SCATTER);
+        const unsigned forms = (1u << TF_FORM_M) | (1u << TF_FORM_A);
+        k_scatter<4><<<grid_for(c, nnz), kBlock, 0, c->stream>>>(nnz, c->seg_start.p, c->contrib.p, na, c->elem.p, forms,
+                                                                  v[0], v[1], v[2], v[3]);
+        ++c->launches;
+    }
+    if (fpar) {
+        TF_TRY(ensure(c, c->vecs[TF_VEC_RHS], (size_t)m));
+        if (m > 0) {
+            k_scatter_rhs<4><<<grid_for(c, m), kBlock, 0, c->stream>>>(m, c->diag_slot.p, c->seg_start.p, c->contrib.p,
+                                                                        c->elem_rhs.p, c->vecs[TF_VEC_RHS].p);
+            ++c->launches;
+        }
+        if (stray > 0) {
+            k_legacy_rhs_stray<<<1, 32, 0, c->stream>>>(na, c->legacy_mask.p, c->loc2glo.p, c->elem_rhs.p,
+                                                        c->vecs[TF_VEC_RHS].p);
+            ++c->launches;
+        }
+    }
+    TF_CUDA(c, cudaGetLastError());
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (nnz_out) *nnz_out = nnz;
     return TF_OK;
 }
 
@@ -1170,6 +1509,16 @@ __global__ void k_legacy_active(MeshView M, int64_t n_cand, const int32_t* __res
 
 int compact_active(Context* c, int64_t* n_active);
 
+// local-to-global map of the cut tets under the legacy numbering (-1: vertex not numbered)
+__global__ void k_legacy_l2g(MeshView M, int64_t n, const int32_t* __restrict__ tets,
+                             const int32_t* __restrict__ dof_vert, int32_t* __restrict__ l2g) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        int32_t v[4];
+        mesh_tet(M, tets[r], v, nullptr);
+        for (int i = 0; i < 4; ++i) l2g[4 * r + i] = dof_vert[v[i]];
+    }
+}
+
 int numb_on_interface_p1(Context* c, double omit_bound) {
     if (!c->has_mesh || !c->has_ls) return set_err(c, TF_ERR_BAD_INPUT, "numbering: mesh and level set required");
     TF_TRY(ensure_tables(c));
@@ -1224,13 +1573,22 @@ int numb_on_interface_p1(Context* c, double omit_bound) {
     }
     int64_t na = 0;
     TF_TRY(exclusive_scan_i32_to_i32(c, flag.p, rank.p, n_cand, &na));
+    // The internal active list stays the cut tets (the tets the reference's
+    // interface accumulators visit); its local-to-global map has -1 for
+    // unnumbered vertices.  The reported count is the reference's.
+    TF_TRY(ensure(c, c->loc2glo, (size_t)(n_cand > 0 ? 4 * n_cand : 1) + 1));
+    if (n_cand > 0) {
+        k_legacy_l2g<<<grid_for(c, n_cand), kBlock, 0, c->stream>>>(M, n_cand, c->active.p, c->dof_vert.p, c->loc2glo.p);
+        ++c->launches;
+    }
     TF_CUDA(c, cudaStreamSynchronize(c->stream));
     TF_CUDA(c, cudaGetLastError());
     release(cand);
     release(nonempty);
     release(rank);
     release(flag);
-    c->n_active = na;
+    c->n_active = n_cand;
+    c->legacy_n_active = na;
     c->n_dofs = ndofs;
     c->fe = TF_P1IF;
     c->legacy_numbering = true;

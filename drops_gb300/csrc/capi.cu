@@ -311,8 +311,18 @@ int tf_create_numb_on_interface_p1(tf_context* t, double omit_bound, int64_t* n_
     Context* c = &t->c;
     cudaSetDevice(c->device);
     TF_TRY(tf::numb_on_interface_p1(c, omit_bound));
-    if (n_active) *n_active = c->n_active;
+    if (n_active) *n_active = c->legacy_n_active;
     if (n_dofs) *n_dofs = c->n_dofs;
+    return TF_OK;
+}
+
+int tf_dofs_info(tf_context* t, int64_t* n_tets, int64_t* n_dofs, int* fe) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    if (!c->fe) return tf::set_err(c, TF_ERR_BAD_INPUT, "no DOF numbering");
+    if (n_tets) *n_tets = c->n_active;
+    if (n_dofs) *n_dofs = c->n_dofs;
+    if (fe) *fe = c->fe;
     return TF_OK;
 }
 
@@ -349,6 +359,14 @@ int tf_setup_fe_system(tf_context* t, unsigned forms, int rhs_kind, const double
     TF_TRY(tf::setup_fe_system(c, forms, rhs_kind, rhs_par, npar));
     if (nnz) *nnz = c->mats[0].nnz;
     return TF_OK;
+}
+
+int tf_setup_interface_p1_legacy(tf_context* t, double alpha, double D, const double* fpar, int64_t* nnz) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (!c->legacy_numbering) return tf::set_err(c, TF_ERR_BAD_INPUT, "legacy forms: tf_create_numb_on_interface_p1 first");
+    return tf::setup_legacy_p1(c, alpha, D, fpar, nnz);
 }
 
 int tf_matrix_info(tf_context* t, int mat, int64_t* rows, int64_t* nnz) {

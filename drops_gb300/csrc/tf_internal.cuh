@@ -225,6 +225,7 @@ struct Context {
     int64_t n_active = 0, n_dofs = 0;
     int64_t dof_version = 0;
     bool legacy_numbering = false;
+    int64_t legacy_n_active = 0;  // active tets as CreateNumbOnInterfaceVertex counts them
     DBuf<int32_t> dof_vert, dof_edge, active, loc2glo;
     DBuf<uint8_t> flags;
     DBuf<int32_t> keys_v, keys_e, owner;
@@ -234,6 +235,7 @@ struct Context {
     DBuf<uint64_t> contrib;  // sorted (col << 32 | contribution) per row
     DBuf<double> elem;       // packed element matrices [form][tet][nsym]
     DBuf<double> elem_rhs;   // [tet][nl]
+    DBuf<uint8_t> legacy_mask;  // legacy forms: tet has a non-empty patch
     CSR mats[TF_NUM_MATS];
     DBuf<double> mat_vals[TF_NUM_MATS];
     DBuf<int32_t> block_rowptr, block_colind, user_rowptr, user_colind;
@@ -386,6 +388,7 @@ int levelset_p1_edges(Context* c);
 int distribute_dofs(Context* c, int fe, double dist);
 int numb_on_interface_p1(Context* c, double omit_bound);
 int setup_fe_system(Context* c, unsigned forms, int rhs_kind, const double* rhs_par, int npar);
+int setup_legacy_p1(Context* c, double alpha, double D, const double* fpar, int64_t* nnz);
 int lincomb(Context* c, int nterms, const int* forms, const double* coeffs);
 int ch_block(Context* c, double alpha, double mob, double rho, double eps2, double beta, int use_lapm);
 int spmv(Context* c, const CSR& A, const double* x, double* y);

@@ -137,6 +137,24 @@ int tf_create_numb_on_interface_p1(tf_context* ctx, double omit_bound, int64_t* 
  * (IdxDescCL::Loc2Glo per active tet); any pointer may be NULL.                 */
 int tf_dofs_download(tf_context* ctx, int32_t* dof_vert, int32_t* dof_edge, int32_t* active_tets,
                      int32_t* loc2glo);
+/* Length of the tet list tf_dofs_download returns (active tets; for the
+ * legacy numbering every cut tet, which the legacy accumulators visit), the
+ * number of DOFs and the FE type.                                             */
+int tf_dofs_info(tf_context* ctx, int64_t* n_tets, int64_t* n_dofs, int* fe);
+/* The legacy P1 surfactant system on the numbering of
+ * tf_create_numb_on_interface_p1: SetupInterfaceMassP1 with
+ * LocalInterfaceMassP1CL (surfactant/ifacetransp.h:881-906: Quad2_2D on the
+ * lattice-2 patch, off-diagonal entries times alpha) into TF_MAT_M,
+ * SetupLBP1 with LocalLaplaceBeltramiP1CL (:1657-1695: facet-normal tangential
+ * gradients times D) into TF_MAT_A, and, when fpar != NULL,
+ * SetupInterfaceRhsP1 (surfactant/ifacetransp.cpp:515-563: Quad5_2D on the
+ * planar pieces of the 8 regular children) into TF_VEC_RHS with
+ * f(x) = fpar[0] + fpar[1..3].x + fpar[4] x^2 + fpar[5] y^2 + fpar[6] z^2
+ *        + fpar[7] xy + fpar[8] xz + fpar[9] yz.
+ * The pattern holds the numbered pairs of every cut tet with a non-empty
+ * patch (MatrixBuilderCL keeps explicit zeros).  TF_MAT_C / TF_MAT_LAPM are
+ * left empty.  Returns TF_ERR_ZERO_PATTERN where the reference throws.       */
+int tf_setup_interface_p1_legacy(tf_context* ctx, double alpha, double D, const double* fpar, int64_t* nnz);
 
 /* Surface patches of the tets tets[0..count) (tet ids, host array) exactly as
  * SPatchCL<3>::make_patch<MergeCutPolicyCL> builds them from the level set

@@ -232,6 +232,32 @@ def ch_block(rowptr, colind, M, A, Cn, alpha, mob, rho, eps2, beta):
     return brp, bci, bv
 
 
+def assemble_legacy_p1(mesh, ls_vert, ls_edge, dof_vert, m, alpha, D, fpar):
+    """SetupInterfaceMassP1 / SetupLBP1 / SetupInterfaceRhsP1: (status, rowptr, colind, M, A, rhs)."""
+    L = lib()
+    rowptr = np.empty(m + 1, np.int64)
+    colind_p = C.POINTER(C.c_int32)()
+    m_p, a_p = C.POINTER(C.c_double)(), C.POINTER(C.c_double)()
+    nnz = C.c_int64()
+    rhs = np.empty(m, np.float64)
+    fpar = np.ascontiguousarray(fpar, dtype=np.float64)
+    dof_vert = np.ascontiguousarray(dof_vert, dtype=np.int32)
+    st = L.orc_assemble_legacy_p1(C.c_int64(mesh.nt), _p(mesh.tet_v, C.c_int32), _p(mesh.tet_e, C.c_int32),
+                                  _p(mesh.coords, C.c_double), _p(ls_vert, C.c_double), _p(ls_edge, C.c_double),
+                                  _p(dof_vert, C.c_int32), C.c_int64(m), C.c_double(alpha), C.c_double(D),
+                                  _p(fpar, C.c_double), _p(rowptr, C.c_int64), C.byref(colind_p), C.byref(nnz),
+                                  C.byref(m_p), C.byref(a_p), _p(rhs, C.c_double))
+    if st != OK:
+        return st, None, None, None, None, None
+    libc = C.CDLL(None)
+    n = nnz.value
+    take = lambda p, ct: np.ctypeslib.as_array(p, shape=(max(n, 1),))[:n].copy()
+    colind, Mv, Av = take(colind_p, C.c_int32), take(m_p, C.c_double), take(a_p, C.c_double)
+    for p in (colind_p, m_p, a_p):
+        libc.free(p)
+    return st, rowptr, colind, Mv, Av, rhs
+
+
 def set_threads(n):
     lib().orc_set_threads(C.c_int(n))
 

@@ -712,6 +712,275 @@ int orc_numb_on_interface_p1(int64_t nt, const int32_t* tet_v, const int32_t* te
 }
 
 /* ======================================================================= */
+/* legacy P1 interface forms (surfactant.cpp path)                           */
+/* ======================================================================= */
+/* Children of the regular refinement in P2-DoF numbering (ChildDataAr,
+ * geom/topo.cpp:333-341): vertices 0..3, edge midpoints 4 + edge.           */
+static const int REG_CHILD[8][4] = {{0, 4, 5, 7}, {4, 1, 6, 8}, {4, 5, 6, 8}, {4, 5, 7, 8},
+                                    {5, 6, 2, 9}, {5, 6, 8, 9}, {5, 7, 8, 9}, {7, 8, 9, 3}};
+
+/* InterfacePatchCL::Sign (num/interfacePatch.h:75): |phi| < 2 eps counts as 0 */
+static int legacy_sign(double phi) {
+    const double approx_zero = 2. * 2.220446049250313e-16;
+    return fabs(phi) < approx_zero ? 0 : (phi > 0 ? 1 : -1);
+}
+
+double orc_rhs_quadratic(const double* p, const double x[3]) {
+    return ((p[0] + p[1] * x[0] + p[2] * x[1] + p[3] * x[2]) + (p[4] * x[0] * x[0] + p[5] * x[1] * x[1] + p[6] * x[2] * x[2])) +
+           (p[7] * x[0] * x[1] + p[8] * x[0] * x[2] + p[9] * x[1] * x[2]);
+}
+
+/* Planar pieces of one regular child (InterfacePatchCL::ComputeVerticesOfCut,
+ * num/interfacePatch.cpp:137-199, InterfaceTriangleCL::ComputeForChild,
+ * :478-512): up to two triangles, barycentric in the parent, with |det|.
+ * Returns the triangle count, -1 for a 3-dimensional zero level.           */
+int orc_legacy_child_triangles(const double xv[4][3], const double ls10[10], int ch, double tri[2][3][4],
+                               double det[2]) {
+    double bdof[10][4], cdof[10][3];
+    int sgn10[10];
+    for (int v = 0; v < 10; ++v) {
+        for (int c = 0; c < 4; ++c) bdof[v][c] = 0.;
+        if (v < 4) {
+            bdof[v][v] = 1.;
+            for (int c = 0; c < 3; ++c) cdof[v][c] = xv[v][c];
+        } else {
+            const int a = EV[v - 4][0], b = EV[v - 4][1];
+            bdof[v][a] = 0.5;
+            bdof[v][b] = 0.5;
+            for (int c = 0; c < 3; ++c) cdof[v][c] = 0.5 * (xv[a][c] + xv[b][c]);
+        }
+        sgn10[v] = legacy_sign(ls10[v]);
+    }
+    const int* cv = REG_CHILD[ch];
+    int ns[3] = {0, 0, 0};
+    for (int k = 0; k < 4; ++k) ++ns[sgn10[cv[k]] + 1];
+    if (ns[0] * ns[2] == 0 && ns[1] < 3) return 0;
+    if (ns[1] == 4) return -1;
+    double bary[4][4], pqrs[4][3];
+    int np = 0;
+    for (int k = 0; k < 4; ++k) {
+        const int v = cv[k];
+        if (sgn10[v] == 0) {
+            memcpy(bary[np], bdof[v], sizeof bary[np]);
+            memcpy(pqrs[np], cdof[v], sizeof pqrs[np]);
+            ++np;
+        }
+    }
+    for (int e = 0; e < 6; ++e) {
+        const int v0 = cv[EV[e][0]], v1 = cv[EV[e][1]];
+        if (sgn10[v0] * sgn10[v1] < 0) {
+            const double lam = ls10[v0] / (ls10[v0] - ls10[v1]);
+            for (int c = 0; c < 4; ++c) bary[np][c] = (1. - lam) * bdof[v0][c] + lam * bdof[v1][c];
+            for (int c = 0; c < 3; ++c) pqrs[np][c] = (1. - lam) * cdof[v0][c] + lam * cdof[v1][c];
+            ++np;
+        }
+    }
+    for (int f = 0; f < 4; ++f) {  /* cut lying on a face of the parent */
+        int on = 0;
+        for (int i = 0; i < np; ++i) on += bary[i][f] < 1e-9;
+        if (on == np) return 0;
+    }
+    if (np < 3) return 0;
+    double u[3], v[3], cr[3];
+    for (int c = 0; c < 3; ++c) {
+        u[c] = pqrs[1][c] - pqrs[0][c];
+        v[c] = pqrs[2][c] - pqrs[0][c];
+    }
+    cr[0] = u[1] * v[2] - u[2] * v[1];
+    cr[1] = u[2] * v[0] - u[0] * v[2];
+    cr[2] = u[0] * v[1] - u[1] * v[0];
+    double d = norm3(cr);
+    if (ns[1] >= 3) d /= 2.; /* EqualToFace: the patch is shared by two children */
+    for (int j = 0; j < 3; ++j) memcpy(tri[0][j], bary[j], sizeof tri[0][j]);
+    det[0] = d;
+    if (np < 4) return 1;
+    /* |(Q-P) a + (R-P) b - (S-P)| -> min (normal equations) */
+    double w[3];
+    for (int c = 0; c < 3; ++c) w[c] = pqrs[3][c] - pqrs[0][c];
+    const double uu = dot3(u, u), uv = dot3(u, v), vv = dot3(v, v), uw = dot3(u, w), vw = dot3(v, w);
+    const double dd = uu * vv - uv * uv;
+    const double aa = (uw * vv - vw * uv) / dd, bb = (vw * uu - uw * uv) / dd;
+    for (int j = 0; j < 3; ++j) memcpy(tri[1][j], bary[j + 1], sizeof tri[1][j]);
+    det[1] = d * (aa + bb - 1.);
+    return 2;
+}
+
+int orc_legacy_local(const double xv[4][3], const double ls10[10], double alpha, double D, const double* fpar,
+                     double mass[16], double lb[16], double rhs[4], int* nonempty) {
+    init_quad();
+    static const double Q2N[4][3] = {{1., 0., 0.}, {0., 1., 0.}, {0., 0., 1.}, {1. / 3., 1. / 3., 1. / 3.}};
+    static const double Q2W[4] = {1. / 24., 1. / 24., 1. / 24., 0.375};
+    for (int k = 0; k < 16; ++k) mass[k] = lb[k] = 0.;
+    for (int k = 0; k < 4; ++k) rhs[k] = 0.;
+    *nonempty = 0;
+    /* matrices on the lattice-2 patch (InterfaceCommonDataP1CL::visit, ifacetransp.h:142-149) */
+    orc_patch_t P;
+    int st = orc_make_patch(ls10, &P);
+    if (st) return st;
+    double T[3][3], dett, gl[4][3];
+    trafo(xv, T, &dett);
+    bary_grads(T, gl);
+    if (P.n_facets > 0) {
+        *nonempty = 1;
+        double qs[4][4] = {{0}};
+        for (int f = 0; f < P.n_facets; ++f) {
+            double wv[3][3];
+            for (int j = 0; j < 3; ++j) {
+                const double* b = P.bary[P.facet[f][j]];
+                for (int c = 0; c < 3; ++c) wv[j][c] = xv[0][c] * b[0] + xv[1][c] * b[1] + xv[2][c] * b[2] + xv[3][c] * b[3];
+            }
+            double u[3], v[3], cr[3];
+            for (int c = 0; c < 3; ++c) {
+                u[c] = wv[1][c] - wv[0][c];
+                v[c] = wv[2][c] - wv[0][c];
+            }
+            cr[0] = u[1] * v[2] - u[2] * v[1];
+            cr[1] = u[2] * v[0] - u[0] * v[2];
+            cr[2] = u[0] * v[1] - u[1] * v[0];
+            const double ad = norm3(cr);
+            /* mass: Quad2_2D composite rule, weights halved on lattice faces */
+            const double wq = ad * (P.boundary[f] ? 0.5 : 1.);
+            for (int q = 0; q < 4; ++q) {
+                double b[4];
+                for (int c = 0; c < 4; ++c)
+                    b[c] = P.bary[P.facet[f][0]][c] * Q2N[q][0] + P.bary[P.facet[f][1]][c] * Q2N[q][1] +
+                           P.bary[P.facet[f][2]][c] * Q2N[q][2];
+                for (int i = 0; i < 4; ++i)
+                    for (int j = 0; j < 4; ++j) qs[i][j] += (wq * Q2W[q]) * (b[i] * b[j]);
+            }
+            /* Laplace-Beltrami: facet normal, D/2 |det| (no halving) */
+            if (ad > 0.) {
+                double n[3] = {cr[0] / ad, cr[1] / ad, cr[2] / ad}, pq[4][3];
+                for (int i = 0; i < 4; ++i) {
+                    const double gn = dot3(gl[i], n);
+                    for (int c = 0; c < 3; ++c) pq[i][c] = gl[i][c] - gn * n[c];
+                }
+                for (int i = 0; i < 4; ++i)
+                    for (int j = 0; j < 4; ++j) lb[4 * i + j] += dot3(pq[i], pq[j]) * ad;
+            }
+        }
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) {
+                mass[4 * i + j] = i == j ? qs[i][i] : alpha * qs[i][j];
+                lb[4 * i + j] *= D * 0.5;
+            }
+    }
+    /* rhs on the regular children (SetupInterfaceRhsP1, ifacetransp.cpp:532-563) */
+    int sg0 = legacy_sign(ls10[0]), inter = 0;
+    for (int v = 1; v < 10; ++v)
+        if (legacy_sign(ls10[v]) != sg0) inter = 1;
+    if (inter) {
+        for (int ch = 0; ch < 8; ++ch) {
+            double tri[2][3][4], det[2];
+            const int nt = orc_legacy_child_triangles(xv, ls10, ch, tri, det);
+            if (nt < 0) return ORC_ERR_ZERO_PATTERN;
+            for (int t = 0; t < nt; ++t)
+                for (int q = 0; q < 7; ++q) {
+                    double b[4], x[3];
+                    for (int c = 0; c < 4; ++c)
+                        b[c] = tri[t][0][c] * Q2D_NODE[q][0] + tri[t][1][c] * Q2D_NODE[q][1] + tri[t][2][c] * Q2D_NODE[q][2];
+                    for (int c = 0; c < 3; ++c) x[c] = xv[0][c] * b[0] + xv[1][c] * b[1] + xv[2][c] * b[2] + xv[3][c] * b[3];
+                    const double fx = orc_rhs_quadratic(fpar, x);
+                    for (int i = 0; i < 4; ++i) rhs[i] += (det[t] * Q2D_W[q]) * (fx * b[i]);
+                }
+        }
+    }
+    return ORC_OK;
+}
+
+int orc_assemble_legacy_p1(int64_t nt, const int32_t* tet_v, const int32_t* tet_e, const double* coords,
+                           const double* ls_vert, const double* ls_edge, const int32_t* dof_vert, int64_t m,
+                           double alpha, double D, const double* fpar, int64_t* rowptr, int32_t** colind_out,
+                           int64_t* nnz_out, double** mass_out, double** lb_out, double* rhs) {
+    uint8_t* vis = (uint8_t*)calloc((size_t)(nt > 0 ? nt : 1), 1);
+    double(*loc)[36] = (double(*)[36])malloc(sizeof(double) * 36 * (size_t)(nt > 0 ? nt : 1));
+    for (int64_t t = 0; t < nt; ++t) {
+        double xv[4][3], ls10[10];
+        for (int i = 0; i < 4; ++i) memcpy(xv[i], coords + 3 * tet_v[4 * t + i], sizeof xv[i]);
+        gather_ls10(tet_v + 4 * t, tet_e + 6 * t, ls_vert, ls_edge, ls10);
+        int ne = 0;
+        int st = orc_legacy_local(xv, ls10, alpha, D, fpar, loc[t], loc[t] + 16, loc[t] + 32, &ne);
+        if (st) {
+            free(vis);
+            free(loc);
+            return st;
+        }
+        vis[t] = (uint8_t)ne;
+    }
+    /* pattern: numbered pairs of the visited tets (MatrixBuilderCL keeps explicit zeros) */
+    int64_t* cnt = (int64_t*)calloc((size_t)m + 1, sizeof(int64_t));
+    for (int64_t t = 0; t < nt; ++t) {
+        if (!vis[t]) continue;
+        for (int i = 0; i < 4; ++i) {
+            const int32_t r = dof_vert[tet_v[4 * t + i]];
+            if (r >= 0) cnt[r + 1] += 4;
+        }
+    }
+    for (int64_t r = 0; r < m; ++r) cnt[r + 1] += cnt[r];
+    int32_t* tmp = (int32_t*)malloc(sizeof(int32_t) * (size_t)(cnt[m] > 0 ? cnt[m] : 1));
+    int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * (size_t)(m + 1));
+    memcpy(fill, cnt, sizeof(int64_t) * (size_t)(m + 1));
+    int64_t* ecnt = (int64_t*)calloc((size_t)m + 1, sizeof(int64_t));
+    for (int64_t t = 0; t < nt; ++t) {
+        if (!vis[t]) continue;
+        for (int i = 0; i < 4; ++i) {
+            const int32_t r = dof_vert[tet_v[4 * t + i]];
+            if (r < 0) continue;
+            for (int j = 0; j < 4; ++j) {
+                const int32_t c = dof_vert[tet_v[4 * t + j]];
+                if (c >= 0) tmp[fill[r]++] = c;
+            }
+        }
+    }
+    rowptr[0] = 0;
+    for (int64_t r = 0; r < m; ++r) {
+        const int64_t b = cnt[r], e = fill[r];
+        qsort(tmp + b, (size_t)(e - b), sizeof(int32_t), cmp_i32);
+        int64_t u = 0;
+        for (int64_t k = b; k < e; ++k)
+            if (k == b || tmp[k] != tmp[k - 1]) ++u;
+        rowptr[r + 1] = rowptr[r] + u;
+    }
+    const int64_t nnz = rowptr[m];
+    int32_t* colind = (int32_t*)malloc(sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1));
+    for (int64_t r = 0; r < m; ++r) {
+        int64_t w = rowptr[r];
+        for (int64_t k = cnt[r]; k < fill[r]; ++k)
+            if (k == cnt[r] || tmp[k] != tmp[k - 1]) colind[w++] = tmp[k];
+    }
+    free(tmp);
+    free(fill);
+    free(cnt);
+    free(ecnt);
+    double* M = (double*)calloc((size_t)(nnz > 0 ? nnz : 1), sizeof(double));
+    double* A = (double*)calloc((size_t)(nnz > 0 ? nnz : 1), sizeof(double));
+    for (int64_t r = 0; r < m; ++r) rhs[r] = 0.;
+    for (int64_t t = 0; t < nt; ++t) {
+        int32_t I[4];
+        for (int i = 0; i < 4; ++i) I[i] = dof_vert[tet_v[4 * t + i]];
+        for (int i = 0; i < 4; ++i)
+            if (I[i] >= 0) rhs[I[i]] += loc[t][32 + i];
+        if (!vis[t]) continue;
+        for (int i = 0; i < 4; ++i) {
+            if (I[i] < 0) continue;
+            for (int j = 0; j < 4; ++j) {
+                if (I[j] < 0) continue;
+                const int64_t pos = find_col(colind, rowptr[I[i]], rowptr[I[i] + 1], I[j]);
+                M[pos] += loc[t][4 * i + j];
+                A[pos] += loc[t][16 + 4 * i + j];
+            }
+        }
+    }
+    free(vis);
+    free(loc);
+    *colind_out = colind;
+    *nnz_out = nnz;
+    *mass_out = M;
+    *lb_out = A;
+    return ORC_OK;
+}
+
+/* ======================================================================= */
 /* sparse linear algebra and Krylov solvers                                  */
 /* ======================================================================= */
 void orc_spmv(int64_t m, const int64_t* rowptr, const int32_t* colind, const double* vals, const double* x,

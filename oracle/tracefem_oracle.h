@@ -110,6 +110,23 @@ int orc_local_forms(const double xv[4][3], const double ls10[10], const orc_asse
                     const double* chi_loc, double out[ORC_NUM_MAT_FORMS][100], double rhs[10],
                     int* n_facets);
 
+/* ---- legacy P1 interface forms (surfactant.cpp path) ------------------- */
+/* f(x) = p0 + p1 x + p2 y + p3 z + p4 x^2 + p5 y^2 + p6 z^2 + p7 xy + p8 xz + p9 yz */
+double orc_rhs_quadratic(const double* p, const double x[3]);
+/* planar pieces of regular child ch (InterfaceTriangleCL::ComputeForChild) */
+int orc_legacy_child_triangles(const double xv[4][3], const double ls10[10], int ch, double tri[2][3][4],
+                               double det[2]);
+/* LocalInterfaceMassP1CL (alpha), LocalLaplaceBeltramiP1CL (D), and the tet's
+ * SetupInterfaceRhsP1 contributions; nonempty = lattice patch has facets     */
+int orc_legacy_local(const double xv[4][3], const double ls10[10], double alpha, double D, const double* fpar,
+                     double mass[16], double lb[16], double rhs[4], int* nonempty);
+/* SetupInterfaceMassP1 / SetupLBP1 / SetupInterfaceRhsP1 over a mesh with a P1
+ * numbering (dof_vert, -1 = not numbered); CSR and values malloc'ed.         */
+int orc_assemble_legacy_p1(int64_t nt, const int32_t* tet_v, const int32_t* tet_e, const double* coords,
+                           const double* ls_vert, const double* ls_edge, const int32_t* dof_vert, int64_t m,
+                           double alpha, double D, const double* fpar, int64_t* rowptr, int32_t** colind,
+                           int64_t* nnz, double** mass, double** lb, double* rhs);
+
 /* ---- sparse linear algebra and solvers --------------------------------- */
 void orc_spmv(int64_t m, const int64_t* rowptr, const int32_t* colind, const double* vals,
               const double* x, double* y);

@@ -94,6 +94,22 @@ def legacy_case():
     print("legacy", {k: v for k, v in out.items() if not k.endswith("dof_vert")})
 
 
+def legacy_forms_case(n=10, a=1.6):
+    d = run("legacy_forms", str(n), repr(a))
+    mesh = O.brick(n, a=a)
+    emap = edge_map(mesh, d["edge_v"])
+    ls_edge = np.empty(mesh.ne)
+    ls_edge[emap] = d["ls_edge"]
+    np.savez_compressed(
+        os.path.join(HERE, f"legacy_forms_sphere_n{n}.npz"), n=n, a=a, alpha=float(d["alpha"][0]), D=float(d["D"][0]),
+        ls_vert=d["ls_vert"], ls_edge=ls_edge, dof_vert=d["dof_vert"].astype(np.int32),
+        n_active=int(d["n_active"][0]), n_dofs=int(d["n_dofs"][0]),
+        rowptr=d["M.rowptr"], colind=d["M.colind"].astype(np.int32), M=d["M.vals"],
+        A_rowptr=d["A.rowptr"], A_colind=d["A.colind"].astype(np.int32), A=d["A.vals"], rhs=d["rhs"],
+        tet_v_sha=sha(d["tet_v"].astype(np.int64)), coords_sha=sha(d["coords"]))
+    print("legacy forms", n, "dofs", int(d["n_dofs"][0]), "nnz", len(d["M.colind"]))
+
+
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
@@ -103,3 +119,4 @@ if __name__ == "__main__":
     system_case("torus_p2_n10.npz", "p2", "lsP2", "torus", 10, 1.6, False)
     area_case()
     legacy_case()
+    legacy_forms_case()

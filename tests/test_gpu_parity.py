@@ -267,6 +267,59 @@ def test_legacy_numbering(ctx, golden):
     assert np.array_equal(ctx.dofs()[0], g["sphere_dof_vert"])
 
 
+LEGACY_F = [1.0, 0, 0, -0.5, 0, 0, 0, 1.0, 0, 0]  # f = 1 + x y - z / 2, the harness's test function
+
+
+def test_legacy_forms_match_reference(ctx, golden):
+    """SetupInterfaceMassP1 / SetupLBP1 / SetupInterfaceRhsP1 on the legacy numbering, unit sphere on 10^3:
+    pattern bit-exact, values within 1e-12 of the reference's."""
+    g = golden("legacy_forms_sphere_n10.npz")
+    brick(ctx, int(g["n"]), float(g["a"]))
+    ctx.levelset_upload(g["ls_vert"], g["ls_edge"])
+    na, nd = ctx.create_numb_on_interface_p1()
+    assert na == int(g["n_active"]) and nd == int(g["n_dofs"])
+    assert np.array_equal(ctx.dofs()[0], g["dof_vert"])
+    nnz = ctx.setup_interface_p1_legacy(float(g["alpha"]), float(g["D"]), LEGACY_F)
+    assert nnz == len(g["colind"])
+    for f, key in ((tf.FORM_M, "M"), (tf.FORM_A, "A")):
+        rp, ci, v = ctx.matrix(f)
+        assert np.array_equal(rp, g["rowptr"]) and np.array_equal(ci, g["colind"])
+        ok, err = mat_close(v, g[key])
+        assert ok, (key, err)
+    ok, err = mat_close(ctx.vec_download(tf.VEC_RHS), g["rhs"])
+    assert ok, err
+    with pytest.raises(tf.TraceFEMError):
+        ctx.matrix(tf.FORM_CN)
+
+
+@pytest.mark.parametrize("n,kind,par,alpha,D,f", [
+    (14, O.LS_TORUS, [1.0, 0.4, 2], 1.0, 1.0, [0.5, 1, -1, 0.25, 0.3, 0, -0.2, 0, 0.1, 0]),
+    (11, O.LS_SPHERE, [0.1, -0.2, 0.05, 0.8], 0.3, 2.5, None),
+])
+def test_legacy_forms_match_oracle(ctx, n, kind, par, alpha, D, f):
+    om = brick(ctx, n, 1.6)
+    ctx.levelset_analytic(kind, par, True)
+    lv, le = O.levelset(om, kind, par, True)
+    na, nd = ctx.create_numb_on_interface_p1()
+    dv = ctx.dofs()[0]
+    st, ona, ond, odv = O.numb_on_interface_p1(om, lv, le)
+    assert st == O.OK and np.array_equal(dv, odv) and nd == ond
+    ctx.vec_fill(tf.VEC_RHS, nd, 7.0)
+    nnz = ctx.setup_interface_p1_legacy(alpha, D, f)
+    st, rp, ci, M, A, rhs = O.assemble_legacy_p1(om, lv, le, odv, ond, alpha, D, f if f is not None else [0.0] * 10)
+    assert st == O.OK and nnz == len(ci)
+    for form, ref in ((tf.FORM_M, M), (tf.FORM_A, A)):
+        grp, gci, v = ctx.matrix(form)
+        assert np.array_equal(grp, rp) and np.array_equal(gci, ci)
+        ok, err = mat_close(v, ref)
+        assert ok, err
+    if f is not None:
+        ok, err = mat_close(ctx.vec_download(tf.VEC_RHS), rhs)
+        assert ok, err
+    else:  # no rhs requested: the vector is left alone
+        assert np.all(ctx.vec_download(tf.VEC_RHS) == 7.0)
+
+
 def oracle_ch_steps(g, nsteps, dt, eps, rho, beta, xi, chi0, restart=50, tol=1e-10, warm=True):
     """surfphasesep BDF1 steps restated on the oracle (CPU)."""
     rp, ci, M = g["rowptr"], g["colind"], g["M"]

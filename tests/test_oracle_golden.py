@@ -125,3 +125,21 @@ def test_legacy_numbering_golden(golden):
         assert st == O.OK and nd == int(g[c + "_n_dofs"]) and na == int(g[c + "_n_active"])
         assert np.array_equal(dv, g[c + "_dof_vert"])
     assert int(g["sphere_n_dofs"]) == 1156 and int(g["plane_n_dofs"]) == 8
+
+
+LEGACY_F = [1.0, 0, 0, -0.5, 0, 0, 0, 1.0, 0, 0]  # f = 1 + x y - z / 2, the harness's test function
+
+
+def test_oracle_legacy_forms_match_reference(golden):
+    """SetupInterfaceMassP1 (alpha on the off-diagonal only), SetupLBP1 (facet normals, no halving on lattice
+    faces) and SetupInterfaceRhsP1 (planar pieces of the regular children) of the reference, on the unit sphere
+    with the legacy interface numbering."""
+    g = golden("legacy_forms_sphere_n10.npz")
+    mesh = O.brick(int(g["n"]), a=float(g["a"]))
+    st, rp, ci, M, A, rhs = O.assemble_legacy_p1(mesh, g["ls_vert"], g["ls_edge"], g["dof_vert"], int(g["n_dofs"]),
+                                                 float(g["alpha"]), float(g["D"]), LEGACY_F)
+    assert st == O.OK
+    assert np.array_equal(rp, g["rowptr"]) and np.array_equal(ci, g["colind"])
+    assert np.array_equal(g["A_rowptr"], g["rowptr"]) and np.array_equal(g["A_colind"], g["colind"])
+    for v, ref in ((M, g["M"]), (A, g["A"]), (rhs, g["rhs"])):
+        assert np.max(np.abs(v - ref)) <= 1e-12 * np.max(np.abs(ref)), np.max(np.abs(v - ref)) / np.max(np.abs(ref))
