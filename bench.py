@@ -142,9 +142,11 @@ class Clocks:
 
 # ---------------------------------------------------------------------------
 def pcg_bytes(m, nnz, iters, fp32):
-    """Algorithmic bytes of the persistent PCG per iteration: CSR values and
-    column indices once, row pointers once, vectors: z and p gathered (counted
-    once), p_new and q written, x, r, p_new, q, diag read and x, r, z written."""
+    """Algorithmic bytes of the persistent PCG per iteration: matrix values and
+    column indices once, row pointers once, and per row 12 vector words: the
+    FP64 kernel reads z, p, x, r, q, diag and writes p, q, x, r, z (+1 for the
+    gathered p); the single-barrier FP32 kernel reads and writes the 4-word
+    state {r, w, s, 1/d}, p and the correction dx."""
     vb = 4 if fp32 else 8
     return iters * ((vb + 4) * nnz + 4 * (m + 1) + 12 * vb * m)
 
@@ -259,7 +261,7 @@ def run_ours(args, rank, ws, dist):
     na, m, nnz = state["na"], state["m"], state["nnz"]
     if dom == "pcg":
         per_launch = pcg_bytes(m, nnz, state["it"], fp32=True)
-        note = "FP32 inner PCG iterations of one solve: (4+4)*nnz + 4*(m+1) + 48*m bytes per iteration"
+        note = "FP32 inner iterations of one single-barrier PCG solve: (4+4)*nnz + 4*(m+1) + 48*m bytes per iteration"
     elif dom == "assemble":
         per_launch = na * (10 * 8 + 3 * 55 * 8 + 10 * 8)
         note = "per cut tet: 10 level-set values read, 3 packed 10x10 element matrices + load vector written"

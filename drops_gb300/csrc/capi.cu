@@ -59,8 +59,12 @@ int tf_create(tf_context** out, int device) {
     // Two measured fastest on GB300 (fewer blocks make the grid barrier
     // cheaper, more hide gather latency); TF_KRY_BLOCKS_PER_SM overrides.
     c->kry_blocks_per_sm = 2;
+    c->kry_threads = 512;  // mixed PCG: one 512-thread block per SM halves the arrivals per grid barrier
     if (const char* e = std::getenv("TF_KRY_BLOCKS_PER_SM")) c->kry_blocks_per_sm = std::atoi(e);
     if (const char* e = std::getenv("TF_KRY_THREADS")) c->kry_threads = std::atoi(e);
+    if (const char* e = std::getenv("TF_PCG_TWO_BARRIER")) c->pcg_two_barrier = std::atoi(e) != 0;
+    if (const char* e = std::getenv("TF_SPMV_PAIR")) c->spmv_pair = std::atoi(e) != 0;
+    if (const char* e = std::getenv("TF_GMRES2_MASTER")) c->gmres2_master = std::atoi(e) != 0;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
         cudaMallocHost((void**)&c->h_status, 4 * sizeof(int)) != cudaSuccess ||
@@ -115,6 +119,8 @@ int tf_destroy(tf_context* t) {
         tf::release(c->sell_perm[i]);
         tf::release(c->sell_v64[i]);
         tf::release(c->sell_v32[i]);
+        tf::release(c->sell_v2f[i]);
+        tf::release(c->sell_rexp[i]);
     }
     tf::release(c->block_rowptr);
     tf::release(c->block_colind);
@@ -122,6 +128,7 @@ int tf_destroy(tf_context* t) {
     tf::release(c->user_colind);
     for (int i = 0; i < TF_NUM_VECS; ++i) tf::release(c->vecs[i]);
     tf::release(c->scratch);
+    tf::release(c->x_pairs);
     tf::release(c->scan_tmp);
     tf::release(c->status);
     tf::release_solver_workspace(c);

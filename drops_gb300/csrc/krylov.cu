@@ -142,7 +142,7 @@ int ensure_sell(Context* c, CSR& A, bool fp32) {
         S.col = c->sell_col[id].p;
         S.src = c->sell_src[id].p;
         S.pattern_gen = A.pattern_gen;
-        S.v64_version = S.v32_version = -1;
+        S.v64_version = S.v32_version = S.v2f_version = -1;
     }
     if (fp32) {
         if (S.v32_version != A.version || !S.v32) {
@@ -176,13 +176,174 @@ __global__ void k_spmv(int64_t nslices, const int32_t* __restrict__ perm, const 
     }
 }
 
+// ---------------------------------------------------------------------------
+// FP64-accurate SpMV on FP32 pairs
+//
+// GB300 issues FP64 at 1/64 of the FP32 rate: one FP64 FMA per non-zero keeps
+// the FP64 pipe about as busy as HBM.  Instead every row is scaled by a power
+// of two 2^-e (its largest |a| lands in [0.5, 1)) and each scaled value is
+// stored as an unevaluated FP32 pair hi + lo (8 bytes, like the FP64 value);
+// x is split the same way (without scaling) once per call.  Products and the
+// row sum are formed in pair arithmetic (exact product error by FMA, two-sum
+// for the running sum): about 12 FP32 operations per non-zero and 4 FP64
+// operations per row.  Each product carries ~2^-48 relative error, so
+// |y - A x| <= ~2^-44 sum_j |a_ij x_j| + 2^-140 max|a_i.| max|x|, far inside
+// the 1e-12 parity bound.  x entries outside {0} U [2^-100, 2^100] (or not
+// finite) raise a flag that switches the same launch to FP64 FMAs.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 split_pair(double v) {
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(v - (double)h));
+}
+
+__device__ __forceinline__ double pow2(int e) {  // 2^e, |e| <= 1022
+    return __longlong_as_double((long long)(e + 1023) << 52);
+}
+
+// warp per slice: row exponent, then the scaled pairs; *bad set on a
+// non-finite value
+__global__ void k_sell_vals_pair(int64_t nslices, const int32_t* __restrict__ ptr, const int32_t* __restrict__ src,
+                                 const double* __restrict__ vals, float2* __restrict__ out, int32_t* __restrict__ rexp,
+                                 int* bad) {
+    const int lane = threadIdx.x & 31;
+    TF_SLICE_LOOP(nslices, s) {
+        const int32_t p0 = ptr[s], w = (ptr[s + 1] - p0) >> 5;
+        double mx = 0.;
+        for (int32_t k = 0; k < w; ++k) {
+            const int32_t q = src[p0 + 32 * k + lane];
+            if (q >= 0) {
+                const double v = vals[q];
+                if (!isfinite(v)) atomicOr(bad, 1);
+                mx = fmax(mx, fabs(v));
+            }
+        }
+        int e = 0;
+        if (mx > 0. && isfinite(mx)) frexp(mx, &e);
+        e = max(-1000, min(1000, e));
+        rexp[s * 32 + lane] = e;
+        const double sc = pow2(-e);
+        for (int32_t k = 0; k < w; ++k) {
+            const int32_t q = src[p0 + 32 * k + lane];
+            out[p0 + 32 * k + lane] = split_pair(q >= 0 ? vals[q] * sc : 0.);
+        }
+    }
+}
+
+// x -> pairs; *flag set when an entry is outside {0} U [2^-100, 2^100]
+__global__ void k_split_x(int64_t n, const double* __restrict__ x, float2* __restrict__ out, int* flag) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = x[i];
+        const double a = fabs(v);
+        if (v != 0. && !(a >= 7.888609052210118e-31 && a <= 1.2676506002282294e30)) atomicOr(flag, 1);
+        out[i] = split_pair(v);
+    }
+}
+
+// (sh, sl) += a * x in pair arithmetic; a = (0, 0) leaves the sum unchanged
+__device__ __forceinline__ void pair_fma(float& sh, float& sl, float2 a, float2 x) {
+    const float p = __fmul_rn(a.x, x.x);
+    const float pe = __fmaf_rn(a.x, x.x, -p);
+    const float t = __fmaf_rn(a.x, x.y, __fmaf_rn(a.y, x.x, pe));
+    const float s = __fadd_rn(sh, p);
+    const float bb = __fsub_rn(s, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    sl = __fadd_rn(sl, __fadd_rn(err, t));
+    sh = s;
+}
+
+// slot row in pair arithmetic, the loads staged like sell_row
+__device__ __forceinline__ double sell_row_pair(const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                                                const float2* __restrict__ val, const int32_t* __restrict__ rexp,
+                                                const float2* __restrict__ x, int64_t s, int lane) {
+    constexpr int U = 8;
+    const int32_t p0 = __ldg(ptr + s);
+    const int32_t w = (__ldg(ptr + s + 1) - p0) >> 5;
+    const int32_t* cp = col + p0 + lane;
+    const float2* vp = val + p0 + lane;
+    float sh = 0.f, sl = 0.f;
+    int32_t cn[U];
+    float2 vn[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const bool in = u < w;
+        cn[u] = in ? __ldg(cp + 32 * u) : -1;
+        vn[u] = in ? __ldg(vp + 32 * u) : make_float2(0.f, 0.f);
+    }
+    for (int32_t k = 0; k < w; k += U) {
+        float2 xv[U], vv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            xv[u] = cn[u] >= 0 ? __ldg(x + cn[u]) : make_float2(0.f, 0.f);
+            vv[u] = vn[u];
+        }
+        const int32_t kn = k + U;
+        if (kn < w) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const bool in = kn + u < w;
+                cn[u] = in ? __ldg(cp + 32 * (kn + u)) : -1;
+                vn[u] = in ? __ldg(vp + 32 * (kn + u)) : make_float2(0.f, 0.f);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) pair_fma(sh, sl, vv[u], xv[u]);
+    }
+    return ((double)sh + (double)sl) * pow2(__ldg(rexp + s * 32 + lane));
+}
+
+__global__ void k_spmv_pair(int64_t nslices, const int32_t* __restrict__ perm, const int32_t* __restrict__ ptr,
+                            const int32_t* __restrict__ col, const float2* __restrict__ v2, const int32_t* __restrict__ rexp,
+                            const double* __restrict__ v64, const float2* __restrict__ x2, const double* __restrict__ x,
+                            const int* __restrict__ flag, double* __restrict__ y) {
+    const int lane = threadIdx.x & 31;
+    const bool native = *flag != 0;
+    TF_SLICE_LOOP(nslices, s) {
+        const double a = native ? sell_row<double>(ptr, col, v64, s, lane, [&](int32_t j) { return __ldg(x + j); })
+                                : sell_row_pair(ptr, col, v2, rexp, x2, s, lane);
+        const int32_t row = perm[s * 32 + lane];
+        if (row >= 0) y[row] = a;
+    }
+}
+
+static int ensure_sell_pair(Context* c, CSR& A) {
+    Sell& S = A.sell;
+    if (S.v2f_version == A.version && S.v2f) return TF_OK;
+    const int id = mat_index(c, A);
+    TF_TRY(ensure(c, c->sell_v2f[id], (size_t)(S.npad > 0 ? S.npad : 1)));
+    TF_TRY(ensure(c, c->sell_rexp[id], (size_t)(S.nslices > 0 ? S.nslices * 32 : 1)));
+    S.v2f = c->sell_v2f[id].p;
+    S.rexp = c->sell_rexp[id].p;
+    TF_CUDA(c, cudaMemsetAsync(c->status.p + 3, 0, sizeof(int), c->stream));
+    k_sell_vals_pair<<<grid_for(c, S.nslices * 32), kBlock, 0, c->stream>>>(S.nslices, S.ptr, S.src, A.vals, S.v2f,
+                                                                            S.rexp, c->status.p + 3);
+    ++c->launches;
+    TF_CUDA(c, cudaGetLastError());
+    int bad = 0;
+    TF_CUDA(c, cudaMemcpyAsync(&bad, c->status.p + 3, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    S.v2f_ok = bad == 0;
+    S.v2f_version = A.version;
+    return TF_OK;
+}
+
 int spmv(Context* c, const CSR& Ac, const double* x, double* y) {
     CSR& A = const_cast<CSR&>(Ac);
     TF_TRY(ensure_sell(c, A, false));
+    if (c->spmv_pair) TF_TRY(ensure_sell_pair(c, A));
     TimedLaunch tl(c, TF_K_SPMV);
-    k_spmv<double><<<grid_for(c, A.sell.nslices * 32), kBlock, 0, c->stream>>>(A.sell.nslices, A.sell.perm, A.sell.ptr,
-                                                                               A.sell.col, A.sell.v64, x, y);
-    ++c->launches;
+    if (!c->spmv_pair || !A.sell.v2f_ok) {
+        k_spmv<double><<<grid_for(c, A.sell.nslices * 32), kBlock, 0, c->stream>>>(
+            A.sell.nslices, A.sell.perm, A.sell.ptr, A.sell.col, A.sell.v64, x, y);
+        ++c->launches;
+    } else {
+        TF_TRY(ensure(c, c->x_pairs, (size_t)(A.m > 0 ? A.m : 1)));
+        TF_CUDA(c, cudaMemsetAsync(c->status.p + 2, 0, sizeof(int), c->stream));
+        k_split_x<<<grid_for(c, A.m), kBlock, 0, c->stream>>>(A.m, x, c->x_pairs.p, c->status.p + 2);
+        k_spmv_pair<<<grid_for(c, A.sell.nslices * 32), kBlock, 0, c->stream>>>(
+            A.sell.nslices, A.sell.perm, A.sell.ptr, A.sell.col, A.sell.v2f, A.sell.rexp, A.sell.v64, c->x_pairs.p, x,
+            c->status.p + 2, y);
+        c->launches += 2;
+    }
     TF_CUDA(c, cudaGetLastError());
     return TF_OK;
 }
@@ -327,7 +488,6 @@ int ch_block(Context* c, double alpha, double mob, double rho, double eps2, doub
 // ---------------------------------------------------------------------------
 template <class T>
 struct PcgArgs {
-    KryScal* sc;     // scalar state (global)
     int64_t m, nslices;
     const int32_t* perm;
     const int32_t* ptr;
@@ -341,8 +501,7 @@ struct PcgArgs {
     T* p0;
     T* p1;
     T* q;
-    double* part;  // [2][nblocks][3]
-    GridSync gs;
+    GridAR g;
     int max_iter;
     double tol;
     int rel;
@@ -350,20 +509,25 @@ struct PcgArgs {
     double* out_resid;
 };
 
-
+// Standard PCG (PCGSolverCL<JACPcCL>::Solve's recurrences): two all-reduce
+// barriers per iteration, <p, A p> and then <r, r>, <z, r>.  The scalar
+// recurrences (square roots, divisions) run on thread 0 of every block on
+// bitwise identical sums and are broadcast through shared memory.
 template <class T>
 __global__ void __launch_bounds__(kKryThreads, sizeof(T) == 4 ? 4 : 3) k_pcg(PcgArgs<T> a) {
-    __shared__ KryScal sc;
+    __shared__ double sh[6];
     const int lane = threadIdx.x & 31;
-    double* partA = a.part;
-    double* partB = a.part + (size_t)gridDim.x * 3;
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
     const double tol = a.tol;
     const int max_iter = a.max_iter, rel = a.rel;
+    unsigned long long epoch = 0;
+    double rho = 0., normb = 1., resid = 0.;
+    int it = 0;
+    bool converged = false, done = false;
 
-    // r = b - A x ; z = r / d ; p0 = z ; partials <r,r>, <b,b>, <z,r>
+    // r = b - A x ; z = r / d ; p0 = z ; sums <r,r>, <b,b>, <z,r>
     {
-        T v[3] = {T(0), T(0), T(0)};
+        double v[3] = {0., 0., 0.};
         const T* x = a.x;
         TF_SLICE_LOOP(a.nslices, s) {
             const T ax = sell_row<T>(a.ptr, a.col, a.val, s, lane, [&](int32_t j) { return kld(x + j); });
@@ -380,29 +544,31 @@ __global__ void __launch_bounds__(kKryThreads, sizeof(T) == 4 ? 4 : 3) k_pcg(Pcg
                 v[2] += zi * ri;
             }
         }
-        block_partials<3>(v, partA);
-    }
-    if (!grid_step<3>(a.gs, partA, a.sc, sc, [&](const double* s, KryScal& g) {
-            double nb = sqrt(s[1]);
+        double o[3];
+        if (!grid_allreduce<double, 3>(a.g, epoch, v, o)) return;
+        if (threadIdx.x == 0) {
+            double nb = sqrt(o[1]);
             if (nb == 0.0 || !rel) nb = 1.0;
-            g.normb = nb;
-            g.resid = sqrt(s[0]) / nb;
-            g.rho = s[2];
-            g.beta = 0.;
-            g.it = 0;
-            g.converged = g.resid <= tol;
-            g.done = g.converged || max_iter <= 0;
-        }))
-        return;
+            sh[0] = nb;
+            sh[1] = sqrt(o[0]) / nb;
+        }
+        __syncthreads();
+        normb = sh[0];
+        resid = sh[1];
+        rho = o[2];
+        converged = resid <= tol;
+        done = converged || max_iter <= 0;
+    }
     T* pc = a.p0;  // previous direction (beta = 0 in the first iteration)
     T* pn = a.p1;
-    while (!sc.done) {
-        const T beta = (T)sc.beta;
+    T beta = T(0);
+    while (!done) {
         // phase A: p_new = z + beta p_old ; q = A p_new ; <q, p_new>
         {
-            T v[1] = {T(0)};
+            double v[1] = {0.};
             const T* z = a.z;
             const T* po = pc;
+            T acc1 = T(0);
             TF_SLICE_LOOP(a.nslices, s) {
                 const T acc = sell_row<T>(a.ptr, a.col, a.val, s, lane,
                                           [&](int32_t j) { return kld(z + j) + beta * kld(po + j); });
@@ -411,43 +577,50 @@ __global__ void __launch_bounds__(kKryThreads, sizeof(T) == 4 ? 4 : 3) k_pcg(Pcg
                     const T pi = kld(z + row) + beta * kld(po + row);
                     pn[row] = pi;
                     a.q[row] = acc;
-                    v[0] += acc * pi;
+                    acc1 += acc * pi;
                 }
             }
-            block_partials<1>(v, partA);
+            v[0] = acc1;
+            double o[1];
+            if (!grid_allreduce<double, 1>(a.g, epoch, v, o)) return;
+            if (threadIdx.x == 0) sh[2] = rho / o[0];
+            __syncthreads();
         }
-        if (!grid_step<1>(a.gs, partA, a.sc, sc, [&](const double* s, KryScal& g) { g.alpha = g.rho / s[0]; })) return;
-        const T alpha = (T)sc.alpha;
+        const T alpha = (T)sh[2];
         // phase B: x += alpha p ; r -= alpha q ; z = r / d ; <r,r>, <z,r>
         {
-            T v[2] = {T(0), T(0)};
+            T v2[2] = {T(0), T(0)};
             for (int64_t i = tid; i < a.m; i += nth) {
                 a.x[i] += alpha * kld(pn + i);
                 const T ri = a.r[i] - alpha * kld(a.q + i);
                 const T zi = ri / a.diag[i];
                 a.r[i] = ri;
                 a.z[i] = zi;
-                v[0] += ri * ri;
-                v[1] += zi * ri;
+                v2[0] += ri * ri;
+                v2[1] += zi * ri;
             }
-            block_partials<2>(v, partB);
+            double v[2] = {(double)v2[0], (double)v2[1]};
+            double o[2];
+            if (!grid_allreduce<double, 2>(a.g, epoch, v, o)) return;
+            if (threadIdx.x == 0) {
+                sh[3] = sqrt(o[0]) / normb;
+                sh[4] = o[1] / rho;
+            }
+            __syncthreads();
+            ++it;
+            resid = sh[3];
+            converged = resid <= tol;
+            done = converged || it >= max_iter;
+            beta = (T)sh[4];
+            rho = o[1];
         }
-        if (!grid_step<2>(a.gs, partB, a.sc, sc, [&](const double* s, KryScal& g) {
-                g.it += 1;
-                g.resid = sqrt(s[0]) / g.normb;
-                g.converged = g.resid <= tol;
-                g.done = g.converged || g.it >= max_iter;
-                g.beta = s[1] / g.rho;
-                g.rho = s[1];
-            }))
-            return;
         T* tmp = pc;
         pc = pn;
         pn = tmp;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        *a.out_iter = sc.converged ? (int)sc.it : -1 - (int)sc.it;
-        *a.out_resid = sc.resid;
+        *a.out_iter = converged ? it : -1 - it;
+        *a.out_resid = resid;
     }
 }
 
@@ -617,6 +790,214 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_mixed(PcgMixedArg
     }
 }
 
+// ---------------------------------------------------------------------------
+// mixed-precision PCG with one grid barrier per iteration
+//
+// Chronopoulos-Gear form of preconditioned CG (s = A p carried by recurrence,
+// w = A u computed): per iteration one SpMV w_{i+1} = A u_{i+1} and one
+// all-reduce of six FP32 dots
+//   gamma = (r,u), (u,w), (u,s), (p,w), (p,s), (r,r)
+// from which every block derives beta = gamma / gamma_old and
+// alpha = gamma / (p_new, s_new), (p_new, s_new) expanded exactly as
+// (u,w) + beta ((u,s) + (p,w)) + beta^2 (p,s).  No second barrier for the
+// vector updates: the SpMV gathers the per-row state V = {r_i, w_i, s_{i-1},
+// 1/d} (one 16-byte load) and forms u_{i+1}[j] = (r_i - alpha (w_i + beta
+// s_{i-1})) / d on the fly with the same rounding as the row's owner, which
+// writes the next state into the other buffer.  The inner loop carries no
+// FP64 arithmetic: the correction dx = sum alpha p is FP32 and is added to the
+// FP64 iterate at each refinement.  Refinement (as in the two-barrier kernel:
+// when the FP32 residual has dropped by kRelUpdate, claims convergence or
+// max_iter is reached): fold x += dx; r = b - A x in FP64 (the convergence
+// test); w = A (r / d) and s = A p in FP32 with p kept, continuing the
+// recurrence with both carried vectors exact again.
+// ---------------------------------------------------------------------------
+struct PcgCg1Args {
+    int64_t m, nslices;
+    const int32_t* perm;
+    const int32_t* ptr;
+    const int32_t* col;
+    const float* val32;
+    const double* val64;
+    const float* diag;
+    const double* b;
+    double* x;
+    float4* V0;
+    float4* V1;
+    float* P;
+    float* dx;
+    GridAR g;
+    int max_iter;
+    double tol;
+    int rel;
+    int* out_iter;
+    double* out_resid;
+    int* out_updates;
+};
+
+// u_{i+1} of one row from its state {r_i, w_i, s_{i-1}, 1/d}; the owner and
+// every gatherer evaluate exactly this sequence
+__device__ __forceinline__ float cg1_s(float4 v, float beta) { return __fmaf_rn(beta, v.z, v.y); }
+__device__ __forceinline__ float cg1_r(float4 v, float s, float alpha) { return __fmaf_rn(-alpha, s, v.x); }
+__device__ __forceinline__ float cg1_u(float4 v, float alpha, float beta) {
+    return __fmul_rn(cg1_r(v, cg1_s(v, beta), alpha), v.w);
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_cg1(PcgCg1Args a) {
+    const int lane = threadIdx.x & 31;
+    unsigned long long epoch = 0;
+    float4* Vc = a.V0;
+    float4* Vn = a.V1;
+    const int max_iter = a.max_iter;
+    const double tol = a.tol;
+    double normb = 1.0, r_last = 0.0, resid = 0.0;
+    int it = 0, updates = 0;
+    bool converged = false;
+    float gam = 0.f, alpha = 0.f, beta = 0.f, thr_rel = 0.f, thr_tol = 0.f;
+
+    // r = b - A x in FP64 into V.r (first: V = {r, 0, 0, 1/d}, p = 0);
+    // returns false on a watchdog timeout, sets done/converged
+    auto true_residual = [&](bool first, bool& done) -> bool {
+        double v[2] = {0., 0.};
+        const double* x = a.x;
+        TF_SLICE_LOOP(a.nslices, s) {
+            const double ax = sell_row<double>(a.ptr, a.col, a.val64, s, lane, [&](int32_t j) { return kld(x + j); });
+            const int32_t row = __ldg(a.perm + s * 32 + lane);
+            if (row >= 0) {
+                const double bi = a.b[row];
+                const double ri = bi - ax;
+                float4 vc;
+                if (first) {
+                    vc = make_float4((float)ri, 0.f, 0.f, 1.0f / a.diag[row]);
+                    a.P[row] = 0.f;
+                } else {
+                    vc = Vc[row];
+                    vc.x = (float)ri;
+                }
+                Vc[row] = vc;
+                v[0] += ri * ri;
+                if (first) v[1] += bi * bi;
+            }
+        }
+        double o[2];
+        if (!grid_allreduce<double, 2>(a.g, epoch, v, o)) return false;
+        // FP64 square roots and division on one thread (FP64 issues at a
+        // small fraction of the FP32 rate), broadcast through shared memory
+        __shared__ double sh[4];
+        if (threadIdx.x == 0) {
+            double nb = normb;
+            if (first) {
+                nb = sqrt(o[1]);
+                if (nb == 0.0 || !a.rel) nb = 1.0;
+            }
+            const double rl = sqrt(o[0]);
+            sh[0] = nb;
+            sh[1] = rl;
+            sh[2] = rl / nb;
+        }
+        __syncthreads();
+        normb = sh[0];
+        r_last = sh[1];
+        resid = sh[2];
+        __syncthreads();
+        ++updates;
+        converged = resid <= tol;
+        done = converged || it >= max_iter;
+        thr_rel = (float)(kRelUpdate * r_last);
+        thr_tol = (float)(tol * normb);
+        return true;
+    };
+
+    // one SpMV pass; refresh: w = A (r / d) and s = A p with r, p kept (after
+    // a true residual), else the CG step with (alpha, beta)
+    auto pass = [&](bool refresh, float (&o)[6]) -> bool {
+        float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        const float al = refresh ? 0.f : alpha, be = refresh ? 0.f : beta;
+        const float4* V = Vc;
+        TF_SLICE_LOOP(a.nslices, s) {
+            const float wn =
+                sell_row<float>(a.ptr, a.col, a.val32, s, lane, [&](int32_t j) { return cg1_u(kld(V + j), al, be); });
+            // refresh: s = A p recomputed, ending the drift of its recurrence
+            const float sx = refresh ? sell_row<float>(a.ptr, a.col, a.val32, s, lane,
+                                                       [&](int32_t j) { return kld(a.P + j); })
+                                     : 0.f;
+            const int32_t row = __ldg(a.perm + s * 32 + lane);
+            if (row >= 0) {
+                const float4 vc = V[row];
+                float sn, rn, pn;
+                if (refresh) {
+                    sn = sx;
+                    rn = vc.x;
+                    pn = a.P[row];
+                } else {
+                    sn = cg1_s(vc, be);
+                    rn = cg1_r(vc, sn, al);
+                    pn = __fmaf_rn(be, a.P[row], __fmul_rn(vc.x, vc.w));
+                    a.P[row] = pn;
+                    a.dx[row] = __fmaf_rn(al, pn, a.dx[row]);
+                }
+                const float un = __fmul_rn(rn, vc.w);
+                Vn[row] = make_float4(rn, wn, sn, vc.w);
+                v[0] += rn * un;
+                v[1] += un * wn;
+                v[2] += un * sn;
+                v[3] += pn * wn;
+                v[4] += pn * sn;
+                v[5] += rn * rn;
+            }
+        }
+        if (!grid_allreduce<float, 6>(a.g, epoch, v, o)) return false;
+        float4* t = Vc;
+        Vc = Vn;
+        Vn = t;
+        return true;
+    };
+
+    // FP64 fold of the FP32 correction (own rows), then a barrier
+    auto fold = [&]() -> bool {
+        TF_SLICE_LOOP(a.nslices, s) {
+            const int32_t row = __ldg(a.perm + s * 32 + lane);
+            if (row >= 0) {
+                a.x[row] += (double)a.dx[row];
+                a.dx[row] = 0.f;
+            }
+        }
+        return grid_sync_ar(a.g, epoch);
+    };
+
+    bool done = false;
+    if (!true_residual(true, done)) return;
+    bool first = true;
+    while (!done) {
+        float o[6];
+        if (!pass(true, o)) return;
+        // continue the recurrence: beta against the gamma that built p
+        beta = first ? 0.f : o[0] / gam;
+        first = false;
+        gam = o[0];
+        alpha = gam / (o[1] + beta * (o[2] + o[3]) + beta * beta * o[4]);
+        bool refine = false;
+        while (!refine) {
+            if (!pass(false, o)) return;
+            ++it;
+            const float rn = sqrtf(o[5]);
+            refine = rn <= thr_rel || rn <= thr_tol || it >= max_iter;
+            if (!refine) {
+                beta = o[0] / gam;
+                gam = o[0];
+                alpha = gam / (o[1] + beta * (o[2] + o[3]) + beta * beta * o[4]);
+            }
+        }
+        if (!fold()) return;
+        if (!true_residual(false, done)) return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *a.out_iter = converged ? it : -1 - it;
+        *a.out_resid = resid;
+        *a.out_updates = updates;
+    }
+}
+
 void release_solver_workspace(Context* c) {
     release(c->kry64);
     release(c->kry32);
@@ -644,7 +1025,8 @@ static int run_pcg_kernel(Context* c, const CSR& A, const T* val, const T* diag,
     const void* fn = (const void*)k_pcg<T>;
     int blocks = 0;
     TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks, kKryThreads));
-    TF_TRY(ensure(c, c->kry_part, (size_t)blocks * 3 * 2 + 16 + kScalWords));
+    const size_t part_d = (size_t)2 * blocks * kArMax;
+    TF_TRY(ensure(c, c->kry_part, part_d + (part_d + 1) / 2 + 16));
     TF_TRY(ensure(c, c->kry_bar, 2));
     TF_TRY(ensure(c, c->kry_iters, 1));
     TF_TRY(ensure(c, c->kry_resid, 1));
@@ -665,9 +1047,10 @@ static int run_pcg_kernel(Context* c, const CSR& A, const T* val, const T* diag,
     a.p0 = work + 2 * A.m;
     a.p1 = work + 3 * A.m;
     a.q = work + 4 * A.m;
-    a.part = c->kry_part.p;
-    a.sc = reinterpret_cast<KryScal*>(c->kry_part.p + (size_t)blocks * 3 * 2 + 16);
-    a.gs = GridSync{c->kry_bar.p, c->kry_bar.p + 1, c->status.p};
+    a.g.count = reinterpret_cast<unsigned long long*>(c->kry_bar.p);
+    a.g.partd = c->kry_part.p;
+    a.g.partf = reinterpret_cast<float*>(c->kry_part.p + part_d);
+    a.g.status = c->status.p;
     a.max_iter = max_iter;
     a.tol = tol;
     a.rel = rel;
@@ -688,6 +1071,68 @@ static int run_pcg_kernel(Context* c, const CSR& A, const T* val, const T* diag,
     return TF_OK;
 }
 
+// single-barrier mixed PCG (k_pcg_cg1); workspace in floats: V0, V1 (4m each,
+// 16-byte aligned), p, dx, FP32 diagonal
+static int run_pcg_cg1(Context* c, const CSR& A, const double* b, double* x, int* max_iter, double* tol, int rel) {
+    const int64_t m = A.m;
+    TF_TRY(ensure(c, c->kry32, (size_t)(11 * m)));
+    float* base = c->kry32.p;
+    float* d32 = base + 10 * m;
+    k_to_f32<<<grid_for(c, m), kBlock, 0, c->stream>>>(m, A.diag, d32);
+    ++c->launches;
+    const int nt = c->kry_threads == 512 ? 512 : 256;
+    const void* fn = nt == 512 ? (const void*)k_pcg_cg1<512> : (const void*)k_pcg_cg1<256>;
+    int blocks = 0;
+    TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks, nt));
+    const size_t part_d = (size_t)2 * blocks * kArMax;
+    TF_TRY(ensure(c, c->kry_part, part_d + (part_d + 1) / 2 + 16));
+    TF_TRY(ensure(c, c->kry_bar, 2));
+    TF_TRY(ensure(c, c->kry_iters, 2));
+    TF_TRY(ensure(c, c->kry_resid, 1));
+    TF_CUDA(c, cudaMemsetAsync(c->kry_bar.p, 0, 2 * sizeof(unsigned), c->stream));
+    TF_CUDA(c, cudaMemsetAsync(c->status.p, 0, 4 * sizeof(int), c->stream));
+    TF_CUDA(c, cudaMemsetAsync(base + 9 * m, 0, sizeof(float) * (size_t)m, c->stream));
+    PcgCg1Args g;
+    g.m = m;
+    g.nslices = A.sell.nslices;
+    g.perm = A.sell.perm;
+    g.ptr = A.sell.ptr;
+    g.col = A.sell.col;
+    g.val32 = A.sell.v32;
+    g.val64 = A.sell.v64;
+    g.diag = d32;
+    g.b = b;
+    g.x = x;
+    g.V0 = reinterpret_cast<float4*>(base);
+    g.V1 = reinterpret_cast<float4*>(base + 4 * m);
+    g.P = base + 8 * m;
+    g.dx = base + 9 * m;
+    g.g.count = reinterpret_cast<unsigned long long*>(c->kry_bar.p);
+    g.g.partd = c->kry_part.p;
+    g.g.partf = reinterpret_cast<float*>(c->kry_part.p + part_d);
+    g.g.status = c->status.p;
+    g.max_iter = *max_iter;
+    g.tol = *tol;
+    g.rel = rel;
+    g.out_iter = c->kry_iters.p;
+    g.out_resid = c->kry_resid.p;
+    g.out_updates = c->kry_iters.p + 1;
+    void* args[] = {&g};
+    TF_CUDA(c, cudaLaunchCooperativeKernel(fn, blocks, nt, args, 0, c->stream));
+    ++c->launches;
+    int it[2] = {0, 0};
+    double res = 0;
+    TF_CUDA(c, cudaMemcpyAsync(it, c->kry_iters.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    TF_CUDA(c, cudaMemcpyAsync(&res, c->kry_resid.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    int st = 0;
+    TF_TRY(sync_status(c, &st));
+    if (st) return set_err(c, st, "pcg (mixed): grid barrier watchdog fired");
+    c->last_refinements = it[1];
+    *max_iter = it[0] >= 0 ? it[0] : -1 - it[0];
+    *tol = res;
+    return it[0] >= 0 ? TF_OK : set_err(c, TF_ERR_NOT_CONVERGED, "pcg (mixed): no convergence within max_iter");
+}
+
 int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, int* max_iter, double* tol, int rel) {
     if (!A.vals || A.m <= 0) return set_err(c, TF_ERR_BAD_INPUT, "pcg: empty matrix");
     TF_TRY(ensure_diag(c, A));
@@ -706,6 +1151,7 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
     }
     // mixed precision: FP32 iterations, FP64 iterate and reliable updates
     TF_TRY(ensure_sell(c, A, false));  // FP64 copy for the refinement residuals
+    if (!c->pcg_two_barrier) return run_pcg_cg1(c, A, b, x, max_iter, tol, rel);
     TF_TRY(ensure(c, c->kry32, (size_t)(6 * m)));
     float* d32 = c->kry32.p;
     k_to_f32<<<grid_for(c, m), kBlock, 0, c->stream>>>(m, A.diag, d32);

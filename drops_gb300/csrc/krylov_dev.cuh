@@ -67,6 +67,30 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
+// Eight sums over the warp at once (a transposing butterfly): round 16 swaps
+// half of the values between the half-warps, round 8 and 4 likewise, then two
+// plain xor rounds; 9 shuffles instead of 40, in independent chains.  Lane l
+// returns the total of value warp_sum8_index(l); the tree is fixed, so the
+// result does not depend on timing.
+__device__ __forceinline__ int warp_sum8_index(int lane) {
+    return ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
+}
+template <class T>
+__device__ __forceinline__ T warp_sum8(const T (&v)[8], int lane) {
+    const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+    T a4[4], a2[2];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        a4[q] = (b4 ? v[q + 4] : v[q]) + __shfl_xor_sync(0xffffffffu, b4 ? v[q] : v[q + 4], 16);
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+        a2[q] = (b3 ? a4[q + 2] : a4[q]) + __shfl_xor_sync(0xffffffffu, b3 ? a4[q] : a4[q + 2], 8);
+    T a1 = (b2 ? a2[1] : a2[0]) + __shfl_xor_sync(0xffffffffu, b2 ? a2[0] : a2[1], 4);
+    a1 += __shfl_xor_sync(0xffffffffu, a1, 2);
+    a1 += __shfl_xor_sync(0xffffffffu, a1, 1);
+    return a1;
+}
+
 template <int NV, class T>
 __device__ void block_partials(T (&v)[NV], double* part /* [nblocks][NV] */) {
     __shared__ double red[NV][32];
@@ -240,6 +264,109 @@ __device__ bool grid_step(const GridSync& g, const double* part, KryScal* gsc, K
     }
     __syncthreads();
     return st == 0;
+}
+
+// ---------------------------------------------------------------------------
+// barrier + all-reduce on one monotone arrival counter
+//
+// Every block publishes NV partial sums, arrives on a 64-bit counter that is
+// never reset inside a launch and waits until the counter reaches
+// (epoch + 1) * gridDim.x.  Arrival is a release of the whole block's writes:
+// bar.sync, then thread 0's fence (cumulative over the writes the barrier
+// ordered before it), then the atomic; the wait ends with an acquire (the
+// polling load and a fence) before the block's bar.sync.  Then
+// every block sums all partials itself, warp k taking value k over the blocks
+// in one fixed order, so all blocks hold bitwise the same sums and derive the
+// same scalars: the critical path is the arrival, one poll round trip and one
+// load of the partials, with no last-arriver reduction and no published
+// result to read back.  Partials alternate between two buffers by epoch
+// parity; a block cannot be more than one barrier ahead of a reader.
+// ---------------------------------------------------------------------------
+constexpr int kArMax = 8;  // values per all-reduce (<= warps per block)
+
+struct GridAR {
+    unsigned long long* count;  // arrivals since launch (zeroed by the host)
+    float* partf;               // [2][nblocks][kArMax]
+    double* partd;              // [2][nblocks][kArMax]
+    int* status;
+};
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// arrive and wait for all blocks of this epoch; false after a watchdog timeout
+__device__ __forceinline__ bool ar_arrive_wait(const GridAR& g, unsigned long long epoch, int* st_sh) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned long long target = (epoch + 1) * (unsigned long long)gridDim.x;
+        __threadfence();
+        atomicAdd(g.count, 1ull);
+        long long spins = 0;
+        while (ld_acquire_u64(g.count) < target) {
+            if (++spins > kSpinLimit) {
+                atomicCAS(g.status, 0, TF_ERR_WATCHDOG);
+                break;
+            }
+            if (spins > 256) __nanosleep(32);
+        }
+        __threadfence();
+        *st_sh = *((volatile int*)g.status);
+    }
+    __syncthreads();
+    return *st_sh == 0;
+}
+
+template <class T>
+__device__ __forceinline__ T* ar_part(const GridAR& g);
+template <>
+__device__ __forceinline__ float* ar_part<float>(const GridAR& g) { return g.partf; }
+template <>
+__device__ __forceinline__ double* ar_part<double>(const GridAR& g) { return g.partd; }
+
+// Sums v[k] over every thread of the grid into out[k] (identical in all
+// threads).  Call from all threads of every block, in uniform control flow.
+template <class T, int NV>
+__device__ bool grid_allreduce(const GridAR& g, unsigned long long& epoch, const T (&v)[NV], T (&out)[NV]) {
+    static_assert(NV >= 1 && NV <= kArMax, "all-reduce width");
+    __shared__ T red[kArMax][32];
+    __shared__ T res[kArMax];
+    __shared__ int st;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    T* part = ar_part<T>(g) + (size_t)(epoch & 1) * gridDim.x * kArMax;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        const T x = warp_sum(v[k]);
+        if (lane == 0) red[k][w] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        T x = T(0);
+        for (int ww = 0; ww < nw; ++ww) x += red[threadIdx.x][ww];
+        part[(size_t)blockIdx.x * kArMax + threadIdx.x] = x;
+    }
+    if (!ar_arrive_wait(g, epoch, &st)) return false;
+    ++epoch;
+    if (w < NV) {
+        T x = T(0);
+        for (unsigned b = lane; b < gridDim.x; b += 32) x += __ldcg(part + (size_t)b * kArMax + w);
+        x = warp_sum(x);
+        if (lane == 0) res[w] = x;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; ++k) out[k] = res[k];
+    return true;
+}
+
+// plain barrier on the same counter
+__device__ __forceinline__ bool grid_sync_ar(const GridAR& g, unsigned long long& epoch) {
+    __shared__ int st;
+    if (!ar_arrive_wait(g, epoch, &st)) return false;
+    ++epoch;
+    return true;
 }
 
 // Slot row of a SELL matrix times the vector given by xload(col), accumulated

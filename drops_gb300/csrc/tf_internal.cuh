@@ -184,7 +184,10 @@ struct Sell {
     int32_t* src = nullptr;  // npad: CSR index or -1 for padding
     double* v64 = nullptr;
     float* v32 = nullptr;
-    int64_t pattern_gen = -1, v64_version = -1, v32_version = -1;
+    float2* v2f = nullptr;   // npad: row-scaled FP64 values as FP32 pairs hi + lo
+    int32_t* rexp = nullptr; // nslices*32: row scale exponent (value = (hi + lo) * 2^rexp)
+    int64_t pattern_gen = -1, v64_version = -1, v32_version = -1, v2f_version = -1;
+    bool v2f_ok = false;     // every value finite (else the pair form is not used)
 };
 
 struct CSR {
@@ -261,11 +264,17 @@ struct Context {
     int64_t launches = 0;
     int last_refinements = 0;  // FP64 residual replacements of the last mixed solve
     int kry_blocks_per_sm = 0; // cap on resident Krylov blocks per SM (0: occupancy limit)
-    int kry_threads = 256;     // block size of the mixed-precision PCG (256 or 512)
+    int kry_threads = 512;     // block size of the mixed-precision PCG (256 or 512)
+    bool pcg_two_barrier = false;  // mixed PCG: classic two-barrier kernel instead of the single-barrier one
+    bool gmres2_master = false;    // CGS2 GMRES: master-block grid steps instead of the all-reduce ones
     int64_t pattern_counter = 0, block_src_gen = -1;
     DBuf<int32_t> sell_ptr[TF_NUM_MATS], sell_col[TF_NUM_MATS], sell_src[TF_NUM_MATS], sell_perm[TF_NUM_MATS];
     DBuf<double> sell_v64[TF_NUM_MATS];
     DBuf<float> sell_v32[TF_NUM_MATS];
+    DBuf<float2> sell_v2f[TF_NUM_MATS];
+    DBuf<int32_t> sell_rexp[TF_NUM_MATS];
+    DBuf<float2> x_pairs;       // SpMV operand split into FP32 pairs
+    bool spmv_pair = false;     // tf_spmv: FP32-pair kernel instead of the FP64-FMA one
     // batch of bricks (tf_mesh_brick_batch); 0 = single mesh
     int batch_count = 0;
     DBuf<BatchBrick> batch_tab;

@@ -55,8 +55,23 @@ def lib():
     return _lib
 
 
+_CT_DTYPE = {C.c_int32: np.int32, C.c_int64: np.int64, C.c_double: np.float64, C.c_float: np.float32,
+             C.c_uint8: np.uint8, C.c_uint16: np.uint16}
+
+
 def _p(a, ct):
-    return a.ctypes.data_as(C.POINTER(ct)) if a is not None else None
+    """Pointer to a's data as ct*; a must already hold ct's type, contiguous (no silent reinterpretation)."""
+    if a is None:
+        return None
+    want = _CT_DTYPE.get(ct)
+    if want is not None and (a.dtype != want or not a.flags["C_CONTIGUOUS"]):
+        raise TypeError(f"oracle argument: expected contiguous {np.dtype(want).name}, got {a.dtype}")
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def _in(a, dtype):
+    """Input array as contiguous dtype (a converted copy is kept alive by the caller's local name)."""
+    return None if a is None else np.ascontiguousarray(a, dtype=dtype)
 
 
 class Mesh:
@@ -102,6 +117,7 @@ def levelset(mesh, kind, par, p2):
 
 def distribute_dofs(mesh, ls_vert, ls_edge, p2, dist=0.0):
     L = lib()
+    ls_vert, ls_edge = _in(ls_vert, np.float64), _in(ls_edge, np.float64)
     na, nd = C.c_int64(), C.c_int64()
     dv = np.empty(mesh.nv, np.int32)
     de = np.empty(mesh.ne, np.int32)
@@ -115,6 +131,7 @@ def distribute_dofs(mesh, ls_vert, ls_edge, p2, dist=0.0):
 
 def numb_on_interface_p1(mesh, ls_vert, ls_edge, omit_bound=-1.0):
     L = lib()
+    ls_vert, ls_edge = _in(ls_vert, np.float64), _in(ls_edge, np.float64)
     na, nd = C.c_int64(), C.c_int64()
     dv = np.empty(mesh.nv, np.int32)
     st = L.orc_numb_on_interface_p1(C.c_int64(mesh.nt), _p(mesh.tet_v, C.c_int32), _p(mesh.tet_e, C.c_int32),
@@ -152,6 +169,7 @@ def make_opts(p2, forms, rhs_kind=RHS_NONE, rhs_par=(), chi=None, degenerate=Fal
     o.rhs_kind = rhs_kind
     for i, v in enumerate(rhs_par):
         o.rhs_par[i] = v
+    chi = _in(chi, np.float64)
     o._chi_keep = chi
     o.chi = _p(chi, C.c_double) if chi is not None else None
     o.degenerate = int(degenerate)
@@ -161,6 +179,8 @@ def make_opts(p2, forms, rhs_kind=RHS_NONE, rhs_par=(), chi=None, degenerate=Fal
 def assemble(mesh, ls_vert, ls_edge, active, dof_vert, dof_edge, m, opts):
     """Returns (status, rowptr, colind, {form: vals}, rhs)."""
     L = lib()
+    ls_vert, ls_edge = _in(ls_vert, np.float64), _in(ls_edge, np.float64)
+    active, dof_vert, dof_edge = _in(active, np.uint8), _in(dof_vert, np.int32), _in(dof_edge, np.int32)
     rowptr = np.empty(m + 1, np.int64)
     colind_p = C.POINTER(C.c_int32)()
     nnz = C.c_int64()
@@ -189,6 +209,9 @@ def spmv(rowptr, colind, vals, x):
     L = lib()
     m = len(rowptr) - 1
     y = np.empty(m, np.float64)
+    rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+    colind = np.ascontiguousarray(colind, dtype=np.int32)
+    vals = np.ascontiguousarray(vals, dtype=np.float64)
     L.orc_spmv(C.c_int64(m), _p(rowptr, C.c_int64), _p(colind, C.c_int32), _p(vals, C.c_double),
                _p(np.ascontiguousarray(x, dtype=np.float64), C.c_double), _p(y, C.c_double))
     return y
@@ -196,6 +219,7 @@ def spmv(rowptr, colind, vals, x):
 
 def pcg_jacobi(rowptr, colind, vals, b, x0=None, max_iter=100000, tol=1e-10, rel=True):
     L = lib()
+    rowptr, colind, vals = _in(rowptr, np.int64), _in(colind, np.int32), _in(vals, np.float64)
     m = len(rowptr) - 1
     x = np.zeros(m) if x0 is None else np.array(x0, dtype=np.float64)
     it = C.c_int(max_iter)
@@ -209,6 +233,7 @@ def pcg_jacobi(rowptr, colind, vals, b, x0=None, max_iter=100000, tol=1e-10, rel
 def gmres_jacobi(rowptr, colind, vals, b, x0=None, restart=50, max_iter=100000, tol=1e-10, rel=True, method=0,
                  block=False):
     L = lib()
+    rowptr, colind, vals = _in(rowptr, np.int64), _in(colind, np.int32), _in(vals, np.float64)
     m = len(rowptr) - 1
     x = np.zeros(m) if x0 is None else np.array(x0, dtype=np.float64)
     it = C.c_int(max_iter)
@@ -221,6 +246,8 @@ def gmres_jacobi(rowptr, colind, vals, b, x0=None, restart=50, max_iter=100000, 
 
 def ch_block(rowptr, colind, M, A, Cn, alpha, mob, rho, eps2, beta):
     L = lib()
+    rowptr, colind = _in(rowptr, np.int64), _in(colind, np.int32)
+    M, A, Cn = _in(M, np.float64), _in(A, np.float64), _in(Cn, np.float64)
     m = len(rowptr) - 1
     nnz = len(colind)
     brp = np.empty(2 * m + 1, np.int64)
@@ -242,6 +269,7 @@ def assemble_legacy_p1(mesh, ls_vert, ls_edge, dof_vert, m, alpha, D, fpar):
     rhs = np.empty(m, np.float64)
     fpar = np.ascontiguousarray(fpar, dtype=np.float64)
     dof_vert = np.ascontiguousarray(dof_vert, dtype=np.int32)
+    ls_vert, ls_edge = _in(ls_vert, np.float64), _in(ls_edge, np.float64)
     st = L.orc_assemble_legacy_p1(C.c_int64(mesh.nt), _p(mesh.tet_v, C.c_int32), _p(mesh.tet_e, C.c_int32),
                                   _p(mesh.coords, C.c_double), _p(ls_vert, C.c_double), _p(ls_edge, C.c_double),
                                   _p(dof_vert, C.c_int32), C.c_int64(m), C.c_double(alpha), C.c_double(D),

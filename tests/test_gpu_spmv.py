@@ -1,0 +1,97 @@
+"""y_Ax (num/spmat.h:1684-1709) through tf_spmv: the FP32-pair kernel and the FP64-FMA kernel against the
+oracle's FP64 product."""
+import os
+
+import numpy as np
+import pytest
+
+import drops_gb300 as tf
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctxs():
+    from drops_gb300 import build
+
+    build.build()
+    native = tf.TraceFEM()
+    os.environ["TF_SPMV_PAIR"] = "1"
+    try:
+        pair = tf.TraceFEM()
+    finally:
+        del os.environ["TF_SPMV_PAIR"]
+    yield pair, native
+    pair.close()
+    native.close()
+
+
+def _spmv(ctx, rp, ci, v, x):
+    ctx.matrix_upload(rp, ci, v)
+    ctx.vec_upload(tf.VEC_X, x)
+    ctx.spmv(tf.MAT_USER, tf.VEC_X, tf.VEC_T0)
+    return ctx.vec_download(tf.VEC_T0)
+
+
+# pair arithmetic carries ~48 significant bits: per product ~3 * 2^-48 relative, summed over the row
+PAIR_REL = 3e-13
+# FP64 FMA chain against the oracle's FP64 sum: a few ulps of sum |a_ij x_j|
+FP64_REL = 4e-15
+
+
+def _check(y, rp, ci, v, x, rel=PAIR_REL):
+    """Per row: |y_i - (A x)_i| <= rel * sum_j |a_ij x_j|."""
+    ref = O.spmv(rp, ci, v, x)
+    mag = O.spmv(rp, ci, np.abs(v), np.abs(x))
+    err = np.abs(y - ref)
+    bound = rel * mag + 1e-300
+    assert np.all(err <= bound), (np.max(err / bound), int(np.argmax(err / bound)))
+    return ref
+
+
+@pytest.mark.parametrize("name,key", [("c1_sphere_p1_n16.npz", "S"), ("sphere_p2_n8.npz", "M"),
+                                      ("torus_p1_n16.npz", "A"), ("torus_p2_n10.npz", "C")])
+def test_spmv_matches_oracle(ctxs, golden, name, key):
+    g = golden(name)
+    rp, ci, v = g["rowptr"], g["colind"], g[key]
+    rng = np.random.default_rng(11)
+    for x in (rng.uniform(-1, 1, len(rp) - 1), g["x"] if "x" in g else rng.standard_normal(len(rp) - 1)):
+        ys = [_spmv(c, rp, ci, v, x) for c in ctxs]
+        _check(ys[0], rp, ci, v, x, PAIR_REL)
+        _check(ys[1], rp, ci, v, x, FP64_REL)
+        # within the 1e-12 parity bound of each other
+        assert np.max(np.abs(ys[0] - ys[1])) <= 1e-12 * max(np.max(np.abs(ys[1])), 1e-300)
+
+
+def test_spmv_wide_range(ctxs):
+    """Row scaling covers rows of any magnitude; x outside [2^-100, 2^100] takes the FP64 path in the same
+    launch; a non-finite matrix value keeps the matrix on the FP64 kernel."""
+    rng = np.random.default_rng(5)
+    m = 3000
+    rp = np.arange(0, 7 * m + 1, 7, dtype=np.int64)
+    ci = np.stack([(np.arange(m) + d) % m for d in (-3, -2, -1, 0, 1, 2, 3)], axis=1).ravel().astype(np.int32)
+    ci = np.sort(ci.reshape(m, 7), axis=1).ravel()
+    v = rng.uniform(-1, 1, 7 * m)
+    scale = 10.0 ** rng.integers(-250, 250, m)  # row magnitudes from 1e-250 to 1e250
+    v *= np.repeat(scale, 7)
+    v[5::97] *= 1e-20  # entries tiny relative to their row
+    x = rng.uniform(-1, 1, m)
+    pair, native = ctxs
+    _check(_spmv(pair, rp, ci, v, x), rp, ci, v, x, PAIR_REL)
+    _check(_spmv(native, rp, ci, v, x), rp, ci, v, x, FP64_REL)
+    # x out of the pair range: the flag sends the launch down the FP64 path (bitwise the FP64 kernel)
+    x2 = x.copy()
+    x2[::500] = 1e-200
+    x2[7] = 1e40
+    y = _spmv(pair, rp, ci, v, x2)
+    _check(y, rp, ci, v, x2, FP64_REL)
+    assert np.array_equal(y, _spmv(native, rp, ci, v, x2))
+    # a non-finite value: the FP64 kernel, whose IEEE result the oracle reproduces
+    v3 = v.copy()
+    v3[100] = np.inf
+    y = _spmv(pair, rp, ci, v3, x)
+    ref = O.spmv(rp, ci, v3, x)
+    assert np.array_equal(np.isfinite(y), np.isfinite(ref))
+    fin = np.isfinite(ref)
+    assert np.all(np.abs(y[fin] - ref[fin]) <= FP64_REL * O.spmv(rp, ci, np.abs(v3), np.abs(x))[fin])
