@@ -151,6 +151,19 @@ def pcg_bytes(m, nnz, iters, fp32):
     return iters * ((vb + 4) * nnz + 4 * (m + 1) + 12 * vb * m)
 
 
+def spmv_cold(ctx, tf, m, nnz):
+    """Standalone FP64 SpMV (y_Ax) on the system matrix, L2 flushed before each of 20 launches; the library
+    queues (flush, event, kernel, event) back to back, so the events bracket the kernel alone.  Beside it, the
+    streaming floor: a plain coalesced read of the same byte count, timed the same way."""
+    t = float(np.median(ctx.spmv_timed(tf.MAT_SYS, tf.VEC_X, tf.VEC_T0, reps=20, cold=True)))
+    b = 12 * nnz + 4 * (m + 1) + 16 * m
+    floor = float(np.median(ctx.stream_read_timed(b, reps=20, cold=True)))
+    return {"ms": round(t, 4), "bytes": b, "achieved_gbs": round(b / (t / 1e3) / 1e9, 1),
+            "stream_read_same_bytes_ms": round(floor, 4), "frac_of_stream_read": round(floor / t, 4),
+            "bytes_model": "12*nnz + 4*(m+1) + 16*m (FP64 values + int32 columns, row pointers, x read, y written)",
+            "timing": "median of 20 launches, L2 flushed before each, CUDA events on the library stream"}
+
+
 def run_ours(args, rank, ws, dist):
     import drops_gb300 as tf
 
@@ -235,17 +248,23 @@ def run_ours(args, rank, ws, dist):
         solve[name] = {"ms": ctx.elapsed_ms(4, 5), "iters": it, "resid": res}
 
     # ---- standalone FP64 SpMV (y_Ax) on the system matrix, cold L2 ---------
-    spmv_ms = []
-    for _ in range(10):
-        ctx.flush_l2()
-        ctx.marker(6)
-        ctx.spmv(tf.MAT_SYS, tf.VEC_X, tf.VEC_T0)
-        ctx.marker(7)
-        spmv_ms.append(ctx.elapsed_ms(6, 7))
-    spmv_t = statistics.median(spmv_ms)
-    spmv_bytes = 12 * state["nnz"] + 4 * (state["m"] + 1) + 16 * state["m"]
-    spmv = {"ms": round(spmv_t, 4), "bytes": spmv_bytes, "achieved_gbs": round(spmv_bytes / (spmv_t / 1e3) / 1e9, 1),
-            "bytes_model": "12*nnz + 4*(m+1) + 16*m (FP64 values + int32 columns, row pointers, x read, y written)"}
+    spmv = spmv_cold(ctx, tf, state["m"], state["nnz"])
+    # the same kernel on the P2 system of twice the resolution (4x the bytes),
+    # where the launch ramp weighs less
+    if args.size == N_CUBES and not args.no_large_spmv:
+        big = tf.TraceFEM(dev)
+        nb = 2 * N_CUBES
+        big.brick_cube(nb, HALF)
+        big.levelset_analytic(tf.LS_SPHERE, SPHERE, p2=True)
+        _, mb = big.distribute_dofs(tf.P2IF)
+        nnzb = big.setup_fe_system(forms, tf.RHS_NONE, [])
+        big.lincomb(forms, [1.0, 1.0, 2 * HALF / nb])
+        big.vec_fill(tf.VEC_X, mb, 1.0)
+        spmv_big = spmv_cold(big, tf, mb, nnzb)
+        spmv_big["system"] = f"P2 sphere {nb}^3 cubes: m={mb}, nnz={nnzb}"
+        big.close()
+    else:
+        spmv_big = None
 
     # ---- roofline of the dominant kernel ------------------------------------
     dom = max(ktimes, key=lambda k: ktimes[k][0])
@@ -256,7 +275,9 @@ def run_ours(args, rank, ws, dist):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    spmv["frac"] = round(spmv["achieved_gbs"] / hbm_peak, 4)
+    for sp in (spmv, spmv_big):
+        if sp:
+            sp["frac"] = round(sp["achieved_gbs"] / hbm_peak, 4)
     ms_d, n_d = ktimes[dom]
     na, m, nnz = state["na"], state["m"], state["nnz"]
     if dom == "pcg":
@@ -286,6 +307,7 @@ def run_ours(args, rank, ws, dist):
         "problem": {"tets": nt, "cut_tets": na, "dofs": m, "nnz": nnz, "pcg_iters_inner": state["it"]},
         "solve_ms": solve,
         "spmv_fp64_cold": spmv,
+        "spmv_fp64_cold_2x": spmv_big,
         "kernel_ms": {k: round(v[0] / args.steps, 4) for k, v in ktimes.items() if v[1]},
     }
     ctx.close()
@@ -640,6 +662,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-large-spmv", action="store_true", help="skip the SpMV timing on the 192^3 system")
     ap.add_argument("--size", type=int, default=N_CUBES, help="cubes per direction (96 = the benchmark workload; "
                     "smaller sizes are for profiling captures)")
     ap.add_argument("--workload", default="poisson", choices=["poisson", "batch", "ch"],

@@ -47,7 +47,7 @@ EXPORTS = [
     "tf_mesh_brick_batch", "tf_levelset_analytic_batch", "tf_batch_info", "tf_batch_lincomb", "tf_batch_pcg_jacobi",
     "tf_batch_tune", "tf_batch_config", "tf_mlp_init", "tf_mlp_get_weights", "tf_mlp_set_weights", "tf_mlp_forward",
     "tf_mlp_gradient", "tf_mlp_train", "tf_ch_features", "tf_ch_steps_learned", "tf_gmres_options", "tf_timing_enable",
-    "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2",
+    "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2", "tf_spmv_timed", "tf_stream_read_timed",
     "tf_host_alloc", "tf_host_free",
 ]
 
@@ -457,6 +457,20 @@ class TraceFEM:
 
     def flush_l2(self):
         self._check(self.L.tf_flush_l2(self.h))
+
+    def stream_read_timed(self, nbytes, reps=10, cold=True):
+        """Device time (ms) of each of `reps` coalesced reads of nbytes (the streaming floor of that size)."""
+        out = np.zeros(reps, dtype=np.float32)
+        self._check(self.L.tf_stream_read_timed(self.h, C.c_int64(int(nbytes)), C.c_int(reps), C.c_int(int(cold)),
+                                                out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def spmv_timed(self, mat, vec_x, vec_y, reps=10, cold=True):
+        """Device time (ms) of each of `reps` SpMV calls, L2 flushed before each when `cold`."""
+        out = np.zeros(reps, dtype=np.float32)
+        self._check(self.L.tf_spmv_timed(self.h, C.c_int(mat), C.c_int(vec_x), C.c_int(vec_y), C.c_int(reps),
+                                         C.c_int(int(cold)), out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
 
 
 class PinnedArray:

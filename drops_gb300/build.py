@@ -40,7 +40,8 @@ def _stale(obj, deps):
 
 def build(force=False, verbose=False, extra=()):
     os.makedirs(OUT, exist_ok=True)
-    headers = [os.path.join(SRC, "tf_internal.cuh"), os.path.join(HERE, "..", "include", "tracefem.h")]
+    headers = [os.path.join(SRC, h) for h in sorted(os.listdir(SRC)) if h.endswith(".cuh")]
+    headers.append(os.path.join(HERE, "..", "include", "tracefem.h"))
     jobs = []
     for u in UNITS:
         src = os.path.join(SRC, u)

@@ -1,6 +1,7 @@
 // extern "C" entry points of libtracefem (include/tracefem.h).
 #include <cstdlib>
 #include <cstring>
+#include <vector>
 
 #include "tf_internal.cuh"
 
@@ -23,6 +24,24 @@ static int mat_need(Context* c, int mat) {
     if (mat < 0 || mat >= TF_NUM_MATS) return tf::set_err(c, TF_ERR_BAD_INPUT, "bad matrix handle");
     if (!c->mats[mat].vals) return tf::set_err(c, TF_ERR_BAD_INPUT, "matrix handle holds no matrix");
     return TF_OK;
+}
+
+// Coalesced read of n16 16-byte words, four independent loads in flight per
+// thread; the xor of everything read keeps the loads live.
+__global__ void k_stream_read(const uint4* __restrict__ p, int64_t n16, unsigned* sink) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    unsigned acc = 0;
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n16; i += 4 * stride) {
+        const uint4 a = __ldg(p + i), b = __ldg(p + i + stride), c = __ldg(p + i + 2 * stride),
+                    d = __ldg(p + i + 3 * stride);
+        acc ^= a.x ^ a.y ^ a.z ^ a.w ^ b.x ^ b.y ^ b.z ^ b.w ^ c.x ^ c.y ^ c.z ^ c.w ^ d.x ^ d.y ^ d.z ^ d.w;
+    }
+    for (; i < n16; i += stride) {
+        const uint4 a = __ldg(p + i);
+        acc ^= a.x ^ a.y ^ a.z ^ a.w;
+    }
+    if (acc == 0x9e3779b9u) *sink = acc;
 }
 
 extern "C" {
@@ -64,6 +83,10 @@ int tf_create(tf_context** out, int device) {
     if (const char* e = std::getenv("TF_KRY_THREADS")) c->kry_threads = std::atoi(e);
     if (const char* e = std::getenv("TF_PCG_TWO_BARRIER")) c->pcg_two_barrier = std::atoi(e) != 0;
     if (const char* e = std::getenv("TF_SPMV_PAIR")) c->spmv_pair = std::atoi(e) != 0;
+    if (const char* e = std::getenv("TF_SPMV_SELL")) c->spmv_sell = std::atoi(e) != 0;
+    if (const char* e = std::getenv("TF_SPMV_BLOCKS_PER_SM")) c->spmv_blocks_per_sm = std::atoi(e);
+    if (const char* e = std::getenv("TF_PCG_BLOCKED")) c->pcg_blocked = std::atoi(e) != 0;
+    if (const char* e = std::getenv("TF_SPMV_THREADS")) c->spmv_threads = std::atoi(e);
     if (const char* e = std::getenv("TF_GMRES2_MASTER")) c->gmres2_master = std::atoi(e) != 0;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
@@ -167,6 +190,7 @@ int tf_destroy(tf_context* t) {
     tf::release(c->gm2_v64);
     tf::release(c->gm2_binv);
     tf::release(c->flush_buf);
+    tf::release(c->stream_buf);
     for (auto& e : c->markers)
         if (e) cudaEventDestroy(e);
     if (c->h_status) cudaFreeHost(c->h_status);
@@ -509,6 +533,81 @@ int tf_spmv(tf_context* t, int mat, int vec_x, int vec_y) {
     TF_TRY(tf::ensure(c, c->vecs[vec_y], (size_t)A.m));
     TF_TRY(tf::spmv(c, A, c->vecs[vec_x].p, c->vecs[vec_y].p));
     TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TF_OK;
+}
+
+int tf_spmv_timed(tf_context* t, int mat, int vec_x, int vec_y, int reps, int cold, float* ms_each) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (reps < 1 || reps > 1024 || !ms_each) return tf::set_err(c, TF_ERR_BAD_INPUT, "spmv_timed: reps in [1, 1024]");
+    TF_TRY(mat_need(c, mat));
+    TF_TRY(vec_need(c, vec_x));
+    TF_TRY(vec_need(c, vec_y));
+    const tf::CSR& A = c->mats[mat];
+    if ((int64_t)c->vecs[vec_x].n != A.m) return tf::set_err(c, TF_ERR_BAD_INPUT, "spmv: x has the wrong size");
+    TF_TRY(tf::ensure(c, c->vecs[vec_y], (size_t)A.m));
+    size_t fbytes = 0;
+    if (cold) {
+        int l2 = 0;
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c->device);
+        fbytes = 2 * (size_t)(l2 > 0 ? l2 : (128 << 20));
+        TF_TRY(tf::ensure(c, c->flush_buf, fbytes));
+    }
+    // first call builds the layout (not timed)
+    TF_TRY(tf::spmv(c, A, c->vecs[vec_x].p, c->vecs[vec_y].p));
+    std::vector<cudaEvent_t> ev(2 * (size_t)reps);
+    for (auto& e : ev) TF_CUDA(c, cudaEventCreate(&e));
+    const int timing = c->timing;
+    c->timing = 0;
+    int st = TF_OK;
+    // Everything is queued without a host wait, so the device never idles
+    // between the flush, the start event and the kernel.
+    for (int r = 0; r < reps && st == TF_OK; ++r) {
+        if (cold) cudaMemsetAsync(c->flush_buf.p, r & 0xff, fbytes, c->stream);
+        cudaEventRecord(ev[2 * r], c->stream);
+        st = tf::spmv(c, A, c->vecs[vec_x].p, c->vecs[vec_y].p);
+        cudaEventRecord(ev[2 * r + 1], c->stream);
+    }
+    c->timing = timing;
+    const cudaError_t e = cudaStreamSynchronize(c->stream);
+    for (int r = 0; r < reps && st == TF_OK && e == cudaSuccess; ++r)
+        cudaEventElapsedTime(ms_each + r, ev[2 * r], ev[2 * r + 1]);
+    for (auto& x : ev) cudaEventDestroy(x);
+    TF_CUDA(c, e);
+    return st;
+}
+
+int tf_stream_read_timed(tf_context* t, int64_t bytes, int reps, int cold, float* ms_each) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (reps < 1 || reps > 1024 || !ms_each || bytes < 16 || bytes > ((int64_t)1 << 34))
+        return tf::set_err(c, TF_ERR_BAD_INPUT, "stream_read_timed: reps in [1, 1024], bytes in [16, 2^34]");
+    const int64_t n16 = bytes / 16;
+    TF_TRY(tf::ensure(c, c->stream_buf, (size_t)n16));
+    TF_CUDA(c, cudaMemsetAsync(c->stream_buf.p, 0, (size_t)n16 * 16, c->stream));
+    size_t fbytes = 0;
+    if (cold) {
+        int l2 = 0;
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c->device);
+        fbytes = 2 * (size_t)(l2 > 0 ? l2 : (128 << 20));
+        TF_TRY(tf::ensure(c, c->flush_buf, fbytes));
+    }
+    const int grid = c->num_sms * 8;
+    std::vector<cudaEvent_t> ev(2 * (size_t)reps);
+    for (auto& e : ev) TF_CUDA(c, cudaEventCreate(&e));
+    for (int r = 0; r < reps; ++r) {
+        if (cold) cudaMemsetAsync(c->flush_buf.p, r & 0xff, fbytes, c->stream);
+        cudaEventRecord(ev[2 * r], c->stream);
+        k_stream_read<<<grid, 256, 0, c->stream>>>(c->stream_buf.p, n16, (unsigned*)c->status.p + 3);
+        cudaEventRecord(ev[2 * r + 1], c->stream);
+    }
+    const cudaError_t e = cudaStreamSynchronize(c->stream);
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) cudaEventElapsedTime(ms_each + r, ev[2 * r], ev[2 * r + 1]);
+    for (auto& x : ev) cudaEventDestroy(x);
+    tf::release(c->stream_buf);
+    TF_CUDA(c, e);
     return TF_OK;
 }
 

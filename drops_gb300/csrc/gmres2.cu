@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres2(Gm2Args<V> a) {
         {
             double v[2] = {0., 0.};
             const double* x = a.x;
-            TF_SLICE_LOOP(a.nslices, sl) {
+            TF_SLICE_LOOP_BAL(a.nslices, sl) {
                 const double ax = sell_row<double>(a.ptr, a.col, a.aval, sl, lane, [&](int32_t j) { return kld(x + j); });
                 const int32_t row = __ldg(a.perm + sl * 32 + lane);
                 if (row >= 0) {
@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres2(Gm2Args<V> a) {
             for (int k = threadIdx.x; k <= i; k += blockDim.x)
                 for (int w = 0; w < kGm2Warps; ++w) wred[k][w] = V(0);
             __syncthreads();
-            TF_SLICE_LOOP(a.nslices, sl) {
+            TF_SLICE_LOOP_BAL(a.nslices, sl) {
                 const V acc = sell_row<V>(a.ptr, a.col, a.bval, sl, lane, [&](int32_t j) { return sci * kld(Vi + j); });
                 const int32_t row = __ldg(a.perm + sl * 32 + lane);
                 if (row >= 0) W[row] = acc;

@@ -27,6 +27,7 @@ namespace tf {
 // SELL-32-sigma layout and SpMV (y_Ax, num/spmat.h:1684-1709)
 // ---------------------------------------------------------------------------
 constexpr int kSigma = 512;  // rows sorted by length inside windows of 512
+static_assert(kSigma / 32 == kSellWinSlices, "slice order of the persistent kernels assumes 16 slices per window");
 
 // one block of kSigma threads per window: bitonic sort of (descending length, row)
 __global__ void __launch_bounds__(kSigma) k_sell_sort(int64_t m, const int32_t* __restrict__ rowptr,
@@ -174,6 +175,49 @@ __global__ void k_spmv(int64_t nslices, const int32_t* __restrict__ perm, const 
         const int32_t row = perm[s * 32 + lane];
         if (row >= 0) y[row] = a;
     }
+}
+
+// ---------------------------------------------------------------------------
+// Balanced SELL SpMV (the standalone y_Ax).  Block b takes the slices
+// [b n/B, (b+1) n/B) of the n slices (B = blocks, a multiple of the SM count,
+// so every SM gets the same share) and its warps split the block's column
+// work evenly (sell_block_balanced): about 3 gather rounds per warp for the
+// P2 matrices instead of the 8 of a 62-wide slice walked by one warp.  FP64
+// multiply-adds only on stored entries (one warp instruction per 32 products;
+// GB300 issues FP64 at ~1/64 of the FP32 rate, so the FP64 pipe and HBM bound
+// this kernel about equally).  Bytes: 12 per stored entry + perm, ptr, x
+// gathered, y written.
+// ---------------------------------------------------------------------------
+template <int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_spmv_bal(int64_t nslices, const int32_t* __restrict__ perm,
+                                                 const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                                                 const double* __restrict__ val, const double* __restrict__ x,
+                                                 double* __restrict__ y) {
+    __shared__ BalShared<NT / 32, double> sh;
+    const int lane = threadIdx.x & 31;
+    const int64_t s0 = (int64_t)blockIdx.x * nslices / gridDim.x;
+    const int64_t s1 = (int64_t)(blockIdx.x + 1) * nslices / gridDim.x;
+    sell_block_balanced<NT / 32, double>(
+        sh, ptr, col, val, s0, (int)(s1 - s0), [&](int32_t j) { return __ldg(x + j); },
+        [&](int64_t s, double v) {
+            const int32_t row = __ldg(perm + s * 32 + lane);
+            if (row >= 0) y[row] = v;
+        });
+}
+
+static void launch_spmv_bal(Context* c, const CSR& A, const double* x, double* y) {
+    const int64_t ns = A.sell.nslices;
+    const int per_sm = c->spmv_blocks_per_sm > 0 ? c->spmv_blocks_per_sm : 2;
+    int64_t nb = (int64_t)c->num_sms * per_sm;
+    const int64_t need = (ns + kBalMaxSlices - 1) / kBalMaxSlices;  // at most kBalMaxSlices slices per block
+    if (nb < need) nb = need;
+    if (nb > ns) nb = ns;
+    if (nb < 1) nb = 1;
+    if (c->spmv_threads == 256)
+        k_spmv_bal<256><<<(unsigned)nb, 256, 0, c->stream>>>(ns, A.sell.perm, A.sell.ptr, A.sell.col, A.sell.v64, x, y);
+    else
+        k_spmv_bal<512><<<(unsigned)nb, 512, 0, c->stream>>>(ns, A.sell.perm, A.sell.ptr, A.sell.col, A.sell.v64, x, y);
+    ++c->launches;
 }
 
 // ---------------------------------------------------------------------------
@@ -329,6 +373,12 @@ static int ensure_sell_pair(Context* c, CSR& A) {
 int spmv(Context* c, const CSR& Ac, const double* x, double* y) {
     CSR& A = const_cast<CSR&>(Ac);
     TF_TRY(ensure_sell(c, A, false));
+    if (!c->spmv_pair && !c->spmv_sell) {
+        TimedLaunch tl(c, TF_K_SPMV);
+        launch_spmv_bal(c, A, x, y);
+        TF_CUDA(c, cudaGetLastError());
+        return TF_OK;
+    }
     if (c->spmv_pair) TF_TRY(ensure_sell_pair(c, A));
     TimedLaunch tl(c, TF_K_SPMV);
     if (!c->spmv_pair || !A.sell.v2f_ok) {
@@ -529,7 +579,7 @@ __global__ void __launch_bounds__(kKryThreads, sizeof(T) == 4 ? 4 : 3) k_pcg(Pcg
     {
         double v[3] = {0., 0., 0.};
         const T* x = a.x;
-        TF_SLICE_LOOP(a.nslices, s) {
+        TF_SLICE_LOOP_BAL(a.nslices, s) {
             const T ax = sell_row<T>(a.ptr, a.col, a.val, s, lane, [&](int32_t j) { return kld(x + j); });
             const int32_t row = __ldg(a.perm + s * 32 + lane);
             if (row >= 0) {
@@ -569,7 +619,7 @@ __global__ void __launch_bounds__(kKryThreads, sizeof(T) == 4 ? 4 : 3) k_pcg(Pcg
             const T* z = a.z;
             const T* po = pc;
             T acc1 = T(0);
-            TF_SLICE_LOOP(a.nslices, s) {
+            TF_SLICE_LOOP_BAL(a.nslices, s) {
                 const T acc = sell_row<T>(a.ptr, a.col, a.val, s, lane,
                                           [&](int32_t j) { return kld(z + j) + beta * kld(po + j); });
                 const int32_t row = __ldg(a.perm + s * 32 + lane);
@@ -680,7 +730,7 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_mixed(PcgMixedArg
     auto true_residual = [&](bool first) {
         double v[3] = {0., 0., 0.};
         const double* x = a.x;
-        TF_SLICE_LOOP(a.nslices, s) {
+        TF_SLICE_LOOP_BAL(a.nslices, s) {
             const double ax = sell_row<double>(a.ptr, a.col, a.val64, s, lane, [&](int32_t j) { return kld(x + j); });
             const int32_t row = __ldg(a.perm + s * 32 + lane);
             if (row >= 0) {
@@ -724,7 +774,7 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_mixed(PcgMixedArg
             float v[1] = {0.f};
             const float* z = a.z;
             const float* po = pc;
-            TF_SLICE_LOOP(a.nslices, s) {
+            TF_SLICE_LOOP_BAL(a.nslices, s) {
                 const float acc = sell_row<float>(a.ptr, a.col, a.val32, s, lane,
                                                   [&](int32_t j) { return kld(z + j) + beta * kld(po + j); });
                 const int32_t row = __ldg(a.perm + s * 32 + lane);
@@ -842,7 +892,7 @@ __device__ __forceinline__ float cg1_u(float4 v, float alpha, float beta) {
     return __fmul_rn(cg1_r(v, cg1_s(v, beta), alpha), v.w);
 }
 
-template <int NT>
+template <int NT, bool BLK>
 __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_cg1(PcgCg1Args a) {
     const int lane = threadIdx.x & 31;
     unsigned long long epoch = 0;
@@ -860,7 +910,7 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_cg1(PcgCg1Args a)
     auto true_residual = [&](bool first, bool& done) -> bool {
         double v[2] = {0., 0.};
         const double* x = a.x;
-        TF_SLICE_LOOP(a.nslices, s) {
+        TF_SLICE_LOOP_BAL(a.nslices, s) {
             const double ax = sell_row<double>(a.ptr, a.col, a.val64, s, lane, [&](int32_t j) { return kld(x + j); });
             const int32_t row = __ldg(a.perm + s * 32 + lane);
             if (row >= 0) {
@@ -910,17 +960,10 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_cg1(PcgCg1Args a)
 
     // one SpMV pass; refresh: w = A (r / d) and s = A p with r, p kept (after
     // a true residual), else the CG step with (alpha, beta)
-    auto pass = [&](bool refresh, float (&o)[6]) -> bool {
-        float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        const float al = refresh ? 0.f : alpha, be = refresh ? 0.f : beta;
-        const float4* V = Vc;
-        TF_SLICE_LOOP(a.nslices, s) {
-            const float wn =
-                sell_row<float>(a.ptr, a.col, a.val32, s, lane, [&](int32_t j) { return cg1_u(kld(V + j), al, be); });
-            // refresh: s = A p recomputed, ending the drift of its recurrence
-            const float sx = refresh ? sell_row<float>(a.ptr, a.col, a.val32, s, lane,
-                                                       [&](int32_t j) { return kld(a.P + j); })
-                                     : 0.f;
+    // row update of slot (s, lane) from its products wn = (A u)_row and, on
+    // a refresh, sx = (A p)_row
+    auto row_update = [&](int64_t s, float wn, float sx, bool refresh, float al, float be, const float4* V,
+                          float (&v)[6]) {
             const int32_t row = __ldg(a.perm + s * 32 + lane);
             if (row >= 0) {
                 const float4 vc = V[row];
@@ -945,6 +988,46 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_cg1(PcgCg1Args a)
                 v[4] += pn * sn;
                 v[5] += rn * rn;
             }
+    };
+
+    // Blocked pass: block b owns the contiguous slices [b n/G, (b+1) n/G)
+    // (neighbouring rows, so the state gathers of an SM share its L1), splits
+    // their column work evenly over its warps (sell_block_balanced), keeps the
+    // row products in shared memory and then updates its rows.  The other form
+    // walks whole slices per warp in the balanced global order.
+    __shared__ BalShared<NT / 32, float> bsh;
+    __shared__ float wsm[BLK ? kBalMaxSlices : 1][32], ssm[BLK ? kBalMaxSlices : 1][32];
+    auto pass = [&](bool refresh, float (&o)[6]) -> bool {
+        float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        const float al = refresh ? 0.f : alpha, be = refresh ? 0.f : beta;
+        const float4* V = Vc;
+        if constexpr (BLK) {
+            const int64_t sb0 = (int64_t)blockIdx.x * a.nslices / gridDim.x;
+            const int64_t sb1 = (int64_t)(blockIdx.x + 1) * a.nslices / gridDim.x;
+            for (int64_t c0 = sb0; c0 < sb1; c0 += kBalMaxSlices) {
+                const int S = (int)(sb1 - c0 < kBalMaxSlices ? sb1 - c0 : kBalMaxSlices);
+                sell_block_balanced<NT / 32, float>(
+                    bsh, a.ptr, a.col, a.val32, c0, S, [&](int32_t j) { return cg1_u(kld(V + j), al, be); },
+                    [&](int64_t s, float val) { wsm[s - c0][lane] = val; });
+                // refresh: s = A p recomputed, ending the drift of its recurrence
+                if (refresh)
+                    sell_block_balanced<NT / 32, float>(
+                        bsh, a.ptr, a.col, a.val32, c0, S, [&](int32_t j) { return kld(a.P + j); },
+                        [&](int64_t s, float val) { ssm[s - c0][lane] = val; });
+                // (the next chunk overwrites wsm only after the first block
+                // barrier inside sell_block_balanced, i.e. after this loop)
+                for (int i = threadIdx.x >> 5; i < S; i += NT / 32)
+                    row_update(c0 + i, wsm[i][lane], refresh ? ssm[i][lane] : 0.f, refresh, al, be, V, v);
+            }
+        } else {
+            TF_SLICE_LOOP_BAL(a.nslices, s) {
+                const float wn = sell_row<float>(a.ptr, a.col, a.val32, s, lane,
+                                                 [&](int32_t j) { return cg1_u(kld(V + j), al, be); });
+                const float sx = refresh ? sell_row<float>(a.ptr, a.col, a.val32, s, lane,
+                                                           [&](int32_t j) { return kld(a.P + j); })
+                                         : 0.f;
+                row_update(s, wn, sx, refresh, al, be, V, v);
+            }
         }
         if (!grid_allreduce<float, 6>(a.g, epoch, v, o)) return false;
         float4* t = Vc;
@@ -955,7 +1038,7 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_cg1(PcgCg1Args a)
 
     // FP64 fold of the FP32 correction (own rows), then a barrier
     auto fold = [&]() -> bool {
-        TF_SLICE_LOOP(a.nslices, s) {
+        TF_SLICE_LOOP_BAL(a.nslices, s) {
             const int32_t row = __ldg(a.perm + s * 32 + lane);
             if (row >= 0) {
                 a.x[row] += (double)a.dx[row];
@@ -1081,7 +1164,8 @@ static int run_pcg_cg1(Context* c, const CSR& A, const double* b, double* x, int
     k_to_f32<<<grid_for(c, m), kBlock, 0, c->stream>>>(m, A.diag, d32);
     ++c->launches;
     const int nt = c->kry_threads == 512 ? 512 : 256;
-    const void* fn = nt == 512 ? (const void*)k_pcg_cg1<512> : (const void*)k_pcg_cg1<256>;
+    const void* fn = c->pcg_blocked ? (nt == 512 ? (const void*)k_pcg_cg1<512, true> : (const void*)k_pcg_cg1<256, true>)
+                                    : (nt == 512 ? (const void*)k_pcg_cg1<512, false> : (const void*)k_pcg_cg1<256, false>);
     int blocks = 0;
     TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks, nt));
     const size_t part_d = (size_t)2 * blocks * kArMax;
@@ -1260,7 +1344,7 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres(GmresArgs a) {
         double* pp = P();
         double v[2] = {0., 0.};
         const double* x0 = a.x;
-        TF_SLICE_LOOP(a.nslices, sl) {
+        TF_SLICE_LOOP_BAL(a.nslices, sl) {
             const double ax = sell_row<double>(a.ptr, a.col, a.val, sl, lane, [&](int32_t j) { return kld(x0 + j); });
             const int32_t row = __ldg(a.perm + sl * 32 + lane);
             if (row >= 0) {
@@ -1320,7 +1404,7 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres(GmresArgs a) {
                     const bool left = a.left;
                     const double* dg = a.diag;
                     const double* Zp = a.binv ? a.Z : nullptr;
-                    TF_SLICE_LOOP(a.nslices, s2) {
+                    TF_SLICE_LOOP_BAL(a.nslices, s2) {
                         double acc = sell_row<double>(a.ptr, a.col, a.val, s2, lane, [&](int32_t j) {
                             if (Zp) return kld(Zp + j);
                             const double vj = sci * kld(Vi + j);
@@ -1434,7 +1518,7 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres(GmresArgs a) {
                 double* pq = P();
                 double v1[1] = {0.};
                 const double* x1 = a.x;
-                TF_SLICE_LOOP(a.nslices, s3) {
+                TF_SLICE_LOOP_BAL(a.nslices, s3) {
                     const double ax = sell_row<double>(a.ptr, a.col, a.val, s3, lane, [&](int32_t j) { return kld(x1 + j); });
                     const int32_t row = __ldg(a.perm + s3 * 32 + lane);
                     if (row >= 0) {

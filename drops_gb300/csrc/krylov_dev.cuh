@@ -369,19 +369,20 @@ __device__ __forceinline__ bool grid_sync_ar(const GridAR& g, unsigned long long
     return true;
 }
 
-// Slot row of a SELL matrix times the vector given by xload(col), accumulated
-// in T.  The row is walked in blocks of eight, the last block masked (the
-// slice width is the same for all 32 lanes, so the mask is warp-uniform): the
-// column indices and values of the next block are loaded while the gathers of
-// the current block are in flight, so a lane keeps up to 16 independent loads
-// outstanding and a row of w entries costs ceil(w/8) gather latencies.  Terms
-// are summed in CSR order; masked terms add +0.
+// Slot row of a SELL matrix times the vector given by xload(col), over the
+// slice columns [c0, c0 + n), accumulated in T.  The columns are walked in
+// blocks of eight: the column indices and values of the next block are loaded
+// while the gathers of the current block are in flight, so a lane keeps up to
+// 16 independent loads outstanding and n columns cost ceil(n/8) gather
+// latencies.  Loads past n are masked and the multiply-adds past n are
+// skipped (n is warp-uniform, so no FP64 pipe time goes to padding).  Terms
+// are summed in CSR order.
 template <class T, class XL>
-__device__ __forceinline__ T sell_row(const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
-                                      const T* __restrict__ val, int64_t s, int lane, XL xload) {
+__device__ __forceinline__ T sell_row_range(const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                                            const T* __restrict__ val, int64_t s, int lane, int32_t c0, int32_t n,
+                                            XL xload) {
     constexpr int U = 8;
-    const int32_t p0 = __ldg(ptr + s);
-    const int32_t w = (__ldg(ptr + s + 1) - p0) >> 5;
+    const int32_t p0 = __ldg(ptr + s) + 32 * c0;
     const int32_t* cp = col + p0 + lane;
     const T* vp = val + p0 + lane;
     T acc = T(0);
@@ -389,11 +390,11 @@ __device__ __forceinline__ T sell_row(const int32_t* __restrict__ ptr, const int
     T vn[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-        const bool in = u < w;
+        const bool in = u < n;
         cn[u] = in ? __ldg(cp + 32 * u) : -1;
         vn[u] = in ? __ldg(vp + 32 * u) : T(0);
     }
-    for (int32_t k = 0; k < w; k += U) {
+    for (int32_t k = 0; k < n; k += U) {
         T xv[U], vv[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
@@ -401,23 +402,142 @@ __device__ __forceinline__ T sell_row(const int32_t* __restrict__ ptr, const int
             vv[u] = vn[u];
         }
         const int32_t kn = k + U;
-        if (kn < w) {
+        if (kn < n) {
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                const bool in = kn + u < w;
+                const bool in = kn + u < n;
                 cn[u] = in ? __ldg(cp + 32 * (kn + u)) : -1;
                 vn[u] = in ? __ldg(vp + 32 * (kn + u)) : T(0);
             }
         }
 #pragma unroll
-        for (int u = 0; u < U; ++u) acc += vv[u] * xv[u];
+        for (int u = 0; u < U; ++u)
+            if (k + u < n) acc += vv[u] * xv[u];
     }
     return acc;
+}
+
+// the whole slot row (all columns of slice s)
+template <class T, class XL>
+__device__ __forceinline__ T sell_row(const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                                      const T* __restrict__ val, int64_t s, int lane, XL xload) {
+    const int32_t w = (__ldg(ptr + s + 1) - __ldg(ptr + s)) >> 5;
+    return sell_row_range<T>(ptr, col, val, s, lane, 0, w, xload);
+}
+
+// ---------------------------------------------------------------------------
+// Balanced SELL product of one block.  The block takes the slices [s0, s1)
+// (at most kBalMaxSlices) and splits their total column count T evenly over
+// its NW warps: warp j walks the column positions [jT/NW, (j+1)T/NW) of the
+// concatenated slices, so a wide slice is shared by several warps and every
+// warp walks about T/NW columns (the gather chain of the slowest warp no
+// longer follows the widest slice).  A slice that lies wholly inside one warp's
+// range is emitted by that warp; a split slice's partial sums go to shared
+// memory and the warp holding its last column adds them in column order
+// (deterministic).  emit(slice, value) is called by all 32 lanes of a warp;
+// zero-width slices (empty rows) are emitted too.  All threads of the block
+// must call this, in uniform control flow; it ends with a block barrier, so
+// what emit wrote to shared memory can be read right after.
+// ---------------------------------------------------------------------------
+constexpr int kBalMaxSlices = 64;
+
+template <int NW, class T>
+struct BalShared {
+    int32_t P[kBalMaxSlices + 1];
+    T tail[NW][32];
+};
+
+template <int NW, class T, class XL, class EMIT>
+__device__ __forceinline__ void sell_block_balanced(BalShared<NW, T>& sh, const int32_t* __restrict__ ptr,
+                                                    const int32_t* __restrict__ col, const T* __restrict__ val,
+                                                    int64_t s0, int S, XL xload, EMIT emit) {
+    const int lane = threadIdx.x & 31, j = threadIdx.x >> 5;
+    if (j == 0) {
+        int carry = 0;
+        for (int b = 0; b < S; b += 32) {
+            const int i = b + lane;
+            int w = i < S ? (__ldg(ptr + s0 + i + 1) - __ldg(ptr + s0 + i)) >> 5 : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += t;
+            }
+            if (i < S) sh.P[i + 1] = carry + w;
+            carry += __shfl_sync(0xffffffffu, w, 31);
+        }
+        if (lane == 0) sh.P[0] = 0;
+    }
+    __syncthreads();
+    const int32_t Tot = sh.P[S];
+    const int32_t g0 = (int32_t)((int64_t)j * Tot / NW), g1 = (int32_t)((int64_t)(j + 1) * Tot / NW);
+    // first slice that overlaps [g0, ..) or starts at g0 (zero width included)
+    int lo = 0, hi = S;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (sh.P[mid + 1] > g0 || sh.P[mid] >= g0) hi = mid;
+        else lo = mid + 1;
+    }
+    T head = T(0);
+    int hslice = -1;
+    for (int i = lo; i < S; ++i) {
+        const int32_t pa = sh.P[i], pb = sh.P[i + 1];
+        if (!(pa < g1 || (j == NW - 1 && pa == Tot))) break;
+        const int32_t c0 = g0 > pa ? g0 - pa : 0;
+        const int32_t c1 = (g1 < pb ? g1 : pb) - pa;
+        const T acc = sell_row_range<T>(ptr, col, val, s0 + i, lane, c0, c1 > c0 ? c1 - c0 : 0, xload);
+        const bool starts = pa >= g0, ends = pb <= g1;
+        if (starts && ends) {
+            emit(s0 + i, acc);
+        } else if (ends) {
+            head = acc;
+            hslice = i;
+        } else {
+            sh.tail[j][lane] = acc;
+        }
+    }
+    __syncthreads();
+    if (hslice >= 0) {
+        // warps from the one holding the slice's first column up to this one
+        const int32_t pa = sh.P[hslice];
+        int ja = j - 1;
+        while (ja > 0 && (int32_t)((int64_t)ja * Tot / NW) > pa) --ja;
+        T sum = T(0);
+        for (int jj = ja; jj < j; ++jj) {
+            const int32_t a0 = (int32_t)((int64_t)jj * Tot / NW), a1 = (int32_t)((int64_t)(jj + 1) * Tot / NW);
+            if (a1 > a0) sum += sh.tail[jj][lane];
+        }
+        emit(s0 + hslice, sum + head);
+    }
+    __syncthreads();  // emits visible to the block; sh free for the next call
 }
 
 #define TF_SLICE_LOOP(nslices, s)                                                    \
     const int64_t warp__ = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;   \
     const int64_t nwarp__ = ((int64_t)gridDim.x * blockDim.x) >> 5;                  \
     for (int64_t s = warp__; s < (nslices); s += nwarp__)
+
+// Slice order of the persistent kernels, where every warp walks several
+// slices between two grid barriers and the barrier waits for the slowest
+// warp.  The SELL rows are sorted by length inside windows of
+// kSellWinSlices slices (512 rows), so slice rank k of every window has about
+// the same width and rank 0 is the widest: taking slices in storage order
+// hands the widest slice of every window to the same warp index.  Here
+// position p runs rank-major (p = k * nwin + win, slice win * 16 + k: widest
+// ranks first), and warp w of n takes positions w, 2n-1-w, 2n+w, ...: the
+// passes alternate direction, so each warp pairs wide slices with narrow ones.
+// A bijection on [0, nslices) for nslices a multiple of kSellWinSlices;
+// warp-uniform control flow.
+constexpr int kSellWinSlices = 16;
+__device__ __forceinline__ int64_t slice_at_rank(int64_t pos, int64_t nwin) {
+    return (pos % nwin) * kSellWinSlices + pos / nwin;
+}
+#define TF_SLICE_LOOP_BAL(nslices, s)                                                                     \
+    const int64_t bw__ = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;                          \
+    const int64_t bn__ = ((int64_t)gridDim.x * blockDim.x) >> 5;                                          \
+    const int64_t bwin__ = (nslices) / kSellWinSlices;                                                    \
+    for (int64_t bi__ = 0; bi__ * bn__ < (nslices); ++bi__)                                               \
+        for (int64_t bp__ = bi__ * bn__ + ((bi__ & 1) ? bn__ - 1 - bw__ : bw__),                          \
+                     s = bp__ < (nslices) ? slice_at_rank(bp__, bwin__) : -1;                             \
+             s >= 0; s = -1)
 
 }  // namespace tf

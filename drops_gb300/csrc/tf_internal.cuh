@@ -260,6 +260,7 @@ struct Context {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t markers[8] = {};
     DBuf<unsigned char> flush_buf;
+    DBuf<uint4> stream_buf;  // tf_stream_read_timed
     KernelTimer timers[TF_NUM_KERNELS];
     int64_t launches = 0;
     int last_refinements = 0;  // FP64 residual replacements of the last mixed solve
@@ -275,6 +276,10 @@ struct Context {
     DBuf<int32_t> sell_rexp[TF_NUM_MATS];
     DBuf<float2> x_pairs;       // SpMV operand split into FP32 pairs
     bool spmv_pair = false;     // tf_spmv: FP32-pair kernel instead of the FP64-FMA one
+    bool spmv_sell = false;     // tf_spmv: one warp per slice instead of the balanced kernel
+    bool pcg_blocked = true;    // mixed PCG: contiguous slices per block, balanced within the block
+    int spmv_blocks_per_sm = 0; // balanced SpMV launch shape (0: default)
+    int spmv_threads = 512;
     // batch of bricks (tf_mesh_brick_batch); 0 = single mesh
     int batch_count = 0;
     DBuf<BatchBrick> batch_tab;

@@ -373,6 +373,15 @@ int64_t tf_launch_count(tf_context* ctx);
  * the elapsed device time between two recorded markers.                     */
 int tf_marker_record(tf_context* ctx, int slot);
 int tf_marker_elapsed(tf_context* ctx, int slot_a, int slot_b, double* ms);
+/* Measurement helper (no reference counterpart): `reps` calls of tf_spmv,
+ * each bracketed by CUDA events on the context's stream and, when `cold` is
+ * set, preceded by an L2 flush; the launches are queued without host waits so
+ * the events time the kernel alone.  ms_each[r] = device time of call r.     */
+int tf_spmv_timed(tf_context* ctx, int mat, int vec_x, int vec_y, int reps, int cold, float* ms_each);
+/* Measurement helper (no reference counterpart): the streaming floor for a
+ * transfer size.  `reps` launches of a coalesced read of `bytes` bytes, timed
+ * like tf_spmv_timed (flush, event, kernel, event queued back to back).      */
+int tf_stream_read_timed(tf_context* ctx, int64_t bytes, int reps, int cold, float* ms_each);
 /* Overwrites a scratch buffer of twice the L2 size on the context's stream,
  * so that the next call starts with a cold L2.                               */
 int tf_flush_l2(tf_context* ctx);

@@ -80,13 +80,14 @@ def test_spmv_wide_range(ctxs):
     pair, native = ctxs
     _check(_spmv(pair, rp, ci, v, x), rp, ci, v, x, PAIR_REL)
     _check(_spmv(native, rp, ci, v, x), rp, ci, v, x, FP64_REL)
-    # x out of the pair range: the flag sends the launch down the FP64 path (bitwise the FP64 kernel)
+    # x out of the pair range: the flag sends the launch down the FP64 path (FP64 FMAs in CSR order, a few
+    # ulps of sum |a_ij x_j| from the oracle and from the balanced FP64 kernel, which splits wide slices)
     x2 = x.copy()
     x2[::500] = 1e-200
     x2[7] = 1e40
     y = _spmv(pair, rp, ci, v, x2)
     _check(y, rp, ci, v, x2, FP64_REL)
-    assert np.array_equal(y, _spmv(native, rp, ci, v, x2))
+    _check(_spmv(native, rp, ci, v, x2), rp, ci, v, x2, FP64_REL)
     # a non-finite value: the FP64 kernel, whose IEEE result the oracle reproduces
     v3 = v.copy()
     v3[100] = np.inf
@@ -95,3 +96,46 @@ def test_spmv_wide_range(ctxs):
     assert np.array_equal(np.isfinite(y), np.isfinite(ref))
     fin = np.isfinite(ref)
     assert np.all(np.abs(y[fin] - ref[fin]) <= FP64_REL * O.spmv(rp, ci, np.abs(v3), np.abs(x))[fin])
+
+
+def _random_csr(rng, lengths, m):
+    """Rows of the given lengths; row r holds the distinct columns (r + k s_r) mod m, k < length, sorted."""
+    lengths = np.asarray(lengths, dtype=np.int64)
+    rp = np.zeros(m + 1, dtype=np.int64)
+    rp[1:] = np.cumsum(lengths)
+    row = np.repeat(np.arange(m), lengths)
+    k = np.arange(rp[-1]) - np.repeat(rp[:-1], lengths)
+    ci = (row + k * (1 + (row % 3))) % m  # steps 1..3 < m / max length: distinct per row
+    order = np.lexsort((ci, row))
+    v = rng.uniform(-1, 1, rp[-1])
+    return rp, ci[order].astype(np.int32), v
+
+
+@pytest.mark.parametrize("case", ["tiny", "empty_rows", "one_long_row", "uneven", "many_slices"])
+def test_spmv_balanced_uneven_rows(ctxs, case):
+    """The balanced kernel splits the column work of a block's slices evenly over its warps, so slices are
+    shared by several warps; uneven rows, empty rows, single-slice matrices and blocks with fewer columns than
+    warps must all give the oracle's product, bit-identical from call to call."""
+    rng = np.random.default_rng({"tiny": 1, "empty_rows": 2, "one_long_row": 3, "uneven": 4, "many_slices": 5}[case])
+    if case == "tiny":
+        m = 5
+        lengths = np.array([1, 0, 3, 5, 2])
+    elif case == "empty_rows":
+        m = 3000
+        lengths = rng.integers(0, 4, m) * (rng.random(m) < 0.3)
+    elif case == "one_long_row":
+        m = 2000
+        lengths = np.ones(m, dtype=np.int64)
+        lengths[777] = 600
+    elif case == "uneven":
+        m = 40000
+        lengths = np.where(rng.random(m) < 0.1, rng.integers(40, 63, m), rng.integers(8, 20, m))
+    else:
+        m = 300000
+        lengths = rng.integers(5, 16, m)
+    rp, ci, v = _random_csr(rng, lengths, m)
+    x = rng.uniform(-1, 1, m)
+    native = ctxs[1]
+    y = _spmv(native, rp, ci, v, x)
+    _check(y, rp, ci, v, x, FP64_REL)
+    assert np.array_equal(y, _spmv(native, rp, ci, v, x))
