@@ -178,11 +178,11 @@ __global__ void k_spmv(int64_t nslices, const int32_t* __restrict__ perm, const 
 }
 
 // ---------------------------------------------------------------------------
-// Balanced SELL SpMV (the standalone y_Ax).  Block b takes the slices
-// [b n/B, (b+1) n/B) of the n slices (B = blocks, a multiple of the SM count,
-// so every SM gets the same share) and its warps split the block's column
-// work evenly (sell_block_balanced): about 3 gather rounds per warp for the
-// P2 matrices instead of the 8 of a 62-wide slice walked by one warp.  FP64
+// Balanced SELL SpMV (the standalone y_Ax).  Block b of B (a multiple of the
+// SM count) takes a contiguous run of n/B slices and its warps split the
+// run's column work evenly (sell_block_balanced, in chunks of at most
+// kBalMaxSlices slices): about 3 gather rounds per warp for the P2 matrices
+// instead of the 8 of a 62-wide slice walked by one warp.  FP64
 // multiply-adds only on stored entries (one warp instruction per 32 products;
 // GB300 issues FP64 at ~1/64 of the FP32 rate, so the FP64 pipe and HBM bound
 // this kernel about equally).  Bytes: 12 per stored entry + perm, ptr, x
@@ -195,22 +195,24 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_spmv_bal(int64_t nslices, con
                                                  double* __restrict__ y) {
     __shared__ BalShared<NT / 32, double> sh;
     const int lane = threadIdx.x & 31;
+    // equal slice counts: a work-balanced split (balanced_part_start) costs
+    // two binary searches of dependent loads, too much for one short launch
     const int64_t s0 = (int64_t)blockIdx.x * nslices / gridDim.x;
     const int64_t s1 = (int64_t)(blockIdx.x + 1) * nslices / gridDim.x;
-    sell_block_balanced<NT / 32, double>(
-        sh, ptr, col, val, s0, (int)(s1 - s0), [&](int32_t j) { return __ldg(x + j); },
-        [&](int64_t s, double v) {
-            const int32_t row = __ldg(perm + s * 32 + lane);
-            if (row >= 0) y[row] = v;
-        });
+    for (int64_t c0 = s0; c0 < s1; c0 += kBalMaxSlices)
+        sell_block_balanced<NT / 32, double>(
+            sh, ptr, col, val, c0, (int)(s1 - c0 < kBalMaxSlices ? s1 - c0 : kBalMaxSlices),
+            [&](int32_t j) { return __ldg(x + j); },
+            [&](int64_t s, double v) {
+                const int32_t row = __ldg(perm + s * 32 + lane);
+                if (row >= 0) y[row] = v;
+            });
 }
 
 static void launch_spmv_bal(Context* c, const CSR& A, const double* x, double* y) {
     const int64_t ns = A.sell.nslices;
     const int per_sm = c->spmv_blocks_per_sm > 0 ? c->spmv_blocks_per_sm : 2;
     int64_t nb = (int64_t)c->num_sms * per_sm;
-    const int64_t need = (ns + kBalMaxSlices - 1) / kBalMaxSlices;  // at most kBalMaxSlices slices per block
-    if (nb < need) nb = need;
     if (nb > ns) nb = ns;
     if (nb < 1) nb = 1;
     if (c->spmv_threads == 256)
@@ -997,13 +999,14 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_cg1(PcgCg1Args a)
     // walks whole slices per warp in the balanced global order.
     __shared__ BalShared<NT / 32, float> bsh;
     __shared__ float wsm[BLK ? kBalMaxSlices : 1][32], ssm[BLK ? kBalMaxSlices : 1][32];
+    // this block's slices: equal shares of column work plus row updates
+    const int64_t sb0 = BLK ? balanced_part_start(a.ptr, a.nslices, blockIdx.x, gridDim.x) : 0;
+    const int64_t sb1 = BLK ? balanced_part_start(a.ptr, a.nslices, blockIdx.x + 1, gridDim.x) : 0;
     auto pass = [&](bool refresh, float (&o)[6]) -> bool {
         float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         const float al = refresh ? 0.f : alpha, be = refresh ? 0.f : beta;
         const float4* V = Vc;
         if constexpr (BLK) {
-            const int64_t sb0 = (int64_t)blockIdx.x * a.nslices / gridDim.x;
-            const int64_t sb1 = (int64_t)(blockIdx.x + 1) * a.nslices / gridDim.x;
             for (int64_t c0 = sb0; c0 < sb1; c0 += kBalMaxSlices) {
                 const int S = (int)(sb1 - c0 < kBalMaxSlices ? sb1 - c0 : kBalMaxSlices);
                 sell_block_balanced<NT / 32, float>(

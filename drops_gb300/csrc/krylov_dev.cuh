@@ -326,6 +326,22 @@ __device__ __forceinline__ float* ar_part<float>(const GridAR& g) { return g.par
 template <>
 __device__ __forceinline__ double* ar_part<double>(const GridAR& g) { return g.partd; }
 
+// the kArMax values of one block's record (L2 only: written by other SMs)
+__device__ __forceinline__ void ar_load_record(const float* p, float (&r)[8]) {
+    const float4 a = __ldcg(reinterpret_cast<const float4*>(p)), b = __ldcg(reinterpret_cast<const float4*>(p) + 1);
+    r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
+    r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
+}
+__device__ __forceinline__ void ar_load_record(const double* p, double (&r)[8]) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const double2 a = __ldcg(reinterpret_cast<const double2*>(p) + q);
+        r[2 * q] = a.x;
+        r[2 * q + 1] = a.y;
+    }
+}
+static_assert(kArMax == 8, "records of eight values");
+
 // Sums v[k] over every thread of the grid into out[k] (identical in all
 // threads).  Call from all threads of every block, in uniform control flow.
 template <class T, int NV>
@@ -336,10 +352,14 @@ __device__ bool grid_allreduce(const GridAR& g, unsigned long long& epoch, const
     __shared__ int st;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     T* part = ar_part<T>(g) + (size_t)(epoch & 1) * gridDim.x * kArMax;
+    // all NV sums of a warp at once (transposing butterfly, 9 shuffles)
+    const int idx = warp_sum8_index(lane);
+    {
+        T v8[8];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-        const T x = warp_sum(v[k]);
-        if (lane == 0) red[k][w] = x;
+        for (int k = 0; k < 8; ++k) v8[k] = k < NV ? v[k] : T(0);
+        const T tot = warp_sum8(v8, lane);
+        if ((lane & 3) == 0 && idx < NV) red[idx][w] = tot;
     }
     __syncthreads();
     if (threadIdx.x < NV) {
@@ -349,11 +369,21 @@ __device__ bool grid_allreduce(const GridAR& g, unsigned long long& epoch, const
     }
     if (!ar_arrive_wait(g, epoch, &st)) return false;
     ++epoch;
-    if (w < NV) {
-        T x = T(0);
-        for (unsigned b = lane; b < gridDim.x; b += 32) x += __ldcg(part + (size_t)b * kArMax + w);
-        x = warp_sum(x);
-        if (lane == 0) res[w] = x;
+    // one warp reads every block's record of kArMax values (32 or 64 bytes,
+    // 16-byte loads: one L2 sector request per block and 16 bytes instead of
+    // one per value) and sums the blocks in a fixed order
+    if (w == 0) {
+        T acc[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) acc[k] = T(0);
+        for (unsigned b = lane; b < gridDim.x; b += 32) {
+            T rec[8];
+            ar_load_record(part + (size_t)b * kArMax, rec);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) acc[k] += k < NV ? rec[k] : T(0);
+        }
+        const T tot = warp_sum8(acc, lane);
+        if ((lane & 3) == 0 && idx < NV) res[idx] = tot;
     }
     __syncthreads();
 #pragma unroll
@@ -440,6 +470,26 @@ __device__ __forceinline__ T sell_row(const int32_t* __restrict__ ptr, const int
 // what emit wrote to shared memory can be read right after.
 // ---------------------------------------------------------------------------
 constexpr int kBalMaxSlices = 64;
+
+// First slice of part b of nparts when the slices [0, nslices) are split at
+// equal work, work(s) = columns(s) + kBalRowCost per slice (the per-row
+// updates that follow the product), using the SELL offsets ptr (32 x columns,
+// a prefix sum): the largest s with work before s <= b W / nparts.
+constexpr int kBalRowCost = 4;
+__device__ __forceinline__ int64_t balanced_part_start(const int32_t* __restrict__ ptr, int64_t nslices, int64_t b,
+                                                       int64_t nparts) {
+    if (b <= 0) return 0;
+    if (b >= nparts) return nslices;
+    const int64_t total = (int64_t)(__ldg(ptr + nslices) >> 5) + kBalRowCost * nslices;
+    const int64_t target = total * b / nparts;
+    int64_t lo = 0, hi = nslices;  // work(lo) <= target < work(hi + 1)
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if ((int64_t)(__ldg(ptr + mid) >> 5) + kBalRowCost * mid <= target) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
 
 template <int NW, class T>
 struct BalShared {
