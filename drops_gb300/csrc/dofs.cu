@@ -13,38 +13,54 @@
 //   3. ranking: the keys are unique, so a scan over the key space turns every
 //      owned key into its DOF number.
 #include <climits>
+#include <cstring>
 
 #include "tf_internal.cuh"
 
 namespace tf {
 
-__device__ inline int sgn(double v) { return (v > 0.) - (v < 0.); }
-
 __device__ inline void set_status(int* st, int code, int64_t where) {
     if (atomicCAS(st, 0, code) == 0) st[1] = (int)where;
 }
 
-__global__ void k_classify(MeshView M, const double* __restrict__ lsv, const double* __restrict__ lse, double dist,
+// The distance test on the IEEE-754 bit patterns, with integer operations
+// only: GB300 issues FP64 compares on its narrow FP64 pipe, and ten values per
+// tet made classification FP64-bound.  For a double with bits b and
+// magnitude bits m = b & 0x7ff..f: sign(d) (misc/utils.h:810-813) is 0 for
+// m == 0 (+-0) and for NaN (m > 0x7ff0..0, where both comparisons of sign()
+// are false), else -1 or +1 by the sign bit; for non-NaN values |a| < |c| iff
+// m_a < m_c, so min |f| is the minimum of the m.
+struct DistTest {
+    unsigned long long dmag;  // magnitude bits of dist (when dist >= 0)
+    int dmag_ok;              // dist >= 0: min |f| <= dist is dmag compare
+    int mixed_active;         // 0 <= dist: a tet with a sign change is active
+};
+
+__global__ void k_classify(MeshView M, const double* __restrict__ lsv, const double* __restrict__ lse, DistTest D,
                            int32_t* __restrict__ flags, int* __restrict__ status) {
+    const long long* bv = reinterpret_cast<const long long*>(lsv);
+    const long long* be = reinterpret_cast<const long long*>(lse);
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < M.nt; t += (int64_t)gridDim.x * blockDim.x) {
         int32_t v[4], e[6];
         mesh_tet(M, t, v, e);
-        double f[10];
-        for (int k = 0; k < 4; ++k) f[k] = lsv[v[k]];
-        for (int k = 0; k < 6; ++k) f[4 + k] = lse[e[k]];
+        long long f[10];
+        for (int k = 0; k < 4; ++k) f[k] = __ldg(bv + v[k]);
+        for (int k = 0; k < 6; ++k) f[4 + k] = __ldg(be + e[k]);
         int sum = 0, zeros = 0;
-        double mn = fabs(f[0]);
+        unsigned long long mn = ~0ull;
         for (int k = 0; k < 10; ++k) {
-            sum += sgn(f[k]);
-            zeros += f[k] == 0.;
-            mn = fmin(mn, fabs(f[k]));
+            const unsigned long long m = (unsigned long long)f[k] & 0x7fffffffffffffffull;
+            const bool zero = m == 0ull, nan = m > 0x7ff0000000000000ull;
+            sum += (zero || nan) ? 0 : (f[k] < 0 ? -1 : 1);
+            zeros += zero;
+            mn = m < mn ? m : mn;
         }
         int active;
         if (sum == 10 || sum == -10) {
-            active = mn <= dist;
+            active = D.dmag_ok && mn <= D.dmag;  // distance() = min |f| <= dist
         } else {
             if (zeros) set_status(status, TF_ERR_ZERO_NODE, t);
-            active = 1;  // distance() == 0 <= dist
+            active = D.mixed_active;  // distance() = 0 <= dist
         }
         flags[t] = active;
     }
@@ -172,7 +188,15 @@ int distribute_dofs(Context* c, int fe, double dist) {
     TF_CUDA(c, cudaMemsetAsync(c->status.p, 0, 4 * sizeof(int), c->stream));
     {
         TimedLaunch tl(c, TF_K_CLASSIFY);
-        k_classify<<<grid_for(c, M.nt), kBlock, 0, c->stream>>>(M, c->ls_vert.p, c->ls_edge.p, dist,
+        DistTest D;
+        D.dmag_ok = dist >= 0.;
+        D.dmag = 0;
+        if (D.dmag_ok) {
+            std::memcpy(&D.dmag, &dist, sizeof(double));
+            D.dmag &= 0x7fffffffffffffffull;
+        }
+        D.mixed_active = 0. <= dist;
+        k_classify<<<grid_for(c, M.nt), kBlock, 0, c->stream>>>(M, c->ls_vert.p, c->ls_edge.p, D,
                                                                   (int32_t*)c->scratch.p, c->status.p);
         ++c->launches;
         TF_CUDA(c, cudaGetLastError());

@@ -86,21 +86,27 @@ __host__ __device__ inline void kuhn_offset(int l, int k, int& d3, int& d2, int&
     if (k == 3) { d3 = d2 = d1 = 1; return; }
     // first step axis and second step axis per tet type, (i3,i2,i1) = axis 0,1,2
     // l=0: +i1, +i2   l=1: +i1, +i3   l=2: +i2, +i1   l=3: +i2, +i3   l=4: +i3, +i1   l=5: +i3, +i2
-    const int first[6] = {2, 2, 1, 1, 0, 0};
-    const int second[6] = {1, 0, 2, 0, 2, 1};
-    int d[3] = {0, 0, 0};
-    d[first[l]] = 1;
-    if (k == 2) d[second[l]] = 1;
-    d3 = d[0]; d2 = d[1]; d1 = d[2];
+    // first = {2,2,1,1,0,0}, second = {1,0,2,0,2,1}, one nibble per type
+    // (packed constants rather than small arrays that a dynamic index would
+    // put in local memory)
+    const int f = (0x001122 >> (4 * l)) & 0xf, s = (0x120201 >> (4 * l)) & 0xf;
+    const bool two = k == 2;
+    d3 = (f == 0) | (two & (s == 0));
+    d2 = (f == 1) | (two & (s == 1));
+    d1 = (f == 2) | (two & (s == 2));
 }
 
 __host__ __device__ inline void brick_tet(const Brick& B, int64_t t, int64_t v0, int64_t e0, int32_t v[4], int32_t e[6]) {
-    const int64_t cube = t / 6;
-    const int l = (int)(t - cube * 6);
-    const int i1 = (int)(cube % B.n1);
-    const int64_t r = cube / B.n1;
-    const int i2 = (int)(r % B.n2);
-    const int i3 = (int)(r / B.n2);
+    // 32-bit divisions (cube < 2^32 for any mesh with 32-bit vertex ids; a
+    // 64-bit division by a runtime divisor is a long emulated sequence)
+    const uint32_t cube = (uint32_t)(t / 6);
+    const int l = (int)(t - (int64_t)cube * 6);
+    const uint32_t n1 = (uint32_t)B.n1, n2 = (uint32_t)B.n2;
+    const uint32_t r = cube / n1;
+    const int i1 = (int)(cube - r * n1);
+    const uint32_t r2 = r / n2;
+    const int i2 = (int)(r - r2 * n2);
+    const int i3 = (int)r2;
     int p[4][3];
     for (int k = 0; k < 4; ++k) {
         int d3, d2, d1;
@@ -138,10 +144,12 @@ __device__ inline void mesh_tet(const MeshView& M, int64_t t, int32_t v[4], int3
 // component with round-to-nearest products and sums (no contraction), as in
 // BrickBuilderCL::build_ser_impl.
 __device__ inline void brick_coord(const Brick& B, int64_t v, double x[3]) {
-    const int i1 = (int)(v % (B.n1 + 1));
-    const int64_t r = v / (B.n1 + 1);
-    const int i2 = (int)(r % (B.n2 + 1));
-    const int i3 = (int)(r / (B.n2 + 1));
+    const uint32_t u = (uint32_t)v, m1 = (uint32_t)B.n1 + 1u, m2 = (uint32_t)B.n2 + 1u;
+    const uint32_t r = u / m1;
+    const int i1 = (int)(u - r * m1);
+    const uint32_t r2 = r / m2;
+    const int i2 = (int)(r - r2 * m2);
+    const int i3 = (int)r2;
     for (int c = 0; c < 3; ++c)
         x[c] = __dadd_rn(__dadd_rn(__dadd_rn(B.orig[c], __dmul_rn((double)i1, B.o1[c])), __dmul_rn((double)i2, B.o2[c])),
                          __dmul_rn((double)i3, B.o3[c]));

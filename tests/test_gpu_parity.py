@@ -88,6 +88,30 @@ def test_dofs_bitexact(ctx, golden, name, kind, par, upload):
         assert np.array_equal(de, ode)
 
 
+@pytest.mark.parametrize("dist", [0.0, -0.0, 0.02, 0.3, -0.1])
+@pytest.mark.parametrize("p2", [False, True])
+def test_dofs_narrow_band_dist(ctx, dist, p2):
+    """DistributeDOFs(level, mg, ls, dist): a tet is active iff distance() <= dist, distance() being min |phi|
+    over its 10 values when they share one sign and 0 otherwise (geom/subtriangulation.tpp:38-46).  Bands
+    of positive width take uncut tets near the sphere; a negative dist takes none."""
+    om = brick(ctx, 12, 5.0 / 3.0)
+    ctx.levelset_analytic(tf.LS_SPHERE, [0.03, -0.02, 0.01, 1.0], p2)
+    lv, le = O.levelset(om, O.LS_SPHERE, [0.03, -0.02, 0.01, 1.0], p2)
+    na, nd = ctx.distribute_dofs(tf.P2IF if p2 else tf.P1IF, dist=dist)
+    st, ona, ond, odv, ode, oact = O.distribute_dofs(om, lv, le, p2, dist=dist)
+    assert st == 0 and (na, nd) == (ona, ond)
+    dv, de, act, l2g = ctx.dofs()
+    assert np.array_equal(act[:na], np.flatnonzero(oact))
+    assert np.array_equal(dv, odv)
+    if p2:
+        assert np.array_equal(de, ode)
+    if dist < 0:
+        assert na == 0
+    elif dist > 0.1:
+        st0, na0, *_ = O.distribute_dofs(om, lv, le, p2, dist=0.0)
+        assert na > na0
+
+
 @pytest.mark.parametrize("name,kind,par", SYSTEMS)
 def test_assembly_parity(ctx, golden, name, kind, par):
     g = golden(name)
