@@ -28,6 +28,7 @@ OK, ERR_CUDA, ERR_ZERO_NODE, ERR_ZERO_PATTERN, ERR_BAD_INPUT, ERR_NOT_CONVERGED,
 P1IF, P2IF = 1, 2
 FORM_M, FORM_A, FORM_CN, FORM_LAPM = 0, 1, 2, 3
 MAT_SYS, MAT_BLOCK, MAT_USER = 4, 5, 6
+FORM_N = 7  # N_P1P1, wind convection (tf_wind_upload)
 VEC_RHS, VEC_X, VEC_B, VEC_CHI, VEC_T0, VEC_T1, VEC_T2, VEC_T3 = range(8)
 LS_SPHERE, LS_TORUS, LS_ELLIPSOID, LS_PLANE = range(4)
 RHS_NONE, RHS_SPHERE_XYZ, RHS_CONST = range(3)
@@ -47,7 +48,7 @@ EXPORTS = [
     "tf_mesh_brick_batch", "tf_levelset_analytic_batch", "tf_batch_info", "tf_batch_lincomb", "tf_batch_pcg_jacobi",
     "tf_batch_tune", "tf_batch_config", "tf_mlp_init", "tf_mlp_get_weights", "tf_mlp_set_weights", "tf_mlp_forward",
     "tf_mlp_gradient", "tf_mlp_train", "tf_ch_features", "tf_ch_steps_learned", "tf_gmres_options", "tf_timing_enable",
-    "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2", "tf_spmv_timed", "tf_stream_read_timed",
+    "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2", "tf_spmv_timed", "tf_stream_read_timed", "tf_wind_upload",
     "tf_host_alloc", "tf_host_free",
 ]
 
@@ -206,6 +207,16 @@ class TraceFEM:
         return coords, tv, te, ev
 
     # ---- level set ---------------------------------------------------------
+    def wind_upload(self, wind_vert, wind_edge):
+        """P2 wind for FORM_N: xyz at every vertex (nv, 3) and at every edge midpoint (ne, 3)."""
+        wv = np.ascontiguousarray(wind_vert, dtype=np.float64).reshape(-1)
+        we = np.ascontiguousarray(wind_edge, dtype=np.float64).reshape(-1)
+        nv, ne, _ = self.mesh_info()
+        if wv.size != 3 * nv or we.size != 3 * ne:
+            raise ValueError("wind_upload: expected (nv, 3) and (ne, 3) arrays")
+        self._check(self.L.tf_wind_upload(self.h, wv.ctypes.data_as(C.POINTER(C.c_double)),
+                                          we.ctypes.data_as(C.POINTER(C.c_double))))
+
     def levelset_upload(self, ls_vert, ls_edge=None):
         ls_vert = np.ascontiguousarray(ls_vert, dtype=np.float64)
         ls_edge = None if ls_edge is None else np.ascontiguousarray(ls_edge, dtype=np.float64)

@@ -489,6 +489,8 @@ struct AsmSmem {
     double sg[32][NL][3];
     double mob[32];
     double fx[32];
+    double wind[NL == 4 ? 30 : 1];    // N_P1P1: P2 wind at the 10 nodes, xyz
+    double wn[NL == 4 ? 32 : 1][4];   // sqrt(w) (wind . surface gradient of phi_j)
 };
 
 struct AsmArgs {
@@ -505,6 +507,9 @@ struct AsmArgs {
     double* elem;       // [form][n_active][nsym]
     double* elem_rhs;   // [n_active][NL]
     int* status;
+    const double* windv;  // N_P1P1 wind, xyz per vertex / edge
+    const double* winde;
+    double* elem_n;       // [n_active][16]: N_P1P1, row i col j
 };
 
 template <int NL>
@@ -518,6 +523,7 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
     const bool wantM = A.forms & (1u << TF_FORM_M), wantA = A.forms & (1u << TF_FORM_A);
     const bool wantC = A.forms & (1u << TF_FORM_CN), wantL = A.forms & (1u << TF_FORM_LAPM);
     const bool wantF = A.rhs.kind != TF_RHS_NONE;
+    const bool wantN = NL == 4 && (A.forms & (1u << TF_FORM_N));
     const int64_t nwarps = (int64_t)gridDim.x * kAsmWarps;
 
     for (int64_t r = (int64_t)blockIdx.x * kAsmWarps + wib; r < A.n_active; r += nwarps) {
@@ -532,6 +538,12 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
         } else if (lane < 10) {
             S.ls10[lane] = A.lse[e[lane - 4]];
         }
+        if constexpr (NL == 4) {
+            if (wantN && lane < 30) {  // node k = lane / 3: vertices 0..3, edges 4..9
+                const int k = lane / 3, r = lane - 3 * (lane / 3);
+                S.wind[lane] = k < 4 ? A.windv[3 * (int64_t)v[k] + r] : A.winde[3 * (int64_t)e[k - 4] + r];
+            }
+        }
         __syncwarp();
         warp_tet_geometry(S.g, S.ls10, S.gM, S.gC, lane);
         double ls10[10];
@@ -544,7 +556,7 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
 
         double accM[EPL], accA[EPL], accL[EPL], accC[EPL];
         for (int q = 0; q < EPL; ++q) accM[q] = accA[q] = accL[q] = accC[q] = 0.;
-        double accF = 0.;
+        double accF = 0., accN = 0.;
         const int npts = 7 * nf;
         for (int base = 0; base < npts; base += 32) {
             const int p = base + lane;
@@ -581,6 +593,21 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
                         x[c] = S.g.X[0][c] * b[0] + S.g.X[1][c] * b[1] + S.g.X[2][c] * b[2] + S.g.X[3][c] * b[3];
                     S.fx[lane] = rhs_value(A.rhs, x);
                 }
+                if constexpr (NL == 4) {
+                    // N_P1P1: the P2 wind at the point (LocalP2CL at b: vertex
+                    // b_i (2 b_i - 1), edge (a,c) 4 b_a b_c) dotted with the
+                    // surface gradients of the hat functions
+                    if (wantN) {
+                        double h[10];
+                        for (int i = 0; i < 4; ++i) h[i] = b[i] * (2. * b[i] - 1.);
+                        for (int k = 0; k < 6; ++k) h[4 + k] = 4. * b[ev0(k)] * b[ev1(k)];
+                        double wv[3] = {0., 0., 0.};
+                        for (int k = 0; k < 10; ++k)
+                            for (int c = 0; c < 3; ++c) wv[c] += S.wind[3 * k + c] * h[k];
+                        for (int j = 0; j < 4; ++j)
+                            S.wn[lane][j] = sw * (wv[0] * sg[j][0] + wv[1] * sg[j][1] + wv[2] * sg[j][2]);
+                    }
+                }
             }
             __syncwarp();
             const int cnt = min(32, npts - base);
@@ -610,6 +637,11 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
             if constexpr (NL == 4) {
                 if (wantF)
                     for (int pp = lane >> 2; pp < cnt; pp += 8) accF += (S.w[pp] * S.fx[pp]) * S.phi[pp][lane & 3];
+                // N: 16 entries (i, j) = (lane / 4 % 4, lane % 4) on 2 point groups
+                if (wantN) {
+                    const int i = (lane >> 2) & 3, j = lane & 3;
+                    for (int pp = lane >> 4; pp < cnt; pp += 2) accN += S.phi[pp][i] * S.wn[pp][j];
+                }
             } else if (wantF && lane < NL) {
                 for (int pp = 0; pp < cnt; ++pp) accF += (S.w[pp] * S.fx[pp]) * S.phi[pp][lane];
             }
@@ -626,6 +658,7 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
             accF += __shfl_down_sync(0xffffffffu, accF, 16);
             accF += __shfl_down_sync(0xffffffffu, accF, 8);
             accF += __shfl_down_sync(0xffffffffu, accF, 4);
+            accN += __shfl_down_sync(0xffffffffu, accN, 16);  // point groups: g0 + g1
         }
         if (wantC) {
             // normal-gradient volume stabilisation on the 15-point Quad5 rule
@@ -671,6 +704,7 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
             if (wantL) A.elem[((int64_t)TF_FORM_LAPM * A.n_active + r) * NSYM + k] = accL[q];
         }
         if (wantF && lane < NL) A.elem_rhs[r * NL + lane] = accF;
+        if (wantN && lane < 16) A.elem_n[r * 16 + lane] = accN;
         __syncwarp();
     }
 }
@@ -785,11 +819,11 @@ __global__ void k_row_emit(int64_t m, const int32_t* __restrict__ start, const u
 template <int NL>
 __global__ void k_scatter(int64_t nnz, const int32_t* __restrict__ seg_start, const uint64_t* __restrict__ contrib,
                           int64_t n_active, const double* __restrict__ elem, unsigned forms, double* v0, double* v1,
-                          double* v2, double* v3) {
+                          double* v2, double* v3, const double* __restrict__ elem_n = nullptr, double* v4 = nullptr) {
     constexpr int NSYM = NL * (NL + 1) / 2;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz; k += (int64_t)gridDim.x * blockDim.x) {
         const int32_t s = seg_start[k], e = seg_start[k + 1];
-        double a0 = 0., a1 = 0., a2 = 0., a3 = 0.;
+        double a0 = 0., a1 = 0., a2 = 0., a3 = 0., a4 = 0.;
         for (int32_t p = s; p < e; ++p) {
             const uint32_t c = (uint32_t)contrib[p];
             const uint32_t r = c / (NL * NL);
@@ -799,11 +833,14 @@ __global__ void k_scatter(int64_t nnz, const int32_t* __restrict__ seg_start, co
             if (forms & 2u) a1 += elem[(int64_t)TF_FORM_A * n_active * NSYM + idx];
             if (forms & 4u) a2 += elem[(int64_t)TF_FORM_CN * n_active * NSYM + idx];
             if (forms & 8u) a3 += elem[(int64_t)TF_FORM_LAPM * n_active * NSYM + idx];
+            // N (not symmetric): row-local i = ij / NL, column-local j = ij % NL
+            if (NL == 4 && (forms & (1u << TF_FORM_N))) a4 += elem_n[(int64_t)r * 16 + ij];
         }
         if (forms & 1u) v0[k] = a0;
         if (forms & 2u) v1[k] = a1;
         if (forms & 4u) v2[k] = a2;
         if (forms & 8u) v3[k] = a3;
+        if (NL == 4 && (forms & (1u << TF_FORM_N))) v4[k] = a4;
     }
 }
 
@@ -874,13 +911,15 @@ static int build_pattern(Context* c, const uint8_t* mask = nullptr) {
     release(bstart);
     TF_CUDA(c, cudaGetLastError());
     const int64_t gen = ++c->pattern_counter;
-    for (int f = 0; f < TF_NUM_FORMS; ++f) {
+    for (int f = 0; f < TF_NUM_MATS; ++f) {
+        if (!is_form_handle(f)) continue;
         CSR& A = c->mats[f];
         A.m = m;
         A.nnz = nnz;
         A.rowptr = c->rowptr.p;
         A.colind = c->colind.p;
         A.pattern_gen = gen;
+        A.vals = nullptr;  // values of the old pattern: every form is assembled again
         ++A.version;
     }
     c->pattern_dof_version = mask ? -1 : c->dof_version;  // a masked pattern is not the DistributeDOFs one
@@ -892,10 +931,13 @@ int setup_fe_system(Context* c, unsigned forms, int rhs_kind, const double* rhs_
     if (c->legacy_numbering)
         return set_err(c, TF_ERR_BAD_INPUT, "setup_fe_system: needs a DistributeDOFs numbering, not the legacy one");
     if (forms == 0 && rhs_kind == TF_RHS_NONE) return TF_OK;
-    if (forms & ~0xFu) return set_err(c, TF_ERR_BAD_INPUT, "setup_fe_system: unknown form bits");
+    if (forms & ~(0xFu | (1u << TF_FORM_N))) return set_err(c, TF_ERR_BAD_INPUT, "setup_fe_system: unknown form bits");
     const bool p2 = c->fe == TF_P2IF;
     if (p2 && (forms & (1u << TF_FORM_LAPM)))
         return set_err(c, TF_ERR_BAD_INPUT, "setup_fe_system: LaplaceM is a P1 form");
+    const bool wantN = forms & (1u << TF_FORM_N);
+    if (wantN && p2) return set_err(c, TF_ERR_BAD_INPUT, "setup_fe_system: N_P1P1 is a P1 form");
+    if (wantN && !c->has_wind) return set_err(c, TF_ERR_BAD_INPUT, "setup_fe_system: N_P1P1 needs tf_wind_upload");
     TF_TRY(ensure_tables(c));
     const int nl = p2 ? 10 : 4, nsym = nl * (nl + 1) / 2;
     const int64_t na = c->n_active, m = c->n_dofs;
@@ -911,8 +953,9 @@ int setup_fe_system(Context* c, unsigned forms, int rhs_kind, const double* rhs_
     if (forms & (1u << TF_FORM_LAPM)) {
         if (c->vecs[TF_VEC_CHI].n == (size_t)m && m > 0) chi = c->vecs[TF_VEC_CHI].p;
     }
+    if (wantN) TF_TRY(ensure(c, c->elem_n, (size_t)(na > 0 ? na : 1) * 16));
     AsmArgs A{c->mesh, c->ls_vert.p, c->ls_edge.p, na, c->active.p, c->loc2glo.p, forms, R, chi, chi ? 1 : 0,
-              c->elem.p, c->elem_rhs.p, c->status.p};
+              c->elem.p, c->elem_rhs.p, c->status.p, c->wind_v.p, c->wind_e.p, wantN ? c->elem_n.p : nullptr};
     TF_CUDA(c, cudaMemsetAsync(c->status.p, 0, 4 * sizeof(int), c->stream));
     if (na > 0) {
         TimedLaunch tl(c, TF_K_ASSEMBLE);
@@ -944,6 +987,12 @@ int setup_fe_system(Context* c, unsigned forms, int rhs_kind, const double* rhs_
         ++c->mats[f].version;
         v[f] = c->mats[f].vals;
     }
+    double* vN = nullptr;
+    if (wantN) {
+        TF_TRY(ensure(c, c->mat_vals[TF_FORM_N], (size_t)(nnz > 0 ? nnz : 1)));
+        c->mats[TF_FORM_N].vals = vN = c->mat_vals[TF_FORM_N].p;
+        ++c->mats[TF_FORM_N].version;
+    }
     if (nnz > 0) {
         TimedLaunch tl(c, TF_K_SCATTER);
         if (p2)
@@ -951,7 +1000,7 @@ int setup_fe_system(Context* c, unsigned forms, int rhs_kind, const double* rhs_
                                                                        forms, v[0], v[1], v[2], v[3]);
         else
             k_scatter<4><<<grid_for(c, nnz), kBlock, 0, c->stream>>>(nnz, c->seg_start.p, c->contrib.p, na, c->elem.p,
-                                                                      forms, v[0], v[1], v[2], v[3]);
+                                                                      forms, v[0], v[1], v[2], v[3], c->elem_n.p, vN);
         ++c->launches;
         if (rhs_kind != TF_RHS_NONE) {
             TF_TRY(ensure(c, c->vecs[TF_VEC_RHS], (size_t)m));
@@ -1263,7 +1312,7 @@ int setup_legacy_p1(Context* c, double alpha, double D, const double* fpar, int6
         ++c->mats[f].version;
         v[f] = c->mats[f].vals;
     }
-    for (int f : {TF_FORM_CN, TF_FORM_LAPM}) c->mats[f].vals = nullptr;  // not part of this pattern
+    for (int f : {TF_FORM_CN, TF_FORM_LAPM, TF_FORM_N}) c->mats[f].vals = nullptr;  // not part of this pattern
     if (nnz > 0) {
         TimedLaunch tl(c, TF_K_SCATTER);
         const unsigned forms = (1u << TF_FORM_M) | (1u << TF_FORM_A);

@@ -94,7 +94,7 @@ int batch_lincomb(Context* c, int nterms, const int* forms, const double* coeffs
     TF_TRY(batch_ranges(c));
     BatchLincombArgs a{};
     for (int t = 0; t < nterms; ++t) {
-        if (forms[t] < 0 || forms[t] >= TF_NUM_FORMS || !c->mats[forms[t]].vals)
+        if (!is_form_handle(forms[t]) || !c->mats[forms[t]].vals)
             return set_err(c, TF_ERR_BAD_INPUT, "batch_lincomb: form not assembled");
         if (c->mats[forms[t]].pattern_gen != c->mats[forms[0]].pattern_gen)
             return set_err(c, TF_ERR_BAD_INPUT, "batch_lincomb: forms of different patterns");

@@ -190,6 +190,9 @@ int tf_destroy(tf_context* t) {
     tf::release(c->gm2_v64);
     tf::release(c->gm2_binv);
     tf::release(c->flush_buf);
+    tf::release(c->wind_v);
+    tf::release(c->wind_e);
+    tf::release(c->elem_n);
     tf::release(c->stream_buf);
     for (auto& e : c->markers)
         if (e) cudaEventDestroy(e);
@@ -248,6 +251,7 @@ int tf_mesh_upload(tf_context* t, int64_t nv, const double* coords, int64_t nt, 
     M.edge_v = c->edge_v.p;
     c->has_mesh = true;
     c->has_ls = false;
+    c->has_wind = false;
     c->fe = 0;
     return TF_OK;
 }
@@ -305,6 +309,23 @@ int tf_levelset_upload(tf_context* t, const double* ls_vert, const double* ls_ed
     c->has_ls = true;
     ++c->ls_version;
     c->fe = 0;
+    return TF_OK;
+}
+
+int tf_wind_upload(tf_context* t, const double* wind_vert, const double* wind_edge) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (!c->has_mesh || !wind_vert || !wind_edge)
+        return tf::set_err(c, TF_ERR_BAD_INPUT, "wind_upload: mesh and vertex and edge values required");
+    TF_TRY(tf::ensure(c, c->wind_v, (size_t)(3 * c->mesh.nv)));
+    TF_TRY(tf::ensure(c, c->wind_e, (size_t)(3 * c->mesh.ne)));
+    TF_CUDA(c, cudaMemcpyAsync(c->wind_v.p, wind_vert, sizeof(double) * 3 * c->mesh.nv, cudaMemcpyHostToDevice,
+                               c->stream));
+    TF_CUDA(c, cudaMemcpyAsync(c->wind_e.p, wind_edge, sizeof(double) * 3 * c->mesh.ne, cudaMemcpyHostToDevice,
+                               c->stream));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->has_wind = true;
     return TF_OK;
 }
 

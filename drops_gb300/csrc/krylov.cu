@@ -459,7 +459,7 @@ int lincomb(Context* c, int nterms, const int* forms, const double* coeffs) {
     if (nterms < 1 || nterms > 8 || !forms || !coeffs) return set_err(c, TF_ERR_BAD_INPUT, "lincomb: 1..8 terms");
     LincombArgs a{};
     for (int t = 0; t < nterms; ++t) {
-        if (forms[t] < 0 || forms[t] >= TF_NUM_FORMS || !c->mats[forms[t]].vals)
+        if (!is_form_handle(forms[t]) || !c->mats[forms[t]].vals)
             return set_err(c, TF_ERR_BAD_INPUT, "lincomb: form not assembled");
         a.src[t] = c->mats[forms[t]].vals;
         a.co[t] = coeffs[t];

@@ -43,6 +43,7 @@ int mesh_set_brick(Context* c, const double orig[3], const double e1[3], const d
         return set_err(c, TF_ERR_CAPACITY, "brick too large for 32-bit vertex/edge ids");
     c->has_mesh = true;
     c->has_ls = false;
+    c->has_wind = false;
     c->fe = 0;
     c->batch_count = 0;
     return TF_OK;
@@ -99,6 +100,7 @@ int mesh_set_brick_batch(Context* c, int count, const int32_t* n, const double* 
     c->batch_dof_version = -1;
     c->has_mesh = true;
     c->has_ls = false;
+    c->has_wind = false;
     c->fe = 0;
     return TF_OK;
 }

@@ -267,6 +267,9 @@ struct Context {
     bool timing = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t markers[8] = {};
+    DBuf<double> wind_v, wind_e;  // N_P1P1 wind, xyz per vertex / edge
+    bool has_wind = false;
+    DBuf<double> elem_n;          // N_P1P1 element matrices [n_active][16] (full, row i col j)
     DBuf<unsigned char> flush_buf;
     DBuf<uint4> stream_buf;  // tf_stream_read_timed
     KernelTimer timers[TF_NUM_KERNELS];
@@ -442,6 +445,9 @@ int mlp_epoch_dev(Context* c, const __nv_bfloat16* X, const float* Y, int64_t n,
                   double* loss);
 int ensure_vals32(Context* c, CSR& A);
 int ensure_sell(Context* c, CSR& A, bool fp32);
+
+// matrix handles that hold an assembled form
+inline bool is_form_handle(int f) { return (f >= 0 && f < TF_NUM_FORMS) || f == TF_FORM_N; }
 
 constexpr int kBlock = 256;
 inline int grid_for(Context* c, int64_t n, int block = kBlock, int per_sm = 8) {

@@ -55,7 +55,8 @@ extern "C" {
 #define TF_MAT_SYS 4     /* linear combination of forms (tf_lincomb), same pattern       */
 #define TF_MAT_BLOCK 5   /* 2x2 Cahn-Hilliard block matrix (tf_ch_block), 2m rows        */
 #define TF_MAT_USER 6    /* matrix uploaded with tf_matrix_upload                         */
-#define TF_NUM_MATS 7
+#define TF_FORM_N 7      /* N_P1P1 :1590-1600 (wind convection, not symmetric; tf_wind_upload) */
+#define TF_NUM_MATS 8
 
 /* vector handles (device vectors owned by the context) */
 #define TF_VEC_RHS 0 /* assembled load vector (F_concentration_P1 :1610 or its P2 analogue) */
@@ -121,6 +122,12 @@ int tf_levelset_upload(tf_context* ctx, const double* ls_vert, const double* ls_
  * gives edge = 0.5*(a+b).  Values equal the host evaluation bit for bit.       */
 int tf_levelset_analytic(tf_context* ctx, int kind, const double* par, int npar, int p2);
 int tf_levelset_download(tf_context* ctx, double* ls_vert, double* ls_edge);
+/* The wind of N_P1P1 (TF_FORM_N): the vecP2IF field u_T of
+ * LocalAssemblerParams::surfCahnHilliardParams (surfactant/ifacetransp.h:933,
+ * buildWindCH :1129-1137), as interpolated by VecDescCL::Interpolate
+ * (misc/problem.h:714-732): xyz at every mesh vertex (wind_vert[3 nv]) and at
+ * every edge midpoint (wind_edge[3 ne], this library's edge numbering).      */
+int tf_wind_upload(tf_context* ctx, const double* wind_vert, const double* wind_edge);
 
 /* ---- interface DOFs -------------------------------------------------------- */
 /* IdxDescCL::DistributeDOFs(level, mg, &levelSet, dist) (misc/problem.cpp:283-336):

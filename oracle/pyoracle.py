@@ -16,8 +16,8 @@ LIB_PATH = os.path.join(HERE, "_build", "libtf_oracle.so")
 OK = 0
 ERR_ZERO_NODE = 2
 ERR_ZERO_PATTERN = 3
-FORM_M, FORM_A, FORM_CN, FORM_LAPM = 0, 1, 2, 3
-NUM_FORMS = 4
+FORM_M, FORM_A, FORM_CN, FORM_LAPM, FORM_N = 0, 1, 2, 3, 4
+NUM_FORMS = 5
 LS_SPHERE, LS_TORUS, LS_ELLIPSOID, LS_PLANE = 0, 1, 2, 3
 RHS_NONE, RHS_SPHERE_XYZ, RHS_CONST = 0, 1, 2
 
@@ -159,10 +159,12 @@ def make_patch(ls10):
 
 class AssembleOpts(C.Structure):
     _fields_ = [("p2", C.c_int), ("forms", C.c_uint), ("rhs_kind", C.c_int), ("rhs_par", C.c_double * 8),
-                ("chi", C.POINTER(C.c_double)), ("degenerate", C.c_int)]
+                ("chi", C.POINTER(C.c_double)), ("degenerate", C.c_int),
+                ("wind_vert", C.POINTER(C.c_double)), ("wind_edge", C.POINTER(C.c_double))]
 
 
-def make_opts(p2, forms, rhs_kind=RHS_NONE, rhs_par=(), chi=None, degenerate=False):
+def make_opts(p2, forms, rhs_kind=RHS_NONE, rhs_par=(), chi=None, degenerate=False, wind=None):
+    """wind: (wind_vert (nv, 3), wind_edge (ne, 3)) for FORM_N, the P2 wind at vertices and edge midpoints."""
     o = AssembleOpts()
     o.p2 = int(p2)
     o.forms = sum(1 << f for f in forms)
@@ -173,6 +175,10 @@ def make_opts(p2, forms, rhs_kind=RHS_NONE, rhs_par=(), chi=None, degenerate=Fal
     o._chi_keep = chi
     o.chi = _p(chi, C.c_double) if chi is not None else None
     o.degenerate = int(degenerate)
+    if wind is not None:
+        wv, we = (_in(np.asarray(w, dtype=np.float64).reshape(-1), np.float64) for w in wind)
+        o._wind_keep = (wv, we)
+        o.wind_vert, o.wind_edge = _p(wv, C.c_double), _p(we, C.c_double)
     return o
 
 
@@ -290,15 +296,18 @@ def set_threads(n):
     lib().orc_set_threads(C.c_int(n))
 
 
-def local_forms(xv, ls10, opts):
-    """Element matrices of one tet: returns (status, {form: (nl, nl)}, rhs[nl], n_facets)."""
+def local_forms(xv, ls10, opts, wind_loc=None):
+    """Element matrices of one tet: returns (status, {form: (nl, nl)}, rhs[nl], n_facets).
+    wind_loc: (10, 3) P2 wind at the tet's 4 vertices and 6 edge midpoints (FORM_N)."""
     L = lib()
     xv = np.ascontiguousarray(xv, dtype=np.float64)
     ls10 = np.ascontiguousarray(ls10, dtype=np.float64)
+    wl = None if wind_loc is None else np.ascontiguousarray(wind_loc, dtype=np.float64).reshape(-1)
     out = np.zeros((NUM_FORMS, 100))
     rhs = np.zeros(10)
     nf = C.c_int()
     st = L.orc_local_forms(_p(xv, C.c_double), _p(ls10, C.c_double), C.byref(opts), None,
+                           _p(wl, C.c_double) if wl is not None else None,
                            _p(out, C.c_double), _p(rhs, C.c_double), C.byref(nf))
     nl = 10 if opts.p2 else 4
     return st, {f: out[f, :nl * nl].reshape(nl, nl) for f in range(NUM_FORMS)}, rhs[:nl], nf.value

@@ -80,6 +80,11 @@ double now() {
 }
 
 // level sets (surfactant/Surface.hpp:71,130)
+// smooth test wind for N_P1P1 (not tangential: the form takes any field)
+Point3DCL wind_value(const Point3DCL& x) {
+    return Point3DCL(-x[1] + 0.2 * x[2], x[0] - 0.1, 0.3 * x[0] * x[1] + 0.05);
+}
+
 double ls_value(const std::string& shape, const Point3DCL& x) {
     if (shape == "sphere") return x.norm() - 1.0;
     if (shape == "torus") {  // R = 1, r = 0.4, symmetry axis z
@@ -238,8 +243,9 @@ int cmd_system(int argc, char** argv) {
         Point3DCL y = x - (x.norm() - 1.0) * (x / x.norm());
         return 13. * y[0] * y[1] * y[2];
     };
-    MatrixCL Mm, Am, Cm;
+    MatrixCL Mm, Am, Cm, Nm;
     VectorCL rhs;
+    double t_asm = 0.;
     t0 = now();
     if (!p2) {
         FEMatDescCL M(&ifIdx, &ifIdx, &LocalAssembler::M_P1P1), A(&ifIdx, &ifIdx, &LocalAssembler::A_P1P1),
@@ -253,6 +259,33 @@ int cmd_system(int argc, char** argv) {
         Cm = C.Data;
         rhs.resize(f.Data.size());
         rhs = f.Data;
+        t_asm = now() - t0;
+        // wind convection N_P1P1 (surfactant/ifacetransp.h:1590-1600) with a
+        // vecP2IF wind interpolated as in surfphasesep/surfphasesep.cpp:198-213, 417-420
+        IdxDescCL velIdx(vecP2IF_FE);
+        velIdx.DistributeDOFs(0, mg, &levelSet);
+        VecDescCL wind(&velIdx);
+        wind.Interpolate(mg, [](Point3DCL const& x) { return wind_value(x); });
+        FESystem nsys;
+        nsys.params.levelSet.SetIdx(&lsIdx);
+        nsys.params.levelSet.Data = levelSet.Data;
+        nsys.params.surfCahnHilliardParams.u_T = &wind;
+        FEMatDescCL N(&ifIdx, &ifIdx, &LocalAssembler::N_P1P1);
+        nsys.matrices = {&N};
+        setupFESystem(mg, nsys);
+        Nm = N.Data;
+        write_csr(w, "N", Nm);
+        std::vector<double> wv, we;
+        DROPS_FOR_TRIANG_VERTEX(mg, 0, it) {
+            const Point3DCL v = wind_value(it->GetCoord());
+            for (int c = 0; c < 3; ++c) wv.push_back(v[c]);
+        }
+        DROPS_FOR_TRIANG_EDGE(mg, 0, it) {
+            const Point3DCL v = wind_value(GetBaryCenter(*it));
+            for (int c = 0; c < 3; ++c) we.push_back(v[c]);
+        }
+        w.d("wind_vert", wv);
+        w.d("wind_edge", we);
     } else {
         // FESystemAccumulator::visit restated for the P2 forms above
         const size_t m = ifIdx.NumUnknowns();
@@ -279,7 +312,8 @@ int cmd_system(int argc, char** argv) {
         bA.Build();
         bC.Build();
     }
-    w.s("time_assemble", now() - t0);
+    if (p2) t_asm = now() - t0;
+    w.s("time_assemble", t_asm);
     write_csr(w, "M", Mm);
     write_csr(w, "A", Am);
     write_csr(w, "C", Cm);

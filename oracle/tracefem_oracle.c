@@ -435,9 +435,12 @@ static double rhs_value(const orc_assemble_opts* o, const double x[3]) {
 }
 
 int orc_local_forms(const double xv[4][3], const double ls10[10], const orc_assemble_opts* o,
-                    const double* chi_loc, double out[ORC_NUM_MAT_FORMS][100], double rhs[10], int* n_facets) {
+                    const double* chi_loc, const double* wind_loc, double out[ORC_NUM_MAT_FORMS][100],
+                    double rhs[10], int* n_facets) {
     init_quad();
     const int nl = o->p2 ? 10 : 4;
+    const int wantN = (o->forms & (1u << ORC_FORM_N)) != 0;
+    if (wantN && (o->p2 || !wind_loc)) return ORC_ERR_BAD_INPUT;
     for (int f = 0; f < ORC_NUM_MAT_FORMS; ++f) memset(out[f], 0, sizeof(double) * 100);
     if (rhs) memset(rhs, 0, sizeof(double) * 10);
     orc_patch_t P;
@@ -496,6 +499,17 @@ int orc_local_forms(const double xv[4][3], const double ls10[10], const orc_asse
                     if (o->forms & (1u << ORC_FORM_A)) out[ORC_FORM_A][i * nl + j] += wq * a;
                     if (o->forms & (1u << ORC_FORM_LAPM)) out[ORC_FORM_LAPM][i * nl + j] += wq * (mob * a);
                 }
+            /* N_P1P1 (surfactant/ifacetransp.h:1590-1600): the P2 wind at the
+               point (LocalP2CL evaluated there, buildWindCH :1129-1137) dotted
+               with the surface gradient of phi_j, times phi_i */
+            if (wantN) {
+                double h[10], wnd[3] = {0., 0., 0.};
+                p2_vals(b, h);
+                for (int k = 0; k < 10; ++k)
+                    for (int r = 0; r < 3; ++r) wnd[r] += wind_loc[3 * k + r] * h[k];
+                for (int i = 0; i < 4; ++i)
+                    for (int j = 0; j < 4; ++j) out[ORC_FORM_N][i * 4 + j] += wq * (dot3(wnd, sg[j]) * phi[i]);
+            }
             if (rhs && o->rhs_kind != ORC_RHS_NONE) {
                 double x[3];
                 for (int c = 0; c < 3; ++c) x[c] = xv[0][c] * b[0] + xv[1][c] * b[1] + xv[2][c] * b[2] + xv[3][c] * b[3];
@@ -521,9 +535,11 @@ int orc_local_forms(const double xv[4][3], const double ls10[10], const orc_asse
         for (int i = 0; i < nl; ++i)
             for (int j = i; j < nl; ++j) out[ORC_FORM_CN][i * nl + j] = acc[i * nl + j] * absdet;
     }
-    for (int f = 0; f < ORC_NUM_MAT_FORMS; ++f)
+    for (int f = 0; f < ORC_NUM_MAT_FORMS; ++f) {
+        if (f == ORC_FORM_N) continue; /* the only form that is not symmetric */
         for (int i = 0; i < nl; ++i)
             for (int j = 0; j < i; ++j) out[f][i * nl + j] = out[f][j * nl + i];
+    }
     return ORC_OK;
 }
 
@@ -614,10 +630,18 @@ int orc_assemble(int64_t nt, const int32_t* tet_v, const int32_t* tet_e, const d
         double xv[4][3], ls10[10];
         for (int i = 0; i < 4; ++i) memcpy(xv[i], coords + 3 * tet_v[4 * t + i], sizeof xv[i]);
         gather_ls10(tet_v + 4 * t, tet_e + 6 * t, ls_vert, ls_edge, ls10);
-        double chi_loc[4], loc[ORC_NUM_MAT_FORMS][100], b[10];
+        double chi_loc[4], wind_loc[30], loc[ORC_NUM_MAT_FORMS][100], b[10];
         if (o->chi)
             for (int i = 0; i < 4; ++i) chi_loc[i] = o->chi[I[i]];
-        int st = orc_local_forms(xv, ls10, o, o->chi ? chi_loc : NULL, loc, b, NULL);
+        const int haveW = o->wind_vert && o->wind_edge;
+        if (haveW) {
+            for (int k = 0; k < 4; ++k)
+                for (int r = 0; r < 3; ++r) wind_loc[3 * k + r] = o->wind_vert[3 * (int64_t)tet_v[4 * t + k] + r];
+            for (int k = 0; k < 6; ++k)
+                for (int r = 0; r < 3; ++r)
+                    wind_loc[3 * (4 + k) + r] = o->wind_edge[3 * (int64_t)tet_e[6 * t + k] + r];
+        }
+        int st = orc_local_forms(xv, ls10, o, o->chi ? chi_loc : NULL, haveW ? wind_loc : NULL, loc, b, NULL);
         if (st) {
             free(colind);
             for (int f = 0; f < ORC_NUM_MAT_FORMS; ++f) { free(vals[f]); vals[f] = NULL; }

@@ -81,7 +81,8 @@ void orc_lattice2(double verts[10][4], int tets[8][4]);
 #define ORC_FORM_A 1        /* A_P1P1 / A_P2P2 (Laplace-Beltrami)                 */
 #define ORC_FORM_CN 2       /* C_n_P1P1 / C_n_P2P2 (normal-gradient volume stab.) */
 #define ORC_FORM_LAPM 3     /* LaplaceM_P1P1 (degenerate mobility)                */
-#define ORC_NUM_MAT_FORMS 4
+#define ORC_FORM_N 4        /* N_P1P1 (wind convection, not symmetric; P1 only)   */
+#define ORC_NUM_MAT_FORMS 5
 #define ORC_RHS_NONE 0
 #define ORC_RHS_SPHERE_XYZ 1 /* f(y) = c*y0*y1*y2 at y = ext(x) of a sphere (par: cx,cy,cz,r,c) */
 #define ORC_RHS_CONST 2      /* f = c                                                          */
@@ -93,6 +94,8 @@ typedef struct {
     double rhs_par[8];
     const double* chi;     /* P1 vector (per DOF) for LaplaceM; NULL -> mobility 1 */
     int degenerate;        /* LaplaceM uses chi(1-chi) clipped at 0 when set        */
+    const double* wind_vert; /* N: P2 wind, xyz per mesh vertex (3 nv)              */
+    const double* wind_edge; /* N: xyz per mesh edge, at its midpoint (3 ne)        */
 } orc_assemble_opts;
 
 /* Builds the CSR pattern (union of active-tet blocks, rows sorted) and the
@@ -107,8 +110,8 @@ int orc_assemble(int64_t nt, const int32_t* tet_v, const int32_t* tet_e, const d
 
 /* local element matrices of one tet (nloc = 4 or 10) for tests */
 int orc_local_forms(const double xv[4][3], const double ls10[10], const orc_assemble_opts* opts,
-                    const double* chi_loc, double out[ORC_NUM_MAT_FORMS][100], double rhs[10],
-                    int* n_facets);
+                    const double* chi_loc, const double* wind_loc, double out[ORC_NUM_MAT_FORMS][100],
+                    double rhs[10], int* n_facets);
 
 /* ---- legacy P1 interface forms (surfactant.cpp path) ------------------- */
 /* f(x) = p0 + p1 x + p2 y + p3 z + p4 x^2 + p5 y^2 + p6 z^2 + p7 xy + p8 xz + p9 yz */

@@ -62,6 +62,12 @@ def system_case(name, fe, ls, shape, n, a, solve):
         M=d["M.vals"], A=d["A.vals"], C=d["C.vals"], rhs=d["rhs"],
         ref_time_dofs=d["time_dofs"][0], ref_time_assemble=d["time_assemble"][0],
     )
+    if "N.vals" in d:
+        # N_P1P1 with the harness wind; nodal wind values per vertex / edge (xyz), edges in this library's order
+        assert np.array_equal(d["N.rowptr"], d["M.rowptr"]) and np.array_equal(d["N.colind"], d["M.colind"])
+        wind_edge = np.empty((mesh.ne, 3))
+        wind_edge[emap] = d["wind_edge"].reshape(-1, 3)
+        out.update(N=d["N.vals"], wind_vert=d["wind_vert"].reshape(-1, 3), wind_edge=wind_edge)
     if solve:
         assert np.array_equal(d["S.rowptr"], d["M.rowptr"]) and np.array_equal(d["S.colind"], d["M.colind"])
         out.update(S=d["S.vals"], x=d["x"], iters=int(d["iters"][0]), resid=float(d["resid"][0]),

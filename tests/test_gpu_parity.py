@@ -112,6 +112,43 @@ def test_dofs_narrow_band_dist(ctx, dist, p2):
         assert na > na0
 
 
+@pytest.mark.parametrize("name,kind,par", [s for s in SYSTEMS if "p1" in s[0]])
+def test_wind_convection_parity(ctx, golden, name, kind, par):
+    """N_P1P1 (surfactant/ifacetransp.h:1590-1600) against the reference's matrix for its vecP2IF wind:
+    the one form that is not symmetric (scatter by row-local and column-local index)."""
+    g = golden(name)
+    om, p2, na, nd = setup_case(ctx, g, kind, par)
+    with pytest.raises(tf.TraceFEMError):  # no wind on this mesh yet
+        ctx.setup_fe_system([tf.FORM_N])
+    ctx.wind_upload(g["wind_vert"], g["wind_edge"])
+    nnz = ctx.setup_fe_system([tf.FORM_M, tf.FORM_N])
+    assert nnz == len(g["colind"])
+    rp, ci, v = ctx.matrix(tf.FORM_N)
+    assert np.array_equal(rp, g["rowptr"]) and np.array_equal(ci, g["colind"])
+    ok, err = mat_close(v, g["N"])
+    assert ok, err
+    # alpha M + N, the convective block of surfphasesep.cpp:432
+    ctx.lincomb([tf.FORM_M, tf.FORM_N], [1000.0, 1.0])
+    rp, ci, s_ = ctx.matrix(tf.MAT_SYS)
+    ok, err = mat_close(s_, 1000.0 * g["M"] + g["N"])
+    assert ok, err
+    # a new mesh drops the wind
+    brick(ctx, int(g["n"]), float(g["a"]))
+    ctx.levelset_analytic(kind, par, False)
+    ctx.distribute_dofs(tf.P1IF)
+    with pytest.raises(tf.TraceFEMError):
+        ctx.setup_fe_system([tf.FORM_N])
+
+
+def test_wind_convection_is_p1_only(ctx, golden):
+    g = golden("sphere_p2_n8.npz")
+    setup_case(ctx, g, tf.LS_SPHERE, [0, 0, 0, 1.0])
+    nv, ne, nt = ctx.mesh_info()
+    ctx.wind_upload(np.zeros((nv, 3)), np.zeros((ne, 3)))
+    with pytest.raises(tf.TraceFEMError):
+        ctx.setup_fe_system([tf.FORM_N])
+
+
 @pytest.mark.parametrize("name,kind,par", SYSTEMS)
 def test_assembly_parity(ctx, golden, name, kind, par):
     g = golden(name)

@@ -53,6 +53,28 @@ def test_assembly_matches_reference(golden, name, kind, par):
     assert ok, err
 
 
+@pytest.mark.parametrize("name,kind,par", [s for s in SYSTEMS if "p1" in s[0]])
+def test_wind_convection_matches_reference(golden, name, kind, par):
+    """N_P1P1 (surfactant/ifacetransp.h:1590-1600): int (w . grad_Gamma phi_j) phi_i with the reference's
+    vecP2IF wind interpolated at vertices and edge midpoints; a form that is not symmetric."""
+    g = golden(name)
+    mesh = O.brick(int(g["n"]), a=float(g["a"]))
+    lv, le = O.levelset(mesh, kind, par, p2=False)
+    st, na, nd, dv, de, act = O.distribute_dofs(mesh, lv, le, False)
+    opts = O.make_opts(False, [O.FORM_M, O.FORM_N], wind=(g["wind_vert"], g["wind_edge"]))
+    st, rp, ci, vals, rhs = O.assemble(mesh, lv, le, act, dv, de, nd, opts)
+    assert st == O.OK
+    assert np.array_equal(rp, g["rowptr"]) and np.array_equal(ci, g["colind"])
+    ok, err = mat_close(vals[O.FORM_N], g["N"])
+    assert ok, err
+    ok, err = mat_close(vals[O.FORM_M], g["M"])
+    assert ok, err
+    # not symmetric: N differs from its transpose
+    import scipy.sparse as sp
+    Nm = sp.csr_matrix((g["N"], g["colind"], g["rowptr"]))
+    assert abs(Nm - Nm.T).max() > 1e-3 * abs(Nm).max()
+
+
 @pytest.mark.parametrize("name", ["c1_sphere_p1_n16.npz", "sphere_p2_n8.npz", "torus_p1_n16.npz"])
 def test_pcg_jacobi_matches_reference(golden, name):
     g = golden(name)
