@@ -48,7 +48,7 @@ EXPORTS = [
     "tf_mesh_brick_batch", "tf_levelset_analytic_batch", "tf_batch_info", "tf_batch_lincomb", "tf_batch_pcg_jacobi",
     "tf_batch_tune", "tf_batch_config", "tf_mlp_init", "tf_mlp_get_weights", "tf_mlp_set_weights", "tf_mlp_forward",
     "tf_mlp_gradient", "tf_mlp_train", "tf_ch_features", "tf_ch_steps_learned", "tf_gmres_options", "tf_timing_enable",
-    "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2", "tf_spmv_timed", "tf_stream_read_timed", "tf_wind_upload",
+    "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2", "tf_spmv_timed", "tf_stream_read_timed", "tf_wind_upload", "tf_vec_write", "tf_vec_read", "tf_ch_stats",
     "tf_host_alloc", "tf_host_free",
 ]
 
@@ -207,6 +207,38 @@ class TraceFEM:
         return coords, tv, te, ev
 
     # ---- level set ---------------------------------------------------------
+    def ch_stats(self, eps, xi=1.0):
+        """The integrals of the reference's per-step statistics (surfphasesep.cpp:324-345) for TF_VEC_CHI."""
+        out = np.zeros(6)
+        self._check(self.L.tf_ch_stats(self.h, C.c_double(eps), C.c_double(xi), _dp(out)))
+        return {"Integral.SurfacaAreaP1": out[0], "Integral.FESolution.RaftFraction": out[1],
+                "Integral.FESolution.PerimeterEstimate": out[2], "Integral.FESolution.LyapunovEnergy": out[3],
+                "c_h.Max": out[4], "c_h.Min": out[5]}
+
+    def write_ch_stats(self, path, t, h, eps, xi=1.0, extra=None):
+        """One stats/t_<i>.json of the reference's exportStats: dotted keys as nested objects."""
+        import json
+
+        flat = {"t": t, "h": h, "DOF.c_h": self.m, "DOF.mu_h": self.m, **self.ch_stats(eps, xi), **(extra or {})}
+        tree = {}
+        for key, val in flat.items():
+            node = tree
+            *parents, leaf = key.split(".")
+            for p in parents:
+                node = node.setdefault(p, {})
+            node[leaf] = float(val) if not isinstance(val, (bool, str)) else val
+        with open(path, "w") as f:
+            json.dump(tree, f, indent=4)
+        return tree
+
+    def vec_write(self, vec, path):
+        """VecDescCL::Write(os, binary=true): 64-bit count, then the doubles."""
+        self._check(self.L.tf_vec_write(self.h, C.c_int(vec), os.fsencode(path)))
+
+    def vec_read(self, vec, path, n_expected=-1):
+        """VecDescCL::Read(is, binary=true); a count other than n_expected (>= 0) raises."""
+        self._check(self.L.tf_vec_read(self.h, C.c_int(vec), os.fsencode(path), C.c_int64(n_expected)))
+
     def wind_upload(self, wind_vert, wind_edge):
         """P2 wind for FORM_N: xyz at every vertex (nv, 3) and at every edge midpoint (ne, 3)."""
         wv = np.ascontiguousarray(wind_vert, dtype=np.float64).reshape(-1)

@@ -1,4 +1,5 @@
 // extern "C" entry points of libtracefem (include/tracefem.h).
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -523,6 +524,49 @@ int tf_vec_download(tf_context* t, int vec, double* host, int64_t n) {
     return TF_OK;
 }
 
+int tf_vec_write(tf_context* t, int vec, const char* path) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    TF_TRY(vec_need(c, vec));
+    if (!path) return tf::set_err(c, TF_ERR_BAD_INPUT, "vec_write: path required");
+    const size_t n = c->vecs[vec].n;
+    std::vector<double> h(n);
+    if (n) TF_CUDA(c, cudaMemcpyAsync(h.data(), c->vecs[vec].p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return tf::set_err(c, TF_ERR_BAD_INPUT, std::string("vec_write: cannot open ") + path);
+    const uint64_t cnt = (uint64_t)n;  // size_t on the 64-bit hosts the reference writes from
+    bool ok = std::fwrite(&cnt, sizeof cnt, 1, f) == 1 && (n == 0 || std::fwrite(h.data(), sizeof(double), n, f) == n);
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? TF_OK : tf::set_err(c, TF_ERR_BAD_INPUT, std::string("vec_write: write failed: ") + path);
+}
+
+int tf_vec_read(tf_context* t, int vec, const char* path, int64_t n_expected) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    TF_TRY(vec_need(c, vec));
+    if (!path) return tf::set_err(c, TF_ERR_BAD_INPUT, "vec_read: path required");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return tf::set_err(c, TF_ERR_BAD_INPUT, std::string("vec_read: cannot open ") + path);
+    uint64_t cnt = 0;
+    const bool head = std::fread(&cnt, sizeof cnt, 1, f) == 1;
+    if (!head || (n_expected >= 0 && cnt != (uint64_t)n_expected) || cnt > ((uint64_t)1 << 40)) {
+        std::fclose(f);
+        return tf::set_err(c, TF_ERR_BAD_INPUT,
+                           "VecDescBaseCL::Read: Number of Unknowns does not match, wrong FE-type?");
+    }
+    std::vector<double> h((size_t)cnt);
+    const bool body = cnt == 0 || std::fread(h.data(), sizeof(double), (size_t)cnt, f) == (size_t)cnt;
+    std::fclose(f);
+    if (!body) return tf::set_err(c, TF_ERR_BAD_INPUT, std::string("vec_read: file too short: ") + path);
+    TF_TRY(tf::ensure(c, c->vecs[vec], (size_t)cnt));
+    if (cnt) TF_CUDA(c, cudaMemcpyAsync(c->vecs[vec].p, h.data(), sizeof(double) * cnt, cudaMemcpyHostToDevice, c->stream));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TF_OK;
+}
+
 int tf_vec_size(tf_context* t, int vec, int64_t* n) {
     CTX_CHECK(t);
     TF_TRY(vec_need(&t->c, vec));
@@ -871,6 +915,14 @@ int tf_ch_steps_learned(tf_context* t, int nsteps, double dt, double mobility, d
     P.mb_tiles = minibatch_tiles;
     P.lr = lr;
     return tf::ch_steps_learned(c, P, iters, resids, used);
+}
+
+int tf_ch_stats(tf_context* t, double eps, double xi, double* out) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (!out) return tf::set_err(c, TF_ERR_BAD_INPUT, "ch_stats: output required");
+    return tf::ch_stats(c, eps, xi, out);
 }
 
 int tf_ch_steps(tf_context* t, int nsteps, double dt, double mobility, double eps, double beta_s, double xi,

@@ -83,4 +83,99 @@ int ch_steps(Context* c, int nsteps, double dt, double mob, double eps, double b
     return TF_OK;
 }
 
+// ---------------------------------------------------------------------------
+// per-step statistics of surfphasesep/surfphasesep.cpp:324-345 (exportStats):
+// with 1 the ones vector and f0(c) = xi (c (1 - c))^2 (:135-139),
+//   area = 1'M1, raft fraction = 1'M chi / area, perimeter = eps chi'A chi,
+//   Lyapunov energy = (M1)'f0(chi) + eps^2/2 chi'A chi, max / min of chi.
+// Row per thread over the shared CSR pattern of M and A; FP64 partial sums
+// per block in a fixed tree, then one block sums the block partials in order.
+// ---------------------------------------------------------------------------
+constexpr int kStatThreads = 256;
+
+__global__ void __launch_bounds__(kStatThreads) k_ch_stats(int64_t m, const int32_t* __restrict__ rowptr,
+                                                           const int32_t* __restrict__ colind,
+                                                           const double* __restrict__ mv, const double* __restrict__ av,
+                                                           const double* __restrict__ chi, double xi,
+                                                           double* __restrict__ part /* [grid][6] */) {
+    double s[4] = {0., 0., 0., 0.};
+    double mx = -INFINITY, mn = INFINITY;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x) {
+        double m1 = 0., mc = 0., ac = 0.;
+        for (int32_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+            const double cj = chi[colind[k]];
+            m1 += mv[k];
+            mc += mv[k] * cj;
+            ac += av[k] * cj;
+        }
+        const double cr = chi[r], q = cr * (1. - cr);
+        s[0] += m1;
+        s[1] += mc;
+        s[2] += cr * ac;
+        s[3] += m1 * (xi * (q * q));
+        mx = fmax(mx, cr);
+        mn = fmin(mn, cr);
+    }
+    __shared__ double red[6][kStatThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        for (int k = 0; k < 4; ++k) s[k] += __shfl_xor_sync(0xffffffffu, s[k], o);
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    }
+    if (lane == 0) {
+        for (int k = 0; k < 4; ++k) red[k][w] = s[k];
+        red[4][w] = mx;
+        red[5][w] = mn;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int k = threadIdx.x;
+        double a = red[k][0];
+        for (int ww = 1; ww < kStatThreads / 32; ++ww)
+            a = k < 4 ? a + red[k][ww] : (k == 4 ? fmax(a, red[k][ww]) : fmin(a, red[k][ww]));
+        part[(size_t)blockIdx.x * 6 + k] = a;
+    }
+}
+
+__global__ void k_ch_stats_final(int nblocks, const double* __restrict__ part, double* __restrict__ out) {
+    if (threadIdx.x < 6) {
+        const int k = threadIdx.x;
+        double a = part[k];
+        for (int b = 1; b < nblocks; ++b) {
+            const double v = part[(size_t)b * 6 + k];
+            a = k < 4 ? a + v : (k == 4 ? fmax(a, v) : fmin(a, v));
+        }
+        out[k] = a;
+    }
+}
+
+int ch_stats(Context* c, double eps, double xi, double* out) {
+    const CSR& M = c->mats[TF_FORM_M];
+    const CSR& A = c->mats[TF_FORM_A];
+    if (!M.vals || !A.vals || M.pattern_gen != A.pattern_gen)
+        return set_err(c, TF_ERR_BAD_INPUT, "ch_stats: assemble M and A (one pattern) first");
+    const int64_t m = M.m;
+    if (m <= 0 || (int64_t)c->vecs[TF_VEC_CHI].n != m)
+        return set_err(c, TF_ERR_BAD_INPUT, "ch_stats: TF_VEC_CHI must hold m values");
+    const int grid = grid_for(c, m, kStatThreads, 4);
+    TF_TRY(ensure(c, c->scratch, sizeof(double) * (6 * (size_t)grid + 8)));
+    double* part = reinterpret_cast<double*>(c->scratch.p);
+    k_ch_stats<<<grid, kStatThreads, 0, c->stream>>>(m, M.rowptr, M.colind, M.vals, A.vals, c->vecs[TF_VEC_CHI].p,
+                                                     xi, part);
+    k_ch_stats_final<<<1, 32, 0, c->stream>>>(grid, part, part + 6 * (size_t)grid);
+    c->launches += 2;
+    TF_CUDA(c, cudaGetLastError());
+    double r[6];
+    TF_CUDA(c, cudaMemcpyAsync(r, part + 6 * (size_t)grid, sizeof r, cudaMemcpyDeviceToHost, c->stream));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    out[0] = r[0];                              // Integral.SurfacaAreaP1
+    out[1] = r[1] / r[0];                       // Integral.FESolution.RaftFraction
+    out[2] = eps * r[2];                        // Integral.FESolution.PerimeterEstimate
+    out[3] = r[3] + 0.5 * eps * eps * r[2];     // Integral.FESolution.LyapunovEnergy
+    out[4] = r[4];                              // c_h.Max
+    out[5] = r[5];                              // c_h.Min
+    return TF_OK;
+}
+
 }  // namespace tf

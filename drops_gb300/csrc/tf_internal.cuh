@@ -438,6 +438,7 @@ int mlp_set_weights(Context* c, const float* w);
 int mlp_get_weights(Context* c, float* w);
 int mlp_forward_dev(Context* c, const __nv_bfloat16* X, int64_t n, float* pred);
 int ch_rhs(Context* c, const double* X, double dt, double beta_s, double xi);
+int ch_stats(Context* c, double eps, double xi, double* out);
 int ch_geometry(Context* c);
 int ch_features_dev(Context* c, const double* xn, const double* xp, const double* xnext);
 int ch_steps_learned(Context* c, const ChLearnParams& P, int* iters, double* resids, int* used);

@@ -204,6 +204,13 @@ int tf_ch_block(tf_context* ctx, double alpha, double mob, double rho, double ep
 int tf_vec_upload(tf_context* ctx, int vec, int64_t n, const double* host);
 int tf_vec_download(tf_context* ctx, int vec, double* host, int64_t n);
 int tf_vec_size(tf_context* ctx, int vec, int64_t* n);
+/* VecDescBaseCL::Write(os, binary = true) (misc/problem.h:928-944): the count
+ * as a 64-bit size_t, then the values as doubles, host byte order.           */
+int tf_vec_write(tf_context* ctx, int vec, const char* path);
+/* VecDescBaseCL::Read(is, binary = true) (misc/problem.h:947-975): a count
+ * other than n_expected (n_expected >= 0) is TF_ERR_BAD_INPUT, where the
+ * reference throws DROPSErrCL; n_expected < 0 takes the file's count.       */
+int tf_vec_read(tf_context* ctx, int vec, const char* path, int64_t n_expected);
 /* Sets vector `vec` to n copies of `value` on the device (e.g. a zero initial guess). */
 int tf_vec_fill(tf_context* ctx, int vec, int64_t n, double value);
 /* y = A x on device vectors (y_Ax, num/spmat.h:1684-1709). */
@@ -338,6 +345,13 @@ int tf_pcg_jacobi_noalloc(int64_t m, const int32_t* rowptr, const int32_t* colin
  * iteration count and relative residual; TF_VEC_CHI receives the final chi. */
 int tf_ch_steps(tf_context* ctx, int nsteps, double dt, double mobility, double eps, double beta_s, double xi,
                 double rho_vol, int restart, double tol, int max_iter, int warm, int* iters, double* resids);
+/* The integrals of the per-step statistics of surfphasesep/surfphasesep.cpp:
+ * 324-345 (exportStats) for chi = TF_VEC_CHI, M = TF_FORM_M, A = TF_FORM_A,
+ * f0(c) = xi (c (1 - c))^2 (:135-139): out[0] = 1'M1 (Integral.SurfacaAreaP1),
+ * out[1] = 1'M chi / out[0] (RaftFraction), out[2] = eps chi'A chi
+ * (PerimeterEstimate), out[3] = (M1)'f0(chi) + eps^2/2 chi'A chi
+ * (LyapunovEnergy), out[4] / out[5] = max / min of chi (c_h.Max / c_h.Min). */
+int tf_ch_stats(tf_context* ctx, double eps, double xi, double* out);
 /* tf_ch_steps with the learned warm start: the MLP (tf_mlp_init first, or a
  * default initialisation) is trained online with `epochs` Adam passes
  * (minibatch_tiles x 128 DOFs, rate lr) on the increment of each of the first

@@ -331,6 +331,11 @@ int cmd_system(int argc, char** argv) {
         w.i("iters", solver.GetIter());
         w.s("resid", solver.GetResid());
         w.d("x", std::vector<double>(std::begin(x), std::end(x)));
+        // the solution as VecDescCL::Write writes it, binary (misc/problem.h:928-944)
+        VecDescCL xv(&ifIdx);
+        xv.Data = x;
+        std::ofstream vf(std::string(argv[argc - 1]) + ".vec", std::ios::binary);
+        xv.Write(vf, true);
     }
     return 0;
 }

@@ -32,10 +32,13 @@ def sha(a):
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-def run(*args):
+def run(*args, keep_vec=None):
     with tempfile.TemporaryDirectory() as d:
         out = os.path.join(d, "out.bin")
         subprocess.check_call([HARNESS, *args, out], cwd=d, stdout=subprocess.DEVNULL)
+        if keep_vec and os.path.exists(out + ".vec"):  # VecDescCL::Write(binary) of the solution
+            with open(out + ".vec", "rb") as src, open(os.path.join(HERE, keep_vec), "wb") as dst:
+                dst.write(src.read())
         return read_tfg(out)
 
 
@@ -44,8 +47,8 @@ def edge_map(mesh, ref_edge_v):
     return np.array([key[tuple(sorted(p))] for p in ref_edge_v.reshape(-1, 2).tolist()], dtype=np.int64)
 
 
-def system_case(name, fe, ls, shape, n, a, solve):
-    d = run("system", fe, ls, shape, str(n), repr(a), "1" if solve else "0")
+def system_case(name, fe, ls, shape, n, a, solve, keep_vec=None):
+    d = run("system", fe, ls, shape, str(n), repr(a), "1" if solve else "0", keep_vec=keep_vec)
     mesh = O.brick(n, a=a)
     emap = edge_map(mesh, d["edge_v"])
     ls_edge = np.empty(mesh.ne)
@@ -119,7 +122,7 @@ def legacy_forms_case(n=10, a=1.6):
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
-    system_case("c1_sphere_p1_n16.npz", "p1", "lsP1", "sphere", 16, 5.0 / 3.0, True)
+    system_case("c1_sphere_p1_n16.npz", "p1", "lsP1", "sphere", 16, 5.0 / 3.0, True, keep_vec="c1_sphere_p1_n16_x.vec")
     system_case("sphere_p2_n8.npz", "p2", "lsP2", "sphere", 8, 5.0 / 3.0, True)
     system_case("torus_p1_n16.npz", "p1", "lsP1", "torus", 16, 1.6, True)
     system_case("torus_p2_n10.npz", "p2", "lsP2", "torus", 10, 1.6, False)

@@ -140,6 +140,29 @@ def test_wind_convection_parity(ctx, golden, name, kind, par):
         ctx.setup_fe_system([tf.FORM_N])
 
 
+def test_vecdesc_write_read(ctx, golden, tmp_path):
+    """tf_vec_write writes exactly the bytes of the reference's VecDescCL::Write(binary); tf_vec_read reads
+    them back and rejects a count that differs from the expected one, as VecDescBaseCL::Read throws."""
+    import os
+
+    g = golden("c1_sphere_p1_n16.npz")
+    ref = open(os.path.join(os.path.dirname(__file__), "golden", "c1_sphere_p1_n16_x.vec"), "rb").read()
+    ctx.vec_upload(tf.VEC_X, g["x"])
+    out = tmp_path / "x.vec"
+    ctx.vec_write(tf.VEC_X, str(out))
+    assert out.read_bytes() == ref
+    ctx.vec_read(tf.VEC_T1, str(out), n_expected=len(g["x"]))
+    assert np.array_equal(ctx.vec_download(tf.VEC_T1), g["x"])
+    with pytest.raises(tf.TraceFEMError):
+        ctx.vec_read(tf.VEC_T1, str(out), n_expected=len(g["x"]) + 1)
+    short = tmp_path / "short.vec"
+    short.write_bytes(ref[:100])
+    with pytest.raises(tf.TraceFEMError):
+        ctx.vec_read(tf.VEC_T1, str(short))
+    with pytest.raises(tf.TraceFEMError):
+        ctx.vec_read(tf.VEC_T1, str(tmp_path / "missing.vec"))
+
+
 def test_wind_convection_is_p1_only(ctx, golden):
     g = golden("sphere_p2_n8.npz")
     setup_case(ctx, g, tf.LS_SPHERE, [0, 0, 0, 1.0])
@@ -416,6 +439,39 @@ def test_ch_steps_parity(ctx, golden):
     assert np.linalg.norm(X[:nd] - OX[:nd]) <= 1e-8 * np.linalg.norm(OX[:nd])
     for a, b in zip(its, oits):
         assert abs(int(a) - b) <= max(5, b // 50), (its, oits)
+
+
+def test_ch_stats(ctx, golden, tmp_path):
+    """Integrals of the per-step statistics (surfphasesep.cpp:324-345) after three CH steps on the torus,
+    against the same formulas on the reference's M and A: area 1'M1, raft fraction 1'M chi / area,
+    perimeter eps chi'A chi, Lyapunov energy (M1)'f0(chi) + eps^2/2 chi'A chi, f0(c) = xi (c (1 - c))^2."""
+    import json
+
+    import scipy.sparse as sp
+
+    g = golden("torus_p1_n16.npz")
+    om, p2, na, nd = setup_case(ctx, g, O.LS_TORUS, [1.0, 0.4, 2])
+    ctx.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN])
+    dt, eps, h, xi = 1e-3, 0.02, 2 * float(g["a"]) / int(g["n"]), 0.7
+    rng = np.random.default_rng(5)
+    ctx.vec_upload(tf.VEC_X, np.concatenate([0.5 + rng.uniform(-0.01, 0.01, nd), np.zeros(nd)]))
+    ctx.ch_steps(3, dt, 1.0, eps, 0.0, xi, h, restart=50, tol=1e-10)
+    chi = ctx.vec_download(tf.VEC_CHI)
+    st = ctx.ch_stats(eps, xi)
+    M = sp.csr_matrix((g["M"], g["colind"], g["rowptr"]))
+    A = sp.csr_matrix((g["A"], g["colind"], g["rowptr"]))
+    one = np.ones(nd)
+    area = one @ (M @ one)
+    f0 = xi * (chi * (1 - chi)) ** 2
+    want = {"Integral.SurfacaAreaP1": area, "Integral.FESolution.RaftFraction": (M @ chi) @ one / area,
+            "Integral.FESolution.PerimeterEstimate": eps * (chi @ (A @ chi)),
+            "Integral.FESolution.LyapunovEnergy": (M @ one) @ f0 + 0.5 * eps * eps * (chi @ (A @ chi)),
+            "c_h.Max": chi.max(), "c_h.Min": chi.min()}
+    for k, v in want.items():
+        assert abs(st[k] - v) <= 1e-12 * abs(v), (k, st[k], v)
+    tree = ctx.write_ch_stats(str(tmp_path / "t_3.json"), t=3 * dt, h=h, eps=eps, xi=xi)
+    back = json.load(open(tmp_path / "t_3.json"))
+    assert back == tree and back["DOF"]["c_h"] == nd and back["Integral"]["FESolution"]["RaftFraction"] > 0
 
 
 def test_patch_topology_bitexact(ctx, golden):

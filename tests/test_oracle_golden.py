@@ -165,3 +165,18 @@ def test_oracle_legacy_forms_match_reference(golden):
     assert np.array_equal(g["A_rowptr"], g["rowptr"]) and np.array_equal(g["A_colind"], g["colind"])
     for v, ref in ((M, g["M"]), (A, g["A"]), (rhs, g["rhs"])):
         assert np.max(np.abs(v - ref)) <= 1e-12 * np.max(np.abs(ref)), np.max(np.abs(v - ref)) / np.max(np.abs(ref))
+
+
+def test_vecdesc_binary_layout(golden):
+    """VecDescBaseCL::Write(os, binary=true) (misc/problem.h:928-944), written by the reference itself: a
+    64-bit count, then the doubles; the solution vector of the C1 system."""
+    import os
+    import struct
+
+    path = os.path.join(os.path.dirname(__file__), "golden", "c1_sphere_p1_n16_x.vec")
+    raw = open(path, "rb").read()
+    (n,) = struct.unpack("<Q", raw[:8])
+    x = np.frombuffer(raw[8:], dtype="<f8")
+    g = golden("c1_sphere_p1_n16.npz")
+    assert n == len(g["x"]) == len(x) and len(raw) == 8 + 8 * n
+    assert np.array_equal(x, g["x"])
