@@ -48,7 +48,7 @@ EXPORTS = [
     "tf_mesh_brick_batch", "tf_levelset_analytic_batch", "tf_batch_info", "tf_batch_lincomb", "tf_batch_pcg_jacobi",
     "tf_batch_tune", "tf_batch_config", "tf_mlp_init", "tf_mlp_get_weights", "tf_mlp_set_weights", "tf_mlp_forward",
     "tf_mlp_gradient", "tf_mlp_train", "tf_ch_features", "tf_ch_steps_learned", "tf_gmres_options", "tf_timing_enable",
-    "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2", "tf_spmv_timed", "tf_stream_read_timed", "tf_wind_upload", "tf_vec_write", "tf_vec_read", "tf_ch_stats",
+    "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2", "tf_spmv_timed", "tf_stream_read_timed", "tf_wind_upload", "tf_vec_write", "tf_vec_read", "tf_ch_stats", "tf_ch_steps_adaptive",
     "tf_host_alloc", "tf_host_free",
 ]
 
@@ -207,6 +207,20 @@ class TraceFEM:
         return coords, tv, te, ev
 
     # ---- level set ---------------------------------------------------------
+    def ch_steps_adaptive(self, t_final, dt0, F_tol, F_rho, F_min, F_max, mobility, eps, beta_s, xi, rho_vol,
+                          t0=0.0, adaptive=True, max_steps=1000, restart=50, tol=1e-10, max_iter=100000):
+        """Adaptive BDF1/BDF2 steps (tf_ch_steps_adaptive): returns (t_end, dts, errors, tries, iterations)."""
+        P = ChAdaptParams(t0, t_final, dt0, F_tol, F_rho, F_min, F_max, int(adaptive), max_steps, mobility, eps,
+                          beta_s, xi, rho_vol, restart, max_iter, tol)
+        n, te = C.c_int(), C.c_double()
+        dts, errs = np.zeros(max(max_steps, 1)), np.zeros(max(max_steps, 1))
+        tries, its = np.zeros(max(max_steps, 1), np.int32), np.zeros(max(max_steps, 1), np.int32)
+        self._check(self.L.tf_ch_steps_adaptive(self.h, C.byref(P), C.byref(n), C.byref(te), _dp(dts), _dp(errs),
+                                                tries.ctypes.data_as(C.POINTER(C.c_int)),
+                                                its.ctypes.data_as(C.POINTER(C.c_int))))
+        k = n.value
+        return te.value, dts[:k], errs[:k], tries[:k], its[:k]
+
     def ch_stats(self, eps, xi=1.0):
         """The integrals of the reference's per-step statistics (surfphasesep.cpp:324-345) for TF_VEC_CHI."""
         out = np.zeros(6)
@@ -514,6 +528,15 @@ class TraceFEM:
         self._check(self.L.tf_spmv_timed(self.h, C.c_int(mat), C.c_int(vec_x), C.c_int(vec_y), C.c_int(reps),
                                          C.c_int(int(cold)), out.ctypes.data_as(C.POINTER(C.c_float))))
         return out
+
+
+class ChAdaptParams(C.Structure):
+    """tf_ch_adapt_params: adaptive BDF1/BDF2 control of surfphasesep.cpp:397-483."""
+    _fields_ = [("t0", C.c_double), ("t_final", C.c_double), ("dt0", C.c_double), ("F_tol", C.c_double),
+                ("F_rho", C.c_double), ("F_min", C.c_double), ("F_max", C.c_double), ("adaptive", C.c_int),
+                ("max_steps", C.c_int), ("mobility", C.c_double), ("eps", C.c_double), ("beta_s", C.c_double),
+                ("xi", C.c_double), ("rho_vol", C.c_double), ("restart", C.c_int), ("max_iter", C.c_int),
+                ("tol", C.c_double)]
 
 
 class PinnedArray:

@@ -192,6 +192,9 @@ int tf_destroy(tf_context* t) {
     tf::release(c->gm2_binv);
     tf::release(c->flush_buf);
     tf::release(c->wind_v);
+    tf::release(c->ch_prev);
+    tf::release(c->ch_x1);
+    tf::release(c->ch_x2);
     tf::release(c->wind_e);
     tf::release(c->elem_n);
     tf::release(c->stream_buf);
@@ -915,6 +918,15 @@ int tf_ch_steps_learned(tf_context* t, int nsteps, double dt, double mobility, d
     P.mb_tiles = minibatch_tiles;
     P.lr = lr;
     return tf::ch_steps_learned(c, P, iters, resids, used);
+}
+
+int tf_ch_steps_adaptive(tf_context* t, const tf_ch_adapt_params* p, int* nsteps, double* t_end, double* dts,
+                         double* errs, int* tries, int* iters) {
+    CTX_CHECK(t);
+    Context* c = &t->c;
+    cudaSetDevice(c->device);
+    if (!p) return tf::set_err(c, TF_ERR_BAD_INPUT, "ch_steps_adaptive: parameters required");
+    return tf::ch_steps_adaptive(c, *p, nsteps, t_end, dts, errs, tries, iters);
 }
 
 int tf_ch_stats(tf_context* t, double eps, double xi, double* out) {

@@ -5,6 +5,8 @@
 //   [[M/dt, mob A + rho C], [eps^2 A + beta_s M + eps^2 rho C, -M]] [chi; omega] = [F_chi; F_omega]
 // solved by GMRES(restart) with nodal 2x2 block-Jacobi from the right.  State:
 // TF_VEC_X = [chi; omega] (previous step = warm start), TF_VEC_CHI = chi.
+#include <cmath>
+
 #include "tf_internal.cuh"
 
 namespace tf {
@@ -80,6 +82,183 @@ int ch_steps(Context* c, int nsteps, double dt, double mob, double eps, double b
     TF_CUDA(c, cudaMemcpyAsync(c->vecs[TF_VEC_CHI].p, c->vecs[TF_VEC_X].p, sizeof(double) * m, cudaMemcpyDeviceToDevice,
                                c->stream));
     TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// adaptive BDF1/BDF2 stepping (surfphasesep/surfphasesep.cpp:397-483)
+// ---------------------------------------------------------------------------
+// BDF2 right-hand side (:456-460) in one pass over M (SELL-32), chi_ext on the fly
+__global__ void k_ch_rhs2(int64_t m, int64_t nslices, const int32_t* __restrict__ perm,
+                          const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                          const double* __restrict__ val, const double* __restrict__ chi,
+                          const double* __restrict__ chi_prev, const double* __restrict__ f, double r, double dt,
+                          double beta, double xi, double* __restrict__ rhs) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t s = warp; s < nslices; s += nwarp) {
+        const int32_t p0 = ptr[s], w = (ptr[s + 1] - p0) >> 5;
+        double mc = 0., mp = 0., me = 0., mf = 0.;
+        for (int32_t k = 0; k < w; ++k) {
+            const int32_t j = col[p0 + 32 * k + lane];
+            const double v = val[p0 + 32 * k + lane];
+            const double cj = chi[j], pj = chi_prev[j];
+            const double ce = (1. + r) * cj - r * pj;
+            mc += v * cj;
+            mp += v * pj;
+            me += v * ce;
+            mf += v * (xi * 2. * ce * (1. - ce) * (1. - 2. * ce));
+        }
+        const int32_t row = perm[s * 32 + lane];
+        if (row >= 0) {
+            rhs[row] = (f ? f[row] : 0.) + ((1. + r) / dt) * mc - (r * r / (1. + r) / dt) * mp;
+            rhs[row + m] = beta * me - mf;
+        }
+    }
+}
+
+// d'M d and x2'M x2 for d = x2 - x1 (chi parts), per block, then in order
+__global__ void __launch_bounds__(256) k_ch_err(int64_t m, const int32_t* __restrict__ rowptr,
+                                                const int32_t* __restrict__ colind, const double* __restrict__ mv,
+                                                const double* __restrict__ x1, const double* __restrict__ x2,
+                                                double* __restrict__ part) {
+    double s0 = 0., s1 = 0.;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x) {
+        double md = 0., m2 = 0.;
+        for (int32_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+            const int32_t j = colind[k];
+            md += mv[k] * (x2[j] - x1[j]);
+            m2 += mv[k] * x2[j];
+        }
+        s0 += (x2[r] - x1[r]) * md;
+        s1 += x2[r] * m2;
+    }
+    __shared__ double red[2][8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    }
+    if (lane == 0) {
+        red[0][w] = s0;
+        red[1][w] = s1;
+    }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+        double a = 0.;
+        for (int ww = 0; ww < 8; ++ww) a += red[threadIdx.x][ww];
+        part[2 * (size_t)blockIdx.x + threadIdx.x] = a;
+    }
+}
+
+__global__ void k_ch_err_final(int nblocks, const double* __restrict__ part, double* __restrict__ out) {
+    if (threadIdx.x < 2) {
+        double a = 0.;
+        for (int b = 0; b < nblocks; ++b) a += part[2 * (size_t)b + threadIdx.x];
+        out[threadIdx.x] = a;
+    }
+}
+
+static int ch_rel_error(Context* c, const double* x1, const double* x2, double* e) {
+    const CSR& M = c->mats[TF_FORM_M];
+    const int grid = grid_for(c, M.m, 256, 4);
+    TF_TRY(ensure(c, c->scratch, sizeof(double) * (2 * (size_t)grid + 4)));
+    double* part = reinterpret_cast<double*>(c->scratch.p);
+    k_ch_err<<<grid, 256, 0, c->stream>>>(M.m, M.rowptr, M.colind, M.vals, x1, x2, part);
+    k_ch_err_final<<<1, 32, 0, c->stream>>>(grid, part, part + 2 * (size_t)grid);
+    c->launches += 2;
+    TF_CUDA(c, cudaGetLastError());
+    double r[2];
+    TF_CUDA(c, cudaMemcpyAsync(r, part + 2 * (size_t)grid, sizeof r, cudaMemcpyDeviceToHost, c->stream));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    *e = r[1] > 0. ? std::sqrt(r[0] / r[1]) : 0.;
+    return TF_OK;
+}
+
+// the step-size rule F of surfphasesep.cpp:117-123
+static double ch_next_dt(const tf_ch_adapt_params& P, double e, double dt) {
+    if (e == 0.) return P.dt0;
+    const double f = P.F_rho * std::sqrt(P.F_tol / e) * dt;
+    if (f > P.F_max) return P.F_max;
+    if (f < P.F_min) return P.F_min;
+    return f;
+}
+
+int ch_steps_adaptive(Context* c, const tf_ch_adapt_params& P, int* nsteps, double* t_end, double* dts, double* errs,
+                      int* tries, int* iters) {
+    CSR& M = c->mats[TF_FORM_M];
+    if (!M.vals || !c->mats[TF_FORM_A].vals || !c->mats[TF_FORM_CN].vals)
+        return set_err(c, TF_ERR_BAD_INPUT, "ch_steps_adaptive: assemble M, A and C_n first");
+    if (!(P.dt0 > 0.) || P.max_steps < 0 || (P.adaptive && !(P.F_min > 0. && P.F_min <= P.F_max && P.F_tol > 0.)))
+        return set_err(c, TF_ERR_BAD_INPUT, "ch_steps_adaptive: dt0 > 0, 0 < F_min <= F_max, F_tol > 0");
+    const int64_t m = M.m;
+    if ((int64_t)c->vecs[TF_VEC_X].n != 2 * m)
+        return set_err(c, TF_ERR_BAD_INPUT, "ch_steps_adaptive: TF_VEC_X must hold [chi; omega] (2m)");
+    TF_TRY(ensure_sell(c, M, false));
+    TF_TRY(ensure(c, c->ch_prev, (size_t)m));
+    TF_TRY(ensure(c, c->ch_x1, (size_t)(2 * m)));
+    TF_TRY(ensure(c, c->ch_x2, (size_t)(2 * m)));
+    TF_TRY(ensure(c, c->vecs[TF_VEC_B], (size_t)(2 * m)));
+    const double* f = (int64_t)c->vecs[TF_VEC_RHS].n == m ? c->vecs[TF_VEC_RHS].p : nullptr;
+    const size_t bytes2 = sizeof(double) * 2 * (size_t)m;
+    double t = P.t0, dt = P.dt0, e = 0.;
+    int i = 0;
+    constexpr int kMaxTries = 64;
+    while (t < P.t_final && i < P.max_steps) {
+        ++i;
+        const double t_prev = t, dt_prev = dt;
+        int ntry = 0, its = 0;
+        double* X = c->vecs[TF_VEC_X].p;
+        do {
+            ++ntry;
+            if (i == 1 || P.adaptive) dt = ch_next_dt(P, e, dt);
+            t = t_prev + dt;
+            // BDF1 (surfphasesep.cpp:412-440)
+            TF_TRY(ch_block(c, 1.0 / dt, P.mobility, P.rho_vol, P.eps * P.eps, P.beta_s, 0));
+            TF_TRY(ch_rhs(c, X, dt, P.beta_s, P.xi));
+            TF_CUDA(c, cudaMemcpyAsync(c->ch_x1.p, X, bytes2, cudaMemcpyDeviceToDevice, c->stream));
+            int it = P.max_iter;
+            double res = P.tol;
+            int st = gmres_jacobi(c, c->mats[TF_MAT_BLOCK], c->vecs[TF_VEC_B].p, c->ch_x1.p, P.restart, 0,
+                                  TF_PREC_FP64, &it, &res, 1);
+            if (st != TF_OK) return st;
+            its += it;
+            if (i == 1) {  // BDF2 solution = BDF1 solution (:447-451)
+                TF_CUDA(c, cudaMemcpyAsync(c->ch_x2.p, c->ch_x1.p, bytes2, cudaMemcpyDeviceToDevice, c->stream));
+                break;
+            }
+            // BDF2 (:452-476)
+            const double r = dt / dt_prev;
+            k_ch_rhs2<<<grid_for(c, M.sell.nslices * 32), kBlock, 0, c->stream>>>(
+                m, M.sell.nslices, M.sell.perm, M.sell.ptr, M.sell.col, M.sell.v64, X, c->ch_prev.p, f, r, dt,
+                P.beta_s, P.xi, c->vecs[TF_VEC_B].p);
+            ++c->launches;
+            TF_CUDA(c, cudaGetLastError());
+            TF_TRY(ch_block(c, (1. + 2. * r) / (1. + r) / dt, P.mobility, P.rho_vol, P.eps * P.eps, P.beta_s, 0));
+            TF_CUDA(c, cudaMemcpyAsync(c->ch_x2.p, c->ch_x1.p, bytes2, cudaMemcpyDeviceToDevice, c->stream));
+            it = P.max_iter;
+            res = P.tol;
+            st = gmres_jacobi(c, c->mats[TF_MAT_BLOCK], c->vecs[TF_VEC_B].p, c->ch_x2.p, P.restart, 0, TF_PREC_FP64,
+                              &it, &res, 1);
+            if (st != TF_OK) return st;
+            its += it;
+            TF_TRY(ch_rel_error(c, c->ch_x1.p, c->ch_x2.p, &e));
+        } while (P.adaptive && e > P.F_tol && P.F_min < dt && dt < P.F_max && ntry < kMaxTries);
+        // chi_prev = chi; [chi; omega] = BDF2 solution (:481-485)
+        TF_CUDA(c, cudaMemcpyAsync(c->ch_prev.p, X, sizeof(double) * m, cudaMemcpyDeviceToDevice, c->stream));
+        TF_CUDA(c, cudaMemcpyAsync(X, c->ch_x2.p, bytes2, cudaMemcpyDeviceToDevice, c->stream));
+        if (dts) dts[i - 1] = dt;
+        if (errs) errs[i - 1] = e;
+        if (tries) tries[i - 1] = ntry;
+        if (iters) iters[i - 1] = its;
+    }
+    TF_TRY(ensure(c, c->vecs[TF_VEC_CHI], (size_t)m));
+    TF_CUDA(c, cudaMemcpyAsync(c->vecs[TF_VEC_CHI].p, c->vecs[TF_VEC_X].p, sizeof(double) * m,
+                               cudaMemcpyDeviceToDevice, c->stream));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (nsteps) *nsteps = i;
+    if (t_end) *t_end = t;
     return TF_OK;
 }
 

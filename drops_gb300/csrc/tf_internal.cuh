@@ -322,6 +322,7 @@ struct Context {
     int64_t mlp_step = 0;
     // learned Cahn-Hilliard warm start
     DBuf<double> ch_part, ch_scales, ch_hist;
+    DBuf<double> ch_prev, ch_x1, ch_x2;  // adaptive BDF1/BDF2: chi_prev, BDF1 and BDF2 states
     DBuf<float> ch_xyz, ch_nrm, ch_Y, ch_pred;
     DBuf<__nv_bfloat16> ch_X;
     int64_t ch_geom_version = -1;
@@ -439,6 +440,8 @@ int mlp_get_weights(Context* c, float* w);
 int mlp_forward_dev(Context* c, const __nv_bfloat16* X, int64_t n, float* pred);
 int ch_rhs(Context* c, const double* X, double dt, double beta_s, double xi);
 int ch_stats(Context* c, double eps, double xi, double* out);
+int ch_steps_adaptive(Context* c, const tf_ch_adapt_params& P, int* nsteps, double* t_end, double* dts, double* errs,
+                      int* tries, int* iters);
 int ch_geometry(Context* c);
 int ch_features_dev(Context* c, const double* xn, const double* xp, const double* xnext);
 int ch_steps_learned(Context* c, const ChLearnParams& P, int* iters, double* resids, int* used);

@@ -345,6 +345,32 @@ int tf_pcg_jacobi_noalloc(int64_t m, const int32_t* rowptr, const int32_t* colin
  * iteration count and relative residual; TF_VEC_CHI receives the final chi. */
 int tf_ch_steps(tf_context* ctx, int nsteps, double dt, double mobility, double eps, double beta_s, double xi,
                 double rho_vol, int restart, double tol, int max_iter, int warm, int* iters, double* resids);
+/* Adaptive BDF1/BDF2 time stepping of surfphasesep/surfphasesep.cpp:397-483
+ * (constant mobility, no wind).  Per step i, attempt after attempt:
+ *   dt = F(e, dt) (first step, and every attempt when adaptive): dt0 for
+ *        e == 0, else F_rho sqrt(F_tol / e) dt clamped to [F_min, F_max] (:117-123);
+ *   BDF1 solve (alpha = 1/dt) from the state [chi; omega];
+ *   BDF2 solve with r = dt/dt_prev, chi_ext = (1+r) chi - r chi_prev,
+ *        F_chi = f + ((1+r)/dt) M chi - r^2/((1+r) dt) M chi_prev,
+ *        F_omega = beta_s M chi_ext - M f0'(chi_ext), alpha = (1+2r)/((1+r) dt);
+ *   e = sqrt(d'M d / chi2'M chi2), d = chi_BDF2 - chi_BDF1;
+ * repeated while adaptive and e > F_tol and F_min < dt < F_max.  Step 1
+ * takes the BDF1 solution.  The accepted state is the BDF2 solution
+ * [chi; omega] in TF_VEC_X.  Solves: GMRES(restart) with nodal block Jacobi
+ * (as tf_ch_steps), warm-started from the previous state.                   */
+typedef struct {
+    double t0, t_final, dt0;            /* start time, final time, Time.StepSize */
+    double F_tol, F_rho, F_min, F_max;  /* step-size control */
+    int adaptive, max_steps;            /* isTimeAdaptive, bound on accepted steps */
+    double mobility, eps, beta_s, xi, rho_vol;
+    int restart, max_iter;
+    double tol;
+} tf_ch_adapt_params;
+/* nsteps: accepted steps; t_end: final time; per accepted step (arrays of
+ * max_steps, may be NULL): dts, errs (e of the last attempt), tries, iters
+ * (GMRES iterations of all its solves).                                      */
+int tf_ch_steps_adaptive(tf_context* ctx, const tf_ch_adapt_params* p, int* nsteps, double* t_end, double* dts,
+                         double* errs, int* tries, int* iters);
 /* The integrals of the per-step statistics of surfphasesep/surfphasesep.cpp:
  * 324-345 (exportStats) for chi = TF_VEC_CHI, M = TF_FORM_M, A = TF_FORM_A,
  * f0(c) = xi (c (1 - c))^2 (:135-139): out[0] = 1'M1 (Integral.SurfacaAreaP1),

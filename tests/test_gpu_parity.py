@@ -441,6 +441,81 @@ def test_ch_steps_parity(ctx, golden):
         assert abs(int(a) - b) <= max(5, b // 50), (its, oits)
 
 
+def oracle_ch_adaptive(g, P, chi0):
+    """surfphasesep.cpp:397-483 (adaptive BDF1/BDF2) restated on the oracle's GMRES (CPU)."""
+    rp, ci, M = g["rowptr"], g["colind"], g["M"]
+    m = len(rp) - 1
+    f0p = lambda c: P["xi"] * 2 * c * (1 - c) * (1 - 2 * c)
+    mv = lambda x: O.spmv(rp, ci, M, x)
+
+    def solve(alpha, b, x0):
+        brp, bci, bv = O.ch_block(rp, ci, M, g["A"], g["C"], alpha, 1.0, P["rho"], P["eps"] ** 2, P["beta"])
+        st, x, it, res = O.gmres_jacobi(brp, bci, bv, b, x0=x0, restart=50, tol=1e-10, max_iter=50000, block=True)
+        assert st == O.OK
+        return x
+
+    def F(e, dt):
+        if e == 0:
+            return P["dt0"]
+        return min(max(P["F_rho"] * np.sqrt(P["F_tol"] / e) * dt, P["F_min"]), P["F_max"])
+
+    X = np.concatenate([chi0, np.zeros(m)])
+    prev = None
+    t, dt, e, i, dts, tries = 0.0, P["dt0"], 0.0, 0, [], []
+    while t < P["t_final"]:
+        i += 1
+        t_prev, dt_prev, n = t, dt, 0
+        while True:
+            n += 1
+            dt = F(e, dt)
+            t = t_prev + dt
+            chi = X[:m]
+            Mc = mv(chi)
+            X1 = solve(1 / dt, np.concatenate([Mc / dt, P["beta"] * Mc - mv(f0p(chi))]), X)
+            if i == 1:
+                X2 = X1
+                break
+            r = dt / dt_prev
+            ce = (1 + r) * chi - r * prev
+            b = np.concatenate([((1 + r) / dt) * Mc - (r * r / (1 + r) / dt) * mv(prev),
+                                P["beta"] * mv(ce) - mv(f0p(ce))])
+            X2 = solve((1 + 2 * r) / (1 + r) / dt, b, X1)
+            d = X2[:m] - X1[:m]
+            e = np.sqrt(d @ mv(d) / (X2[:m] @ mv(X2[:m])))
+            if not (e > P["F_tol"] and P["F_min"] < dt < P["F_max"]):
+                break
+        prev = X[:m].copy()
+        X = X2
+        dts.append(dt)
+        tries.append(n)
+    return t, np.array(dts), np.array(tries), X
+
+
+def test_ch_adaptive_parity(ctx, golden):
+    """Adaptive BDF1/BDF2 Cahn-Hilliard steps (surfphasesep.cpp:397-483) on the torus (P1, n=16): the same
+    step sizes, retries and state as the oracle restatement."""
+    g = golden("torus_p1_n16.npz")
+    om, p2, na, nd = setup_case(ctx, g, O.LS_TORUS, [1.0, 0.4, 2])
+    ctx.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN])
+    h = 2 * float(g["a"]) / int(g["n"])
+    # an attempt grows dt to 2.6e-3 and is rejected; steps 3, 4 and 6 retry, dt shrinks; dt >= 1e-3 keeps
+    # GMRES(50) with nodal block Jacobi converging on both the BDF1 and the BDF2 systems
+    P = dict(t_final=0.014, dt0=2e-3, F_tol=1e-2, F_rho=0.9, F_min=1e-3, F_max=4e-3, eps=0.02, beta=0.0, xi=1.0,
+             rho=h)
+    rng = np.random.default_rng(3)
+    chi0 = 0.5 + rng.uniform(-0.05, 0.05, nd)
+    ctx.vec_upload(tf.VEC_X, np.concatenate([chi0, np.zeros(nd)]))
+    te, dts, errs, tries, its = ctx.ch_steps_adaptive(P["t_final"], P["dt0"], P["F_tol"], P["F_rho"], P["F_min"],
+                                                      P["F_max"], 1.0, P["eps"], P["beta"], P["xi"], P["rho"])
+    ot, odts, otries, OX = oracle_ch_adaptive(g, P, chi0)
+    assert len(dts) == len(odts) and np.array_equal(tries, otries), (dts, odts, tries, otries)
+    assert np.allclose(dts, odts, rtol=1e-6, atol=0) and abs(te - ot) <= 1e-9
+    assert np.any(tries > 1) and dts.min() < P["dt0"]  # the controller rejected steps and shrank dt
+    X = ctx.vec_download(tf.VEC_X)
+    # ~20 solves to 1e-10, each GPU and CPU iterate within the solver tolerance of the other
+    assert np.linalg.norm(X[:nd] - OX[:nd]) <= 1e-7 * np.linalg.norm(OX[:nd])
+
+
 def test_ch_stats(ctx, golden, tmp_path):
     """Integrals of the per-step statistics (surfphasesep.cpp:324-345) after three CH steps on the torus,
     against the same formulas on the reference's M and A: area 1'M1, raft fraction 1'M chi / area,
