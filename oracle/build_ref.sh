@@ -42,3 +42,22 @@ for p in "${pids[@]}"; do wait "$p"; done
 "$CXX" "${FLAGS[@]}" -c "$HERE/ref_stubs.cpp" -o "$OBJ/ref_stubs.o"
 "$CXX" -fopenmp -o "$OUT/ref_harness" "$OBJ"/*.o
 echo "built $OUT/ref_harness"
+
+# The DROPS drop-in shim (drops_gb300/adapter) compiled against the reference's
+# own headers, and its check driver, linked with the reference objects and
+# libtracefem (built first by drops_gb300/build.py).
+REPO="$(cd "$HERE/.." && pwd)"
+LIBDIR="$REPO/drops_gb300/_lib"
+if [[ -f "$LIBDIR/libtracefem.so" ]]; then
+  AOBJ="$OUT/adapter_obj"
+  mkdir -p "$AOBJ"
+  AFLAGS=("${FLAGS[@]}" -I "$REPO/include" -I "$REPO/drops_gb300/adapter")
+  "$CXX" "${AFLAGS[@]}" -c "$REPO/drops_gb300/adapter/tracefem_drops.cpp" -o "$AOBJ/tracefem_drops.o"
+  "$CXX" "${AFLAGS[@]}" -c "$HERE/adapter_check.cpp" -o "$AOBJ/adapter_check.o"
+  REFOBJ=()
+  for o in "$OBJ"/*.o; do [[ "$(basename "$o")" == ref_harness.o ]] || REFOBJ+=("$o"); done
+  CUDALIB="${CUDA_HOME:-/usr/local/cuda}/lib64"
+  "$CXX" -fopenmp -o "$OUT/adapter_check" "$AOBJ/adapter_check.o" "$AOBJ/tracefem_drops.o" "${REFOBJ[@]}" \
+    -L "$LIBDIR" -ltracefem -Wl,-rpath,"$LIBDIR" -L "$CUDALIB" -Wl,-rpath,"$CUDALIB"
+  echo "built $OUT/adapter_check"
+fi

@@ -238,6 +238,30 @@ def test_explicit_mesh_equals_brick(ctx, golden):
         assert ok, (key, err)
 
 
+def test_explicit_mesh_any_edge_order(ctx, golden):
+    """The DROPS shim uploads a level with the triangulation's own edge numbering: numbering, pattern and
+    values must not depend on the global edge ids (permuted here at random)."""
+    g = golden("sphere_p2_n8.npz")
+    om = O.brick(int(g["n"]), a=float(g["a"]))
+    perm = np.random.default_rng(7).permutation(om.ne)  # old edge id -> new edge id
+    edge_v = np.empty_like(om.edge_v)
+    edge_v[perm] = om.edge_v[:, ::-1]  # and each edge's vertices swapped
+    ls_edge = np.empty(om.ne)
+    ls_edge[perm] = g["ls_edge"]
+    ctx.mesh_upload(om.coords, om.tet_v, perm[om.tet_e].astype(np.int32), edge_v)
+    ctx.levelset_upload(g["ls_vert"], ls_edge)
+    na, nd = ctx.distribute_dofs(tf.P2IF)
+    assert na == int(g["n_active"]) and nd == int(g["n_dofs"])
+    dv, de, act, l2g = ctx.dofs()
+    assert np.array_equal(l2g, g["loc2glo"])
+    ctx.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN], tf.RHS_SPHERE_XYZ, [0, 0, 0, 1.0, 13.0])
+    for f, key in ((tf.FORM_M, "M"), (tf.FORM_A, "A"), (tf.FORM_CN, "C")):
+        rp, ci, v = ctx.matrix(f)
+        assert np.array_equal(rp, g["rowptr"]) and np.array_equal(ci, g["colind"])
+        ok, err = mat_close(v, g[key])
+        assert ok, (key, err)
+
+
 def test_zero_node_is_an_error(ctx):
     """distance() throws for an exact zero at a node of a cut tet (geom/subtriangulation.tpp:43-44)."""
     om = brick(ctx, (10, 1, 1), orig=np.zeros(3), e=np.eye(3))
