@@ -87,6 +87,7 @@ int tf_create(tf_context** out, int device) {
     if (const char* e = std::getenv("TF_SPMV_SELL")) c->spmv_sell = std::atoi(e) != 0;
     if (const char* e = std::getenv("TF_SPMV_BLOCKS_PER_SM")) c->spmv_blocks_per_sm = std::atoi(e);
     if (const char* e = std::getenv("TF_PCG_BLOCKED")) c->pcg_blocked = std::atoi(e) != 0;
+    if (const char* e = std::getenv("TF_PCG_SMEM_CACHE_KB")) c->pcg_smem_cache_kb = std::atoi(e);
     if (const char* e = std::getenv("TF_SPMV_THREADS")) c->spmv_threads = std::atoi(e);
     if (const char* e = std::getenv("TF_GMRES2_MASTER")) c->gmres2_master = std::atoi(e) != 0;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||

@@ -884,6 +884,7 @@ struct PcgCg1Args {
     int* out_iter;
     double* out_resid;
     int* out_updates;
+    int32_t cache_cap;  // slots of the block's FP32 SELL run kept in shared memory (blocked pass)
 };
 
 // u_{i+1} of one row from its state {r_i, w_i, s_{i-1}, 1/d}; the owner and
@@ -1002,6 +1003,29 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_cg1(PcgCg1Args a)
     // this block's slices: equal shares of column work plus row updates
     const int64_t sb0 = BLK ? balanced_part_start(a.ptr, a.nslices, blockIdx.x, gridDim.x) : 0;
     const int64_t sb1 = BLK ? balanced_part_start(a.ptr, a.nslices, blockIdx.x + 1, gridDim.x) : 0;
+    // The FP32 matrix does not change during the solve: the leading slots of
+    // the block's run (as many as the dynamic shared memory holds) are copied
+    // once and every pass reads them from shared memory, so only the state
+    // gathers go to L1/L2.
+    extern __shared__ __align__(16) unsigned char cg1_dyn[];
+    SellCache<float> cache;
+    if constexpr (BLK) {
+        if (a.cache_cap > 0) {
+            const int32_t pb = __ldg(a.ptr + sb0), pe = __ldg(a.ptr + sb1);
+            const int32_t ns = pe - pb < a.cache_cap ? pe - pb : a.cache_cap;
+            int32_t* ccol = reinterpret_cast<int32_t*>(cg1_dyn);
+            float* cval = reinterpret_cast<float*>(cg1_dyn + sizeof(int32_t) * (size_t)a.cache_cap);
+            for (int32_t k = threadIdx.x; k < ns; k += NT) {
+                ccol[k] = __ldg(a.col + pb + k);
+                cval[k] = __ldg(a.val32 + pb + k);
+            }
+            __syncthreads();
+            cache.col = ccol;
+            cache.val = cval;
+            cache.base = pb;
+            cache.cap = ns;
+        }
+    }
     auto pass = [&](bool refresh, float (&o)[6]) -> bool {
         float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         const float al = refresh ? 0.f : alpha, be = refresh ? 0.f : beta;
@@ -1011,12 +1035,12 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_cg1(PcgCg1Args a)
                 const int S = (int)(sb1 - c0 < kBalMaxSlices ? sb1 - c0 : kBalMaxSlices);
                 sell_block_balanced<NT / 32, float>(
                     bsh, a.ptr, a.col, a.val32, c0, S, [&](int32_t j) { return cg1_u(kld(V + j), al, be); },
-                    [&](int64_t s, float val) { wsm[s - c0][lane] = val; });
+                    [&](int64_t s, float val) { wsm[s - c0][lane] = val; }, cache);
                 // refresh: s = A p recomputed, ending the drift of its recurrence
                 if (refresh)
                     sell_block_balanced<NT / 32, float>(
                         bsh, a.ptr, a.col, a.val32, c0, S, [&](int32_t j) { return kld(a.P + j); },
-                        [&](int64_t s, float val) { ssm[s - c0][lane] = val; });
+                        [&](int64_t s, float val) { ssm[s - c0][lane] = val; }, cache);
                 // (the next chunk overwrites wsm only after the first block
                 // barrier inside sell_block_balanced, i.e. after this loop)
                 for (int i = threadIdx.x >> 5; i < S; i += NT / 32)
@@ -1094,9 +1118,9 @@ void release_solver_workspace(Context* c) {
 }
 
 // blocks of a cooperative launch: all co-resident, at most one row slice per warp
-int coop_blocks(Context* c, const void* fn, int64_t nslices, int* out, int threads) {
+int coop_blocks(Context* c, const void* fn, int64_t nslices, int* out, int threads, size_t dyn_smem) {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess || per_sm < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, dyn_smem) != cudaSuccess || per_sm < 1)
         return set_err(c, TF_ERR_CUDA, "occupancy query failed");
     if (c->kry_blocks_per_sm > 0 && c->kry_blocks_per_sm < per_sm) per_sm = c->kry_blocks_per_sm;
     const int64_t want = (nslices * 32 + threads - 1) / threads;
@@ -1169,8 +1193,25 @@ static int run_pcg_cg1(Context* c, const CSR& A, const double* b, double* x, int
     const int nt = c->kry_threads == 512 ? 512 : 256;
     const void* fn = c->pcg_blocked ? (nt == 512 ? (const void*)k_pcg_cg1<512, true> : (const void*)k_pcg_cg1<256, true>)
                                     : (nt == 512 ? (const void*)k_pcg_cg1<512, false> : (const void*)k_pcg_cg1<256, false>);
+    // dynamic shared memory for the matrix cache: what the opt-in limit leaves
+    // after the static shared memory (one block per SM at 512 threads)
+    size_t dyn = 0;
+    int32_t cap = 0;
+    if (c->pcg_blocked && nt == 512 && c->pcg_smem_cache_kb > 0) {
+        cudaFuncAttributes fa{};
+        int optin = 0;
+        TF_CUDA(c, cudaFuncGetAttributes(&fa, fn));
+        TF_CUDA(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+        const int64_t room = std::min<int64_t>((int64_t)optin - (int64_t)fa.sharedSizeBytes - 1024,
+                                               (int64_t)c->pcg_smem_cache_kb * 1024);
+        if (room > 4096) {
+            cap = (int32_t)((room / 8) & ~(int64_t)3);
+            dyn = (size_t)cap * 8;
+            TF_CUDA(c, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+        }
+    }
     int blocks = 0;
-    TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks, nt));
+    TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks, nt, dyn));
     const size_t part_d = (size_t)2 * blocks * kArMax;
     TF_TRY(ensure(c, c->kry_part, part_d + (part_d + 1) / 2 + 16));
     TF_TRY(ensure(c, c->kry_bar, 2));
@@ -1204,8 +1245,9 @@ static int run_pcg_cg1(Context* c, const CSR& A, const double* b, double* x, int
     g.out_iter = c->kry_iters.p;
     g.out_resid = c->kry_resid.p;
     g.out_updates = c->kry_iters.p + 1;
+    g.cache_cap = cap;
     void* args[] = {&g};
-    TF_CUDA(c, cudaLaunchCooperativeKernel(fn, blocks, nt, args, 0, c->stream));
+    TF_CUDA(c, cudaLaunchCooperativeKernel(fn, blocks, nt, args, dyn, c->stream));
     ++c->launches;
     int it[2] = {0, 0};
     double res = 0;

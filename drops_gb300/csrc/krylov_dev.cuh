@@ -297,22 +297,36 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
     return v;
 }
 
-// arrive and wait for all blocks of this epoch; false after a watchdog timeout
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void red_release_add_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void fence_acquire_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
+// Arrive and wait for all blocks of this epoch; false after a watchdog
+// timeout.  Arrival is one release reduction by thread 0 after the block's
+// bar.sync (cumulative: it releases every write the barrier ordered before
+// it); the wait spins on relaxed loads and ends with one acquire fence, which
+// the closing bar.sync extends to the whole block.  No sequentially
+// consistent fence is needed on either side.
 __device__ __forceinline__ bool ar_arrive_wait(const GridAR& g, unsigned long long epoch, int* st_sh) {
     __syncthreads();
     if (threadIdx.x == 0) {
         const unsigned long long target = (epoch + 1) * (unsigned long long)gridDim.x;
-        __threadfence();
-        atomicAdd(g.count, 1ull);
+        red_release_add_u64(g.count, 1ull);
         long long spins = 0;
-        while (ld_acquire_u64(g.count) < target) {
+        while (ld_relaxed_u64(g.count) < target) {
             if (++spins > kSpinLimit) {
                 atomicCAS(g.status, 0, TF_ERR_WATCHDOG);
                 break;
             }
             if (spins > 256) __nanosleep(32);
         }
-        __threadfence();
+        fence_acquire_gpu();
         *st_sh = *((volatile int*)g.status);
     }
     __syncthreads();
@@ -399,30 +413,37 @@ __device__ __forceinline__ bool grid_sync_ar(const GridAR& g, unsigned long long
     return true;
 }
 
-// Slot row of a SELL matrix times the vector given by xload(col), over the
-// slice columns [c0, c0 + n), accumulated in T.  The columns are walked in
-// blocks of eight: the column indices and values of the next block are loaded
-// while the gathers of the current block are in flight, so a lane keeps up to
-// 16 independent loads outstanding and n columns cost ceil(n/8) gather
-// latencies.  Loads past n are masked and the multiply-adds past n are
-// skipped (n is warp-uniform, so no FP64 pipe time goes to padding).  Terms
-// are summed in CSR order.
-template <class T, class XL>
-__device__ __forceinline__ T sell_row_range(const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
-                                            const T* __restrict__ val, int64_t s, int lane, int32_t c0, int32_t n,
-                                            XL xload) {
+// Shared-memory copy of a contiguous run of SELL slots: slots [base, base +
+// cap) of the column and value arrays, laid out as in global memory.  A slice
+// whose slots all lie in the run is read from shared memory.
+template <class T>
+struct SellCache {
+    const int32_t* col = nullptr;  // shared memory
+    const T* val = nullptr;
+    int32_t base = 0, cap = 0;
+};
+
+// n columns of a slot row from cp / vp (already at slot lane of the first
+// column, 32 slots per column): in blocks of eight, the loads of the next
+// block issued while the gathers of the current block are in flight, so a
+// lane keeps up to 16 independent loads outstanding and n columns cost
+// ceil(n/8) gather latencies.  SH: cp / vp point to shared memory.  Loads past
+// n are masked and the multiply-adds past n are skipped (n is warp-uniform,
+// so no FP64 pipe time goes to padding).  Terms are summed in CSR order.
+template <bool SH, class T, class XL>
+__device__ __forceinline__ T sell_row_walk(const int32_t* __restrict__ cp, const T* __restrict__ vp, int32_t n,
+                                           XL xload) {
     constexpr int U = 8;
-    const int32_t p0 = __ldg(ptr + s) + 32 * c0;
-    const int32_t* cp = col + p0 + lane;
-    const T* vp = val + p0 + lane;
+    auto ldc = [](const int32_t* p) { return SH ? *p : __ldg(p); };
+    auto ldv = [](const T* p) { return SH ? *p : __ldg(p); };
     T acc = T(0);
     int32_t cn[U];
     T vn[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const bool in = u < n;
-        cn[u] = in ? __ldg(cp + 32 * u) : -1;
-        vn[u] = in ? __ldg(vp + 32 * u) : T(0);
+        cn[u] = in ? ldc(cp + 32 * u) : -1;
+        vn[u] = in ? ldv(vp + 32 * u) : T(0);
     }
     for (int32_t k = 0; k < n; k += U) {
         T xv[U], vv[U];
@@ -436,8 +457,8 @@ __device__ __forceinline__ T sell_row_range(const int32_t* __restrict__ ptr, con
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const bool in = kn + u < n;
-                cn[u] = in ? __ldg(cp + 32 * (kn + u)) : -1;
-                vn[u] = in ? __ldg(vp + 32 * (kn + u)) : T(0);
+                cn[u] = in ? ldc(cp + 32 * (kn + u)) : -1;
+                vn[u] = in ? ldv(vp + 32 * (kn + u)) : T(0);
             }
         }
 #pragma unroll
@@ -445,6 +466,20 @@ __device__ __forceinline__ T sell_row_range(const int32_t* __restrict__ ptr, con
             if (k + u < n) acc += vv[u] * xv[u];
     }
     return acc;
+}
+
+// Slot row of a SELL matrix times the vector given by xload(col), over the
+// slice columns [c0, c0 + n), accumulated in T; from the shared-memory copy
+// when the cache holds the whole slice.
+template <class T, class XL>
+__device__ __forceinline__ T sell_row_range(const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                                            const T* __restrict__ val, int64_t s, int lane, int32_t c0, int32_t n,
+                                            XL xload, const SellCache<T>& cache = SellCache<T>()) {
+    const int32_t ps = __ldg(ptr + s), p0 = ps + 32 * c0;
+    if (cache.cap > 0 && ps >= cache.base && __ldg(ptr + s + 1) - cache.base <= cache.cap)
+        return sell_row_walk<true, T>(cache.col + (p0 - cache.base) + lane, cache.val + (p0 - cache.base) + lane, n,
+                                      xload);
+    return sell_row_walk<false, T>(col + p0 + lane, val + p0 + lane, n, xload);
 }
 
 // the whole slot row (all columns of slice s)
@@ -500,7 +535,8 @@ struct BalShared {
 template <int NW, class T, class XL, class EMIT>
 __device__ __forceinline__ void sell_block_balanced(BalShared<NW, T>& sh, const int32_t* __restrict__ ptr,
                                                     const int32_t* __restrict__ col, const T* __restrict__ val,
-                                                    int64_t s0, int S, XL xload, EMIT emit) {
+                                                    int64_t s0, int S, XL xload, EMIT emit,
+                                                    const SellCache<T>& cache = SellCache<T>()) {
     const int lane = threadIdx.x & 31, j = threadIdx.x >> 5;
     if (j == 0) {
         int carry = 0;
@@ -534,7 +570,7 @@ __device__ __forceinline__ void sell_block_balanced(BalShared<NW, T>& sh, const 
         if (!(pa < g1 || (j == NW - 1 && pa == Tot))) break;
         const int32_t c0 = g0 > pa ? g0 - pa : 0;
         const int32_t c1 = (g1 < pb ? g1 : pb) - pa;
-        const T acc = sell_row_range<T>(ptr, col, val, s0 + i, lane, c0, c1 > c0 ? c1 - c0 : 0, xload);
+        const T acc = sell_row_range<T>(ptr, col, val, s0 + i, lane, c0, c1 > c0 ? c1 - c0 : 0, xload, cache);
         const bool starts = pa >= g0, ends = pb <= g1;
         if (starts && ends) {
             emit(s0 + i, acc);

@@ -289,6 +289,7 @@ struct Context {
     bool spmv_pair = false;     // tf_spmv: FP32-pair kernel instead of the FP64-FMA one
     bool spmv_sell = false;     // tf_spmv: one warp per slice instead of the balanced kernel
     bool pcg_blocked = true;    // mixed PCG: contiguous slices per block, balanced within the block
+    int pcg_smem_cache_kb = 0;  // mixed PCG: KB of the block's FP32 matrix slots kept in shared memory (0: off)
     int spmv_blocks_per_sm = 0; // balanced SpMV launch shape (0: default)
     int spmv_threads = 512;
     // batch of bricks (tf_mesh_brick_batch); 0 = single mesh
@@ -422,7 +423,7 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
 int gmres_jacobi(Context* c, CSR& A, const double* b, double* x, int restart, int method, int precision,
                  int* max_iter, double* tol, int rel);
 int ensure_diag(Context* c, CSR& A);
-int coop_blocks(Context* c, const void* fn, int64_t nslices, int* out, int threads);
+int coop_blocks(Context* c, const void* fn, int64_t nslices, int* out, int threads, size_t dyn_smem = 0);
 int gmres2(Context* c, CSR& A, const double* b, double* x, int restart, bool mixed, int* max_iter, double* tol, int rel);
 int ch_steps(Context* c, int nsteps, double dt, double mob, double eps, double beta_s, double xi, double rho_vol,
              int restart, double tol, int max_iter, int warm, int* iters, double* resids);
