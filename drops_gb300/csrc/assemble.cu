@@ -491,6 +491,11 @@ struct AsmSmem {
     double fx[32];
     double wind[NL == 4 ? 30 : 1];    // N_P1P1: P2 wind at the 10 nodes, xyz
     double wn[NL == 4 ? 32 : 1][4];   // sqrt(w) (wind . surface gradient of phi_j)
+    // linear level set on the tet (P1 forms): constant surface gradients of
+    // the hat functions, their Gram matrix (packed) and n . grad(phi_i)
+    double lin_sg[NL == 4 ? 4 : 1][3];
+    double lin_G[NL == 4 ? 10 : 1];
+    double lin_dn[NL == 4 ? 4 : 1];
 };
 
 struct AsmArgs {
@@ -550,6 +555,44 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
         for (int k = 0; k < 10; ++k) ls10[k] = S.ls10[k];
         __syncwarp();
         const int nf = warp_patch(ls10, S.g.X, S.P, lane, A.status, t);
+        // A P1 level set is stored as a P2 vector whose edge values are the
+        // means of the end values.  Where that holds bit for bit on all six
+        // edges, the level set is linear on the tet: grad(phi_h) and the normal
+        // are constant, and so are the surface gradients sg_i of the P1 hat
+        // functions.  Then A_ij = (sum_p w_p) sg_i.sg_j, LaplaceM_ij =
+        // (sum_p w_p mob_p) sg_i.sg_j and C_ij = |det| (sum_q w_q) dn_i dn_j:
+        // the same integrals as the per-point evaluation (which differs only by
+        // rounding), without the per-point normals and projections that make
+        // up most of the FP64 work.  (warp-uniform)
+        bool lin = false;
+        if constexpr (NL == 4) {
+            lin = true;
+            for (int k = 0; k < 6; ++k) {
+                const double mean = __dmul_rn(0.5, __dadd_rn(ls10[ev0(k)], ls10[ev1(k)]));
+                lin = lin && __double_as_longlong(mean) == __double_as_longlong(ls10[4 + k]);
+            }
+            if (lin) {
+                const double bc[4] = {0.25, 0.25, 0.25, 0.25};
+                double n[3];
+                unit_normal(S.g, bc, n);
+                if (lane < 12) {
+                    const int v = lane / 3, c = lane - 3 * (lane / 3);
+                    const double ng = n[0] * S.g.gl[v][0] + n[1] * S.g.gl[v][1] + n[2] * S.g.gl[v][2];
+                    S.lin_sg[v][c] = S.g.gl[v][c] - ng * n[c];
+                }
+                __syncwarp();
+                if (lane < 10) {
+                    int i, j;
+                    sym_entry(4, lane, i, j);
+                    S.lin_G[lane] = S.lin_sg[j][0] * S.lin_sg[i][0] + S.lin_sg[j][1] * S.lin_sg[i][1] +
+                                    S.lin_sg[j][2] * S.lin_sg[i][2];
+                } else if (lane < 14) {
+                    const int i = lane - 10;
+                    S.lin_dn[i] = n[0] * S.g.gl[i][0] + n[1] * S.g.gl[i][1] + n[2] * S.g.gl[i][2];
+                }
+                __syncwarp();
+            }
+        }
         double chi_loc[4] = {0, 0, 0, 0};
         if (wantL && A.chi && A.degenerate)
             for (int k = 0; k < 4; ++k) chi_loc[k] = A.chi[A.l2g[r * NL + k]];
@@ -569,14 +612,19 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
                 const double w = S.P.fw[f] * cT.q2_w[q];
                 // values are stored times sqrt(w): sum_p w u_i u_j = sum_p (sqrt(w) u_i)(sqrt(w) u_j)
                 const double sw = w > 0. ? w * rsqrt_fp64(w) : 0.;
-                double n[3];
-                unit_normal(S.g, b, n);
                 double phi[NL], sg[NL][3];
-                surf_basis<P2>(S.g, b, n, phi, sg);
+                if (NL == 4 && lin) {
+                    for (int i = 0; i < NL; ++i) phi[i] = b[i];
+                } else {
+                    double n[3];
+                    unit_normal(S.g, b, n);
+                    surf_basis<P2>(S.g, b, n, phi, sg);
+                }
                 S.w[lane] = sw;
                 for (int i = 0; i < NL; ++i) {
                     S.phi[lane][i] = sw * phi[i];
-                    for (int c = 0; c < 3; ++c) S.sg[lane][i][c] = sw * sg[i][c];
+                    if (!(NL == 4 && lin))
+                        for (int c = 0; c < 3; ++c) S.sg[lane][i][c] = sw * sg[i][c];
                 }
                 if (wantL) {
                     double m = 1.0;
@@ -604,8 +652,10 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
                         double wv[3] = {0., 0., 0.};
                         for (int k = 0; k < 10; ++k)
                             for (int c = 0; c < 3; ++c) wv[c] += S.wind[3 * k + c] * h[k];
-                        for (int j = 0; j < 4; ++j)
-                            S.wn[lane][j] = sw * (wv[0] * sg[j][0] + wv[1] * sg[j][1] + wv[2] * sg[j][2]);
+                        for (int j = 0; j < 4; ++j) {
+                            const double* g = lin ? S.lin_sg[j] : sg[j];
+                            S.wn[lane][j] = sw * (wv[0] * g[0] + wv[1] * g[1] + wv[2] * g[2]);
+                        }
                     }
                 }
             }
@@ -624,8 +674,11 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
                 for (int pp = grp; pp < cnt; pp += kGroups) {
                     if (wantM) sm += S.phi[pp][j] * S.phi[pp][i];
                     if (wantA || wantL) {
-                        const double d = S.sg[pp][j][0] * S.sg[pp][i][0] + S.sg[pp][j][1] * S.sg[pp][i][1] +
-                                         S.sg[pp][j][2] * S.sg[pp][i][2];
+                        // linear level set: the point weight (times sg_i.sg_j after the sum)
+                        const double d = (NL == 4 && lin)
+                                             ? S.w[pp] * S.w[pp]
+                                             : S.sg[pp][j][0] * S.sg[pp][i][0] + S.sg[pp][j][1] * S.sg[pp][i][1] +
+                                                   S.sg[pp][j][2] * S.sg[pp][i][2];
                         sa += d;
                         if (wantL) sl += S.mob[pp] * d;
                     }
@@ -655,12 +708,23 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
             accM[0] = (accM[0] + m1) + m2;
             accA[0] = (accA[0] + a1) + a2;
             accL[0] = (accL[0] + l1) + l2;
+            if (lin && lane < 10) {  // sum_p w_p (and w_p mob_p) times the constant sg_i.sg_j
+                accA[0] *= S.lin_G[lane];
+                accL[0] *= S.lin_G[lane];
+            }
             accF += __shfl_down_sync(0xffffffffu, accF, 16);
             accF += __shfl_down_sync(0xffffffffu, accF, 8);
             accF += __shfl_down_sync(0xffffffffu, accF, 4);
             accN += __shfl_down_sync(0xffffffffu, accN, 16);  // point groups: g0 + g1
         }
-        if (wantC) {
+        if (NL == 4 && wantC && lin) {
+            // constant n . grad(phi_i): the 15-point rule reduces to its weight sum
+            double s3 = 0.;
+            for (int pp = 0; pp < 15; ++pp) s3 += cT.q3_w[pp];
+            int i, j;
+            sym_entry(4, lane % 10, i, j);
+            accC[0] = (s3 * (S.lin_dn[j] * S.lin_dn[i])) * S.g.absdet;
+        } else if (wantC) {
             // normal-gradient volume stabilisation on the 15-point Quad5 rule
             if (lane < 15) {
                 double b[4];
