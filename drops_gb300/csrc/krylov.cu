@@ -966,8 +966,7 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_cg1(PcgCg1Args a)
     // row update of slot (s, lane) from its products wn = (A u)_row and, on
     // a refresh, sx = (A p)_row
     auto row_update = [&](int64_t s, float wn, float sx, bool refresh, float al, float be, const float4* V,
-                          float (&v)[6]) {
-            const int32_t row = __ldg(a.perm + s * 32 + lane);
+                          float (&v)[6], int32_t row) {
             if (row >= 0) {
                 const float4 vc = V[row];
                 float sn, rn, pn;
@@ -1026,6 +1025,14 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_cg1(PcgCg1Args a)
             cache.cap = ns;
         }
     }
+    // a block whose run fits one chunk plans its column split once and keeps
+    // the rows of its slots (perm) in shared memory
+    const bool planned = BLK && sb1 - sb0 <= kBalMaxSlices;
+    __shared__ int32_t sperm[BLK ? kBalMaxSlices : 1][32];
+    if (planned) {
+        for (int k = threadIdx.x; k < (int)(sb1 - sb0) * 32; k += NT) sperm[k >> 5][k & 31] = __ldg(a.perm + sb0 * 32 + k);
+        sell_block_plan<NT / 32, float>(bsh, a.ptr, sb0, (int)(sb1 - sb0));
+    }
     auto pass = [&](bool refresh, float (&o)[6]) -> bool {
         float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         const float al = refresh ? 0.f : alpha, be = refresh ? 0.f : beta;
@@ -1033,18 +1040,20 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_cg1(PcgCg1Args a)
         if constexpr (BLK) {
             for (int64_t c0 = sb0; c0 < sb1; c0 += kBalMaxSlices) {
                 const int S = (int)(sb1 - c0 < kBalMaxSlices ? sb1 - c0 : kBalMaxSlices);
-                sell_block_balanced<NT / 32, float>(
+                if (!planned) sell_block_plan<NT / 32, float>(bsh, a.ptr, c0, S);
+                sell_block_walk<NT / 32, float>(
                     bsh, a.ptr, a.col, a.val32, c0, S, [&](int32_t j) { return cg1_u(kld(V + j), al, be); },
                     [&](int64_t s, float val) { wsm[s - c0][lane] = val; }, cache);
                 // refresh: s = A p recomputed, ending the drift of its recurrence
                 if (refresh)
-                    sell_block_balanced<NT / 32, float>(
+                    sell_block_walk<NT / 32, float>(
                         bsh, a.ptr, a.col, a.val32, c0, S, [&](int32_t j) { return kld(a.P + j); },
                         [&](int64_t s, float val) { ssm[s - c0][lane] = val; }, cache);
                 // (the next chunk overwrites wsm only after the first block
                 // barrier inside sell_block_balanced, i.e. after this loop)
                 for (int i = threadIdx.x >> 5; i < S; i += NT / 32)
-                    row_update(c0 + i, wsm[i][lane], refresh ? ssm[i][lane] : 0.f, refresh, al, be, V, v);
+                    row_update(c0 + i, wsm[i][lane], refresh ? ssm[i][lane] : 0.f, refresh, al, be, V, v,
+                               planned ? sperm[i][lane] : __ldg(a.perm + (c0 + i) * 32 + lane));
             }
         } else {
             TF_SLICE_LOOP_BAL(a.nslices, s) {
@@ -1053,7 +1062,7 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_cg1(PcgCg1Args a)
                 const float sx = refresh ? sell_row<float>(a.ptr, a.col, a.val32, s, lane,
                                                            [&](int32_t j) { return kld(a.P + j); })
                                          : 0.f;
-                row_update(s, wn, sx, refresh, al, be, V, v);
+                row_update(s, wn, sx, refresh, al, be, V, v, __ldg(a.perm + s * 32 + lane));
             }
         }
         if (!grid_allreduce<float, 6>(a.g, epoch, v, o)) return false;

@@ -532,11 +532,11 @@ struct BalShared {
     T tail[NW][32];
 };
 
-template <int NW, class T, class XL, class EMIT>
-__device__ __forceinline__ void sell_block_balanced(BalShared<NW, T>& sh, const int32_t* __restrict__ ptr,
-                                                    const int32_t* __restrict__ col, const T* __restrict__ val,
-                                                    int64_t s0, int S, XL xload, EMIT emit,
-                                                    const SellCache<T>& cache = SellCache<T>()) {
+// The column prefix of the slices [s0, s0 + S) into sh.P (one block
+// barrier); a block that walks the same slices repeatedly plans once.
+template <int NW, class T>
+__device__ __forceinline__ void sell_block_plan(BalShared<NW, T>& sh, const int32_t* __restrict__ ptr, int64_t s0,
+                                                int S) {
     const int lane = threadIdx.x & 31, j = threadIdx.x >> 5;
     if (j == 0) {
         int carry = 0;
@@ -554,6 +554,15 @@ __device__ __forceinline__ void sell_block_balanced(BalShared<NW, T>& sh, const 
         if (lane == 0) sh.P[0] = 0;
     }
     __syncthreads();
+}
+
+// The product over planned slices (sh.P holds the prefix of [s0, s0 + S)).
+template <int NW, class T, class XL, class EMIT>
+__device__ __forceinline__ void sell_block_walk(BalShared<NW, T>& sh, const int32_t* __restrict__ ptr,
+                                                const int32_t* __restrict__ col, const T* __restrict__ val,
+                                                int64_t s0, int S, XL xload, EMIT emit,
+                                                const SellCache<T>& cache = SellCache<T>()) {
+    const int lane = threadIdx.x & 31, j = threadIdx.x >> 5;
     const int32_t Tot = sh.P[S];
     const int32_t g0 = (int32_t)((int64_t)j * Tot / NW), g1 = (int32_t)((int64_t)(j + 1) * Tot / NW);
     // first slice that overlaps [g0, ..) or starts at g0 (zero width included)
@@ -594,7 +603,16 @@ __device__ __forceinline__ void sell_block_balanced(BalShared<NW, T>& sh, const 
         }
         emit(s0 + hslice, sum + head);
     }
-    __syncthreads();  // emits visible to the block; sh free for the next call
+    __syncthreads();  // emits visible to the block; sh.tail free for the next call
+}
+
+template <int NW, class T, class XL, class EMIT>
+__device__ __forceinline__ void sell_block_balanced(BalShared<NW, T>& sh, const int32_t* __restrict__ ptr,
+                                                    const int32_t* __restrict__ col, const T* __restrict__ val,
+                                                    int64_t s0, int S, XL xload, EMIT emit,
+                                                    const SellCache<T>& cache = SellCache<T>()) {
+    sell_block_plan<NW, T>(sh, ptr, s0, S);
+    sell_block_walk<NW, T>(sh, ptr, col, val, s0, S, xload, emit, cache);
 }
 
 #define TF_SLICE_LOOP(nslices, s)                                                    \
