@@ -29,6 +29,7 @@ P1IF, P2IF = 1, 2
 FORM_M, FORM_A, FORM_CN, FORM_LAPM = 0, 1, 2, 3
 MAT_SYS, MAT_BLOCK, MAT_USER = 4, 5, 6
 FORM_N = 7  # N_P1P1, wind convection (tf_wind_upload)
+CH_DEGENERATE_MOBILITY, CH_WIND = 1, 2  # tf_ch_options
 VEC_RHS, VEC_X, VEC_B, VEC_CHI, VEC_T0, VEC_T1, VEC_T2, VEC_T3 = range(8)
 LS_SPHERE, LS_TORUS, LS_ELLIPSOID, LS_PLANE = range(4)
 RHS_NONE, RHS_SPHERE_XYZ, RHS_CONST = range(3)
@@ -48,7 +49,7 @@ EXPORTS = [
     "tf_mesh_brick_batch", "tf_levelset_analytic_batch", "tf_batch_info", "tf_batch_lincomb", "tf_batch_pcg_jacobi",
     "tf_batch_tune", "tf_batch_config", "tf_mlp_init", "tf_mlp_get_weights", "tf_mlp_set_weights", "tf_mlp_forward",
     "tf_mlp_gradient", "tf_mlp_train", "tf_ch_features", "tf_ch_steps_learned", "tf_gmres_options", "tf_timing_enable",
-    "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2", "tf_spmv_timed", "tf_stream_read_timed", "tf_wind_upload", "tf_vec_write", "tf_vec_read", "tf_ch_stats", "tf_ch_steps_adaptive",
+    "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2", "tf_spmv_timed", "tf_stream_read_timed", "tf_wind_upload", "tf_vec_write", "tf_vec_read", "tf_ch_stats", "tf_ch_steps_adaptive", "tf_ch_options",
     "tf_host_alloc", "tf_host_free",
 ]
 
@@ -221,6 +222,10 @@ class TraceFEM:
         k = n.value
         return te.value, dts[:k], errs[:k], tries[:k], its[:k]
 
+    def ch_options(self, flags):
+        """Mobility and wind of the CH time loops: CH_DEGENERATE_MOBILITY | CH_WIND (tf_ch_options)."""
+        self._check(self.L.tf_ch_options(self.h, C.c_int(flags)))
+
     def ch_stats(self, eps, xi=1.0):
         """The integrals of the reference's per-step statistics (surfphasesep.cpp:324-345) for TF_VEC_CHI."""
         out = np.zeros(6)
@@ -363,7 +368,9 @@ class TraceFEM:
         c = np.ascontiguousarray(coeffs, dtype=np.float64)
         self._check(self.L.tf_lincomb(self.h, C.c_int(f.size), f.ctypes.data_as(C.POINTER(C.c_int)), _dp(c)))
 
-    def ch_block(self, alpha, mob, rho, eps2, beta, use_lapm=False):
+    def ch_block(self, alpha, mob, rho, eps2, beta, flags=0):
+        """TF_MAT_BLOCK of surfphasesep.cpp:431-434; flags: CH_DEGENERATE_MOBILITY | CH_WIND (tf_ch_block)."""
+        use_lapm = int(flags)
         self._check(self.L.tf_ch_block(self.h, C.c_double(alpha), C.c_double(mob), C.c_double(rho), C.c_double(eps2),
                                        C.c_double(beta), C.c_int(int(use_lapm))))
 

@@ -497,6 +497,13 @@ int tf_lincomb(tf_context* t, int nterms, const int* forms, const double* coeffs
     return TF_OK;
 }
 
+int tf_ch_options(tf_context* t, int flags) {
+    CTX_CHECK(t);
+    if (flags & ~(TF_CH_DEGENERATE_MOBILITY | TF_CH_WIND)) return tf::set_err(&t->c, TF_ERR_BAD_INPUT, "ch_options: unknown flags");
+    t->c.ch_flags = flags;
+    return TF_OK;
+}
+
 int tf_ch_block(tf_context* t, double alpha, double mob, double rho, double eps2, double beta, int use_lapm) {
     CTX_CHECK(t);
     cudaSetDevice(t->c.device);

@@ -56,6 +56,26 @@ int ch_rhs(Context* c, const double* X, double dt, double beta_s, double xi) {
     return TF_OK;
 }
 
+// Mobility and wind of the time loops (tf_ch_options).  Degenerate mobility:
+// LaplaceM_P1P1 assembled again from the chi in TF_VEC_CHI before each solve
+// (surfphasesep.cpp:414-418, 452-455), then the block matrix; wind: N_P1P1 of
+// the uploaded (time-independent) wind, assembled once per loop (:417-420).
+int ch_loop_begin(Context* c) {
+    if (c->ch_flags & TF_CH_WIND) TF_TRY(setup_fe_system(c, 1u << TF_FORM_N, TF_RHS_NONE, nullptr, 0));
+    return TF_OK;
+}
+int ch_step_block(Context* c, double alpha, double mob, double rho, double eps2, double beta) {
+    if (c->ch_flags & TF_CH_DEGENERATE_MOBILITY)
+        TF_TRY(setup_fe_system(c, 1u << TF_FORM_LAPM, TF_RHS_NONE, nullptr, 0));
+    return ch_block(c, alpha, mob, rho, eps2, beta, c->ch_flags);
+}
+
+__global__ void k_ch_extrap(int64_t m, const double* __restrict__ chi, const double* __restrict__ prev, double r,
+                            double* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (1. + r) * chi[i] - r * prev[i];
+}
+
 int ch_steps(Context* c, int nsteps, double dt, double mob, double eps, double beta_s, double xi, double rho_vol,
              int restart, double tol, int max_iter, int warm, int* iters, double* resids) {
     CSR& M = c->mats[TF_FORM_M];
@@ -64,10 +84,13 @@ int ch_steps(Context* c, int nsteps, double dt, double mob, double eps, double b
     if (dt <= 0. || nsteps < 0) return set_err(c, TF_ERR_BAD_INPUT, "ch_steps: dt > 0, nsteps >= 0");
     const int64_t m = M.m;
     if ((int64_t)c->vecs[TF_VEC_X].n != 2 * m) return set_err(c, TF_ERR_BAD_INPUT, "ch_steps: TF_VEC_X must hold [chi; omega] (2m)");
-    TF_TRY(ch_block(c, 1.0 / dt, mob, rho_vol, eps * eps, beta_s, 0));
+    TF_TRY(ch_loop_begin(c));
+    const bool per_step = c->ch_flags & TF_CH_DEGENERATE_MOBILITY;
+    if (!per_step) TF_TRY(ch_block(c, 1.0 / dt, mob, rho_vol, eps * eps, beta_s, c->ch_flags));
     for (int step = 0; step < nsteps; ++step) {
         double* X = c->vecs[TF_VEC_X].p;
-        TF_TRY(ch_rhs(c, X, dt, beta_s, xi));
+        TF_TRY(ch_rhs(c, X, dt, beta_s, xi));  // also TF_VEC_CHI = chi_n
+        if (per_step) TF_TRY(ch_step_block(c, 1.0 / dt, mob, rho_vol, eps * eps, beta_s));
         if (!warm) TF_CUDA(c, cudaMemsetAsync(X, 0, sizeof(double) * 2 * m, c->stream));
         int it = max_iter;
         double res = tol;
@@ -202,6 +225,7 @@ int ch_steps_adaptive(Context* c, const tf_ch_adapt_params& P, int* nsteps, doub
     TF_TRY(ensure(c, c->vecs[TF_VEC_B], (size_t)(2 * m)));
     const double* f = (int64_t)c->vecs[TF_VEC_RHS].n == m ? c->vecs[TF_VEC_RHS].p : nullptr;
     const size_t bytes2 = sizeof(double) * 2 * (size_t)m;
+    TF_TRY(ch_loop_begin(c));
     double t = P.t0, dt = P.dt0, e = 0.;
     int i = 0;
     constexpr int kMaxTries = 64;
@@ -215,8 +239,8 @@ int ch_steps_adaptive(Context* c, const tf_ch_adapt_params& P, int* nsteps, doub
             if (i == 1 || P.adaptive) dt = ch_next_dt(P, e, dt);
             t = t_prev + dt;
             // BDF1 (surfphasesep.cpp:412-440)
-            TF_TRY(ch_block(c, 1.0 / dt, P.mobility, P.rho_vol, P.eps * P.eps, P.beta_s, 0));
-            TF_TRY(ch_rhs(c, X, dt, P.beta_s, P.xi));
+            TF_TRY(ch_rhs(c, X, dt, P.beta_s, P.xi));  // also TF_VEC_CHI = chi (mobility of the BDF1 solve)
+            TF_TRY(ch_step_block(c, 1.0 / dt, P.mobility, P.rho_vol, P.eps * P.eps, P.beta_s));
             TF_CUDA(c, cudaMemcpyAsync(c->ch_x1.p, X, bytes2, cudaMemcpyDeviceToDevice, c->stream));
             int it = P.max_iter;
             double res = P.tol;
@@ -235,7 +259,11 @@ int ch_steps_adaptive(Context* c, const tf_ch_adapt_params& P, int* nsteps, doub
                 P.beta_s, P.xi, c->vecs[TF_VEC_B].p);
             ++c->launches;
             TF_CUDA(c, cudaGetLastError());
-            TF_TRY(ch_block(c, (1. + 2. * r) / (1. + r) / dt, P.mobility, P.rho_vol, P.eps * P.eps, P.beta_s, 0));
+            if (c->ch_flags & TF_CH_DEGENERATE_MOBILITY) {  // mobility of the BDF2 solve from chi_ext
+                k_ch_extrap<<<grid_for(c, m), kBlock, 0, c->stream>>>(m, X, c->ch_prev.p, r, c->vecs[TF_VEC_CHI].p);
+                ++c->launches;
+            }
+            TF_TRY(ch_step_block(c, (1. + 2. * r) / (1. + r) / dt, P.mobility, P.rho_vol, P.eps * P.eps, P.beta_s));
             TF_CUDA(c, cudaMemcpyAsync(c->ch_x2.p, c->ch_x1.p, bytes2, cudaMemcpyDeviceToDevice, c->stream));
             it = P.max_iter;
             res = P.tol;

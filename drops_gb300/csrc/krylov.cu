@@ -486,10 +486,14 @@ __global__ void k_block_rowptr(int64_t m, const int32_t* __restrict__ rp, int32_
         else brp[r] = 2 * rp[m] + 2 * rp[r - m];
     }
 }
+// rows of [[alpha M (+ N), mob Amob + rho C], [eps2 A + beta M + eps2 rho C, -M]]
+// (surfphasesep/surfphasesep.cpp:431-434): Amob is A_deg (LaplaceM) or A_one,
+// the lower-left block always takes A_one; N (wind convection) may be null
 __global__ void k_block_fill(int64_t m, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
                              const double* __restrict__ M, const double* __restrict__ A, const double* __restrict__ C,
-                             double alpha, double mob, double rho, double eps2, double beta,
-                             const int32_t* __restrict__ brp, int32_t* __restrict__ bci, double* __restrict__ bv) {
+                             const double* __restrict__ Amob, const double* __restrict__ N, double alpha, double mob,
+                             double rho, double eps2, double beta, const int32_t* __restrict__ brp,
+                             int32_t* __restrict__ bci, double* __restrict__ bv) {
     for (int64_t R = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; R < 2 * m; R += (int64_t)gridDim.x * blockDim.x) {
         const int half = R >= m;
         const int64_t r = half ? R - m : R;
@@ -497,7 +501,7 @@ __global__ void k_block_fill(int64_t m, const int32_t* __restrict__ rp, const in
         for (int blk = 0; blk < 2; ++blk)
             for (int32_t k = rp[r]; k < rp[r + 1]; ++k) {
                 double v;
-                if (!half) v = blk == 0 ? alpha * M[k] : mob * A[k] + rho * C[k];
+                if (!half) v = blk == 0 ? (N ? alpha * M[k] + N[k] : alpha * M[k]) : mob * Amob[k] + rho * C[k];
                 else v = blk == 0 ? (eps2 * A[k] + beta * M[k]) + (eps2 * rho) * C[k] : -1. * M[k];
                 bci[w] = ci[k] + (int32_t)(blk * m);
                 bv[w] = v;
@@ -506,11 +510,14 @@ __global__ void k_block_fill(int64_t m, const int32_t* __restrict__ rp, const in
     }
 }
 
-int ch_block(Context* c, double alpha, double mob, double rho, double eps2, double beta, int use_lapm) {
+int ch_block(Context* c, double alpha, double mob, double rho, double eps2, double beta, int flags) {
     const CSR& M = c->mats[TF_FORM_M];
-    const CSR& A = c->mats[use_lapm ? TF_FORM_LAPM : TF_FORM_A];
+    const CSR& A = c->mats[TF_FORM_A];
+    const CSR& Amob = c->mats[(flags & TF_CH_DEGENERATE_MOBILITY) ? TF_FORM_LAPM : TF_FORM_A];
     const CSR& C = c->mats[TF_FORM_CN];
-    if (!M.vals || !A.vals || !C.vals) return set_err(c, TF_ERR_BAD_INPUT, "ch_block: assemble M, A (or LaplaceM) and C_n first");
+    const CSR& N = c->mats[TF_FORM_N];
+    if (!M.vals || !A.vals || !Amob.vals || !C.vals || ((flags & TF_CH_WIND) && !N.vals))
+        return set_err(c, TF_ERR_BAD_INPUT, "ch_block: assemble M, A, C_n (and LaplaceM / N when asked) first");
     const int64_t m = M.m, nnz = M.nnz;
     if (4 * nnz >= INT32_MAX) return set_err(c, TF_ERR_CAPACITY, "ch_block: too many non-zeros");
     CSR& B = c->mats[TF_MAT_BLOCK];
@@ -527,8 +534,9 @@ int ch_block(Context* c, double alpha, double mob, double rho, double eps2, doub
     B.colind = c->block_colind.p;
     B.vals = c->mat_vals[TF_MAT_BLOCK].p;
     k_block_rowptr<<<grid_for(c, 2 * m + 1), kBlock, 0, c->stream>>>(m, M.rowptr, B.rowptr);
-    k_block_fill<<<grid_for(c, 2 * m), kBlock, 0, c->stream>>>(m, M.rowptr, M.colind, M.vals, A.vals, C.vals, alpha, mob,
-                                                               rho, eps2, beta, B.rowptr, B.colind, B.vals);
+    k_block_fill<<<grid_for(c, 2 * m), kBlock, 0, c->stream>>>(
+        m, M.rowptr, M.colind, M.vals, A.vals, C.vals, Amob.vals, (flags & TF_CH_WIND) ? N.vals : nullptr, alpha, mob,
+        rho, eps2, beta, B.rowptr, B.colind, B.vals);
     c->launches += 2;
     TF_CUDA(c, cudaGetLastError());
     ++B.version;

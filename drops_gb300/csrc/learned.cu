@@ -231,7 +231,9 @@ int ch_steps_learned(Context* c, const ChLearnParams& P, int* iters, double* res
     if ((int64_t)c->vecs[TF_VEC_X].n != 2 * m)
         return set_err(c, TF_ERR_BAD_INPUT, "ch_steps_learned: TF_VEC_X must hold [chi; omega] (2m)");
     TF_TRY(ch_geometry(c));
-    TF_TRY(ch_block(c, 1.0 / P.dt, P.mob, P.rho_vol, P.eps * P.eps, P.beta_s, 0));
+    TF_TRY(ch_loop_begin(c));
+    const bool per_step = c->ch_flags & TF_CH_DEGENERATE_MOBILITY;
+    if (!per_step) TF_TRY(ch_block(c, 1.0 / P.dt, P.mob, P.rho_vol, P.eps * P.eps, P.beta_s, c->ch_flags));
     CSR& B = c->mats[TF_MAT_BLOCK];
     TF_TRY(ensure(c, c->ch_hist, (size_t)(6 * m)));  // x_old, guess
     TF_TRY(ensure(c, c->ch_pred, (size_t)(2 * m)));
@@ -245,6 +247,7 @@ int ch_steps_learned(Context* c, const ChLearnParams& P, int* iters, double* res
     for (int step = 0; step < P.nsteps; ++step) {
         double* X = c->vecs[TF_VEC_X].p;  // x_n (previous state)
         TF_TRY(ch_rhs(c, X, P.dt, P.beta_s, P.xi));
+        if (per_step) TF_TRY(ch_step_block(c, 1.0 / P.dt, P.mob, P.rho_vol, P.eps * P.eps, P.beta_s));
         const bool have_hist = step > 0;
         bool use = false;
         if (have_hist) TF_TRY(ch_features_dev(c, X, x_old, nullptr));

@@ -269,6 +269,7 @@ struct Context {
     cudaEvent_t markers[8] = {};
     DBuf<double> wind_v, wind_e;  // N_P1P1 wind, xyz per vertex / edge
     bool has_wind = false;
+    int ch_flags = 0;             // TF_CH_DEGENERATE_MOBILITY | TF_CH_WIND for the time loops
     DBuf<double> elem_n;          // N_P1P1 element matrices [n_active][16] (full, row i col j)
     DBuf<unsigned char> flush_buf;
     DBuf<uint4> stream_buf;  // tf_stream_read_timed
@@ -417,7 +418,9 @@ int numb_on_interface_p1(Context* c, double omit_bound);
 int setup_fe_system(Context* c, unsigned forms, int rhs_kind, const double* rhs_par, int npar);
 int setup_legacy_p1(Context* c, double alpha, double D, const double* fpar, int64_t* nnz);
 int lincomb(Context* c, int nterms, const int* forms, const double* coeffs);
-int ch_block(Context* c, double alpha, double mob, double rho, double eps2, double beta, int use_lapm);
+int ch_block(Context* c, double alpha, double mob, double rho, double eps2, double beta, int flags);
+int ch_loop_begin(Context* c);
+int ch_step_block(Context* c, double alpha, double mob, double rho, double eps2, double beta);
 int spmv(Context* c, const CSR& A, const double* x, double* y);
 int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, int* max_iter, double* tol, int rel);
 int gmres_jacobi(Context* c, CSR& A, const double* b, double* x, int restart, int method, int precision,

@@ -196,9 +196,22 @@ int tf_matrix_upload(tf_context* ctx, int64_t m, const int64_t* rowptr, const in
  * TF_MAT_SYS = sum_k coeffs[k] * forms[k].                                      */
 int tf_lincomb(tf_context* ctx, int nterms, const int* forms, const double* coeffs);
 /* The Cahn-Hilliard block matrix of surfphasesep/surfphasesep.cpp:431-434 as
- * TF_MAT_BLOCK: [[alpha M, mob A + rho C], [eps2 A + beta M + eps2 rho C, -M]],
- * A = TF_FORM_LAPM when use_lapm else TF_FORM_A.                              */
-int tf_ch_block(tf_context* ctx, double alpha, double mob, double rho, double eps2, double beta, int use_lapm);
+ * TF_MAT_BLOCK: [[alpha M (+ N), mob Amob + rho C], [eps2 A + beta M + eps2 rho C, -M]]
+ * with A = TF_FORM_A (A_one); flags (bit mask): TF_CH_DEGENERATE_MOBILITY
+ * takes Amob = TF_FORM_LAPM (A_deg) in the upper-right block, else A_one;
+ * TF_CH_WIND adds TF_FORM_N to the upper-left block (the reference does so
+ * when the wind is not zero, :419-420).                                      */
+#define TF_CH_DEGENERATE_MOBILITY 1
+#define TF_CH_WIND 2
+int tf_ch_block(tf_context* ctx, double alpha, double mob, double rho, double eps2, double beta, int flags);
+/* Mobility and wind of the time loops (tf_ch_steps, tf_ch_steps_learned,
+ * tf_ch_steps_adaptive), the options of surfphasesep/surfphasesep.cpp:414-420:
+ * TF_CH_DEGENERATE_MOBILITY assembles LaplaceM_P1P1 (mobility chi (1 - chi),
+ * cut off at 0) from the current chi before every solve (chi_ext for the BDF2
+ * solves) and uses it in the block; TF_CH_WIND adds N_P1P1 of the uploaded
+ * wind (tf_wind_upload; constant in time) to the upper-left block.  0 (the
+ * default): constant mobility, no wind.                                       */
+int tf_ch_options(tf_context* ctx, int flags);
 
 /* ---- vectors ----------------------------------------------------------------- */
 int tf_vec_upload(tf_context* ctx, int vec, int64_t n, const double* host);
@@ -335,7 +348,7 @@ int tf_pcg_jacobi_noalloc(int64_t m, const int32_t* rowptr, const int32_t* colin
  * surfphasesep/surfphasesep.cpp:397-440 (constant mobility, no wind):
  *   F_chi = f + (1/dt) M chi,  F_omega = beta_s M chi - M f0'(chi),
  *   f0'(c) = xi 2c(1-c)(1-2c) (surfphasesep.cpp:140-150),
- * block matrix [[M/dt, mob A + rho C], [eps^2 A + beta_s M + eps^2 rho C, -M]]
+ * block matrix [[M/dt (+ N), mob Amob + rho C], [eps^2 A + beta_s M + eps^2 rho C, -M]]
  * (TF_MAT_BLOCK), GMRES(restart) with nodal 2x2 block-Jacobi applied from the
  * right, relative residual tol.  Needs TF_FORM_M/A/CN assembled; f is
  * TF_VEC_RHS when it holds m values, else 0.  TF_VEC_X holds [chi; omega]

@@ -250,17 +250,21 @@ def gmres_jacobi(rowptr, colind, vals, b, x0=None, restart=50, max_iter=100000, 
     return st, x, it.value, t.value
 
 
-def ch_block(rowptr, colind, M, A, Cn, alpha, mob, rho, eps2, beta):
+def ch_block(rowptr, colind, M, A, Cn, alpha, mob, rho, eps2, beta, Amob=None, N=None):
+    """Block matrix of surfphasesep.cpp:431-434; Amob (A_deg) replaces A in the upper-right block, N is added to
+    the upper-left one."""
     L = lib()
     rowptr, colind = _in(rowptr, np.int64), _in(colind, np.int32)
     M, A, Cn = _in(M, np.float64), _in(A, np.float64), _in(Cn, np.float64)
+    Amob, N = _in(Amob, np.float64), _in(N, np.float64)
     m = len(rowptr) - 1
     nnz = len(colind)
     brp = np.empty(2 * m + 1, np.int64)
     bci = np.empty(4 * nnz, np.int32)
     bv = np.empty(4 * nnz, np.float64)
     L.orc_ch_block(C.c_int64(m), _p(rowptr, C.c_int64), _p(colind, C.c_int32), _p(M, C.c_double),
-                   _p(A, C.c_double), _p(Cn, C.c_double), C.c_double(alpha), C.c_double(mob), C.c_double(rho),
+                   _p(A, C.c_double), _p(Cn, C.c_double), _p(Amob, C.c_double), _p(N, C.c_double),
+                   C.c_double(alpha), C.c_double(mob), C.c_double(rho),
                    C.c_double(eps2), C.c_double(beta), _p(brp, C.c_int64), _p(bci, C.c_int32), _p(bv, C.c_double))
     return brp, bci, bv
 

@@ -80,6 +80,10 @@ double now() {
 }
 
 // level sets (surfactant/Surface.hpp:71,130)
+// concentration for the degenerate mobility of LaplaceM_P1P1: values in
+// about [-0.2, 1.2], so the cut-off at 0 of chi (1 - chi) is exercised
+double chi_value(const Point3DCL& x) { return 0.5 + 0.7 * std::sin(2.0 * x[0] + 0.5) * std::cos(1.5 * x[1]) + 0.1 * x[2]; }
+
 // smooth test wind for N_P1P1 (not tangential: the form takes any field)
 Point3DCL wind_value(const Point3DCL& x) {
     return Point3DCL(-x[1] + 0.2 * x[2], x[0] - 0.1, 0.3 * x[0] * x[1] + 0.05);
@@ -275,6 +279,23 @@ int cmd_system(int argc, char** argv) {
         setupFESystem(mg, nsys);
         Nm = N.Data;
         write_csr(w, "N", Nm);
+        // LaplaceM_P1P1 (:1533-1544) with the degenerate mobility chi (1 - chi),
+        // cut off at 0 (buildMobility :1176-1190), chi interpolated on the
+        // interface index
+        {
+            VecDescCL chi(&ifIdx);
+            chi.Interpolate(mg, [](Point3DCL const& x) { return chi_value(x); });
+            FESystem lsys;
+            lsys.params.levelSet.SetIdx(&lsIdx);
+            lsys.params.levelSet.Data = levelSet.Data;
+            lsys.params.surfCahnHilliardParams.useDegenerateMobility = true;
+            lsys.params.surfCahnHilliardParams.chi = &chi;
+            FEMatDescCL L(&ifIdx, &ifIdx, &LocalAssembler::LaplaceM_P1P1);
+            lsys.matrices = {&L};
+            setupFESystem(mg, lsys);
+            write_csr(w, "LapM", L.Data);
+            w.d("chi", std::vector<double>(std::begin(chi.Data), std::end(chi.Data)));
+        }
         std::vector<double> wv, we;
         DROPS_FOR_TRIANG_VERTEX(mg, 0, it) {
             const Point3DCL v = wind_value(it->GetCoord());

@@ -1273,9 +1273,12 @@ done:
 }
 
 int orc_ch_block(int64_t m, const int64_t* rowptr, const int32_t* colind, const double* M, const double* A,
-                 const double* C, double alpha, double mob, double rho, double eps2, double beta, int64_t* browptr,
-                 int32_t* bcolind, double* bvals) {
-    /* row r of the top blocks: [alpha*M | mob*A + rho*C]; bottom: [eps2*A + beta*M + eps2*rho*C | -M] */
+                 const double* C, const double* Amob, const double* N, double alpha, double mob, double rho,
+                 double eps2, double beta, int64_t* browptr, int32_t* bcolind, double* bvals) {
+    /* surfphasesep/surfphasesep.cpp:431-434: row r of the top blocks
+       [alpha*M (+ N) | mob*Amob + rho*C] (Amob: A_deg or, when NULL, A_one);
+       bottom: [eps2*A + beta*M + eps2*rho*C | -M] with A = A_one */
+    if (!Amob) Amob = A;
     int64_t w = 0;
     browptr[0] = 0;
     for (int half = 0; half < 2; ++half)
@@ -1283,7 +1286,7 @@ int orc_ch_block(int64_t m, const int64_t* rowptr, const int32_t* colind, const 
             for (int blk = 0; blk < 2; ++blk)
                 for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
                     double v;
-                    if (half == 0) v = blk == 0 ? alpha * M[k] : mob * A[k] + rho * C[k];
+                    if (half == 0) v = blk == 0 ? (N ? alpha * M[k] + N[k] : alpha * M[k]) : mob * Amob[k] + rho * C[k];
                     else v = blk == 0 ? (eps2 * A[k] + beta * M[k]) + (eps2 * rho) * C[k] : -1. * M[k];
                     bcolind[w] = (int32_t)(colind[k] + blk * m);
                     bvals[w] = v;

@@ -149,8 +149,8 @@ int orc_gmres(int64_t m, const int64_t* rowptr, const int32_t* colind, const dou
 /* Cahn-Hilliard 2x2 block system (surfphasesep/surfphasesep.cpp:431-434):
  * [[a*M, mob*A + rho*C], [eps2*A + beta*M + eps2*rho*C, -M]] with the shared
  * pattern of M/A/C.  Output pattern has 2m rows.                            */
-int orc_ch_block(int64_t m, const int64_t* rowptr, const int32_t* colind, const double* M,
-                 const double* A, const double* C, double alpha, double mob, double rho,
+int orc_ch_block(int64_t m, const int64_t* rowptr, const int32_t* colind, const double* M, const double* A,
+                 const double* C, const double* Amob, const double* N, double alpha, double mob, double rho,
                  double eps2, double beta, int64_t* browptr, int32_t* bcolind, double* bvals);
 
 /* 2 threads per call unless set; 1 means serial. */

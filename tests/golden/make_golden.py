@@ -71,6 +71,10 @@ def system_case(name, fe, ls, shape, n, a, solve, keep_vec=None):
         wind_edge = np.empty((mesh.ne, 3))
         wind_edge[emap] = d["wind_edge"].reshape(-1, 3)
         out.update(N=d["N.vals"], wind_vert=d["wind_vert"].reshape(-1, 3), wind_edge=wind_edge)
+    if "LapM.vals" in d:
+        # LaplaceM_P1P1 with the degenerate mobility of the harness chi (per interface DOF)
+        assert np.array_equal(d["LapM.rowptr"], d["M.rowptr"]) and np.array_equal(d["LapM.colind"], d["M.colind"])
+        out.update(LapM=d["LapM.vals"], chi=d["chi"])
     if solve:
         assert np.array_equal(d["S.rowptr"], d["M.rowptr"]) and np.array_equal(d["S.colind"], d["M.colind"])
         out.update(S=d["S.vals"], x=d["x"], iters=int(d["iters"][0]), resid=float(d["resid"][0]),

@@ -163,6 +163,82 @@ def test_vecdesc_write_read(ctx, golden, tmp_path):
         ctx.vec_read(tf.VEC_T1, str(tmp_path / "missing.vec"))
 
 
+@pytest.mark.parametrize("name,kind,par", [s for s in SYSTEMS if "p1" in s[0]])
+def test_laplace_m_degenerate_parity(ctx, golden, name, kind, par):
+    """LaplaceM_P1P1 with the degenerate mobility chi (1 - chi) cut off at 0 (surfactant/ifacetransp.h:
+    1533-1544, 1176-1190) against the reference's matrix; chi per interface DOF in TF_VEC_CHI."""
+    g = golden(name)
+    setup_case(ctx, g, kind, par)
+    ctx.vec_upload(tf.VEC_CHI, g["chi"])
+    ctx.setup_fe_system([tf.FORM_LAPM])
+    rp, ci, v = ctx.matrix(tf.FORM_LAPM)
+    assert np.array_equal(ci, g["colind"])
+    ok, err = mat_close(v, g["LapM"])
+    assert ok, err
+
+
+def test_ch_block_mobility_and_wind(ctx, golden):
+    """[[alpha M + N, mob A_deg + rho C], [eps2 A_one + beta M + eps2 rho C, -M]] (surfphasesep.cpp:431-434):
+    the degenerate-mobility matrix only in the upper-right block, A_one below."""
+    g = golden("torus_p1_n16.npz")
+    om, p2, na, nd = setup_case(ctx, g, tf.LS_TORUS, [1.0, 0.4, 2])
+    ctx.vec_upload(tf.VEC_CHI, g["chi"])
+    ctx.wind_upload(g["wind_vert"], g["wind_edge"])
+    ctx.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN, tf.FORM_LAPM, tf.FORM_N])
+    alpha, rho, eps, beta = 1000.0, 0.2, 0.02, 0.3
+    ctx.ch_block(alpha, 0.7, rho, eps * eps, beta, tf.CH_DEGENERATE_MOBILITY | tf.CH_WIND)
+    brp, bci, bv = O.ch_block(g["rowptr"], g["colind"], g["M"], g["A"], g["C"], alpha, 0.7, rho, eps * eps, beta,
+                              Amob=g["LapM"], N=g["N"])
+    rp, ci, v = ctx.matrix(tf.MAT_BLOCK)
+    assert np.array_equal(rp, brp) and np.array_equal(ci, bci)
+    ok, err = mat_close(v, bv)
+    assert ok, err
+
+
+def oracle_ch_steps_opts(g, om, kind, par, nsteps, dt, eps, rho, beta, xi, chi0, wind):
+    """BDF1 steps with degenerate mobility (LaplaceM assembled from the current chi before each solve) and
+    the wind block alpha M + N, restated on the oracle."""
+    rp, ci, M = g["rowptr"], g["colind"], g["M"]
+    m = len(rp) - 1
+    lv, le = O.levelset(om, kind, par, p2=False)
+    st, na, nd, dv, de, act = O.distribute_dofs(om, lv, le, False)
+    N = g["N"] if wind else None
+    X = np.concatenate([chi0, np.zeros(m)])
+    for _ in range(nsteps):
+        chi = X[:m]
+        st, _, _, vals, _ = O.assemble(om, lv, le, act, dv, None, m,
+                                       O.make_opts(False, [O.FORM_LAPM], chi=chi, degenerate=True))
+        brp, bci, bv = O.ch_block(rp, ci, M, g["A"], g["C"], 1.0 / dt, 1.0, rho, eps * eps, beta,
+                                  Amob=vals[O.FORM_LAPM], N=N)
+        Mc = O.spmv(rp, ci, M, chi)
+        Mf = O.spmv(rp, ci, M, xi * 2 * chi * (1 - chi) * (1 - 2 * chi))
+        b = np.concatenate([Mc / dt, beta * Mc - Mf])
+        st, X, it, res = O.gmres_jacobi(brp, bci, bv, b, x0=X, restart=50, tol=1e-10, max_iter=50000, block=True)
+        assert st == O.OK
+    return X
+
+
+def test_ch_steps_degenerate_mobility_and_wind(ctx, golden):
+    """tf_ch_options(TF_CH_DEGENERATE_MOBILITY | TF_CH_WIND): three BDF1 steps on the torus against the oracle
+    restatement (LaplaceM reassembled every step from the evolving chi)."""
+    g = golden("torus_p1_n16.npz")
+    om, p2, na, nd = setup_case(ctx, g, O.LS_TORUS, [1.0, 0.4, 2])
+    ctx.wind_upload(g["wind_vert"], g["wind_edge"])
+    ctx.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN])
+    dt, eps, h, beta, xi = 1e-3, 0.02, 2 * float(g["a"]) / int(g["n"]), 0.0, 1.0
+    chi0 = 0.5 + np.random.default_rng(9).uniform(-0.3, 0.3, nd)
+    try:
+        ctx.ch_options(tf.CH_DEGENERATE_MOBILITY | tf.CH_WIND)
+        ctx.vec_upload(tf.VEC_X, np.concatenate([chi0, np.zeros(nd)]))
+        st, its, res = ctx.ch_steps(3, dt, 1.0, eps, beta, xi, h, restart=50, tol=1e-10)
+    finally:
+        ctx.ch_options(0)
+    assert st == tf.OK and np.all(res <= 1e-10)
+    X = ctx.vec_download(tf.VEC_X)
+    OX = oracle_ch_steps_opts(g, om, O.LS_TORUS, [1.0, 0.4, 2], 3, dt, eps, h, beta, xi, chi0, wind=True)
+    assert np.linalg.norm(X[:nd] - OX[:nd]) <= 1e-8 * np.linalg.norm(OX[:nd])
+
+
 def test_wind_convection_is_p1_only(ctx, golden):
     g = golden("sphere_p2_n8.npz")
     setup_case(ctx, g, tf.LS_SPHERE, [0, 0, 0, 1.0])

@@ -75,6 +75,21 @@ def test_wind_convection_matches_reference(golden, name, kind, par):
     assert abs(Nm - Nm.T).max() > 1e-3 * abs(Nm).max()
 
 
+@pytest.mark.parametrize("name,kind,par", [s for s in SYSTEMS if "p1" in s[0]])
+def test_laplace_m_degenerate_matches_reference(golden, name, kind, par):
+    """LaplaceM_P1P1 (surfactant/ifacetransp.h:1533-1544) with the degenerate mobility chi (1 - chi), cut off
+    at 0 (buildMobility :1176-1190), chi given per interface DOF."""
+    g = golden(name)
+    mesh = O.brick(int(g["n"]), a=float(g["a"]))
+    lv, le = O.levelset(mesh, kind, par, p2=False)
+    st, na, nd, dv, de, act = O.distribute_dofs(mesh, lv, le, False)
+    opts = O.make_opts(False, [O.FORM_LAPM], chi=g["chi"], degenerate=True)
+    st, rp, ci, vals, rhs = O.assemble(mesh, lv, le, act, dv, de, nd, opts)
+    assert st == O.OK and np.array_equal(ci, g["colind"])
+    ok, err = mat_close(vals[O.FORM_LAPM], g["LapM"])
+    assert ok, err
+
+
 @pytest.mark.parametrize("name", ["c1_sphere_p1_n16.npz", "sphere_p2_n8.npz", "torus_p1_n16.npz"])
 def test_pcg_jacobi_matches_reference(golden, name):
     g = golden(name)
