@@ -155,13 +155,20 @@ def spmv_cold(ctx, tf, m, nnz):
     """Standalone FP64 SpMV (y_Ax) on the system matrix, L2 flushed before each of 20 launches; the library
     queues (flush, event, kernel, event) back to back, so the events bracket the kernel alone.  Beside it, the
     streaming floor: a plain coalesced read of the same byte count, timed the same way."""
-    t = float(np.median(ctx.spmv_timed(tf.MAT_SYS, tf.VEC_X, tf.VEC_T0, reps=20, cold=True)))
+    t = float(np.median(ctx.spmv_timed(tf.MAT_SYS, tf.VEC_X, tf.VEC_T0, reps=20, cold=1)))
     b = 12 * nnz + 4 * (m + 1) + 16 * m
-    floor = float(np.median(ctx.stream_read_timed(b, reps=20, cold=True)))
+    floor = float(np.median(ctx.stream_read_timed(b, reps=20, cold=1)))
+    # the same with an L2 left clean (flushed by reading), so DRAM serves only this kernel's traffic
+    tc = float(np.median(ctx.spmv_timed(tf.MAT_SYS, tf.VEC_X, tf.VEC_T0, reps=20, cold=2)))
+    fc = float(np.median(ctx.stream_read_timed(b, reps=20, cold=2)))
     return {"ms": round(t, 4), "bytes": b, "achieved_gbs": round(b / (t / 1e3) / 1e9, 1),
             "stream_read_same_bytes_ms": round(floor, 4), "frac_of_stream_read": round(floor / t, 4),
+            "clean_l2": {"ms": round(tc, 4), "achieved_gbs": round(b / (tc / 1e3) / 1e9, 1),
+                         "stream_read_same_bytes_ms": round(fc, 4), "frac_of_stream_read": round(fc / tc, 4)},
             "bytes_model": "12*nnz + 4*(m+1) + 16*m (FP64 values + int32 columns, row pointers, x read, y written)",
-            "timing": "median of 20 launches, L2 flushed before each, CUDA events on the library stream"}
+            "timing": "median of 20 launches, CUDA events on the library stream; L2 flushed before each by writing "
+                      "2x its size (dirty lines left, whose write-back shares DRAM with the reads); clean_l2: "
+                      "flushed by reading 2x its size"}
 
 
 def run_ours(args, rank, ws, dist):
@@ -249,22 +256,22 @@ def run_ours(args, rank, ws, dist):
 
     # ---- standalone FP64 SpMV (y_Ax) on the system matrix, cold L2 ---------
     spmv = spmv_cold(ctx, tf, state["m"], state["nnz"])
-    # the same kernel on the P2 system of twice the resolution (4x the bytes),
-    # where the launch ramp weighs less
+    # the same kernel on the P2 systems of twice and four times the resolution
+    # (4x and 16x the bytes), where the launch and the ramp of HBM weigh less
+    spmv_big = {}
     if args.size == N_CUBES and not args.no_large_spmv:
-        big = tf.TraceFEM(dev)
-        nb = 2 * N_CUBES
-        big.brick_cube(nb, HALF)
-        big.levelset_analytic(tf.LS_SPHERE, SPHERE, p2=True)
-        _, mb = big.distribute_dofs(tf.P2IF)
-        nnzb = big.setup_fe_system(forms, tf.RHS_NONE, [])
-        big.lincomb(forms, [1.0, 1.0, 2 * HALF / nb])
-        big.vec_fill(tf.VEC_X, mb, 1.0)
-        spmv_big = spmv_cold(big, tf, mb, nnzb)
-        spmv_big["system"] = f"P2 sphere {nb}^3 cubes: m={mb}, nnz={nnzb}"
-        big.close()
-    else:
-        spmv_big = None
+        for f in (2, 4):
+            big = tf.TraceFEM(dev)
+            nb = f * N_CUBES
+            big.brick_cube(nb, HALF)
+            big.levelset_analytic(tf.LS_SPHERE, SPHERE, p2=True)
+            _, mb = big.distribute_dofs(tf.P2IF)
+            nnzb = big.setup_fe_system(forms, tf.RHS_NONE, [])
+            big.lincomb(forms, [1.0, 1.0, 2 * HALF / nb])
+            big.vec_fill(tf.VEC_X, mb, 1.0)
+            spmv_big[f] = spmv_cold(big, tf, mb, nnzb)
+            spmv_big[f]["system"] = f"P2 sphere {nb}^3 cubes: m={mb}, nnz={nnzb}"
+            big.close()
 
     # ---- roofline of the dominant kernel ------------------------------------
     dom = max(ktimes, key=lambda k: ktimes[k][0])
@@ -275,9 +282,10 @@ def run_ours(args, rank, ws, dist):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    for sp in (spmv, spmv_big):
+    for sp in (spmv, *spmv_big.values()):
         if sp:
             sp["frac"] = round(sp["achieved_gbs"] / hbm_peak, 4)
+            sp["clean_l2"]["frac"] = round(sp["clean_l2"]["achieved_gbs"] / hbm_peak, 4)
     ms_d, n_d = ktimes[dom]
     na, m, nnz = state["na"], state["m"], state["nnz"]
     if dom == "pcg":
@@ -313,7 +321,8 @@ def run_ours(args, rank, ws, dist):
         "problem": {"tets": nt, "cut_tets": na, "dofs": m, "nnz": nnz, "pcg_iters_inner": state["it"]},
         "solve_ms": solve,
         "spmv_fp64_cold": spmv,
-        "spmv_fp64_cold_2x": spmv_big,
+        "spmv_fp64_cold_2x": spmv_big.get(2),
+        "spmv_fp64_cold_4x": spmv_big.get(4),
         "kernel_ms": {k: round(v[0] / args.steps, 4) for k, v in ktimes.items() if v[1]},
     }
     ctx.close()
@@ -668,7 +677,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-large-spmv", action="store_true", help="skip the SpMV timing on the 192^3 system")
+    ap.add_argument("--no-large-spmv", action="store_true", help="skip the SpMV timings on the 192^3 and 384^3 systems")
     ap.add_argument("--size", type=int, default=N_CUBES, help="cubes per direction (96 = the benchmark workload; "
                     "smaller sizes are for profiling captures)")
     ap.add_argument("--workload", default="poisson", choices=["poisson", "batch", "ch"],

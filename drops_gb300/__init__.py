@@ -522,15 +522,16 @@ class TraceFEM:
     def flush_l2(self):
         self._check(self.L.tf_flush_l2(self.h))
 
-    def stream_read_timed(self, nbytes, reps=10, cold=True):
-        """Device time (ms) of each of `reps` coalesced reads of nbytes (the streaming floor of that size)."""
+    def stream_read_timed(self, nbytes, reps=10, cold=1):
+        """Device time (ms) of each of `reps` coalesced reads of nbytes (the streaming floor of that size);
+        cold: 0 warm, 1 L2 flushed by writing (dirty), 2 flushed by reading (clean)."""
         out = np.zeros(reps, dtype=np.float32)
         self._check(self.L.tf_stream_read_timed(self.h, C.c_int64(int(nbytes)), C.c_int(reps), C.c_int(int(cold)),
                                                 out.ctypes.data_as(C.POINTER(C.c_float))))
         return out
 
-    def spmv_timed(self, mat, vec_x, vec_y, reps=10, cold=True):
-        """Device time (ms) of each of `reps` SpMV calls, L2 flushed before each when `cold`."""
+    def spmv_timed(self, mat, vec_x, vec_y, reps=10, cold=1):
+        """Device time (ms) of each of `reps` SpMV calls; cold: 0 warm, 1 L2 flushed by writing, 2 by reading."""
         out = np.zeros(reps, dtype=np.float32)
         self._check(self.L.tf_spmv_timed(self.h, C.c_int(mat), C.c_int(vec_x), C.c_int(vec_y), C.c_int(reps),
                                          C.c_int(int(cold)), out.ctypes.data_as(C.POINTER(C.c_float))))

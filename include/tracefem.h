@@ -434,9 +434,11 @@ int64_t tf_launch_count(tf_context* ctx);
 int tf_marker_record(tf_context* ctx, int slot);
 int tf_marker_elapsed(tf_context* ctx, int slot_a, int slot_b, double* ms);
 /* Measurement helper (no reference counterpart): `reps` calls of tf_spmv,
- * each bracketed by CUDA events on the context's stream and, when `cold` is
- * set, preceded by an L2 flush; the launches are queued without host waits so
- * the events time the kernel alone.  ms_each[r] = device time of call r.     */
+ * each bracketed by CUDA events on the context's stream and preceded by an L2
+ * flush when `cold` is 1 (twice the L2 size written: dirty lines left behind)
+ * or 2 (twice the L2 size read: L2 left clean); the launches are queued
+ * without host waits so the events time the kernel alone.  ms_each[r] =
+ * device time of call r.                                                      */
 int tf_spmv_timed(tf_context* ctx, int mat, int vec_x, int vec_y, int reps, int cold, float* ms_each);
 /* Measurement helper (no reference counterpart): the streaming floor for a
  * transfer size.  `reps` launches of a coalesced read of `bytes` bytes, timed
