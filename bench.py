@@ -151,10 +151,12 @@ def pcg_bytes(m, nnz, iters, fp32):
     return iters * ((vb + 4) * nnz + 4 * (m + 1) + 12 * vb * m)
 
 
-def spmv_cold(ctx, tf, m, nnz):
-    """Standalone FP64 SpMV (y_Ax) on the system matrix, L2 flushed before each of 20 launches; the library
+def spmv_cold(ctx, tf, m, nnz, kernel=None):
+    """Standalone SpMV (y_Ax) on the system matrix, L2 flushed before each of 20 launches; the library
     queues (flush, event, kernel, event) back to back, so the events bracket the kernel alone.  Beside it, the
-    streaming floor: a plain coalesced read of the same byte count, timed the same way."""
+    streaming floor: a plain coalesced read of the same byte count, timed the same way.  kernel: the
+    tf_spmv_options kernel (FP64 FMAs by default; the pair kernel's time includes its split pass of x)."""
+    ctx.spmv_options(tf.SPMV_KERNEL_FP64 if kernel is None else kernel)
     t = float(np.median(ctx.spmv_timed(tf.MAT_SYS, tf.VEC_X, tf.VEC_T0, reps=20, cold=1)))
     b = 12 * nnz + 4 * (m + 1) + 16 * m
     floor = float(np.median(ctx.stream_read_timed(b, reps=20, cold=1)))
@@ -258,7 +260,7 @@ def run_ours(args, rank, ws, dist):
     spmv = spmv_cold(ctx, tf, state["m"], state["nnz"])
     # the same kernel on the P2 systems of twice and four times the resolution
     # (4x and 16x the bytes), where the launch and the ramp of HBM weigh less
-    spmv_big = {}
+    spmv_big, spmv_pair = {}, {}
     if args.size == N_CUBES and not args.no_large_spmv:
         for f in (2, 4):
             big = tf.TraceFEM(dev)
@@ -271,6 +273,10 @@ def run_ours(args, rank, ws, dist):
             big.vec_fill(tf.VEC_X, mb, 1.0)
             spmv_big[f] = spmv_cold(big, tf, mb, nnzb)
             spmv_big[f]["system"] = f"P2 sphere {nb}^3 cubes: m={mb}, nnz={nnzb}"
+            spmv_pair[f] = spmv_cold(big, tf, mb, nnzb, tf.SPMV_KERNEL_PAIR)
+            spmv_pair[f]["system"] = spmv_big[f]["system"]
+            spmv_pair[f]["kernel"] = ("FP32-pair products (tf_spmv_options TF_SPMV_KERNEL_PAIR), split pass of x "
+                                      "included; same algorithmic bytes")
             big.close()
 
     # ---- roofline of the dominant kernel ------------------------------------
@@ -282,7 +288,7 @@ def run_ours(args, rank, ws, dist):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    for sp in (spmv, *spmv_big.values()):
+    for sp in (spmv, *spmv_big.values(), *spmv_pair.values()):
         if sp:
             sp["frac"] = round(sp["achieved_gbs"] / hbm_peak, 4)
             sp["clean_l2"]["frac"] = round(sp["clean_l2"]["achieved_gbs"] / hbm_peak, 4)
@@ -323,6 +329,8 @@ def run_ours(args, rank, ws, dist):
         "spmv_fp64_cold": spmv,
         "spmv_fp64_cold_2x": spmv_big.get(2),
         "spmv_fp64_cold_4x": spmv_big.get(4),
+        "spmv_pair_cold_2x": spmv_pair.get(2),
+        "spmv_pair_cold_4x": spmv_pair.get(4),
         "kernel_ms": {k: round(v[0] / args.steps, 4) for k, v in ktimes.items() if v[1]},
     }
     ctx.close()

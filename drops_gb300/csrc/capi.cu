@@ -901,6 +901,14 @@ int tf_ch_features(tf_context* t, int vec_cur, int vec_old, int vec_next, uint16
     return TF_OK;
 }
 
+int tf_spmv_options(tf_context* t, int kernel) {
+    CTX_CHECK(t);
+    if (kernel != TF_SPMV_KERNEL_FP64 && kernel != TF_SPMV_KERNEL_PAIR)
+        return tf::set_err(&t->c, TF_ERR_BAD_INPUT, "spmv_options: kernel");
+    t->c.spmv_pair = kernel == TF_SPMV_KERNEL_PAIR;
+    return TF_OK;
+}
+
 int tf_gmres_options(tf_context* t, int orth) {
     CTX_CHECK(t);
     if (orth != TF_ORTH_MGS && orth != TF_ORTH_CGS2) return tf::set_err(&t->c, TF_ERR_BAD_INPUT, "gmres_options: orth");

@@ -275,16 +275,6 @@ __global__ void k_sell_vals_pair(int64_t nslices, const int32_t* __restrict__ pt
     }
 }
 
-// x -> pairs; *flag set when an entry is outside {0} U [2^-100, 2^100]
-__global__ void k_split_x(int64_t n, const double* __restrict__ x, float2* __restrict__ out, int* flag) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double v = x[i];
-        const double a = fabs(v);
-        if (v != 0. && !(a >= 7.888609052210118e-31 && a <= 1.2676506002282294e30)) atomicOr(flag, 1);
-        out[i] = split_pair(v);
-    }
-}
-
 // (sh, sl) += a * x in pair arithmetic; a = (0, 0) leaves the sum unchanged
 __device__ __forceinline__ void pair_fma(float& sh, float& sl, float2 a, float2 x) {
     const float p = __fmul_rn(a.x, x.x);
@@ -297,25 +287,63 @@ __device__ __forceinline__ void pair_fma(float& sh, float& sl, float2 a, float2 
     sh = s;
 }
 
-// slot row in pair arithmetic, the loads staged like sell_row
-__device__ __forceinline__ double sell_row_pair(const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
-                                                const float2* __restrict__ val, const int32_t* __restrict__ rexp,
-                                                const float2* __restrict__ x, int64_t s, int lane) {
-    constexpr int U = 8;
-    const int32_t p0 = __ldg(ptr + s);
-    const int32_t w = (__ldg(ptr + s + 1) - p0) >> 5;
-    const int32_t* cp = col + p0 + lane;
-    const float2* vp = val + p0 + lane;
+// x -> pairs with integer operations only (no conversions, which GB300 runs
+// on its narrow FP64 pipe): hi = the top 24 bits of the significand
+// (truncated), lo = the remaining 29 bits normalised and truncated to 24, so
+// |x - hi - lo| <= 2^-47 |x|.  Valid for |x| in [2^-74, 2^100], where lo is a
+// normal float; other non-zero x (and non-finite x) set *flag, which sends the
+// launch to FP64 FMAs.
+__global__ void k_split_x_int(int64_t n, const double* __restrict__ x, float2* __restrict__ out, int* flag) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(x[i]);
+        float2 r = make_float2(0.f, 0.f);
+        if ((b << 1) != 0ull) {
+            const unsigned e = (unsigned)(b >> 52) & 0x7ffu, sgn = (unsigned)(b >> 63) << 31;
+            if (e < 949u || e > 1123u) {
+                atomicOr(flag, 1);
+            } else {
+                const unsigned long long mant = b & 0xfffffffffffffull;
+                const unsigned hb = sgn | ((e - 896u) << 23) | (unsigned)(mant >> 29);
+                const unsigned rem = (unsigned)(mant & 0x1fffffffu);
+                unsigned lb = 0u;
+                if (rem) {
+                    const int lz = __clz((int)rem);          // >= 3
+                    const unsigned p = 31u - (unsigned)lz;   // leading bit of rem
+                    const unsigned m23 = (unsigned)((((unsigned long long)rem << (lz + 1)) & 0xffffffffull) >> 9);
+                    lb = sgn | ((p + e - 948u) << 23) | m23;  // rem * 2^(e - 1075)
+                }
+                r = make_float2(__int_as_float((int)hb), __int_as_float((int)lb));
+            }
+        }
+        out[i] = r;
+    }
+}
+
+// n columns of a slot row in pair arithmetic (loads staged like sell_row_walk)
+struct Pair2 {
+    float h, l;
+    __device__ Pair2(float a = 0.f, float b = 0.f) : h(a), l(b) {}
+};
+__device__ __forceinline__ Pair2 operator+(Pair2 a, Pair2 b) {  // two-sum of the highs, lows added
+    const float s = __fadd_rn(a.h, b.h);
+    const float bb = __fsub_rn(s, a.h);
+    const float err = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+    return Pair2(s, __fadd_rn(__fadd_rn(a.l, b.l), err));
+}
+
+__device__ __forceinline__ Pair2 pair_row_walk(const int32_t* __restrict__ cp, const float2* __restrict__ vp, int32_t n,
+                                               const float2* __restrict__ x) {
+    constexpr int U = 4;  // 8 spills at 64 registers
     float sh = 0.f, sl = 0.f;
     int32_t cn[U];
     float2 vn[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-        const bool in = u < w;
+        const bool in = u < n;
         cn[u] = in ? __ldg(cp + 32 * u) : -1;
         vn[u] = in ? __ldg(vp + 32 * u) : make_float2(0.f, 0.f);
     }
-    for (int32_t k = 0; k < w; k += U) {
+    for (int32_t k = 0; k < n; k += U) {
         float2 xv[U], vv[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
@@ -323,31 +351,63 @@ __device__ __forceinline__ double sell_row_pair(const int32_t* __restrict__ ptr,
             vv[u] = vn[u];
         }
         const int32_t kn = k + U;
-        if (kn < w) {
+        if (kn < n) {
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                const bool in = kn + u < w;
+                const bool in = kn + u < n;
                 cn[u] = in ? __ldg(cp + 32 * (kn + u)) : -1;
                 vn[u] = in ? __ldg(vp + 32 * (kn + u)) : make_float2(0.f, 0.f);
             }
         }
 #pragma unroll
-        for (int u = 0; u < U; ++u) pair_fma(sh, sl, vv[u], xv[u]);
+        for (int u = 0; u < U; ++u)
+            if (k + u < n) pair_fma(sh, sl, vv[u], xv[u]);
     }
-    return ((double)sh + (double)sl) * pow2(__ldg(rexp + s * 32 + lane));
+    return Pair2(sh, sl);
 }
 
-__global__ void k_spmv_pair(int64_t nslices, const int32_t* __restrict__ perm, const int32_t* __restrict__ ptr,
-                            const int32_t* __restrict__ col, const float2* __restrict__ v2, const int32_t* __restrict__ rexp,
-                            const double* __restrict__ v64, const float2* __restrict__ x2, const double* __restrict__ x,
-                            const int* __restrict__ flag, double* __restrict__ y) {
+// Balanced SpMV in pair arithmetic: the block split of k_spmv_bal, FP32
+// operations per non-zero, 4 FP64 operations per row (the epilogue
+// ((double)hi + (double)lo) 2^e).  *flag (x out of the pair range) switches
+// the whole launch to FP64 FMAs.
+template <int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT)
+    k_spmv_pair_bal(int64_t nslices, const int32_t* __restrict__ perm, const int32_t* __restrict__ ptr,
+                    const int32_t* __restrict__ col, const float2* __restrict__ v2, const int32_t* __restrict__ rexp,
+                    const double* __restrict__ v64, const float2* __restrict__ x2, const double* __restrict__ x,
+                    const int* __restrict__ flag, double* __restrict__ y) {
+    constexpr int NW = NT / 32;
+    constexpr size_t kRaw = sizeof(BalShared<NW, double>) > sizeof(BalShared<NW, Pair2>) ? sizeof(BalShared<NW, double>)
+                                                                                           : sizeof(BalShared<NW, Pair2>);
+    __shared__ __align__(16) unsigned char raw[kRaw];
     const int lane = threadIdx.x & 31;
     const bool native = *flag != 0;
-    TF_SLICE_LOOP(nslices, s) {
-        const double a = native ? sell_row<double>(ptr, col, v64, s, lane, [&](int32_t j) { return __ldg(x + j); })
-                                : sell_row_pair(ptr, col, v2, rexp, x2, s, lane);
-        const int32_t row = perm[s * 32 + lane];
-        if (row >= 0) y[row] = a;
+    const int64_t s0 = (int64_t)blockIdx.x * nslices / gridDim.x;
+    const int64_t s1 = (int64_t)(blockIdx.x + 1) * nslices / gridDim.x;
+    for (int64_t c0 = s0; c0 < s1; c0 += kBalMaxSlices) {
+        const int S = (int)(s1 - c0 < kBalMaxSlices ? s1 - c0 : kBalMaxSlices);
+        if (native) {
+            auto& sh = *reinterpret_cast<BalShared<NW, double>*>(raw);
+            sell_block_balanced<NW, double>(
+                sh, ptr, col, v64, c0, S, [&](int32_t j) { return __ldg(x + j); },
+                [&](int64_t s, double v) {
+                    const int32_t row = __ldg(perm + s * 32 + lane);
+                    if (row >= 0) y[row] = v;
+                });
+        } else {
+            auto& sh = *reinterpret_cast<BalShared<NW, Pair2>*>(raw);
+            sell_block_plan<NW, Pair2>(sh, ptr, c0, S);
+            sell_block_walk_fn<NW, Pair2>(
+                sh, c0, S,
+                [&](int64_t s, int32_t cc, int32_t n) {
+                    const int32_t p0 = __ldg(ptr + s) + 32 * cc;
+                    return pair_row_walk(col + p0 + lane, v2 + p0 + lane, n, x2);
+                },
+                [&](int64_t s, Pair2 q) {
+                    const int32_t row = __ldg(perm + s * 32 + lane);
+                    if (row >= 0) y[row] = ((double)q.h + (double)q.l) * pow2(__ldg(rexp + s * 32 + lane));
+                });
+        }
     }
 }
 
@@ -375,25 +435,30 @@ static int ensure_sell_pair(Context* c, CSR& A) {
 int spmv(Context* c, const CSR& Ac, const double* x, double* y) {
     CSR& A = const_cast<CSR&>(Ac);
     TF_TRY(ensure_sell(c, A, false));
-    if (!c->spmv_pair && !c->spmv_sell) {
+    if (c->spmv_sell) {  // one warp per slice (kept for comparisons)
         TimedLaunch tl(c, TF_K_SPMV);
-        launch_spmv_bal(c, A, x, y);
-        TF_CUDA(c, cudaGetLastError());
-        return TF_OK;
-    }
-    if (c->spmv_pair) TF_TRY(ensure_sell_pair(c, A));
-    TimedLaunch tl(c, TF_K_SPMV);
-    if (!c->spmv_pair || !A.sell.v2f_ok) {
         k_spmv<double><<<grid_for(c, A.sell.nslices * 32), kBlock, 0, c->stream>>>(
             A.sell.nslices, A.sell.perm, A.sell.ptr, A.sell.col, A.sell.v64, x, y);
         ++c->launches;
+        TF_CUDA(c, cudaGetLastError());
+        return TF_OK;
+    }
+    const bool pair = c->spmv_pair;
+    if (pair) TF_TRY(ensure_sell_pair(c, A));
+    TimedLaunch tl(c, TF_K_SPMV);
+    if (!pair || !A.sell.v2f_ok) {
+        launch_spmv_bal(c, A, x, y);
     } else {
         TF_TRY(ensure(c, c->x_pairs, (size_t)(A.m > 0 ? A.m : 1)));
         TF_CUDA(c, cudaMemsetAsync(c->status.p + 2, 0, sizeof(int), c->stream));
-        k_split_x<<<grid_for(c, A.m), kBlock, 0, c->stream>>>(A.m, x, c->x_pairs.p, c->status.p + 2);
-        k_spmv_pair<<<grid_for(c, A.sell.nslices * 32), kBlock, 0, c->stream>>>(
-            A.sell.nslices, A.sell.perm, A.sell.ptr, A.sell.col, A.sell.v2f, A.sell.rexp, A.sell.v64, c->x_pairs.p, x,
-            c->status.p + 2, y);
+        k_split_x_int<<<grid_for(c, A.m), kBlock, 0, c->stream>>>(A.m, x, c->x_pairs.p, c->status.p + 2);
+        const int64_t ns = A.sell.nslices;
+        int64_t nb = (int64_t)c->num_sms * 2;
+        if (nb > ns) nb = ns;
+        if (nb < 1) nb = 1;
+        k_spmv_pair_bal<512><<<(unsigned)nb, 512, 0, c->stream>>>(ns, A.sell.perm, A.sell.ptr, A.sell.col, A.sell.v2f,
+                                                                 A.sell.rexp, A.sell.v64, c->x_pairs.p, x,
+                                                                 c->status.p + 2, y);
         c->launches += 2;
     }
     TF_CUDA(c, cudaGetLastError());

@@ -556,12 +556,11 @@ __device__ __forceinline__ void sell_block_plan(BalShared<NW, T>& sh, const int3
     __syncthreads();
 }
 
-// The product over planned slices (sh.P holds the prefix of [s0, s0 + S)).
-template <int NW, class T, class XL, class EMIT>
-__device__ __forceinline__ void sell_block_walk(BalShared<NW, T>& sh, const int32_t* __restrict__ ptr,
-                                                const int32_t* __restrict__ col, const T* __restrict__ val,
-                                                int64_t s0, int S, XL xload, EMIT emit,
-                                                const SellCache<T>& cache = SellCache<T>()) {
+// The product over planned slices (sh.P holds the prefix of [s0, s0 + S)):
+// row(slice, c0, n) returns one lane's partial sum over the slice columns
+// [c0, c0 + n); T needs T(0) and +.
+template <int NW, class T, class ROW, class EMIT>
+__device__ __forceinline__ void sell_block_walk_fn(BalShared<NW, T>& sh, int64_t s0, int S, ROW row, EMIT emit) {
     const int lane = threadIdx.x & 31, j = threadIdx.x >> 5;
     const int32_t Tot = sh.P[S];
     const int32_t g0 = (int32_t)((int64_t)j * Tot / NW), g1 = (int32_t)((int64_t)(j + 1) * Tot / NW);
@@ -579,7 +578,7 @@ __device__ __forceinline__ void sell_block_walk(BalShared<NW, T>& sh, const int3
         if (!(pa < g1 || (j == NW - 1 && pa == Tot))) break;
         const int32_t c0 = g0 > pa ? g0 - pa : 0;
         const int32_t c1 = (g1 < pb ? g1 : pb) - pa;
-        const T acc = sell_row_range<T>(ptr, col, val, s0 + i, lane, c0, c1 > c0 ? c1 - c0 : 0, xload, cache);
+        const T acc = row(s0 + i, c0, c1 > c0 ? c1 - c0 : 0);
         const bool starts = pa >= g0, ends = pb <= g1;
         if (starts && ends) {
             emit(s0 + i, acc);
@@ -599,11 +598,23 @@ __device__ __forceinline__ void sell_block_walk(BalShared<NW, T>& sh, const int3
         T sum = T(0);
         for (int jj = ja; jj < j; ++jj) {
             const int32_t a0 = (int32_t)((int64_t)jj * Tot / NW), a1 = (int32_t)((int64_t)(jj + 1) * Tot / NW);
-            if (a1 > a0) sum += sh.tail[jj][lane];
+            if (a1 > a0) sum = sum + sh.tail[jj][lane];
         }
         emit(s0 + hslice, sum + head);
     }
     __syncthreads();  // emits visible to the block; sh.tail free for the next call
+}
+
+template <int NW, class T, class XL, class EMIT>
+__device__ __forceinline__ void sell_block_walk(BalShared<NW, T>& sh, const int32_t* __restrict__ ptr,
+                                                const int32_t* __restrict__ col, const T* __restrict__ val,
+                                                int64_t s0, int S, XL xload, EMIT emit,
+                                                const SellCache<T>& cache = SellCache<T>()) {
+    const int lane = threadIdx.x & 31;
+    sell_block_walk_fn<NW, T>(
+        sh, s0, S,
+        [&](int64_t s, int32_t c0, int32_t n) { return sell_row_range<T>(ptr, col, val, s, lane, c0, n, xload, cache); },
+        emit);
 }
 
 template <int NW, class T, class XL, class EMIT>

@@ -228,6 +228,16 @@ int tf_vec_read(tf_context* ctx, int vec, const char* path, int64_t n_expected);
 int tf_vec_fill(tf_context* ctx, int vec, int64_t n, double value);
 /* y = A x on device vectors (y_Ax, num/spmat.h:1684-1709). */
 int tf_spmv(tf_context* ctx, int mat, int vec_x, int vec_y);
+/* Kernel of tf_spmv (no reference counterpart; the solvers have their own).
+ * TF_SPMV_KERNEL_FP64 (default): FP64 FMAs, a few ulps of sum |a_ij x_j|
+ * per row.  TF_SPMV_KERNEL_PAIR: FP32-pair products (values stored as
+ * row-scaled float pairs, x split per call), within 3e-13 of
+ * sum |a_ij x_j| per row; a matrix with a value a pair cannot hold, or a
+ * call whose x has a non-zero entry outside [2^-74, 2^100] or a non-finite
+ * one, runs the FP64 FMAs.                                                    */
+#define TF_SPMV_KERNEL_FP64 0
+#define TF_SPMV_KERNEL_PAIR 1
+int tf_spmv_options(tf_context* ctx, int kernel);
 
 /* ---- solvers ------------------------------------------------------------------- */
 /* PCGSolverCL<JACPcCL>(pc, max_iter, tol, rel).Solve(A, x, b) (num/krylovsolver.h:

@@ -1,7 +1,5 @@
 """y_Ax (num/spmat.h:1684-1709) through tf_spmv: the FP32-pair kernel and the FP64-FMA kernel against the
 oracle's FP64 product."""
-import os
-
 import numpy as np
 import pytest
 
@@ -16,12 +14,9 @@ def ctxs():
     from drops_gb300 import build
 
     build.build()
-    native = tf.TraceFEM()
-    os.environ["TF_SPMV_PAIR"] = "1"
-    try:
-        pair = tf.TraceFEM()
-    finally:
-        del os.environ["TF_SPMV_PAIR"]
+    pair, native = tf.TraceFEM(), tf.TraceFEM()
+    pair.spmv_options(tf.SPMV_KERNEL_PAIR)
+    native.spmv_options(tf.SPMV_KERNEL_FP64)
     yield pair, native
     pair.close()
     native.close()
@@ -65,8 +60,8 @@ def test_spmv_matches_oracle(ctxs, golden, name, key):
 
 
 def test_spmv_wide_range(ctxs):
-    """Row scaling covers rows of any magnitude; x outside [2^-100, 2^100] takes the FP64 path in the same
-    launch; a non-finite matrix value keeps the matrix on the FP64 kernel."""
+    """Row scaling covers rows of any magnitude; non-zero x outside [2^-74, 2^100] takes the FP64 path in the
+    same launch; a non-finite matrix value keeps the matrix on the FP64 kernel."""
     rng = np.random.default_rng(5)
     m = 3000
     rp = np.arange(0, 7 * m + 1, 7, dtype=np.int64)
@@ -135,7 +130,46 @@ def test_spmv_balanced_uneven_rows(ctxs, case):
         lengths = rng.integers(5, 16, m)
     rp, ci, v = _random_csr(rng, lengths, m)
     x = rng.uniform(-1, 1, m)
-    native = ctxs[1]
+    pair, native = ctxs
     y = _spmv(native, rp, ci, v, x)
     _check(y, rp, ci, v, x, FP64_REL)
     assert np.array_equal(y, _spmv(native, rp, ci, v, x))
+    yp = _spmv(pair, rp, ci, v, x)
+    _check(yp, rp, ci, v, x, PAIR_REL)
+    assert np.array_equal(yp, _spmv(pair, rp, ci, v, x))
+
+
+def test_spmv_split_edges(ctxs):
+    """x at the edges of the pair range (2^-74, 2^100, significands with all low bits set, single low bits,
+    zeros of both signs): the integer split keeps |x - hi - lo| <= 2^-47 |x|."""
+    base = np.array([2.0 ** -74, 2.0 ** 100, 1.0, 0.0, np.nextafter(1.0, 2.0), np.nextafter(2.0, 0.0),
+                     1.0 + 2.0 ** -24, 1.0 + 2.0 ** -23 + 2.0 ** -52, np.nextafter(2.0 ** 101, 0.0), 0.1, np.pi])
+    x = np.concatenate([base, -base, base * 1.25, base * (1 + 2.0 ** -30), base * 2.0 ** -20, base * 2.0 ** 20])
+    mag = np.abs(x)
+    x = x[(mag == 0) | ((mag >= 2.0 ** -74) & (mag < 2.0 ** 101))]
+    m = len(x)
+    rp = np.arange(m + 1, dtype=np.int64)
+    ci = np.arange(m, dtype=np.int32)
+    v = np.ones(m)
+    y = _spmv(ctxs[0], rp, ci, v, x)
+    assert np.all(np.abs(y - x) <= 2.0 ** -47 * np.abs(x)), np.max(np.abs(y - x) / np.maximum(np.abs(x), 1e-300))
+
+
+def test_spmv_pair_large(ctxs):
+    """The pair kernel on a matrix of 9M stored entries (a few hundred blocks of 64 slices each, several chunks
+    per block) and the default kernel (FP64), bit-identical to the forced FP64 context; an unknown kernel is
+    refused."""
+    pair, native = ctxs
+    rng = np.random.default_rng(21)
+    m = 400000
+    rp, ci, v = _random_csr(rng, rng.integers(18, 26, m), m)
+    assert rp[-1] >= 8 << 20
+    x = rng.uniform(-1, 1, m)
+    _check(_spmv(pair, rp, ci, v, x), rp, ci, v, x, PAIR_REL)
+    default = tf.TraceFEM()
+    try:
+        with pytest.raises(tf.TraceFEMError):
+            default.spmv_options(2)
+        assert np.array_equal(_spmv(default, rp, ci, v, x), _spmv(native, rp, ci, v, x))
+    finally:
+        default.close()
