@@ -1038,21 +1038,23 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_cg1(PcgCg1Args a)
     // a true residual), else the CG step with (alpha, beta)
     // row update of slot (s, lane) from its products wn = (A u)_row and, on
     // a refresh, sx = (A p)_row
+    // pp / pdx: where the row's p and dx live (shared memory for a planned
+    // block, which owns its rows for the whole solve; else global memory)
     auto row_update = [&](int64_t s, float wn, float sx, bool refresh, float al, float be, const float4* V,
-                          float (&v)[6], int32_t row) {
+                          float (&v)[6], int32_t row, float* pp, float* pdx) {
             if (row >= 0) {
                 const float4 vc = V[row];
                 float sn, rn, pn;
                 if (refresh) {
                     sn = sx;
                     rn = vc.x;
-                    pn = a.P[row];
+                    pn = *pp;
                 } else {
                     sn = cg1_s(vc, be);
                     rn = cg1_r(vc, sn, al);
-                    pn = __fmaf_rn(be, a.P[row], __fmul_rn(vc.x, vc.w));
-                    a.P[row] = pn;
-                    a.dx[row] = __fmaf_rn(al, pn, a.dx[row]);
+                    pn = __fmaf_rn(be, *pp, __fmul_rn(vc.x, vc.w));
+                    *pp = pn;
+                    *pdx = __fmaf_rn(al, pn, *pdx);
                 }
                 const float un = __fmul_rn(rn, vc.w);
                 Vn[row] = make_float4(rn, wn, sn, vc.w);
@@ -1100,10 +1102,17 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_cg1(PcgCg1Args a)
     }
     // a block whose run fits one chunk plans its column split once and keeps
     // the rows of its slots (perm) in shared memory
+    // (and its rows' p and dx: only the owner reads or writes them between two
+    // refinements; the fold publishes p for the refresh pass, which gathers it)
     const bool planned = BLK && sb1 - sb0 <= kBalMaxSlices;
     __shared__ int32_t sperm[BLK ? kBalMaxSlices : 1][32];
+    __shared__ float sP[BLK ? kBalMaxSlices : 1][32], sdx[BLK ? kBalMaxSlices : 1][32];
     if (planned) {
-        for (int k = threadIdx.x; k < (int)(sb1 - sb0) * 32; k += NT) sperm[k >> 5][k & 31] = __ldg(a.perm + sb0 * 32 + k);
+        for (int k = threadIdx.x; k < (int)(sb1 - sb0) * 32; k += NT) {
+            sperm[k >> 5][k & 31] = __ldg(a.perm + sb0 * 32 + k);
+            sP[k >> 5][k & 31] = 0.f;
+            sdx[k >> 5][k & 31] = 0.f;
+        }
         sell_block_plan<NT / 32, float>(bsh, a.ptr, sb0, (int)(sb1 - sb0));
     }
     auto pass = [&](bool refresh, float (&o)[6]) -> bool {
@@ -1124,9 +1133,12 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_cg1(PcgCg1Args a)
                         [&](int64_t s, float val) { ssm[s - c0][lane] = val; }, cache);
                 // (the next chunk overwrites wsm only after the first block
                 // barrier inside sell_block_balanced, i.e. after this loop)
-                for (int i = threadIdx.x >> 5; i < S; i += NT / 32)
-                    row_update(c0 + i, wsm[i][lane], refresh ? ssm[i][lane] : 0.f, refresh, al, be, V, v,
-                               planned ? sperm[i][lane] : __ldg(a.perm + (c0 + i) * 32 + lane));
+                for (int i = threadIdx.x >> 5; i < S; i += NT / 32) {
+                    const int32_t row = planned ? sperm[i][lane] : __ldg(a.perm + (c0 + i) * 32 + lane);
+                    row_update(c0 + i, wsm[i][lane], refresh ? ssm[i][lane] : 0.f, refresh, al, be, V, v, row,
+                               planned ? &sP[i][lane] : a.P + (row >= 0 ? row : 0),
+                               planned ? &sdx[i][lane] : a.dx + (row >= 0 ? row : 0));
+                }
             }
         } else {
             TF_SLICE_LOOP_BAL(a.nslices, s) {
@@ -1135,7 +1147,9 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_cg1(PcgCg1Args a)
                 const float sx = refresh ? sell_row<float>(a.ptr, a.col, a.val32, s, lane,
                                                            [&](int32_t j) { return kld(a.P + j); })
                                          : 0.f;
-                row_update(s, wn, sx, refresh, al, be, V, v, __ldg(a.perm + s * 32 + lane));
+                const int32_t row = __ldg(a.perm + s * 32 + lane);
+                row_update(s, wn, sx, refresh, al, be, V, v, row, a.P + (row >= 0 ? row : 0),
+                           a.dx + (row >= 0 ? row : 0));
             }
         }
         if (!grid_allreduce<float, 6>(a.g, epoch, v, o)) return false;
@@ -1145,13 +1159,33 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_pcg_cg1(PcgCg1Args a)
         return true;
     };
 
-    // FP64 fold of the FP32 correction (own rows), then a barrier
+    // FP64 fold of the FP32 correction (own rows; a planned block also
+    // publishes its p), then a barrier
     auto fold = [&]() -> bool {
-        TF_SLICE_LOOP_BAL(a.nslices, s) {
-            const int32_t row = __ldg(a.perm + s * 32 + lane);
-            if (row >= 0) {
-                a.x[row] += (double)a.dx[row];
-                a.dx[row] = 0.f;
+        if (planned) {
+            for (int i = threadIdx.x >> 5; i < (int)(sb1 - sb0); i += NT / 32) {
+                const int32_t row = sperm[i][lane];
+                if (row >= 0) {
+                    a.x[row] += (double)sdx[i][lane];
+                    sdx[i][lane] = 0.f;
+                    a.P[row] = sP[i][lane];
+                }
+            }
+        } else if (BLK) {
+            for (int64_t s = sb0 + (threadIdx.x >> 5); s < sb1; s += NT / 32) {
+                const int32_t row = __ldg(a.perm + s * 32 + lane);
+                if (row >= 0) {
+                    a.x[row] += (double)a.dx[row];
+                    a.dx[row] = 0.f;
+                }
+            }
+        } else {
+            TF_SLICE_LOOP_BAL(a.nslices, s) {
+                const int32_t row = __ldg(a.perm + s * 32 + lane);
+                if (row >= 0) {
+                    a.x[row] += (double)a.dx[row];
+                    a.dx[row] = 0.f;
+                }
             }
         }
         return grid_sync_ar(a.g, epoch);

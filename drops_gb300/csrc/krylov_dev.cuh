@@ -361,8 +361,9 @@ static_assert(kArMax == 8, "records of eight values");
 template <class T, int NV>
 __device__ bool grid_allreduce(const GridAR& g, unsigned long long& epoch, const T (&v)[NV], T (&out)[NV]) {
     static_assert(NV >= 1 && NV <= kArMax, "all-reduce width");
+    constexpr int kReadWarps = 8;  // warps that load block records
     __shared__ T red[kArMax][32];
-    __shared__ T res[kArMax];
+    __shared__ T tot_w[kArMax][kReadWarps];  // read after the last barrier of a call: not reused before the next
     __shared__ int st;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     T* part = ar_part<T>(g) + (size_t)(epoch & 1) * gridDim.x * kArMax;
@@ -383,25 +384,38 @@ __device__ bool grid_allreduce(const GridAR& g, unsigned long long& epoch, const
     }
     if (!ar_arrive_wait(g, epoch, &st)) return false;
     ++epoch;
-    // one warp reads every block's record of kArMax values (32 or 64 bytes,
-    // 16-byte loads: one L2 sector request per block and 16 bytes instead of
-    // one per value) and sums the blocks in a fixed order
-    if (w == 0) {
+    // the block records (kArMax values: 32 or 64 bytes, 16-byte loads, one
+    // L2 sector request per record) are spread over up to kReadWarps warps,
+    // one record per lane, so that they are in flight at once; each warp sums
+    // its records (in the order of the chunks it took, then the fixed shuffle
+    // tree) and every thread adds the warp totals in warp order, so every
+    // block derives the same bits
+    const int nchunks = (int)((gridDim.x + 31) / 32);
+    const int nread = nw < kReadWarps ? nw : kReadWarps;
+    if (w < nread) {
         T acc[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) acc[k] = T(0);
-        for (unsigned b = lane; b < gridDim.x; b += 32) {
-            T rec[8];
-            ar_load_record(part + (size_t)b * kArMax, rec);
+        for (int ch = w; ch < nchunks; ch += nread) {
+            const unsigned b = (unsigned)ch * 32u + (unsigned)lane;
+            if (b < gridDim.x) {
+                T rec[8];
+                ar_load_record(part + (size_t)b * kArMax, rec);
 #pragma unroll
-            for (int k = 0; k < 8; ++k) acc[k] += k < NV ? rec[k] : T(0);
+                for (int k = 0; k < 8; ++k) acc[k] += k < NV ? rec[k] : T(0);
+            }
         }
         const T tot = warp_sum8(acc, lane);
-        if ((lane & 3) == 0 && idx < NV) res[idx] = tot;
+        if ((lane & 3) == 0 && idx < NV) tot_w[idx][w] = tot;
     }
     __syncthreads();
+    const int nused = nchunks < nread ? nchunks : nread;
 #pragma unroll
-    for (int k = 0; k < NV; ++k) out[k] = res[k];
+    for (int k = 0; k < NV; ++k) {
+        T x = tot_w[k][0];
+        for (int ww = 1; ww < nused; ++ww) x += tot_w[k][ww];
+        out[k] = x;
+    }
     return true;
 }
 
