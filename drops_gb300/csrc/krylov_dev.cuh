@@ -363,7 +363,8 @@ __device__ bool grid_allreduce(const GridAR& g, unsigned long long& epoch, const
     static_assert(NV >= 1 && NV <= kArMax, "all-reduce width");
     constexpr int kReadWarps = 8;  // warps that load block records
     __shared__ T red[kArMax][32];
-    __shared__ T tot_w[kArMax][kReadWarps];  // read after the last barrier of a call: not reused before the next
+    __shared__ T tot_w[kArMax][kReadWarps];
+    __shared__ T res[kArMax];
     __shared__ int st;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     T* part = ar_part<T>(g) + (size_t)(epoch & 1) * gridDim.x * kArMax;
@@ -388,8 +389,9 @@ __device__ bool grid_allreduce(const GridAR& g, unsigned long long& epoch, const
     // L2 sector request per record) are spread over up to kReadWarps warps,
     // one record per lane, so that they are in flight at once; each warp sums
     // its records (in the order of the chunks it took, then the fixed shuffle
-    // tree) and every thread adds the warp totals in warp order, so every
-    // block derives the same bits
+    // tree), and NV lanes of warp 0 add the warp totals in warp order, so
+    // every block derives the same bits.  Only the NV used values are added:
+    // FP64 adds issue at a small fraction of the FP32 rate.
     const int nchunks = (int)((gridDim.x + 31) / 32);
     const int nread = nw < kReadWarps ? nw : kReadWarps;
     if (w < nread) {
@@ -402,20 +404,22 @@ __device__ bool grid_allreduce(const GridAR& g, unsigned long long& epoch, const
                 T rec[8];
                 ar_load_record(part + (size_t)b * kArMax, rec);
 #pragma unroll
-                for (int k = 0; k < 8; ++k) acc[k] += k < NV ? rec[k] : T(0);
+                for (int k = 0; k < NV; ++k) acc[k] += rec[k];
             }
         }
         const T tot = warp_sum8(acc, lane);
         if ((lane & 3) == 0 && idx < NV) tot_w[idx][w] = tot;
     }
     __syncthreads();
-    const int nused = nchunks < nread ? nchunks : nread;
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-        T x = tot_w[k][0];
-        for (int ww = 1; ww < nused; ++ww) x += tot_w[k][ww];
-        out[k] = x;
+    if (threadIdx.x < NV) {
+        const int nused = nchunks < nread ? nchunks : nread;
+        T x = tot_w[threadIdx.x][0];
+        for (int ww = 1; ww < nused; ++ww) x += tot_w[threadIdx.x][ww];
+        res[threadIdx.x] = x;
     }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; ++k) out[k] = res[k];
     return true;
 }
 
