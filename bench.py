@@ -306,7 +306,7 @@ def run_ours(args, rank, ws, dist):
     achieved = per_launch / ((ms_d / max(n_d, 1)) / 1e3) / 1e9 if ms_d > 0 else 0.0
     # DRAM bytes of one launch from an ncu capture of this workload (96^3):
     # dram__bytes_read.sum + dram__bytes_write.sum of k_pcg_cg1 / k_assemble<10>
-    traffic = {"pcg": 62.81e6, "assemble": None}.get(dom) if N == N_CUBES else None
+    traffic = {"pcg": 61.90e6, "assemble": None}.get(dom) if N == N_CUBES else None
     roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
                 "frac": round(achieved / hbm_peak, 4), "traffic": traffic, "peak_source": peak_src,
                 "bytes_model": note, "launch_ms": round(ms_d / max(n_d, 1), 4),
