@@ -95,3 +95,23 @@ def test_single_barrier_edge_cases(ctxs):
     x = ctx.vec_download(tf.VEC_X)
     rp, ci, S = ctx.matrix(tf.MAT_SYS)
     assert np.linalg.norm(b - O.spmv(rp, ci, S, x)) <= 1.01e-9
+
+
+def test_single_barrier_large_runs(ctxs):
+    """P2 system on 144^3 cubes (~327k rows, ~10k slices): the blocks' slice runs exceed one planned chunk of
+    64 slices, so blocks that walk several chunks and keep p and dx in global memory meet blocks that plan
+    once and keep them in shared memory; the solution must match FP64 PCG."""
+    ctx = ctxs[0]
+    nd = _system(ctx, 144, tf.P2IF)
+    assert nd > 64 * 32 * 152
+    ctx.vec_fill(tf.VEC_X, nd, 0.0)
+    st, it, res = ctx.pcg_jacobi(tf.MAT_SYS, tf.VEC_RHS, tf.VEC_X, tol=1e-10, precision=tf.PREC_MIXED)
+    assert st == tf.OK and res <= 1e-10
+    x = ctx.vec_download(tf.VEC_X)
+    assert _fp64_resid(ctx, x) <= 1.01e-10
+    ctx.vec_fill(tf.VEC_X, nd, 0.0)
+    st, it64, res = ctx.pcg_jacobi(tf.MAT_SYS, tf.VEC_RHS, tf.VEC_X, tol=1e-10, precision=tf.PREC_FP64)
+    assert st == tf.OK
+    print("iterations mixed", it, "fp64", it64)
+    ok, err = sol_close(x, ctx.vec_download(tf.VEC_X))
+    assert ok, err
