@@ -392,8 +392,11 @@ __device__ bool grid_allreduce(const GridAR& g, unsigned long long& epoch, const
     // tree), and NV lanes of warp 0 add the warp totals in warp order, so
     // every block derives the same bits.  Only the NV used values are added:
     // FP64 adds issue at a small fraction of the FP32 rate.
+    // FP64 records (the FP64 solvers, up to 3 blocks per SM) stay on one warp:
+    // the warp-sum trees of eight warps cost more FP64 issue than the
+    // sequential loads save
     const int nchunks = (int)((gridDim.x + 31) / 32);
-    const int nread = nw < kReadWarps ? nw : kReadWarps;
+    const int nread = sizeof(T) == 8 ? 1 : nw < kReadWarps ? nw : kReadWarps;
     if (w < nread) {
         T acc[8];
 #pragma unroll
