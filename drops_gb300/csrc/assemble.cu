@@ -488,7 +488,7 @@ struct AsmSmem {
     double phi[32][NL];   // also n.grad(phi) for the volume rule
     double sg[32][NL][3];
     double mob[32];
-    double fx[32];
+    double fx[32];  // sqrt(w) f(x_p): the load vector is sum_p (sqrt(w) f)(sqrt(w) phi_i)
     double wind[NL == 4 ? 30 : 1];    // N_P1P1: P2 wind at the 10 nodes, xyz
     double wn[NL == 4 ? 32 : 1][4];   // sqrt(w) (wind . surface gradient of phi_j)
     // linear level set on the tet (P1 forms): constant surface gradients of
@@ -639,7 +639,7 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
                     double x[3];
                     for (int c = 0; c < 3; ++c)
                         x[c] = S.g.X[0][c] * b[0] + S.g.X[1][c] * b[1] + S.g.X[2][c] * b[2] + S.g.X[3][c] * b[3];
-                    S.fx[lane] = rhs_value(A.rhs, x);
+                    S.fx[lane] = sw * rhs_value(A.rhs, x);
                 }
                 if constexpr (NL == 4) {
                     // N_P1P1: the P2 wind at the point (LocalP2CL at b: vertex
@@ -689,14 +689,16 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
             }
             if constexpr (NL == 4) {
                 if (wantF)
-                    for (int pp = lane >> 2; pp < cnt; pp += 8) accF += (S.w[pp] * S.fx[pp]) * S.phi[pp][lane & 3];
+                    for (int pp = lane >> 2; pp < cnt; pp += 8) accF += S.fx[pp] * S.phi[pp][lane & 3];
                 // N: 16 entries (i, j) = (lane / 4 % 4, lane % 4) on 2 point groups
                 if (wantN) {
                     const int i = (lane >> 2) & 3, j = lane & 3;
                     for (int pp = lane >> 4; pp < cnt; pp += 2) accN += S.phi[pp][i] * S.wn[pp][j];
                 }
-            } else if (wantF && lane < NL) {
-                for (int pp = 0; pp < cnt; ++pp) accF += (S.w[pp] * S.fx[pp]) * S.phi[pp][lane];
+            } else if (wantF && lane < 30) {
+                // P2: 10 rows x 3 point groups (combined after the last chunk)
+                const int i = lane % 10;
+                for (int pp = lane / 10; pp < cnt; pp += 3) accF += S.fx[pp] * S.phi[pp][i];
             }
             __syncwarp();
         }
@@ -716,6 +718,10 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
             accF += __shfl_down_sync(0xffffffffu, accF, 8);
             accF += __shfl_down_sync(0xffffffffu, accF, 4);
             accN += __shfl_down_sync(0xffffffffu, accN, 16);  // point groups: g0 + g1
+        } else if (wantF) {
+            // P2 load vector: point groups (g0 + g1) + g2
+            const double f1 = __shfl_down_sync(0xffffffffu, accF, 10), f2 = __shfl_down_sync(0xffffffffu, accF, 20);
+            accF = (accF + f1) + f2;
         }
         if (NL == 4 && wantC && lin) {
             // constant n . grad(phi_i): the 15-point rule reduces to its weight sum
