@@ -265,18 +265,20 @@ __device__ inline void unit_normal(const TetGeom& g, const double b[4], double n
     n[2] = v[2] * inv;
 }
 
-// Surface gradients (I - n n^T) grad(phi_i) and values phi_i at barycentric b.
+// Surface gradients scale (I - n n^T) grad(phi_i) and values phi_i at
+// barycentric b (the scale, sqrt of the point weight, enters through the four
+// projected grad(lambda_v), which every surface gradient combines linearly).
 // grad(phi_i) = sum_v c_iv(b) grad(lambda_v) with at most two terms (P2:
 // vertex i: (4 b_i - 1) grad(lambda_i); edge (a,c): 4 b_c grad(lambda_a) +
 // 4 b_a grad(lambda_c)), so the projection is applied to the four
 // grad(lambda_v) once and combined afterwards.
 template <bool P2>
-__device__ inline void surf_basis(const TetGeom& g, const double b[4], const double n[3], double* phi,
+__device__ inline void surf_basis(const TetGeom& g, const double b[4], const double n[3], double scale, double* phi,
                                   double (*sg)[3]) {
     double pg[4][3];
     for (int v = 0; v < 4; ++v) {
         const double ng = n[0] * g.gl[v][0] + n[1] * g.gl[v][1] + n[2] * g.gl[v][2];
-        for (int r = 0; r < 3; ++r) pg[v][r] = g.gl[v][r] - ng * n[r];
+        for (int r = 0; r < 3; ++r) pg[v][r] = scale * (g.gl[v][r] - ng * n[r]);
     }
     if constexpr (!P2) {
         for (int i = 0; i < 4; ++i) {
@@ -612,19 +614,19 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
                 const double w = S.P.fw[f] * cT.q2_w[q];
                 // values are stored times sqrt(w): sum_p w u_i u_j = sum_p (sqrt(w) u_i)(sqrt(w) u_j)
                 const double sw = w > 0. ? w * rsqrt_fp64(w) : 0.;
-                double phi[NL], sg[NL][3];
+                double phi[NL], sg[NL][3];  // sg: surface gradients times sqrt(w)
                 if (NL == 4 && lin) {
                     for (int i = 0; i < NL; ++i) phi[i] = b[i];
                 } else {
                     double n[3];
                     unit_normal(S.g, b, n);
-                    surf_basis<P2>(S.g, b, n, phi, sg);
+                    surf_basis<P2>(S.g, b, n, sw, phi, sg);
                 }
                 S.w[lane] = sw;
                 for (int i = 0; i < NL; ++i) {
                     S.phi[lane][i] = sw * phi[i];
                     if (!(NL == 4 && lin))
-                        for (int c = 0; c < 3; ++c) S.sg[lane][i][c] = sw * sg[i][c];
+                        for (int c = 0; c < 3; ++c) S.sg[lane][i][c] = sg[i][c];
                 }
                 if (wantL) {
                     double m = 1.0;
@@ -653,8 +655,12 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
                         for (int k = 0; k < 10; ++k)
                             for (int c = 0; c < 3; ++c) wv[c] += S.wind[3 * k + c] * h[k];
                         for (int j = 0; j < 4; ++j) {
-                            const double* g = lin ? S.lin_sg[j] : sg[j];
-                            S.wn[lane][j] = sw * (wv[0] * g[0] + wv[1] * g[1] + wv[2] * g[2]);
+                            if (lin) {
+                                const double* g = S.lin_sg[j];
+                                S.wn[lane][j] = sw * (wv[0] * g[0] + wv[1] * g[1] + wv[2] * g[2]);
+                            } else {  // sg carries sqrt(w) already
+                                S.wn[lane][j] = wv[0] * sg[j][0] + wv[1] * sg[j][1] + wv[2] * sg[j][2];
+                            }
                         }
                     }
                 }
