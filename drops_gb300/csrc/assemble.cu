@@ -40,7 +40,7 @@ struct Tables {
     signed char pat_bnd[81];
     signed char pat_f[81][2][3];  // ext ids: 0..3 vertex, 4..9 edge + 4
     double q2_node[7][3], q2_w[7];
-    double q3_node[15][4], q3_w[15];
+    double q3_node[15][4], q3_w[15], q3_sw[15];  // q3_sw = sqrt(q3_w)
     double qq2_node[4][3], qq2_w[4];  // Quad2_2D (legacy numbering)
     int sym_i[55], sym_j[55];  // packed upper triangle, NL = 10
     int sym4_i[10], sym4_j[10];  // NL = 4
@@ -163,6 +163,7 @@ static void build_tables(Tables& T) {
     for (int i = 1; i <= 4; ++i) T.q3_w[i] = 0.01198951396316977000173064248499538621936;
     for (int i = 5; i <= 8; ++i) T.q3_w[i] = 0.01151136787104539754677023934921978132914;
     for (int i = 9; i <= 14; ++i) T.q3_w[i] = 0.008818342151675485008818342151675485008818;
+    for (int i = 0; i < 15; ++i) T.q3_sw[i] = std::sqrt(T.q3_w[i]);
     const double qq[4][3] = {{1., 0., 0.}, {0., 1., 0.}, {0., 0., 1.}, {1. / 3., 1. / 3., 1. / 3.}};
     for (int i = 0; i < 4; ++i)
         for (int j = 0; j < 3; ++j) T.qq2_node[i][j] = qq[i][j];
@@ -301,11 +302,13 @@ __device__ inline void surf_basis(const TetGeom& g, const double b[4], const dou
     }
 }
 
-// n . grad(phi_i) at barycentric b (volume stabilisation)
+// scale n . grad(phi_i) at barycentric b (volume stabilisation; the scale,
+// sqrt of the point weight, enters through the four n . grad(lambda_v))
 template <bool P2>
-__device__ inline void normal_derivs(const TetGeom& g, const double b[4], const double n[3], double* dn) {
+__device__ inline void normal_derivs(const TetGeom& g, const double b[4], const double n[3], double scale,
+                                     double* dn) {
     double ng[4];
-    for (int v = 0; v < 4; ++v) ng[v] = n[0] * g.gl[v][0] + n[1] * g.gl[v][1] + n[2] * g.gl[v][2];
+    for (int v = 0; v < 4; ++v) ng[v] = scale * (n[0] * g.gl[v][0] + n[1] * g.gl[v][1] + n[2] * g.gl[v][2]);
     if constexpr (!P2) {
         for (int i = 0; i < 4; ++i) dn[i] = ng[i];
     } else {
@@ -744,7 +747,7 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
                 double n[3];
                 unit_normal(S.g, b, n);
                 double dn[NL];
-                normal_derivs<P2>(S.g, b, n, dn);
+                normal_derivs<P2>(S.g, b, n, cT.q3_sw[lane], dn);
                 for (int i = 0; i < NL; ++i) S.phi[lane][i] = dn[i];
             }
             __syncwarp();
@@ -753,7 +756,7 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
                 if (lane < 30) {
                     int i, j;
                     sym_entry(NL, lane % 10, i, j);
-                    for (int pp = lane / 10; pp < 15; pp += 3) sc += cT.q3_w[pp] * (S.phi[pp][j] * S.phi[pp][i]);
+                    for (int pp = lane / 10; pp < 15; pp += 3) sc += S.phi[pp][j] * S.phi[pp][i];
                 }
                 const double s1 = __shfl_down_sync(0xffffffffu, sc, 10), s2 = __shfl_down_sync(0xffffffffu, sc, 20);
                 accC[0] = ((sc + s1) + s2) * S.g.absdet;
@@ -764,7 +767,7 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
                     int i, j;
                     sym_entry(NL, k, i, j);
                     double sc = 0.;
-                    for (int pp = 0; pp < 15; ++pp) sc += cT.q3_w[pp] * (S.phi[pp][j] * S.phi[pp][i]);
+                    for (int pp = 0; pp < 15; ++pp) sc += S.phi[pp][j] * S.phi[pp][i];
                     accC[q] = sc * S.g.absdet;
                 }
             }
