@@ -63,7 +63,17 @@ struct Ctrl {
     unsigned count, gen;
     int status, iters;
     double resid;
+    int converged;
 };
+
+// block 0 publishes the outcome of the solve (every exit path calls this)
+__device__ void finish(Ctrl* ctl, int iters, double resid, bool converged) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        ctl->iters = iters;
+        ctl->resid = resid;
+        ctl->converged = converged ? 1 : 0;
+    }
+}
 
 __device__ bool barrier(Ctrl* ctl) {
     __threadfence();
@@ -152,6 +162,9 @@ template <int G>
 __global__ void __launch_bounds__(kThreads) k_pcg_noalloc(Args a) {
     const int64_t m = a.m;
     Ctrl* ctl = reinterpret_cast<Ctrl*>(a.scratch);
+    // Partials alternate between two buffers, one per reduction in turn (set-up: B;
+    // each iteration: A then B).  A block may only rewrite a buffer after every
+    // block has passed the barrier that follows its last read of that buffer.
     double* partA = a.scratch + kCtrlDoubles;
     double* partB = partA + (size_t)gridDim.x * 3;
     double* r = a.scratch + kCtrlDoubles + kPartDoubles;
@@ -196,19 +209,16 @@ __global__ void __launch_bounds__(kThreads) k_pcg_noalloc(Args a) {
                 v[2] += zi * ri;
             }
         }
-        partials<3>(v, partA);
+        partials<3>(v, partB);
     }
     if (!barrier(ctl)) return;
     double s0[3];
-    reduce_all<3>(partA, s0);
+    reduce_all<3>(partB, s0);
     double normb = sqrt(s0[1]);
     if (normb == 0.0 || !a.rel) normb = 1.0;
     double resid = sqrt(s0[0]) / normb, rho = s0[2], beta = 0.;
-    if (resid <= a.tol) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            ctl->iters = 0;
-            ctl->resid = resid;
-        }
+    if (resid <= a.tol || a.max_iter == 0) {
+        finish(ctl, 0, resid, resid <= a.tol);
         return;
     }
     double* pc = p0;
@@ -260,10 +270,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_noalloc(Args a) {
         reduce_all<2>(partB, s2);
         resid = sqrt(s2[0]) / normb;
         if (resid <= a.tol || it == a.max_iter) {
-            if (blockIdx.x == 0 && threadIdx.x == 0) {
-                ctl->iters = resid <= a.tol ? it : -it;
-                ctl->resid = resid;
-            }
+            finish(ctl, it, resid, resid <= a.tol);
             return;
         }
         const double rho1 = rho;
@@ -315,7 +322,7 @@ extern "C" int tf_pcg_jacobi_noalloc(int64_t m, const int32_t* rowptr, const int
         cudaStreamSynchronize(s) != cudaSuccess)
         return TF_ERR_CUDA;
     if (ctl.status != 0) return ctl.status;
-    *max_iter = ctl.iters >= 0 ? ctl.iters : -ctl.iters;
+    *max_iter = ctl.iters;
     *tol = ctl.resid;
-    return ctl.iters >= 0 ? TF_OK : TF_ERR_NOT_CONVERGED;
+    return ctl.converged ? TF_OK : TF_ERR_NOT_CONVERGED;
 }

@@ -345,10 +345,15 @@ int tf_ch_features(tf_context* ctx, int vec_cur, int vec_old, int vec_next, uint
  * hundred KB, about 13 MB), which every GPU that loads the library holds until
  * the process exits.  The call allocates nothing.  m > TF_NOALLOC_MAX_ROWS
  * returns TF_ERR_CAPACITY.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress) and must come before any stream
- * capture on that device.  Every call reuses the same array: calls that
- * overlap on the GPU (two streams, two host threads) race on it and must be
- * serialised by the caller.                                                    */
+ * device address (cudaGetSymbolAddress) and should come before any stream
+ * capture on that device.  Every call blocks the host: it reads nnz =
+ * rowptr[m] back before the launch and waits on `stream` for the outcome.
+ * Every call reuses
+ * the same array: calls that overlap on the GPU (two streams, two host
+ * threads) race on it and must be serialised by the caller.  Outcome as
+ * tf_pcg_jacobi: TF_OK on convergence; TF_ERR_NOT_CONVERGED with *max_iter =
+ * the iterations run and *tol = the true relative residual otherwise
+ * (max_iter = 0 runs none and reports the initial residual).                  */
 #define TF_NOALLOC_MAX_ROWS 262144
 int tf_pcg_jacobi_noalloc(int64_t m, const int32_t* rowptr, const int32_t* colind, const double* vals,
                           const double* b, double* x, int* max_iter, double* tol, int rel, void* stream);
