@@ -314,11 +314,21 @@ def run_ours(args, rank, ws, dist):
                 "traffic_note": "DRAM bytes per launch (ncu, profiles/k_pcg_cg1_p2_sphere96.md): the algorithmic "
                                 "bytes of the iterations are served from L2 after a one-time load"}
 
+    # ---- products of the step, for the parity check against the oracle (untimed) -----------
+    products = {"xs": {}}
+    for prec, name in ((tf.PREC_MIXED, "mixed"), (tf.PREC_FP64, "fp64")):
+        ctx.vec_fill(tf.VEC_X, state["m"], 0.0)
+        ctx.pcg_jacobi(tf.MAT_SYS, tf.VEC_RHS, tf.VEC_X, tol=TOL, precision=prec)
+        products["xs"][name] = ctx.vec_download(tf.VEC_X)
+    _, _, products["act"], products["l2g"] = ctx.dofs()
+    products["mats"] = [ctx.matrix(f) for f in forms]
+    products["rhs"] = ctx.vec_download(tf.VEC_RHS)
+
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": "cut_tets/s", "n_gpus": ws, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic (analytic level set)",
-        "config": CONFIG,
+        "config": CONFIG, "_products": products,
         "e2e": {"value": round(e2e_value, 1), "unit": "cut_tets/s", "h2d_bytes_per_step": 8 * (nv + ne),
                 "d2h_bytes_per_step": 8 * state["m"], "ms_per_step": round(e2e_total / args.steps, 3)},
         "gpu_launches": int(launches),
@@ -621,8 +631,12 @@ def ch_cpu_sample(args, threads, budget_s=20.0):
 
 
 # ---------------------------------------------------------------------------
+CPU_THREADING = "DistributeDOFs serial, assembly serial, PCG's SpMV on all host threads (OpenMP)"
+
+
 def cpu_workload(threads, N=N_CUBES):
-    """The same step with the oracle (C restatement of the reference) on the host."""
+    """The same step with the oracle (C restatement of the reference) on the host.  step(keep) returns
+    (cut tets, seconds, PCG iterations, seconds per phase, the step's products if keep)."""
     from oracle import pyoracle as O
 
     O.set_threads(threads)
@@ -631,15 +645,51 @@ def cpu_workload(threads, N=N_CUBES):
     lv, le = O.levelset(mesh, O.LS_SPHERE, SPHERE, True)
     opts = O.make_opts(True, [O.FORM_M, O.FORM_A, O.FORM_CN], O.RHS_SPHERE_XYZ, RHS)
 
-    def step():
+    def step(keep=False):
         t0 = time.perf_counter()
         st, na, m, dv, de, act = O.distribute_dofs(mesh, lv, le, True)
+        t1 = time.perf_counter()
         st, rp, ci, vals, rhs = O.assemble(mesh, lv, le, act, dv, de, m, opts)
+        t2 = time.perf_counter()
         S = vals[O.FORM_M] + vals[O.FORM_A] + H * vals[O.FORM_CN]
         st, x, it, res = O.pcg_jacobi(rp, ci, S, rhs, tol=TOL)
-        return na, time.perf_counter() - t0, it
+        t3 = time.perf_counter()
+        phases = {"dofs_s": round(t1 - t0, 3), "assemble_s": round(t2 - t1, 3), "solve_s": round(t3 - t2, 3)}
+        prod = None
+        if keep:
+            from tests.helpers import loc2glo
+
+            prod = {"act": np.nonzero(act)[0], "l2g": loc2glo(mesh, act, dv, de, True), "rowptr": rp, "colind": ci,
+                    "vals": [vals[O.FORM_M], vals[O.FORM_A], vals[O.FORM_CN]], "rhs": rhs, "S": S, "x": x}
+        return na, t3 - t0, it, phases, prod
 
     return step
+
+
+def parity_report(gpu, ref):
+    """The GPU step's products against the oracle's FP64 ones on the same inputs (outside any timed region):
+    pattern and numbering bit for bit, matrix entries per entry against their row's scale (tolerance 1e-12,
+    tests/helpers.py), the worst plain per-entry relative error (entries above 1e-12 max|b|), and each GPU
+    solution's error against the oracle's FP64 PCG solution with the oracle's FP64 residual of it."""
+    from oracle import pyoracle as O
+    from tests.helpers import entry_rel_err, mat_close, sha
+
+    same = (sha(gpu["act"].astype(np.int64)) == sha(ref["act"].astype(np.int64))
+            and sha(gpu["l2g"].astype(np.int64)) == sha(ref["l2g"].astype(np.int64))
+            and all(sha(rp.astype(np.int64)) == sha(ref["rowptr"].astype(np.int64))
+                    and sha(ci.astype(np.int64)) == sha(ref["colind"].astype(np.int64)) for rp, ci, _ in gpu["mats"]))
+    row_err = max(mat_close(v, rv, ref["rowptr"])[1] for (_, _, v), rv in zip(gpu["mats"], ref["vals"]))
+    ent_err = max(entry_rel_err(v, rv) for (_, _, v), rv in zip(gpu["mats"], ref["vals"]))
+    nb = np.linalg.norm(ref["rhs"])
+    sol = {}
+    for name, x in gpu["xs"].items():
+        sol[name] = {"rel_err": float(np.linalg.norm(x - ref["x"]) / np.linalg.norm(ref["x"])),
+                     "oracle_fp64_resid": float(np.linalg.norm(ref["rhs"] - O.spmv(ref["rowptr"], ref["colind"],
+                                                                                    ref["S"], x)) / nb)}
+    return {"against": "oracle (C restatement of the reference, FP64; pinned to the reference's outputs)",
+            "pattern_numbering_sha_equal": bool(same), "max_row_scaled_entry_err": row_err,
+            "max_rel_entry_err": ent_err, "rhs_err": mat_close(gpu["rhs"], ref["rhs"])[1],
+            "entry_tolerance": "|a_ij - b_ij| <= 1e-12 * max(max_k |b_ik|, 1e-4 max|b|); rhs: 1e-12 max|b|", "solution": sol}
 
 
 def run_reference(args, rank, ws, dist):
@@ -662,7 +712,7 @@ def run_reference(args, rank, ws, dist):
         step()
     tot_t, tot_cut = 0.0, 0
     for _ in range(args.steps):
-        na, dt, it = step()
+        na, dt, it, phases, _ = step()
         tot_t += dt
         tot_cut += na
     value = tot_cut / tot_t
@@ -673,7 +723,8 @@ def run_reference(args, rank, ws, dist):
         "data": "synthetic (analytic level set)", "config": CONFIG,
         "cpu_baseline": {"value": round(value, 1), "unit": "cut_tets/s", "cores": threads, "kind": "port",
                          "sample": "the full workload per step (FP64 Jacobi-PCG as in the reference); "
-                                   "C restatement of the reference in oracle/, SpMV on all host threads"},
+                                   "C restatement of the reference in oracle/: " + CPU_THREADING,
+                         "phases_last_step": phases},
         "e2e": {"value": round(value, 1), "unit": "cut_tets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -738,12 +789,16 @@ def main():
     if args.size != N_CUBES:
         out["config"] = dict(out["config"], workload=f"PROFILING SIZE {args.size}^3 (not the benchmark workload)")
     if rank == 0:
+        products = out.pop("_products")
         if ws == 1 and not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
             step = cpu_workload(threads, args.size)
-            na, dt, it = step()
+            na, dt, it, phases, ref = step(keep=True)
             out["cpu_baseline"] = {"value": round(na / dt, 1), "unit": "cut_tets/s", "cores": threads, "kind": "port",
-                                   "sample": f"one full step of the same workload ({dt:.1f} s, FP64 PCG {it} iterations)"}
+                                   "sample": f"one full step of the same workload ({dt:.1f} s, FP64 PCG {it} "
+                                             f"iterations); {CPU_THREADING}",
+                                   "phases": phases}
+            out["parity"] = parity_report(products, ref)
         print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()

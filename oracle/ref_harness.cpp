@@ -17,7 +17,16 @@
 //       (surfactant/ifacetransp.cpp:367-380, 499-512, 532-563) on the unit sphere,
 //       P2 level set, CreateNumbering(P1IF_FE)
 //   ref_harness area <out>                  tests/principallattice.cpp:316-347
-//   ref_harness gmres <n> <a> <steps> <out> Cahn-Hilliard BDF1 steps, DROPS GMRES
+//   ref_harness gmres <n> <a> <steps> <out>
+//       Torus (R = 1, r = 0.4) P1 system on [-a,a]^3, n^3 cubes:
+//       GMRES (num/krylovsolver.h:320-463) with JACPcCL on M + A + h C_n, right
+//       and left preconditioned; the 2x2 Cahn-Hilliard block matrix of
+//       surfphasesep/surfphasesep.cpp:431-434 built by the block constructor
+//       (num/spmat.h:718-750) and solved by GMRES(50); <steps> warm-started
+//       BDF1 steps (surfphasesep.cpp:414-440), plain and with degenerate
+//       mobility + wind.  The block solves use a nodal 2x2 block-Jacobi
+//       preconditioner written here (DROPS's own driver preconditions with a
+//       KLU factorisation through Trilinos, which is not buildable).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -531,6 +540,202 @@ int cmd_area(int argc, char** argv) {
     return 0;
 }
 
+// Nodal 2x2 block Jacobi for a 2x2 block system of size 2h: for DOF i the
+// inverse of [[B(i,i), B(i,i+h)], [B(i+h,i), B(i+h,i+h)]] applied to
+// (b_i, b_{i+h}).  Test infrastructure with the Apply(A, x, b, ex) interface
+// that DROPS's GMRES calls on its preconditioner.
+class NodalBlockJacobiPcCL {
+    std::vector<double> inv_;
+    size_t h_ = 0;
+
+  public:
+    explicit NodalBlockJacobiPcCL(const MatrixCL& B) : inv_(2 * B.num_rows()), h_(B.num_rows() / 2) {
+        auto at = [&](size_t r, size_t c) {
+            for (size_t k = B.raw_row()[r]; k < B.raw_row()[r + 1]; ++k)
+                if (B.raw_col()[k] == c) return B.raw_val()[k];
+            return 0.;
+        };
+        for (size_t i = 0; i < h_; ++i) {
+            const double a11 = at(i, i), a12 = at(i, i + h_), a21 = at(i + h_, i), a22 = at(i + h_, i + h_);
+            const double det = a11 * a22 - a12 * a21;
+            inv_[4 * i] = a22 / det;
+            inv_[4 * i + 1] = -a12 / det;
+            inv_[4 * i + 2] = -a21 / det;
+            inv_[4 * i + 3] = a11 / det;
+        }
+    }
+    template <typename Mat, typename Vec, typename ExT>
+    void Apply(const Mat&, Vec& x, const Vec& b, const ExT&) const {
+        for (size_t i = 0; i < h_; ++i) {
+            const double u = b[i], v = b[i + h_];
+            x[i] = inv_[4 * i] * u + inv_[4 * i + 1] * v;
+            x[i + h_] = inv_[4 * i + 2] * u + inv_[4 * i + 3] * v;
+        }
+    }
+};
+
+int cmd_gmres(int argc, char** argv) {
+    if (argc < 6) throw std::invalid_argument("usage: gmres n a steps out");
+    const int n = std::atoi(argv[2]);
+    const double a = std::atof(argv[3]);
+    const int steps = std::atoi(argv[4]);
+    Writer w(argv[5]);
+
+    BrickBuilderCL brick(Point3DCL(-a), 2. * a * std_basis<3>(1), 2. * a * std_basis<3>(2), 2. * a * std_basis<3>(3), n, n,
+                         n);
+    MultiGridCL mg(brick);
+    FESystem sys;
+    auto& levelSet = sys.params.levelSet;
+    IdxDescCL lsIdx(P2_FE);
+    lsIdx.DistributeDOFs(0, mg);
+    levelSet.SetIdx(&lsIdx);
+    const Uint li = lsIdx.GetIdx();
+    // P1 level set stored as a P2 vector (LinearLSInit, surfactant/surfactant.cpp:748-758)
+    DROPS_FOR_TRIANG_VERTEX(mg, 0, it) levelSet.Data[it->Unknowns(li)] = ls_value("torus", it->GetCoord());
+    DROPS_FOR_TRIANG_EDGE(mg, 0, it)
+        levelSet.Data[it->Unknowns(li)] = 0.5 * (levelSet.Data[it->GetVertex(0)->Unknowns(li)] +
+                                                 levelSet.Data[it->GetVertex(1)->Unknowns(li)]);
+    IdxDescCL ifIdx(P1IF_FE);
+    ifIdx.DistributeDOFs(0, mg, &levelSet);
+    const size_t m = ifIdx.NumUnknowns();
+    w.i("n_dofs", (int64_t)m);
+    sys.params.surfCahnHilliardParams.f = [](Point3DCL const& x, double) {
+        Point3DCL y = x - (x.norm() - 1.0) * (x / x.norm());
+        return 13. * y[0] * y[1] * y[2];
+    };
+    FEMatDescCL M(&ifIdx, &ifIdx, &LocalAssembler::M_P1P1), A(&ifIdx, &ifIdx, &LocalAssembler::A_P1P1),
+        C(&ifIdx, &ifIdx, &LocalAssembler::C_n_P1P1);
+    FEVecDescCL f(&ifIdx, &LocalAssembler::F_concentration_P1);
+    sys.matrices = {&M, &A, &C};
+    sys.vectors = {&f};
+    setupFESystem(mg, sys);
+    write_csr(w, "M", M.Data);
+    const double h = 2. * a / n;
+
+    // GMRES(20) with point Jacobi on the surface Poisson system, both preconditioning sides
+    {
+        MatrixCL S(1., M.Data, 1., A.Data, h, C.Data);
+        write_csr(w, "S", S);
+        w.d("rhs", std::vector<double>(std::begin(f.Data), std::end(f.Data)));
+        JACPcCL pc;
+        const char* side[2] = {"right", "left"};
+        for (int s = 0; s < 2; ++s) {
+            VectorCL x(0., m);
+            int it = 100000;
+            double tol = 1e-10;
+            const bool ok = GMRES(S, x, f.Data, ifIdx.GetEx(), pc, 20, it, tol, true, false,
+                                  s == 0 ? RightPreconditioning : LeftPreconditioning);
+            w.i(std::string("gmres_") + side[s] + "_ok", ok ? 1 : 0);
+            w.i(std::string("gmres_") + side[s] + "_iters", it);
+            w.s(std::string("gmres_") + side[s] + "_resid", tol);
+            w.d(std::string("gmres_") + side[s] + "_x", std::vector<double>(std::begin(x), std::end(x)));
+        }
+    }
+
+    // Cahn-Hilliard: dt = 1e-3, mobility 1, eps = 0.02, rho_vol = h, beta_s = 0, xi = 1
+    const double dt = 1e-3, alpha = 1. / dt, mob = 1., eps = 0.02, rho = h, beta_s = 0., xi = 1.;
+    w.s("dt", dt);
+    w.s("eps", eps);
+    w.s("rho", rho);
+    w.s("beta_s", beta_s);
+    w.s("xi", xi);
+    auto chemicalPotential = [&](double c) { return xi * 2 * c * (1 - c) * (1 - 2 * c); };  // surfphasesep.cpp:140-151
+    auto block = [&](const MatrixCL& UL, const MatrixCL& Amob) {  // surfphasesep.cpp:431-434
+        return MatrixCL(UL, MatrixCL(mob, Amob, rho, C.Data), MatrixCL(eps * eps, A.Data, beta_s, M.Data, eps * eps * rho, C.Data),
+                        MatrixCL(-1., M.Data));
+    };
+    // right-hand side of a BDF1 step from chi (surfphasesep.cpp:421-425, f = 0)
+    auto rhs_of = [&](const VectorCL& chi) {
+        VectorCL F_chi((1. / dt) * (M.Data * chi));
+        VectorCL fp(m);
+        for (size_t i = 0; i < m; ++i) fp[i] = chemicalPotential(chi[i]);
+        VectorCL F_omega(beta_s * (M.Data * chi) - M.Data * fp);
+        VectorCL b(2 * m);
+        b[std::slice(0, m, 1)] = F_chi;
+        b[std::slice(m, m, 1)] = F_omega;
+        return b;
+    };
+    auto solve = [&](const MatrixCL& B, VectorCL& x, const VectorCL& b, int& it, double& tol) {
+        NodalBlockJacobiPcCL pc(B);
+        it = 20000;
+        tol = 1e-10;
+        return GMRES(B, x, b, ifIdx.GetEx(), pc, 50, it, tol, true, false, RightPreconditioning);
+    };
+    std::mt19937_64 rng(11);
+    std::uniform_real_distribution<double> U(-0.01, 0.01);
+    VectorCL chi0(m);
+    for (size_t i = 0; i < m; ++i) chi0[i] = 0.5 + U(rng);
+    w.d("chi0", std::vector<double>(std::begin(chi0), std::end(chi0)));
+    {
+        const MatrixCL B = block(MatrixCL(alpha, M.Data), A.Data);
+        write_csr(w, "B", B);
+        // one solve from a zero initial guess
+        VectorCL x(0., 2 * m);
+        int it;
+        double tol;
+        const bool ok = solve(B, x, rhs_of(chi0), it, tol);
+        w.i("block_ok", ok ? 1 : 0);
+        w.i("block_iters", it);
+        w.s("block_resid", tol);
+        w.d("block_x", std::vector<double>(std::begin(x), std::end(x)));
+        // BDF1 steps, each warm-started from the previous [chi; omega]
+        VectorCL X(0., 2 * m);
+        X[std::slice(0, m, 1)] = chi0;
+        std::vector<int64_t> its;
+        std::vector<double> res, states;
+        for (int k = 0; k < steps; ++k) {
+            VectorCL chi(X[std::slice(0, m, 1)]);
+            if (!solve(B, X, rhs_of(chi), it, tol)) throw std::runtime_error("BDF1 step did not converge");
+            its.push_back(it);
+            res.push_back(tol);
+            states.insert(states.end(), std::begin(X), std::end(X));
+        }
+        w.l("steps_iters", its);
+        w.d("steps_resid", res);
+        w.d("steps_X", states);
+    }
+    // BDF1 steps with degenerate mobility (LaplaceM_P1P1 from the current chi,
+    // surfactant/ifacetransp.h:1533-1544) and wind convection N_P1P1 (:1590-1600)
+    {
+        IdxDescCL velIdx(vecP2IF_FE);
+        velIdx.DistributeDOFs(0, mg, &levelSet);
+        VecDescCL wind(&velIdx);
+        wind.Interpolate(mg, [](Point3DCL const& x) { return wind_value(x); });
+        std::uniform_real_distribution<double> U3(-0.3, 0.3);
+        std::mt19937_64 rng3(9);
+        VectorCL X(0., 2 * m);
+        for (size_t i = 0; i < m; ++i) X[i] = 0.5 + U3(rng3);
+        w.d("dm_chi0", std::vector<double>(std::begin(X), std::begin(X) + m));
+        VecDescCL chi(&ifIdx);
+        std::vector<int64_t> its;
+        std::vector<double> res, states;
+        for (int k = 0; k < steps; ++k) {
+            chi.Data = VectorCL(X[std::slice(0, m, 1)]);
+            FESystem csys;
+            csys.params.levelSet.SetIdx(&lsIdx);
+            csys.params.levelSet.Data = levelSet.Data;
+            csys.params.surfCahnHilliardParams.useDegenerateMobility = true;
+            csys.params.surfCahnHilliardParams.chi = &chi;
+            csys.params.surfCahnHilliardParams.u_T = &wind;
+            FEMatDescCL Adeg(&ifIdx, &ifIdx, &LocalAssembler::LaplaceM_P1P1), N(&ifIdx, &ifIdx, &LocalAssembler::N_P1P1);
+            csys.matrices = {&Adeg, &N};
+            setupFESystem(mg, csys);
+            const MatrixCL B = block(MatrixCL(alpha, M.Data, 1., N.Data), Adeg.Data);
+            if (k == 0) write_csr(w, "dm_B0", B);
+            int it;
+            double tol;
+            if (!solve(B, X, rhs_of(chi.Data), it, tol)) throw std::runtime_error("BDF1 step did not converge");
+            its.push_back(it);
+            res.push_back(tol);
+            states.insert(states.end(), std::begin(X), std::end(X));
+        }
+        w.l("dm_steps_iters", its);
+        w.d("dm_steps_resid", res);
+        w.d("dm_steps_X", states);
+    }
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -541,6 +746,7 @@ int main(int argc, char** argv) {
         if (cmd == "legacy_numb") return cmd_legacy_numb(argc, argv);
         if (cmd == "legacy_forms") return cmd_legacy_forms(argc, argv);
         if (cmd == "area") return cmd_area(argc, argv);
+        if (cmd == "gmres") return cmd_gmres(argc, argv);
         throw std::invalid_argument("unknown command " + cmd);
     } catch (std::exception& e) {
         std::cerr << "ref_harness: " << e.what() << "\n";

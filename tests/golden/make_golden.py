@@ -123,6 +123,35 @@ def legacy_forms_case(n=10, a=1.6):
     print("legacy forms", n, "dofs", int(d["n_dofs"][0]), "nnz", len(d["M.colind"]))
 
 
+def ch_case(n=16, a=1.6, steps=3):
+    """GMRES with point Jacobi (both sides) on M + A + h C_n, the 2x2 Cahn-Hilliard block matrix and
+    warm-started BDF1 steps (plain; degenerate mobility + wind) on the P1 torus, all by the reference's
+    own GMRES and block constructor."""
+    d = run("gmres", str(n), repr(a), str(steps))
+    t = np.load(os.path.join(HERE, "torus_p1_n16.npz"))
+    assert np.array_equal(d["M.rowptr"], t["rowptr"]) and np.array_equal(d["M.colind"], t["colind"])
+    assert np.array_equal(d["M.vals"], t["M"]) and np.array_equal(d["S.vals"], t["S"]) and np.array_equal(d["rhs"], t["rhs"])
+    out = dict(n=n, a=a, n_dofs=int(d["n_dofs"][0]))
+    for k in ("dt", "eps", "rho", "beta_s", "xi"):
+        out[k] = float(d[k][0])
+    for side in ("right", "left"):
+        assert int(d[f"gmres_{side}_ok"][0]) == 1
+        out[f"gmres_{side}_iters"] = int(d[f"gmres_{side}_iters"][0])
+        out[f"gmres_{side}_resid"] = float(d[f"gmres_{side}_resid"][0])
+        out[f"gmres_{side}_x"] = d[f"gmres_{side}_x"]
+    out.update(chi0=d["chi0"], B_rowptr=d["B.rowptr"], B_colind=d["B.colind"].astype(np.int32), B=d["B.vals"])
+    assert int(d["block_ok"][0]) == 1
+    out.update(block_iters=int(d["block_iters"][0]), block_resid=float(d["block_resid"][0]), block_x=d["block_x"])
+    out.update(steps_iters=d["steps_iters"].astype(np.int32), steps_resid=d["steps_resid"],
+               steps_X=d["steps_X"].reshape(steps, -1))
+    assert np.array_equal(d["dm_B0.rowptr"], d["B.rowptr"]) and np.array_equal(d["dm_B0.colind"], d["B.colind"])
+    out.update(dm_chi0=d["dm_chi0"], dm_B0=d["dm_B0.vals"], dm_steps_iters=d["dm_steps_iters"].astype(np.int32),
+               dm_steps_resid=d["dm_steps_resid"], dm_steps_X=d["dm_steps_X"].reshape(steps, -1))
+    np.savez_compressed(os.path.join(HERE, f"ch_torus_p1_n{n}.npz"), **out)
+    print("ch", n, "dofs", out["n_dofs"], "gmres", out["gmres_right_iters"], out["gmres_left_iters"], "block",
+          out["block_iters"], "steps", out["steps_iters"].tolist(), "dm steps", out["dm_steps_iters"].tolist())
+
+
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
@@ -133,3 +162,4 @@ if __name__ == "__main__":
     area_case()
     legacy_case()
     legacy_forms_case()
+    ch_case()

@@ -74,9 +74,9 @@ def test_batch_numbering_and_matrices_bitexact(ctx, batch):
         assert np.array_equal(rp[r0:r1 + 1] - z0, R["rp"])
         assert np.array_equal(ci[z0:z1] - r0, R["ci"])
         for f in FORMS:
-            ok, err = mat_close(mats[f][2][z0:z1], R["vals"][f])
+            ok, err = mat_close(mats[f][2][z0:z1], R["vals"][f], R["rp"])
             assert ok, (i, f, err)
-        ok, err = mat_close(S[z0:z1], R["S"])
+        ok, err = mat_close(S[z0:z1], R["S"], R["rp"])
         assert ok, (i, err)
         ok, err = mat_close(rhs[r0:r1], R["rhs"])
         assert ok, (i, err)

@@ -1,4 +1,4 @@
-"""CGS2 GMRES (FP64 and FP32 Arnoldi cycles inside FP64 refinement) against the oracle's GMRES."""
+"""CGS2 GMRES (FP64 and FP32 Arnoldi cycles inside FP64 refinement) against the reference's GMRES solutions."""
 import numpy as np
 import pytest
 
@@ -26,19 +26,22 @@ def resid(rp, ci, v, x, b):
 
 @pytest.mark.parametrize("precision,orth", [(tf.PREC_MIXED, tf.ORTH_MGS), (tf.PREC_FP64, tf.ORTH_CGS2)])
 def test_ch_block_gmres2(ctx, golden, precision, orth):
-    g = golden("torus_p1_n16.npz")
-    om, p2, na, nd = setup_case(ctx, g, O.LS_TORUS, [1.0, 0.4, 2])
+    """CGS2 GMRES (FP32 cycles in FP64 refinement, or FP64) on the Cahn-Hilliard block system against the
+    reference's own GMRES(50) solve of the same system (ch_torus_p1_n16.npz): FP64 residual 1e-10 on the
+    reference's block matrix, solution within 1e-5 of the reference's (the block system's conditioning
+    turns a 1e-10 residual into ~1e-7 differences between two solvers), deterministic."""
+    t, g = golden("torus_p1_n16.npz"), golden("ch_torus_p1_n16.npz")
+    om, p2, na, nd = setup_case(ctx, t, O.LS_TORUS, [1.0, 0.4, 2])
     ctx.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN])
-    dt, eps, h = 1e-3, 0.02, 2 * float(g["a"]) / int(g["n"])
-    alpha, rho, beta = 1.0 / dt, h, 0.0
+    dt, eps, rho, beta = float(g["dt"]), float(g["eps"]), float(g["rho"]), float(g["beta_s"])
+    alpha = 1.0 / dt
     ctx.ch_block(alpha, 1.0, rho, eps * eps, beta)
-    brp, bci, bv = O.ch_block(g["rowptr"], g["colind"], g["M"], g["A"], g["C"], alpha, 1.0, rho, eps * eps, beta)
-    rng = np.random.default_rng(7)
-    chi = 0.5 + rng.uniform(-0.01, 0.01, nd)
-    Mchi = O.spmv(g["rowptr"], g["colind"], g["M"], chi)
+    brp, bci, bv = g["B_rowptr"], g["B_colind"], g["B"]
+    chi = g["chi0"]
+    Mchi = O.spmv(t["rowptr"], t["colind"], t["M"], chi)
     fp = 2 * chi * (1 - chi) * (1 - 2 * chi)
-    rhs = np.concatenate([alpha * Mchi, beta * Mchi - O.spmv(g["rowptr"], g["colind"], g["M"], fp)])
-    ost, ox, oit, ores = O.gmres_jacobi(brp, bci, bv, rhs, restart=50, tol=1e-10, max_iter=20000, block=True)
+    rhs = np.concatenate([alpha * Mchi, beta * Mchi - O.spmv(t["rowptr"], t["colind"], t["M"], fp)])
+    rx, rit = g["block_x"], int(g["block_iters"])
     ctx.gmres_options(orth)
     try:
         ctx.vec_upload(tf.VEC_B, rhs)
@@ -54,11 +57,11 @@ def test_ch_block_gmres2(ctx, golden, precision, orth):
         ctx.gmres_options(tf.ORTH_MGS)
     assert st == tf.OK and res <= 1e-10
     r = resid(brp, bci, bv, x, rhs)
-    print(f"iterations {it} (oracle MGS {oit}), FP64 residual {r:.3e}, |x-x_ref|/|x_ref| "
-          f"{np.linalg.norm(x - ox) / np.linalg.norm(ox):.3e}")
+    print(f"iterations {it} (reference MGS {rit}), FP64 residual {r:.3e}, |x-x_ref|/|x_ref| "
+          f"{np.linalg.norm(x - rx) / np.linalg.norm(rx):.3e}")
     assert r <= 1.01e-10
-    assert it <= 1.5 * oit + 60
-    assert np.linalg.norm(x - ox) <= 1e-5 * np.linalg.norm(ox)
+    assert it <= 1.5 * rit + 60
+    assert np.linalg.norm(x - rx) <= 1e-5 * np.linalg.norm(rx)
 
 
 @pytest.mark.parametrize("name,kind,par", [SYSTEMS[0], SYSTEMS[1]])
@@ -69,7 +72,7 @@ def test_point_jacobi_gmres2_mixed(ctx, golden, name, kind, par):
     h = 2 * float(g["a"]) / int(g["n"])
     ctx.lincomb([tf.FORM_M, tf.FORM_A, tf.FORM_CN], [1.0, 1.0, h])
     rp, ci, S = ctx.matrix(tf.MAT_SYS)
-    ok, err = mat_close(S, g["S"])
+    ok, err = mat_close(S, g["S"], rp)
     assert ok, err
     ctx.vec_fill(tf.VEC_X, nd, 0.0)
     st, it, res = ctx.gmres_jacobi(tf.MAT_SYS, tf.VEC_RHS, tf.VEC_X, restart=30, tol=1e-10, max_iter=20000,

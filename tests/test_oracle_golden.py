@@ -47,7 +47,7 @@ def test_assembly_matches_reference(golden, name, kind, par):
     assert st == O.OK
     assert np.array_equal(rp, g["rowptr"]) and np.array_equal(ci, g["colind"])
     for f, key in ((O.FORM_M, "M"), (O.FORM_A, "A"), (O.FORM_CN, "C")):
-        ok, err = mat_close(vals[f], g[key])
+        ok, err = mat_close(vals[f], g[key], g["rowptr"])
         assert ok, (key, err)
     ok, err = mat_close(rhs, g["rhs"])
     assert ok, err
@@ -65,9 +65,9 @@ def test_wind_convection_matches_reference(golden, name, kind, par):
     st, rp, ci, vals, rhs = O.assemble(mesh, lv, le, act, dv, de, nd, opts)
     assert st == O.OK
     assert np.array_equal(rp, g["rowptr"]) and np.array_equal(ci, g["colind"])
-    ok, err = mat_close(vals[O.FORM_N], g["N"])
+    ok, err = mat_close(vals[O.FORM_N], g["N"], g["rowptr"])
     assert ok, err
-    ok, err = mat_close(vals[O.FORM_M], g["M"])
+    ok, err = mat_close(vals[O.FORM_M], g["M"], g["rowptr"])
     assert ok, err
     # not symmetric: N differs from its transpose
     import scipy.sparse as sp
@@ -86,7 +86,7 @@ def test_laplace_m_degenerate_matches_reference(golden, name, kind, par):
     opts = O.make_opts(False, [O.FORM_LAPM], chi=g["chi"], degenerate=True)
     st, rp, ci, vals, rhs = O.assemble(mesh, lv, le, act, dv, de, nd, opts)
     assert st == O.OK and np.array_equal(ci, g["colind"])
-    ok, err = mat_close(vals[O.FORM_LAPM], g["LapM"])
+    ok, err = mat_close(vals[O.FORM_LAPM], g["LapM"], g["rowptr"])
     assert ok, err
 
 
@@ -101,10 +101,79 @@ def test_pcg_jacobi_matches_reference(golden, name):
     assert ok, err
 
 
+@pytest.mark.parametrize("side,method", [("right", 0), ("left", 1)])
+def test_gmres_jacobi_matches_reference(golden, side, method):
+    """DROPS GMRES(20) with JACPcCL (num/krylovsolver.h:320-463) on the torus system M + A + h C_n:
+    the oracle takes the same iteration count and lands on the same solution."""
+    t, g = golden("torus_p1_n16.npz"), golden("ch_torus_p1_n16.npz")
+    st, x, it, res = O.gmres_jacobi(t["rowptr"], t["colind"], t["S"], t["rhs"], restart=20, tol=1e-10, method=method)
+    assert st == O.OK and it == int(g[f"gmres_{side}_iters"])
+    assert abs(res - float(g[f"gmres_{side}_resid"])) <= 1e-14
+    ok, err = sol_close(x, g[f"gmres_{side}_x"], 1e-12)
+    assert ok, err
+
+
+def ch_rhs(t, chi, dt, beta, xi=1.0):
+    """Right-hand side of a BDF1 Cahn-Hilliard step, f = 0 (surfphasesep.cpp:421-425)."""
+    Mc = O.spmv(t["rowptr"], t["colind"], t["M"], chi)
+    Mf = O.spmv(t["rowptr"], t["colind"], t["M"], xi * 2 * chi * (1 - chi) * (1 - 2 * chi))
+    return np.concatenate([Mc / dt, beta * Mc - Mf])
+
+
+def test_ch_block_and_gmres_match_reference(golden):
+    """The 2x2 block matrix of surfphasesep.cpp:431-434 from the reference's block constructor
+    (num/spmat.h:718-750) bit for bit, and DROPS GMRES(50) with nodal block Jacobi on it: the same
+    iteration count, one solve from zero and three warm-started BDF1 steps."""
+    t, g = golden("torus_p1_n16.npz"), golden("ch_torus_p1_n16.npz")
+    rp, ci = t["rowptr"], t["colind"]
+    dt, eps, rho, beta = float(g["dt"]), float(g["eps"]), float(g["rho"]), float(g["beta_s"])
+    brp, bci, bv = O.ch_block(rp, ci, t["M"], t["A"], t["C"], 1 / dt, 1.0, rho, eps * eps, beta)
+    assert np.array_equal(brp, g["B_rowptr"]) and np.array_equal(bci, g["B_colind"]) and np.array_equal(bv, g["B"])
+    st, x, it, res = O.gmres_jacobi(brp, bci, bv, ch_rhs(t, g["chi0"], dt, beta), restart=50, tol=1e-10,
+                                    max_iter=20000, block=True)
+    assert st == O.OK and it == int(g["block_iters"])
+    ok, err = sol_close(x, g["block_x"], 1e-12)
+    assert ok, err
+    m = len(rp) - 1
+    X = np.concatenate([g["chi0"], np.zeros(m)])
+    for k in range(len(g["steps_iters"])):
+        st, X, it, res = O.gmres_jacobi(brp, bci, bv, ch_rhs(t, X[:m], dt, beta), x0=X, restart=50, tol=1e-10,
+                                        max_iter=20000, block=True)
+        assert st == O.OK and abs(it - int(g["steps_iters"][k])) <= 1, (k, it, g["steps_iters"])
+        ok, err = sol_close(X, g["steps_X"][k], 1e-12)
+        assert ok, (k, err)
+
+
+def test_ch_steps_degenerate_mobility_wind_match_reference(golden):
+    """BDF1 steps with LaplaceM_P1P1 reassembled from the current chi (degenerate mobility) and the wind
+    block alpha M + N, against the reference's setupFESystem, block constructor and GMRES."""
+    t, g = golden("torus_p1_n16.npz"), golden("ch_torus_p1_n16.npz")
+    rp, ci = t["rowptr"], t["colind"]
+    m = len(rp) - 1
+    dt, eps, rho, beta = float(g["dt"]), float(g["eps"]), float(g["rho"]), float(g["beta_s"])
+    mesh = O.brick(int(g["n"]), a=float(g["a"]))
+    lv, le = O.levelset(mesh, O.LS_TORUS, [1.0, 0.4, 2], p2=False)
+    st, na, nd, dv, de, act = O.distribute_dofs(mesh, lv, le, False)
+    X = np.concatenate([g["dm_chi0"], np.zeros(m)])
+    for k in range(len(g["dm_steps_iters"])):
+        st, _, _, vals, _ = O.assemble(mesh, lv, le, act, dv, None, m,
+                                       O.make_opts(False, [O.FORM_LAPM], chi=X[:m], degenerate=True))
+        brp, bci, bv = O.ch_block(rp, ci, t["M"], t["A"], t["C"], 1 / dt, 1.0, rho, eps * eps, beta,
+                                  Amob=vals[O.FORM_LAPM], N=t["N"])
+        if k == 0:
+            ok, err = mat_close(bv, g["dm_B0"], g["B_rowptr"], 1e-15)
+            assert ok, err
+        st, X, it, res = O.gmres_jacobi(brp, bci, bv, ch_rhs(t, X[:m], dt, beta), x0=X, restart=50, tol=1e-10,
+                                        max_iter=20000, block=True)
+        assert st == O.OK and abs(it - int(g["dm_steps_iters"][k])) <= 1, (k, it, g["dm_steps_iters"])
+        ok, err = sol_close(X, g["dm_steps_X"][k], 1e-12)
+        assert ok, (k, err)
+
+
 def test_lincomb_matches_reference(golden):
     g = golden("c1_sphere_p1_n16.npz")
     h = 2 * float(g["a"]) / int(g["n"])
-    ok, err = mat_close(g["M"] + g["A"] + h * g["C"], g["S"])
+    ok, err = mat_close(g["M"] + g["A"] + h * g["C"], g["S"], g["rowptr"])
     assert ok, err
 
 
