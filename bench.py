@@ -631,7 +631,9 @@ def ch_cpu_sample(args, threads, budget_s=20.0):
 
 
 # ---------------------------------------------------------------------------
-CPU_THREADING = "DistributeDOFs serial, assembly serial, PCG's SpMV on all host threads (OpenMP)"
+CPU_THREADING = ("OpenMP on all host threads where the reference threads or the work is per tet: the distance test of "
+                 "every tet, the element matrices (accumulated serially in tet order), the pattern's row sorts and "
+                 "PCG's SpMV; serial as in the reference: first-touch DOF numbering, PCG's dots and vector updates")
 
 
 def cpu_workload(threads, N=N_CUBES):

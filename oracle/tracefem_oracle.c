@@ -178,14 +178,23 @@ int orc_distribute_dofs(int64_t nt, const int32_t* tet_v, const int32_t* tet_e, 
     for (int64_t v = 0; v < nv; ++v) dof_vert[v] = -1;
     if (p2)
         for (int64_t e = 0; e < ne; ++e) dof_edge[e] = -1;
-    int64_t na = 0, block = 0;
+    /* the distance test of every tet on all threads (independent per tet);
+       the first-touch numbering below stays serial in tet order, as the
+       reference's */
+    const int nth = g_threads > 0 ? g_threads : omp_get_max_threads();
+    int zero = 0;
+#pragma omp parallel for num_threads(nth) schedule(static) reduction(| : zero)
     for (int64_t t = 0; t < nt; ++t) {
         double f[10];
         gather_ls10(tet_v + 4 * t, tet_e + 6 * t, ls_vert, ls_edge, f);
-        double d = tet_distance(f, 10);
-        if (d < 0.) return ORC_ERR_ZERO_NODE;
-        active[t] = 0;
-        if (d <= dist) {
+        const double d = tet_distance(f, 10);
+        zero |= d < 0.;
+        active[t] = d >= 0. && d <= dist;
+    }
+    if (zero) return ORC_ERR_ZERO_NODE;
+    int64_t na = 0, block = 0;
+    for (int64_t t = 0; t < nt; ++t) {
+        if (active[t]) {
             ++na;
             active[t] = 1;
             for (int i = 0; i < 4; ++i) {
@@ -597,17 +606,21 @@ int orc_assemble(int64_t nt, const int32_t* tet_v, const int32_t* tet_e, const d
         for (int i = 0; i < nl; ++i)
             for (int j = 0; j < nl; ++j) tmp[fill[I[i]]++] = I[j];
     }
+    const int nth = g_threads > 0 ? g_threads : omp_get_max_threads();
     rowptr[0] = 0;
+#pragma omp parallel for num_threads(nth) schedule(dynamic, 256)
     for (int64_t r = 0; r < m; ++r) {
         int64_t b = cnt[r], e = cnt[r + 1];
         qsort(tmp + b, (size_t)(e - b), sizeof(int32_t), cmp_i32);
         int64_t u = 0;
         for (int64_t k = b; k < e; ++k)
             if (k == b || tmp[k] != tmp[k - 1]) ++u;
-        rowptr[r + 1] = rowptr[r] + u;
+        rowptr[r + 1] = u;
     }
+    for (int64_t r = 0; r < m; ++r) rowptr[r + 1] += rowptr[r];
     int64_t nnz = rowptr[m];
     int32_t* colind = (int32_t*)malloc(sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1));
+#pragma omp parallel for num_threads(nth) schedule(static)
     for (int64_t r = 0; r < m; ++r) {
         int64_t b = cnt[r], e = cnt[r + 1], w = rowptr[r];
         for (int64_t k = b; k < e; ++k)
@@ -622,9 +635,27 @@ int orc_assemble(int64_t nt, const int32_t* tet_v, const int32_t* tet_e, const d
     }
     if (rhs)
         for (int64_t r = 0; r < m; ++r) rhs[r] = 0.;
-    /* values: element loop in triangulation order (serial accumulate) */
-    for (int64_t t = 0; t < nt; ++t) {
-        if (!active[t]) continue;
+    /* values: the element matrices of all active tets on all threads (each
+       depends on its tet only, like the reference's colour-class loop,
+       num/accumulator.h:161-190), then accumulated serially in triangulation
+       order, so the sums do not depend on the thread count */
+    int64_t na = 0;
+    for (int64_t t = 0; t < nt; ++t) na += active[t] != 0;
+    int64_t* tl = (int64_t*)malloc(sizeof(int64_t) * (size_t)(na > 0 ? na : 1));
+    na = 0;
+    for (int64_t t = 0; t < nt; ++t)
+        if (active[t]) tl[na++] = t;
+    int fl[ORC_NUM_MAT_FORMS], nfl = 0;
+    for (int f = 0; f < ORC_NUM_MAT_FORMS; ++f)
+        if (vals[f]) fl[nfl++] = f;
+    const int64_t stride = (int64_t)nfl * nl * nl + nl;
+    double* E = (double*)malloc(sizeof(double) * (size_t)(na > 0 ? na * stride : 1));
+    int64_t err_at = na;
+    int err_st = 0;
+    init_quad();
+#pragma omp parallel for num_threads(nth) schedule(dynamic, 64)
+    for (int64_t q = 0; q < na; ++q) {
+        const int64_t t = tl[q];
         int32_t I[10];
         tet_dofs(tet_v + 4 * t, tet_e + 6 * t, dof_vert, dof_edge, o->p2, I);
         double xv[4][3], ls10[10];
@@ -643,20 +674,40 @@ int orc_assemble(int64_t nt, const int32_t* tet_v, const int32_t* tet_e, const d
         }
         int st = orc_local_forms(xv, ls10, o, o->chi ? chi_loc : NULL, haveW ? wind_loc : NULL, loc, b, NULL);
         if (st) {
-            free(colind);
-            for (int f = 0; f < ORC_NUM_MAT_FORMS; ++f) { free(vals[f]); vals[f] = NULL; }
-            return st;
+#pragma omp critical(orc_assemble_err)
+            if (q < err_at) {
+                err_at = q;
+                err_st = st;
+            }
+            continue;
         }
+        double* e = E + q * stride;
+        for (int k = 0; k < nfl; ++k) memcpy(e + (int64_t)k * nl * nl, loc[fl[k]], sizeof(double) * nl * nl);
+        memcpy(e + (int64_t)nfl * nl * nl, b, sizeof(double) * nl);
+    }
+    if (err_at < na) {
+        free(E);
+        free(tl);
+        free(colind);
+        for (int f = 0; f < ORC_NUM_MAT_FORMS; ++f) { free(vals[f]); vals[f] = NULL; }
+        return err_st;
+    }
+    for (int64_t q = 0; q < na; ++q) {
+        const int64_t t = tl[q];
+        int32_t I[10];
+        tet_dofs(tet_v + 4 * t, tet_e + 6 * t, dof_vert, dof_edge, o->p2, I);
+        const double* e = E + q * stride;
         for (int i = 0; i < nl; ++i) {
             int32_t r = I[i];
             for (int j = 0; j < nl; ++j) {
                 int64_t pos = find_col(colind, rowptr[r], rowptr[r + 1], I[j]);
-                for (int f = 0; f < ORC_NUM_MAT_FORMS; ++f)
-                    if (vals[f]) vals[f][pos] += loc[f][i * nl + j];
+                for (int k = 0; k < nfl; ++k) vals[fl[k]][pos] += e[(int64_t)k * nl * nl + i * nl + j];
             }
-            if (rhs && o->rhs_kind != ORC_RHS_NONE) rhs[r] += b[i];
+            if (rhs && o->rhs_kind != ORC_RHS_NONE) rhs[r] += e[(int64_t)nfl * nl * nl + i];
         }
     }
+    free(E);
+    free(tl);
     *colind_out = colind;
     *nnz_out = nnz;
     return ORC_OK;
