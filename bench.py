@@ -246,15 +246,28 @@ def run_ours(args, rank, ws, dist):
     e2e_total = all_max(dist, sum(e2e_ms))
     e2e_value = all_sum(dist, e2e_cut) / (e2e_total / 1e3)
 
-    # ---- mixed vs plain FP64 solve time on the same system ----------------
+    # ---- solve time on the same system: FP64 with the reference's recurrences (two grid barriers per
+    # iteration), FP64 on the single-barrier resident kernel, mixed precision (the benchmark's solver) -----
     solve = {}
-    for prec, name in ((tf.PREC_FP64, "fp64"), (tf.PREC_MIXED, "mixed")):
-        ctx.vec_fill(tf.VEC_X, state["m"], 0.0)
-        ctx.flush_l2()
-        ctx.marker(4)
-        st, it, res = ctx.pcg_jacobi(tf.MAT_SYS, tf.VEC_RHS, tf.VEC_X, tol=TOL, precision=prec)
-        ctx.marker(5)
-        solve[name] = {"ms": ctx.elapsed_ms(4, 5), "iters": it, "resid": res}
+    for prec, k64, name in ((tf.PREC_FP64, tf.PCG_FP64_CLASSIC, "fp64"), (tf.PREC_FP64, tf.PCG_FP64_CG1, "fp64_cg1"),
+                            (tf.PREC_MIXED, tf.PCG_FP64_CLASSIC, "mixed")):
+        ctx.pcg_options(k64)
+        ts = []
+        for rep in range(3):
+            ctx.vec_fill(tf.VEC_X, state["m"], 0.0)
+            ctx.flush_l2()
+            ctx.marker(4)
+            st, it, res = ctx.pcg_jacobi(tf.MAT_SYS, tf.VEC_RHS, tf.VEC_X, tol=TOL, precision=prec)
+            ctx.marker(5)
+            ts.append(ctx.elapsed_ms(4, 5))
+        solve[name] = {"ms": round(statistics.median(ts), 4), "iters": it, "resid": res,
+                       "us_per_iter": round(1e3 * statistics.median(ts) / max(it, 1), 3)}
+    ctx.pcg_options(tf.PCG_FP64_CLASSIC)
+    solve["note"] = ("median of 3 solves from x = 0, L2 flushed before each; fp64: PCGSolverCL's recurrences "
+                     "(two grid barriers per iteration); fp64_cg1: the single-barrier form of the mixed solver in "
+                     "FP64; mixed: FP32 iterations in FP64 refinement (the benchmark's solver)")
+    solve["mixed_vs_fp64"] = round(solve["fp64"]["ms"] / solve["mixed"]["ms"], 3)
+    solve["mixed_vs_fp64_cg1"] = round(solve["fp64_cg1"]["ms"] / solve["mixed"]["ms"], 3)
 
     # ---- standalone FP64 SpMV (y_Ax) on the system matrix, cold L2 ---------
     spmv = spmv_cold(ctx, tf, state["m"], state["nnz"])

@@ -36,6 +36,7 @@ RHS_NONE, RHS_SPHERE_XYZ, RHS_CONST = range(3)
 PREC_FP64, PREC_MIXED = 0, 1
 ORTH_MGS, ORTH_CGS2 = 0, 1
 SPMV_KERNEL_FP64, SPMV_KERNEL_PAIR = 0, 1  # tf_spmv_options
+PCG_FP64_CLASSIC, PCG_FP64_CG1 = 0, 1  # tf_pcg_options
 MLP_IN, MLP_WEIGHTS = 80, 16640
 K_CLASSIFY, K_NUMBER, K_ASSEMBLE, K_PATTERN, K_SCATTER, K_SPMV, K_PCG, K_GMRES, K_LEVELSET, K_BATCH = range(10)
 KERNEL_NAMES = ["classify", "number", "assemble", "pattern", "scatter", "spmv", "pcg", "gmres", "levelset", "batch"]
@@ -49,7 +50,7 @@ EXPORTS = [
     "tf_vec_download", "tf_vec_size", "tf_vec_fill", "tf_spmv", "tf_spmv_options", "tf_pcg_jacobi", "tf_gmres_jacobi", "tf_pcg_jacobi_noalloc", "tf_ch_steps",
     "tf_mesh_brick_batch", "tf_levelset_analytic_batch", "tf_batch_info", "tf_batch_lincomb", "tf_batch_pcg_jacobi",
     "tf_batch_tune", "tf_batch_config", "tf_mlp_init", "tf_mlp_get_weights", "tf_mlp_set_weights", "tf_mlp_forward",
-    "tf_mlp_gradient", "tf_mlp_train", "tf_ch_features", "tf_ch_steps_learned", "tf_gmres_options", "tf_timing_enable",
+    "tf_mlp_gradient", "tf_mlp_train", "tf_ch_features", "tf_ch_steps_learned", "tf_gmres_options", "tf_pcg_options", "tf_timing_enable",
     "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2", "tf_spmv_timed", "tf_stream_read_timed", "tf_wind_upload", "tf_vec_write", "tf_vec_read", "tf_ch_stats", "tf_ch_steps_adaptive", "tf_ch_options",
     "tf_host_alloc", "tf_host_free",
 ]
@@ -468,6 +469,9 @@ class TraceFEM:
     def spmv_options(self, kernel=SPMV_KERNEL_FP64):
         """Kernel of tf_spmv: SPMV_KERNEL_FP64 (default) or SPMV_KERNEL_PAIR (FP32 pairs)."""
         self._check(self.L.tf_spmv_options(self.h, C.c_int(kernel)))
+
+    def pcg_options(self, fp64_kernel=PCG_FP64_CLASSIC):
+        self._check(self.L.tf_pcg_options(self.h, C.c_int(fp64_kernel)))
 
     def gmres_options(self, orth=ORTH_MGS):
         self._check(self.L.tf_gmres_options(self.h, C.c_int(orth)))

@@ -110,6 +110,8 @@ int tf_create(tf_context** out, int device) {
     if (const char* e = std::getenv("TF_PCG_SMEM_CACHE_KB")) c->pcg_smem_cache_kb = std::atoi(e);
     if (const char* e = std::getenv("TF_SPMV_THREADS")) c->spmv_threads = std::atoi(e);
     if (const char* e = std::getenv("TF_GMRES2_MASTER")) c->gmres2_master = std::atoi(e) != 0;
+    if (const char* e = std::getenv("TF_PCG_RESIDENT")) c->pcg_resident = std::atoi(e) != 0;
+    if (const char* e = std::getenv("TF_PCG_RES_VCAP_KB")) c->pcg_res_vcap_kb = std::atoi(e);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
         cudaMallocHost((void**)&c->h_status, 4 * sizeof(int)) != cudaSuccess ||
@@ -906,6 +908,14 @@ int tf_spmv_options(tf_context* t, int kernel) {
     if (kernel != TF_SPMV_KERNEL_FP64 && kernel != TF_SPMV_KERNEL_PAIR)
         return tf::set_err(&t->c, TF_ERR_BAD_INPUT, "spmv_options: kernel");
     t->c.spmv_pair = kernel == TF_SPMV_KERNEL_PAIR;
+    return TF_OK;
+}
+
+int tf_pcg_options(tf_context* t, int fp64_kernel) {
+    CTX_CHECK(t);
+    if (fp64_kernel != TF_PCG_FP64_CLASSIC && fp64_kernel != TF_PCG_FP64_CG1)
+        return tf::set_err(&t->c, TF_ERR_BAD_INPUT, "pcg_options: fp64_kernel");
+    t->c.pcg_fp64_kernel = fp64_kernel;
     return TF_OK;
 }
 

@@ -1385,6 +1385,11 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
     const int64_t m = A.m;
     TimedLaunch tl(c, TF_K_PCG);
     if (precision == TF_PREC_FP64) {
+        if (c->pcg_fp64_kernel == TF_PCG_FP64_CG1) {
+            bool applied = false;
+            const int st = pcg_resident<double>(c, A, b, x, max_iter, tol, rel, &applied);
+            if (applied || st != TF_OK) return st;
+        }
         TF_TRY(ensure(c, c->kry64, (size_t)(5 * m)));
         int it = 0;
         double res = 0.;
@@ -1396,6 +1401,11 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
     }
     // mixed precision: FP32 iterations, FP64 iterate and reliable updates
     TF_TRY(ensure_sell(c, A, false));  // FP64 copy for the refinement residuals
+    if (!c->pcg_two_barrier && c->pcg_resident) {
+        bool applied = false;
+        const int st = pcg_resident<float>(c, A, b, x, max_iter, tol, rel, &applied);
+        if (applied || st != TF_OK) return st;
+    }
     if (!c->pcg_two_barrier) return run_pcg_cg1(c, A, b, x, max_iter, tol, rel);
     TF_TRY(ensure(c, c->kry32, (size_t)(6 * m)));
     float* d32 = c->kry32.p;

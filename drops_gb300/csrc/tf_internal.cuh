@@ -196,6 +196,16 @@ struct Sell {
     int32_t* rexp = nullptr; // nslices*32: row scale exponent (value = (hi + lo) * 2^rexp)
     int64_t pattern_gen = -1, v64_version = -1, v32_version = -1, v2f_version = -1;
     bool v2f_ok = false;     // every value finite (else the pair form is not used)
+    // resident PCG (krylov_res.cu): row -> slot map, columns translated to the
+    // owning block's vector, per-block halo lists, sizes of the largest run
+    int32_t* iperm = nullptr;
+    int64_t iperm_gen = -1;
+    uint16_t* col_tr = nullptr;
+    int32_t* halo_rows = nullptr;  // [block][halo capacity]
+    int32_t* halo_n = nullptr;     // [block]
+    int res_blocks = 0, res_smax = 0, res_hmax = 0;
+    int32_t res_maxslots = 0;
+    bool res_ok = false;
 };
 
 struct CSR {
@@ -286,6 +296,11 @@ struct Context {
     DBuf<float> sell_v32[TF_NUM_MATS];
     DBuf<float2> sell_v2f[TF_NUM_MATS];
     DBuf<int32_t> sell_rexp[TF_NUM_MATS];
+    DBuf<int32_t> sell_iperm[TF_NUM_MATS], sell_halo[TF_NUM_MATS];
+    DBuf<uint16_t> sell_coltr[TF_NUM_MATS];
+    bool pcg_resident = true;   // PCG: block share of the system resident in shared memory where it fits
+    int pcg_fp64_kernel = 0;    // TF_PCG_FP64_CLASSIC or TF_PCG_FP64_CG1
+    int pcg_res_vcap_kb = -1;   // resident PCG: cap on the KB of matrix values kept in shared memory (-1: none)
     DBuf<float2> x_pairs;       // SpMV operand split into FP32 pairs
     bool spmv_pair = false;     // tf_spmv: FP32-pair kernel instead of the FP64-FMA one
     bool spmv_sell = false;     // tf_spmv: one warp per slice instead of the balanced kernel
@@ -423,6 +438,8 @@ int ch_loop_begin(Context* c);
 int ch_step_block(Context* c, double alpha, double mob, double rho, double eps2, double beta);
 int spmv(Context* c, const CSR& A, const double* x, double* y);
 int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, int* max_iter, double* tol, int rel);
+template <class T>
+int pcg_resident(Context* c, CSR& A, const double* b, double* x, int* max_iter, double* tol, int rel, bool* applied);
 int gmres_jacobi(Context* c, CSR& A, const double* b, double* x, int restart, int method, int precision,
                  int* max_iter, double* tol, int rel);
 int ensure_diag(Context* c, CSR& A);

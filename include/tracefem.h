@@ -248,6 +248,17 @@ int tf_spmv_options(tf_context* ctx, int kernel);
  * residual.  Returns TF_ERR_NOT_CONVERGED where the reference returns false.  */
 int tf_pcg_jacobi(tf_context* ctx, int mat, int vec_b, int vec_x, int precision, int* max_iter, double* tol,
                   int rel);
+/* FP64 kernel of tf_pcg_jacobi (TF_PREC_FP64).  No counterpart in the
+ * reference, which has one PCG.  TF_PCG_FP64_CLASSIC (default) runs
+ * PCGSolverCL's recurrences with two grid barriers per iteration (iteration
+ * counts as the reference's).  TF_PCG_FP64_CG1 runs the single-barrier
+ * Chronopoulos-Gear form of the mixed solver in FP64, with each block's share
+ * of the system resident in shared memory where it fits (else the classic
+ * kernel); it stops on the recursive residual and confirms convergence on the
+ * true residual b - A x.                                                       */
+#define TF_PCG_FP64_CLASSIC 0
+#define TF_PCG_FP64_CG1 1
+int tf_pcg_options(tf_context* ctx, int fp64_kernel);
 /* GMResSolverCL / GMRES (num/krylovsolver.h:320-463, 1924-1975): restarted
  * GMRES(restart) with modified Gram-Schmidt and Givens rotations, Jacobi
  * preconditioning of the diagonal (for TF_MAT_BLOCK: of both diagonal blocks),

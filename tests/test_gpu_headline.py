@@ -8,8 +8,9 @@ to relative residual 1e-10.  Checked:
   - M, A, C_n per entry within 1e-12 of their row's scale and the load vector
     within 1e-12 of its largest entry (tests/helpers.py), with the worst plain
     per-entry relative error printed beside;
-  - the mixed-precision and the FP64 PCG solutions within 1e-9 of the oracle's
-    FP64 PCG solution, and the oracle's FP64 residual of each GPU solution.
+  - the mixed-precision, the FP64 and the FP64 single-barrier PCG solutions
+    within 1e-9 of the oracle's FP64 PCG solution, and the oracle's FP64
+    residual of each GPU solution.
 The oracle (C restatement of the reference, pinned to the reference's own
 outputs by tests/test_oracle_golden.py) takes a few seconds on this size.
 """
@@ -43,11 +44,14 @@ def test_p2_sphere96_against_oracle():
         mats = {f: ctx.matrix(f) for f in forms}
         rhs = ctx.vec_download(tf.VEC_RHS)
         xs = {}
-        for prec in (tf.PREC_MIXED, tf.PREC_FP64):
+        for key, prec, k64 in (("mixed", tf.PREC_MIXED, tf.PCG_FP64_CLASSIC), ("fp64", tf.PREC_FP64, tf.PCG_FP64_CLASSIC),
+                               ("fp64_cg1", tf.PREC_FP64, tf.PCG_FP64_CG1)):
+            ctx.pcg_options(k64)
             ctx.vec_fill(tf.VEC_X, m, 0.0)
             st, it, res = ctx.pcg_jacobi(tf.MAT_SYS, tf.VEC_RHS, tf.VEC_X, tol=1e-10, precision=prec)
-            assert st == tf.OK and res <= 1e-10, (prec, st, res)
-            xs[prec] = ctx.vec_download(tf.VEC_X)
+            assert st == tf.OK and res <= 1e-10, (key, st, res)
+            xs[key] = ctx.vec_download(tf.VEC_X)
+        ctx.pcg_options(tf.PCG_FP64_CLASSIC)
 
     O.set_threads(0)
     mesh = O.brick(N, a=HALF)
@@ -74,8 +78,7 @@ def test_p2_sphere96_against_oracle():
     S = vals[O.FORM_M] + vals[O.FORM_A] + h * vals[O.FORM_CN]
     st, ox, oit, ores = O.pcg_jacobi(orp, oci, S, orhs, tol=1e-10)
     assert st == O.OK
-    for prec, name in ((tf.PREC_MIXED, "mixed"), (tf.PREC_FP64, "fp64")):
-        x = xs[prec]
+    for name, x in xs.items():
         r = np.linalg.norm(orhs - O.spmv(orp, oci, S, x)) / np.linalg.norm(orhs)
         ok, err = sol_close(x, ox)
         report[f"x_{name}"] = (err, r)
