@@ -485,7 +485,7 @@ class TraceFEM:
         st = self.L.tf_ch_steps_learned(self.h, C.c_int(nsteps), C.c_double(dt), C.c_double(mobility),
                                         C.c_double(eps), C.c_double(beta_s), C.c_double(xi), C.c_double(rho_vol),
                                         C.c_int(restart), C.c_double(tol), C.c_int(max_iter), C.c_int(precision),
-                                        C.c_int(int(learned)),  # 0 plain, 1 MLP, 2 extrapolation
+                                        C.c_int(int(learned)),  # 0 plain, 1 projection + MLP, 2 extrapolation, 3 projection
                                         C.c_int(train_steps), C.c_int(epochs), C.c_int(minibatch_tiles),
                                         C.c_float(lr), _ip(its), _dp(res), _ip(used))
         if check:

@@ -934,7 +934,7 @@ int tf_ch_steps_learned(tf_context* t, int nsteps, double dt, double mobility, d
     Context* c = &t->c;
     cudaSetDevice(c->device);
     if (restart < 2 || max_iter < 1 || tol <= 0. || epochs < 0 || minibatch_tiles < 1 || lr < 0.f ||
-        (precision != TF_PREC_FP64 && precision != TF_PREC_MIXED) || learned < 0 || learned > 2)
+        (precision != TF_PREC_FP64 && precision != TF_PREC_MIXED) || learned < 0 || learned > 3)
         return tf::set_err(c, TF_ERR_BAD_INPUT, "ch_steps_learned: bad arguments");
     tf::ChLearnParams P;
     P.nsteps = nsteps;

@@ -20,10 +20,24 @@
 // and the guess is x_n + (x_n - x_{n-1}) + s * prediction, so an untrained
 // network (prediction ~ 0) already gives the extrapolated state.
 //
+// Minimal-residual projection.  A restarted GMRES(50) solve to 1e-10 gains
+// only a little from a better start, and a correction of linear
+// extrapolation gains nothing unless it is very accurate.  The guess of
+// learned = 1 is therefore the combination of the recent states and the
+// network's correction that minimises the FP64 residual: with the backward
+// differences D_0 = x_n, D_1 = x_n - x_{n-1}, ... of the last kProjStates
+// states and the correction vector s * prediction as basis V, it solves
+// min_c ||b - A V c|| (the Gram matrix of A V in FP64, scaled by its
+// diagonal and solved by a truncated eigen-decomposition on the host) and
+// starts from V c.  learned = 3 is the same projection without the network,
+// so the network's own contribution is the difference between the two.
+// Both contain x_n and the extrapolated state in their span, so neither
+// starts from a larger residual than the previous state or extrapolation.
+//
 // Guard: the learned guess is used only when its FP64 residual is smaller
 // than the previous-step guess's, and after a step whose learned solve took
-// more GMRES iterations than the last plain solve the next step falls back to
-// the previous-step guess.
+// more than 5/4 of the GMRES iterations of the last plain solve the next step
+// falls back to the previous-step guess.
 //
 // Compiled without contraction (like the mesh code), so features equal a host
 // restatement in IEEE double bit for bit.
@@ -150,6 +164,70 @@ __global__ void k_ch_apply(int64_t m, const double* __restrict__ xn, const doubl
     }
 }
 
+constexpr int kProjStates = 6;  // states of the projection basis (backward differences)
+constexpr int kProjMax = kProjStates + 1;
+
+// backward differences of the ring of states (newest first): D_j = sum_k (-1)^k C(j,k) s_k
+struct RingPtrs {
+    const double* s[kProjStates];
+    double* d[kProjStates];
+};
+__global__ void k_ch_diffs(int64_t n, int ns, RingPtrs R) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double t[kProjStates];
+        for (int k = 0; k < ns; ++k) t[k] = R.s[k][i];
+        // difference table: after level j, t[0] holds D_j
+        for (int j = 0; j < ns; ++j) {
+            R.d[j][i] = t[0];
+            for (int k = 0; k + 1 < ns - j; ++k) t[k] = t[k] - t[k + 1];
+        }
+    }
+}
+
+// all products <y_j, y_k> (j <= k) and <y_j, b> of nv vectors, per block (blockIdx.y = product)
+struct DotPtrs {
+    const double* a[kProjMax * (kProjMax + 1) / 2 + kProjMax];
+    const double* b[kProjMax * (kProjMax + 1) / 2 + kProjMax];
+};
+__global__ void k_ch_dots(int64_t n, DotPtrs P, double* __restrict__ part) {
+    __shared__ double sh[32];
+    const double* __restrict__ a = P.a[blockIdx.y];
+    const double* __restrict__ b = P.b[blockIdx.y];
+    double s = 0.;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s += a[i] * b[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double v = 0.;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += sh[w];
+        part[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = v;
+    }
+}
+
+// guess = sum_j c_j V_j
+struct CombPtrs {
+    const double* v[kProjMax];
+    double c[kProjMax];
+};
+__global__ void k_ch_combine(int64_t n, int nv, CombPtrs C, double* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double g = 0.;
+        for (int j = 0; j < nv; ++j) g += C.c[j] * C.v[j][i];
+        out[i] = g;
+    }
+}
+
+// correction vector of the network: (s_chi, s_omega) * prediction
+__global__ void k_ch_corr(int64_t m, const float* __restrict__ pred, const double* __restrict__ sc,
+                          double* __restrict__ corr) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 2 * m; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t d = i < m ? i : i - m;
+        corr[i] = sc[i < m ? 0 : 1] * (double)pred[2 * d + (i < m ? 0 : 1)];
+    }
+}
+
 // ||b - A x||^2 into out (one value), fixed order: rows in chunks, one block
 __global__ void k_resid_sq(int64_t m, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
                            const double* __restrict__ val, const double* __restrict__ b, const double* __restrict__ x,
@@ -184,6 +262,100 @@ static int resid_norm(Context* c, const CSR& A, const double* b, const double* x
     double s = 0.;
     for (double v : h) s += v;
     *out = std::sqrt(s);
+    return TF_OK;
+}
+
+// Symmetric eigen-decomposition of a small n x n matrix (cyclic Jacobi
+// rotations); a is overwritten, eigenvalues in w, eigenvectors in the columns of v.
+static void sym_eig(int n, double a[kProjMax][kProjMax], double w[kProjMax], double v[kProjMax][kProjMax]) {
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) v[i][j] = i == j ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        double off = 0.;
+        for (int p = 0; p < n; ++p)
+            for (int q = p + 1; q < n; ++q) off += a[p][q] * a[p][q];
+        if (off < 1e-300) break;
+        for (int p = 0; p < n; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                if (a[p][q] == 0.) continue;
+                const double th = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+                const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+                const double cs = 1.0 / std::sqrt(t * t + 1.0), sn = t * cs;
+                for (int k = 0; k < n; ++k) {
+                    const double akp = a[k][p], akq = a[k][q];
+                    a[k][p] = cs * akp - sn * akq;
+                    a[k][q] = sn * akp + cs * akq;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double apk = a[p][k], aqk = a[q][k];
+                    a[p][k] = cs * apk - sn * aqk;
+                    a[q][k] = sn * apk + cs * aqk;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double vkp = v[k][p], vkq = v[k][q];
+                    v[k][p] = cs * vkp - sn * vkq;
+                    v[k][q] = sn * vkp + cs * vkq;
+                }
+            }
+    }
+    for (int i = 0; i < n; ++i) w[i] = a[i][i];
+}
+
+// guess = V c with c = argmin ||b - A V c|| over the nv basis vectors V (device);
+// scratch ch_av holds A V
+static int ch_project(Context* c, CSR& B, const double* b, const double* const* V, int nv, double* guess) {
+    const int64_t n = B.m;
+    TF_TRY(ensure(c, c->ch_av, (size_t)(kProjMax * n)));
+    for (int j = 0; j < nv; ++j) TF_TRY(spmv(c, B, V[j], c->ch_av.p + (size_t)j * n));
+    DotPtrs P{};
+    int np = 0;
+    int pj[kProjMax * (kProjMax + 1) / 2 + kProjMax], pk[kProjMax * (kProjMax + 1) / 2 + kProjMax];
+    for (int j = 0; j < nv; ++j)
+        for (int k = j; k <= nv; ++k) {  // k == nv: the right-hand side
+            P.a[np] = c->ch_av.p + (size_t)j * n;
+            P.b[np] = k < nv ? c->ch_av.p + (size_t)k * n : b;
+            pj[np] = j;
+            pk[np] = k;
+            ++np;
+        }
+    const int gx = c->num_sms;
+    TF_TRY(ensure(c, c->ch_part, (size_t)(gx * np)));
+    k_ch_dots<<<dim3(gx, np), 256, 0, c->stream>>>(n, P, c->ch_part.p);
+    ++c->launches;
+    TF_CUDA(c, cudaGetLastError());
+    std::vector<double> h((size_t)gx * np);
+    TF_CUDA(c, cudaMemcpyAsync(h.data(), c->ch_part.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    double G[kProjMax][kProjMax] = {}, r[kProjMax] = {};
+    for (int q = 0; q < np; ++q) {
+        double sum = 0.;
+        for (int x = 0; x < gx; ++x) sum += h[(size_t)q * gx + x];
+        if (pk[q] == nv) r[pj[q]] = sum;
+        else G[pj[q]][pk[q]] = G[pk[q]][pj[q]] = sum;
+    }
+    // scale by the diagonal, truncated eigen-solve (directions below 1e-12 of the largest are dropped)
+    double sc[kProjMax], Gs[kProjMax][kProjMax], w[kProjMax], U[kProjMax][kProjMax], cf[kProjMax] = {};
+    for (int j = 0; j < nv; ++j) sc[j] = G[j][j] > 0. ? 1.0 / std::sqrt(G[j][j]) : 0.;
+    for (int j = 0; j < nv; ++j)
+        for (int k = 0; k < nv; ++k) Gs[j][k] = sc[j] * G[j][k] * sc[k];
+    sym_eig(nv, Gs, w, U);
+    double wmax = 0.;
+    for (int j = 0; j < nv; ++j) wmax = std::max(wmax, w[j]);
+    for (int e = 0; e < nv; ++e) {
+        if (!(w[e] > 1e-12 * wmax)) continue;
+        double t = 0.;
+        for (int j = 0; j < nv; ++j) t += U[j][e] * sc[j] * r[j];
+        t /= w[e];
+        for (int j = 0; j < nv; ++j) cf[j] += U[j][e] * t;
+    }
+    CombPtrs Cp{};
+    for (int j = 0; j < nv; ++j) {
+        Cp.v[j] = V[j];
+        Cp.c[j] = cf[j] * sc[j];
+    }
+    k_ch_combine<<<grid_for(c, n), kBlock, 0, c->stream>>>(n, nv, Cp, guess);
+    ++c->launches;
+    TF_CUDA(c, cudaGetLastError());
     return TF_OK;
 }
 
@@ -241,6 +413,20 @@ int ch_steps_learned(Context* c, const ChLearnParams& P, int* iters, double* res
     double* guess = c->ch_hist.p + 2 * m;
     double* x_prev = c->ch_hist.p + 4 * m;  // x_n kept for the targets
     TF_CUDA(c, cudaMemcpyAsync(x_old, c->vecs[TF_VEC_X].p, sizeof(double) * 2 * m, cudaMemcpyDeviceToDevice, c->stream));
+    // projection: ring of the last kProjStates states (slot of state n: n % kProjStates), their
+    // differences and the network's correction vector
+    const bool project = P.learned == 1 || P.learned == 3;
+    int ring_n = 0, ring_head = -1;
+    if (project) {
+        TF_TRY(ensure(c, c->ch_ring, (size_t)(2 * kProjStates + 1) * 2 * m));
+        ring_head = 0;
+        ring_n = 1;
+        TF_CUDA(c, cudaMemcpyAsync(c->ch_ring.p, c->vecs[TF_VEC_X].p, sizeof(double) * 2 * m, cudaMemcpyDeviceToDevice,
+                                   c->stream));
+    }
+    auto ring_state = [&](int k) { return c->ch_ring.p + (size_t)((ring_head - k + kProjStates) % kProjStates) * 2 * m; };
+    double* diffs = project ? c->ch_ring.p + (size_t)kProjStates * 2 * m : nullptr;
+    double* corr = project ? c->ch_ring.p + (size_t)(2 * kProjStates) * 2 * m : nullptr;
     int trained = 0, plain_ref = -1;
     bool fallback_next = false;
     c->ch_train_loss = 0.;
@@ -251,13 +437,33 @@ int ch_steps_learned(Context* c, const ChLearnParams& P, int* iters, double* res
         const bool have_hist = step > 0;
         bool use = false;
         if (have_hist) TF_TRY(ch_features_dev(c, X, x_old, nullptr));
-        const bool mlp_ready = P.learned == 2 || (P.learned == 1 && trained >= P.min_trained);
-        if (have_hist && mlp_ready && !fallback_next) {
-            if (P.learned == 1) TF_TRY(mlp_forward_dev(c, c->ch_X.p, m, c->ch_pred.p));
-            k_ch_apply<<<grid_for(c, 2 * m), kBlock, 0, c->stream>>>(m, X, x_old, P.learned == 1 ? c->ch_pred.p : nullptr,
-                                                                     c->ch_scales.p, guess);
-            ++c->launches;
-            TF_CUDA(c, cudaGetLastError());
+        const bool mlp_ready = P.learned == 1 && trained >= P.min_trained;
+        if (have_hist && !fallback_next && (P.learned == 2 || project)) {
+            if (project) {
+                // basis: differences of the ring (newest first), then the network's correction
+                RingPtrs R{};
+                const double* V[kProjMax];
+                for (int k = 0; k < ring_n; ++k) {
+                    R.s[k] = ring_state(k);
+                    R.d[k] = diffs + (size_t)k * 2 * m;
+                    V[k] = R.d[k];
+                }
+                k_ch_diffs<<<grid_for(c, 2 * m), kBlock, 0, c->stream>>>(2 * m, ring_n, R);
+                ++c->launches;
+                int nv = ring_n;
+                if (mlp_ready) {
+                    TF_TRY(mlp_forward_dev(c, c->ch_X.p, m, c->ch_pred.p));
+                    k_ch_corr<<<grid_for(c, 2 * m), kBlock, 0, c->stream>>>(m, c->ch_pred.p, c->ch_scales.p, corr);
+                    ++c->launches;
+                    V[nv++] = corr;
+                }
+                TF_CUDA(c, cudaGetLastError());
+                TF_TRY(ch_project(c, B, c->vecs[TF_VEC_B].p, V, nv, guess));
+            } else {
+                k_ch_apply<<<grid_for(c, 2 * m), kBlock, 0, c->stream>>>(m, X, x_old, nullptr, c->ch_scales.p, guess);
+                ++c->launches;
+                TF_CUDA(c, cudaGetLastError());
+            }
             double r_plain = 0., r_learn = 0.;
             TF_TRY(resid_norm(c, B, c->vecs[TF_VEC_B].p, X, &r_plain));
             TF_TRY(resid_norm(c, B, c->vecs[TF_VEC_B].p, guess, &r_learn));
@@ -274,9 +480,14 @@ int ch_steps_learned(Context* c, const ChLearnParams& P, int* iters, double* res
         if (used) used[step] = use ? 1 : 0;
         if (st != TF_OK) return st;
         if (use) {
-            if (plain_ref >= 0 && it > plain_ref) fallback_next = true;
+            if (plain_ref >= 0 && 4 * it > 5 * plain_ref) fallback_next = true;
         } else {
             plain_ref = it;
+        }
+        if (project) {  // the new state enters the ring
+            ring_head = (ring_head + 1) % kProjStates;
+            ring_n = std::min(ring_n + 1, kProjStates);
+            TF_CUDA(c, cudaMemcpyAsync(ring_state(0), X, sizeof(double) * 2 * m, cudaMemcpyDeviceToDevice, c->stream));
         }
         // online training on this step's increment
         if (have_hist && P.learned == 1 && step < P.train_steps) {

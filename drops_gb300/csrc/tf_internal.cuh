@@ -339,6 +339,7 @@ struct Context {
     int64_t mlp_step = 0;
     // learned Cahn-Hilliard warm start
     DBuf<double> ch_part, ch_scales, ch_hist;
+    DBuf<double> ch_ring, ch_av;  // learned warm start: recent states, differences, A V of the projection
     DBuf<double> ch_prev, ch_x1, ch_x2;  // adaptive BDF1/BDF2: chi_prev, BDF1 and BDF2 states
     DBuf<float> ch_xyz, ch_nrm, ch_Y, ch_pred;
     DBuf<__nv_bfloat16> ch_X;
@@ -358,7 +359,8 @@ struct ChLearnParams {
     double tol = 1e-10;
     int max_iter = 100000;
     int precision = TF_PREC_FP64;  // TF_PREC_MIXED: FP32 Arnoldi cycles in FP64 refinement
-    int learned = 1;        // 0: previous-step guess (the reference's warm start), 1: MLP, 2: extrapolation only
+    int learned = 1;        // 0: previous-step guess (the reference's warm start), 1: projection with the MLP's
+                            // correction, 2: linear extrapolation, 3: projection without the MLP
     int train_steps = 100;  // online training during the first steps
     int epochs = 2;
     int mb_tiles = 16;      // tiles of 128 DOFs per mini-batch

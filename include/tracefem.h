@@ -420,14 +420,16 @@ int tf_ch_stats(tf_context* ctx, double eps, double xi, double* out);
 /* tf_ch_steps with the learned warm start: the MLP (tf_mlp_init first, or a
  * default initialisation) is trained online with `epochs` Adam passes
  * (minibatch_tiles x 128 DOFs, rate lr) on the increment of each of the first
- * train_steps steps; from its third training step on, the guess of a step is
- * x_n + predicted increment when that guess has the smaller FP64 residual,
- * else the previous state, and a step whose learned solve needed more GMRES
- * iterations than the last plain solve makes the next step use the previous
- * state.  The network predicts the deviation from linear extrapolation, so
- * the guess is x_n + (x_n - x_{n-1}) + predicted correction.  learned = 0
- * gives the plain previous-state warm start, learned = 2 linear extrapolation
- * without the network (same residual guard).  precision as
+ * train_steps steps.  The network predicts the deviation of the next state
+ * from linear extrapolation.  learned = 1: the guess of a step is the
+ * combination of the last 6 states (as backward differences) and, from the
+ * network's third training step on, its predicted correction that minimises
+ * the FP64 residual ||b - A x||; learned = 3: the same projection without the
+ * network; learned = 2: linear extrapolation x_n + (x_n - x_{n-1});
+ * learned = 0: the plain previous-state warm start of the reference.  A guess
+ * is used when its FP64 residual is below the previous state's, and a step
+ * whose guessed solve needed more than 5/4 of the GMRES iterations of the
+ * last plain solve makes the next step use the previous state.  precision as
  * in tf_gmres_jacobi (the orthogonalisation of tf_gmres_options applies to
  * TF_PREC_FP64).  used[nsteps]
  * (may be NULL) flags the steps that started from the learned guess.          */

@@ -132,26 +132,31 @@ def test_ch_features_bitexact(ctx):
 
 
 def test_learned_warm_start_converges_and_gains(ctx):
-    """Same CH run three times: previous-state warm start (the reference's), linear extrapolation, and the
-    MLP correction of it (trained online on steps 1..12).  Every solve reaches the tolerance and the states
-    agree; on the steps where a guess was used it needed fewer GMRES iterations in total than the
-    previous-state guess on the same steps."""
+    """Same CH run four times: previous-state warm start (the reference's), linear extrapolation, the
+    minimal-residual projection onto the last 6 states, and that projection with the MLP's correction
+    added to its basis (trained online on steps 1..12).  Every solve reaches the tolerance and the final
+    states agree.  In total GMRES iterations: learned < extrapolated < previous state, and projected <
+    extrapolated; the learned run stays within 5% of the projection without the network (the network's
+    own contribution, printed)."""
     nd, h = _torus(ctx, 20)
     rng = np.random.default_rng(21)
     x0 = np.concatenate([0.5 + rng.uniform(-0.01, 0.01, nd), np.zeros(nd)])
     args = (24, 1e-3, 1.0, 0.02, 0.0, 1.0, h)
     runs = {}
-    for mode in (0, 2, 1):
+    for mode in (0, 2, 3, 1):
         ctx.mlp_init(3)
         ctx.vec_upload(tf.VEC_X, x0)
         st, its, res, used = ctx.ch_steps_learned(*args, learned=mode, train_steps=12, epochs=3, lr=2e-3)
         assert st == tf.OK and np.all(res <= 1e-10)
         runs[mode] = (its, used.astype(bool), ctx.vec_download(tf.VEC_X))
-        print("mode", mode, "iterations", its.tolist(), "used", used.tolist())
+        print("mode", mode, "iterations", int(its.sum()), its.tolist(), "used", int(used.sum()))
     it_p, used_p, xp = runs[0]
     assert not used_p.any()
-    for mode in (2, 1):
+    for mode in (2, 3, 1):
         its, u, x = runs[mode]
         assert np.linalg.norm(x - xp) <= 1e-6 * np.linalg.norm(xp)
         assert u.sum() >= 3, (mode, u)
-        assert its[u].sum() < it_p[u].sum(), (mode, its[u], it_p[u])
+    tot = {k: int(v[0].sum()) for k, v in runs.items()}
+    assert tot[1] < tot[2] < tot[0], tot
+    assert tot[3] < tot[2], tot
+    assert tot[1] <= 1.05 * tot[3], tot
