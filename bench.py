@@ -570,6 +570,9 @@ def run_ch(args, rank, ws, dist):
                 ("mixed_projected", tf.PREC_MIXED, tf.ORTH_MGS, 3), ("mixed_learned", tf.PREC_MIXED, tf.ORTH_MGS, 1)]
     if args.ch_quick:
         variants = [variants[0], variants[5]]
+    if args.ch_variants:
+        keep = args.ch_variants.split(",")
+        variants = [v for v in variants if v[0] in keep]
     train = min(100, max(args.ch_steps // 3, 4))
     runs = {}
     launches0 = ctx.launch_count()
@@ -595,7 +598,8 @@ def run_ch(args, rank, ws, dist):
     ctx.gmres_options(tf.ORTH_MGS)
     launches = ctx.launch_count() - launches0
     clocks = clk.summary()
-    base, best = runs["fp64_mgs_plain"], runs["mixed_learned"]
+    base = runs.get("fp64_mgs_plain", next(iter(runs.values())))
+    best = runs.get("mixed_learned", next(iter(runs.values())))
     value = steps / (best["ms"] / 1e3)
     ratios = {f"{k}_vs_fp64_mgs_plain": round(base["ms"] / v["ms"], 3) for k, v in runs.items() if k != "fp64_mgs_plain"}
     if "fp64_cgs2_plain" in runs:
@@ -760,7 +764,7 @@ def extra_workloads(args, rank, ws, dist):
                                "roofline", "clocks", "gpu_launches")}
     batch["steps"], batch["warmup"], batch["config"] = a.steps, a.warmup, b["config"]
     c = argparse.Namespace(**vars(args))
-    c.ch_steps, c.ch_quick = args.extra_ch_steps, False
+    c.ch_steps, c.ch_quick, c.ch_variants = args.extra_ch_steps, False, ""
     r = run_ch(c, rank, ws, dist)
     ch = {k: r[k] for k in ("metric", "value", "unit", "ms_per_step", "speedup_vs_plain_fp64", "ratios", "runs",
                             "problem", "clocks", "gpu_launches", "config")}
@@ -784,6 +788,7 @@ def main():
     ap.add_argument("--ch-n", type=int, default=CH_N)
     ap.add_argument("--ch-steps", type=int, default=CH_STEPS)
     ap.add_argument("--ch-quick", action="store_true", help="only the plain FP64 and the mixed + learned runs")
+    ap.add_argument("--ch-variants", default="", help="comma-separated subset of the Cahn-Hilliard variants")
     ap.add_argument("--no-extra", action="store_true",
                     help="poisson only: skip the batch and Cahn-Hilliard runs reported inside the headline line")
     ap.add_argument("--extra-ch-steps", type=int, default=30,

@@ -1,5 +1,6 @@
 // extern "C" entry points of libtracefem (include/tracefem.h).
 #include <cstdio>
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -101,16 +102,35 @@ int tf_create(tf_context** out, int device) {
     c->kry_blocks_per_sm = 2;
     c->kry_threads = 512;  // mixed PCG: one 512-thread block per SM halves the arrivals per grid barrier
     if (const char* e = std::getenv("TF_KRY_BLOCKS_PER_SM")) c->kry_blocks_per_sm = std::atoi(e);
-    if (const char* e = std::getenv("TF_KRY_THREADS")) c->kry_threads = std::atoi(e);
+    if (const char* e = std::getenv("TF_KRY_THREADS")) {
+        c->kry_threads = std::atoi(e);
+        c->pcg_shape_fixed = true;
+    }
     if (const char* e = std::getenv("TF_PCG_TWO_BARRIER")) c->pcg_two_barrier = std::atoi(e) != 0;
     if (const char* e = std::getenv("TF_SPMV_PAIR")) c->spmv_pair = std::atoi(e) != 0;
     if (const char* e = std::getenv("TF_SPMV_SELL")) c->spmv_sell = std::atoi(e) != 0;
-    if (const char* e = std::getenv("TF_SPMV_BLOCKS_PER_SM")) c->spmv_blocks_per_sm = std::atoi(e);
-    if (const char* e = std::getenv("TF_PCG_BLOCKED")) c->pcg_blocked = std::atoi(e) != 0;
-    if (const char* e = std::getenv("TF_PCG_SMEM_CACHE_KB")) c->pcg_smem_cache_kb = std::atoi(e);
-    if (const char* e = std::getenv("TF_SPMV_THREADS")) c->spmv_threads = std::atoi(e);
+    if (const char* e = std::getenv("TF_SPMV_BLOCKS_PER_SM")) {
+        c->spmv_blocks_per_sm = std::atoi(e);
+        c->spmv_shape_fixed = true;
+    }
+    if (const char* e = std::getenv("TF_PCG_BLOCKED")) {
+        c->pcg_blocked = std::atoi(e) != 0;
+        c->pcg_shape_fixed = true;
+    }
+    if (const char* e = std::getenv("TF_PCG_SMEM_CACHE_KB")) {
+        c->pcg_smem_cache_kb = std::atoi(e);
+        c->pcg_shape_fixed = true;
+    }
+    if (const char* e = std::getenv("TF_SPMV_THREADS")) {
+        c->spmv_threads = std::atoi(e);
+        c->spmv_shape_fixed = true;
+    }
+    if (const char* e = std::getenv("TF_AUTOTUNE")) c->autotune = std::atoi(e) != 0;
     if (const char* e = std::getenv("TF_GMRES2_MASTER")) c->gmres2_master = std::atoi(e) != 0;
-    if (const char* e = std::getenv("TF_PCG_RESIDENT")) c->pcg_resident = std::atoi(e) != 0;
+    if (const char* e = std::getenv("TF_PCG_RESIDENT")) {
+        c->pcg_resident = std::atoi(e) != 0;
+        c->pcg_shape_fixed = true;
+    }
     if (const char* e = std::getenv("TF_PCG_RES_VCAP_KB")) c->pcg_res_vcap_kb = std::atoi(e);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
@@ -224,6 +244,8 @@ int tf_destroy(tf_context* t) {
     for (auto& e : c->markers)
         if (e) cudaEventDestroy(e);
     if (c->h_status) cudaFreeHost(c->h_status);
+    for (auto& e : c->tune_ev)
+        if (e) cudaEventDestroy(e);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -909,6 +931,30 @@ int tf_spmv_options(tf_context* t, int kernel) {
         return tf::set_err(&t->c, TF_ERR_BAD_INPUT, "spmv_options: kernel");
     t->c.spmv_pair = kernel == TF_SPMV_KERNEL_PAIR;
     return TF_OK;
+}
+
+int tf_autotune(tf_context* t, int on) {
+    CTX_CHECK(t);
+    t->c.autotune = on != 0;
+    return TF_OK;
+}
+
+int tf_autotune_info(tf_context* t, int mat, int* spmv_threads, int* spmv_blocks_per_sm, int* pcg_kind,
+                     float* spmv_us, float* pcg_us) {
+    CTX_CHECK(t);
+    tf::Context* c = &t->c;
+    if (mat < 0 || mat >= TF_NUM_MATS) return tf::set_err(c, TF_ERR_BAD_INPUT, "autotune_info: matrix handle");
+    const tf::CSR& A = c->mats[mat];
+    for (const auto& e : c->tuned)
+        if (e.m == A.m && e.nnz == A.nnz && e.npad == A.sell.npad) {
+            if (spmv_threads) *spmv_threads = e.spmv_threads;
+            if (spmv_blocks_per_sm) *spmv_blocks_per_sm = e.spmv_per_sm;
+            if (pcg_kind) *pcg_kind = e.pcg_kind;
+            if (spmv_us) std::copy(e.spmv_us, e.spmv_us + 4, spmv_us);
+            if (pcg_us) std::copy(e.pcg_us, e.pcg_us + 3, pcg_us);
+            return TF_OK;
+        }
+    return tf::set_err(c, TF_ERR_BAD_INPUT, "autotune_info: the matrix has not been tuned");
 }
 
 int tf_pcg_options(tf_context* t, int fp64_kernel) {

@@ -209,13 +209,12 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_spmv_bal(int64_t nslices, con
             });
 }
 
-static void launch_spmv_bal(Context* c, const CSR& A, const double* x, double* y) {
+void launch_spmv_shape(Context* c, const CSR& A, const double* x, double* y, int threads, int per_sm) {
     const int64_t ns = A.sell.nslices;
-    const int per_sm = c->spmv_blocks_per_sm > 0 ? c->spmv_blocks_per_sm : 2;
     int64_t nb = (int64_t)c->num_sms * per_sm;
     if (nb > ns) nb = ns;
     if (nb < 1) nb = 1;
-    if (c->spmv_threads == 256)
+    if (threads == 256)
         k_spmv_bal<256><<<(unsigned)nb, 256, 0, c->stream>>>(ns, A.sell.perm, A.sell.ptr, A.sell.col, A.sell.v64, x, y);
     else
         k_spmv_bal<512><<<(unsigned)nb, 512, 0, c->stream>>>(ns, A.sell.perm, A.sell.ptr, A.sell.col, A.sell.v64, x, y);
@@ -445,9 +444,11 @@ int spmv(Context* c, const CSR& Ac, const double* x, double* y) {
     }
     const bool pair = c->spmv_pair;
     if (pair) TF_TRY(ensure_sell_pair(c, A));
+    int threads = c->spmv_threads == 256 ? 256 : 512, per_sm = c->spmv_blocks_per_sm > 0 ? c->spmv_blocks_per_sm : 2;
+    if (!pair && c->autotune && !c->spmv_shape_fixed) TF_TRY(tuned_spmv_shape(c, A, &threads, &per_sm));
     TimedLaunch tl(c, TF_K_SPMV);
     if (!pair || !A.sell.v2f_ok) {
-        launch_spmv_bal(c, A, x, y);
+        launch_spmv_shape(c, A, x, y, threads, per_sm);
     } else {
         TF_TRY(ensure(c, c->x_pairs, (size_t)(A.m > 0 ? A.m : 1)));
         TF_CUDA(c, cudaMemsetAsync(c->status.p + 2, 0, sizeof(int), c->stream));
@@ -1299,14 +1300,14 @@ static int run_pcg_kernel(Context* c, const CSR& A, const T* val, const T* diag,
 
 // single-barrier mixed PCG (k_pcg_cg1); workspace in floats: V0, V1 (4m each,
 // 16-byte aligned), p, dx, FP32 diagonal
-static int run_pcg_cg1(Context* c, const CSR& A, const double* b, double* x, int* max_iter, double* tol, int rel) {
+static int run_pcg_cg1(Context* c, const CSR& A, const double* b, double* x, int* max_iter, double* tol, int rel,
+                       int nt) {
     const int64_t m = A.m;
     TF_TRY(ensure(c, c->kry32, (size_t)(11 * m)));
     float* base = c->kry32.p;
     float* d32 = base + 10 * m;
     k_to_f32<<<grid_for(c, m), kBlock, 0, c->stream>>>(m, A.diag, d32);
     ++c->launches;
-    const int nt = c->kry_threads == 512 ? 512 : 256;
     const void* fn = c->pcg_blocked ? (nt == 512 ? (const void*)k_pcg_cg1<512, true> : (const void*)k_pcg_cg1<256, true>)
                                     : (nt == 512 ? (const void*)k_pcg_cg1<512, false> : (const void*)k_pcg_cg1<256, false>);
     // dynamic shared memory for the matrix cache: what the opt-in limit leaves
@@ -1378,6 +1379,17 @@ static int run_pcg_cg1(Context* c, const CSR& A, const double* b, double* x, int
     return it[0] >= 0 ? TF_OK : set_err(c, TF_ERR_NOT_CONVERGED, "pcg (mixed): no convergence within max_iter");
 }
 
+// the single-barrier mixed solver of the given kind (the resident kernel falls
+// back to the 512-thread k_pcg_cg1 where the block runs do not fit)
+int pcg_mixed_kind(Context* c, CSR& A, const double* b, double* x, int kind, int* max_iter, double* tol, int rel) {
+    if (kind == kPcgResident) {
+        bool applied = false;
+        const int st = pcg_resident<float>(c, A, b, x, max_iter, tol, rel, &applied);
+        if (applied || st != TF_OK) return st;
+    }
+    return run_pcg_cg1(c, A, b, x, max_iter, tol, rel, kind == kPcgCg1_256 ? 256 : 512);
+}
+
 int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, int* max_iter, double* tol, int rel) {
     if (!A.vals || A.m <= 0) return set_err(c, TF_ERR_BAD_INPUT, "pcg: empty matrix");
     TF_TRY(ensure_diag(c, A));
@@ -1401,12 +1413,11 @@ int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, in
     }
     // mixed precision: FP32 iterations, FP64 iterate and reliable updates
     TF_TRY(ensure_sell(c, A, false));  // FP64 copy for the refinement residuals
-    if (!c->pcg_two_barrier && c->pcg_resident) {
-        bool applied = false;
-        const int st = pcg_resident<float>(c, A, b, x, max_iter, tol, rel, &applied);
-        if (applied || st != TF_OK) return st;
+    if (!c->pcg_two_barrier) {
+        int kind = c->pcg_resident ? kPcgResident : c->kry_threads == 256 ? kPcgCg1_256 : kPcgCg1_512;
+        if (c->autotune && !c->pcg_shape_fixed) TF_TRY(tuned_pcg_kind(c, A, b, &kind));
+        return pcg_mixed_kind(c, A, b, x, kind, max_iter, tol, rel);
     }
-    if (!c->pcg_two_barrier) return run_pcg_cg1(c, A, b, x, max_iter, tol, rel);
     TF_TRY(ensure(c, c->kry32, (size_t)(6 * m)));
     float* d32 = c->kry32.p;
     k_to_f32<<<grid_for(c, m), kBlock, 0, c->stream>>>(m, A.diag, d32);

@@ -208,6 +208,14 @@ struct Sell {
     bool res_ok = false;
 };
 
+// measured choices for one matrix structure (rows, stored entries, SELL slots)
+struct TuneEntry {
+    int64_t m = 0, nnz = 0, npad = 0;
+    int spmv_threads = 0, spmv_per_sm = 0;  // 0: not tuned yet
+    int pcg_kind = -1;                      // -1: not tuned yet
+    float spmv_us[4] = {}, pcg_us[3] = {};  // measured times of the candidates
+};
+
 struct CSR {
     int64_t m = 0, nnz = 0;
     int64_t pattern_gen = 0;    // bumps whenever the pattern changes
@@ -299,6 +307,11 @@ struct Context {
     DBuf<int32_t> sell_iperm[TF_NUM_MATS], sell_halo[TF_NUM_MATS];
     DBuf<uint16_t> sell_coltr[TF_NUM_MATS];
     bool pcg_resident = true;   // PCG: block share of the system resident in shared memory where it fits
+    bool autotune = true;       // measured launch shapes per matrix structure (tune.cu)
+    bool spmv_shape_fixed = false, pcg_shape_fixed = false;  // set by the environment switches
+    std::vector<TuneEntry> tuned;
+    DBuf<double> tune_buf;
+    cudaEvent_t tune_ev[2] = {};
     int pcg_fp64_kernel = 0;    // TF_PCG_FP64_CLASSIC or TF_PCG_FP64_CG1
     int pcg_res_vcap_kb = -1;   // resident PCG: cap on the KB of matrix values kept in shared memory (-1: none)
     DBuf<float2> x_pairs;       // SpMV operand split into FP32 pairs
@@ -442,6 +455,12 @@ int spmv(Context* c, const CSR& A, const double* x, double* y);
 int pcg_jacobi(Context* c, CSR& A, const double* b, double* x, int precision, int* max_iter, double* tol, int rel);
 template <class T>
 int pcg_resident(Context* c, CSR& A, const double* b, double* x, int* max_iter, double* tol, int rel, bool* applied);
+// kinds of the single-barrier mixed PCG (autotuned per matrix structure, tune.cu)
+constexpr int kPcgResident = 0, kPcgCg1_512 = 1, kPcgCg1_256 = 2;
+int pcg_mixed_kind(Context* c, CSR& A, const double* b, double* x, int kind, int* max_iter, double* tol, int rel);
+void launch_spmv_shape(Context* c, const CSR& A, const double* x, double* y, int threads, int per_sm);
+int tuned_spmv_shape(Context* c, CSR& A, int* threads, int* per_sm);
+int tuned_pcg_kind(Context* c, CSR& A, const double* b, int* kind);
 int gmres_jacobi(Context* c, CSR& A, const double* b, double* x, int restart, int method, int precision,
                  int* max_iter, double* tol, int rel);
 int ensure_diag(Context* c, CSR& A);

@@ -259,6 +259,20 @@ int tf_pcg_jacobi(tf_context* ctx, int mat, int vec_b, int vec_x, int precision,
 #define TF_PCG_FP64_CLASSIC 0
 #define TF_PCG_FP64_CG1 1
 int tf_pcg_options(tf_context* ctx, int fp64_kernel);
+/* Autotuned launch shapes.  No counterpart in the reference (its kernels are
+ * OpenMP loops).  With tuning on (the default), the first tf_spmv / mixed
+ * tf_pcg_jacobi on a matrix structure (rows, non-zeros, SELL slots) times the
+ * candidate shapes on that matrix -- SpMV: 512 x {1, 2} and 256 x {2, 4}
+ * threads x blocks per SM; mixed PCG: the shared-memory resident kernel, the
+ * single-barrier kernel with 512 or with 256 threads per block -- on internal
+ * scratch vectors and keeps the fastest for the context.  on = 0 keeps the
+ * fixed defaults.  tf_autotune_info reports the choice for a matrix handle:
+ * spmv_us[4] and pcg_us[3] (may be NULL) the measured microseconds per SpMV /
+ * per PCG iteration of each candidate, pcg_kind 0 resident, 1 512 threads,
+ * 2 256 threads.                                                               */
+int tf_autotune(tf_context* ctx, int on);
+int tf_autotune_info(tf_context* ctx, int mat, int* spmv_threads, int* spmv_blocks_per_sm, int* pcg_kind,
+                     float* spmv_us, float* pcg_us);
 /* GMResSolverCL / GMRES (num/krylovsolver.h:320-463, 1924-1975): restarted
  * GMRES(restart) with modified Gram-Schmidt and Givens rotations, Jacobi
  * preconditioning of the diagonal (for TF_MAT_BLOCK: of both diagonal blocks),

@@ -21,6 +21,7 @@ def ctxs():
 
     build.build()
     res = tf.TraceFEM()
+    res.autotune(False)  # the resident kernel itself, not the tuner's pick
     os.environ["TF_PCG_RESIDENT"] = "0"
     try:
         plain = tf.TraceFEM()
@@ -147,3 +148,36 @@ def test_too_large_for_shared_memory_falls_back(ctxs):
         st, it, res, x = _solve(ctx, nd, prec, k64, tol=1e-10)
         assert st == tf.OK and res <= 1e-10
         assert _fp64_resid(ctx, x) <= 1.01e-10
+
+
+def test_autotune_picks_the_fastest_measured_shape():
+    """tf_autotune: the first SpMV and mixed PCG on a matrix structure time the candidate launch shapes on
+    that matrix; the kept choice is the fastest measured, the caller's vectors are untouched by the timing
+    runs (a non-zero initial guess is honoured), and a rebuilt identical pattern keeps the choice."""
+    from drops_gb300 import build
+
+    build.build()
+    with tf.TraceFEM() as ctx:
+        nd = _system(ctx, 48, tf.P2IF)
+        rng = np.random.default_rng(8)
+        x0 = rng.standard_normal(nd)
+        ctx.vec_upload(tf.VEC_X, x0)
+        ctx.spmv(tf.MAT_SYS, tf.VEC_X, tf.VEC_T0)
+        rp, ci, S = ctx.matrix(tf.MAT_SYS)
+        y = ctx.vec_download(tf.VEC_T0)
+        ref = O.spmv(rp, ci, S, x0)
+        assert np.abs(y - ref).max() <= 1e-12 * np.abs(ref).max()
+        ctx.vec_upload(tf.VEC_X, x0)
+        st, it, res = ctx.pcg_jacobi(tf.MAT_SYS, tf.VEC_RHS, tf.VEC_X, tol=1e-10, precision=tf.PREC_MIXED)
+        assert st == tf.OK and res <= 1e-10
+        assert _fp64_resid(ctx, ctx.vec_download(tf.VEC_X)) <= 1.01e-10
+        thr, bps, kind, spmv_us, pcg_us = ctx.autotune_info(tf.MAT_SYS)
+        print("spmv", thr, bps, spmv_us, "pcg kind", kind, pcg_us)
+        cand = [(512, 1), (512, 2), (256, 2), (256, 4)]
+        assert (thr, bps) == cand[int(np.argmin(spmv_us))] and all(t > 0 for t in spmv_us)
+        assert kind == int(np.argmin(pcg_us)) and all(t > 0 for t in pcg_us)
+        # the same structure again (a rebuilt pattern): the choice is kept
+        _system(ctx, 48, tf.P2IF)
+        ctx.vec_fill(tf.VEC_X, nd, 0.0)
+        st, it2, res = ctx.pcg_jacobi(tf.MAT_SYS, tf.VEC_RHS, tf.VEC_X, tol=1e-10, precision=tf.PREC_MIXED)
+        assert st == tf.OK and ctx.autotune_info(tf.MAT_SYS)[2] == kind
