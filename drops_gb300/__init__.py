@@ -50,7 +50,7 @@ EXPORTS = [
     "tf_vec_download", "tf_vec_size", "tf_vec_fill", "tf_spmv", "tf_spmv_options", "tf_pcg_jacobi", "tf_gmres_jacobi", "tf_pcg_jacobi_noalloc", "tf_ch_steps",
     "tf_mesh_brick_batch", "tf_levelset_analytic_batch", "tf_batch_info", "tf_batch_lincomb", "tf_batch_pcg_jacobi",
     "tf_batch_tune", "tf_batch_config", "tf_mlp_init", "tf_mlp_get_weights", "tf_mlp_set_weights", "tf_mlp_forward",
-    "tf_mlp_gradient", "tf_mlp_train", "tf_ch_features", "tf_ch_steps_learned", "tf_gmres_options", "tf_pcg_options", "tf_autotune", "tf_autotune_info", "tf_timing_enable",
+    "tf_mlp_gradient", "tf_mlp_train", "tf_ch_features", "tf_ch_steps_learned", "tf_gmres_options", "tf_pcg_options", "tf_autotune", "tf_autotune_info", "tf_setup_quaqua_p2", "tf_timing_enable",
     "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2", "tf_spmv_timed", "tf_stream_read_timed", "tf_wind_upload", "tf_vec_write", "tf_vec_read", "tf_ch_stats", "tf_ch_steps_adaptive", "tf_ch_options",
     "tf_host_alloc", "tf_host_free",
 ]
@@ -469,6 +469,14 @@ class TraceFEM:
     def spmv_options(self, kernel=SPMV_KERNEL_FP64):
         """Kernel of tf_spmv: SPMV_KERNEL_FP64 (default) or SPMV_KERNEL_PAIR (FP32 pairs)."""
         self._check(self.L.tf_spmv_options(self.h, C.c_int(kernel)))
+
+    def setup_quaqua_p2(self, f_coeff=13.0, newton_tol=1e-13, newton_maxiter=100):
+        """Isoparametric P2 forms with the QuaQua mapper into FORM_M, FORM_A and VEC_RHS; returns the largest
+        Newton iteration count of a quadrature point."""
+        it = C.c_int()
+        self._check(self.L.tf_setup_quaqua_p2(self.h, C.c_double(f_coeff), C.c_double(newton_tol),
+                                              C.c_int(newton_maxiter), C.byref(it)))
+        return it.value
 
     def autotune(self, on=True):
         self._check(self.L.tf_autotune(self.h, C.c_int(int(on))))

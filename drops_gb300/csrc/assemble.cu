@@ -1098,6 +1098,38 @@ int setup_fe_system(Context* c, unsigned forms, int rhs_kind, const double* rhs_
 }
 
 // ---------------------------------------------------------------------------
+// isoparametric P2 forms (QuaQua mapper, quaqua.cu) into TF_FORM_M, TF_FORM_A
+// and TF_VEC_RHS on the DistributeDOFs pattern
+// ---------------------------------------------------------------------------
+int setup_quaqua_p2(Context* c, double rhs_c, double tol, int maxiter, int* newton_max) {
+    if (!c->fe) return set_err(c, TF_ERR_BAD_INPUT, "setup_quaqua_p2: distribute DOFs first");
+    if (tol <= 0. || maxiter < 1) return set_err(c, TF_ERR_BAD_INPUT, "setup_quaqua_p2: tol > 0, maxiter >= 1");
+    if (c->pattern_dof_version != c->dof_version) TF_TRY(build_pattern(c));
+    TF_TRY(quaqua_elements(c, rhs_c, tol, maxiter, newton_max));
+    const int64_t na = c->n_active, m = c->n_dofs, nnz = c->mats[0].nnz;
+    double* v[2];
+    for (int f = 0; f < 2; ++f) {  // TF_FORM_M, TF_FORM_A
+        TF_TRY(ensure(c, c->mat_vals[f], (size_t)(nnz > 0 ? nnz : 1)));
+        c->mats[f].vals = c->mat_vals[f].p;
+        ++c->mats[f].version;
+        v[f] = c->mats[f].vals;
+    }
+    TF_TRY(ensure(c, c->vecs[TF_VEC_RHS], (size_t)m));
+    if (nnz > 0) {
+        TimedLaunch tl(c, TF_K_SCATTER);
+        k_scatter<10><<<grid_for(c, nnz), kBlock, 0, c->stream>>>(nnz, c->seg_start.p, c->contrib.p, na, c->elem.p,
+                                                                   (1u << TF_FORM_M) | (1u << TF_FORM_A), v[0], v[1],
+                                                                   nullptr, nullptr);
+        k_scatter_rhs<10><<<grid_for(c, m), kBlock, 0, c->stream>>>(m, c->diag_slot.p, c->seg_start.p, c->contrib.p,
+                                                                     c->elem_rhs.p, c->vecs[TF_VEC_RHS].p);
+        c->launches += 2;
+        TF_CUDA(c, cudaGetLastError());
+    }
+    TF_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TF_OK;
+}
+
+// ---------------------------------------------------------------------------
 // legacy P1 interface forms of the surfactant.cpp path
 // ---------------------------------------------------------------------------
 // InterfacePatchCL::Sign (num/interfacePatch.h:75): |phi| < 2 eps counts as 0

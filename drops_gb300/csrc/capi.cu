@@ -933,6 +933,13 @@ int tf_spmv_options(tf_context* t, int kernel) {
     return TF_OK;
 }
 
+int tf_setup_quaqua_p2(tf_context* t, double f_coeff, double newton_tol, int newton_maxiter, int* newton_iters_max) {
+    CTX_CHECK(t);
+    tf::Context* c = &t->c;
+    cudaSetDevice(c->device);
+    return tf::setup_quaqua_p2(c, f_coeff, newton_tol, newton_maxiter, newton_iters_max);
+}
+
 int tf_autotune(tf_context* t, int on) {
     CTX_CHECK(t);
     t->c.autotune = on != 0;

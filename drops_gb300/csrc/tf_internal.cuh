@@ -352,7 +352,8 @@ struct Context {
     int64_t mlp_step = 0;
     // learned Cahn-Hilliard warm start
     DBuf<double> ch_part, ch_scales, ch_hist;
-    DBuf<double> ch_ring, ch_av;  // learned warm start: recent states, differences, A V of the projection
+    DBuf<double> ch_ring, ch_av;
+    DBuf<double> qq_grad;  // isoparametric P2: recovered level-set gradient per interface DOF  // learned warm start: recent states, differences, A V of the projection
     DBuf<double> ch_prev, ch_x1, ch_x2;  // adaptive BDF1/BDF2: chi_prev, BDF1 and BDF2 states
     DBuf<float> ch_xyz, ch_nrm, ch_Y, ch_pred;
     DBuf<__nv_bfloat16> ch_X;
@@ -490,6 +491,8 @@ int ch_steps_learned(Context* c, const ChLearnParams& P, int* iters, double* res
 int mlp_epoch_dev(Context* c, const __nv_bfloat16* X, const float* Y, int64_t n, int mb_tiles, float lr, float* gsum,
                   double* loss);
 int ensure_vals32(Context* c, CSR& A);
+int quaqua_elements(Context* c, double rhs_c, double tol, int maxiter, int* newton_max);
+int setup_quaqua_p2(Context* c, double rhs_c, double tol, int maxiter, int* newton_max);
 int ensure_sell(Context* c, CSR& A, bool fp32);
 
 // matrix handles that hold an assembled form

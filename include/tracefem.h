@@ -356,6 +356,24 @@ int tf_mlp_train(tf_context* ctx, const uint16_t* X, const float* Y, int64_t n, 
  * Cahn-Hilliard loop builds them; needs the P1 numbering and TF_FORM_M.       */
 int tf_ch_features(tf_context* ctx, int vec_cur, int vec_old, int vec_next, uint16_t* X, float* Y);
 
+/* ---- isoparametric P2 TraceFEM (QuaQua mapper) ------------------------------------ */
+/* The P2 driver of surfactant/surfactant.cpp:1581-1640: InterfaceCommonDataP2CL
+ * on PrincipalLatticeCL::instance(1) with QuaQuaMapperCL (Newton form,
+ * levelset/levelsetmapper.cpp) and averaging_P2_gradient_recovery
+ * (num/gradient_recovery.cpp:82), accumulating LocalMassP2CL,
+ * LocalLaplaceBeltramiP2CL (D = 1) and LocalVectorP2CL with f(y) = f_coeff
+ * y0 y1 y2 at the base points y (surfactant/ifacetransp.h:2286-2402).  Needs a
+ * single brick mesh, a P2 level set and the P2IF numbering of tf_distribute_dofs;
+ * writes the isoparametric mass matrix into TF_FORM_M, the Laplace-Beltrami
+ * matrix into TF_FORM_A (on the DistributeDOFs pattern: entries of tets with
+ * an empty linear interface are explicit zeros) and the load vector into
+ * TF_VEC_RHS.  newton_tol / newton_maxiter: the mapper's Newton (the reference
+ * driver reads them from LevelsetMapper.Tol / Iter); newton_iters_max (may be
+ * NULL) receives the largest Newton count of a quadrature point.  As in the
+ * reference, every base point is sought on its own tet's P2 level set and
+ * recovered gradient, extended beyond the tet.                                   */
+int tf_setup_quaqua_p2(tf_context* ctx, double f_coeff, double newton_tol, int newton_maxiter, int* newton_iters_max);
+
 /* ---- allocation-free PCG -------------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory: applications that manage every GPU byte through their own pool and

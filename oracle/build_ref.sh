@@ -8,7 +8,8 @@
 #
 # Flags: -O2 -fopenmp, no --fast-math (the reference's default DEBUG-less
 # build), -include cstring (geom/signtraits.h) and -include iomanip
-# (misc/progressaccu.cpp) for headers the sources assume, and oracle/refshim/ on the
+# (misc/progressaccu.cpp) and -include memory (levelset/levelsetmapper.h names
+# std::unique_ptr without including <memory>) for headers the sources assume, and oracle/refshim/ on the
 # include path in place of Boost.PropertyTree.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
@@ -17,12 +18,13 @@ OUT="$HERE/_ref"
 OBJ="$OUT/obj"
 mkdir -p "$OBJ"
 CXX="${CXX:-g++}"
-FLAGS=(-std=c++17 -O2 -fopenmp -ffp-contract=off -w -include cstring -include iomanip -I "$SRC" -I "$HERE/refshim")
+FLAGS=(-std=c++17 -O2 -fopenmp -ffp-contract=off -w -include cstring -include iomanip -include memory -I "$SRC" -I "$HERE/refshim")
 UNITS=(
   geom/topo.cpp geom/simplex.cpp geom/multigrid.cpp geom/builder.cpp geom/boundary.cpp
   geom/principallattice.cpp geom/reftetracut.cpp geom/subtriangulation.cpp geom/locator.cpp
   geom/deformation.cpp
   num/discretize.cpp num/quadrature.cpp num/unknowns.cpp num/fe.cpp num/interfacePatch.cpp num/bndData.cpp
+  num/gradient_recovery.cpp levelset/levelsetmapper.cpp
   misc/utils.cpp misc/problem.cpp misc/params.cpp misc/scopetimer.cpp
   surfactant/ifacetransp.cpp
   levelset/levelset.cpp levelset/surfacetension.cpp levelset/fastmarch.cpp levelset/volume_adjustment.cpp
@@ -39,7 +41,6 @@ for u in "${UNITS[@]}"; do compile "$u" & pids+=($!);
 done
 for p in "${pids[@]}"; do wait "$p"; done
 "$CXX" "${FLAGS[@]}" -fno-access-control -c "$HERE/ref_harness.cpp" -o "$OBJ/ref_harness.o"
-"$CXX" "${FLAGS[@]}" -c "$HERE/ref_stubs.cpp" -o "$OBJ/ref_stubs.o"
 "$CXX" -fopenmp -o "$OUT/ref_harness" "$OBJ"/*.o
 echo "built $OUT/ref_harness"
 

@@ -351,3 +351,65 @@ def mlp_gradient(w, X, Y, exact=False):
     loss = L.orc_mlp_gradient(_p(w, C.c_float), _p(X, C.c_uint16), _p(Y, C.c_float), C.c_int64(X.shape[0]),
                               C.c_int(int(exact)), _p(g, C.c_float))
     return g, loss
+
+
+class _QQCtx(C.Structure):
+    _fields_ = [("coords", C.c_void_p), ("tet_v", C.c_void_p), ("tet_e", C.c_void_p), ("ls_vert", C.c_void_p),
+                ("ls_edge", C.c_void_p), ("grad_vert", C.c_void_p), ("grad_edge", C.c_void_p), ("tol", C.c_double),
+                ("armijo", C.c_double), ("maxiter", C.c_int), ("max_damping", C.c_int), ("rhs_c", C.c_double)]
+
+
+def grad_recovery(mesh, ls_vert, ls_edge):
+    """averaging_P2_gradient_recovery (num/gradient_recovery.cpp:82-89): (grad_vert[nv,3], grad_edge[ne,3])."""
+    L = lib()
+    nv, ne, nt = mesh.nv, mesh.ne, mesh.nt
+    gv, ge = np.zeros((nv, 3)), np.zeros((ne, 3))
+    L.orc_grad_recovery(C.c_int64(nt), _p(mesh.tet_v, C.c_int32), _p(mesh.tet_e, C.c_int32), _p(mesh.coords, C.c_double),
+                        C.c_int64(nv), C.c_int64(ne), _p(_in(ls_vert, np.float64), C.c_double),
+                        _p(_in(ls_edge, np.float64), C.c_double), _p(gv, C.c_double), _p(ge, C.c_double))
+    return gv, ge
+
+
+def _qq_ctx(mesh, ls_vert, ls_edge, gv, ge, rhs_c=13.0, tol=1e-13, maxiter=100, armijo=1e-4, max_damping=8):
+    q = _QQCtx()
+    keep = (mesh.coords, mesh.tet_v, mesh.tet_e, _in(ls_vert, np.float64), _in(ls_edge, np.float64),
+            _in(gv, np.float64), _in(ge, np.float64))
+    q.coords, q.tet_v, q.tet_e = keep[0].ctypes.data, keep[1].ctypes.data, keep[2].ctypes.data
+    q.ls_vert, q.ls_edge, q.grad_vert, q.grad_edge = (k.ctypes.data for k in keep[3:])
+    q.tol, q.armijo, q.maxiter, q.max_damping, q.rhs_c = tol, armijo, maxiter, max_damping, rhs_c
+    return q, keep
+
+
+def quaqua_point(mesh, ls_vert, ls_edge, grad, t, b0):
+    """One base point of tet t's point b0: (base tet, base bary, dh, Jacobian 3x3, Newton iterations)."""
+    q, keep = _qq_ctx(mesh, ls_vert, ls_edge, *grad)
+    bt, it, dh = C.c_int64(), C.c_int(), C.c_double()
+    bb, J = np.zeros(4), np.zeros(9)
+    st = lib().orc_qq_point(C.byref(q), C.c_int64(int(t)), _p(np.ascontiguousarray(b0, dtype=np.float64), C.c_double),
+                            C.byref(bt), _p(bb, C.c_double), C.byref(dh), _p(J, C.c_double), C.byref(it))
+    if st:
+        raise RuntimeError(f"orc_qq_point: status {st}")
+    return bt.value, bb, dh.value, J.reshape(3, 3), it.value
+
+
+def quaqua_elements(mesh, ls_vert, ls_edge, tets, rhs_c=13.0, tol=1e-13, maxiter=100, armijo=1e-4, max_damping=8,
+                    grad=None):
+    """LocalMassP2CL / LocalLaplaceBeltramiP2CL / LocalVectorP2CL with the QuaQua mapper for the tets `tets`:
+    (M[k,10,10], A[k,10,10], b[k,10], points[k], newton iterations[k])."""
+    L = lib()
+    gv, ge = grad if grad is not None else grad_recovery(mesh, ls_vert, ls_edge)
+    q, keep = _qq_ctx(mesh, ls_vert, ls_edge, gv, ge, rhs_c, tol, maxiter, armijo, max_damping)
+    k = len(tets)
+    M, A, b = np.zeros((k, 10, 10)), np.zeros((k, 10, 10)), np.zeros((k, 10))
+    npts, newton = np.zeros(k, np.int32), np.zeros(k, np.int32)
+    Mt, At, bt = np.zeros(100), np.zeros(100), np.zeros(10)
+    ip, it = C.c_int(), C.c_int()
+    for i, t in enumerate(tets):
+        st = L.orc_qq_local(C.byref(q), C.c_int64(int(t)), _p(Mt, C.c_double), _p(At, C.c_double), _p(bt, C.c_double),
+                            C.byref(ip), C.byref(it))
+        if st:
+            raise RuntimeError(f"orc_qq_local: status {st} at tet {t}")
+        M[i], A[i], b[i] = Mt.reshape(10, 10), At.reshape(10, 10), bt
+        npts[i], newton[i] = ip.value, it.value
+    del keep
+    return M, A, b, npts, newton

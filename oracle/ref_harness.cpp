@@ -17,6 +17,14 @@
 //       (surfactant/ifacetransp.cpp:367-380, 499-512, 532-563) on the unit sphere,
 //       P2 level set, CreateNumbering(P1IF_FE)
 //   ref_harness area <out>                  tests/principallattice.cpp:316-347
+//   ref_harness quaqua <n> <a> <out>
+//       Isoparametric P2 TraceFEM on the unit sphere (surfactant/surfactant.cpp:
+//       1581-1640): P2 level set by nodal interpolation, the recovered
+//       gradient (averaging_P2_gradient_recovery, num/gradient_recovery.cpp:82),
+//       the QuaQua mapper (levelset/levelsetmapper.cpp, Newton form) and
+//       LocalMassP2CL / LocalLaplaceBeltramiP2CL / LocalVectorP2CL
+//       (surfactant/ifacetransp.h:2286-2402) on the linear interface
+//       (principal lattice 1), accumulated on the DistributeDOFs P2IF numbering.
 //   ref_harness gmres <n> <a> <steps> <out>
 //       Torus (R = 1, r = 0.4) P1 system on [-a,a]^3, n^3 cubes:
 //       GMRES (num/krylovsolver.h:320-463) with JACPcCL on M + A + h C_n, right
@@ -55,6 +63,8 @@
 // is why this file is compiled with -fno-access-control.
 #include "geom/builder.h"
 #include "misc/problem.h"
+#include "levelset/levelsetmapper.h"
+#include "num/gradient_recovery.h"
 #include "num/krylovsolver.h"
 #include "num/precond.h"
 #include "surfactant/ifacetransp.h"
@@ -736,6 +746,84 @@ int cmd_gmres(int argc, char** argv) {
     return 0;
 }
 
+// f = 13 xyz on the unit sphere at the projected points (Surface.hpp:46-52 restated as in cmd_system)
+double quaqua_f(const Point3DCL& x, double) { return 13. * x[0] * x[1] * x[2]; }
+
+int cmd_quaqua(int argc, char** argv) {
+    if (argc < 5) throw std::invalid_argument("usage: quaqua n a out");
+    const int n = std::atoi(argv[2]);
+    const double a = std::atof(argv[3]);
+    Writer w(argv[4]);
+    BrickBuilderCL brick(Point3DCL(-a), 2. * a * std_basis<3>(1), 2. * a * std_basis<3>(2), 2. * a * std_basis<3>(3), n,
+                         n, n);
+    MultiGridCL mg(brick);
+    Flat F = flatten(mg);
+    IdxDescCL lsIdx(P2_FE);
+    lsIdx.DistributeDOFs(0, mg);
+    VecDescCL ls(&lsIdx);
+    const Uint li = lsIdx.GetIdx();
+    DROPS_FOR_TRIANG_VERTEX(mg, 0, it) ls.Data[it->Unknowns(li)] = ls_value("sphere", it->GetCoord());
+    DROPS_FOR_TRIANG_EDGE(mg, 0, it)
+        ls.Data[it->Unknowns(li)] = ls_value("sphere", 0.5 * (it->GetVertex(0)->GetCoord() + it->GetVertex(1)->GetCoord()));
+    BndCondT bc[6] = {NoBC, NoBC, NoBC, NoBC, NoBC, NoBC};
+    BndDataCL<> lsbnd(6, bc);
+    {
+        std::vector<double> lv, le;
+        std::vector<int64_t> ev;
+        DROPS_FOR_TRIANG_VERTEX(mg, 0, it) lv.push_back(ls.Data[it->Unknowns(li)]);
+        DROPS_FOR_TRIANG_EDGE(mg, 0, it) {
+            le.push_back(ls.Data[it->Unknowns(li)]);
+            ev.push_back(F.vid[it->GetVertex(0)]);
+            ev.push_back(F.vid[it->GetVertex(1)]);
+        }
+        w.d("ls_vert", lv);
+        w.d("ls_edge", le);
+        w.l("edge_v", ev);
+    }
+    // interface P2 numbering (DistributeDOFs, the UH API)
+    IdxDescCL ifIdx(P2IF_FE);
+    ifIdx.DistributeDOFs(0, mg, &ls);
+    w.i("n_dofs", (int64_t)ifIdx.NumUnknowns());
+    // recovered gradient of the level set: P2 vector field, nodal averages over the tets
+    IdxDescCL vecIdx(vecP2_FE);
+    vecIdx.CreateNumbering(0, mg);
+    VecDescCL grad(&vecIdx);
+    averaging_P2_gradient_recovery(mg, ls, lsbnd, grad);
+    {
+        const Uint gi = vecIdx.GetIdx();
+        std::vector<double> gv, ge;
+        DROPS_FOR_TRIANG_VERTEX(mg, 0, it)
+            for (int c = 0; c < 3; ++c) gv.push_back(grad.Data[it->Unknowns(gi) + c]);
+        DROPS_FOR_TRIANG_EDGE(mg, 0, it)
+            for (int c = 0; c < 3; ++c) ge.push_back(grad.Data[it->Unknowns(gi) + c]);
+        w.d("grad_vert", gv);
+        w.d("grad_edge", ge);
+    }
+    const PrincipalLatticeCL& lat = PrincipalLatticeCL::instance(1);
+    TetraToTetrasT nbh;
+    compute_tetra_neighborhoods(mg, ls, lsbnd, lat, nbh);
+    // Newton form of the mapper, tolerance far below the one of the reference's parameter files so
+    // that every base point is the root to rounding
+    QuaQuaMapperCL quaqua(mg, ls, grad, &nbh, 100, 1e-13, false, 1e-4);
+    TetraAccumulatorTupleCL accus;
+    InterfaceCommonDataP2CL cdata(ls, lsbnd, quaqua, lat);
+    accus.push_back(&cdata);
+    MatDescCL M(&ifIdx, &ifIdx), A(&ifIdx, &ifIdx);
+    InterfaceMatrixAccuCL<LocalMassP2CL, InterfaceCommonDataP2CL> accuM(&M, LocalMassP2CL(), cdata, "Mp2");
+    accus.push_back(&accuM);
+    InterfaceMatrixAccuCL<LocalLaplaceBeltramiP2CL, InterfaceCommonDataP2CL> accuA(&A, LocalLaplaceBeltramiP2CL(1.0),
+                                                                                 cdata, "Ap2");
+    accus.push_back(&accuA);
+    VecDescCL b(&ifIdx);
+    InterfaceVectorAccuCL<LocalVectorP2CL, InterfaceCommonDataP2CL> accub(&b, LocalVectorP2CL(quaqua_f, 0.), cdata);
+    accus.push_back(&accub);
+    accumulate(accus, mg, ifIdx.TriangLevel(), ifIdx.GetBndInfo());
+    write_csr(w, "M", M.Data);
+    write_csr(w, "A", A.Data);
+    w.d("rhs", std::vector<double>(std::begin(b.Data), std::end(b.Data)));
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -747,6 +835,7 @@ int main(int argc, char** argv) {
         if (cmd == "legacy_forms") return cmd_legacy_forms(argc, argv);
         if (cmd == "area") return cmd_area(argc, argv);
         if (cmd == "gmres") return cmd_gmres(argc, argv);
+        if (cmd == "quaqua") return cmd_quaqua(argc, argv);
         throw std::invalid_argument("unknown command " + cmd);
     } catch (std::exception& e) {
         std::cerr << "ref_harness: " << e.what() << "\n";

@@ -255,13 +255,9 @@ void orc_lattice2(double verts[10][4], int tets[8][4]) {
 /* P2 local dof -> lattice vertex (geom/principallattice.cpp p2_dof_on_lattice_2) */
 static const int P2_ON_LAT[10] = {0, 4, 7, 9, 1, 2, 5, 3, 6, 8};
 
-int orc_make_patch(const double ls10[10], orc_patch_t* p) {
-    double LV[10][4];
-    int LT[8][4];
-    orc_lattice2(LV, LT);
-    double lat_ls[10];
-    for (int k = 0; k < 10; ++k) lat_ls[P2_ON_LAT[k]] = ls10[k];
-
+/* SPatchCL<3>::make_patch<MergeCutPolicyCL> on a principal lattice with nsub
+ * sub-tets LT over the lattice vertices LV, level set lat_ls at the vertices */
+static int make_patch_lat(int nsub, const double (*LV)[4], const int (*LT)[4], const double* lat_ls, orc_patch_t* p) {
     /* MergeCut memo: lattice edge (lo,hi) -> cut vertex number */
     int cut_key[ORC_MAX_PVERTS][2];
     double cut_bary[ORC_MAX_PVERTS][4];
@@ -273,7 +269,7 @@ int orc_make_patch(const double ls10[10], orc_patch_t* p) {
     int zuse_f[3 * ORC_MAX_FACETS], zuse_j[3 * ORC_MAX_FACETS], n_zuse = 0;
 
     p->n_facets = 0;
-    for (int s = 0; s < 8; ++s) {
+    for (int s = 0; s < nsub; ++s) {
         double loc[4];
         int sg[4], sum = 0;
         for (int k = 0; k < 4; ++k) {
@@ -340,6 +336,22 @@ int orc_make_patch(const double ls10[10], orc_patch_t* p) {
     p->n_cut_verts = n_cut;
     p->n_verts = n_cut + n_zero;
     return ORC_OK;
+}
+
+int orc_make_patch(const double ls10[10], orc_patch_t* p) {
+    double LV[10][4];
+    int LT[8][4];
+    orc_lattice2(LV, LT);
+    double lat_ls[10];
+    for (int k = 0; k < 10; ++k) lat_ls[P2_ON_LAT[k]] = ls10[k];
+    return make_patch_lat(8, (const double(*)[4])LV, (const int(*)[4])LT, lat_ls, p);
+}
+
+/* the patch on PrincipalLatticeCL::instance(1): the tet itself, its 4 vertices */
+int orc_make_patch1(const double ls4[4], orc_patch_t* p) {
+    static const double LV[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
+    static const int LT[1][4] = {{0, 1, 2, 3}};
+    return make_patch_lat(1, LV, LT, ls4, p);
 }
 
 /* ======================================================================= */
@@ -1345,5 +1357,396 @@ int orc_ch_block(int64_t m, const int64_t* rowptr, const int32_t* colind, const 
                 }
             browptr[half * m + r + 1] = w;
         }
+    return ORC_OK;
+}
+
+/* ======================================================================= */
+/* isoparametric P2 TraceFEM: the QuaQua mapper (levelset/levelsetmapper.cpp)  */
+/* and LocalMassP2CL / LocalLaplaceBeltramiP2CL / LocalVectorP2CL              */
+/* (surfactant/ifacetransp.h:2286-2402) on the linear interface              */
+/* ======================================================================= */
+/* averaging_P2_gradient_recovery (num/gradient_recovery.cpp:82-89,
+ * OswaldProjectionP2AccuCL num/oswald_projection.h:102-125): per tet the
+ * gradient of the P2 level set at its vertices, the mean of the end values on
+ * its edges; every P2 node averages the values of all its tets, running mean
+ * in tet order. */
+void orc_grad_recovery(int64_t nt, const int32_t* tet_v, const int32_t* tet_e, const double* coords, int64_t nv,
+                       int64_t ne, const double* ls_vert, const double* ls_edge, double* grad_vert, double* grad_edge) {
+    double* cv = (double*)calloc((size_t)(nv + ne), sizeof(double));
+    double* ce = cv + nv;
+    for (int64_t i = 0; i < 3 * nv; ++i) grad_vert[i] = 0.;
+    for (int64_t i = 0; i < 3 * ne; ++i) grad_edge[i] = 0.;
+    for (int64_t t = 0; t < nt; ++t) {
+        double xv[4][3], T[3][3], det, gl[4][3], f[10], gv[4][3];
+        for (int i = 0; i < 4; ++i) memcpy(xv[i], coords + 3 * tet_v[4 * t + i], sizeof xv[i]);
+        trafo(xv, T, &det);
+        bary_grads(T, gl);
+        gather_ls10(tet_v + 4 * t, tet_e + 6 * t, ls_vert, ls_edge, f);
+        for (int i = 0; i < 4; ++i) {
+            double b[4] = {0, 0, 0, 0}, g[10][3];
+            b[i] = 1.;
+            p2_grads(b, gl, g);
+            for (int r = 0; r < 3; ++r) {
+                double s = 0.;
+                for (int k = 0; k < 10; ++k) s += f[k] * g[k][r];
+                gv[i][r] = s;
+            }
+        }
+        for (int i = 0; i < 10; ++i) {
+            double val[3], *dst, *cnt;
+            if (i < 4) {
+                for (int r = 0; r < 3; ++r) val[r] = gv[i][r];
+                dst = grad_vert + 3 * (int64_t)tet_v[4 * t + i];
+                cnt = cv + tet_v[4 * t + i];
+            } else {
+                for (int r = 0; r < 3; ++r) val[r] = 0.5 * (gv[EV[i - 4][0]][r] + gv[EV[i - 4][1]][r]);
+                dst = grad_edge + 3 * (int64_t)tet_e[6 * t + i - 4];
+                cnt = ce + tet_e[6 * t + i - 4];
+            }
+            const double n = (*cnt += 1.);
+            for (int r = 0; r < 3; ++r) dst[r] = ((n - 1.) / n) * dst[r] + (1. / n) * val[r];
+        }
+    }
+    free(cv);
+}
+
+/* barycentric coordinates of the world point x with respect to tet t (they
+ * may lie outside [0, 1]: the mapper extrapolates the tet's polynomials) */
+static void qq_world2bary(const orc_qq_ctx* q, int64_t t, const double x[3], double b[4]) {
+    double xv[4][3], T[3][3], det, gl[4][3];
+    for (int i = 0; i < 4; ++i) memcpy(xv[i], q->coords + 3 * q->tet_v[4 * t + i], sizeof xv[i]);
+    trafo(xv, T, &det);
+    bary_grads(T, gl);
+    double d[3] = {x[0] - xv[0][0], x[1] - xv[0][1], x[2] - xv[0][2]};
+    b[0] = 1.;
+    for (int k = 1; k < 4; ++k) {
+        b[k] = dot3(gl[k], d);
+        b[0] -= b[k];
+    }
+}
+
+/* P2 level set, recovered gradient and the P2 basis gradients of tet t at b */
+typedef struct {
+    int64_t t;
+    double gl[4][3], h, f[10], gh[10][3];
+} qq_tet;
+static void qq_set_tet(const orc_qq_ctx* q, int64_t t, qq_tet* c) {
+    double xv[4][3], T[3][3], det;
+    for (int i = 0; i < 4; ++i) memcpy(xv[i], q->coords + 3 * q->tet_v[4 * t + i], sizeof xv[i]);
+    trafo(xv, T, &det);
+    bary_grads(T, c->gl);
+    c->h = cbrt(fabs(det));
+    gather_ls10(q->tet_v + 4 * t, q->tet_e + 6 * t, q->ls_vert, q->ls_edge, c->f);
+    for (int k = 0; k < 4; ++k) memcpy(c->gh[k], q->grad_vert + 3 * (int64_t)q->tet_v[4 * t + k], sizeof c->gh[k]);
+    for (int k = 0; k < 6; ++k) memcpy(c->gh[4 + k], q->grad_edge + 3 * (int64_t)q->tet_e[6 * t + k], sizeof c->gh[k]);
+    c->t = t;
+}
+static void qq_eval(const qq_tet* c, const double b[4], double* ls, double g_ls[3], double gh[3], double dgh[3][3]) {
+    double phi[10], g[10][3];
+    p2_vals(b, phi);
+    p2_grads(b, c->gl, g);
+    double l = 0.;
+    for (int k = 0; k < 10; ++k) l += c->f[k] * phi[k];
+    *ls = l;
+    for (int r = 0; r < 3; ++r) {
+        double s = 0., s2 = 0.;
+        for (int k = 0; k < 10; ++k) {
+            s += c->f[k] * g[k][r];
+            s2 += c->gh[k][r] * phi[k];
+        }
+        g_ls[r] = s;
+        gh[r] = s2;
+    }
+    if (dgh)
+        for (int r = 0; r < 3; ++r)
+            for (int s = 0; s < 3; ++s) {
+                double v = 0.;
+                for (int k = 0; k < 10; ++k) v += c->gh[k][r] * g[k][s];
+                dgh[r][s] = v; /* sum_k gh_k (x) grad phi_k */
+            }
+}
+/* solve the n x n system A x = b by Gaussian elimination with partial pivoting */
+static int qq_solve(int n, double A[4][4], double b[4]) {
+    for (int k = 0; k < n; ++k) {
+        int p = k;
+        for (int i = k + 1; i < n; ++i)
+            if (fabs(A[i][k]) > fabs(A[p][k])) p = i;
+        if (A[p][k] == 0.) return 0;
+        if (p != k) {
+            for (int j = 0; j < n; ++j) { double t = A[k][j]; A[k][j] = A[p][j]; A[p][j] = t; }
+            double t = b[k]; b[k] = b[p]; b[p] = t;
+        }
+        for (int i = k + 1; i < n; ++i) {
+            const double m = A[i][k] / A[k][k];
+            for (int j = k; j < n; ++j) A[i][j] -= m * A[k][j];
+            b[i] -= m * b[k];
+        }
+    }
+    for (int k = n - 1; k >= 0; --k) {
+        double s = b[k];
+        for (int j = k + 1; j < n; ++j) s -= A[k][j] * b[j];
+        b[k] = s / A[k][k];
+    }
+    return 1;
+}
+
+/* base point of the point b0 of tet t (QuaQuaMapperCL::base_point_newton,
+ * levelset/levelsetmapper.cpp:551-566): Newton on F(x, s) = (x0 - x - s gh(x),
+ * -ls(x)) with the Armijo backtracking of newton_solve (num/newton.h:70-113).
+ * Every iterate is evaluated on tet t's own P2 level set and recovered
+ * gradient, extended beyond the tet: in the reference, locate_new_point
+ * (levelsetmapper.cpp:463-490) searches the neighbourhood only while its tet
+ * argument is null, and QuaQuaMapperFunctionCL::set_point (:178-208) always
+ * passes the current tet, so the base tet never changes.  Returns the tet and
+ * barycentric coordinates of the base point, the quasi-distance dh and the
+ * Newton iterations. */
+static int qq_base_point(const orc_qq_ctx* q, int64_t t, const double b0[4], int64_t* bt, double bb[4], double* dh,
+                         int* iters) {
+    qq_tet c;
+    qq_set_tet(q, t, &c);
+    double x0[3];
+    for (int r = 0; r < 3; ++r) {
+        double s = 0.;
+        for (int k = 0; k < 4; ++k) s += q->coords[3 * (int64_t)q->tet_v[4 * t + k] + r] * b0[k];
+        x0[r] = s;
+    }
+    double x[4] = {x0[0], x0[1], x0[2], 0.}, b[4];
+    memcpy(b, b0, sizeof b);
+    double ls, g_ls[3], gh[3], dgh[3][3], F[4];
+    qq_eval(&c, b, &ls, g_ls, gh, NULL);
+    F[0] = F[1] = F[2] = 0.;
+    F[3] = -ls;
+    int iter;
+    for (iter = 0;; ++iter) {
+        const double normF = sqrt(F[0] * F[0] + F[1] * F[1] + F[2] * F[2] + F[3] * F[3]);
+        if (iter >= q->maxiter || normF < q->tol) break;
+        qq_eval(&c, b, &ls, g_ls, gh, dgh);
+        double dF[4][4];
+        for (int i = 0; i < 3; ++i) {
+            for (int j = 0; j < 3; ++j) dF[i][j] = -x[3] * dgh[i][j];
+            dF[i][i] -= 1.;
+            dF[i][3] = -gh[i];
+            dF[3][i] = -g_ls[i];
+        }
+        dF[3][3] = 0.;
+        double A4[4][4], dx[4];
+        memcpy(A4, dF, sizeof A4);
+        memcpy(dx, F, sizeof dx);
+        if (!qq_solve(4, A4, dx)) return ORC_ERR_BAD_INPUT;
+        double Jdx[4] = {0, 0, 0, 0};
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) Jdx[i] += dF[i][j] * dx[j];
+        const double slope = q->armijo * (F[0] * Jdx[0] + F[1] * Jdx[1] + F[2] * Jdx[2] + F[3] * Jdx[3]) / normF;
+        double l = 0.5 * c.h / sqrt(dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
+        if (!(l < 1.)) l = 1.;
+        int j, accepted = 0;
+        double bn[4], Fn[4];
+        for (j = 0; j < q->max_damping && l >= 1e-7; ++j, l *= 0.5) {
+            double xn[4];
+            for (int i = 0; i < 4; ++i) xn[i] = x[i] - l * dx[i];
+            qq_world2bary(q, c.t, xn, bn);
+            double lsn, gn[3], ghn[3];
+            qq_eval(&c, bn, &lsn, gn, ghn, NULL);
+            for (int i = 0; i < 3; ++i) Fn[i] = x0[i] - xn[i] - xn[3] * ghn[i];
+            Fn[3] = -lsn;
+            if (sqrt(Fn[0] * Fn[0] + Fn[1] * Fn[1] + Fn[2] * Fn[2] + Fn[3] * Fn[3]) < normF + slope * l) {
+                accepted = 1;
+                break;
+            }
+        }
+        if (l < 1e-7) break;
+        /* as newton_solve: without an accepted step the last halved factor is taken */
+        for (int i = 0; i < 4; ++i) x[i] -= l * dx[i];
+        if (!accepted) {
+            qq_world2bary(q, c.t, x, bn);
+            double lsn, gn[3], ghn[3];
+            qq_eval(&c, bn, &lsn, gn, ghn, NULL);
+            for (int i = 0; i < 3; ++i) Fn[i] = x0[i] - x[i] - x[3] * ghn[i];
+            Fn[3] = -lsn;
+        }
+        memcpy(b, bn, sizeof b);
+        memcpy(F, Fn, sizeof F);
+    }
+    qq_eval(&c, b, &ls, g_ls, gh, NULL);
+    *dh = x[3] * norm3(gh);
+    *bt = c.t;
+    memcpy(bb, b, sizeof b);
+    *iters = iter;
+    return ORC_OK;
+}
+
+/* Jacobian of the mapping at the base point (QuaQuaMapperCL::jacobian,
+ * levelset/levelsetmapper.cpp:590-638) and the unit normal n of the level set
+ * there */
+static void qq_jacobian(const orc_qq_ctx* q, int64_t bt, const double bb[4], double dh, double dph[3][3], double n[3]) {
+    qq_tet c;
+    qq_set_tet(q, bt, &c);
+    double ls, g_ls[3], gh[3], dgh[3][3];
+    qq_eval(&c, bb, &ls, g_ls, gh, dgh);
+    const double ngh = norm3(gh), nn = norm3(g_ls);
+    double qn[3];
+    for (int r = 0; r < 3; ++r) {
+        qn[r] = gh[r] / ngh;
+        n[r] = g_ls[r] / nn;
+    }
+    double tq[3];  /* dgh^T q_n */
+    for (int s = 0; s < 3; ++s) tq[s] = dgh[0][s] * qn[0] + dgh[1][s] * qn[1] + dgh[2][s] * qn[2];
+    double dn[3][3], Q[3][3];
+    const double qdn = dot3(qn, n);
+    for (int r = 0; r < 3; ++r)
+        for (int s = 0; s < 3; ++s) {
+            dn[r][s] = (1. / ngh) * (dgh[r][s] - qn[r] * tq[s]);
+            Q[r][s] = (r == s ? 1. : 0.) - (qn[r] / qdn) * n[s];
+        }
+    double B[3][3];  /* I + dh Q dn */
+    for (int r = 0; r < 3; ++r)
+        for (int s = 0; s < 3; ++s) {
+            double v = 0.;
+            for (int k = 0; k < 3; ++k) v += Q[r][k] * dn[k][s];
+            B[r][s] = (r == s ? 1. : 0.) + dh * v;
+        }
+    for (int col = 0; col < 3; ++col) {
+        double A4[4][4] = {{0}}, rhs[4] = {Q[0][col], Q[1][col], Q[2][col], 0.};
+        for (int r = 0; r < 3; ++r)
+            for (int s = 0; s < 3; ++s) A4[r][s] = B[r][s];
+        qq_solve(3, A4, rhs);
+        for (int r = 0; r < 3; ++r) dph[r][col] = rhs[r];
+    }
+}
+
+int orc_qq_local(const orc_qq_ctx* q, int64_t t, double M[100], double A[100], double b[10], int* npts, int* newton) {
+    init_quad();
+    memset(M, 0, sizeof(double) * 100);
+    memset(A, 0, sizeof(double) * 100);
+    memset(b, 0, sizeof(double) * 10);
+    *npts = 0;
+    *newton = 0;
+    double f10[10], ls4[4];
+    gather_ls10(q->tet_v + 4 * t, q->tet_e + 6 * t, q->ls_vert, q->ls_edge, f10);
+    memcpy(ls4, f10, sizeof ls4);
+    int sg0 = sgn(ls4[0]), mixed = 0;
+    for (int k = 1; k < 4; ++k) mixed |= sgn(ls4[k]) != sg0;
+    if (!mixed) return ORC_OK; /* equalSigns on lattice 1: no patch */
+    orc_patch_t P;
+    int st = orc_make_patch1(ls4, &P);
+    if (st) return st;
+    if (P.n_facets == 0) return ORC_OK;
+    double xv[4][3], T[3][3], det, gl[4][3];
+    for (int i = 0; i < 4; ++i) memcpy(xv[i], q->coords + 3 * q->tet_v[4 * t + i], sizeof xv[i]);
+    trafo(xv, T, &det);
+    bary_grads(T, gl);
+    /* the facets' world vertices; normal nl of facet 0 (SPatchCL::compute_normals) */
+    double nl[3];
+    {
+        double w[3][3];
+        for (int j = 0; j < 3; ++j)
+            for (int c = 0; c < 3; ++c) {
+                const double* bj = P.bary[P.facet[0][j]];
+                w[j][c] = xv[0][c] * bj[0] + xv[1][c] * bj[1] + xv[2][c] * bj[2] + xv[3][c] * bj[3];
+            }
+        double u[3], v[3];
+        for (int c = 0; c < 3; ++c) { u[c] = w[1][c] - w[0][c]; v[c] = w[2][c] - w[0][c]; }
+        nl[0] = u[1] * v[2] - u[2] * v[1];
+        nl[1] = u[2] * v[0] - u[0] * v[2];
+        nl[2] = u[0] * v[1] - u[1] * v[0];
+        const double nn = norm3(nl);
+        for (int c = 0; c < 3; ++c) nl[c] /= nn;
+    }
+    for (int f = 0; f < P.n_facets; ++f) {
+        double w[3][3];
+        for (int j = 0; j < 3; ++j) {
+            const double* bj = P.bary[P.facet[f][j]];
+            for (int c = 0; c < 3; ++c) w[j][c] = xv[0][c] * bj[0] + xv[1][c] * bj[1] + xv[2][c] * bj[2] + xv[3][c] * bj[3];
+        }
+        double u[3], v[3], cr[3];
+        for (int c = 0; c < 3; ++c) { u[c] = w[1][c] - w[0][c]; v[c] = w[2][c] - w[0][c]; }
+        cr[0] = u[1] * v[2] - u[2] * v[1];
+        cr[1] = u[2] * v[0] - u[0] * v[2];
+        cr[2] = u[0] * v[1] - u[1] * v[0];
+        const double fdet = norm3(cr) * (P.boundary[f] ? 0.5 : 1.0);
+        /* orthonormal basis U of the facet plane (Gram-Schmidt of the edges) */
+        double U[2][3];
+        const double nu = norm3(u);
+        for (int c = 0; c < 3; ++c) U[0][c] = u[c] / nu;
+        const double vu = dot3(v, U[0]);
+        double v2[3];
+        for (int c = 0; c < 3; ++c) v2[c] = v[c] - vu * U[0][c];
+        const double nv2 = norm3(v2);
+        for (int c = 0; c < 3; ++c) U[1][c] = v2[c] / nv2;
+        for (int qp = 0; qp < 7; ++qp) {
+            double bq[4];
+            for (int c = 0; c < 4; ++c)
+                bq[c] = P.bary[P.facet[f][0]][c] * Q2D_NODE[qp][0] + P.bary[P.facet[f][1]][c] * Q2D_NODE[qp][1] +
+                        P.bary[P.facet[f][2]][c] * Q2D_NODE[qp][2];
+            const double wq = fdet * Q2D_W[qp];
+            int64_t bt;
+            double bb[4], dh;
+            int it = 0;
+            st = qq_base_point(q, t, bq, &bt, bb, &dh, &it);
+            if (st) return st;
+            *newton += it;
+            ++*npts;
+            double dph[3][3], n[3];
+            qq_jacobian(q, bt, bb, dh, dph, n);
+            /* surface measure: sqrt det Gram(dph U) (surfactant/ifacetransp.cpp:865-891) */
+            double DU[2][3];
+            for (int k = 0; k < 2; ++k)
+                for (int r = 0; r < 3; ++r) DU[k][r] = dph[r][0] * U[k][0] + dph[r][1] * U[k][1] + dph[r][2] * U[k][2];
+            const double g00 = dot3(DU[0], DU[0]), g01 = dot3(DU[0], DU[1]), g11 = dot3(DU[1], DU[1]);
+            const double absd = sqrt(g00 * g11 - g01 * g01);
+            /* W = dph^T + nl (n / (nl.n) - dph nl)^T (gradient_trafo, surfactant/ifacetransp.cpp:894-914), W^-1 */
+            double dnl[3];
+            for (int r = 0; r < 3; ++r) dnl[r] = dph[r][0] * nl[0] + dph[r][1] * nl[1] + dph[r][2] * nl[2];
+            const double nln = dot3(nl, n);
+            double W[3][3], Winv[3][3];
+            for (int r = 0; r < 3; ++r)
+                for (int s = 0; s < 3; ++s) W[r][s] = dph[s][r] + nl[r] * (n[s] / nln - dnl[s]);
+            for (int col = 0; col < 3; ++col) {
+                double A4[4][4] = {{0}}, rhs[4] = {col == 0, col == 1, col == 2, 0.};
+                for (int r = 0; r < 3; ++r)
+                    for (int s = 0; s < 3; ++s) A4[r][s] = W[r][s];
+                qq_solve(3, A4, rhs);
+                for (int r = 0; r < 3; ++r) Winv[r][col] = rhs[r];
+            }
+            double phi[10], g[10][3], sg[10][3];
+            p2_vals(bq, phi);
+            p2_grads(bq, gl, g);
+            for (int i = 0; i < 10; ++i) {
+                double tg[3];
+                const double gn = dot3(g[i], nl);
+                for (int r = 0; r < 3; ++r) tg[r] = g[i][r] - gn * nl[r];
+                for (int r = 0; r < 3; ++r) sg[i][r] = Winv[r][0] * tg[0] + Winv[r][1] * tg[1] + Winv[r][2] * tg[2];
+            }
+            const double wa = wq * absd;
+            for (int i = 0; i < 10; ++i)
+                for (int j = 0; j < 10; ++j) {
+                    M[i * 10 + j] += wa * phi[i] * phi[j];
+                    A[i * 10 + j] += wa * dot3(sg[i], sg[j]);
+                }
+            /* load vector: f = c xyz at the base point */
+            qq_tet cb;
+            qq_set_tet(q, bt, &cb);
+            double y[3];
+            for (int r = 0; r < 3; ++r) {
+                double s = 0.;
+                for (int k = 0; k < 4; ++k) s += q->coords[3 * (int64_t)q->tet_v[4 * bt + k] + r] * bb[k];
+                y[r] = s;
+            }
+            const double fy = q->rhs_c * y[0] * y[1] * y[2];
+            for (int i = 0; i < 10; ++i) b[i] += wa * fy * phi[i];
+        }
+    }
+    return ORC_OK;
+}
+
+/* one base point and the Jacobian there (test aid) */
+int orc_qq_point(const orc_qq_ctx* q, int64_t t, const double b0[4], int64_t* bt, double bb[4], double* dh,
+                 double dph[9], int* iters) {
+    int st = qq_base_point(q, t, b0, bt, bb, dh, iters);
+    if (st) return st;
+    double J[3][3], n[3];
+    qq_jacobian(q, *bt, bb, *dh, J, n);
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) dph[3 * r + c] = J[r][c];
     return ORC_OK;
 }

@@ -74,6 +74,8 @@ typedef struct {
 /* SPatchCL<3>::make_patch<MergeCutPolicyCL> (geom/subtriangulation.tpp:191-228)
  * ls10: level set in P2 local order (4 vertices, 6 edges).                */
 int orc_make_patch(const double ls10[10], orc_patch_t* p);
+/* the same on PrincipalLatticeCL::instance(1) (the tet itself); ls4 at its vertices */
+int orc_make_patch1(const double ls4[4], orc_patch_t* p);
 void orc_lattice2(double verts[10][4], int tets[8][4]);
 
 /* ---- assembly: setupFESystem (surfactant/ifacetransp.cpp:566-622) ------ */
@@ -159,4 +161,29 @@ void orc_set_threads(int n);
 #ifdef __cplusplus
 }
 #endif
+
+/* ---- isoparametric P2 TraceFEM (QuaQua mapper) ----------------------------- */
+/* averaging_P2_gradient_recovery (num/gradient_recovery.cpp:82-89): grad_vert[3 nv], grad_edge[3 ne] */
+void orc_grad_recovery(int64_t nt, const int32_t* tet_v, const int32_t* tet_e, const double* coords, int64_t nv,
+                       int64_t ne, const double* ls_vert, const double* ls_edge, double* grad_vert, double* grad_edge);
+typedef struct {
+    const double* coords;
+    const int32_t* tet_v;
+    const int32_t* tet_e;
+    const double* ls_vert;   /* P2 level set */
+    const double* ls_edge;
+    const double* grad_vert; /* recovered gradient */
+    const double* grad_edge;
+    double tol, armijo;      /* Newton of the mapper */
+    int maxiter, max_damping;
+    double rhs_c;            /* load f = rhs_c x y z at the base points */
+} orc_qq_ctx;
+/* LocalMassP2CL, LocalLaplaceBeltramiP2CL (D = 1) and LocalVectorP2CL of tet t
+ * (surfactant/ifacetransp.h:2286-2402): full 10x10 M, A (row-major), b[10];
+ * npts quadrature points, newton the Newton iterations of their base points */
+int orc_qq_local(const orc_qq_ctx* q, int64_t t, double M[100], double A[100], double b[10], int* npts, int* newton);
+/* one base point of tet t's point b0 (barycentric), its quasi-distance and the Jacobian of the mapping there */
+int orc_qq_point(const orc_qq_ctx* q, int64_t t, const double b0[4], int64_t* bt, double bb[4], double* dh,
+                 double dph[9], int* iters);
+
 #endif

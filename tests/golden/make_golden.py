@@ -152,6 +152,23 @@ def ch_case(n=16, a=1.6, steps=3):
           out["block_iters"], "steps", out["steps_iters"].tolist(), "dm steps", out["dm_steps_iters"].tolist())
 
 
+def quaqua_case(n=8, a=5.0 / 3.0):
+    """Isoparametric P2 TraceFEM with the reference's QuaQua mapper on the unit sphere: the recovered
+    gradient, LocalMassP2CL, LocalLaplaceBeltramiP2CL and LocalVectorP2CL (f = 13 xyz at the base points)."""
+    d = run("quaqua", str(n), repr(a))
+    mesh = O.brick(n, a=a)
+    emap = edge_map(mesh, d["edge_v"])
+    lv, le = O.levelset(mesh, O.LS_SPHERE, [0, 0, 0, 1.0], True)
+    assert np.array_equal(lv, d["ls_vert"]) and np.array_equal(le[emap], d["ls_edge"])
+    grad_edge = np.empty((mesh.ne, 3))
+    grad_edge[emap] = d["grad_edge"].reshape(-1, 3)
+    out = dict(n=n, a=a, n_dofs=int(d["n_dofs"][0]), grad_vert=d["grad_vert"].reshape(-1, 3), grad_edge=grad_edge,
+               M_rowptr=d["M.rowptr"], M_colind=d["M.colind"].astype(np.int32), M=d["M.vals"],
+               A_rowptr=d["A.rowptr"], A_colind=d["A.colind"].astype(np.int32), A=d["A.vals"], rhs=d["rhs"])
+    np.savez_compressed(os.path.join(HERE, f"quaqua_sphere_p2_n{n}.npz"), **out)
+    print("quaqua", n, "dofs", out["n_dofs"], "nnz", len(out["M"]), "area", out["M"].sum())
+
+
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
         subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
@@ -163,3 +180,4 @@ if __name__ == "__main__":
     legacy_case()
     legacy_forms_case()
     ch_case()
+    quaqua_case()

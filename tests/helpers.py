@@ -74,3 +74,18 @@ def loc2glo(mesh, active, dof_vert, dof_edge, p2):
     if p2:
         return np.concatenate([dof_vert[mesh.tet_v[ts]], dof_edge[mesh.tet_e[ts]]], axis=1).ravel()
     return dof_vert[mesh.tet_v[ts]].ravel()
+
+
+def sparse_close(X, G, rtol=MAT_RTOL, floor=MAT_FLOOR):
+    """mat_close for two scipy sparse matrices whose patterns may differ (entries missing from one
+    count as zeros): |X_ij - G_ij| <= rtol * max(max_k |G_ik|, floor * max|G|).  Returns (ok, worst)."""
+    import scipy.sparse as sp
+
+    X, G = sp.csr_matrix(X), sp.csr_matrix(G)
+    D = abs(X - G).tocsr()
+    if D.nnz == 0:
+        return True, 0.0
+    rowmax = abs(G).max(axis=1).toarray().ravel()
+    s = np.maximum(rowmax, floor * abs(G).max())
+    worst = float(D.multiply(1.0 / s[:, None]).max())
+    return worst <= rtol, worst

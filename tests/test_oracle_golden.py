@@ -264,3 +264,48 @@ def test_vecdesc_binary_layout(golden):
     g = golden("c1_sphere_p1_n16.npz")
     assert n == len(g["x"]) == len(x) and len(raw) == 8 + 8 * n
     assert np.array_equal(x, g["x"])
+
+
+def quaqua_system(g, mesh, lv, le, grad):
+    """The oracle's isoparametric P2 forms of the fixture's case, scattered in tet order."""
+    import scipy.sparse as sp
+
+    st, na, m, dv, de, act = O.distribute_dofs(mesh, lv, le, True)
+    assert st == O.OK and m == int(g["n_dofs"])
+    tets = np.nonzero(act)[0]
+    M, A, b, npts, newton = O.quaqua_elements(mesh, lv, le, tets, grad=grad)
+    I = np.concatenate([dv[mesh.tet_v[tets]], de[mesh.tet_e[tets]]], axis=1)
+    rows, cols = np.repeat(I, 10, axis=1).ravel(), np.tile(I, (1, 10)).ravel()
+    Ms = sp.coo_matrix((M.ravel(), (rows, cols)), shape=(m, m)).tocsr()
+    As = sp.coo_matrix((A.ravel(), (rows, cols)), shape=(m, m)).tocsr()
+    rhs = np.zeros(m)
+    np.add.at(rhs, I.ravel(), b.ravel())
+    return Ms, As, rhs, npts, newton
+
+
+def test_quaqua_p2_matches_reference(golden):
+    """Isoparametric P2 TraceFEM (surfactant.cpp:1581-1640): the recovered gradient
+    (num/gradient_recovery.cpp:82), the QuaQua mapper (levelset/levelsetmapper.cpp, Newton form) and
+    LocalMassP2CL / LocalLaplaceBeltramiP2CL / LocalVectorP2CL against the reference's own accumulation on
+    the unit sphere (8^3 cubes)."""
+    import scipy.sparse as sp
+
+    from tests.helpers import sparse_close
+
+    g = golden("quaqua_sphere_p2_n8.npz")
+    n, a = int(g["n"]), float(g["a"])
+    mesh = O.brick(n, a=a)
+    lv, le = O.levelset(mesh, O.LS_SPHERE, [0, 0, 0, 1.0], True)
+    gv, ge = O.grad_recovery(mesh, lv, le)
+    assert np.abs(gv - g["grad_vert"]).max() <= 1e-14 and np.abs(ge - g["grad_edge"]).max() <= 1e-14
+    Ms, As, rhs, npts, newton = quaqua_system(g, mesh, lv, le, (gv, ge))
+    m = int(g["n_dofs"])
+    Mg = sp.csr_matrix((g["M"], g["M_colind"], g["M_rowptr"]), shape=(m, m))
+    Ag = sp.csr_matrix((g["A"], g["A_colind"], g["A_rowptr"]), shape=(m, m))
+    for X, G in ((Ms, Mg), (As, Ag)):
+        ok, err = sparse_close(X, G)
+        assert ok, err
+    ok, err = mat_close(rhs, g["rhs"])
+    assert ok, err
+    assert abs(Ms.sum() - 4 * np.pi) < 2e-2  # the discrete sphere's area
+    assert newton.sum() > 0 and newton.max() <= 10 * npts.max()
