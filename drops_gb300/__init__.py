@@ -36,6 +36,7 @@ RHS_NONE, RHS_SPHERE_XYZ, RHS_CONST = range(3)
 PREC_FP64, PREC_MIXED = 0, 1
 ORTH_MGS, ORTH_CGS2 = 0, 1
 SPMV_KERNEL_FP64, SPMV_KERNEL_PAIR = 0, 1  # tf_spmv_options
+ASM_KERNEL_PAIR, ASM_KERNEL_FP64 = 0, 1  # tf_assemble_options
 PCG_FP64_CLASSIC, PCG_FP64_CG1 = 0, 1  # tf_pcg_options
 MLP_IN, MLP_WEIGHTS = 80, 16640
 K_CLASSIFY, K_NUMBER, K_ASSEMBLE, K_PATTERN, K_SCATTER, K_SPMV, K_PCG, K_GMRES, K_LEVELSET, K_BATCH = range(10)
@@ -47,7 +48,7 @@ EXPORTS = [
     "tf_mesh_info", "tf_mesh_download", "tf_levelset_upload", "tf_levelset_analytic", "tf_levelset_download",
     "tf_distribute_dofs", "tf_create_numb_on_interface_p1", "tf_dofs_download", "tf_dofs_info", "tf_setup_interface_p1_legacy", "tf_patches_download", "tf_setup_fe_system",
     "tf_matrix_info", "tf_matrix_download", "tf_matrix_upload", "tf_lincomb", "tf_ch_block", "tf_vec_upload",
-    "tf_vec_download", "tf_vec_size", "tf_vec_fill", "tf_spmv", "tf_spmv_options", "tf_pcg_jacobi", "tf_gmres_jacobi", "tf_pcg_jacobi_noalloc", "tf_ch_steps",
+    "tf_vec_download", "tf_vec_size", "tf_vec_fill", "tf_spmv", "tf_spmv_options", "tf_assemble_options", "tf_pcg_jacobi", "tf_gmres_jacobi", "tf_pcg_jacobi_noalloc", "tf_ch_steps",
     "tf_mesh_brick_batch", "tf_levelset_analytic_batch", "tf_batch_info", "tf_batch_lincomb", "tf_batch_pcg_jacobi",
     "tf_batch_tune", "tf_batch_config", "tf_mlp_init", "tf_mlp_get_weights", "tf_mlp_set_weights", "tf_mlp_forward",
     "tf_mlp_gradient", "tf_mlp_train", "tf_ch_features", "tf_ch_steps_learned", "tf_gmres_options", "tf_pcg_options", "tf_autotune", "tf_autotune_info", "tf_setup_quaqua_p2", "tf_timing_enable",
@@ -469,6 +470,10 @@ class TraceFEM:
     def spmv_options(self, kernel=SPMV_KERNEL_FP64):
         """Kernel of tf_spmv: SPMV_KERNEL_FP64 (default) or SPMV_KERNEL_PAIR (FP32 pairs)."""
         self._check(self.L.tf_spmv_options(self.h, C.c_int(kernel)))
+
+    def assemble_options(self, kernel=ASM_KERNEL_PAIR):
+        """Arithmetic of the P2 forms: ASM_KERNEL_PAIR (default, FP32 pairs) or ASM_KERNEL_FP64."""
+        self._check(self.L.tf_assemble_options(self.h, C.c_int(kernel)))
 
     def setup_quaqua_p2(self, f_coeff=13.0, newton_tol=1e-13, newton_maxiter=100):
         """Isoparametric P2 forms with the QuaQua mapper into FORM_M, FORM_A and VEC_RHS; returns the largest

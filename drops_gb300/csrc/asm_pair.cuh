@@ -1,0 +1,259 @@
+// P2 surface forms M, A, C_n and the load vector in pair arithmetic (ff.cuh).
+//
+// The FP64 kernel k_assemble<10> keeps the FP64 pipe 86% busy: per quadrature
+// point ~190 FP64 operations for the basis and ~220 lane FMAs for the M and A
+// sums, and GB300 issues FP64 at 1/64 of the FP32 rate.  This kernel keeps
+// the per-tet work in FP64 (GetTrafoTr, the lattice patch with its cut points
+// and facet areas: the same code as k_assemble), splits the per-tet results
+// into float pairs, and runs everything per point -- quadrature node,
+// weight and its square root, the level-set normal, the projected P2
+// gradients, the load function -- and the element sums on the FP32 pipe in
+// pair arithmetic.  The sums are formed in the same point order as the FP64
+// kernel; the results differ from it by rounding (pair arithmetic carries
+// ~48 significant bits), far inside the 1e-12 row-scaled parity bound.
+// Covers the forms of the P2 path (M, A, C_n; load vector constant or
+// TF_RHS_SPHERE_XYZ); everything else runs k_assemble<10>.
+
+struct TablesFF {
+    ff q2_node[7][3], q2_w[7];
+    ff q3_node[15][4], q3_sw[15];
+};
+__constant__ TablesFF cTF;
+static bool g_tables_ff_ready[64] = {false};
+
+static ff host_split(double x) {
+    const float h = (float)x;
+    return ff{h, (float)(x - (double)h)};
+}
+
+static int ensure_tables_ff(Context* c) {
+    if (c->device >= 0 && c->device < 64 && g_tables_ff_ready[c->device]) return TF_OK;
+    Tables T;
+    build_tables(T);
+    TablesFF F;
+    for (int i = 0; i < 7; ++i) {
+        for (int j = 0; j < 3; ++j) F.q2_node[i][j] = host_split(T.q2_node[i][j]);
+        F.q2_w[i] = host_split(T.q2_w[i]);
+    }
+    for (int i = 0; i < 15; ++i) {
+        for (int j = 0; j < 4; ++j) F.q3_node[i][j] = host_split(T.q3_node[i][j]);
+        F.q3_sw[i] = host_split(T.q3_sw[i]);
+    }
+    TF_CUDA(c, cudaMemcpyToSymbol(cTF, &F, sizeof(TablesFF)));
+    if (c->device >= 0 && c->device < 64) g_tables_ff_ready[c->device] = true;
+    return TF_OK;
+}
+
+// Per warp.  The FP64 per-tet scratch (geometry, patch) is dead once split
+// into pairs, so it shares storage with the point rows.  Point rows are padded
+// to an odd number of pairs per lane (11 and 31): a lane's row starts 22 or 62
+// words after its neighbour's, so the lanes' 64-bit stores of one column fall
+// in distinct banks, and the contraction's reads of one row (one point, ten
+// columns) do too.
+struct AsmPairFp64 {
+    TetGeom g;
+    double gM[9], gC[9];
+    double ls10[10];
+    PatchSmem P;
+};
+struct AsmPairPts {
+    ff phi[32][11];  // sqrt(w) phi_i; n . grad(phi_i) sqrt(w) for the volume rule
+    ff sg[32][31];   // [3 i + c]: sqrt(w) (I - n n^T) grad(phi_i)
+};
+struct AsmPairSmem {
+    union {
+        AsmPairFp64 d;
+        AsmPairPts p;
+    } u;
+    ff gl[4][3], G[4][3], X[4][3], absdet;
+    ff fb[16][3][4], fw[16];
+    ff fx[32];  // sqrt(w) f(x_p)
+};
+
+// the unit normal grad(phi_h) / |grad(phi_h)| at barycentric b
+__device__ __noinline__ void ff_normal(const AsmPairSmem& S, const ff b[4], ff n[3]) {
+    ff v[3];
+    for (int r = 0; r < 3; ++r) {
+        v[r] = ff_mul(b[0], S.G[0][r]);
+        for (int k = 1; k < 4; ++k) v[r] = ff_fma(b[k], S.G[k][r], v[r]);
+    }
+    const ff nn = ff_fma(v[2], v[2], ff_fma(v[1], v[1], ff_mul(v[0], v[0])));
+    const ff inv = ff_rsqrt(nn);
+    for (int r = 0; r < 3; ++r) n[r] = ff_mul(v[r], inv);
+}
+
+__device__ __forceinline__ ff ff_dot3(const ff a[3], const ff b[3]) {
+    return ff_fma(a[2], b[2], ff_fma(a[1], b[1], ff_mul(a[0], b[0])));
+}
+
+// TF_RHS_SPHERE_XYZ: c * y0 y1 y2 at the closest point y of the sphere
+__device__ __noinline__ ff ff_rhs(const RhsPar& R, const ff x[3]) {
+    if (R.kind == TF_RHS_CONST) return ff_split(R.p[0]);
+    if (R.kind != TF_RHS_SPHERE_XYZ) return ff_of(0.f);
+    ff d[3];
+    for (int r = 0; r < 3; ++r) d[r] = ff_sub(x[r], ff_split(R.p[r]));
+    const ff n2 = ff_dot3(d, d);
+    const ff inv = ff_rsqrt(n2);
+    const ff dist = ff_sub(ff_mul(n2, inv), ff_split(R.p[3]));
+    const ff s = ff_mul(dist, inv);
+    ff y[3];
+    for (int r = 0; r < 3; ++r) y[r] = ff_sub(x[r], ff_mul(s, d[r]));
+    return ff_mul(ff_mul(ff_mul(ff_split(R.p[4]), y[0]), y[1]), y[2]);
+}
+
+__global__ void __launch_bounds__(32 * kAsmWarps) k_assemble_p2_pair(AsmArgs A) {
+    constexpr int NL = 10, NSYM = 55, EPL = 2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    AsmPairSmem& S = reinterpret_cast<AsmPairSmem*>(smem_raw)[wib];
+    const bool wantM = A.forms & (1u << TF_FORM_M), wantA = A.forms & (1u << TF_FORM_A);
+    const bool wantC = A.forms & (1u << TF_FORM_CN);
+    const bool wantF = A.rhs.kind != TF_RHS_NONE;
+    const int64_t nwarps = (int64_t)gridDim.x * kAsmWarps;
+
+    for (int64_t r = (int64_t)blockIdx.x * kAsmWarps + wib; r < A.n_active; r += nwarps) {
+        const int32_t t = A.active[r];
+        int32_t v[4], e[6];
+        mesh_tet(A.M, t, v, e);
+        AsmPairFp64& D = S.u.d;
+        if (lane < 4) {
+            double x[3];
+            mesh_coord(A.M, v[lane], x);
+            for (int c = 0; c < 3; ++c) D.g.X[lane][c] = x[c];
+            D.ls10[lane] = A.lsv[v[lane]];
+        } else if (lane < 10) {
+            D.ls10[lane] = A.lse[e[lane - 4]];
+        }
+        __syncwarp();
+        warp_tet_geometry(D.g, D.ls10, D.gM, D.gC, lane);
+        double ls10[10];
+        for (int k = 0; k < 10; ++k) ls10[k] = D.ls10[k];
+        __syncwarp();
+        const int nf = warp_patch(ls10, D.g.X, D.P, lane, A.status, t);
+        // per-tet data as pairs: gl, G, X (36 values), |det|, the facets' vertices and weights
+        for (int k = lane; k < 37; k += 32) {
+            const int m = k / 12, v3 = (k % 12) / 3, c = k % 3;
+            if (k == 36)
+                S.absdet = ff_split(D.g.absdet);
+            else
+                (m == 0 ? S.gl : m == 1 ? S.G : S.X)[v3][c] =
+                    ff_split(m == 0 ? D.g.gl[v3][c] : m == 1 ? D.g.G[v3][c] : D.g.X[v3][c]);
+        }
+        for (int k = lane; k < 13 * nf; k += 32) {
+            const int f = k / 13, j = k % 13;
+            if (j == 12)
+                S.fw[f] = ff_split(D.P.fw[f]);
+            else
+                S.fb[f][j >> 2][j & 3] = ff_split(D.P.fb[f][j >> 2][j & 3]);
+        }
+        __syncwarp();  // the FP64 scratch is dead from here: the point rows reuse it
+        AsmPairPts& P = S.u.p;
+
+        ffacc accM[EPL], accA[EPL], accF;
+        const int npts = 7 * nf;
+        for (int base = 0; base < npts; base += 32) {
+            const int p = base + lane;
+            if (p < npts) {
+                const int f = p / 7, q = p - 7 * (p / 7);
+                ff b[4];
+                for (int c = 0; c < 4; ++c)
+                    b[c] = ff_fma(S.fb[f][2][c], cTF.q2_node[q][2],
+                                  ff_fma(S.fb[f][1][c], cTF.q2_node[q][1], ff_mul(S.fb[f][0][c], cTF.q2_node[q][0])));
+                const ff sw = ff_sqrt(ff_mul(S.fw[f], cTF.q2_w[q]));
+                ff n[3];
+                ff_normal(S, b, n);
+                ff pg[4][3];
+                for (int k = 0; k < 4; ++k) {
+                    const ff ng = ff_dot3(n, S.gl[k]);
+                    for (int c = 0; c < 3; ++c) pg[k][c] = ff_mul(sw, ff_sub(S.gl[k][c], ff_mul(ng, n[c])));
+                }
+                ff q4[4];
+                for (int i = 0; i < 4; ++i) {
+                    q4[i] = ff_scale(b[i], 4.f);
+                    // phi_i = b_i (2 b_i - 1)
+                    P.phi[lane][i] = ff_mul(sw, ff_mul(b[i], ff_add_f(ff_scale(b[i], 2.f), -1.f)));
+                    const ff fq = ff_add_f(q4[i], -1.f);
+                    for (int c = 0; c < 3; ++c) P.sg[lane][3 * i + c] = ff_mul(fq, pg[i][c]);
+                }
+                for (int k = 0; k < 6; ++k) {
+                    const int a = ev0(k), c2 = ev1(k);
+                    P.phi[lane][4 + k] = ff_mul(sw, ff_mul(q4[a], b[c2]));
+                    for (int c = 0; c < 3; ++c)
+                        P.sg[lane][3 * (4 + k) + c] = ff_fma(q4[c2], pg[a][c], ff_mul(q4[a], pg[c2][c]));
+                }
+                if (wantF) {
+                    ff x[3];
+                    for (int c = 0; c < 3; ++c)
+                        x[c] = ff_fma(b[3], S.X[3][c],
+                                      ff_fma(b[2], S.X[2][c], ff_fma(b[1], S.X[1][c], ff_mul(b[0], S.X[0][c]))));
+                    S.fx[lane] = ff_mul(sw, ff_rhs(A.rhs, x));
+                }
+            }
+            __syncwarp();
+            const int cnt = min(32, npts - base);
+            // entries k0 = lane and k1 = lane + 32 in one pass (lanes past the 55th entry repeat
+            // the last one and do not store it)
+            const int k1 = min(lane + 32, NSYM - 1);
+            const int i0 = cT.sym_i[lane], j0 = cT.sym_j[lane], i1 = cT.sym_i[k1], j1 = cT.sym_j[k1];
+            for (int pp = 0; pp < cnt; ++pp) {
+                if (wantM) {
+                    accM[0].add_prod(P.phi[pp][j0], P.phi[pp][i0]);
+                    accM[1].add_prod(P.phi[pp][j1], P.phi[pp][i1]);
+                }
+                if (wantA)
+                    for (int c = 0; c < 3; ++c) {
+                        accA[0].add_prod(P.sg[pp][3 * j0 + c], P.sg[pp][3 * i0 + c]);
+                        accA[1].add_prod(P.sg[pp][3 * j1 + c], P.sg[pp][3 * i1 + c]);
+                    }
+            }
+            if (wantF && lane < 30) {  // 10 rows x 3 point groups (combined after the last chunk)
+                const int i = lane % 10;
+                for (int pp = lane / 10; pp < cnt; pp += 3) accF.add_prod(S.fx[pp], P.phi[pp][i]);
+            }
+            __syncwarp();
+        }
+        ff Fv = ff_of(0.f);
+        if (wantF) {  // point groups (g0 + g1) + g2
+            const ff f0 = accF.value();
+            const ff f1{__shfl_down_sync(0xffffffffu, f0.h, 10), __shfl_down_sync(0xffffffffu, f0.l, 10)};
+            const ff f2{__shfl_down_sync(0xffffffffu, f0.h, 20), __shfl_down_sync(0xffffffffu, f0.l, 20)};
+            Fv = ff_add(ff_add(f0, f1), f2);
+        }
+        ffacc accC[EPL];
+        if (wantC) {
+            // normal-gradient volume stabilisation on the 15-point Quad5 rule
+            if (lane < 15) {
+                ff b[4];
+                for (int c = 0; c < 4; ++c) b[c] = cTF.q3_node[lane][c];
+                ff n[3];
+                ff_normal(S, b, n);
+                ff ng[4];
+                for (int k = 0; k < 4; ++k) ng[k] = ff_mul(cTF.q3_sw[lane], ff_dot3(n, S.gl[k]));
+                for (int i = 0; i < 4; ++i) P.phi[lane][i] = ff_mul(ff_add_f(ff_scale(b[i], 4.f), -1.f), ng[i]);
+                for (int k = 0; k < 6; ++k) {
+                    const int a = ev0(k), c2 = ev1(k);
+                    P.phi[lane][4 + k] = ff_scale(ff_fma(b[c2], ng[a], ff_mul(b[a], ng[c2])), 4.f);
+                }
+            }
+            __syncwarp();
+            const int k1 = min(lane + 32, NSYM - 1);
+            const int i0 = cT.sym_i[lane], j0 = cT.sym_j[lane], i1 = cT.sym_i[k1], j1 = cT.sym_j[k1];
+            for (int pp = 0; pp < 15; ++pp) {
+                accC[0].add_prod(P.phi[pp][j0], P.phi[pp][i0]);
+                accC[1].add_prod(P.phi[pp][j1], P.phi[pp][i1]);
+            }
+            __syncwarp();
+        }
+        for (int qq = 0; qq < EPL; ++qq) {
+            const int k = lane + 32 * qq;
+            if (k >= NSYM) break;
+            if (wantM) A.elem[((int64_t)TF_FORM_M * A.n_active + r) * NSYM + k] = ff_to_double(accM[qq].value());
+            if (wantA) A.elem[((int64_t)TF_FORM_A * A.n_active + r) * NSYM + k] = ff_to_double(accA[qq].value());
+            if (wantC)
+                A.elem[((int64_t)TF_FORM_CN * A.n_active + r) * NSYM + k] =
+                    ff_to_double(ff_mul(accC[qq].value(), S.absdet));
+        }
+        if (wantF && lane < NL) A.elem_rhs[r * NL + lane] = ff_to_double(Fv);
+        __syncwarp();
+    }
+}

@@ -21,6 +21,7 @@
 // reference's triangulation-order accumulation, without atomics.
 #include <climits>
 
+#include "ff.cuh"
 #include "tf_internal.cuh"
 
 namespace tf {
@@ -788,6 +789,8 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
     }
 }
 
+#include "asm_pair.cuh"
+
 // ---------------------------------------------------------------------------
 // CSR pattern: contributions bucketed by row, sorted by (column, contribution)
 // ---------------------------------------------------------------------------
@@ -1039,7 +1042,14 @@ int setup_fe_system(Context* c, unsigned forms, int rhs_kind, const double* rhs_
     if (na > 0) {
         TimedLaunch tl(c, TF_K_ASSEMBLE);
         const int blocks = grid_for(c, (na + kAsmWarps - 1) / kAsmWarps, 1, 8);
-        if (p2) {
+        const bool pair = p2 && !c->asm_fp64 && !(forms & ~((1u << TF_FORM_M) | (1u << TF_FORM_A) | (1u << TF_FORM_CN))) &&
+                          (rhs_kind == TF_RHS_NONE || rhs_kind == TF_RHS_CONST || rhs_kind == TF_RHS_SPHERE_XYZ);
+        if (pair) {
+            TF_TRY(ensure_tables_ff(c));
+            const size_t sm = sizeof(AsmPairSmem) * kAsmWarps;
+            TF_CUDA(c, cudaFuncSetAttribute(k_assemble_p2_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            k_assemble_p2_pair<<<blocks, 32 * kAsmWarps, sm, c->stream>>>(A);
+        } else if (p2) {
             const size_t sm = sizeof(AsmSmem<10>) * kAsmWarps;
             TF_CUDA(c, cudaFuncSetAttribute(k_assemble<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
             k_assemble<10><<<blocks, 32 * kAsmWarps, sm, c->stream>>>(A);

@@ -108,6 +108,7 @@ int tf_create(tf_context** out, int device) {
     }
     if (const char* e = std::getenv("TF_PCG_TWO_BARRIER")) c->pcg_two_barrier = std::atoi(e) != 0;
     if (const char* e = std::getenv("TF_SPMV_PAIR")) c->spmv_pair = std::atoi(e) != 0;
+    if (const char* e = std::getenv("TF_ASM_FP64")) c->asm_fp64 = std::atoi(e) != 0;
     if (const char* e = std::getenv("TF_SPMV_SELL")) c->spmv_sell = std::atoi(e) != 0;
     if (const char* e = std::getenv("TF_SPMV_BLOCKS_PER_SM")) {
         c->spmv_blocks_per_sm = std::atoi(e);
@@ -930,6 +931,14 @@ int tf_spmv_options(tf_context* t, int kernel) {
     if (kernel != TF_SPMV_KERNEL_FP64 && kernel != TF_SPMV_KERNEL_PAIR)
         return tf::set_err(&t->c, TF_ERR_BAD_INPUT, "spmv_options: kernel");
     t->c.spmv_pair = kernel == TF_SPMV_KERNEL_PAIR;
+    return TF_OK;
+}
+
+int tf_assemble_options(tf_context* t, int kernel) {
+    CTX_CHECK(t);
+    if (kernel != TF_ASM_KERNEL_PAIR && kernel != TF_ASM_KERNEL_FP64)
+        return tf::set_err(&t->c, TF_ERR_BAD_INPUT, "assemble_options: kernel");
+    t->c.asm_fp64 = kernel == TF_ASM_KERNEL_FP64;
     return TF_OK;
 }
 

@@ -316,6 +316,7 @@ struct Context {
     int pcg_res_vcap_kb = -1;   // resident PCG: cap on the KB of matrix values kept in shared memory (-1: none)
     DBuf<float2> x_pairs;       // SpMV operand split into FP32 pairs
     bool spmv_pair = false;     // tf_spmv: FP32-pair kernel instead of the FP64-FMA one
+    bool asm_fp64 = false;      // P2 forms: the FP64 kernel instead of the FP32-pair one
     bool spmv_sell = false;     // tf_spmv: one warp per slice instead of the balanced kernel
     bool pcg_blocked = true;    // mixed PCG: contiguous slices per block, balanced within the block
     int pcg_smem_cache_kb = 0;  // mixed PCG: KB of the block's FP32 matrix slots kept in shared memory (0: off)

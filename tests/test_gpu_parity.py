@@ -231,11 +231,18 @@ def test_wind_convection_is_p1_only(ctx, golden):
         ctx.setup_fe_system([tf.FORM_N])
 
 
+@pytest.mark.parametrize("asm", [tf.ASM_KERNEL_PAIR, tf.ASM_KERNEL_FP64])
 @pytest.mark.parametrize("name,kind,par", SYSTEMS)
-def test_assembly_parity(ctx, golden, name, kind, par):
+def test_assembly_parity(ctx, golden, name, kind, par, asm):
+    """Forms and load vector against the reference's own assembly, with the P2 forms in pair arithmetic
+    (the default) and in FP64 (the P1 forms are FP64 either way)."""
     g = golden(name)
     om, p2, na, nd = setup_case(ctx, g, kind, par)
-    nnz = ctx.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN], tf.RHS_SPHERE_XYZ, [0, 0, 0, 1.0, 13.0])
+    ctx.assemble_options(asm)
+    try:
+        nnz = ctx.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN], tf.RHS_SPHERE_XYZ, [0, 0, 0, 1.0, 13.0])
+    finally:
+        ctx.assemble_options(tf.ASM_KERNEL_PAIR)
     assert nnz == len(g["colind"])
     for f, key in ((tf.FORM_M, "M"), (tf.FORM_A, "A"), (tf.FORM_CN, "C")):
         rp, ci, v = ctx.matrix(f)
@@ -349,22 +356,33 @@ def test_assembly_and_pcg_deterministic(ctx):
     assert np.array_equal(outs[0][1], outs[1][1]) and outs[0][2] == outs[1][2]
 
 
-def test_p2_against_oracle_mid_size(ctx):
-    """n = 32 P2 sphere (P2 level set): GPU vs oracle, pattern bit-exact, values 1e-12."""
-    n, a = 32, 5.0 / 3.0
+ELLIPSOID = [0.05, -0.03, 0.02, 1.2, 0.8, 0.7] + list(np.linalg.qr(np.arange(9.0).reshape(3, 3) + np.eye(3))[0].ravel())
+
+
+@pytest.mark.parametrize("asm", [tf.ASM_KERNEL_PAIR, tf.ASM_KERNEL_FP64])
+@pytest.mark.parametrize("n,kind,par", [(32, tf.LS_SPHERE, [0, 0, 0, 1.0]), (28, tf.LS_TORUS, [1.0, 0.4, 2]),
+                                        (30, tf.LS_ELLIPSOID, ELLIPSOID)])
+def test_p2_against_oracle_mid_size(ctx, n, kind, par, asm):
+    """P2 level set on n^3 cubes: GPU (pair and FP64 forms) vs oracle, pattern bit-exact, values 1e-12."""
+    a = 5.0 / 3.0
     om = brick(ctx, n, a)
-    ctx.levelset_analytic(tf.LS_SPHERE, [0, 0, 0, 1.0], True)
+    ctx.levelset_analytic(kind, par, True)
     na, nd = ctx.distribute_dofs(tf.P2IF)
-    lv, le = O.levelset(om, O.LS_SPHERE, [0, 0, 0, 1.0], True)
+    lv, le = O.levelset(om, kind, par, True)
     st, ona, ond, odv, ode, oact = O.distribute_dofs(om, lv, le, True)
     assert (na, nd) == (ona, ond)
-    ctx.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN], tf.RHS_SPHERE_XYZ, [0, 0, 0, 1.0, 13.0])
+    ctx.assemble_options(asm)
+    try:
+        ctx.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN], tf.RHS_SPHERE_XYZ, [0, 0, 0, 1.0, 13.0])
+    finally:
+        ctx.assemble_options(tf.ASM_KERNEL_PAIR)
     opts = O.make_opts(True, [O.FORM_M, O.FORM_A, O.FORM_CN], O.RHS_SPHERE_XYZ, [0, 0, 0, 1.0, 13.0])
     st, rp, ci, vals, rhs = O.assemble(om, lv, le, oact, odv, ode, ond, opts)
     for f in (tf.FORM_M, tf.FORM_A, tf.FORM_CN):
         grp, gci, gv = ctx.matrix(f)
         assert np.array_equal(grp, rp) and np.array_equal(gci, ci)
         ok, err = mat_close(gv, vals[f], grp)
+        print(n, kind, asm, f, err)
         assert ok, err
     ok, err = mat_close(ctx.vec_download(tf.VEC_RHS), rhs)
     assert ok, err
