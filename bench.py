@@ -269,6 +269,27 @@ def run_ours(args, rank, ws, dist):
     solve["mixed_vs_fp64"] = round(solve["fp64"]["ms"] / solve["mixed"]["ms"], 3)
     solve["mixed_vs_fp64_cg1"] = round(solve["fp64_cg1"]["ms"] / solve["mixed"]["ms"], 3)
 
+    # ---- P2 forms: pair-arithmetic kernel (the default) against the FP64 kernel -------------
+    asm = {}
+    for kern, name in ((tf.ASM_KERNEL_PAIR, "pair"), (tf.ASM_KERNEL_FP64, "fp64")):
+        ctx.assemble_options(kern)
+        ts = []
+        for rep in range(3):
+            ctx.flush_l2()
+            ctx.timing(True)
+            ctx.timing_reset()
+            ctx.setup_fe_system(forms, tf.RHS_SPHERE_XYZ, RHS)
+            ts.append(ctx.timing_get(tf.K_ASSEMBLE)[0])
+            ctx.timing(False)
+        asm[name] = round(statistics.median(ts), 4)
+    ctx.assemble_options(tf.ASM_KERNEL_PAIR)
+    ctx.setup_fe_system(forms, tf.RHS_SPHERE_XYZ, RHS)
+    ctx.lincomb(forms, [1.0, 1.0, H])
+    asm["pair_vs_fp64"] = round(asm["fp64"] / asm["pair"], 3)
+    asm["note"] = ("element-form kernel time (ms, median of 3, L2 flushed): M, A, C_n and the load vector; pair: "
+                   "per-point work and element sums in FP32-pair arithmetic (tf_assemble_options default), fp64: "
+                   "FP64 throughout")
+
     # ---- standalone FP64 SpMV (y_Ax) on the system matrix, cold L2 ---------
     spmv = spmv_cold(ctx, tf, state["m"], state["nnz"])
     # the same kernel on the P2 systems of twice and four times the resolution
@@ -319,13 +340,14 @@ def run_ours(args, rank, ws, dist):
     achieved = per_launch / ((ms_d / max(n_d, 1)) / 1e3) / 1e9 if ms_d > 0 else 0.0
     # DRAM bytes of one launch from an ncu capture of this workload (96^3):
     # dram__bytes_read.sum + dram__bytes_write.sum of k_pcg_cg1 / k_assemble<10>
-    traffic = {"pcg": 61.90e6, "assemble": None}.get(dom) if N == N_CUBES else None
+    traffic = {"pcg": 69.94e6, "assemble": None}.get(dom) if N == N_CUBES else None
     roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
                 "frac": round(achieved / hbm_peak, 4), "traffic": traffic, "peak_source": peak_src,
                 "bytes_model": note, "launch_ms": round(ms_d / max(n_d, 1), 4),
                 "bytes_per_launch": per_launch,
-                "traffic_note": "DRAM bytes per launch (ncu, profiles/k_pcg_cg1_p2_sphere96.md): the algorithmic "
-                                "bytes of the iterations are served from L2 after a one-time load"}
+                "traffic_note": "DRAM bytes per launch of the resident mixed PCG (ncu, "
+                                "profiles/k_pcg_res_p2_sphere96.md): the algorithmic bytes of the iterations are "
+                                "served from shared memory and L2 after a one-time load"}
 
     # ---- products of the step, for the parity check against the oracle (untimed) -----------
     products = {"xs": {}}
@@ -349,6 +371,7 @@ def run_ours(args, rank, ws, dist):
         "clocks": clocks,
         "problem": {"tets": nt, "cut_tets": na, "dofs": m, "nnz": nnz, "pcg_iters_inner": state["it"]},
         "solve_ms": solve,
+        "assemble_ms": asm,
         "spmv_fp64_cold": spmv,
         "spmv_fp64_cold_2x": spmv_big.get(2),
         "spmv_fp64_cold_4x": spmv_big.get(4),

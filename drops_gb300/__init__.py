@@ -472,7 +472,7 @@ class TraceFEM:
         self._check(self.L.tf_spmv_options(self.h, C.c_int(kernel)))
 
     def assemble_options(self, kernel=ASM_KERNEL_PAIR):
-        """Arithmetic of the P2 forms: ASM_KERNEL_PAIR (default, FP32 pairs) or ASM_KERNEL_FP64."""
+        """Arithmetic of the M, A, C_n and load-vector forms: ASM_KERNEL_PAIR (default, FP32 pairs) or ASM_KERNEL_FP64."""
         self._check(self.L.tf_assemble_options(self.h, C.c_int(kernel)))
 
     def setup_quaqua_p2(self, f_coeff=13.0, newton_tol=1e-13, newton_maxiter=100):

@@ -1,18 +1,20 @@
-// P2 surface forms M, A, C_n and the load vector in pair arithmetic (ff.cuh).
+// Surface forms M, A, C_n and the load vector in pair arithmetic (ff.cuh).
 //
-// The FP64 kernel k_assemble<10> keeps the FP64 pipe 86% busy: per quadrature
-// point ~190 FP64 operations for the basis and ~220 lane FMAs for the M and A
-// sums, and GB300 issues FP64 at 1/64 of the FP32 rate.  This kernel keeps
+// The FP64 kernels k_assemble<NL> keep the FP64 pipe 85% busy: per quadrature
+// point ~190 FP64 operations for the P2 basis and ~220 lane FMAs for the M and
+// A sums, and GB300 issues FP64 at 1/64 of the FP32 rate.  These kernels keep
 // the per-tet work in FP64 (GetTrafoTr, the lattice patch with its cut points
-// and facet areas: the same code as k_assemble), splits the per-tet results
-// into float pairs, and runs everything per point -- quadrature node,
-// weight and its square root, the level-set normal, the projected P2
-// gradients, the load function -- and the element sums on the FP32 pipe in
-// pair arithmetic.  The sums are formed in the same point order as the FP64
-// kernel; the results differ from it by rounding (pair arithmetic carries
-// ~48 significant bits), far inside the 1e-12 row-scaled parity bound.
-// Covers the forms of the P2 path (M, A, C_n; load vector constant or
-// TF_RHS_SPHERE_XYZ); everything else runs k_assemble<10>.
+// and facet areas: the same code as k_assemble), split the per-tet results
+// into float pairs, and run everything per point -- quadrature node, weight
+// and its square root, the level-set normal, the projected gradients, the
+// load function -- and the element sums on the FP32 pipe in pair arithmetic.
+// The sums are formed in the FP64 kernels' point order and point groups; the
+// results differ from them by rounding (pair arithmetic carries ~48
+// significant bits), inside the 1e-12 row-scaled parity bound.  Covered: M, A,
+// C_n (P1 and P2) and a constant or TF_RHS_SPHERE_XYZ load vector; LaplaceM
+// and N_P1P1 run k_assemble<4>.  (Pair arithmetic for the per-tet work as
+// well was measured slower: the cut points and facet areas then take more
+// issue slots on few lanes than their FP64 form takes on the FP64 pipe.)
 
 struct TablesFF {
     ff q2_node[7][3], q2_w[7];
@@ -254,6 +256,217 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble_p2_pair(AsmArgs A) 
                     ff_to_double(ff_mul(accC[qq].value(), S.absdet));
         }
         if (wantF && lane < NL) A.elem_rhs[r * NL + lane] = ff_to_double(Fv);
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// P1 forms M, A, C_n and the load vector in pair arithmetic (k_assemble_p1_pair).
+// The structure of k_assemble<4>: on a tet whose level set is linear (every
+// edge value the mean of its end values, bit for bit) the normal and the hat
+// functions' surface gradients are constant, A = (sum_p w_p) sg_i.sg_j and
+// C_n = |det| (sum_q w_q) dn_i dn_j from FP64 per-tet constants; otherwise the
+// normal, the projected gradients and the 15-point volume rule run per point.
+// Per point (node, weight and its square root, normal, gradients, load
+// function) and every sum over points run in pair arithmetic; the point
+// groups of the sums are those of k_assemble<4> (entries on 3 groups of
+// 10 lanes, the load vector on 8 groups of 4).
+// ---------------------------------------------------------------------------
+struct AsmPair1Pts {
+    ff phi[32][5];  // sqrt(w) b_i; n . grad(b_i) sqrt(w_q) for the volume rule (odd pitch: no bank conflicts)
+    ff sg[32][13];  // [3 i + c]: sqrt(w) (I - n n^T) grad(b_i)
+};
+struct AsmPair1Smem {
+    union {
+        AsmPairFp64 d;
+        AsmPair1Pts p;
+    } u;
+    ff gl[4][3], G[4][3], X[4][3];
+    ff fb[16][3][4], fw[16];
+    ff wt[32], fx[32];  // w_p; sqrt(w) f(x_p)
+    double lin_sg[4][3], lin_G[10], lin_dn[4];
+};
+
+__device__ __forceinline__ ff ff_shfl_down(ff a, int d) {
+    return ff{__shfl_down_sync(0xffffffffu, a.h, d), __shfl_down_sync(0xffffffffu, a.l, d)};
+}
+
+__device__ __noinline__ void ff_normal1(const ff (*G)[3], const ff b[4], ff n[3]) {
+    ff v[3];
+    for (int r = 0; r < 3; ++r) {
+        v[r] = ff_mul(b[0], G[0][r]);
+        for (int k = 1; k < 4; ++k) v[r] = ff_fma(b[k], G[k][r], v[r]);
+    }
+    const ff nn = ff_fma(v[2], v[2], ff_fma(v[1], v[1], ff_mul(v[0], v[0])));
+    const ff inv = ff_rsqrt(nn);
+    for (int r = 0; r < 3; ++r) n[r] = ff_mul(v[r], inv);
+}
+
+__global__ void __launch_bounds__(32 * kAsmWarps) k_assemble_p1_pair(AsmArgs A) {
+    constexpr int NL = 4, NSYM = 10;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    AsmPair1Smem& S = reinterpret_cast<AsmPair1Smem*>(smem_raw)[wib];
+    const bool wantM = A.forms & (1u << TF_FORM_M), wantA = A.forms & (1u << TF_FORM_A);
+    const bool wantC = A.forms & (1u << TF_FORM_CN);
+    const bool wantF = A.rhs.kind != TF_RHS_NONE;
+    const int64_t nwarps = (int64_t)gridDim.x * kAsmWarps;
+    double s3 = 0.;  // the 15-point rule's weight sum (linear level set: n . grad(phi_i) is constant)
+    for (int pp = 0; pp < 15; ++pp) s3 += cT.q3_w[pp];
+
+    for (int64_t r = (int64_t)blockIdx.x * kAsmWarps + wib; r < A.n_active; r += nwarps) {
+        const int32_t t = A.active[r];
+        int32_t v[4], e[6];
+        mesh_tet(A.M, t, v, e);
+        AsmPairFp64& D = S.u.d;
+        if (lane < 4) {
+            double x[3];
+            mesh_coord(A.M, v[lane], x);
+            for (int c = 0; c < 3; ++c) D.g.X[lane][c] = x[c];
+            D.ls10[lane] = A.lsv[v[lane]];
+        } else if (lane < 10) {
+            D.ls10[lane] = A.lse[e[lane - 4]];
+        }
+        __syncwarp();
+        warp_tet_geometry(D.g, D.ls10, D.gM, D.gC, lane);
+        double ls10[10];
+        for (int k = 0; k < 10; ++k) ls10[k] = D.ls10[k];
+        __syncwarp();
+        const int nf = warp_patch(ls10, D.g.X, D.P, lane, A.status, t);
+        // linear level set on the tet: every edge value the mean of its end values, bit for bit
+        bool e_lin = true;
+        if (lane < 6) {
+            const double mean = __dmul_rn(0.5, __dadd_rn(ls10[ev0(lane)], ls10[ev1(lane)]));
+            e_lin = __double_as_longlong(mean) == __double_as_longlong(ls10[4 + lane]);
+        }
+        const bool lin = __all_sync(0xffffffffu, e_lin);
+        if (lin) {  // FP64 per-tet constants, as k_assemble<4>
+            const double bc[4] = {0.25, 0.25, 0.25, 0.25};
+            double n[3];
+            unit_normal(D.g, bc, n);
+            if (lane < 12) {
+                const int vv = lane / 3, c = lane - 3 * (lane / 3);
+                const double ng = n[0] * D.g.gl[vv][0] + n[1] * D.g.gl[vv][1] + n[2] * D.g.gl[vv][2];
+                S.lin_sg[vv][c] = D.g.gl[vv][c] - ng * n[c];
+            }
+            __syncwarp();
+            if (lane < 10) {
+                int i, j;
+                sym_entry(4, lane, i, j);
+                S.lin_G[lane] = S.lin_sg[j][0] * S.lin_sg[i][0] + S.lin_sg[j][1] * S.lin_sg[i][1] +
+                                S.lin_sg[j][2] * S.lin_sg[i][2];
+            } else if (lane < 14) {
+                const int i = lane - 10;
+                S.lin_dn[i] = n[0] * D.g.gl[i][0] + n[1] * D.g.gl[i][1] + n[2] * D.g.gl[i][2];
+            }
+        }
+        const double absdet = D.g.absdet;
+        for (int k = lane; k < 36; k += 32) {
+            const int m = k / 12, v3 = (k % 12) / 3, c = k % 3;
+            (m == 0 ? S.gl : m == 1 ? S.G : S.X)[v3][c] =
+                ff_split(m == 0 ? D.g.gl[v3][c] : m == 1 ? D.g.G[v3][c] : D.g.X[v3][c]);
+        }
+        for (int k = lane; k < 13 * nf; k += 32) {
+            const int f = k / 13, j = k % 13;
+            if (j == 12)
+                S.fw[f] = ff_split(D.P.fw[f]);
+            else
+                S.fb[f][j >> 2][j & 3] = ff_split(D.P.fb[f][j >> 2][j & 3]);
+        }
+        __syncwarp();  // the FP64 scratch is dead from here: the point rows reuse it
+        AsmPair1Pts& P = S.u.p;
+
+        ffacc accM, accA, accF;
+        const int grp = lane / 10, k10 = lane % 10;
+        int ei, ej;
+        sym_entry(4, k10, ei, ej);
+        const int npts = 7 * nf;
+        for (int base = 0; base < npts; base += 32) {
+            const int p = base + lane;
+            if (p < npts) {
+                const int f = p / 7, q = p - 7 * (p / 7);
+                ff b[4];
+                for (int c = 0; c < 4; ++c)
+                    b[c] = ff_fma(S.fb[f][2][c], cTF.q2_node[q][2],
+                                  ff_fma(S.fb[f][1][c], cTF.q2_node[q][1], ff_mul(S.fb[f][0][c], cTF.q2_node[q][0])));
+                const ff w = ff_mul(S.fw[f], cTF.q2_w[q]);
+                const ff sw = ff_sqrt(w);
+                S.wt[lane] = w;
+                for (int i = 0; i < 4; ++i) P.phi[lane][i] = ff_mul(sw, b[i]);
+                if (!lin) {
+                    ff n[3];
+                    ff_normal1(S.G, b, n);
+                    for (int k = 0; k < 4; ++k) {
+                        const ff ng = ff_dot3(n, S.gl[k]);
+                        for (int c = 0; c < 3; ++c) P.sg[lane][3 * k + c] = ff_mul(sw, ff_sub(S.gl[k][c], ff_mul(ng, n[c])));
+                    }
+                }
+                if (wantF) {
+                    ff x[3];
+                    for (int c = 0; c < 3; ++c)
+                        x[c] = ff_fma(b[3], S.X[3][c],
+                                      ff_fma(b[2], S.X[2][c], ff_fma(b[1], S.X[1][c], ff_mul(b[0], S.X[0][c]))));
+                    S.fx[lane] = ff_mul(sw, ff_rhs(A.rhs, x));
+                }
+            }
+            __syncwarp();
+            const int cnt = min(32, npts - base);
+            if (grp < 3) {
+                for (int pp = grp; pp < cnt; pp += 3) {
+                    if (wantM) accM.add_prod(P.phi[pp][ej], P.phi[pp][ei]);
+                    if (wantA) {
+                        if (lin) {
+                            accA.add(S.wt[pp]);
+                        } else {
+                            accA.add_prod(P.sg[pp][3 * ej], P.sg[pp][3 * ei]);
+                            accA.add_prod(P.sg[pp][3 * ej + 1], P.sg[pp][3 * ei + 1]);
+                            accA.add_prod(P.sg[pp][3 * ej + 2], P.sg[pp][3 * ei + 2]);
+                        }
+                    }
+                }
+            }
+            if (wantF)
+                for (int pp = lane >> 2; pp < cnt; pp += 8) accF.add_prod(S.fx[pp], P.phi[pp][lane & 3]);
+            __syncwarp();
+        }
+        // point groups: entries (g0 + g1) + g2, the load vector a tree over 8 groups
+        ff vM = accM.value(), vA = accA.value(), vF = accF.value();
+        vM = ff_add(ff_add(vM, ff_shfl_down(vM, 10)), ff_shfl_down(vM, 20));
+        vA = ff_add(ff_add(vA, ff_shfl_down(vA, 10)), ff_shfl_down(vA, 20));
+        vF = ff_add(vF, ff_shfl_down(vF, 16));
+        vF = ff_add(vF, ff_shfl_down(vF, 8));
+        vF = ff_add(vF, ff_shfl_down(vF, 4));
+        double outC = 0.;
+        if (wantC) {
+            if (lin) {
+                outC = (s3 * (S.lin_dn[ej] * S.lin_dn[ei])) * absdet;
+            } else {
+                __syncwarp();
+                if (lane < 15) {
+                    ff b[4];
+                    for (int c = 0; c < 4; ++c) b[c] = cTF.q3_node[lane][c];
+                    ff n[3];
+                    ff_normal1(S.G, b, n);
+                    for (int k = 0; k < 4; ++k) P.phi[lane][k] = ff_mul(cTF.q3_sw[lane], ff_dot3(n, S.gl[k]));
+                }
+                __syncwarp();
+                ffacc accC;
+                if (grp < 3)
+                    for (int pp = grp; pp < 15; pp += 3) accC.add_prod(P.phi[pp][ej], P.phi[pp][ei]);
+                ff vC = accC.value();
+                vC = ff_add(ff_add(vC, ff_shfl_down(vC, 10)), ff_shfl_down(vC, 20));
+                outC = ff_to_double(vC) * absdet;
+            }
+        }
+        if (lane < NSYM) {
+            if (wantM) A.elem[((int64_t)TF_FORM_M * A.n_active + r) * NSYM + lane] = ff_to_double(vM);
+            if (wantA) {
+                const double a = ff_to_double(vA);
+                A.elem[((int64_t)TF_FORM_A * A.n_active + r) * NSYM + lane] = lin ? a * S.lin_G[lane] : a;
+            }
+            if (wantC) A.elem[((int64_t)TF_FORM_CN * A.n_active + r) * NSYM + lane] = outC;
+        }
+        if (wantF && lane < NL) A.elem_rhs[r * NL + lane] = ff_to_double(vF);
         __syncwarp();
     }
 }

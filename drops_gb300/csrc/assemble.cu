@@ -1049,6 +1049,12 @@ int setup_fe_system(Context* c, unsigned forms, int rhs_kind, const double* rhs_
             const size_t sm = sizeof(AsmPairSmem) * kAsmWarps;
             TF_CUDA(c, cudaFuncSetAttribute(k_assemble_p2_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
             k_assemble_p2_pair<<<blocks, 32 * kAsmWarps, sm, c->stream>>>(A);
+        } else if (!p2 && !c->asm_fp64 && !(forms & ~((1u << TF_FORM_M) | (1u << TF_FORM_A) | (1u << TF_FORM_CN))) &&
+                   (rhs_kind == TF_RHS_NONE || rhs_kind == TF_RHS_CONST || rhs_kind == TF_RHS_SPHERE_XYZ)) {
+            TF_TRY(ensure_tables_ff(c));
+            const size_t sm = sizeof(AsmPair1Smem) * kAsmWarps;
+            TF_CUDA(c, cudaFuncSetAttribute(k_assemble_p1_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            k_assemble_p1_pair<<<blocks, 32 * kAsmWarps, sm, c->stream>>>(A);
         } else if (p2) {
             const size_t sm = sizeof(AsmSmem<10>) * kAsmWarps;
             TF_CUDA(c, cudaFuncSetAttribute(k_assemble<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));

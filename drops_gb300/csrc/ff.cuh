@@ -59,7 +59,7 @@ __device__ __forceinline__ ff ff_mul_f(ff a, float b) {
     return ff_fast_two_sum(p, e);
 }
 
-// exact scaling by a power of two
+// scaling by a power of two (exact; any other factor needs ff_mul_f)
 __device__ __forceinline__ ff ff_scale(ff a, float pow2) { return ff{__fmul_rn(a.h, pow2), __fmul_rn(a.l, pow2)}; }
 
 // a + b for a float b

@@ -238,12 +238,12 @@ int tf_spmv(tf_context* ctx, int mat, int vec_x, int vec_y);
 #define TF_SPMV_KERNEL_FP64 0
 #define TF_SPMV_KERNEL_PAIR 1
 int tf_spmv_options(tf_context* ctx, int kernel);
-/* Arithmetic of the P2 element forms in tf_setup_fe_system (no reference
+/* Arithmetic of the element forms in tf_setup_fe_system (no reference
  * counterpart).  TF_ASM_KERNEL_PAIR (default): per-tet geometry and the patch
  * in FP64, the quadrature points, the basis and the element sums in FP32-pair
- * arithmetic (~48 significant bits; M, A, C_n and the constant or
- * TF_RHS_SPHERE_XYZ load vector).  TF_ASM_KERNEL_FP64: FP64 throughout.  The
- * P1 forms always use FP64.                                                   */
+ * arithmetic (~48 significant bits) for M, A, C_n (P1 and P2) and the constant
+ * or TF_RHS_SPHERE_XYZ load vector.  TF_ASM_KERNEL_FP64: FP64 throughout.
+ * LaplaceM_P1P1 and N_P1P1 always use FP64.                                    */
 #define TF_ASM_KERNEL_PAIR 0
 #define TF_ASM_KERNEL_FP64 1
 int tf_assemble_options(tf_context* ctx, int kernel);

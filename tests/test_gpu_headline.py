@@ -9,8 +9,10 @@ to relative residual 1e-10.  Checked:
     within 1e-12 of its largest entry (tests/helpers.py), with the worst plain
     per-entry relative error printed beside;
   - the mixed-precision, the FP64 and the FP64 single-barrier PCG solutions
-    within 1e-9 of the oracle's FP64 PCG solution, and the oracle's FP64
-    residual of each GPU solution.
+    within 1e-9 of the oracle's FP64 PCG solution; the FP64 residual of each
+    on the GPU's own system (host arithmetic) within 1.01e-10, and on the
+    oracle's system within 1.1e-10 (the two systems differ by the forms'
+    rounding, ~1e-12 of the row scale, which moves the residual by ~1e-12).
 The oracle (C restatement of the reference, pinned to the reference's own
 outputs by tests/test_oracle_golden.py) takes a few seconds on this size.
 """
@@ -78,12 +80,14 @@ def test_p2_sphere96_against_oracle():
     S = vals[O.FORM_M] + vals[O.FORM_A] + h * vals[O.FORM_CN]
     st, ox, oit, ores = O.pcg_jacobi(orp, oci, S, orhs, tol=1e-10)
     assert st == O.OK
+    Sg = mats[tf.FORM_M][2] + mats[tf.FORM_A][2] + h * mats[tf.FORM_CN][2]
     for name, x in xs.items():
         r = np.linalg.norm(orhs - O.spmv(orp, oci, S, x)) / np.linalg.norm(orhs)
+        rg = np.linalg.norm(rhs - O.spmv(orp, oci, Sg, x)) / np.linalg.norm(rhs)
         ok, err = sol_close(x, ox)
-        report[f"x_{name}"] = (err, r)
-        if not ok or r > 1.01e-10:
+        report[f"x_{name}"] = (err, r, rg)
+        if not ok or rg > 1.01e-10 or r > 1.1e-10:
             fails.append(f"x_{name}")
-    for k, (a, b) in report.items():
-        print(f"{k}: {a:.3e} {b:.3e}")
+    for k, vs in report.items():
+        print(f"{k}: " + " ".join(f"{a:.3e}" for a in vs))
     assert not fails, (fails, report)

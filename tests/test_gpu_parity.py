@@ -388,6 +388,37 @@ def test_p2_against_oracle_mid_size(ctx, n, kind, par, asm):
     assert ok, err
 
 
+@pytest.mark.parametrize("asm", [tf.ASM_KERNEL_PAIR, tf.ASM_KERNEL_FP64])
+@pytest.mark.parametrize("n,kind,par,p2ls", [(24, tf.LS_SPHERE, [0, 0, 0, 1.0], False),
+                                             (24, tf.LS_TORUS, [1.0, 0.4, 2], True),
+                                             (20, tf.LS_ELLIPSOID, ELLIPSOID, True)])
+def test_p1_against_oracle_mid_size(ctx, n, kind, par, p2ls, asm):
+    """P1 forms on n^3 cubes, GPU (pair and FP64) vs oracle: a P1 level set (constant normal per tet) and
+    P2 level sets (normal per point, volume rule per tet); pattern bit-exact, values 1e-12."""
+    a = 5.0 / 3.0
+    om = brick(ctx, n, a)
+    ctx.levelset_analytic(kind, par, p2ls)
+    na, nd = ctx.distribute_dofs(tf.P1IF)
+    lv, le = O.levelset(om, kind, par, p2ls)
+    st, ona, ond, odv, ode, oact = O.distribute_dofs(om, lv, le, False)
+    assert (na, nd) == (ona, ond)
+    ctx.assemble_options(asm)
+    try:
+        ctx.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN], tf.RHS_SPHERE_XYZ, [0, 0, 0, 1.0, 13.0])
+    finally:
+        ctx.assemble_options(tf.ASM_KERNEL_PAIR)
+    opts = O.make_opts(False, [O.FORM_M, O.FORM_A, O.FORM_CN], O.RHS_SPHERE_XYZ, [0, 0, 0, 1.0, 13.0])
+    st, rp, ci, vals, rhs = O.assemble(om, lv, le, oact, odv, ode, ond, opts)
+    for f in (tf.FORM_M, tf.FORM_A, tf.FORM_CN):
+        grp, gci, gv = ctx.matrix(f)
+        assert np.array_equal(grp, rp) and np.array_equal(gci, ci)
+        ok, err = mat_close(gv, vals[f], grp)
+        print(n, kind, p2ls, asm, f, err)
+        assert ok, err
+    ok, err = mat_close(ctx.vec_download(tf.VEC_RHS), rhs)
+    assert ok, err
+
+
 @pytest.mark.parametrize("method,side", [(0, "right"), (1, "left")])
 def test_gmres_parity(ctx, golden, method, side):
     """GMRES(20) with Jacobi, right (0) and left (1) preconditioning, against DROPS's own GMRES
