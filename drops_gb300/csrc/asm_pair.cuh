@@ -164,24 +164,27 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble_p2_pair(AsmArgs A) 
                 const ff sw = ff_sqrt(ff_mul(S.fw[f], cTF.q2_w[q]));
                 ff n[3];
                 ff_normal(S, b, n);
-                ff pg[4][3];
+                // The basis loops are kept rolled (their operands in L1-resident local
+                // memory): unrolled, the per-point pair code overflows the instruction cache.
+                ff pg[4][3], q4[4];
+#pragma unroll 1
                 for (int k = 0; k < 4; ++k) {
                     const ff ng = ff_dot3(n, S.gl[k]);
                     for (int c = 0; c < 3; ++c) pg[k][c] = ff_mul(sw, ff_sub(S.gl[k][c], ff_mul(ng, n[c])));
+                    q4[k] = ff_scale(b[k], 4.f);
                 }
-                ff q4[4];
-                for (int i = 0; i < 4; ++i) {
-                    q4[i] = ff_scale(b[i], 4.f);
-                    // phi_i = b_i (2 b_i - 1)
-                    P.phi[lane][i] = ff_mul(sw, ff_mul(b[i], ff_add_f(ff_scale(b[i], 2.f), -1.f)));
-                    const ff fq = ff_add_f(q4[i], -1.f);
-                    for (int c = 0; c < 3; ++c) P.sg[lane][3 * i + c] = ff_mul(fq, pg[i][c]);
-                }
-                for (int k = 0; k < 6; ++k) {
-                    const int a = ev0(k), c2 = ev1(k);
-                    P.phi[lane][4 + k] = ff_mul(sw, ff_mul(q4[a], b[c2]));
-                    for (int c = 0; c < 3; ++c)
-                        P.sg[lane][3 * (4 + k) + c] = ff_fma(q4[c2], pg[a][c], ff_mul(q4[a], pg[c2][c]));
+#pragma unroll 1
+                for (int i = 0; i < 10; ++i) {
+                    // vertex i: phi = b_i (2 b_i - 1), grad = (4 b_i - 1) grad(b_i);
+                    // edge (a, c): phi = 4 b_a b_c, grad = 4 b_c grad(b_a) + 4 b_a grad(b_c)
+                    const int a = i < 4 ? i : ev0(i - 4), c2 = i < 4 ? i : ev1(i - 4);
+                    const ff ph = i < 4 ? ff_mul(b[a], ff_add_f(ff_scale(b[a], 2.f), -1.f)) : ff_mul(q4[a], b[c2]);
+                    P.phi[lane][i] = ff_mul(sw, ph);
+                    const ff fa = i < 4 ? ff_add_f(q4[a], -1.f) : q4[c2];
+                    for (int c = 0; c < 3; ++c) {
+                        const ff t = ff_mul(fa, pg[a][c]);
+                        P.sg[lane][3 * i + c] = i < 4 ? t : ff_fma(q4[a], pg[c2][c], t);
+                    }
                 }
                 if (wantF) {
                     ff x[3];
@@ -396,6 +399,7 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble_p1_pair(AsmArgs A) 
                 if (!lin) {
                     ff n[3];
                     ff_normal1(S.G, b, n);
+#pragma unroll 1
                     for (int k = 0; k < 4; ++k) {
                         const ff ng = ff_dot3(n, S.gl[k]);
                         for (int c = 0; c < 3; ++c) P.sg[lane][3 * k + c] = ff_mul(sw, ff_sub(S.gl[k][c], ff_mul(ng, n[c])));

@@ -94,26 +94,28 @@ int tuned_pcg_kind(Context* c, CSR& A, const double* b, int* kind) {
         TF_TRY(ensure(c, c->tune_buf, (size_t)(2 * m)));
         double* x = c->tune_buf.p;
         float best = 1e30f;
-        constexpr int kIters = 40;
+        // per-iteration time as the slope between a short and a long run, so that the launch and
+        // the kernels' one-time set-up (the resident kernel loads its run into shared memory) do
+        // not count: a solve runs hundreds to thousands of iterations per launch
+        constexpr int kShort = 40, kLong = 160;
         const std::string keep_err = c->err;
         for (int k = kPcgResident; k <= kPcgCg1_256; ++k) {
-            // a short warm-up (first-use set-up of the kernel), then kIters iterations from x = 0
-            for (int pass = 0; pass < 2; ++pass) {
+            float ms_run[3] = {0.f, 0.f, 0.f};
+            for (int pass = 0; pass < 3; ++pass) {  // warm-up (first use), short, long; from x = 0
                 k_tune_fill<<<grid_for(c, m), kBlock, 0, c->stream>>>(m, x, 0.0);
                 ++c->launches;
-                int it = pass == 0 ? 4 : kIters;
+                int it = pass == 0 ? 4 : pass == 1 ? kShort : kLong;
                 double tol = 1e-300;  // never reached: every run takes exactly `it` iterations
-                float ms = 0.f;
                 const int st = timed(
                     c,
                     [&]() {
                         const int r = pcg_mixed_kind(c, A, b, x, k, &it, &tol, 1);
                         return r == TF_ERR_NOT_CONVERGED ? TF_OK : r;
                     },
-                    &ms);
+                    &ms_run[pass]);
                 if (st != TF_OK) return st;
-                if (pass == 1) e.pcg_us[k] = 1e3f * ms / (float)std::max(it, 1);
             }
+            e.pcg_us[k] = 1e3f * std::max(ms_run[2] - ms_run[1], 1e-6f) / (float)(kLong - kShort);
             if (e.pcg_us[k] < best) {
                 best = e.pcg_us[k];
                 e.pcg_kind = k;

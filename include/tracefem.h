@@ -277,8 +277,9 @@ int tf_pcg_options(tf_context* ctx, int fp64_kernel);
  * scratch vectors and keeps the fastest for the context.  on = 0 keeps the
  * fixed defaults.  tf_autotune_info reports the choice for a matrix handle:
  * spmv_us[4] and pcg_us[3] (may be NULL) the measured microseconds per SpMV /
- * per PCG iteration of each candidate, pcg_kind 0 resident, 1 512 threads,
- * 2 256 threads.                                                               */
+ * per PCG iteration of each candidate (for the PCG the slope between a 40- and
+ * a 160-iteration run, launch and set-up excluded), pcg_kind 0 resident, 1 512
+ * threads, 2 256 threads.                                                      */
 int tf_autotune(tf_context* ctx, int on);
 int tf_autotune_info(tf_context* ctx, int mat, int* spmv_threads, int* spmv_blocks_per_sm, int* pcg_kind,
                      float* spmv_us, float* pcg_us);
