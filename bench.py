@@ -777,6 +777,53 @@ def run_reference(args, rank, ws, dist):
     }
 
 
+def run_quaqua(args):
+    """Isoparametric P2 forms with the QuaQua mapper (tf_setup_quaqua_p2) on the headline mesh and surface:
+    device time per setup (recovered gradient, per-point Newton base points, mapped quadrature, scatter),
+    median of 3 after one warm-up; the discrete area (sum of M) against 4 pi as a size-independent check."""
+    import drops_gb300 as tf
+
+    ctx = tf.TraceFEM(0)
+    ctx.brick_cube(N_CUBES, HALF)
+    ctx.levelset_analytic(tf.LS_SPHERE, SPHERE, p2=True)
+    na, m = ctx.distribute_dofs(tf.P2IF)
+    newton = ctx.setup_quaqua_p2(13.0, 1e-13, 100)
+    ts = []
+    for _ in range(3):
+        ctx.flush_l2()
+        ctx.marker(6)
+        newton = ctx.setup_quaqua_p2(13.0, 1e-13, 100)
+        ctx.marker(7)
+        ts.append(ctx.elapsed_ms(6, 7))
+    rp, ci, mv = ctx.matrix(tf.FORM_M)
+    ctx.close()
+    ms = statistics.median(ts)
+    return {"ms": round(ms, 4), "cut_tets": na, "dofs": m, "nnz": len(ci), "cut_tets_per_s": round(na / (ms / 1e3), 1),
+            "newton_iters_max": newton, "area": float(mv.sum()), "area_err_vs_4pi": float(mv.sum() - 4 * np.pi),
+            "note": "tf_setup_quaqua_p2 on the 96^3 P2 sphere (f = 13xyz at the base points, Newton tol 1e-13), "
+                    "device time from the call to the assembled M, A and load vector, median of 3, L2 flushed"}
+
+
+def quaqua_cpu_sample(threads, sample=4000):
+    """The oracle's QuaQua element forms on the first `sample` cut tets of the same problem (one thread: the
+    reference accumulates them serially), as cut tets/s."""
+    from oracle import pyoracle as O
+
+    mesh = O.brick(N_CUBES, a=HALF)
+    lv, le = O.levelset(mesh, O.LS_SPHERE, SPHERE, True)
+    st, na, m, dv, de, act = O.distribute_dofs(mesh, lv, le, True)
+    tets = np.nonzero(act)[0][:sample]
+    t0 = time.perf_counter()
+    grad = O.grad_recovery(mesh, lv, le)
+    t1 = time.perf_counter()
+    O.quaqua_elements(mesh, lv, le, tets, grad=grad)
+    t2 = time.perf_counter()
+    per_tet = (t2 - t1) / len(tets)
+    total = (t1 - t0) + per_tet * na
+    return na / total, (f"the oracle on one core: recovered gradient of all {na} cut tets ({t1 - t0:.2f} s) and the "
+                        f"mapped forms of the first {len(tets)} ({t2 - t1:.2f} s), extrapolated per tet")
+
+
 def extra_workloads(args, rank, ws, dist):
     """The batch of 256 ellipsoids and the Cahn-Hilliard loop on the 128^3 torus, run after the headline
     workload with short step counts and reported inside its line (their own lines: --workload batch|ch)."""
@@ -861,6 +908,7 @@ def main():
         out["config"] = dict(out["config"], workload=f"PROFILING SIZE {args.size}^3 (not the benchmark workload)")
     if rank == 0 and ws == 1 and args.size == N_CUBES and not args.no_extra:
         out["batch"], out["ch"] = extra_workloads(args, rank, ws, dist)
+        out["quaqua"] = run_quaqua(args)
     if rank == 0:
         products = out.pop("_products")
         if ws == 1 and not args.no_cpu_baseline:
@@ -872,6 +920,10 @@ def main():
                                              f"iterations); {CPU_THREADING}",
                                    "phases": phases}
             out["parity"] = parity_report(products, ref)
+            if "quaqua" in out:
+                v, sample = quaqua_cpu_sample(threads)
+                out["quaqua"]["cpu_baseline"] = {"value": round(v, 1), "unit": "cut_tets/s", "cores": 1,
+                                                 "kind": "port", "sample": sample}
         print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()
