@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libtracefem.so")
-UNITS = ["common.cu", "mesh_levelset.cu", "dofs.cu", "assemble.cu", "krylov.cu", "krylov_res.cu", "ch.cu", "capi.cu", "noalloc.cu", "batch.cu", "mlp.cu", "learned.cu", "gmres2.cu", "tune.cu", "quaqua.cu"]
+UNITS = ["common.cu", "mesh_levelset.cu", "dofs.cu", "assemble.cu", "krylov.cu", "krylov_res.cu", "ch.cu", "capi.cu", "noalloc.cu", "batch.cu", "mlp.cu", "learned.cu", "gmres2.cu", "tune.cu", "quaqua.cu", "order.cu"]
 NO_FMA = {"mesh_levelset.cu", "learned.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -109,6 +109,7 @@ int tf_create(tf_context** out, int device) {
     if (const char* e = std::getenv("TF_PCG_TWO_BARRIER")) c->pcg_two_barrier = std::atoi(e) != 0;
     if (const char* e = std::getenv("TF_SPMV_PAIR")) c->spmv_pair = std::atoi(e) != 0;
     if (const char* e = std::getenv("TF_ASM_FP64")) c->asm_fp64 = std::atoi(e) != 0;
+    if (const char* e = std::getenv("TF_LOCALITY_ORDER")) c->locality_order = std::atoi(e) != 0;
     if (const char* e = std::getenv("TF_SPMV_SELL")) c->spmv_sell = std::atoi(e) != 0;
     if (const char* e = std::getenv("TF_SPMV_BLOCKS_PER_SM")) {
         c->spmv_blocks_per_sm = std::atoi(e);
@@ -190,6 +191,19 @@ int tf_destroy(tf_context* t) {
         tf::release(c->sell_v2f[i]);
         tf::release(c->sell_rexp[i]);
     }
+    for (int i = 0; i < TF_NUM_MATS; ++i) {
+        tf::release(c->sell_iperm[i]);
+        tf::release(c->sell_halo[i]);
+        tf::release(c->sell_coltr[i]);
+    }
+    tf::release(c->dof_order);
+    tf::release(c->order_keys);
+    tf::release(c->order_tmp);
+    tf::release(c->qq_grad);
+    tf::release(c->tune_buf);
+    tf::release(c->ch_ring);
+    tf::release(c->ch_av);
+    tf::release(c->legacy_mask);
     tf::release(c->block_rowptr);
     tf::release(c->block_colind);
     tf::release(c->user_rowptr);

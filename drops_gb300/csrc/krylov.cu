@@ -29,13 +29,16 @@ namespace tf {
 constexpr int kSigma = 512;  // rows sorted by length inside windows of 512
 static_assert(kSigma / 32 == kSellWinSlices, "slice order of the persistent kernels assumes 16 slices per window");
 
-// one block of kSigma threads per window: bitonic sort of (descending length, row)
+// one block of kSigma threads per window: bitonic sort of (descending length,
+// row); window w holds rows order[w kSigma ..] (order == nullptr: the rows in
+// numbering order)
 __global__ void __launch_bounds__(kSigma) k_sell_sort(int64_t m, const int32_t* __restrict__ rowptr,
-                                                      int32_t* __restrict__ perm) {
+                                                      const int32_t* __restrict__ order, int32_t* __restrict__ perm) {
     __shared__ uint64_t key[kSigma];
     const int t = threadIdx.x;
-    const int64_t row = (int64_t)blockIdx.x * kSigma + t;
-    if (row < m) {
+    const int64_t idx = (int64_t)blockIdx.x * kSigma + t;
+    const int64_t row = idx < m && order ? order[idx] : idx;
+    if (idx < m) {
         const uint32_t len = (uint32_t)(rowptr[row + 1] - rowptr[row]);
         key[t] = ((uint64_t)(0x7fffffffu - len) << 32) | (uint64_t)(uint32_t)row;
     } else {
@@ -124,7 +127,12 @@ int ensure_sell(Context* c, CSR& A, bool fp32) {
         TF_TRY(ensure(c, c->sell_ptr[id], (size_t)ns + 1));
         TF_TRY(ensure(c, c->scratch, sizeof(int32_t) * (size_t)(ns + 1)));
         int32_t* w = (int32_t*)c->scratch.p;
-        k_sell_sort<<<(unsigned)nwin, kSigma, 0, c->stream>>>(A.m, A.rowptr, c->sell_perm[id].p);
+        // a matrix on the current DistributeDOFs pattern takes its windows in the locality order of the DOFs
+        const int32_t* order = nullptr;
+        if (c->locality_order && A.rowptr == c->rowptr.p && A.m == c->n_dofs &&
+            c->pattern_dof_version == c->dof_version)
+            TF_TRY(dof_locality_order(c, &order));
+        k_sell_sort<<<(unsigned)nwin, kSigma, 0, c->stream>>>(A.m, A.rowptr, order, c->sell_perm[id].p);
         k_sell_width<<<grid_for(c, ns * 32), kBlock, 0, c->stream>>>(ns, A.rowptr, c->sell_perm[id].p, w);
         c->launches += 2;
         int64_t npad = 0;

@@ -38,6 +38,33 @@ struct BatchBrick {
     int64_t v0, e0, t0;
 };
 
+// Doubled brick-grid position of a node: 2 (i1, i2, i3) for a vertex, the sum
+// of its two end vertices' positions for an edge (node = vertex id, or nv +
+// edge id).  Edge classes run over the seven directions (d3 d2 d1) of the
+// Kuhn cube's edges (class -> bits 1, 2, 4, 3, 5, 6, 7), each numbered by its
+// lower vertex over the grid shortened by one in the set directions.
+__device__ inline void brick_node_grid2(const Brick& B, int64_t node, int64_t nv, int g[3]) {
+    int64_t v = node;
+    int d3 = 0, d2 = 0, d1 = 0;
+    if (node >= nv) {
+        const int64_t id = node - nv;
+        int cls = 0;
+        while (cls < 6 && id >= B.eoff[cls + 1]) ++cls;
+        const int code = (int)((0x7653421 >> (4 * cls)) & 0xf);
+        d3 = (code >> 2) & 1;
+        d2 = (code >> 1) & 1;
+        d1 = code & 1;
+        const int64_t r = id - B.eoff[cls];
+        const int64_t w1 = B.n1 + 1 - d1, w2 = B.n2 + 1 - d2;
+        const int64_t a1 = r % w1, q = r / w1, a2 = q % w2, a3 = q / w2;
+        v = (a3 * (B.n2 + 1) + a2) * (B.n1 + 1) + a1;
+    }
+    const int64_t i1 = v % (B.n1 + 1), q = v / (B.n1 + 1), i2 = q % (B.n2 + 1), i3 = q / (B.n2 + 1);
+    g[0] = (int)(2 * i1 + d1);
+    g[1] = (int)(2 * i2 + d2);
+    g[2] = (int)(2 * i3 + d3);
+}
+
 struct MeshView {
     int explicit_mesh;
     int nbatch;  // > 0: concatenation of nbatch bricks, instance after instance
@@ -256,6 +283,12 @@ struct Context {
     bool legacy_numbering = false;
     int64_t legacy_n_active = 0;  // active tets as CreateNumbOnInterfaceVertex counts them
     DBuf<int32_t> dof_vert, dof_edge, active, loc2glo;
+    // rows of the DistributeDOFs numbering in Morton order of their nodes on the
+    // brick (the SELL windows of the solvers follow it), for dof_order_version
+    DBuf<int32_t> dof_order;
+    DBuf<unsigned long long> order_keys;
+    DBuf<unsigned char> order_tmp;
+    int64_t dof_order_version = -1;
     DBuf<uint8_t> flags;
     DBuf<int32_t> keys_v, keys_e, owner;
     // pattern
@@ -317,6 +350,7 @@ struct Context {
     DBuf<float2> x_pairs;       // SpMV operand split into FP32 pairs
     bool spmv_pair = false;     // tf_spmv: FP32-pair kernel instead of the FP64-FMA one
     bool asm_fp64 = false;      // P2 forms: the FP64 kernel instead of the FP32-pair one
+    bool locality_order = true; // SELL windows of the DOF pattern in the Morton order of the DOFs' nodes
     bool spmv_sell = false;     // tf_spmv: one warp per slice instead of the balanced kernel
     bool pcg_blocked = true;    // mixed PCG: contiguous slices per block, balanced within the block
     int pcg_smem_cache_kb = 0;  // mixed PCG: KB of the block's FP32 matrix slots kept in shared memory (0: off)
@@ -432,6 +466,9 @@ struct TimedLaunch {
 // device-wide exclusive scan of int32 counts -> int64 offsets (out[n] = total)
 int exclusive_scan_i32(Context* c, const int32_t* in, int64_t* out, int64_t n);
 int exclusive_scan_i32_to_i32(Context* c, const int32_t* in, int32_t* out, int64_t n, int64_t* total);
+// *order: the rows of the current DistributeDOFs numbering in Morton order of
+// their nodes, or nullptr where there is none (explicit or batch meshes)
+int dof_locality_order(Context* c, const int32_t** order);
 int sync_status(Context* c, int* status_out);
 int fill_f64(Context* c, double* p, int64_t n, double v);
 
