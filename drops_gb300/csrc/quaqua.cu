@@ -27,9 +27,11 @@
 //   4. LocalMassP2CL, LocalLaplaceBeltramiP2CL (W^-1 applied to the tangential
 //      P2 gradients) and LocalVectorP2CL (f at the base points)
 //      (surfactant/ifacetransp.h:2286-2402).
-// One warp per active tet; lane p < 14 owns quadrature point p (two facets at
-// most on the linear interface).  The points' data go to shared memory and
-// the element entries are summed over the points in point order.
+// One half-warp per active tet (two tets per warp: an FP64 warp instruction
+// costs the same with 14 active lanes as with 32); lane p < 14 of the half
+// owns quadrature point p (two facets at most on the linear interface).  The
+// points' data go to shared memory and the element entries are summed over
+// the points in point order.
 #include "tf_internal.cuh"
 
 namespace tf {
@@ -115,11 +117,32 @@ __device__ void qq_vertex_grad(const double gl[4][3], const double f[10], int k,
 }
 
 // the recovered gradient at every node that carries an interface DOF: the
-// running mean over the node's tets in tet order
+// running mean over the node's tets in tet order.  On the uniform Kuhn brick
+// the barycentric gradients of a tet depend only on its type (its index in the
+// cube) up to the rounding of the vertex coordinates (~1e-14 relative), so the
+// block forms them once per type; the running mean's weights (n-1)/n and 1/n
+// come from a table of the same FP64 divisions.
+constexpr int kQqMaxTets = 48;  // tets around a node (24 on the Kuhn brick)
 __global__ void k_qq_grad(MeshView M, const double* __restrict__ lsv, const double* __restrict__ lse,
                           const int32_t* __restrict__ dof_vert, const int32_t* __restrict__ dof_edge,
                           double* __restrict__ grad) {
+    __shared__ double glT[6][4][3];
+    __shared__ double rmA[kQqMaxTets + 1], rmB[kQqMaxTets + 1];
     const Brick& B = M.b;
+    if (threadIdx.x < 6) {
+        double X[4][3], f[10], gl[4][3], det;
+        int32_t tv[4], te[6];
+        qq_tet_data(M, lsv, lse, threadIdx.x, X, f, tv, te);
+        qq_trafo(X, gl, &det);
+        for (int k = 0; k < 4; ++k)
+            for (int r = 0; r < 3; ++r) glT[threadIdx.x][k][r] = gl[k][r];
+    }
+    for (int k = threadIdx.x; k <= kQqMaxTets; k += blockDim.x) {
+        const double n = (double)(k > 0 ? k : 1);
+        rmA[k] = (n - 1.) / n;
+        rmB[k] = 1. / n;
+    }
+    __syncthreads();
     const int64_t nvert = M.nv, total = M.nv + M.ne;
     for (int64_t node = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; node < total;
          node += (int64_t)gridDim.x * blockDim.x) {
@@ -143,7 +166,8 @@ __global__ void k_qq_grad(MeshView M, const double* __restrict__ lsv, const doub
             v = (a3 * (B.n2 + 1) + a2) * (B.n1 + 1) + a1;
         }
         const int64_t i1 = v % (B.n1 + 1), q = v / (B.n1 + 1), i2 = q % (B.n2 + 1), i3 = q / (B.n2 + 1);
-        double avg[3] = {0., 0., 0.}, n = 0.;
+        double avg[3] = {0., 0., 0.};
+        int n = 0;
         for (int a3 = 1; a3 >= 0; --a3)
             for (int a2 = 1; a2 >= 0; --a2)
                 for (int a1 = 1; a1 >= 0; --a1) {
@@ -153,7 +177,7 @@ __global__ void k_qq_grad(MeshView M, const double* __restrict__ lsv, const doub
                     const int64_t cube = (c3 * B.n2 + c2) * B.n1 + c1;
                     for (int l = 0; l < 6; ++l) {
                         const int64_t t = 6 * cube + l;
-                        double X[4][3], f[10], gl[4][3], det;
+                        double f[10], gl[4][3];
                         int32_t tv[4], te[6];
                         brick_tet(B, t, 0, 0, tv, te);
                         int k = -1;
@@ -165,8 +189,10 @@ __global__ void k_qq_grad(MeshView M, const double* __restrict__ lsv, const doub
                                 if (te[j] == (int32_t)id) k = 4 + j;
                         }
                         if (k < 0) continue;
-                        qq_tet_data(M, lsv, lse, t, X, f, tv, te);
-                        qq_trafo(X, gl, &det);
+                        for (int j = 0; j < 4; ++j) f[j] = lsv[tv[j]];
+                        for (int j = 0; j < 6; ++j) f[4 + j] = lse[te[j]];
+                        for (int j = 0; j < 4; ++j)
+                            for (int r = 0; r < 3; ++r) gl[j][r] = glT[l][j][r];
                         double val[3];
                         if (k < 4) {
                             qq_vertex_grad(gl, f, k, val);
@@ -176,8 +202,8 @@ __global__ void k_qq_grad(MeshView M, const double* __restrict__ lsv, const doub
                             qq_vertex_grad(gl, f, ev1(k - 4), gb);
                             for (int r = 0; r < 3; ++r) val[r] = 0.5 * (ga[r] + gb[r]);
                         }
-                        n += 1.;
-                        for (int r = 0; r < 3; ++r) avg[r] = ((n - 1.) / n) * avg[r] + (1. / n) * val[r];
+                        n = n < kQqMaxTets ? n + 1 : n;
+                        for (int r = 0; r < 3; ++r) avg[r] = rmA[n] * avg[r] + rmB[n] * val[r];
                     }
                 }
         for (int r = 0; r < 3; ++r) grad[3 * (int64_t)dof + r] = avg[r];
@@ -268,21 +294,25 @@ __device__ inline double dt3(const double a[3], const double b[3]) { return a[0]
 __global__ void __launch_bounds__(32 * kQqWarps) k_qq_assemble(QqArgs a) {
     extern __shared__ __align__(16) unsigned char qq_dyn[];
     QqSmem* all = reinterpret_cast<QqSmem*>(qq_dyn);
-    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    QqSmem& S = all[wl];
+    const int wl = threadIdx.x >> 5, half = (threadIdx.x >> 4) & 1, lane = threadIdx.x & 15;
+    QqSmem& S = all[2 * wl + half];
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5, nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t qa = gw; qa < a.n_active; qa += nw) {
-        const int64_t t = a.active[qa];
-        if (lane == 0) {
-            int32_t tv[4], te[6];
-            qq_tet_data(a.M, a.ls_vert, a.ls_edge, t, S.X, S.f, tv, te);
-            double det;
-            qq_trafo(S.X, S.gl, &det);
-            S.h = cbrt(fabs(det));
-        }
-        if (lane < 30) {
-            const int k = lane / 3, r = lane - 3 * k;
-            S.gh[k][r] = a.grad[3 * (int64_t)a.loc2glo[qa * 10 + k] + r];
+    for (int64_t pr = gw; 2 * pr < a.n_active; pr += nw) {
+        const int64_t qa = 2 * pr + half;
+        const bool live = qa < a.n_active;  // the second half of the last pair may have no tet
+        if (live) {
+            const int64_t t = a.active[qa];
+            if (lane == 0) {
+                int32_t tv[4], te[6];
+                qq_tet_data(a.M, a.ls_vert, a.ls_edge, t, S.X, S.f, tv, te);
+                double det;
+                qq_trafo(S.X, S.gl, &det);
+                S.h = cbrt(fabs(det));
+            }
+            for (int q = lane; q < 30; q += 16) {
+                const int k = q / 3, r = q - 3 * k;
+                S.gh[k][r] = a.grad[3 * (int64_t)a.loc2glo[qa * 10 + k] + r];
+            }
         }
         __syncwarp();
         // the linear interface of the vertex values (SignTraitsCL / RefPatchCL on one sub-tet)
@@ -300,8 +330,8 @@ __global__ void __launch_bounds__(32 * kQqWarps) k_qq_assemble(QqArgs a) {
             for (int e = 0; e < 6 && nr < 4; ++e)
                 if (sg[ev0(e)] * sg[ev1(e)] == -1) cut[nr++] = e + 4;
         }
-        if (nz == 4 && lane == 0) atomicCAS(a.status, 0, TF_ERR_ZERO_PATTERN);
-        const int nf = nr >= 3 ? nr - 2 : 0;
+        if (live && nz == 4 && lane == 0) atomicCAS(a.status, 0, TF_ERR_ZERO_PATTERN);
+        const int nf = live && nr >= 3 ? nr - 2 : 0;
         const bool bnd = nz == 3;
         const int npts = 7 * nf;
         // facet vertices (barycentric) of facet f, vertex j
@@ -493,7 +523,7 @@ __global__ void __launch_bounds__(32 * kQqWarps) k_qq_assemble(QqArgs a) {
         }
         __syncwarp();
         // element entries, summed over the points in point order: 55 M, 55 A, 10 b
-        for (int e = lane; e < 120; e += 32) {
+        for (int e = lane; e < 120 && live; e += 16) {
             double s = 0.;
             if (e < 110) {
                 const int k = e < 55 ? e : e - 55;
@@ -565,9 +595,10 @@ int quaqua_elements(Context* c, double rhs_c, double tol, int maxiter, int* newt
     TF_CUDA(c, cudaMemsetAsync(c->status.p, 0, 4 * sizeof(int), c->stream));
     if (na > 0) {
         TimedLaunch tl(c, TF_K_ASSEMBLE);
-        const size_t sm = sizeof(QqSmem) * kQqWarps;
+        const size_t sm = sizeof(QqSmem) * 2 * kQqWarps;
         TF_CUDA(c, cudaFuncSetAttribute(k_qq_assemble, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_qq_assemble<<<grid_for(c, (na + kQqWarps - 1) / kQqWarps, 1, 8), 32 * kQqWarps, sm, c->stream>>>(a);
+        const int64_t pairs = (na + 1) / 2;
+        k_qq_assemble<<<grid_for(c, (pairs + kQqWarps - 1) / kQqWarps, 1, 8), 32 * kQqWarps, sm, c->stream>>>(a);
         ++c->launches;
         TF_CUDA(c, cudaGetLastError());
     }

@@ -181,3 +181,30 @@ def test_autotune_picks_the_fastest_measured_shape():
         ctx.vec_fill(tf.VEC_X, nd, 0.0)
         st, it2, res = ctx.pcg_jacobi(tf.MAT_SYS, tf.VEC_RHS, tf.VEC_X, tol=1e-10, precision=tf.PREC_MIXED)
         assert st == tf.OK and ctx.autotune_info(tf.MAT_SYS)[2] == kind
+
+
+def test_locality_order_across_numberings():
+    """The solvers' SELL windows follow the Morton order of the DOFs' nodes (order.cu).  One context
+    switches between P2 and P1 numberings (a P1 numbering leaves the edge DOF array unset) and solves each
+    system in mixed and FP64 precision; the solutions match those of a context without the order."""
+    from drops_gb300 import build
+
+    build.build()
+    os.environ["TF_LOCALITY_ORDER"] = "0"
+    try:
+        plain = tf.TraceFEM()
+    finally:
+        del os.environ["TF_LOCALITY_ORDER"]
+    with tf.TraceFEM() as ctx:
+        for n, fe in ((24, tf.P2IF), (16, tf.P1IF), (16, tf.P2IF), (22, tf.P1IF)):
+            for prec in (tf.PREC_MIXED, tf.PREC_FP64):
+                out = []
+                for c in (ctx, plain):
+                    nd = _system(c, n, fe)
+                    st, it, res, x = _solve(c, nd, prec, tol=1e-10)
+                    assert st == tf.OK and res <= 1e-10
+                    assert _fp64_resid(c, x) <= 1.01e-10
+                    out.append(x)
+                ok, err = sol_close(out[0], out[1])
+                assert ok, (n, fe, prec, err)
+    plain.close()
