@@ -24,6 +24,9 @@ namespace tf {
 constexpr int kGm2MaxR = 64;
 constexpr int kGm2Stride = kGm2MaxR + 2;  // partials per block
 constexpr int kGm2Warps = kKryThreads / 32;
+constexpr int kGm2Chunks = 10;                   // 32-block chunks the master reads per value
+constexpr int kGm2MaxBlocks = 32 * kGm2Chunks;   // blocks of the launch (two per SM on 152 SMs: 304)
+constexpr int kGm2Group = 4;                     // values a master warp reads at once
 
 struct Gm2Scal {
     double normb, resid, beta;
@@ -106,27 +109,36 @@ __device__ bool gm2_step(const GridSync& g, const S* part, int n, Gm2Scal* gsc, 
     }
     __syncthreads();
     if (st != 0) return false;
-    // warp w sums the values k = w, w + 8, ...; its lanes split the blocks
-    // (independent loads in flight), then a fixed warp tree per value
+    // The partials are value-major (part[k][block]).  Warp w sums the values
+    // k = w, w + 8, ..., kGm2Group of them at a time: its lanes load the
+    // blocks lane, lane + 32, ... of each, all kGm2Group x kGm2Chunks loads
+    // independent and coalesced (one round trip), then add them in chunk
+    // order and close with a fixed warp tree, so the sum does not depend on
+    // timing.  (Block-major partials read block after block took about ten
+    // dependent round trips per grid step.)
     {
-        constexpr int kPerWarp = (kGm2Stride + kGm2Warps - 1) / kGm2Warps;
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        S acc[kPerWarp];
+        const int nb = (int)gridDim.x;
+        for (int k0 = warp; k0 < n; k0 += kGm2Warps * kGm2Group) {
+            S v[kGm2Group][kGm2Chunks];
 #pragma unroll
-        for (int q = 0; q < kPerWarp; ++q) acc[q] = S(0);
-        for (unsigned b = lane; b < gridDim.x; b += 32) {
-            const S* pb = part + (size_t)b * kGm2Stride;
+            for (int g = 0; g < kGm2Group; ++g) {
+                const int k = k0 + g * kGm2Warps;
 #pragma unroll
-            for (int q = 0; q < kPerWarp; ++q) {
-                const int k = warp + q * kGm2Warps;
-                if (k < n) acc[q] += __ldcg(pb + k);
+                for (int j = 0; j < kGm2Chunks; ++j) {
+                    const int b = lane + 32 * j;
+                    v[g][j] = k < n && b < nb ? __ldcg(part + (size_t)k * nb + b) : S(0);
+                }
             }
-        }
 #pragma unroll
-        for (int q = 0; q < kPerWarp; ++q) {
-            const S v = warp_sum(acc[q]);
-            const int k = warp + q * kGm2Warps;
-            if (lane == 0 && k < n) sums[k] = v;
+            for (int g = 0; g < kGm2Group; ++g) {
+                S acc = S(0);
+#pragma unroll
+                for (int j = 0; j < kGm2Chunks; ++j) acc += v[g][j];
+                acc = warp_sum(acc);
+                const int k = k0 + g * kGm2Warps;
+                if (lane == 0 && k < n) sums[k] = acc;
+            }
         }
     }
     __syncthreads();
@@ -144,14 +156,14 @@ __device__ bool gm2_step(const GridSync& g, const S* part, int n, Gm2Scal* gsc, 
     return true;
 }
 
-// warp partials (wred[k][warp]) -> block partials part[block][k]
+// warp partials (wred[k][warp]) -> block partials part[k][block] (value-major)
 template <class S>
 __device__ __forceinline__ void gm2_block_partials(S (*wred)[kGm2Warps], int n, S* part) {
     __syncthreads();
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
         S x = S(0);
         for (int w = 0; w < kGm2Warps; ++w) x += wred[k][w];
-        part[(size_t)blockIdx.x * kGm2Stride + k] = x;
+        part[(size_t)k * gridDim.x + blockIdx.x] = x;
     }
 }
 
@@ -461,6 +473,7 @@ static int run_gmres2(Context* c, CSR& A, const double* b, double* x, int R, int
     const void* fn = (const void*)k_gmres2<V>;
     int blocks = 0;
     TF_TRY(coop_blocks(c, fn, A.sell.nslices, &blocks, kKryThreads));
+    blocks = std::min(blocks, kGm2MaxBlocks);  // the master's partial reads cover kGm2MaxBlocks blocks
     // H (R+1) x R, cs R, sn R, s R+1, y R, scl R+1, coef R+1
     const size_t small = (size_t)(R + 1) * R + 6 * (size_t)R + 3;
     DBuf<V>& basis = *reinterpret_cast<DBuf<V>*>(sizeof(V) == 4 ? (void*)&c->gm2_v32 : (void*)&c->gm2_v64);
