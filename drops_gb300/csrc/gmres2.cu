@@ -50,6 +50,7 @@ struct Gm2Args {
     Gm2Scal* sc;
     V* small;             // H (R+1) x R column-major, cs[R], sn[R], s[R+1], y[R], scl[R+1], coef[R+1]
     GridSync gs;
+    unsigned* mcount;  // grid-step arrivals (monotone)
     int R, max_iter, rel;
     double tol, inner_floor;
     int* out_iter;
@@ -66,19 +67,36 @@ struct Gm2Args {
 // releases the others, which copy it.  The Arnoldi dots of the FP32 cycles
 // reduce in FP32 all the way (S = float): FP64 instructions tie up the FP64
 // pipe whatever the number of active lanes, and the basis itself is FP32.
+// Grid-step synchronisation words: arrivals of the non-master blocks on a
+// monotone counter (one release reduction each), the master's release of the
+// step on the generation word (also bumped by grid_barrier, so monotone too).
+// Every block keeps the generation and the step count it expects, so no word
+// is read before arriving.
+struct Gm2Sync {
+    unsigned gen = 0;    // generation word value after the last grid step or barrier
+    unsigned steps = 0;  // grid steps so far
+};
+__device__ __forceinline__ void gm2_red_release_add(unsigned* p, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned gm2_ld_relaxed(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
 template <class S, class F>
-__device__ bool gm2_step(const GridSync& g, const S* part, int n, Gm2Scal* gsc, Gm2Scal& ssc, F f) {
+__device__ bool gm2_step(const GridSync& g, unsigned* mcount, Gm2Sync& sy, const S* part, int n, Gm2Scal* gsc,
+                         Gm2Scal& ssc, F f) {
     __shared__ int st;
     __shared__ S sums[kGm2Stride];
+    const unsigned target_gen = sy.gen + 1;
     __syncthreads();
     if (blockIdx.x != 0) {
         if (threadIdx.x == 0) {
-            volatile unsigned* vgen = g.gen;
-            const unsigned my = *vgen;
-            __threadfence();
-            atomicAdd(g.count, 1u);
+            gm2_red_release_add(mcount, 1u);  // releases the block's partials (ordered by the barrier above)
             long long spins = 0;
-            while (*vgen == my) {
+            while ((int)(gm2_ld_relaxed(g.gen) - target_gen) < 0) {
                 if (++spins > kSpinLimit) {
                     atomicCAS(g.status, 0, TF_ERR_WATCHDOG);
                     break;
@@ -86,18 +104,23 @@ __device__ bool gm2_step(const GridSync& g, const S* part, int n, Gm2Scal* gsc, 
                 if (spins > 256) __nanosleep(32);
             }
             __threadfence();
-            st = *((volatile int*)g.status);
+            // the published state and the status in one round of loads
             const unsigned long long* src = reinterpret_cast<const unsigned long long*>(gsc);
             unsigned long long* dst = reinterpret_cast<unsigned long long*>(&ssc);
+            const int stv = __ldcg(g.status);
+#pragma unroll
             for (int k = 0; k < (int)(sizeof(Gm2Scal) / 8); ++k) dst[k] = __ldcg(src + k);
+            st = stv;
         }
         __syncthreads();
+        sy.gen = target_gen;
+        ++sy.steps;
         return st == 0;
     }
     if (threadIdx.x == 0) {
-        volatile unsigned* vcount = g.count;
+        const unsigned target = (sy.steps + 1) * (gridDim.x - 1);
         long long spins = 0;
-        while (*vcount != gridDim.x - 1) {
+        while ((int)(gm2_ld_relaxed(mcount) - target) < 0) {
             if (++spins > kSpinLimit) {
                 atomicCAS(g.status, 0, TF_ERR_WATCHDOG);
                 break;
@@ -105,7 +128,7 @@ __device__ bool gm2_step(const GridSync& g, const S* part, int n, Gm2Scal* gsc, 
             if (spins > 256) __nanosleep(32);
         }
         __threadfence();
-        st = *((volatile int*)g.status);
+        st = __ldcg(g.status);
     }
     __syncthreads();
     if (st != 0) return false;
@@ -147,12 +170,11 @@ __device__ bool gm2_step(const GridSync& g, const S* part, int n, Gm2Scal* gsc, 
         const unsigned long long* src = reinterpret_cast<const unsigned long long*>(&ssc);
         unsigned long long* dst = reinterpret_cast<unsigned long long*>(gsc);
         for (int k = 0; k < (int)(sizeof(Gm2Scal) / 8); ++k) dst[k] = src[k];
-        __threadfence();
-        *g.count = 0;
-        __threadfence();
-        atomicAdd(g.gen, 1u);
+        gm2_red_release_add(g.gen, 1u);  // releases the state and what f published
     }
     __syncthreads();
+    sy.gen = target_gen;
+    ++sy.steps;
     return true;
 }
 
@@ -189,6 +211,7 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres2(Gm2Args<V> a) {
     const double tol = a.tol, inner_floor = a.inner_floor;
     const int max_iter = a.max_iter, rel = a.rel;
     bool first = true;
+    Gm2Sync sy;
 
     for (;;) {
         // ---- cycle start: r = b - A x (FP64) into basis_0; |r|^2, |b|^2 ----
@@ -212,7 +235,7 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres2(Gm2Args<V> a) {
             }
             gm2_block_partials<double>(wres, 2, part64);
             const bool init = first;
-            if (!gm2_step<double>(a.gs, part64, 2, a.sc, sc, [&](const double* t, Gm2Scal& g) {
+            if (!gm2_step<double>(a.gs, a.mcount, sy, part64, 2, a.sc, sc, [&](const double* t, Gm2Scal& g) {
                     if (init) {
                         double nb = sqrt(t[1]);
                         if (nb == 0.0 || !rel) nb = 1.0;
@@ -258,7 +281,7 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres2(Gm2Args<V> a) {
                 }
             }
             gm2_block_partials<V>(wred, i + 1, partV);
-            if (!gm2_step<V>(a.gs, partV, i + 1, a.sc, sc, [&](const V* t, Gm2Scal& g) {
+            if (!gm2_step<V>(a.gs, a.mcount, sy, partV, i + 1, a.sc, sc, [&](const V* t, Gm2Scal& g) {
                     for (int k = 0; k <= i; ++k) {
                         coef[k] = (V)t[k];
                         H[(size_t)i * (R + 1) + k] = (V)t[k];
@@ -305,7 +328,7 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres2(Gm2Args<V> a) {
                 }
                 if (pass == 0) {
                     gm2_block_partials<V>(wred, i + 1, partV);
-                    if (!gm2_step<V>(a.gs, partV, i + 1, a.sc, sc, [&](const V* t, Gm2Scal& g) {
+                    if (!gm2_step<V>(a.gs, a.mcount, sy, partV, i + 1, a.sc, sc, [&](const V* t, Gm2Scal& g) {
                             for (int k = 0; k <= i; ++k) {
                                 coef[k] = (V)t[k];
                                 H[(size_t)i * (R + 1) + k] += (V)t[k];
@@ -314,7 +337,7 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres2(Gm2Args<V> a) {
                         return;
                 } else {
                     gm2_block_partials<V>(wred, 1, partV);
-                    if (!gm2_step<V>(a.gs, partV, 1, a.sc, sc, [&](const V* t, Gm2Scal& g) {
+                    if (!gm2_step<V>(a.gs, a.mcount, sy, partV, 1, a.sc, sc, [&](const V* t, Gm2Scal& g) {
                             V* hc = H + (size_t)i * (R + 1);
                             const V hn = (V)sqrt(t[0]);
                             hc[i + 1] = hn;
@@ -383,6 +406,7 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres2(Gm2Args<V> a) {
                 }
             }
             if (!grid_barrier(a.gs)) return;
+            ++sy.gen;  // the barrier's last arrival bumped the generation word
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -479,10 +503,10 @@ static int run_gmres2(Context* c, CSR& A, const double* b, double* x, int R, int
     DBuf<V>& basis = *reinterpret_cast<DBuf<V>*>(sizeof(V) == 4 ? (void*)&c->gm2_v32 : (void*)&c->gm2_v64);
     TF_TRY(ensure(c, basis, (size_t)(R + 1) * m + small));
     TF_TRY(ensure(c, c->kry_part, (size_t)blocks * kGm2Stride + 16 + sizeof(Gm2Scal) / 8));
-    TF_TRY(ensure(c, c->kry_bar, 2));
+    TF_TRY(ensure(c, c->kry_bar, 4));
     TF_TRY(ensure(c, c->kry_iters, 2));
     TF_TRY(ensure(c, c->kry_resid, 1));
-    TF_CUDA(c, cudaMemsetAsync(c->kry_bar.p, 0, 2 * sizeof(unsigned), c->stream));
+    TF_CUDA(c, cudaMemsetAsync(c->kry_bar.p, 0, 4 * sizeof(unsigned), c->stream));
     TF_CUDA(c, cudaMemsetAsync(c->status.p, 0, 4 * sizeof(int), c->stream));
     Gm2Args<V> g{};
     g.m = m;
@@ -501,6 +525,7 @@ static int run_gmres2(Context* c, CSR& A, const double* b, double* x, int R, int
     g.part = c->kry_part.p;
     g.sc = reinterpret_cast<Gm2Scal*>(c->kry_part.p + (size_t)blocks * kGm2Stride + 16);
     g.gs = GridSync{c->kry_bar.p, c->kry_bar.p + 1, c->status.p};
+    g.mcount = c->kry_bar.p + 2;
     g.R = R;
     g.max_iter = *max_iter;
     g.rel = rel;
