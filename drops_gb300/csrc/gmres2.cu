@@ -274,10 +274,17 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres2(Gm2Args<V> a) {
                 const V acc = sell_row<V>(a.ptr, a.col, a.bval, sl, lane, [&](int32_t j) { return sci * kld(Vi + j); });
                 const int32_t row = __ldg(a.perm + sl * 32 + lane);
                 if (row >= 0) W[row] = acc;
-                for (int k = 0; k <= i; ++k) {
-                    V t = row >= 0 ? scl[k] * kld(a.basis + (size_t)k * m + row) * acc : V(0);
-                    t = warp_sum(t);
-                    if (lane == 0) wred[k][warp] += t;
+                // eight dots per transposing warp butterfly (9 shuffles instead of 40)
+                for (int k0 = 0; k0 <= i; k0 += 8) {
+                    V t8[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const int k = k0 + q;
+                        t8[q] = row >= 0 && k <= i ? scl[k] * kld(a.basis + (size_t)k * m + row) * acc : V(0);
+                    }
+                    const V tot = warp_sum8(t8, lane);
+                    const int k = k0 + warp_sum8_index(lane);
+                    if ((lane & 3) == 0 && k <= i) wred[k][warp] += tot;
                 }
             }
             gm2_block_partials<V>(wred, i + 1, partV);
@@ -309,14 +316,23 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres2(Gm2Args<V> a) {
                         if (in[q]) W[e] = w;
                     }
                     if (pass == 0) {
-                        for (int k = 0; k <= i; ++k) {
-                            const V* Vk = a.basis + (size_t)k * m;
-                            V t = V(0);
+                        for (int k0 = 0; k0 <= i; k0 += 8) {
+                            V t8[8];
 #pragma unroll
-                            for (int q = 0; q < 4; ++q)
-                                if (in[q]) t += scl[k] * kld(Vk + e0 + q * nth) * wv[q];
-                            t = warp_sum(t);
-                            if (lane == 0) wred[k][warp] += t;
+                            for (int g = 0; g < 8; ++g) {
+                                const int k = k0 + g;
+                                V t = V(0);
+                                if (k <= i) {
+                                    const V* Vk = a.basis + (size_t)k * m;
+#pragma unroll
+                                    for (int q = 0; q < 4; ++q)
+                                        if (in[q]) t += scl[k] * kld(Vk + e0 + q * nth) * wv[q];
+                                }
+                                t8[g] = t;
+                            }
+                            const V tot = warp_sum8(t8, lane);
+                            const int k = k0 + warp_sum8_index(lane);
+                            if ((lane & 3) == 0 && k <= i) wred[k][warp] += tot;
                         }
                     } else {
                         V t = V(0);
