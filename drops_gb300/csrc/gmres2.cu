@@ -8,8 +8,9 @@
 // (k_gmres, one grid barrier per projection, about restart/2 barriers per
 // Arnoldi step), CGS2 projects against all basis vectors at once: an Arnoldi
 // step costs three grid barriers, (1) w = B v_i fused with the first
-// projection dots, (2) first update fused with the second dots, (3) second
-// update fused with |w|^2.  The preconditioned operator B = A P^{-1} (P point
+// projection dots, (2) first update fused with the second dots and |w1|^2
+// (|w2|^2 = |w1|^2 - |h'|^2 on the orthonormal basis), (3) second update and a
+// plain grid barrier.  The preconditioned operator B = A P^{-1} (P point
 // or nodal 2x2 block Jacobi) is formed once per matrix in SELL order, so the
 // Arnoldi loop is a plain SpMV; x += P^{-1} V y at the end of a cycle.  The
 // Hessenberg matrix, Givens rotations and the small triangular solve are
@@ -295,7 +296,10 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres2(Gm2Args<V> a) {
                     }
                 }))
                 return;
-            // (2) w -= sum_k h_k v_k, second dots; (3) w -= sum_k h'_k v_k, |w|^2
+            // (2) w1 = w - sum_k h_k v_k with the second dots h'_k = <v_k, w1> and |w1|^2 (one grid
+            // step: the master forms |w2|^2 = |w1|^2 - sum_k h'_k^2, the basis being orthonormal, and
+            // with it the rotation and the stopping test); (3) w2 = w1 - sum_k h'_k v_k, then a grid
+            // barrier, as the next product gathers w2 across blocks
             for (int pass = 0; pass < 2; ++pass) {
                 for (int k = threadIdx.x; k <= i + 1; k += blockDim.x)
                     for (int w = 0; w < kGm2Warps; ++w) wred[k][w] = V(0);
@@ -316,7 +320,8 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres2(Gm2Args<V> a) {
                         if (in[q]) W[e] = w;
                     }
                     if (pass == 0) {
-                        for (int k0 = 0; k0 <= i; k0 += 8) {
+                        // values 0..i: <v_k, w1>; value i + 1: |w1|^2
+                        for (int k0 = 0; k0 <= i + 1; k0 += 8) {
                             V t8[8];
 #pragma unroll
                             for (int g = 0; g < 8; ++g) {
@@ -327,75 +332,73 @@ __global__ void __launch_bounds__(kKryThreads, 2) k_gmres2(Gm2Args<V> a) {
 #pragma unroll
                                     for (int q = 0; q < 4; ++q)
                                         if (in[q]) t += scl[k] * kld(Vk + e0 + q * nth) * wv[q];
+                                } else if (k == i + 1) {
+#pragma unroll
+                                    for (int q = 0; q < 4; ++q) t += wv[q] * wv[q];
                                 }
                                 t8[g] = t;
                             }
                             const V tot = warp_sum8(t8, lane);
                             const int k = k0 + warp_sum8_index(lane);
-                            if ((lane & 3) == 0 && k <= i) wred[k][warp] += tot;
+                            if ((lane & 3) == 0 && k <= i + 1) wred[k][warp] += tot;
                         }
-                    } else {
-                        V t = V(0);
-#pragma unroll
-                        for (int q = 0; q < 4; ++q) t += wv[q] * wv[q];
-                        t = warp_sum(t);
-                        if (lane == 0) wred[0][warp] += t;
                     }
                 }
-                if (pass == 0) {
-                    gm2_block_partials<V>(wred, i + 1, partV);
-                    if (!gm2_step<V>(a.gs, a.mcount, sy, partV, i + 1, a.sc, sc, [&](const V* t, Gm2Scal& g) {
-                            for (int k = 0; k <= i; ++k) {
-                                coef[k] = (V)t[k];
-                                H[(size_t)i * (R + 1) + k] += (V)t[k];
-                            }
-                        }))
-                        return;
-                } else {
-                    gm2_block_partials<V>(wred, 1, partV);
-                    if (!gm2_step<V>(a.gs, a.mcount, sy, partV, 1, a.sc, sc, [&](const V* t, Gm2Scal& g) {
-                            V* hc = H + (size_t)i * (R + 1);
-                            const V hn = (V)sqrt(t[0]);
-                            hc[i + 1] = hn;
-                            scl[i + 1] = hn != V(0) ? V(1) / hn : V(0);
-                            // previous rotations on column i, then the new one
-                            for (int k = 0; k < i; ++k) {
-                                const V t0 = cs[k] * hc[k] + sn[k] * hc[k + 1];
-                                hc[k + 1] = -sn[k] * hc[k] + cs[k] * hc[k + 1];
-                                hc[k] = t0;
-                            }
-                            const V dx = hc[i], dy = hc[i + 1];
-                            if (dy == V(0)) {
-                                cs[i] = V(1);
-                                sn[i] = V(0);
-                            } else {
-                                const V r = sqrt(dx * dx + dy * dy);
-                                cs[i] = dx / r;
-                                sn[i] = dy / r;
-                            }
-                            hc[i] = cs[i] * dx + sn[i] * dy;
-                            hc[i + 1] = V(0);
-                            const V si = s[i];
-                            s[i] = cs[i] * si;
-                            s[i + 1] = -sn[i] * si;
-                            g.it += 1;
-                            const double est = fabs((double)s[i + 1]);
-                            const bool stop = est <= fmax(inner_floor * g.beta, 0.5 * tol * g.normb) || i + 1 == R ||
-                                              g.it >= max_iter || hn == V(0);
-                            if (stop) {
-                                // y = H^{-1} s on the leading (i+1) x (i+1) triangle
-                                for (int q = i; q >= 0; --q) {
-                                    V acc = s[q];
-                                    for (int p2 = q + 1; p2 <= i; ++p2) acc -= H[(size_t)p2 * (R + 1) + q] * ys[p2];
-                                    ys[q] = acc / H[(size_t)q * (R + 1) + q];
-                                }
-                                for (int q = 0; q <= i; ++q) y[q] = ys[q];
-                                g.cycle_end = 1;
-                            }
-                            g.i = i + 1;
-                        }))
-                        return;
+                if (pass == 1) {
+                    if (!grid_barrier(a.gs)) return;
+                    ++sy.gen;  // the barrier's last arrival bumped the generation word
+                    continue;
                 }
+                gm2_block_partials<V>(wred, i + 2, partV);
+                if (!gm2_step<V>(a.gs, a.mcount, sy, partV, i + 2, a.sc, sc, [&](const V* t, Gm2Scal& g) {
+                        V* hc = H + (size_t)i * (R + 1);
+                        V h2sq = V(0);
+                        for (int k = 0; k <= i; ++k) {
+                            coef[k] = (V)t[k];
+                            hc[k] += (V)t[k];
+                            h2sq += (V)t[k] * (V)t[k];
+                        }
+                        const V n2 = (V)t[i + 1] - h2sq;
+                        const V hn = n2 > V(0) ? (V)sqrt(n2) : V(0);
+                        hc[i + 1] = hn;
+                        scl[i + 1] = hn != V(0) ? V(1) / hn : V(0);
+                        // previous rotations on column i, then the new one
+                        for (int k = 0; k < i; ++k) {
+                            const V t0 = cs[k] * hc[k] + sn[k] * hc[k + 1];
+                            hc[k + 1] = -sn[k] * hc[k] + cs[k] * hc[k + 1];
+                            hc[k] = t0;
+                        }
+                        const V dx = hc[i], dy = hc[i + 1];
+                        if (dy == V(0)) {
+                            cs[i] = V(1);
+                            sn[i] = V(0);
+                        } else {
+                            const V r = sqrt(dx * dx + dy * dy);
+                            cs[i] = dx / r;
+                            sn[i] = dy / r;
+                        }
+                        hc[i] = cs[i] * dx + sn[i] * dy;
+                        hc[i + 1] = V(0);
+                        const V si = s[i];
+                        s[i] = cs[i] * si;
+                        s[i + 1] = -sn[i] * si;
+                        g.it += 1;
+                        const double est = fabs((double)s[i + 1]);
+                        const bool stop = est <= fmax(inner_floor * g.beta, 0.5 * tol * g.normb) || i + 1 == R ||
+                                          g.it >= max_iter || hn == V(0);
+                        if (stop) {
+                            // y = H^{-1} s on the leading (i+1) x (i+1) triangle
+                            for (int q = i; q >= 0; --q) {
+                                V acc = s[q];
+                                for (int p2 = q + 1; p2 <= i; ++p2) acc -= H[(size_t)p2 * (R + 1) + q] * ys[p2];
+                                ys[q] = acc / H[(size_t)q * (R + 1) + q];
+                            }
+                            for (int q = 0; q <= i; ++q) y[q] = ys[q];
+                            g.cycle_end = 1;
+                        }
+                        g.i = i + 1;
+                    }))
+                    return;
             }
         }
         // ---- x += P^{-1} sum_k y_k v_k (FP64 update) ----
