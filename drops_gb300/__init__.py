@@ -24,7 +24,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libtracefem.so")
 
 # status codes
-OK, ERR_CUDA, ERR_ZERO_NODE, ERR_ZERO_PATTERN, ERR_BAD_INPUT, ERR_NOT_CONVERGED, ERR_CAPACITY, ERR_WATCHDOG, ERR_NO_DEVICE = range(9)
+OK, ERR_CUDA, ERR_ZERO_NODE, ERR_ZERO_PATTERN, ERR_BAD_INPUT, ERR_NOT_CONVERGED, ERR_CAPACITY, ERR_WATCHDOG, ERR_NO_DEVICE, \
+    ERR_INTERNAL = range(10)
 P1IF, P2IF = 1, 2
 FORM_M, FORM_A, FORM_CN, FORM_LAPM = 0, 1, 2, 3
 MAT_SYS, MAT_BLOCK, MAT_USER = 4, 5, 6
@@ -53,7 +54,8 @@ EXPORTS = [
     "tf_batch_tune", "tf_batch_config", "tf_mlp_init", "tf_mlp_get_weights", "tf_mlp_set_weights", "tf_mlp_forward",
     "tf_mlp_gradient", "tf_mlp_train", "tf_ch_features", "tf_ch_steps_learned", "tf_gmres_options", "tf_pcg_options", "tf_autotune", "tf_autotune_info", "tf_setup_quaqua_p2", "tf_timing_enable",
     "tf_timing_get", "tf_timing_reset", "tf_launch_count", "tf_marker_record", "tf_marker_elapsed", "tf_flush_l2", "tf_spmv_timed", "tf_stream_read_timed", "tf_wind_upload", "tf_vec_write", "tf_vec_read", "tf_ch_stats", "tf_ch_steps_adaptive", "tf_ch_options",
-    "tf_host_alloc", "tf_host_free",
+    "tf_host_alloc", "tf_host_free", "tf_mesh_refine_band", "tf_refine_band", "tf_refined_info", "tf_refined_get",
+    "tf_refined_free", "tf_refine_rules",
 ]
 
 
@@ -81,8 +83,50 @@ def load_library(path=LIB_PATH):
     L.tf_host_alloc.restype = C.c_void_p
     L.tf_host_alloc.argtypes = [C.c_size_t]
     L.tf_host_free.argtypes = [C.c_void_p]
+    L.tf_refined_free.argtypes = [C.c_void_p]
+    L.tf_refined_free.restype = None
     _lib = L
     return L
+
+
+def refine_band(coords, tet_v, kind, par, width, coarse_level, fine_level):
+    """Narrow-band refinement (AdapTriangCL::MakeInitialTriang with DistMarkingStrategyCL) of a level-0 mesh on
+    the host, no device needed.  Returns a dict: coords, tet_v, tet_e, edge_v, tet_level, tets_per_level,
+    last_level, steps; raises TraceFEMError on bad input."""
+    L = load_library()
+    coords = np.ascontiguousarray(coords, dtype=np.float64)
+    tet_v = np.ascontiguousarray(tet_v, dtype=np.int32)
+    par = np.ascontiguousarray(par, dtype=np.float64)
+    h = C.c_void_p()
+    st = L.tf_refine_band(C.c_int64(coords.size // 3), _dp(coords), C.c_int64(tet_v.size // 4), _ip(tet_v),
+                          C.c_int(kind), _dp(par), C.c_int(par.size), C.c_double(width), C.c_int(coarse_level),
+                          C.c_int(fine_level), C.byref(h))
+    if st != OK:
+        raise TraceFEMError(st, L.tf_status_string(st).decode())
+    try:
+        nv, ne, nt = C.c_int64(), C.c_int64(), C.c_int64()
+        ll, steps = C.c_int(), C.c_int()
+        L.tf_refined_info(h, C.byref(nv), C.byref(ne), C.byref(nt), C.byref(ll), C.byref(steps))
+        out = dict(coords=np.empty((nv.value, 3)), tet_v=np.empty((nt.value, 4), np.int32),
+                   tet_e=np.empty((nt.value, 6), np.int32), edge_v=np.empty((ne.value, 2), np.int32),
+                   tet_level=np.empty(nt.value, np.int32), tets_per_level=np.empty(ll.value + 1, np.int64))
+        L.tf_refined_get(h, _dp(out["coords"]), _ip(out["tet_v"]), _ip(out["tet_e"]), _ip(out["edge_v"]),
+                         _ip(out["tet_level"]), _lp(out["tets_per_level"]))
+    finally:
+        L.tf_refined_free(h)
+    out.update(last_level=ll.value, steps=steps.value)
+    return out
+
+
+def refine_rules():
+    """The 64 refinement rules: (nch[64], children[64, 8, 4]) local points, -1 past nch."""
+    L = load_library()
+    nch = np.empty(64, np.int32)
+    ch = np.empty((64, 8, 4), np.int32)
+    st = L.tf_refine_rules(_ip(nch), _ip(ch))
+    if st != OK:
+        raise TraceFEMError(st, L.tf_status_string(st).decode())
+    return nch, ch
 
 
 def _dp(a):
@@ -195,6 +239,17 @@ class TraceFEM:
         edge_v = np.ascontiguousarray(edge_v, dtype=np.int32)
         self._check(self.L.tf_mesh_upload(self.h, C.c_int64(coords.size // 3), _dp(coords), C.c_int64(tet_v.size // 4),
                                           _ip(tet_v), _ip(tet_e), C.c_int64(edge_v.size // 2), _ip(edge_v)))
+
+    def mesh_refine_band(self, kind, par, width, coarse_level, fine_level):
+        """Refines the context's mesh towards the zero level of the distance function and replaces it by the last
+        triangulation level; returns (last_level, steps)."""
+        par = np.ascontiguousarray(par, dtype=np.float64)
+        ll, steps = C.c_int(), C.c_int()
+        self._check(self.L.tf_mesh_refine_band(self.h, C.c_int(kind), _dp(par), C.c_int(par.size), C.c_double(width),
+                                               C.c_int(coarse_level), C.c_int(fine_level), C.byref(ll),
+                                               C.byref(steps)))
+        self.fe = None
+        return ll.value, steps.value
 
     def mesh_info(self):
         nv, ne, nt = C.c_int64(), C.c_int64(), C.c_int64()

@@ -3,7 +3,8 @@
 Each translation unit is compiled in parallel, then linked into
 drops_gb300/_lib/libtracefem.so.  mesh_levelset.cu is compiled with
 -fmad=false so that vertex coordinates and level-set values round exactly like
-the reference's host arithmetic.
+the reference's host arithmetic; refine.cu's host code (the distance tests of
+the refinement marks) with -ffp-contract=off for the same reason.
 """
 import concurrent.futures as cf
 import os
@@ -14,8 +15,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libtracefem.so")
-UNITS = ["common.cu", "mesh_levelset.cu", "dofs.cu", "assemble.cu", "krylov.cu", "krylov_res.cu", "ch.cu", "capi.cu", "noalloc.cu", "batch.cu", "mlp.cu", "learned.cu", "gmres2.cu", "tune.cu", "quaqua.cu", "order.cu"]
-NO_FMA = {"mesh_levelset.cu", "learned.cu"}
+UNITS = ["common.cu", "mesh_levelset.cu", "dofs.cu", "assemble.cu", "krylov.cu", "krylov_res.cu", "ch.cu", "capi.cu", "noalloc.cu", "batch.cu", "mlp.cu", "learned.cu", "gmres2.cu", "tune.cu", "quaqua.cu", "order.cu", "refine.cu"]
+NO_FMA = {"mesh_levelset.cu", "learned.cu", "refine.cu"}
+# host arithmetic that must round like the reference's (no fused multiply-add)
+HOST_NO_CONTRACT = {"refine.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -31,6 +34,8 @@ def _flags(unit, extra=()):
          "--expt-relaxed-constexpr", "-I", os.path.join(HERE, "..", "include")]
     if unit in NO_FMA:
         f.append("-fmad=false")
+    if unit in HOST_NO_CONTRACT:
+        f += ["-Xcompiler", "-ffp-contract=off"]
     return f + list(extra)
 
 

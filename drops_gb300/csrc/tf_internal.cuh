@@ -474,6 +474,18 @@ int fill_f64(Context* c, double* p, int64_t n, double v);
 
 // sub-module entry points (host)
 int mesh_materialise(Context* c, double* coords, int32_t* tet_v, int32_t* tet_e, int32_t* edge_v);
+
+// narrow-band refinement (refine.cu): the last triangulation level of
+// MakeInitialTriang on a level-0 mesh, vertices and edges by first touch
+struct RefinedMesh {
+    std::vector<double> coords;
+    std::vector<int32_t> tet_v, tet_e, edge_v, tet_level;
+    std::vector<int64_t> per_level;
+    int last_level = 0;
+    int steps = 0;
+};
+int refine_band(int64_t nv, const double* coords, int64_t nt, const int32_t* tet_v, int kind, const double* par,
+                int npar, double width, int clevel, int flevel, RefinedMesh& out);
 int ensure_tables(Context* c);
 int patch_dump(Context* c, const int32_t* tets, int64_t count, int32_t* nf, int32_t* facets, int32_t* bnd,
                int32_t* nverts, double* verts);

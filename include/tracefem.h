@@ -41,6 +41,7 @@ extern "C" {
 #define TF_ERR_CAPACITY 6      /* a fixed per-row / per-tet capacity was exceeded                */
 #define TF_ERR_WATCHDOG 7      /* a device-side wait gave up (bounded spin); context stays usable */
 #define TF_ERR_NO_DEVICE 8     /* no CUDA device, or the library was not built for it            */
+#define TF_ERR_INTERNAL 9      /* an internal consistency check failed                          */
 
 /* ---- finite elements, forms, level sets -------------------------------- */
 #define TF_P1IF 1 /* P1IF_FE (misc/problem.h:73) */
@@ -111,6 +112,40 @@ int tf_mesh_upload(tf_context* ctx, int64_t nv, const double* coords, int64_t nt
 int tf_mesh_info(tf_context* ctx, int64_t* nv, int64_t* ne, int64_t* nt);
 /* Materialises the mesh arrays on the host (any pointer may be NULL). */
 int tf_mesh_download(tf_context* ctx, double* coords, int32_t* tet_v, int32_t* tet_e, int32_t* edge_v);
+
+/* ---- narrow-band refinement: AdapTriangCL + DistMarkingStrategyCL --------- */
+/* The surface driver's mesh step (surfphasesep/surfphasesep.cpp:170-181):
+ * DistMarkingStrategyCL(dist, width, coarse_level, fine_level)
+ * (levelset/marking_strategy.cpp:356-398) and AdapTriangCL::MakeInitialTriang
+ * (levelset/adaptriang.cpp:36-44), i.e. at most 2 * fine_level rounds of
+ * marking and MultiGridCL::Refine (geom/multigrid.cpp:389-453), with the
+ * distance function of a TF_LS_SPHERE / TF_LS_TORUS / TF_LS_PLANE kind.
+ * The context's mesh is replaced by the last triangulation level
+ * (TriangFillCL order, geom/multigrid.cpp:1072-1083) as an uploaded mesh:
+ * tets, their vertex order and the coordinates are the reference's; vertices
+ * and edges are numbered by first touch.  The level set and everything after
+ * it must be set up again.  last_level, steps: may be NULL.
+ * TF_ERR_BAD_INPUT also when the mesh's tets do not list their vertices in
+ * one global order (BrickBuilderCL's do; the refinement relies on it).       */
+int tf_mesh_refine_band(tf_context* ctx, int kind, const double* par, int npar, double width, int coarse_level,
+                        int fine_level, int* last_level, int* steps);
+/* The same refinement on host arrays, without a context or a device: a level-0
+ * mesh (coords[3*nv], tet_v[4*nt]) in, a handle to the refined mesh out.      */
+typedef struct tf_refined tf_refined;
+int tf_refine_band(int64_t nv, const double* coords, int64_t nt, const int32_t* tet_v, int kind, const double* par,
+                   int npar, double width, int coarse_level, int fine_level, tf_refined** out);
+int tf_refined_info(const tf_refined* r, int64_t* nv, int64_t* ne, int64_t* nt, int* last_level, int* steps);
+/* coords[3*nv], tet_v[4*nt], tet_e[6*nt], edge_v[2*ne], tet_level[nt],
+ * tets_per_level[last_level+1] (the level lists of the multigrid, all tets
+ * of each level); any pointer may be NULL.                                    */
+int tf_refined_get(const tf_refined* r, double* coords, int32_t* tet_v, int32_t* tet_e, int32_t* edge_v,
+                   int32_t* tet_level, int64_t* tets_per_level);
+void tf_refined_free(tf_refined* r);
+/* The 64 refinement rules the refinement uses (RefRuleCL / ChildDataCL,
+ * geom/topo.h:185-223, geom/triang.cpp): nch[64] children per edge pattern,
+ * children[64*8*4] their local points (vertex i < 4, midpoint of edge i - 4),
+ * -1 past nch.  Either pointer may be NULL.                                   */
+int tf_refine_rules(int32_t* nch, int32_t* children);
 
 /* ---- level set: the P2 VecDescCL LocalAssemblerParams::levelSet ------------ */
 /* Host values per vertex and per edge.  ls_edge == NULL gives the

@@ -27,6 +27,7 @@ UNITS=(
   num/gradient_recovery.cpp levelset/levelsetmapper.cpp
   misc/utils.cpp misc/problem.cpp misc/params.cpp misc/scopetimer.cpp
   surfactant/ifacetransp.cpp
+  levelset/adaptriang.cpp levelset/marking_strategy.cpp
   levelset/levelset.cpp levelset/surfacetension.cpp levelset/fastmarch.cpp levelset/volume_adjustment.cpp
   out/vtkOut.cpp out/ensightOut.cpp misc/progressaccu.cpp misc/base64.cpp
 )

@@ -12,6 +12,13 @@
 //       interface index DistributeDOFs (misc/problem.cpp:283-336),
 //       setupFESystem (surfactant/ifacetransp.cpp:615-622) for M, A, C_n (+F),
 //       optional PCGSolverCL<JACPcCL> on M + A + h C_n (num/krylovsolver.h:1805).
+//   ref_harness system_ref <p1|p2> <lsP1|lsP2> <shape> <n> <a> <solve> <width> <coarse> <fine> <out>
+//       the same on the last level after narrow-band refinement of the brick
+//       (solve -1: the mesh only)
+//       (AdapTriangCL::MakeInitialTriang with DistMarkingStrategyCL,
+//       surfphasesep/surfphasesep.cpp:170-181; levelset/adaptriang.cpp,
+//       levelset/marking_strategy.cpp:356-398, geom/multigrid.cpp:389-453).
+//   ref_harness rules <out>                 the 64 refinement rules (geom/topo.cpp)
 //   ref_harness legacy_numb <case> <out>    CreateNumbOnInterface test cases
 //   ref_harness legacy_forms <n> <a> <out>  SetupInterfaceMassP1 / SetupLBP1 / SetupInterfaceRhsP1
 //       (surfactant/ifacetransp.cpp:367-380, 499-512, 532-563) on the unit sphere,
@@ -63,7 +70,9 @@
 // is why this file is compiled with -fno-access-control.
 #include "geom/builder.h"
 #include "misc/problem.h"
+#include "levelset/adaptriang.h"
 #include "levelset/levelsetmapper.h"
+#include "levelset/marking_strategy.h"
 #include "num/gradient_recovery.h"
 #include "num/krylovsolver.h"
 #include "num/precond.h"
@@ -137,14 +146,14 @@ struct Flat {
     std::vector<int64_t> tet_v, tet_ev;
     std::vector<double> coords;
 };
-Flat flatten(MultiGridCL& mg) {
+Flat flatten(MultiGridCL& mg, int L = 0) {
     Flat F;
     int64_t k = 0;
-    DROPS_FOR_TRIANG_VERTEX(mg, 0, it) {
+    DROPS_FOR_TRIANG_VERTEX(mg, L, it) {
         F.vid[&*it] = k++;
         for (int c = 0; c < 3; ++c) F.coords.push_back(it->GetCoord()[c]);
     }
-    DROPS_FOR_TRIANG_TETRA(mg, 0, it) {
+    DROPS_FOR_TRIANG_TETRA(mg, L, it) {
         for (int i = 0; i < 4; ++i) F.tet_v.push_back(F.vid[it->GetVertex(i)]);
         for (int e = 0; e < 6; ++e) {
             F.tet_ev.push_back(F.vid[it->GetEdge(e)->GetVertex(0)]);
@@ -188,35 +197,68 @@ LocalAssembler::vec F_P2(LocalAssembler& a) {
 }
 
 int cmd_system(int argc, char** argv) {
-    if (argc < 9) throw std::invalid_argument("usage: system p1|p2 lsP1|lsP2 shape n a solve out");
+    // "system_ref": three more arguments before <out> (width, coarse and fine
+    // level): the brick is first refined towards the surface as the
+    // surfphasesep driver does (surfphasesep.cpp:170-181: AdapTriangCL with
+    // DistMarkingStrategyCL on the distance function, MakeInitialTriang), and
+    // everything below runs on the last triangulation level.
+    const bool refine = std::string(argv[1]) == "system_ref";
+    if (argc < (refine ? 12 : 9))
+        throw std::invalid_argument("usage: system p1|p2 lsP1|lsP2 shape n a solve out | "
+                                    "system_ref p1|p2 lsP1|lsP2 shape n a solve width coarse fine out");
     const bool p2 = std::string(argv[2]) == "p2";
     const bool lsp2 = std::string(argv[3]) == "lsP2";
     const std::string shape = argv[4];
     const int n = std::atoi(argv[5]);
     const double a = std::atof(argv[6]);
-    const bool solve = std::atoi(argv[7]) != 0;
-    Writer w(argv[8]);
+    const int solve_arg = std::atoi(argv[7]);  // -1: the mesh only
+    const bool solve = solve_arg > 0;
+    Writer w(argv[refine ? 11 : 8]);
 
     double t0 = now();
     BrickBuilderCL brick(Point3DCL(-a), 2. * a * std_basis<3>(1), 2. * a * std_basis<3>(2), 2. * a * std_basis<3>(3), n, n,
                          n);
     MultiGridCL mg(brick);
-    Flat F = flatten(mg);
+    if (refine) {
+        const double width = std::atof(argv[8]);
+        const int clevel = std::atoi(argv[9]), flevel = std::atoi(argv[10]);
+        AdapTriangCL adap(mg);
+        DistMarkingStrategyCL marker([&](Point3DCL const& x, double) { return ls_value(shape, x); }, width, clevel,
+                                     flevel);
+        adap.set_marking_strategy(&marker);
+        t0 = now();
+        adap.MakeInitialTriang();
+        w.s("time_refine", now() - t0);
+        adap.set_marking_strategy(nullptr);
+        std::vector<int64_t> per_level;
+        for (int l = 0; l <= (int)mg.GetLastLevel(); ++l) {
+            int64_t c = 0;
+            for (auto it = mg.GetTetrasBegin(l), e = mg.GetTetrasEnd(l); it != e; ++it) ++c;
+            per_level.push_back(c);
+        }
+        w.l("tets_per_level", per_level);
+        std::vector<int64_t> tl;
+        DROPS_FOR_TRIANG_TETRA(mg, (int)mg.GetLastLevel(), it) tl.push_back((int64_t)it->GetLevel());
+        w.l("tet_level", tl);
+    }
+    const int L = (int)mg.GetLastLevel();
+    Flat F = flatten(mg, L);
     w.l("tet_v", F.tet_v);
     w.l("tet_ev", F.tet_ev);
     w.d("coords", F.coords);
     w.s("time_mesh", now() - t0);
+    if (solve_arg < 0) return 0;
 
     FESystem sys;
     auto& levelSet = sys.params.levelSet;
     IdxDescCL lsIdx(P2_FE);
-    lsIdx.DistributeDOFs(0, mg);
+    lsIdx.DistributeDOFs(L, mg);
     levelSet.SetIdx(&lsIdx);
     const Uint li = lsIdx.GetIdx();
     // vertex values, then edges: P2 nodal (LSInit) or P1-linear (LinearLSInit),
     // surfactant/surfactant.cpp:733-758.
-    DROPS_FOR_TRIANG_VERTEX(mg, 0, it) levelSet.Data[it->Unknowns(li)] = ls_value(shape, it->GetCoord());
-    DROPS_FOR_TRIANG_EDGE(mg, 0, it) {
+    DROPS_FOR_TRIANG_VERTEX(mg, L, it) levelSet.Data[it->Unknowns(li)] = ls_value(shape, it->GetCoord());
+    DROPS_FOR_TRIANG_EDGE(mg, L, it) {
         if (lsp2)
             levelSet.Data[it->Unknowns(li)] =
                 ls_value(shape, 0.5 * (it->GetVertex(0)->GetCoord() + it->GetVertex(1)->GetCoord()));
@@ -227,8 +269,8 @@ int cmd_system(int argc, char** argv) {
     {
         std::vector<double> lv, le;
         std::vector<int64_t> ev;
-        DROPS_FOR_TRIANG_VERTEX(mg, 0, it) lv.push_back(levelSet.Data[it->Unknowns(li)]);
-        DROPS_FOR_TRIANG_EDGE(mg, 0, it) {
+        DROPS_FOR_TRIANG_VERTEX(mg, L, it) lv.push_back(levelSet.Data[it->Unknowns(li)]);
+        DROPS_FOR_TRIANG_EDGE(mg, L, it) {
             le.push_back(levelSet.Data[it->Unknowns(li)]);
             ev.push_back(F.vid[it->GetVertex(0)]);
             ev.push_back(F.vid[it->GetVertex(1)]);
@@ -240,7 +282,7 @@ int cmd_system(int argc, char** argv) {
 
     IdxDescCL ifIdx(p2 ? P2IF_FE : P1IF_FE);
     t0 = now();
-    size_t n_active = ifIdx.DistributeDOFs(0, mg, &levelSet);
+    size_t n_active = ifIdx.DistributeDOFs(L, mg, &levelSet);
     w.s("time_dofs", now() - t0);
     w.i("n_active", (int64_t)n_active);
     w.i("n_dofs", (int64_t)ifIdx.NumUnknowns());
@@ -248,7 +290,7 @@ int cmd_system(int argc, char** argv) {
         std::vector<int64_t> l2g;
         std::vector<int64_t> act;
         int64_t k = 0;
-        DROPS_FOR_TRIANG_TETRA(mg, 0, it) {
+        DROPS_FOR_TRIANG_TETRA(mg, L, it) {
             auto I = ifIdx.Loc2Glo(*it);
             if (!I.empty()) {
                 act.push_back(k);
@@ -286,7 +328,7 @@ int cmd_system(int argc, char** argv) {
         // wind convection N_P1P1 (surfactant/ifacetransp.h:1590-1600) with a
         // vecP2IF wind interpolated as in surfphasesep/surfphasesep.cpp:198-213, 417-420
         IdxDescCL velIdx(vecP2IF_FE);
-        velIdx.DistributeDOFs(0, mg, &levelSet);
+        velIdx.DistributeDOFs(L, mg, &levelSet);
         VecDescCL wind(&velIdx);
         wind.Interpolate(mg, [](Point3DCL const& x) { return wind_value(x); });
         FESystem nsys;
@@ -316,11 +358,11 @@ int cmd_system(int argc, char** argv) {
             w.d("chi", std::vector<double>(std::begin(chi.Data), std::end(chi.Data)));
         }
         std::vector<double> wv, we;
-        DROPS_FOR_TRIANG_VERTEX(mg, 0, it) {
+        DROPS_FOR_TRIANG_VERTEX(mg, L, it) {
             const Point3DCL v = wind_value(it->GetCoord());
             for (int c = 0; c < 3; ++c) wv.push_back(v[c]);
         }
-        DROPS_FOR_TRIANG_EDGE(mg, 0, it) {
+        DROPS_FOR_TRIANG_EDGE(mg, L, it) {
             const Point3DCL v = wind_value(GetBaryCenter(*it));
             for (int c = 0; c < 3; ++c) we.push_back(v[c]);
         }
@@ -331,7 +373,7 @@ int cmd_system(int argc, char** argv) {
         const size_t m = ifIdx.NumUnknowns();
         MatrixBuilderCL bM(&Mm, m, m), bA(&Am, m, m), bC(&Cm, m, m);
         rhs.resize(m, 0.);
-        DROPS_FOR_TRIANG_TETRA(mg, 0, it) {
+        DROPS_FOR_TRIANG_TETRA(mg, L, it) {
             auto I = ifIdx.Loc2Glo(*it);
             if (I.empty()) continue;
             LocalAssembler as(*it, sys.params);
@@ -824,13 +866,32 @@ int cmd_quaqua(int argc, char** argv) {
     return 0;
 }
 
+// The 64 refinement rules (geom/topo.h:196-223): per edge pattern the
+// children's local points (ChildDataCL::Vertices) in rule order.
+int cmd_rules(int argc, char** argv) {
+    if (argc < 3) throw std::invalid_argument("usage: rules out");
+    Writer w(argv[2]);
+    std::vector<int64_t> nch, ch;
+    for (Uint p = 0; p < 64; ++p) {
+        const RefRuleCL& R = GetRefRule((Ubyte)p);
+        nch.push_back(R.ChildNum);
+        for (Uint c = 0; c < 8; ++c)
+            for (Uint k = 0; k < 4; ++k)
+                ch.push_back(c < R.ChildNum ? (int64_t)GetChildData(R.Children[c]).Vertices[k] : -1);
+    }
+    w.l("nch", nch);
+    w.l("children", ch);
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
     try {
         if (argc < 2) throw std::invalid_argument("usage: ref_harness <cmd> ...");
         std::string cmd = argv[1];
-        if (cmd == "system") return cmd_system(argc, argv);
+        if (cmd == "system" || cmd == "system_ref") return cmd_system(argc, argv);
+        if (cmd == "rules") return cmd_rules(argc, argv);
         if (cmd == "legacy_numb") return cmd_legacy_numb(argc, argv);
         if (cmd == "legacy_forms") return cmd_legacy_forms(argc, argv);
         if (cmd == "area") return cmd_area(argc, argv);

@@ -83,6 +83,65 @@ def system_case(name, fe, ls, shape, n, a, solve, keep_vec=None):
     print(name, "active", out["n_active"], "dofs", out["n_dofs"], "nnz", len(out["colind"]))
 
 
+def refine_case(name, fe, ls, shape, n, a, width, clevel, flevel, solve):
+    """Narrow-band refinement of the brick (AdapTriangCL::MakeInitialTriang with DistMarkingStrategyCL) and the
+    TraceFEM system on the last triangulation level.  The mesh is pinned by the per-level tet counts, each
+    triangulation tet's level and a digest of its four vertices' coordinates in order (independent of how the
+    vertices are numbered)."""
+    d = run("system_ref", fe, ls, shape, str(n), repr(a), "1" if solve else "0", repr(width), str(clevel),
+            str(flevel))
+    tet_xyz = d["coords"].reshape(-1, 3)[d["tet_v"].reshape(-1, 4)]
+    out = dict(
+        n=n, a=a, width=width, clevel=clevel, flevel=flevel, p2=int(fe == "p2"), ls_p2=int(ls == "lsP2"),
+        shape=shape, tets_per_level=d["tets_per_level"], tet_level=d["tet_level"].astype(np.int8),
+        tet_xyz_sha=sha(tet_xyz), nt=len(d["tet_level"]), ref_time_refine=d["time_refine"][0],
+        n_active=int(d["n_active"][0]), n_dofs=int(d["n_dofs"][0]),
+        active_tets=d["active_tets"].astype(np.int32), loc2glo=d["loc2glo"].astype(np.int32),
+        rowptr=d["M.rowptr"], colind=d["M.colind"].astype(np.int32),
+        M=d["M.vals"], A=d["A.vals"], C=d["C.vals"], rhs=d["rhs"],
+    )
+    if solve:
+        assert np.array_equal(d["S.rowptr"], d["M.rowptr"]) and np.array_equal(d["S.colind"], d["M.colind"])
+        out.update(S=d["S.vals"], x=d["x"], iters=int(d["iters"][0]), resid=float(d["resid"][0]))
+    np.savez_compressed(os.path.join(HERE, name), **out)
+    print(name, "levels", out["tets_per_level"].tolist(), "tets", out["nt"], "dofs", out["n_dofs"])
+
+
+REFINE_MESHES = [  # shape, n, a, width, coarse, fine
+    ("sphere", 6, 5.0 / 3.0, 0.2, 0, 3),
+    ("torus", 5, 1.6, 0.05, 0, 3),
+    ("sphere", 5, 5.0 / 3.0, 0.0, 1, 2),
+    ("torus", 4, 1.6, 0.3, 1, 3),
+    ("sphere", 3, 5.0 / 3.0, 0.5, 0, 4),
+]
+
+
+def refine_meshes_case():
+    """Refined meshes only (up to four levels, 330k tets), pinned by digests."""
+    rows = []
+    for shape, n, a, width, cl, fl in REFINE_MESHES:
+        d = run("system_ref", "p1", "lsP2", shape, str(n), repr(a), "-1", repr(width), str(cl), str(fl))
+        tet_xyz = d["coords"].reshape(-1, 3)[d["tet_v"].reshape(-1, 4)]
+        rows.append(dict(per_level=d["tets_per_level"], xyz=sha(tet_xyz), lvl=sha(d["tet_level"].astype(np.int8)),
+                         t=d["time_refine"][0]))
+    np.savez_compressed(
+        os.path.join(HERE, "refine_meshes.npz"),
+        shape=np.array([c[0] for c in REFINE_MESHES]), n=np.array([c[1] for c in REFINE_MESHES]),
+        a=np.array([c[2] for c in REFINE_MESHES]), width=np.array([c[3] for c in REFINE_MESHES]),
+        clevel=np.array([c[4] for c in REFINE_MESHES]), flevel=np.array([c[5] for c in REFINE_MESHES]),
+        per_level=np.array([",".join(map(str, r["per_level"].tolist())) for r in rows]),
+        tet_xyz_sha=np.array([r["xyz"] for r in rows]), tet_level_sha=np.array([r["lvl"] for r in rows]),
+        ref_time_refine=np.array([r["t"] for r in rows]))
+    print("refine meshes", [r["per_level"].tolist() for r in rows])
+
+
+def rules_case():
+    """The 64 refinement rules of geom/topo.cpp: children per edge pattern, local points in order."""
+    d = run("rules")
+    np.savez_compressed(os.path.join(HERE, "refine_rules.npz"), nch=d["nch"].astype(np.int32),
+                        children=d["children"].astype(np.int32).reshape(64, 8, 4))
+
+
 def area_case():
     d = run("area")
     np.savez_compressed(
@@ -181,3 +240,7 @@ if __name__ == "__main__":
     legacy_forms_case()
     ch_case()
     quaqua_case()
+    refine_case("refine_sphere_p1_n4.npz", "p1", "lsP2", "sphere", 4, 5.0 / 3.0, 0.1, 0, 2, True)
+    refine_case("refine_torus_p2_n3.npz", "p2", "lsP2", "torus", 3, 1.62, 0.05, 0, 1, False)
+    rules_case()
+    refine_meshes_case()

@@ -1,0 +1,90 @@
+"""The TraceFEM path on narrow-band refined meshes (tf_mesh_refine_band), through the C ABI, against the
+reference's own refinement, numbering, forms and PCG solve on the last triangulation level."""
+import hashlib
+
+import numpy as np
+import pytest
+
+import drops_gb300 as tf
+from tests.helpers import mat_close, sol_close
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    ("refine_sphere_p1_n4.npz", tf.LS_SPHERE, [0.0, 0.0, 0.0, 1.0]),
+    ("refine_torus_p2_n3.npz", tf.LS_TORUS, [1.0, 0.4, 2]),
+]
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from drops_gb300 import build
+
+    build.build()
+    c = tf.TraceFEM()
+    yield c
+    c.close()
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def setup(ctx, g, kind, par):
+    n, a = int(g["n"]), float(g["a"])
+    ctx.brick_cube(n, a)
+    last, steps = ctx.mesh_refine_band(kind, par, float(g["width"]), int(g["clevel"]), int(g["flevel"]))
+    assert last == int(g["flevel"]) and steps >= 1
+    coords, tv, te, ev = ctx.mesh_download()
+    assert sha(coords[tv]) == str(g["tet_xyz_sha"])
+    ctx.levelset_analytic(kind, par, bool(g["ls_p2"]))
+    return ctx.distribute_dofs(tf.P2IF if bool(g["p2"]) else tf.P1IF)
+
+
+@pytest.mark.parametrize("name,kind,par", CASES)
+def test_refined_dofs_and_forms(ctx, golden, name, kind, par):
+    g = golden(name)
+    na, nd = setup(ctx, g, kind, par)
+    assert na == int(g["n_active"]) and nd == int(g["n_dofs"])
+    dv, de, act, l2g = ctx.dofs()
+    assert np.array_equal(act, g["active_tets"])
+    assert np.array_equal(l2g, g["loc2glo"])
+    nnz = ctx.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN], tf.RHS_SPHERE_XYZ, [0, 0, 0, 1.0, 13.0])
+    assert nnz == len(g["colind"])
+    for f, key in ((tf.FORM_M, "M"), (tf.FORM_A, "A"), (tf.FORM_CN, "C")):
+        rp, ci, v = ctx.matrix(f)
+        assert np.array_equal(rp, g["rowptr"]) and np.array_equal(ci, g["colind"])
+        ok, err = mat_close(v, g[key], rp)
+        assert ok, (key, err)
+    ok, err = mat_close(ctx.vec_download(tf.VEC_RHS), g["rhs"])
+    assert ok, err
+
+
+@pytest.mark.parametrize("precision", [tf.PREC_FP64, tf.PREC_MIXED])
+def test_refined_pcg(ctx, golden, precision):
+    """PCGSolverCL<JACPcCL> on M + A + h C_n of the refined sphere mesh (h the coarse mesh width, as the
+    reference driver's)."""
+    g = golden("refine_sphere_p1_n4.npz")
+    na, nd = setup(ctx, g, tf.LS_SPHERE, [0.0, 0.0, 0.0, 1.0])
+    ctx.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN], tf.RHS_SPHERE_XYZ, [0, 0, 0, 1.0, 13.0])
+    h = 2 * float(g["a"]) / int(g["n"])
+    ctx.lincomb([tf.FORM_M, tf.FORM_A, tf.FORM_CN], [1.0, 1.0, h])
+    rp, ci, S = ctx.matrix(tf.MAT_SYS)
+    ok, err = mat_close(S, g["S"], rp)
+    assert ok, err
+    ctx.vec_upload(tf.VEC_X, np.zeros(nd))
+    st, it, res = ctx.pcg_jacobi(tf.MAT_SYS, tf.VEC_RHS, tf.VEC_X, tol=1e-10, precision=precision)
+    assert st == tf.OK and res <= 1e-10
+    if precision == tf.PREC_FP64:
+        assert abs(it - int(g["iters"])) <= 1, (it, int(g["iters"]))
+    ok, err = sol_close(ctx.vec_download(tf.VEC_X), g["x"])
+    assert ok, err
+
+
+def test_refine_then_brick_again(ctx, golden):
+    """A refined mesh is replaced by the next mesh call like any uploaded mesh."""
+    g = golden("refine_sphere_p1_n4.npz")
+    setup(ctx, g, tf.LS_SPHERE, [0.0, 0.0, 0.0, 1.0])
+    ctx.brick_cube(4, 1.0)
+    nv, ne, nt = ctx.mesh_info()
+    assert nt == 6 * 4 ** 3 and nv == 5 ** 3
