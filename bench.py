@@ -804,6 +804,51 @@ def run_quaqua(args):
                     "device time from the call to the assembled M, A and load vector, median of 3, L2 flushed"}
 
 
+REFINE_N, REFINE_WIDTH, REFINE_LEVELS = 32, 0.05, 2
+
+
+def run_refine(args):
+    """Narrow-band refinement of a 32^3 brick of the same box towards the same sphere (width 0.05, levels 0..2,
+    AdapTriangCL::MakeInitialTriang with DistMarkingStrategyCL) and the P2 TraceFEM path on its last
+    triangulation level.  The refinement runs on the host (one core, wall clock, median of 3, including the
+    mesh's download and upload); the path (level set, DistributeDOFs, setupFESystem of M, A, C_n and the load
+    vector, LinComb, mixed PCG to 1e-10) is device time between stream markers, median of 3 after one warm-up."""
+    import drops_gb300 as tf
+
+    ctx = tf.TraceFEM(0)
+    tr = []
+    for _ in range(3):
+        ctx.brick_cube(REFINE_N, HALF)
+        t0 = time.perf_counter()
+        last, steps = ctx.mesh_refine_band(tf.LS_SPHERE, SPHERE, REFINE_WIDTH, 0, REFINE_LEVELS)
+        tr.append((time.perf_counter() - t0) * 1e3)
+    nv, ne, nt = ctx.mesh_info()
+    h = 2 * HALF / REFINE_N
+    ts, its = [], []
+    for rep in range(4):
+        ctx.flush_l2()
+        ctx.marker(6)
+        ctx.levelset_analytic(tf.LS_SPHERE, SPHERE, p2=True)
+        na, m = ctx.distribute_dofs(tf.P2IF)
+        ctx.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN], tf.RHS_SPHERE_XYZ, list(SPHERE) + [13.0])
+        ctx.lincomb([tf.FORM_M, tf.FORM_A, tf.FORM_CN], [1.0, 1.0, h])
+        ctx.vec_fill(tf.VEC_X, m, 0.0)
+        st, it, res = ctx.pcg_jacobi(tf.MAT_SYS, tf.VEC_RHS, tf.VEC_X, tol=1e-10, precision=tf.PREC_MIXED)
+        ctx.marker(7)
+        if rep:
+            ts.append(ctx.elapsed_ms(6, 7))
+            its.append(it)
+        assert st == tf.OK and res <= 1e-10
+    ctx.close()
+    ms = statistics.median(ts)
+    return {"refine_ms": round(statistics.median(tr), 1), "levels": last, "steps": steps, "tets": nt, "vertices": nv,
+            "cut_tets": na, "dofs": m, "path_ms": round(ms, 3), "cut_tets_per_s": round(na / (ms / 1e3), 1),
+            "pcg_iters": int(statistics.median(its)),
+            "note": f"{REFINE_N}^3 Kuhn cubes on [-5/3,5/3]^3 refined towards the unit sphere (width "
+                    f"{REFINE_WIDTH}, levels 0..{REFINE_LEVELS}); refine_ms on one host core, path_ms on the device "
+                    "(P2, mixed PCG), L2 flushed before each path"}
+
+
 def quaqua_cpu_sample(threads, sample=4000):
     """The oracle's QuaQua element forms on the first `sample` cut tets of the same problem (one thread: the
     reference accumulates them serially), as cut tets/s."""
@@ -909,6 +954,7 @@ def main():
     if rank == 0 and ws == 1 and args.size == N_CUBES and not args.no_extra:
         out["batch"], out["ch"] = extra_workloads(args, rank, ws, dist)
         out["quaqua"] = run_quaqua(args)
+        out["refine"] = run_refine(args)
     if rank == 0:
         products = out.pop("_products")
         if ws == 1 and not args.no_cpu_baseline:

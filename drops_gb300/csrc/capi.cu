@@ -314,6 +314,15 @@ int tf_mesh_upload(tf_context* t, int64_t nv, const double* coords, int64_t nt, 
     M.tet_v = c->tet_v.p;
     M.tet_e = c->tet_e.p;
     M.edge_v = c->edge_v.p;
+    for (int k = 0; k < 3; ++k) {
+        double lo = coords[k], hi = coords[k];
+        for (int64_t v = 1; v < nv; ++v) {
+            lo = std::min(lo, coords[3 * v + k]);
+            hi = std::max(hi, coords[3 * v + k]);
+        }
+        M.bb_lo[k] = lo;
+        M.bb_scale[k] = hi > lo ? 1048576.0 / (hi - lo) : 0.0;
+    }
     c->has_mesh = true;
     c->has_ls = false;
     c->has_wind = false;

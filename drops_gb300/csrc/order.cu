@@ -37,8 +37,10 @@ __global__ void k_order_init(int64_t m, unsigned long long* __restrict__ keys, i
     }
 }
 
-// the Morton key of each numbered node's doubled grid position; edge nodes
-// only for a P2 numbering (a P1 numbering leaves dof_edge unset)
+// the Morton key of each numbered node's doubled grid position (a brick), or
+// of its position on a 2^20 grid over the bounding box (an uploaded mesh: the
+// vertex, or the edge's midpoint); edge nodes only for a P2 numbering (a P1
+// numbering leaves dof_edge unset)
 __global__ void k_dof_morton(MeshView M, const int32_t* __restrict__ dof_vert, const int32_t* __restrict__ dof_edge,
                              int p2, int64_t m, unsigned long long* __restrict__ keys) {
     const int64_t total = M.nv + (p2 ? M.ne : 0);
@@ -47,7 +49,18 @@ __global__ void k_dof_morton(MeshView M, const int32_t* __restrict__ dof_vert, c
         const int32_t dof = node < M.nv ? dof_vert[node] : dof_edge[node - M.nv];
         if (dof < 0 || dof >= m) continue;
         int g[3];
-        brick_node_grid2(M.b, node, M.nv, g);
+        if (M.explicit_mesh) {
+            double x[3];
+            if (node < M.nv) {
+                for (int k = 0; k < 3; ++k) x[k] = M.coords[3 * node + k];
+            } else {
+                const int32_t a = M.edge_v[2 * (node - M.nv)], b = M.edge_v[2 * (node - M.nv) + 1];
+                for (int k = 0; k < 3; ++k) x[k] = 0.5 * (M.coords[3 * (int64_t)a + k] + M.coords[3 * (int64_t)b + k]);
+            }
+            for (int k = 0; k < 3; ++k) g[k] = (int)fmin(fmax((x[k] - M.bb_lo[k]) * M.bb_scale[k], 0.0), 2097151.0);
+        } else {
+            brick_node_grid2(M.b, node, M.nv, g);
+        }
         keys[dof] = spread3((unsigned)g[0]) | spread3((unsigned)g[1]) << 1 | spread3((unsigned)g[2]) << 2;
     }
 }
@@ -57,10 +70,8 @@ __global__ void k_dof_morton(MeshView M, const int32_t* __restrict__ dof_vert, c
 int dof_locality_order(Context* c, const int32_t** order) {
     *order = nullptr;
     const MeshView& M = c->mesh;
-    if (M.explicit_mesh || M.nbatch || c->legacy_numbering || (c->fe != TF_P1IF && c->fe != TF_P2IF) ||
-        c->n_dofs <= 0)
-        return TF_OK;
-    if (2 * (int64_t)std::max({M.b.n1, M.b.n2, M.b.n3}) + 1 >= (1 << 21)) return TF_OK;
+    if (M.nbatch || c->legacy_numbering || (c->fe != TF_P1IF && c->fe != TF_P2IF) || c->n_dofs <= 0) return TF_OK;
+    if (!M.explicit_mesh && 2 * (int64_t)std::max({M.b.n1, M.b.n2, M.b.n3}) + 1 >= (1 << 21)) return TF_OK;
     const int64_t m = c->n_dofs;
     if (c->dof_order_version != c->dof_version) {
         TF_TRY(ensure(c, c->order_keys, (size_t)(2 * m)));

@@ -80,6 +80,9 @@ struct MeshView {
     const int32_t* tet_v;
     const int32_t* tet_e;
     const int32_t* edge_v;
+    // explicit meshes: the bounding box's low corner and 2^20 / extent per
+    // axis (grid positions for the locality order)
+    double bb_lo[3], bb_scale[3];
 };
 
 // instance owning index x: the largest i with start[i] <= x (start[0] = 0)
