@@ -15,10 +15,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libtracefem.so")
-UNITS = ["common.cu", "mesh_levelset.cu", "dofs.cu", "assemble.cu", "krylov.cu", "krylov_res.cu", "ch.cu", "capi.cu", "noalloc.cu", "batch.cu", "mlp.cu", "learned.cu", "gmres2.cu", "tune.cu", "quaqua.cu", "order.cu", "refine.cu"]
-NO_FMA = {"mesh_levelset.cu", "learned.cu", "refine.cu"}
+UNITS = ["common.cu", "mesh_levelset.cu", "dofs.cu", "assemble.cu", "krylov.cu", "krylov_res.cu", "ch.cu", "capi.cu", "noalloc.cu", "batch.cu", "mlp.cu", "learned.cu", "gmres2.cu", "tune.cu", "quaqua.cu", "order.cu", "refine.cu", "refine_par.cu"]
+NO_FMA = {"mesh_levelset.cu", "learned.cu", "refine.cu", "refine_par.cu"}
 # host arithmetic that must round like the reference's (no fused multiply-add)
-HOST_NO_CONTRACT = {"refine.cu"}
+HOST_NO_CONTRACT = {"refine.cu", "refine_par.cu"}
+# kernel bodies written as __host__ __device__ lambdas
+EXTENDED_LAMBDA = {"refine_par.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -36,6 +38,8 @@ def _flags(unit, extra=()):
         f.append("-fmad=false")
     if unit in HOST_NO_CONTRACT:
         f += ["-Xcompiler", "-ffp-contract=off"]
+    if unit in EXTENDED_LAMBDA:
+        f.append("--extended-lambda")
     return f + list(extra)
 
 

@@ -370,20 +370,9 @@ int tf_mesh_refine_band(tf_context* t, int kind, const double* par, int npar, do
                         int fine_level, int* last_level, int* steps) {
     CTX_CHECK(t);
     Context* c = &t->c;
+    cudaSetDevice(c->device);
     if (!c->has_mesh || c->batch_count) return tf::set_err(c, TF_ERR_BAD_INPUT, "mesh_refine_band: one mesh required");
-    const int64_t nv = c->mesh.nv, nt = c->mesh.nt;
-    std::vector<double> coords((size_t)(3 * nv));
-    std::vector<int32_t> tet_v((size_t)(4 * nt));
-    TF_TRY(tf_mesh_download(t, coords.data(), tet_v.data(), nullptr, nullptr));
-    tf::RefinedMesh R;
-    const int st = tf::refine_band(nv, coords.data(), nt, tet_v.data(), kind, par, npar, width, coarse_level,
-                                   fine_level, R);
-    if (st != TF_OK) return tf::set_err(c, st, "mesh_refine_band: bad parameters or an unoriented mesh");
-    TF_TRY(tf_mesh_upload(t, (int64_t)(R.coords.size() / 3), R.coords.data(), (int64_t)R.tet_level.size(),
-                          R.tet_v.data(), R.tet_e.data(), (int64_t)(R.edge_v.size() / 2), R.edge_v.data()));
-    if (last_level) *last_level = R.last_level;
-    if (steps) *steps = R.steps;
-    return TF_OK;
+    return tf::refine_band_device(c, kind, par, npar, width, coarse_level, fine_level, last_level, steps);
 }
 
 int tf_levelset_upload(tf_context* t, const double* ls_vert, const double* ls_edge) {

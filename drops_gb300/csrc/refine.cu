@@ -828,6 +828,24 @@ int tf_refined_get(const tf_refined* r, double* coords, int32_t* tet_v, int32_t*
 
 void tf_refined_free(tf_refined* r) { delete r; }
 
+// The device engine's kernel bodies run as host loops, for checking them
+// against the reference's fixtures without a device (not part of the header).
+int tf_refine_band_parallel_host(int64_t nv, const double* coords, int64_t nt, const int32_t* tet_v, int kind,
+                                 const double* par, int npar, double width, int coarse_level, int fine_level,
+                                 tf_refined** out) {
+    if (!out) return TF_ERR_BAD_INPUT;
+    *out = nullptr;
+    tf_refined* r = new tf_refined;
+    const int st = tf::refine_band_parallel_host(nv, coords, nt, tet_v, kind, par, npar, width, coarse_level,
+                                                 fine_level, r->m);
+    if (st != TF_OK) {
+        delete r;
+        return st;
+    }
+    *out = r;
+    return TF_OK;
+}
+
 int tf_refine_rules(int32_t* nch, int32_t* children) {
     const tf::refine::Tables& T = tf::refine::tables();
     if (!T.ok) return TF_ERR_INTERNAL;

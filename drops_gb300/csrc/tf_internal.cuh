@@ -489,6 +489,12 @@ struct RefinedMesh {
 };
 int refine_band(int64_t nv, const double* coords, int64_t nt, const int32_t* tet_v, int kind, const double* par,
                 int npar, double width, int clevel, int flevel, RefinedMesh& out);
+// the data-parallel form of the same refinement (refine_par.cu): on the host
+// (its kernel bodies as loops), and on the device for a context's mesh
+int refine_band_parallel_host(int64_t nv, const double* coords, int64_t nt, const int32_t* tet_v, int kind,
+                              const double* par, int npar, double width, int clevel, int flevel, RefinedMesh& out);
+int refine_band_device(Context* c, int kind, const double* par, int npar, double width, int clevel, int flevel,
+                       int* last_level, int* steps);
 int ensure_tables(Context* c);
 int patch_dump(Context* c, const int32_t* tets, int64_t count, int32_t* nf, int32_t* facets, int32_t* bnd,
                int32_t* nverts, double* verts);

@@ -81,6 +81,30 @@ def test_refined_pcg(ctx, golden, precision):
     assert ok, err
 
 
+def _rows():
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "refine_meshes.npz"))
+    return [(str(g["shape"][i]), int(g["n"][i]), float(g["a"][i]), float(g["width"][i]), int(g["clevel"][i]),
+             int(g["flevel"][i]), i) for i in range(len(g["n"]))]
+
+
+@pytest.mark.parametrize("shape,n,a,width,cl,fl,i", _rows())
+def test_device_refinement_matches_reference(ctx, golden, shape, n, a, width, cl, fl, i):
+    """The device engine's mesh (up to four levels, 330k tets) against the reference's: every tet's vertices'
+    coordinates in tet order and local vertex order."""
+    g = golden("refine_meshes.npz")
+    kind, par = (tf.LS_SPHERE, [0.0, 0.0, 0.0, 1.0]) if shape == "sphere" else (tf.LS_TORUS, [1.0, 0.4, 2])
+    ctx.brick_cube(n, a)
+    last, steps = ctx.mesh_refine_band(kind, par, width, cl, fl)
+    assert last == fl
+    coords, tv, te, ev = ctx.mesh_download()
+    assert sha(coords[tv]) == str(g["tet_xyz_sha"][i])
+    # every edge of every tet is the uploaded edge between its two vertices
+    pairs = np.sort(np.stack([tv[:, [0, 0, 1, 0, 1, 2]], tv[:, [1, 2, 2, 3, 3, 3]]], -1), -1)
+    assert np.array_equal(np.sort(ev[te], -1), pairs)
+
+
 def test_refine_then_brick_again(ctx, golden):
     """A refined mesh is replaced by the next mesh call like any uploaded mesh."""
     g = golden("refine_sphere_p1_n4.npz")

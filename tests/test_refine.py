@@ -69,6 +69,44 @@ def test_refined_mesh_matches_reference(golden, shape, n, a, width, cl, fl, i):
     assert abs(vol - (2 * a) ** 3) <= 1e-9 * (2 * a) ** 3
 
 
+def parallel_host(shape, n, a, width, cl, fl):
+    """The device engine's kernel bodies run as host loops (tf_refine_band_parallel_host, outside the header)."""
+    import ctypes as C
+
+    L = tf.load_library()
+    om = O.brick(int(n), a=float(a))
+    kind, par = kind_par(shape)
+    par = np.asarray(par, np.float64)
+    h = C.c_void_p()
+    st = L.tf_refine_band_parallel_host(C.c_int64(len(om.coords)), om.coords.ctypes.data_as(C.c_void_p),
+                                        C.c_int64(len(om.tet_v)), om.tet_v.ctypes.data_as(C.c_void_p), C.c_int(kind),
+                                        par.ctypes.data_as(C.c_void_p), C.c_int(len(par)), C.c_double(width),
+                                        C.c_int(cl), C.c_int(fl), C.byref(h))
+    assert st == tf.OK, st
+    nv, ne, nt = C.c_int64(), C.c_int64(), C.c_int64()
+    ll, steps = C.c_int(), C.c_int()
+    L.tf_refined_info(h, C.byref(nv), C.byref(ne), C.byref(nt), C.byref(ll), C.byref(steps))
+    co = np.empty((nv.value, 3))
+    tv = np.empty((nt.value, 4), np.int32)
+    tl = np.empty(nt.value, np.int32)
+    pl = np.empty(ll.value + 1, np.int64)
+    p = lambda x: x.ctypes.data_as(C.c_void_p)
+    L.tf_refined_get(h, p(co), p(tv), None, None, p(tl), p(pl))
+    L.tf_refined_free(h)
+    return co, tv, tl, pl
+
+
+@pytest.mark.parametrize("shape,n,a,width,cl,fl,i", _rows())
+def test_parallel_engine_matches_reference(golden, shape, n, a, width, cl, fl, i):
+    """The data-parallel engine (level-synchronous passes, scans, two-phase edge table) gives the reference's
+    mesh bit for bit; on the device the same bodies run as kernels."""
+    g = golden("refine_meshes.npz")
+    co, tv, tl, pl = parallel_host(shape, n, a, width, cl, fl)
+    assert ",".join(map(str, pl.tolist())) == str(g["per_level"][i])
+    assert sha(tl.astype(np.int8)) == str(g["tet_level_sha"][i])
+    assert sha(co[tv]) == str(g["tet_xyz_sha"][i])
+
+
 @pytest.mark.parametrize("name", ["refine_sphere_p1_n4.npz", "refine_torus_p2_n3.npz"])
 def test_refined_system_mesh_and_oracle_numbering(golden, name):
     """The system fixtures' meshes, and the first-touch numbering of the oracle on the refined mesh against
