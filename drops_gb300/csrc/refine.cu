@@ -13,11 +13,12 @@
 // on any uploaded mesh, so the tet order, each tet's vertex order and the
 // vertex coordinates must be the reference's bit for bit.
 //
-// The refinement is a sequential walk over per-level tet lists whose order
-// is the product (children are appended in rule order, removed ones leave
-// gaps that later children do not fill); it runs on the host, once per mesh,
-// in time linear in the number of tets, and the mesh it produces is uploaded
-// to the device for the rest of the path.
+// This file is the sequential form: a walk over per-level tet lists whose
+// order is the product (children are appended in rule order, removed ones
+// leave the list, survivors keep their places), step by step as the
+// reference does it.  It serves tf_refine_band (host arrays, no device) and
+// generates the refinement rules.  The device path (tf_mesh_refine_band)
+// runs the same algorithm as data-parallel passes (refine_par.cu).
 //
 // Object model (what the order and the marks depend on):
 //   vertices  coordinates, level, removal mark;

@@ -120,7 +120,8 @@ int tf_mesh_download(tf_context* ctx, double* coords, int32_t* tet_v, int32_t* t
  * (levelset/adaptriang.cpp:36-44), i.e. at most 2 * fine_level rounds of
  * marking and MultiGridCL::Refine (geom/multigrid.cpp:389-453), with the
  * distance function of a TF_LS_SPHERE / TF_LS_TORUS / TF_LS_PLANE kind.
- * The context's mesh is replaced by the last triangulation level
+ * Runs on the device (level-synchronous passes; scans keep the reference's
+ * list order).  The context's mesh is replaced by the last triangulation level
  * (TriangFillCL order, geom/multigrid.cpp:1072-1083) as an uploaded mesh:
  * tets, their vertex order and the coordinates are the reference's; vertices
  * and edges are numbered by first touch.  The level set and everything after
@@ -129,8 +130,9 @@ int tf_mesh_download(tf_context* ctx, double* coords, int32_t* tet_v, int32_t* t
  * one global order (BrickBuilderCL's do; the refinement relies on it).       */
 int tf_mesh_refine_band(tf_context* ctx, int kind, const double* par, int npar, double width, int coarse_level,
                         int fine_level, int* last_level, int* steps);
-/* The same refinement on host arrays, without a context or a device: a level-0
- * mesh (coords[3*nv], tet_v[4*nt]) in, a handle to the refined mesh out.      */
+/* The same refinement on host arrays, without a context or a device (the
+ * reference's sequential steps on one core): a level-0 mesh (coords[3*nv],
+ * tet_v[4*nt]) in, a handle to the refined mesh out.                          */
 typedef struct tf_refined tf_refined;
 int tf_refine_band(int64_t nv, const double* coords, int64_t nt, const int32_t* tet_v, int kind, const double* par,
                    int npar, double width, int coarse_level, int fine_level, tf_refined** out);
