@@ -1,9 +1,11 @@
-"""Narrow-band refinement (tf_refine_band, host code of the library) against the reference.
+"""Narrow-band refinement on the host against the reference: the sequential form (tf_refine_band) and the
+device engine's kernel bodies run as host loops.
 
 The fixtures come from the reference's own AdapTriangCL::MakeInitialTriang with DistMarkingStrategyCL
 (oracle/ref_harness.cpp system_ref, tests/golden/make_golden.py): per-level tet counts, each triangulation tet's
 level and a digest of its vertices' coordinates in tet order and local vertex order.  The refinement rules are
-compared with the reference's table of geom/topo.cpp.  No device is needed.
+compared with the reference's table of geom/topo.cpp.  No device is needed; tests/test_gpu_refine.py runs the
+device engine.
 """
 import hashlib
 
