@@ -810,9 +810,10 @@ REFINE_N, REFINE_WIDTH, REFINE_LEVELS = 32, 0.05, 2
 def run_refine(args):
     """Narrow-band refinement of a 32^3 brick of the same box towards the same sphere (width 0.05, levels 0..2,
     AdapTriangCL::MakeInitialTriang with DistMarkingStrategyCL) and the P2 TraceFEM path on its last
-    triangulation level.  The refinement runs on the host (one core, wall clock, median of 3, including the
-    mesh's download and upload); the path (level set, DistributeDOFs, setupFESystem of M, A, C_n and the load
-    vector, LinComb, mixed PCG to 1e-10) is device time between stream markers, median of 3 after one warm-up."""
+    triangulation level.  The refinement runs on the device (wall clock of tf_mesh_refine_band, median of 3,
+    including reading back the level-0 mesh); the path (level set, DistributeDOFs, setupFESystem of M, A, C_n
+    and the load vector, LinComb, mixed PCG to 1e-10) is device time between stream markers, median of 3 after
+    one warm-up."""
     import drops_gb300 as tf
 
     ctx = tf.TraceFEM(0)
@@ -845,8 +846,8 @@ def run_refine(args):
             "cut_tets": na, "dofs": m, "path_ms": round(ms, 3), "cut_tets_per_s": round(na / (ms / 1e3), 1),
             "pcg_iters": int(statistics.median(its)),
             "note": f"{REFINE_N}^3 Kuhn cubes on [-5/3,5/3]^3 refined towards the unit sphere (width "
-                    f"{REFINE_WIDTH}, levels 0..{REFINE_LEVELS}); refine_ms on one host core, path_ms on the device "
-                    "(P2, mixed PCG), L2 flushed before each path"}
+                    f"{REFINE_WIDTH}, levels 0..{REFINE_LEVELS}); refine_ms: tf_mesh_refine_band on the device (wall "
+                    "clock), path_ms: the P2 path with mixed PCG on the device, L2 flushed before each path"}
 
 
 def quaqua_cpu_sample(threads, sample=4000):
