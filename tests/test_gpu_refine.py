@@ -105,6 +105,41 @@ def test_device_refinement_matches_reference(ctx, golden, shape, n, a, width, cl
     assert np.array_equal(np.sort(ev[te], -1), pairs)
 
 
+@pytest.mark.parametrize("case", [
+    ("upload", tf.LS_SPHERE, [0.0, 0.0, 0.0, 1.0], 0.1, 0, 2),
+    ("brick", tf.LS_PLANE, [0.3, 0.5, -0.2, 0.1], 0.05, 0, 2),
+    ("brick", tf.LS_SPHERE, [0.1, -0.2, 0.05, 0.8], 0.0, 1, 1),
+    ("brick", tf.LS_TORUS, [1.0, 0.4, 2], 0.02, 0, 3),
+])
+def test_device_refinement_equals_sequential_form(ctx, case):
+    """The device engine against the sequential form (pinned to the reference above) on other inputs: an
+    uploaded mesh, a plane, uniform refinement (coarse = fine level), a thin band at three levels."""
+    from oracle import pyoracle as O
+
+    how, kind, par, width, cl, fl = case
+    n, a = 5, 1.55
+    om = O.brick(n, a=a)
+    if how == "upload":
+        ctx.mesh_upload(om.coords, om.tet_v, om.tet_e, om.edge_v)
+    else:
+        ctx.brick_cube(n, a)
+    last, steps = ctx.mesh_refine_band(kind, par, width, cl, fl)
+    coords, tv, te, ev = ctx.mesh_download()
+    r = tf.refine_band(om.coords, om.tet_v, kind, par, width, cl, fl)
+    assert last == r["last_level"] and steps == r["steps"]
+    assert np.array_equal(coords[tv], r["coords"][r["tet_v"]])
+
+
+def test_refine_rejects_bad_input_on_device(ctx):
+    ctx.brick_cube(3, 1.0)
+    with pytest.raises(tf.TraceFEMError):
+        ctx.mesh_refine_band(tf.LS_SPHERE, [0.0, 0.0, 0.0, 1.0], 0.1, 2, 1)
+    with pytest.raises(tf.TraceFEMError):
+        ctx.mesh_refine_band(tf.LS_ELLIPSOID, [0.0] * 15, 0.1, 0, 1)
+    # the context keeps its mesh after a refused call
+    assert ctx.mesh_info()[2] == 6 * 27
+
+
 def test_refine_then_brick_again(ctx, golden):
     """A refined mesh is replaced by the next mesh call like any uploaded mesh."""
     g = golden("refine_sphere_p1_n4.npz")
