@@ -24,6 +24,9 @@
 //       (surfactant/ifacetransp.cpp:367-380, 499-512, 532-563) on the unit sphere,
 //       P2 level set, CreateNumbering(P1IF_FE)
 //   ref_harness area <out>                  tests/principallattice.cpp:316-347
+//   ref_harness gmres_ref <n> <a> <steps> <width> <coarse> <fine> <out>
+//       the same on the last level of the brick refined towards the torus
+//       (AdapTriangCL::MakeInitialTriang, DistMarkingStrategyCL).
 //   ref_harness quaqua <n> <a> <out>
 //       Isoparametric P2 TraceFEM on the unit sphere (surfactant/surfactant.cpp:
 //       1581-1640): P2 level set by nodal interpolation, the recovered
@@ -627,28 +630,45 @@ class NodalBlockJacobiPcCL {
 };
 
 int cmd_gmres(int argc, char** argv) {
-    if (argc < 6) throw std::invalid_argument("usage: gmres n a steps out");
+    // "gmres_ref": the brick first refined towards the torus (width, coarse
+    // and fine level before <out>, surfphasesep.cpp:170-181), everything on
+    // the last level
+    const bool refine = std::string(argv[1]) == "gmres_ref";
+    if (argc < (refine ? 9 : 6))
+        throw std::invalid_argument("usage: gmres n a steps out | gmres_ref n a steps width coarse fine out");
     const int n = std::atoi(argv[2]);
     const double a = std::atof(argv[3]);
     const int steps = std::atoi(argv[4]);
-    Writer w(argv[5]);
+    Writer w(argv[refine ? 8 : 5]);
 
     BrickBuilderCL brick(Point3DCL(-a), 2. * a * std_basis<3>(1), 2. * a * std_basis<3>(2), 2. * a * std_basis<3>(3), n, n,
                          n);
     MultiGridCL mg(brick);
+    if (refine) {
+        AdapTriangCL adap(mg);
+        DistMarkingStrategyCL marker([&](Point3DCL const& x, double) { return ls_value("torus", x); },
+                                     std::atof(argv[5]), std::atoi(argv[6]), std::atoi(argv[7]));
+        adap.set_marking_strategy(&marker);
+        adap.MakeInitialTriang();
+        adap.set_marking_strategy(nullptr);
+        Flat F = flatten(mg, (int)mg.GetLastLevel());
+        w.l("tet_v", F.tet_v);
+        w.d("coords", F.coords);
+    }
+    const int L = (int)mg.GetLastLevel();
     FESystem sys;
     auto& levelSet = sys.params.levelSet;
     IdxDescCL lsIdx(P2_FE);
-    lsIdx.DistributeDOFs(0, mg);
+    lsIdx.DistributeDOFs(L, mg);
     levelSet.SetIdx(&lsIdx);
     const Uint li = lsIdx.GetIdx();
     // P1 level set stored as a P2 vector (LinearLSInit, surfactant/surfactant.cpp:748-758)
-    DROPS_FOR_TRIANG_VERTEX(mg, 0, it) levelSet.Data[it->Unknowns(li)] = ls_value("torus", it->GetCoord());
-    DROPS_FOR_TRIANG_EDGE(mg, 0, it)
+    DROPS_FOR_TRIANG_VERTEX(mg, L, it) levelSet.Data[it->Unknowns(li)] = ls_value("torus", it->GetCoord());
+    DROPS_FOR_TRIANG_EDGE(mg, L, it)
         levelSet.Data[it->Unknowns(li)] = 0.5 * (levelSet.Data[it->GetVertex(0)->Unknowns(li)] +
                                                  levelSet.Data[it->GetVertex(1)->Unknowns(li)]);
     IdxDescCL ifIdx(P1IF_FE);
-    ifIdx.DistributeDOFs(0, mg, &levelSet);
+    ifIdx.DistributeDOFs(L, mg, &levelSet);
     const size_t m = ifIdx.NumUnknowns();
     w.i("n_dofs", (int64_t)m);
     sys.params.surfCahnHilliardParams.f = [](Point3DCL const& x, double) {
@@ -750,7 +770,7 @@ int cmd_gmres(int argc, char** argv) {
     // surfactant/ifacetransp.h:1533-1544) and wind convection N_P1P1 (:1590-1600)
     {
         IdxDescCL velIdx(vecP2IF_FE);
-        velIdx.DistributeDOFs(0, mg, &levelSet);
+        velIdx.DistributeDOFs(L, mg, &levelSet);
         VecDescCL wind(&velIdx);
         wind.Interpolate(mg, [](Point3DCL const& x) { return wind_value(x); });
         std::uniform_real_distribution<double> U3(-0.3, 0.3);
@@ -895,7 +915,7 @@ int main(int argc, char** argv) {
         if (cmd == "legacy_numb") return cmd_legacy_numb(argc, argv);
         if (cmd == "legacy_forms") return cmd_legacy_forms(argc, argv);
         if (cmd == "area") return cmd_area(argc, argv);
-        if (cmd == "gmres") return cmd_gmres(argc, argv);
+        if (cmd == "gmres" || cmd == "gmres_ref") return cmd_gmres(argc, argv);
         if (cmd == "quaqua") return cmd_quaqua(argc, argv);
         throw std::invalid_argument("unknown command " + cmd);
     } catch (std::exception& e) {

@@ -135,6 +135,20 @@ def refine_meshes_case():
     print("refine meshes", [r["per_level"].tolist() for r in rows])
 
 
+def ch_refined_case(n=6, a=1.62, width=0.1, clevel=0, flevel=2, steps=3):
+    """Cahn-Hilliard BDF1 steps (the reference's block constructor and GMRES(50)) on the brick refined
+    towards the torus first, as the surface driver does (surfphasesep.cpp:170-181, 414-440)."""
+    d = run("gmres_ref", str(n), repr(a), str(steps), repr(width), str(clevel), str(flevel))
+    tet_xyz = d["coords"].reshape(-1, 3)[d["tet_v"].reshape(-1, 4)]
+    m = int(d["n_dofs"][0])
+    out = dict(n=n, a=a, width=width, clevel=clevel, flevel=flevel, tet_xyz_sha=sha(tet_xyz), n_dofs=m,
+               dt=d["dt"][0], eps=d["eps"][0], rho=d["rho"][0], beta_s=d["beta_s"][0], xi=d["xi"][0],
+               chi0=d["chi0"], block_iters=int(d["block_iters"][0]), block_x=d["block_x"],
+               steps_iters=d["steps_iters"], steps_X=d["steps_X"].reshape(steps, 2 * m))
+    np.savez_compressed(os.path.join(HERE, f"ch_torus_refined_n{n}.npz"), **out)
+    print("ch refined", n, "dofs", m, "block", out["block_iters"], "steps", out["steps_iters"].tolist())
+
+
 def rules_case():
     """The 64 refinement rules of geom/topo.cpp: children per edge pattern, local points in order."""
     d = run("rules")
@@ -244,3 +258,4 @@ if __name__ == "__main__":
     refine_case("refine_torus_p2_n3.npz", "p2", "lsP2", "torus", 3, 1.62, 0.05, 0, 1, False)
     rules_case()
     refine_meshes_case()
+    ch_refined_case()

@@ -147,3 +147,55 @@ def test_refine_then_brick_again(ctx, golden):
     ctx.brick_cube(4, 1.0)
     nv, ne, nt = ctx.mesh_info()
     assert nt == 6 * 4 ** 3 and nv == 5 ** 3
+
+
+def ch_setup(ctx, g):
+    """The brick refined towards the torus, P1 level set, P1IF numbering, M, A, C_n."""
+    ctx.brick_cube(int(g["n"]), float(g["a"]))
+    ctx.mesh_refine_band(tf.LS_TORUS, [1.0, 0.4, 2], float(g["width"]), int(g["clevel"]), int(g["flevel"]))
+    coords, tv, te, ev = ctx.mesh_download()
+    assert sha(coords[tv]) == str(g["tet_xyz_sha"])
+    ctx.levelset_analytic(tf.LS_TORUS, [1.0, 0.4, 2], False)
+    na, nd = ctx.distribute_dofs(tf.P1IF)
+    assert nd == int(g["n_dofs"])
+    ctx.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN])
+    return nd
+
+
+def test_refined_ch_block_solve(ctx, golden):
+    """One implicit Cahn-Hilliard step on the refined torus mesh: the block matrix of surfphasesep.cpp:431-434
+    and GMRES(50) with nodal block Jacobi from a zero guess, against the reference's (iterations within 2,
+    solution within 1e-9)."""
+    g = golden("ch_torus_refined_n6.npz")
+    nd = ch_setup(ctx, g)
+    dt, eps, rho, beta, xi = (float(g[k]) for k in ("dt", "eps", "rho", "beta_s", "xi"))
+    ctx.ch_block(1.0 / dt, 1.0, rho, eps * eps, beta)
+    rp, ci, M = ctx.matrix(tf.FORM_M)
+    chi = g["chi0"]
+    from oracle import pyoracle as O
+
+    Mc = O.spmv(rp, ci, M, chi)
+    Mf = O.spmv(rp, ci, M, xi * 2 * chi * (1 - chi) * (1 - 2 * chi))
+    ctx.vec_upload(tf.VEC_B, np.concatenate([Mc / dt, beta * Mc - Mf]))
+    ctx.vec_fill(tf.VEC_X, 2 * nd, 0.0)
+    st, it, res = ctx.gmres_jacobi(tf.MAT_BLOCK, tf.VEC_B, tf.VEC_X, restart=50, tol=1e-10, max_iter=20000)
+    assert st == tf.OK and res <= 1e-10, (st, it, res)
+    assert abs(it - int(g["block_iters"])) <= 2, (it, int(g["block_iters"]))
+    ok, err = sol_close(ctx.vec_download(tf.VEC_X), g["block_x"])
+    assert ok, err
+
+
+def test_refined_ch_steps(ctx, golden):
+    """Three warm-started BDF1 steps on the refined torus mesh (the surface driver's pipeline: refinement,
+    interface numbering, forms, block GMRES) against the reference: iterations within 2 per step, state
+    within 1e-9 after each step."""
+    g = golden("ch_torus_refined_n6.npz")
+    nd = ch_setup(ctx, g)
+    dt, eps, rho, beta, xi = (float(g[k]) for k in ("dt", "eps", "rho", "beta_s", "xi"))
+    ctx.vec_upload(tf.VEC_X, np.concatenate([g["chi0"], np.zeros(nd)]))
+    for k in range(len(g["steps_iters"])):
+        st, its, res = ctx.ch_steps(1, dt, 1.0, eps, beta, xi, rho, restart=50, tol=1e-10)
+        assert st == tf.OK and np.all(res <= 1e-10)
+        assert abs(int(its[0]) - int(g["steps_iters"][k])) <= 2, (k, its, g["steps_iters"])
+        ok, err = sol_close(ctx.vec_download(tf.VEC_X), g["steps_X"][k])
+        assert ok, (k, err)
