@@ -24,7 +24,8 @@
 //
 // T = float: the mixed-precision solver (FP32 iterations, the FP32 correction
 // folded into the FP64 iterate at each refinement, refinement when the FP32
-// residual has dropped by 0.1, claims convergence or max_iter is reached;
+// residual has dropped by a factor 0.2 (TF_PCG_REL_UPDATE), claims
+// convergence or max_iter is reached;
 // convergence is decided on the FP64 residual b - A x).
 // T = double: the FP64 solver on the same structure (32-byte state, FP64
 // dots); it refines only when the recursive residual claims convergence or at
@@ -626,7 +627,7 @@ int pcg_resident(Context* c, CSR& A, const double* b, double* x, int* max_iter, 
     g.max_iter = *max_iter;
     g.tol = *tol;
     g.rel = rel;
-    g.rel_update = sizeof(T) == 4 ? 0.1 : 0.0;
+    g.rel_update = sizeof(T) == 4 ? c->pcg_rel_update : 0.0;
     g.out_iter = c->kry_iters.p;
     g.out_resid = c->kry_resid.p;
     g.out_updates = c->kry_iters.p + 1;
