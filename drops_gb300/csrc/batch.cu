@@ -193,9 +193,8 @@ struct BatchPcgArgs {
     int max_iter;
     double tol;
     int rel;
+    double rel_update;      // mixed: FP64 residual replacement when the FP32 one dropped by this factor
 };
-
-constexpr double kBatchRelUpdate = 0.1;
 
 // scalar state of one instance's solve, owned by thread 0, read by all
 struct BatchScalars {
@@ -210,7 +209,7 @@ struct BatchScalars {
 //               like the reference;
 //   V = float:  FP32 iterations; x accumulates in FP64 and the FP64 true
 //               residual replaces the FP32 one whenever the latter dropped by
-//               kBatchRelUpdate or claims convergence (reliable updates).
+//               a.rel_update or claims convergence (reliable updates).
 template <int G, class V>
 __device__ void batch_pcg_instance(const BatchPcgArgs& a, int inst, double* sh, BatchScalars& sc) {
     constexpr bool kMixed = sizeof(V) == 4;
@@ -331,7 +330,7 @@ __device__ void batch_pcg_instance(const BatchPcgArgs& a, int inst, double* sh, 
             cta_sum<2, V>(v, sh, [&](const double* s) {
                 const double rn = sqrt(s[0]);
                 if (kMixed) {
-                    sc.true_res = rn <= kBatchRelUpdate * sc.r_last || rn / sc.normb <= tol || it == max_iter;
+                    sc.true_res = rn <= a.rel_update * sc.r_last || rn / sc.normb <= tol || it == max_iter;
                     if (!sc.true_res) {
                         sc.beta_d = s[1] / sc.rho;
                         sc.beta_f = (float)sc.beta_d;
@@ -519,6 +518,7 @@ static int batch_launch(Context* c, const BatchSetup& s, const double* b, double
     a.x = x;
     a.max_iter = max_iter;
     a.tol = tol;
+    a.rel_update = c->batch_rel_update;
     a.rel = rel;
     TF_CUDA(c, cudaMemsetAsync(a.queue, 0, sizeof(int), c->stream));
     void* args[] = {&a};

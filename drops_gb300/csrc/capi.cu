@@ -136,6 +136,7 @@ int tf_create(tf_context** out, int device) {
     }
     if (const char* e = std::getenv("TF_PCG_RES_VCAP_KB")) c->pcg_res_vcap_kb = std::atoi(e);
     if (const char* e = std::getenv("TF_PCG_REL_UPDATE")) c->pcg_rel_update = std::atof(e);
+    if (const char* e = std::getenv("TF_BATCH_REL_UPDATE")) c->batch_rel_update = std::atof(e);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
         cudaMallocHost((void**)&c->h_status, 4 * sizeof(int)) != cudaSuccess ||

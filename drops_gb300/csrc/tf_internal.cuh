@@ -351,6 +351,7 @@ struct Context {
     int pcg_fp64_kernel = 0;    // TF_PCG_FP64_CLASSIC or TF_PCG_FP64_CG1
     int pcg_res_vcap_kb = -1;   // resident PCG: cap on the KB of matrix values kept in shared memory (-1: none)
     double pcg_rel_update = 0.2;  // mixed resident PCG: FP64 refinement when the FP32 residual dropped by this
+    double batch_rel_update = 0.2;  // mixed batched PCG: the same factor
     DBuf<float2> x_pairs;       // SpMV operand split into FP32 pairs
     bool spmv_pair = false;     // tf_spmv: FP32-pair kernel instead of the FP64-FMA one
     bool asm_fp64 = false;      // P2 forms: the FP64 kernel instead of the FP32-pair one
