@@ -850,6 +850,21 @@ def run_refine(args):
                     "clock), path_ms: the P2 path with mixed PCG on the device, L2 flushed before each path"}
 
 
+def refine_cpu_sample():
+    """The sequential form of the same refinement (tf_refine_band: the reference's steps on one core, no
+    device), on the same brick, median of 3 wall clocks in ms."""
+    import drops_gb300 as tf
+    from oracle import pyoracle as O
+
+    om = O.brick(REFINE_N, a=HALF)
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        r = tf.refine_band(om.coords, om.tet_v, tf.LS_SPHERE, SPHERE, REFINE_WIDTH, 0, REFINE_LEVELS)
+        ts.append((time.perf_counter() - t0) * 1e3)
+    return statistics.median(ts), len(r["tet_level"])
+
+
 def quaqua_cpu_sample(threads, sample=4000):
     """The oracle's QuaQua element forms on the first `sample` cut tets of the same problem (one thread: the
     reference accumulates them serially), as cut tets/s."""
@@ -971,6 +986,12 @@ def main():
                 v, sample = quaqua_cpu_sample(threads)
                 out["quaqua"]["cpu_baseline"] = {"value": round(v, 1), "unit": "cut_tets/s", "cores": 1,
                                                  "kind": "port", "sample": sample}
+            if "refine" in out:
+                ms, ntets = refine_cpu_sample()
+                out["refine"]["cpu_baseline"] = {
+                    "value": round(ms, 1), "unit": "ms", "cores": 1, "kind": "port",
+                    "sample": f"the same refinement ({ntets} tets) by tf_refine_band, the library's sequential form "
+                              "of the reference's steps (pinned to its refined meshes), one core, median of 3"}
         print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()
