@@ -203,6 +203,8 @@ int tf_destroy(tf_context* t) {
     tf::release(c->order_keys);
     tf::release(c->order_tmp);
     tf::release(c->qq_grad);
+    tf::release(c->qq_base);
+    tf::release(c->qq_idx);
     tf::release(c->tune_buf);
     tf::release(c->ch_ring);
     tf::release(c->ch_av);

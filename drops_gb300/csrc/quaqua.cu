@@ -27,19 +27,19 @@
 //   4. LocalMassP2CL, LocalLaplaceBeltramiP2CL (W^-1 applied to the tangential
 //      P2 gradients) and LocalVectorP2CL (f at the base points)
 //      (surfactant/ifacetransp.h:2286-2402).
-// One half-warp per active tet (two tets per warp: an FP64 warp instruction
-// costs the same with 14 active lanes as with 32); lane p < 14 of the half
-// owns quadrature point p (two facets at most on the linear interface).  The
-// points' data go to shared memory and the element entries are summed over
-// the points in point order.
+// The tets are set up once (one thread each); their quadrature points (7 per
+// facet, two facets at most on the linear interface) are numbered densely and
+// run one thread each, in two passes (the Newton solve; the Jacobian, measure
+// and transformation), so that every FP64 warp instruction has 32 active
+// lanes.  The element entries are summed per tet over its points in point
+// order.
 #include "tf_internal.cuh"
 
 namespace tf {
 
 namespace {
 
-constexpr int kQqWarps = 4;
-constexpr int kQqPts = 14;
+constexpr int kQqPts = 14;  // quadrature points of a tet, at most
 
 struct Q5 {
     double node[7][3], w[7];
@@ -58,15 +58,18 @@ struct QqArgs {
     double* elem_rhs;  // [n_active][10]
     int* status;
     int* newton_max;  // largest Newton iteration count of a point
+    double* base;     // [points][8]: base point x, s and its barycentric b (Newton pass -> forms pass)
     Q5 q;
     double tol, armijo, rhs_c;
     int maxiter, max_damping;
 };
 
-struct QqSmem {
+// one cut tet: vertices, level-set values, barycentric gradients, the
+// recovered gradient at its 10 nodes, h, and the linear interface's cut points
+struct QqTet {
     double X[4][3], gl[4][3], f[10], gh[10][3], h;
-    double wa[kQqPts], fy[kQqPts], phi[kQqPts][10], sg[kQqPts][10][3];
-    int npts;
+    int cut[4];
+    int nr, bnd, npts, pad;
 };
 
 // world gradients of the barycentric coordinates (GetTrafoTr) and det J
@@ -223,32 +226,41 @@ __device__ void qq_p2(const double b[4], const double gl[4][3], double phi[10], 
     }
 }
 
-// ls, its gradient, gh and (optionally) dgh = sum_k gh_k (x) grad phi_k of the tet's polynomials at b
-__device__ void qq_eval(const QqSmem& S, const double b[4], double* ls, double gls[3], double gh[3], double (*dgh)[3]) {
-    double phi[10], g[10][3];
-    qq_p2(b, S.gl, phi, g);
-    double l = 0.;
-    for (int k = 0; k < 10; ++k) l += S.f[k] * phi[k];
+// ls, its gradient, gh and (optionally) dgh = sum_k gh_k (x) grad phi_k of the tet's polynomials at b;
+// the basis functions one at a time (FE_P2CL's values and gradients), every sum in k order
+__device__ void qq_eval(const QqTet& S, const double b[4], double* ls, double gls[3], double gh[3], double (*dgh)[3]) {
+    double l = 0., s[3] = {0., 0., 0.}, s2[3] = {0., 0., 0.}, v[3][3] = {{0., 0., 0.}, {0., 0., 0.}, {0., 0., 0.}};
+#pragma unroll 1
+    for (int k = 0; k < 10; ++k) {
+        double phi, g[3];
+        if (k < 4) {
+            phi = b[k] * (2. * b[k] - 1.);
+            for (int r = 0; r < 3; ++r) g[r] = (4. * b[k] - 1.) * S.gl[k][r];
+        } else {
+            const int a = ev0(k - 4), c = ev1(k - 4);
+            phi = 4. * b[a] * b[c];
+            for (int r = 0; r < 3; ++r) g[r] = 4. * (b[c] * S.gl[a][r] + b[a] * S.gl[c][r]);
+        }
+        l += S.f[k] * phi;
+        for (int r = 0; r < 3; ++r) {
+            s[r] += S.f[k] * g[r];
+            s2[r] += S.gh[k][r] * phi;
+        }
+        if (dgh)
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) v[r][c] += S.gh[k][r] * g[c];
+    }
     *ls = l;
     for (int r = 0; r < 3; ++r) {
-        double s = 0., s2 = 0.;
-        for (int k = 0; k < 10; ++k) {
-            s += S.f[k] * g[k][r];
-            s2 += S.gh[k][r] * phi[k];
-        }
-        gls[r] = s;
-        gh[r] = s2;
+        gls[r] = s[r];
+        gh[r] = s2[r];
     }
     if (dgh)
         for (int r = 0; r < 3; ++r)
-            for (int c = 0; c < 3; ++c) {
-                double v = 0.;
-                for (int k = 0; k < 10; ++k) v += S.gh[k][r] * g[k][c];
-                dgh[r][c] = v;
-            }
+            for (int c = 0; c < 3; ++c) dgh[r][c] = v[r][c];
 }
 
-__device__ void qq_w2b(const QqSmem& S, const double x[3], double b[4]) {
+__device__ void qq_w2b(const QqTet& S, const double x[3], double b[4]) {
     const double d[3] = {x[0] - S.X[0][0], x[1] - S.X[0][1], x[2] - S.X[0][2]};
     b[0] = 1.;
     for (int k = 1; k < 4; ++k) {
@@ -291,30 +303,30 @@ __device__ bool qq_solve(int n, double A[4][4], double x[4]) {
 __device__ inline double nrm3(const double v[3]) { return sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
 __device__ inline double dt3(const double a[3], const double b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
 
-__global__ void __launch_bounds__(32 * kQqWarps) k_qq_assemble(QqArgs a) {
-    extern __shared__ __align__(16) unsigned char qq_dyn[];
-    QqSmem* all = reinterpret_cast<QqSmem*>(qq_dyn);
-    const int wl = threadIdx.x >> 5, half = (threadIdx.x >> 4) & 1, lane = threadIdx.x & 15;
-    QqSmem& S = all[2 * wl + half];
-    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5, nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t pr = gw; 2 * pr < a.n_active; pr += nw) {
-        const int64_t qa = 2 * pr + half;
-        const bool live = qa < a.n_active;  // the second half of the last pair may have no tet
-        if (live) {
-            const int64_t t = a.active[qa];
-            if (lane == 0) {
-                int32_t tv[4], te[6];
-                qq_tet_data(a.M, a.ls_vert, a.ls_edge, t, S.X, S.f, tv, te);
-                double det;
-                qq_trafo(S.X, S.gl, &det);
-                S.h = cbrt(fabs(det));
-            }
-            for (int q = lane; q < 30; q += 16) {
-                const int k = q / 3, r = q - 3 * k;
-                S.gh[k][r] = a.grad[3 * (int64_t)a.loc2glo[qa * 10 + k] + r];
-            }
+// The tets' data (coordinates, level set, barycentric gradients, the
+// recovered gradient at the 10 nodes, the linear interface's cut points) are
+// set up once per tet; the quadrature points of all tets are then numbered
+// densely (7 per facet, a scan over the tets) and run one thread each: the
+// Newton solve for the base point, then the mapping's Jacobian, the measure
+// and the gradient transformation (FP64 work: full warps keep all 32 lanes of
+// every FP64 warp instruction busy, where a half-warp per tet used 7 or 14).
+// The element entries are summed per tet over its points in point order.
+constexpr int kQqPtData = 42;  // per point: w |det|, f(y), the 10 P2 values, the 10 transformed surface gradients
+
+__global__ void k_qq_tets(QqArgs a, QqTet* __restrict__ tets, int32_t* __restrict__ npts) {
+    for (int64_t qa = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; qa < a.n_active;
+         qa += (int64_t)gridDim.x * blockDim.x) {
+        QqTet& S = tets[qa];
+        const int64_t t = a.active[qa];
+        int32_t tv[4], te[6];
+        qq_tet_data(a.M, a.ls_vert, a.ls_edge, t, S.X, S.f, tv, te);
+        double det;
+        qq_trafo(S.X, S.gl, &det);
+        S.h = cbrt(fabs(det));
+        for (int q = 0; q < 30; ++q) {
+            const int k = q / 3, r = q - 3 * k;
+            S.gh[k][r] = a.grad[3 * (int64_t)a.loc2glo[qa * 10 + k] + r];
         }
-        __syncwarp();
         // the linear interface of the vertex values (SignTraitsCL / RefPatchCL on one sub-tet)
         int sg[4], nz = 0;
         bool mixed = false;
@@ -323,18 +335,45 @@ __global__ void __launch_bounds__(32 * kQqWarps) k_qq_assemble(QqArgs a) {
             mixed |= sg[k] != sg[0];
             nz += sg[k] == 0;
         }
-        int cut[4], nr = 0;
+        int nr = 0;
+        for (int k = 0; k < 4; ++k) S.cut[k] = 0;
         if (mixed) {
             for (int k = 0; k < 4; ++k)
-                if (sg[k] == 0) cut[nr++] = k;
+                if (sg[k] == 0) S.cut[nr++] = k;
             for (int e = 0; e < 6 && nr < 4; ++e)
-                if (sg[ev0(e)] * sg[ev1(e)] == -1) cut[nr++] = e + 4;
+                if (sg[ev0(e)] * sg[ev1(e)] == -1) S.cut[nr++] = e + 4;
         }
-        if (live && nz == 4 && lane == 0) atomicCAS(a.status, 0, TF_ERR_ZERO_PATTERN);
-        const int nf = live && nr >= 3 ? nr - 2 : 0;
-        const bool bnd = nz == 3;
-        const int npts = 7 * nf;
-        // facet vertices (barycentric) of facet f, vertex j
+        if (nz == 4) atomicCAS(a.status, 0, TF_ERR_ZERO_PATTERN);
+        const int nf = nr >= 3 ? nr - 2 : 0;
+        S.nr = nr;
+        S.bnd = nz == 3;
+        S.npts = 7 * nf;
+        npts[qa] = 7 * nf;
+    }
+}
+
+__global__ void k_qq_point_tets(int64_t na, const int32_t* __restrict__ npts, const int32_t* __restrict__ off,
+                                int32_t* __restrict__ pt_tet) {
+    for (int64_t qa = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; qa < na; qa += (int64_t)gridDim.x * blockDim.x)
+        for (int j = 0; j < npts[qa]; ++j) pt_tet[off[qa] + j] = (int32_t)qa;
+}
+
+// PH 0: the base point (x, s) by Newton and its barycentric b; PH 1: from the
+// stored base point, the point's weight x measure, f(y), P2 values and
+// transformed surface gradients.  Both phases rebuild the facet geometry of
+// the point with the same operations.
+template <int PH>
+__global__ void __launch_bounds__(128) k_qq_points(QqArgs a, const QqTet* __restrict__ tets,
+                                                   const int32_t* __restrict__ off,
+                                                   const int32_t* __restrict__ pt_tet, int64_t npt,
+                                                   double* __restrict__ pdata) {
+    for (int64_t pid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; pid < npt;
+         pid += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t qa = pt_tet[pid];
+        const QqTet& S = tets[qa];
+        const int lane = (int)(pid - off[qa]);
+        const int* cut = S.cut;
+        const bool bnd = S.bnd != 0;
         auto fvert = [&](int f, int j, double b[4]) {
             const int cv = cut[f + j];
             for (int c = 0; c < 4; ++c) b[c] = 0.;
@@ -350,7 +389,7 @@ __global__ void __launch_bounds__(32 * kQqWarps) k_qq_assemble(QqArgs a) {
         auto world = [&](const double b[4], double x[3]) {
             for (int r = 0; r < 3; ++r) x[r] = S.X[0][r] * b[0] + S.X[1][r] * b[1] + S.X[2][r] * b[2] + S.X[3][r] * b[3];
         };
-        if (lane < npts) {
+        {
             const int f = lane / 7, qn = lane - 7 * f;
             double B[3][4], W3[3][3];
             for (int j = 0; j < 3; ++j) {
@@ -395,11 +434,17 @@ __global__ void __launch_bounds__(32 * kQqWarps) k_qq_assemble(QqArgs a) {
             double bq[4];
             for (int c = 0; c < 4; ++c) bq[c] = B[0][c] * a.q.node[qn][0] + B[1][c] * a.q.node[qn][1] + B[2][c] * a.q.node[qn][2];
             const double wq = fdet * a.q.w[qn];
+            double* const bp = a.base + (size_t)pid * 8;
+            double x[4], b[4];
+            double ls, gls[3], gh[3], dgh[3][3];
+            if constexpr (PH == 0) {
             // Newton for the base point on the tet's extended polynomials
             double x0[3];
             world(bq, x0);
-            double x[4] = {x0[0], x0[1], x0[2], 0.}, b[4] = {bq[0], bq[1], bq[2], bq[3]};
-            double ls, gls[3], gh[3], dgh[3][3], F[4];
+            for (int i = 0; i < 3; ++i) x[i] = x0[i];
+            x[3] = 0.;
+            for (int i = 0; i < 4; ++i) b[i] = bq[i];
+            double F[4];
             qq_eval(S, b, &ls, gls, gh, nullptr);
             F[0] = F[1] = F[2] = 0.;
             F[3] = -ls;
@@ -460,6 +505,16 @@ __global__ void __launch_bounds__(32 * kQqWarps) k_qq_assemble(QqArgs a) {
                 }
             }
             atomicMax(a.newton_max, iter);
+            for (int i = 0; i < 4; ++i) {
+                bp[i] = x[i];
+                bp[4 + i] = b[i];
+            }
+            } else {
+            double* const P = pdata + (size_t)pid * kQqPtData;
+            for (int i = 0; i < 4; ++i) {
+                x[i] = bp[i];
+                b[i] = bp[4 + i];
+            }
             // Jacobian of the mapping at the base point
             qq_eval(S, b, &ls, gls, gh, dgh);
             const double ngh = nrm3(gh), dh = x[3] * ngh, ngl = nrm3(gls);
@@ -509,42 +564,56 @@ __global__ void __launch_bounds__(32 * kQqWarps) k_qq_assemble(QqArgs a) {
             }
             double phi[10], g[10][3];
             qq_p2(bq, S.gl, phi, g);
-            S.wa[lane] = wq * absd;
+            P[0] = wq * absd;
             double y[3];
             for (int r = 0; r < 3; ++r) y[r] = x[r];
-            S.fy[lane] = a.rhs_c * y[0] * y[1] * y[2];
+            P[1] = a.rhs_c * y[0] * y[1] * y[2];
             for (int i = 0; i < 10; ++i) {
-                S.phi[lane][i] = phi[i];
+                P[2 + i] = phi[i];
                 const double gn = dt3(g[i], nl);
                 double tg[3];
                 for (int r = 0; r < 3; ++r) tg[r] = g[i][r] - gn * nl[r];
-                for (int r = 0; r < 3; ++r) S.sg[lane][i][r] = Wi[r][0] * tg[0] + Wi[r][1] * tg[1] + Wi[r][2] * tg[2];
+                for (int r = 0; r < 3; ++r) P[12 + 3 * i + r] = Wi[r][0] * tg[0] + Wi[r][1] * tg[1] + Wi[r][2] * tg[2];
+            }
             }
         }
-        __syncwarp();
-        // element entries, summed over the points in point order: 55 M, 55 A, 10 b
-        for (int e = lane; e < 120 && live; e += 16) {
-            double s = 0.;
-            if (e < 110) {
-                const int k = e < 55 ? e : e - 55;
-                int i = 0, rem = k;
-                while (rem >= 10 - i) {
-                    rem -= 10 - i;
-                    ++i;
-                }
-                const int j = i + rem;
+    }
+}
+
+// the element entries of tet qa, summed over its points in point order: 55 M, 55 A, 10 b
+__global__ void k_qq_sums(QqArgs a, const int32_t* __restrict__ off, const double* __restrict__ pdata) {
+    const int64_t total = a.n_active * 120;
+    for (int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; id < total;
+         id += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t qa = id / 120;
+        const int e = (int)(id - qa * 120);
+        const int64_t p0 = off[qa];
+        const int npts = off[qa + 1] - off[qa];
+        double s = 0.;
+        if (e < 110) {
+            const int k = e < 55 ? e : e - 55;
+            int i = 0, rem = k;
+            while (rem >= 10 - i) {
+                rem -= 10 - i;
+                ++i;
+            }
+            const int j = i + rem;
+            for (int p = 0; p < npts; ++p) {
+                const double* P = pdata + (size_t)(p0 + p) * kQqPtData;
                 if (e < 55)
-                    for (int p = 0; p < npts; ++p) s += S.wa[p] * S.phi[p][i] * S.phi[p][j];
+                    s += P[0] * P[2 + i] * P[2 + j];
                 else
-                    for (int p = 0; p < npts; ++p) s += S.wa[p] * dt3(S.sg[p][i], S.sg[p][j]);
-                (e < 55 ? a.elem_m : a.elem_a)[qa * 55 + k] = s;
-            } else {
-                const int i = e - 110;
-                for (int p = 0; p < npts; ++p) s += S.wa[p] * S.fy[p] * S.phi[p][i];
-                a.elem_rhs[qa * 10 + i] = s;
+                    s += P[0] * dt3(P + 12 + 3 * i, P + 12 + 3 * j);
             }
+            (e < 55 ? a.elem_m : a.elem_a)[qa * 55 + k] = s;
+        } else {
+            const int i = e - 110;
+            for (int p = 0; p < npts; ++p) {
+                const double* P = pdata + (size_t)(p0 + p) * kQqPtData;
+                s += P[0] * P[1] * P[2 + i];
+            }
+            a.elem_rhs[qa * 10 + i] = s;
         }
-        __syncwarp();
     }
 }
 
@@ -559,6 +628,16 @@ int quaqua_elements(Context* c, double rhs_c, double tol, int maxiter, int* newt
     TF_TRY(ensure(c, c->qq_grad, (size_t)(3 * (m > 0 ? m : 1))));
     TF_TRY(ensure(c, c->elem, (size_t)TF_NUM_FORMS * (size_t)(na > 0 ? na : 1) * 55));
     TF_TRY(ensure(c, c->elem_rhs, (size_t)(na > 0 ? na : 1) * 10));
+    // per tet its data; per point (at most 14 per tet) the base point and the point data
+    const size_t tet_words = ((size_t)(na > 0 ? na : 1) * sizeof(QqTet) + 7) / 8;
+    const size_t max_pts = (size_t)(na > 0 ? na : 1) * kQqPts;
+    TF_TRY(ensure(c, c->qq_base, tet_words + max_pts * (8 + kQqPtData)));
+    TF_TRY(ensure(c, c->qq_idx, (size_t)(2 * (na + 1)) + max_pts));
+    QqTet* tets = reinterpret_cast<QqTet*>(c->qq_base.p);
+    double* pdata = c->qq_base.p + tet_words + max_pts * 8;
+    int32_t* npts = c->qq_idx.p;
+    int32_t* off = npts + (na + 1);
+    int32_t* pt_tet = off + (na + 1);
     const int64_t nodes = c->mesh.nv + c->mesh.ne;
     k_qq_grad<<<grid_for(c, nodes), kBlock, 0, c->stream>>>(c->mesh, c->ls_vert.p, c->ls_edge.p, c->dof_vert.p,
                                                             c->dof_edge.p, c->qq_grad.p);
@@ -577,6 +656,7 @@ int quaqua_elements(Context* c, double rhs_c, double tol, int maxiter, int* newt
     a.elem_rhs = c->elem_rhs.p;
     a.status = c->status.p;
     a.newton_max = c->status.p + 3;
+    a.base = c->qq_base.p + tet_words;
     const double s15 = std::sqrt(15.0);
     const double A1 = (6.0 - s15) / 21.0, B1 = (9.0 + 2.0 * s15) / 21.0;
     const double A2 = (6.0 + s15) / 21.0, B2 = (9.0 - 2.0 * s15) / 21.0;
@@ -595,11 +675,17 @@ int quaqua_elements(Context* c, double rhs_c, double tol, int maxiter, int* newt
     TF_CUDA(c, cudaMemsetAsync(c->status.p, 0, 4 * sizeof(int), c->stream));
     if (na > 0) {
         TimedLaunch tl(c, TF_K_ASSEMBLE);
-        const size_t sm = sizeof(QqSmem) * 2 * kQqWarps;
-        TF_CUDA(c, cudaFuncSetAttribute(k_qq_assemble, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        const int64_t pairs = (na + 1) / 2;
-        k_qq_assemble<<<grid_for(c, (pairs + kQqWarps - 1) / kQqWarps, 1, 8), 32 * kQqWarps, sm, c->stream>>>(a);
-        ++c->launches;
+        k_qq_tets<<<grid_for(c, na), kBlock, 0, c->stream>>>(a, tets, npts);
+        TF_CUDA(c, cudaGetLastError());
+        int64_t npt = 0;
+        TF_TRY(exclusive_scan_i32_to_i32(c, npts, off, na, &npt));  // off[na] = npt
+        if (npt > (int64_t)max_pts) return set_err(c, TF_ERR_INTERNAL, "quaqua: point count");
+        k_qq_point_tets<<<grid_for(c, na), kBlock, 0, c->stream>>>(na, npts, off, pt_tet);
+        const int gp = grid_for(c, npt, 128);
+        k_qq_points<0><<<gp, 128, 0, c->stream>>>(a, tets, off, pt_tet, npt, pdata);
+        k_qq_points<1><<<gp, 128, 0, c->stream>>>(a, tets, off, pt_tet, npt, pdata);
+        k_qq_sums<<<grid_for(c, na * 120), kBlock, 0, c->stream>>>(a, off, pdata);
+        c->launches += 6;  // with the scan's
         TF_CUDA(c, cudaGetLastError());
     }
     int h[4] = {0, 0, 0, 0};

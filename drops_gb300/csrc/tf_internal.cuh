@@ -393,7 +393,9 @@ struct Context {
     // learned Cahn-Hilliard warm start
     DBuf<double> ch_part, ch_scales, ch_hist;
     DBuf<double> ch_ring, ch_av;
-    DBuf<double> qq_grad;  // isoparametric P2: recovered level-set gradient per interface DOF  // learned warm start: recent states, differences, A V of the projection
+    DBuf<double> qq_grad;  // isoparametric P2: recovered level-set gradient per interface DOF
+    DBuf<double> qq_base;   // isoparametric P2: per cut tet its data, per quadrature point the base point and the point data
+    DBuf<int32_t> qq_idx;   // isoparametric P2: points per tet, their offsets, each point's tet
     DBuf<double> ch_prev, ch_x1, ch_x2;  // adaptive BDF1/BDF2: chi_prev, BDF1 and BDF2 states
     DBuf<float> ch_xyz, ch_nrm, ch_Y, ch_pred;
     DBuf<__nv_bfloat16> ch_X;
