@@ -126,9 +126,21 @@ __device__ void qq_vertex_grad(const double gl[4][3], const double f[10], int k,
 // block forms them once per type; the running mean's weights (n-1)/n and 1/n
 // come from a table of the same FP64 divisions.
 constexpr int kQqMaxTets = 48;  // tets around a node (24 on the Kuhn brick)
+// the node (vertex, or nv + edge) of every interface DOF
+__global__ void k_qq_dof_nodes(MeshView M, const int32_t* __restrict__ dof_vert, const int32_t* __restrict__ dof_edge,
+                               int64_t m, int32_t* __restrict__ nodes) {
+    const int64_t total = M.nv + M.ne;
+    for (int64_t node = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; node < total;
+         node += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t dof = node < M.nv ? dof_vert[node] : dof_edge[node - M.nv];
+        if (dof >= 0 && dof < m) nodes[dof] = (int32_t)node;
+    }
+}
+
+// one thread per interface DOF (the nodes without one do no work, so that
+// the FP64 work of the gradients runs in full warps)
 __global__ void k_qq_grad(MeshView M, const double* __restrict__ lsv, const double* __restrict__ lse,
-                          const int32_t* __restrict__ dof_vert, const int32_t* __restrict__ dof_edge,
-                          double* __restrict__ grad) {
+                          const int32_t* __restrict__ nodes, int64_t m, double* __restrict__ grad) {
     __shared__ double glT[6][4][3];
     __shared__ double rmA[kQqMaxTets + 1], rmB[kQqMaxTets + 1];
     const Brick& B = M.b;
@@ -146,13 +158,11 @@ __global__ void k_qq_grad(MeshView M, const double* __restrict__ lsv, const doub
         rmB[k] = 1. / n;
     }
     __syncthreads();
-    const int64_t nvert = M.nv, total = M.nv + M.ne;
-    for (int64_t node = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; node < total;
-         node += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t nvert = M.nv;
+    for (int64_t dof = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; dof < m; dof += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t node = nodes[dof];
         const bool isv = node < nvert;
         const int64_t id = isv ? node : node - nvert;
-        const int32_t dof = isv ? dof_vert[id] : dof_edge[id];
-        if (dof < 0) continue;
         // lower vertex (i3, i2, i1) of the node
         int64_t v = id;
         int d3 = 0, d2 = 0, d1 = 0;
@@ -580,40 +590,47 @@ __global__ void __launch_bounds__(128) k_qq_points(QqArgs a, const QqTet* __rest
     }
 }
 
-// the element entries of tet qa, summed over its points in point order: 55 M, 55 A, 10 b
-__global__ void k_qq_sums(QqArgs a, const int32_t* __restrict__ off, const double* __restrict__ pdata) {
-    const int64_t total = a.n_active * 120;
-    for (int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; id < total;
-         id += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t qa = id / 120;
-        const int e = (int)(id - qa * 120);
+// the element entries of tet qa, summed over its points in point order: 55 M, 55 A, 10 b; one warp per
+// tet, its points' records staged in shared memory
+constexpr int kQqSumWarps = 4;
+__global__ void __launch_bounds__(32 * kQqSumWarps) k_qq_sums(QqArgs a, const int32_t* __restrict__ off,
+                                                             const double* __restrict__ pdata) {
+    __shared__ double rec[kQqSumWarps][kQqPts * kQqPtData];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double* R = rec[w];
+    for (int64_t qa = blockIdx.x * (int64_t)kQqSumWarps + w; qa < a.n_active; qa += (int64_t)gridDim.x * kQqSumWarps) {
         const int64_t p0 = off[qa];
         const int npts = off[qa + 1] - off[qa];
-        double s = 0.;
-        if (e < 110) {
-            const int k = e < 55 ? e : e - 55;
-            int i = 0, rem = k;
-            while (rem >= 10 - i) {
-                rem -= 10 - i;
-                ++i;
+        for (int k = lane; k < npts * kQqPtData; k += 32) R[k] = pdata[(size_t)p0 * kQqPtData + k];
+        __syncwarp();
+        for (int e = lane; e < 120; e += 32) {
+            double s = 0.;
+            if (e < 110) {
+                const int k = e < 55 ? e : e - 55;
+                int i = 0, rem = k;
+                while (rem >= 10 - i) {
+                    rem -= 10 - i;
+                    ++i;
+                }
+                const int j = i + rem;
+                for (int p = 0; p < npts; ++p) {
+                    const double* P = R + p * kQqPtData;
+                    if (e < 55)
+                        s += P[0] * P[2 + i] * P[2 + j];
+                    else
+                        s += P[0] * dt3(P + 12 + 3 * i, P + 12 + 3 * j);
+                }
+                (e < 55 ? a.elem_m : a.elem_a)[qa * 55 + k] = s;
+            } else {
+                const int i = e - 110;
+                for (int p = 0; p < npts; ++p) {
+                    const double* P = R + p * kQqPtData;
+                    s += P[0] * P[1] * P[2 + i];
+                }
+                a.elem_rhs[qa * 10 + i] = s;
             }
-            const int j = i + rem;
-            for (int p = 0; p < npts; ++p) {
-                const double* P = pdata + (size_t)(p0 + p) * kQqPtData;
-                if (e < 55)
-                    s += P[0] * P[2 + i] * P[2 + j];
-                else
-                    s += P[0] * dt3(P + 12 + 3 * i, P + 12 + 3 * j);
-            }
-            (e < 55 ? a.elem_m : a.elem_a)[qa * 55 + k] = s;
-        } else {
-            const int i = e - 110;
-            for (int p = 0; p < npts; ++p) {
-                const double* P = pdata + (size_t)(p0 + p) * kQqPtData;
-                s += P[0] * P[1] * P[2 + i];
-            }
-            a.elem_rhs[qa * 10 + i] = s;
         }
+        __syncwarp();
     }
 }
 
@@ -628,20 +645,23 @@ int quaqua_elements(Context* c, double rhs_c, double tol, int maxiter, int* newt
     TF_TRY(ensure(c, c->qq_grad, (size_t)(3 * (m > 0 ? m : 1))));
     TF_TRY(ensure(c, c->elem, (size_t)TF_NUM_FORMS * (size_t)(na > 0 ? na : 1) * 55));
     TF_TRY(ensure(c, c->elem_rhs, (size_t)(na > 0 ? na : 1) * 10));
-    // per tet its data; per point (at most 14 per tet) the base point and the point data
+    // per tet its data; per point (at most 14 per tet) the base point and the point data; the index buffer
+    // first holds the DOFs' nodes, then the points per tet, their offsets and each point's tet
     const size_t tet_words = ((size_t)(na > 0 ? na : 1) * sizeof(QqTet) + 7) / 8;
     const size_t max_pts = (size_t)(na > 0 ? na : 1) * kQqPts;
     TF_TRY(ensure(c, c->qq_base, tet_words + max_pts * (8 + kQqPtData)));
-    TF_TRY(ensure(c, c->qq_idx, (size_t)(2 * (na + 1)) + max_pts));
+    TF_TRY(ensure(c, c->qq_idx, std::max((size_t)(2 * (na + 1)) + max_pts, (size_t)(m > 0 ? m : 1))));
     QqTet* tets = reinterpret_cast<QqTet*>(c->qq_base.p);
     double* pdata = c->qq_base.p + tet_words + max_pts * 8;
     int32_t* npts = c->qq_idx.p;
     int32_t* off = npts + (na + 1);
     int32_t* pt_tet = off + (na + 1);
-    const int64_t nodes = c->mesh.nv + c->mesh.ne;
-    k_qq_grad<<<grid_for(c, nodes), kBlock, 0, c->stream>>>(c->mesh, c->ls_vert.p, c->ls_edge.p, c->dof_vert.p,
-                                                            c->dof_edge.p, c->qq_grad.p);
-    ++c->launches;
+    const int64_t nnodes = c->mesh.nv + c->mesh.ne;
+    k_qq_dof_nodes<<<grid_for(c, nnodes), kBlock, 0, c->stream>>>(c->mesh, c->dof_vert.p, c->dof_edge.p, m,
+                                                                  c->qq_idx.p);
+    k_qq_grad<<<grid_for(c, m), kBlock, 0, c->stream>>>(c->mesh, c->ls_vert.p, c->ls_edge.p, c->qq_idx.p, m,
+                                                        c->qq_grad.p);
+    c->launches += 2;
     TF_CUDA(c, cudaGetLastError());
     QqArgs a{};
     a.M = c->mesh;
@@ -684,7 +704,8 @@ int quaqua_elements(Context* c, double rhs_c, double tol, int maxiter, int* newt
         const int gp = grid_for(c, npt, 128);
         k_qq_points<0><<<gp, 128, 0, c->stream>>>(a, tets, off, pt_tet, npt, pdata);
         k_qq_points<1><<<gp, 128, 0, c->stream>>>(a, tets, off, pt_tet, npt, pdata);
-        k_qq_sums<<<grid_for(c, na * 120), kBlock, 0, c->stream>>>(a, off, pdata);
+        k_qq_sums<<<grid_for(c, (na + kQqSumWarps - 1) / kQqSumWarps, 1, 8), 32 * kQqSumWarps, 0, c->stream>>>(
+            a, off, pdata);
         c->launches += 6;  // with the scan's
         TF_CUDA(c, cudaGetLastError());
     }
