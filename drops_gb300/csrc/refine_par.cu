@@ -239,7 +239,7 @@ __host__ __device__ inline int32_t vert_mid(const View& V, int32_t t, int p) {
 // ---- the engine --------------------------------------------------------------
 struct Engine {
     Exec X;
-    Buf<int32_t> tv, te, tlev, tpar, tch, ev, elev, emfr, emid, esub, vlev, cnt, tmp32, hval;
+    Buf<int32_t> tv, te, tlev, tpar, tch, ev, elev, emfr, emid, esub, vlev, cnt, tmp32, hval, sel_n;
     Buf<int64_t> tmp64;
     Buf<int8_t> tnch;
     Buf<uint8_t> trule, tmark, tchg, erm, ealive, esplit, vrm, valive, flag8;
@@ -264,12 +264,14 @@ struct Engine {
         X.nsm = nsm;
         setup(tv), setup(te), setup(tlev), setup(tpar), setup(tch), setup(ev), setup(elev), setup(emfr), setup(emid);
         setup(esub), setup(vlev), setup(cnt), setup(tmp32), setup(hval), setup(tmp64), setup(tnch), setup(trule);
+        setup(sel_n);
         setup(tmark), setup(tchg), setup(erm), setup(ealive), setup(esplit), setup(vrm), setup(valive);
         setup(flag8), setup(vx), setup(hkey), setup(rules), setup(cub_tmp);
     }
     ~Engine() {
         tv.release(), te.release(), tlev.release(), tpar.release(), tch.release(), ev.release(), elev.release();
         emfr.release(), emid.release(), esub.release(), vlev.release(), cnt.release(), tmp32.release();
+        sel_n.release();
         hval.release(), tmp64.release(), tnch.release(), trule.release(), tmark.release(), tchg.release();
         erm.release(), ealive.release(), esplit.release(), vrm.release(), valive.release(), flag8.release();
         vx.release(), hkey.release(), rules.release(), cub_tmp.release();
@@ -380,24 +382,20 @@ struct Engine {
     // stable selection of src[i] with flag8[i] != 0 into dst; returns the count
     int64_t select(const int32_t* src, int64_t n, int32_t* dst) {
         if (X.dev) {
-            Buf<int32_t> cntb;
-            setup(cntb);
-            if (!cntb.grow(1, 0)) {
+            if (!sel_n.grow(1, 0)) {
                 ok = false;
                 return 0;
             }
             size_t bytes = 0;
-            cub::DeviceSelect::Flagged(nullptr, bytes, src, flag8.p, dst, cntb.p, (int)n, X.s);
+            cub::DeviceSelect::Flagged(nullptr, bytes, src, flag8.p, dst, sel_n.p, (int)n, X.s);
             if (!cub_tmp.grow((int64_t)bytes + 1, 0)) {
                 ok = false;
-                cntb.release();
                 return 0;
             }
-            if (cub::DeviceSelect::Flagged(cub_tmp.p, bytes, src, flag8.p, dst, cntb.p, (int)n, X.s) != cudaSuccess)
+            if (cub::DeviceSelect::Flagged(cub_tmp.p, bytes, src, flag8.p, dst, sel_n.p, (int)n, X.s) != cudaSuccess)
                 ok = false;
             int32_t k = 0;
-            get(&k, cntb.p, sizeof k);
-            cntb.release();
+            get(&k, sel_n.p, sizeof k);
             return k;
         }
         int64_t k = 0;
