@@ -33,6 +33,9 @@
 // and transformation), so that every FP64 warp instruction has 32 active
 // lanes.  The element entries are summed per tet over its points in point
 // order.
+#include <cub/device/device_select.cuh>
+#include <thrust/iterator/counting_iterator.h>
+
 #include "tf_internal.cuh"
 
 namespace tf {
@@ -126,20 +129,22 @@ __device__ void qq_vertex_grad(const double gl[4][3], const double f[10], int k,
 // block forms them once per type; the running mean's weights (n-1)/n and 1/n
 // come from a table of the same FP64 divisions.
 constexpr int kQqMaxTets = 48;  // tets around a node (24 on the Kuhn brick)
-// the node (vertex, or nv + edge) of every interface DOF
-__global__ void k_qq_dof_nodes(MeshView M, const int32_t* __restrict__ dof_vert, const int32_t* __restrict__ dof_edge,
-                               int64_t m, int32_t* __restrict__ nodes) {
-    const int64_t total = M.nv + M.ne;
-    for (int64_t node = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; node < total;
-         node += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t dof = node < M.nv ? dof_vert[node] : dof_edge[node - M.nv];
-        if (dof >= 0 && dof < m) nodes[dof] = (int32_t)node;
+// the nodes (vertex, or nv + edge) that carry an interface DOF, in node order
+struct QqHasDof {
+    int64_t nv;
+    const int32_t* dof_vert;
+    const int32_t* dof_edge;
+    __device__ bool operator()(int32_t node) const {
+        return (node < nv ? dof_vert[node] : dof_edge[node - nv]) >= 0;
     }
-}
+};
 
-// one thread per interface DOF (the nodes without one do no work, so that
-// the FP64 work of the gradients runs in full warps)
+// one thread per interface DOF, the DOFs in node order: the nodes without one
+// do no work and a warp holds vertices or edges, whose gathers differ (up to
+// 48 candidate tets around a vertex, fewer around an edge), so that the FP64
+// work of the gradients runs in full warps
 __global__ void k_qq_grad(MeshView M, const double* __restrict__ lsv, const double* __restrict__ lse,
+                          const int32_t* __restrict__ dof_vert, const int32_t* __restrict__ dof_edge,
                           const int32_t* __restrict__ nodes, int64_t m, double* __restrict__ grad) {
     __shared__ double glT[6][4][3];
     __shared__ double rmA[kQqMaxTets + 1], rmB[kQqMaxTets + 1];
@@ -159,10 +164,11 @@ __global__ void k_qq_grad(MeshView M, const double* __restrict__ lsv, const doub
     }
     __syncthreads();
     const int64_t nvert = M.nv;
-    for (int64_t dof = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; dof < m; dof += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t node = nodes[dof];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t node = nodes[i];
         const bool isv = node < nvert;
         const int64_t id = isv ? node : node - nvert;
+        const int32_t dof = isv ? dof_vert[id] : dof_edge[id];
         // lower vertex (i3, i2, i1) of the node
         int64_t v = id;
         int d3 = 0, d2 = 0, d1 = 0;
@@ -650,18 +656,27 @@ int quaqua_elements(Context* c, double rhs_c, double tol, int maxiter, int* newt
     const size_t tet_words = ((size_t)(na > 0 ? na : 1) * sizeof(QqTet) + 7) / 8;
     const size_t max_pts = (size_t)(na > 0 ? na : 1) * kQqPts;
     TF_TRY(ensure(c, c->qq_base, tet_words + max_pts * (8 + kQqPtData)));
-    TF_TRY(ensure(c, c->qq_idx, std::max((size_t)(2 * (na + 1)) + max_pts, (size_t)(m > 0 ? m : 1))));
+    TF_TRY(ensure(c, c->qq_idx, std::max((size_t)(2 * (na + 1)) + max_pts, (size_t)(m > 0 ? m : 1) + 1)));
     QqTet* tets = reinterpret_cast<QqTet*>(c->qq_base.p);
     double* pdata = c->qq_base.p + tet_words + max_pts * 8;
     int32_t* npts = c->qq_idx.p;
     int32_t* off = npts + (na + 1);
     int32_t* pt_tet = off + (na + 1);
     const int64_t nnodes = c->mesh.nv + c->mesh.ne;
-    k_qq_dof_nodes<<<grid_for(c, nnodes), kBlock, 0, c->stream>>>(c->mesh, c->dof_vert.p, c->dof_edge.p, m,
-                                                                  c->qq_idx.p);
-    k_qq_grad<<<grid_for(c, m), kBlock, 0, c->stream>>>(c->mesh, c->ls_vert.p, c->ls_edge.p, c->qq_idx.p, m,
-                                                        c->qq_grad.p);
-    c->launches += 2;
+    if (nnodes > INT32_MAX) return set_err(c, TF_ERR_CAPACITY, "quaqua: 32-bit node ids");
+    {
+        const QqHasDof pred{c->mesh.nv, c->dof_vert.p, c->dof_edge.p};
+        thrust::counting_iterator<int32_t> first(0);
+        size_t bytes = 0;
+        TF_CUDA(c, cub::DeviceSelect::If(nullptr, bytes, first, c->qq_idx.p, c->qq_idx.p + m, (int)nnodes, pred,
+                                         c->stream));
+        TF_TRY(ensure(c, c->order_tmp, bytes > 0 ? bytes : 1));
+        TF_CUDA(c, cub::DeviceSelect::If(c->order_tmp.p, bytes, first, c->qq_idx.p, c->qq_idx.p + m, (int)nnodes, pred,
+                                         c->stream));
+    }
+    k_qq_grad<<<grid_for(c, m), kBlock, 0, c->stream>>>(c->mesh, c->ls_vert.p, c->ls_edge.p, c->dof_vert.p,
+                                                        c->dof_edge.p, c->qq_idx.p, m, c->qq_grad.p);
+    c->launches += 3;  // with the selection's
     TF_CUDA(c, cudaGetLastError());
     QqArgs a{};
     a.M = c->mesh;
