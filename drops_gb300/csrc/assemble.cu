@@ -521,6 +521,9 @@ struct AsmArgs {
     const double* windv;  // N_P1P1 wind, xyz per vertex / edge
     const double* winde;
     double* elem_n;       // [n_active][16]: N_P1P1, row i col j
+    // P1 pair forms: the per-tet records of active tets [c0, c1) (k_prep_p1)
+    void* prep;
+    int64_t c0, c1;
 };
 
 template <int NL>
@@ -1054,7 +1057,20 @@ int setup_fe_system(Context* c, unsigned forms, int rhs_kind, const double* rhs_
             TF_TRY(ensure_tables_ff(c));
             const size_t sm = sizeof(AsmPair1Smem) * kAsmWarps;
             TF_CUDA(c, cudaFuncSetAttribute(k_assemble_p1_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            k_assemble_p1_pair<<<blocks, 32 * kAsmWarps, sm, c->stream>>>(A);
+            // per chunk of active tets: the per-tet records (one thread per tet), then the forms (warp per tet)
+            const int64_t chunk = std::min<int64_t>(na, kPrep1Chunk);
+            TF_TRY(ensure(c, c->prep1, (size_t)chunk * sizeof(Prep1)));
+            A.prep = c->prep1.p;
+            for (int64_t c0 = 0; c0 < na; c0 += chunk) {
+                A.c0 = c0;
+                A.c1 = std::min<int64_t>(na, c0 + chunk);
+                const int64_t n = A.c1 - A.c0;
+                k_prep_p1<<<grid_for(c, n, 128), 128, 0, c->stream>>>(A);
+                k_assemble_p1_pair<<<grid_for(c, (n + kAsmWarps - 1) / kAsmWarps, 1, 8), 32 * kAsmWarps, sm,
+                                     c->stream>>>(A);
+                c->launches += 2;
+            }
+            --c->launches;  // counted per chunk above
         } else if (p2) {
             const size_t sm = sizeof(AsmSmem<10>) * kAsmWarps;
             TF_CUDA(c, cudaFuncSetAttribute(k_assemble<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));

@@ -205,6 +205,7 @@ int tf_destroy(tf_context* t) {
     tf::release(c->qq_grad);
     tf::release(c->qq_base);
     tf::release(c->qq_idx);
+    tf::release(c->prep1);
     tf::release(c->tune_buf);
     tf::release(c->ch_ring);
     tf::release(c->ch_av);
