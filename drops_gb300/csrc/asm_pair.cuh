@@ -103,6 +103,150 @@ __device__ __noinline__ ff ff_rhs(const RhsPar& R, const ff x[3]) {
     return ff_mul(ff_mul(ff_mul(ff_split(R.p[4]), y[0]), y[1]), y[2]);
 }
 
+// The pair forms' per-tet data, one thread per tet: the tet geometry
+// (GetTrafoTr and the level set's vertex gradients), the patch on the
+// order-2 lattice and (P1, LIN) the linear-level-set test and its constants,
+// with the arithmetic of warp_tet_geometry, warp_patch and the P1 kernel's
+// linear path done serially.  The FP64 work of a tet is then one thread's
+// instead of a warp's with 4 to 25 lanes active, so that every FP64 warp
+// instruction works for 32 tets (GB300 runs FP64 at 1/64 of the FP32 rate).
+struct TetPrep {
+    ff gl[4][3], G[4][3], X[4][3];
+    ff fb[16][3][4], fw[16];
+    double lin_sg[4][3], lin_G[10], lin_dn[4];
+    double absdet;
+    ff absdet_ff;
+    int nf, lin;
+};
+constexpr int64_t kPrepChunk = 1 << 18;  // tets per prep pass (about 0.6 GB of records)
+
+template <bool LIN>
+__global__ void __launch_bounds__(128) k_prep_tets(AsmArgs A) {
+    TetPrep* const out = reinterpret_cast<TetPrep*>(A.prep);
+    for (int64_t r = A.c0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < A.c1;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        TetPrep& Q = out[r - A.c0];
+        const int32_t t = A.active[r];
+        int32_t v[4], e[6];
+        mesh_tet(A.M, t, v, e);
+        TetGeom g;
+        double ls10[10];
+        for (int k = 0; k < 4; ++k) {
+            mesh_coord(A.M, v[k], g.X[k]);
+            ls10[k] = A.lsv[v[k]];
+        }
+        for (int k = 0; k < 6; ++k) ls10[4 + k] = A.lse[e[k]];
+        // warp_tet_geometry, lane by lane
+        double Ms[9], Cs[9];
+        for (int l = 0; l < 9; ++l) {
+            const int rr = l / 3, c = l % 3;
+            Ms[l] = g.X[c + 1][rr] - g.X[0][rr];
+        }
+        for (int l = 0; l < 9; ++l) {
+            const int rr = l / 3, c = l % 3;
+            const int r1 = (rr + 1) % 3, r2 = (rr + 2) % 3, c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+            Cs[l] = Ms[3 * r1 + c1] * Ms[3 * r2 + c2] - Ms[3 * r1 + c2] * Ms[3 * r2 + c1];
+        }
+        const double d = Ms[0] * Cs[0] + Ms[1] * Cs[1] + Ms[2] * Cs[2];
+        const double inv = 1.0 / d;
+        for (int vv = 0; vv < 4; ++vv)
+            for (int rr = 0; rr < 3; ++rr)
+                g.gl[vv][rr] = vv == 0 ? (-(Cs[3 * rr] * inv) - Cs[3 * rr + 1] * inv) - Cs[3 * rr + 2] * inv
+                                       : Cs[3 * rr + vv - 1] * inv;
+        g.absdet = fabs(d);
+        for (int vv = 0; vv < 4; ++vv)
+            for (int rr = 0; rr < 3; ++rr) {
+                double sum = 0.;
+                for (int i = 0; i < 4; ++i) sum += ls10[i] * ((i == vv ? 3. : -1.) * g.gl[i][rr]);
+                for (int k = 0; k < 6; ++k) {
+                    const int ea = ev0(k), eb = ev1(k);
+                    if (eb == vv) sum += ls10[4 + k] * (4. * g.gl[ea][rr]);
+                    if (ea == vv) sum += ls10[4 + k] * (4. * g.gl[eb][rr]);
+                }
+                g.G[vv][rr] = sum;
+            }
+        // warp_patch, lane by lane: cut points of the lattice edges, the sub-tets' facets in order
+        double lat[10];
+        for (int k = 0; k < 10; ++k) lat[cP2OnLat[k]] = ls10[k];
+        double cut[25][4];
+        for (int k = 0; k < 25; ++k) {
+            const int a = cT.edge_a[k], b = cT.edge_b[k];
+            const double va = lat[a], vb = lat[b];
+            if ((va > 0. && vb < 0.) || (va < 0. && vb > 0.)) cut_point(lat, a, b, cut[k]);
+        }
+        int nf = 0;
+        for (int sub = 0; sub < 8; ++sub) {
+            int pat = 0;
+            for (int k = 0; k < 4; ++k) {
+                const double val = lat[cT.lat_t[sub][k]];
+                pat += ((val > 0.) - (val < 0.) + 1) * (k == 0 ? 1 : k == 1 ? 3 : k == 2 ? 9 : 27);
+            }
+            int nfs = cT.pat_nf[pat];
+            if (nfs < 0) {
+                set_status(A.status, TF_ERR_ZERO_PATTERN, t);
+                nfs = 0;
+            }
+            for (int f = 0; f < nfs && nf < 16; ++f, ++nf) {
+                double w[3][3];
+                for (int j = 0; j < 3; ++j) {
+                    const int ext = cT.pat_f[pat][f][j];
+                    double b[4];
+                    if (ext < 4) {
+                        const int Lv = cT.lat_t[sub][ext];
+                        for (int c = 0; c < 4; ++c) b[c] = cT.lat_v[Lv][c];
+                    } else {
+                        const int id = cT.ledge[sub][ext - 4];
+                        for (int c = 0; c < 4; ++c) b[c] = cut[id][c];
+                    }
+                    for (int c = 0; c < 4; ++c) Q.fb[nf][j][c] = ff_split(b[c]);
+                    for (int rr = 0; rr < 3; ++rr)
+                        w[j][rr] = g.X[0][rr] * b[0] + g.X[1][rr] * b[1] + g.X[2][rr] * b[2] + g.X[3][rr] * b[3];
+                }
+                double u[3], vq[3];
+                for (int rr = 0; rr < 3; ++rr) {
+                    u[rr] = w[1][rr] - w[0][rr];
+                    vq[rr] = w[2][rr] - w[0][rr];
+                }
+                const double c0 = u[1] * vq[2] - u[2] * vq[1], c1 = u[2] * vq[0] - u[0] * vq[2],
+                             c2 = u[0] * vq[1] - u[1] * vq[0];
+                Q.fw[nf] = ff_split(sqrt(c0 * c0 + c1 * c1 + c2 * c2) * (cT.pat_bnd[pat] ? 0.5 : 1.0));
+            }
+        }
+        Q.nf = nf;
+        // linear level set on the tet: every edge value the mean of its end values, bit for bit
+        bool lin = LIN;
+        for (int k = 0; LIN && k < 6; ++k) {
+            const double mean = __dmul_rn(0.5, __dadd_rn(ls10[ev0(k)], ls10[ev1(k)]));
+            lin = lin && __double_as_longlong(mean) == __double_as_longlong(ls10[4 + k]);
+        }
+        Q.lin = lin;
+        if (lin) {
+            const double bc[4] = {0.25, 0.25, 0.25, 0.25};
+            double n[3];
+            unit_normal(g, bc, n);
+            for (int vv = 0; vv < 4; ++vv) {
+                const double ng = n[0] * g.gl[vv][0] + n[1] * g.gl[vv][1] + n[2] * g.gl[vv][2];
+                for (int c = 0; c < 3; ++c) Q.lin_sg[vv][c] = g.gl[vv][c] - ng * n[c];
+            }
+            for (int k = 0; k < 10; ++k) {
+                int i, j;
+                sym_entry(4, k, i, j);
+                Q.lin_G[k] = Q.lin_sg[j][0] * Q.lin_sg[i][0] + Q.lin_sg[j][1] * Q.lin_sg[i][1] +
+                             Q.lin_sg[j][2] * Q.lin_sg[i][2];
+            }
+            for (int i = 0; i < 4; ++i) Q.lin_dn[i] = n[0] * g.gl[i][0] + n[1] * g.gl[i][1] + n[2] * g.gl[i][2];
+        }
+        Q.absdet = g.absdet;
+        Q.absdet_ff = ff_split(g.absdet);
+        for (int vv = 0; vv < 4; ++vv)
+            for (int c = 0; c < 3; ++c) {
+                Q.gl[vv][c] = ff_split(g.gl[vv][c]);
+                Q.G[vv][c] = ff_split(g.G[vv][c]);
+                Q.X[vv][c] = ff_split(g.X[vv][c]);
+            }
+    }
+}
+
 __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble_p2_pair(AsmArgs A) {
     constexpr int NL = 10, NSYM = 55, EPL = 2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -113,42 +257,26 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble_p2_pair(AsmArgs A) 
     const bool wantF = A.rhs.kind != TF_RHS_NONE;
     const int64_t nwarps = (int64_t)gridDim.x * kAsmWarps;
 
-    for (int64_t r = (int64_t)blockIdx.x * kAsmWarps + wib; r < A.n_active; r += nwarps) {
-        const int32_t t = A.active[r];
-        int32_t v[4], e[6];
-        mesh_tet(A.M, t, v, e);
-        AsmPairFp64& D = S.u.d;
-        if (lane < 4) {
-            double x[3];
-            mesh_coord(A.M, v[lane], x);
-            for (int c = 0; c < 3; ++c) D.g.X[lane][c] = x[c];
-            D.ls10[lane] = A.lsv[v[lane]];
-        } else if (lane < 10) {
-            D.ls10[lane] = A.lse[e[lane - 4]];
-        }
-        __syncwarp();
-        warp_tet_geometry(D.g, D.ls10, D.gM, D.gC, lane);
-        double ls10[10];
-        for (int k = 0; k < 10; ++k) ls10[k] = D.ls10[k];
-        __syncwarp();
-        const int nf = warp_patch(ls10, D.g.X, D.P, lane, A.status, t);
-        // per-tet data as pairs: gl, G, X (36 values), |det|, the facets' vertices and weights
+    const TetPrep* const prep = reinterpret_cast<const TetPrep*>(A.prep);
+    for (int64_t r = A.c0 + (int64_t)blockIdx.x * kAsmWarps + wib; r < A.c1; r += nwarps) {
+        // the tet's record (k_prep_tets): gl, G, X, |det| and the facets as pairs
+        const TetPrep& Q = prep[r - A.c0];
+        const int nf = Q.nf;
         for (int k = lane; k < 37; k += 32) {
             const int m = k / 12, v3 = (k % 12) / 3, c = k % 3;
             if (k == 36)
-                S.absdet = ff_split(D.g.absdet);
+                S.absdet = Q.absdet_ff;
             else
-                (m == 0 ? S.gl : m == 1 ? S.G : S.X)[v3][c] =
-                    ff_split(m == 0 ? D.g.gl[v3][c] : m == 1 ? D.g.G[v3][c] : D.g.X[v3][c]);
+                (m == 0 ? S.gl : m == 1 ? S.G : S.X)[v3][c] = (m == 0 ? Q.gl : m == 1 ? Q.G : Q.X)[v3][c];
         }
         for (int k = lane; k < 13 * nf; k += 32) {
             const int f = k / 13, j = k % 13;
             if (j == 12)
-                S.fw[f] = ff_split(D.P.fw[f]);
+                S.fw[f] = Q.fw[f];
             else
-                S.fb[f][j >> 2][j & 3] = ff_split(D.P.fb[f][j >> 2][j & 3]);
+                S.fb[f][j >> 2][j & 3] = Q.fb[f][j >> 2][j & 3];
         }
-        __syncwarp();  // the FP64 scratch is dead from here: the point rows reuse it
+        __syncwarp();
         AsmPairPts& P = S.u.p;
 
         ffacc accM[EPL], accA[EPL], accF;
@@ -302,147 +430,6 @@ __device__ __noinline__ void ff_normal1(const ff (*G)[3], const ff b[4], ff n[3]
     for (int r = 0; r < 3; ++r) n[r] = ff_mul(v[r], inv);
 }
 
-// The P1 forms' per-tet data, one thread per tet: the tet geometry
-// (GetTrafoTr and the level set's vertex gradients), the patch on the
-// order-2 lattice, the linear-level-set test and its constants, with the
-// arithmetic of warp_tet_geometry, warp_patch and the warp kernel's linear
-// path done serially.  The FP64 work of a tet is then one thread's instead
-// of a warp's with 4 to 25 lanes active, so that every FP64 warp instruction
-// works for 32 tets (GB300 runs FP64 at 1/64 of the FP32 rate).
-struct Prep1 {
-    ff gl[4][3], G[4][3], X[4][3];
-    ff fb[16][3][4], fw[16];
-    double lin_sg[4][3], lin_G[10], lin_dn[4];
-    double absdet;
-    int nf, lin;
-};
-constexpr int64_t kPrep1Chunk = 1 << 18;  // tets per prep pass (about 0.6 GB of records)
-
-__global__ void __launch_bounds__(128) k_prep_p1(AsmArgs A) {
-    Prep1* const out = reinterpret_cast<Prep1*>(A.prep);
-    for (int64_t r = A.c0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < A.c1;
-         r += (int64_t)gridDim.x * blockDim.x) {
-        Prep1& Q = out[r - A.c0];
-        const int32_t t = A.active[r];
-        int32_t v[4], e[6];
-        mesh_tet(A.M, t, v, e);
-        TetGeom g;
-        double ls10[10];
-        for (int k = 0; k < 4; ++k) {
-            mesh_coord(A.M, v[k], g.X[k]);
-            ls10[k] = A.lsv[v[k]];
-        }
-        for (int k = 0; k < 6; ++k) ls10[4 + k] = A.lse[e[k]];
-        // warp_tet_geometry, lane by lane
-        double Ms[9], Cs[9];
-        for (int l = 0; l < 9; ++l) {
-            const int rr = l / 3, c = l % 3;
-            Ms[l] = g.X[c + 1][rr] - g.X[0][rr];
-        }
-        for (int l = 0; l < 9; ++l) {
-            const int rr = l / 3, c = l % 3;
-            const int r1 = (rr + 1) % 3, r2 = (rr + 2) % 3, c1 = (c + 1) % 3, c2 = (c + 2) % 3;
-            Cs[l] = Ms[3 * r1 + c1] * Ms[3 * r2 + c2] - Ms[3 * r1 + c2] * Ms[3 * r2 + c1];
-        }
-        const double d = Ms[0] * Cs[0] + Ms[1] * Cs[1] + Ms[2] * Cs[2];
-        const double inv = 1.0 / d;
-        for (int vv = 0; vv < 4; ++vv)
-            for (int rr = 0; rr < 3; ++rr)
-                g.gl[vv][rr] = vv == 0 ? (-(Cs[3 * rr] * inv) - Cs[3 * rr + 1] * inv) - Cs[3 * rr + 2] * inv
-                                       : Cs[3 * rr + vv - 1] * inv;
-        g.absdet = fabs(d);
-        for (int vv = 0; vv < 4; ++vv)
-            for (int rr = 0; rr < 3; ++rr) {
-                double sum = 0.;
-                for (int i = 0; i < 4; ++i) sum += ls10[i] * ((i == vv ? 3. : -1.) * g.gl[i][rr]);
-                for (int k = 0; k < 6; ++k) {
-                    const int ea = ev0(k), eb = ev1(k);
-                    if (eb == vv) sum += ls10[4 + k] * (4. * g.gl[ea][rr]);
-                    if (ea == vv) sum += ls10[4 + k] * (4. * g.gl[eb][rr]);
-                }
-                g.G[vv][rr] = sum;
-            }
-        // warp_patch, lane by lane: cut points of the lattice edges, the sub-tets' facets in order
-        double lat[10];
-        for (int k = 0; k < 10; ++k) lat[cP2OnLat[k]] = ls10[k];
-        double cut[25][4];
-        for (int k = 0; k < 25; ++k) {
-            const int a = cT.edge_a[k], b = cT.edge_b[k];
-            const double va = lat[a], vb = lat[b];
-            if ((va > 0. && vb < 0.) || (va < 0. && vb > 0.)) cut_point(lat, a, b, cut[k]);
-        }
-        int nf = 0;
-        for (int sub = 0; sub < 8; ++sub) {
-            int pat = 0;
-            for (int k = 0; k < 4; ++k) {
-                const double val = lat[cT.lat_t[sub][k]];
-                pat += ((val > 0.) - (val < 0.) + 1) * (k == 0 ? 1 : k == 1 ? 3 : k == 2 ? 9 : 27);
-            }
-            int nfs = cT.pat_nf[pat];
-            if (nfs < 0) {
-                set_status(A.status, TF_ERR_ZERO_PATTERN, t);
-                nfs = 0;
-            }
-            for (int f = 0; f < nfs && nf < 16; ++f, ++nf) {
-                double w[3][3];
-                for (int j = 0; j < 3; ++j) {
-                    const int ext = cT.pat_f[pat][f][j];
-                    double b[4];
-                    if (ext < 4) {
-                        const int Lv = cT.lat_t[sub][ext];
-                        for (int c = 0; c < 4; ++c) b[c] = cT.lat_v[Lv][c];
-                    } else {
-                        const int id = cT.ledge[sub][ext - 4];
-                        for (int c = 0; c < 4; ++c) b[c] = cut[id][c];
-                    }
-                    for (int c = 0; c < 4; ++c) Q.fb[nf][j][c] = ff_split(b[c]);
-                    for (int rr = 0; rr < 3; ++rr)
-                        w[j][rr] = g.X[0][rr] * b[0] + g.X[1][rr] * b[1] + g.X[2][rr] * b[2] + g.X[3][rr] * b[3];
-                }
-                double u[3], vq[3];
-                for (int rr = 0; rr < 3; ++rr) {
-                    u[rr] = w[1][rr] - w[0][rr];
-                    vq[rr] = w[2][rr] - w[0][rr];
-                }
-                const double c0 = u[1] * vq[2] - u[2] * vq[1], c1 = u[2] * vq[0] - u[0] * vq[2],
-                             c2 = u[0] * vq[1] - u[1] * vq[0];
-                Q.fw[nf] = ff_split(sqrt(c0 * c0 + c1 * c1 + c2 * c2) * (cT.pat_bnd[pat] ? 0.5 : 1.0));
-            }
-        }
-        Q.nf = nf;
-        // linear level set on the tet: every edge value the mean of its end values, bit for bit
-        bool lin = true;
-        for (int k = 0; k < 6; ++k) {
-            const double mean = __dmul_rn(0.5, __dadd_rn(ls10[ev0(k)], ls10[ev1(k)]));
-            lin = lin && __double_as_longlong(mean) == __double_as_longlong(ls10[4 + k]);
-        }
-        Q.lin = lin;
-        if (lin) {
-            const double bc[4] = {0.25, 0.25, 0.25, 0.25};
-            double n[3];
-            unit_normal(g, bc, n);
-            for (int vv = 0; vv < 4; ++vv) {
-                const double ng = n[0] * g.gl[vv][0] + n[1] * g.gl[vv][1] + n[2] * g.gl[vv][2];
-                for (int c = 0; c < 3; ++c) Q.lin_sg[vv][c] = g.gl[vv][c] - ng * n[c];
-            }
-            for (int k = 0; k < 10; ++k) {
-                int i, j;
-                sym_entry(4, k, i, j);
-                Q.lin_G[k] = Q.lin_sg[j][0] * Q.lin_sg[i][0] + Q.lin_sg[j][1] * Q.lin_sg[i][1] +
-                             Q.lin_sg[j][2] * Q.lin_sg[i][2];
-            }
-            for (int i = 0; i < 4; ++i) Q.lin_dn[i] = n[0] * g.gl[i][0] + n[1] * g.gl[i][1] + n[2] * g.gl[i][2];
-        }
-        Q.absdet = g.absdet;
-        for (int vv = 0; vv < 4; ++vv)
-            for (int c = 0; c < 3; ++c) {
-                Q.gl[vv][c] = ff_split(g.gl[vv][c]);
-                Q.G[vv][c] = ff_split(g.G[vv][c]);
-                Q.X[vv][c] = ff_split(g.X[vv][c]);
-            }
-    }
-}
-
 __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble_p1_pair(AsmArgs A) {
     constexpr int NL = 4, NSYM = 10;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -455,10 +442,10 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble_p1_pair(AsmArgs A) 
     double s3 = 0.;  // the 15-point rule's weight sum (linear level set: n . grad(phi_i) is constant)
     for (int pp = 0; pp < 15; ++pp) s3 += cT.q3_w[pp];
 
-    const Prep1* const prep = reinterpret_cast<const Prep1*>(A.prep);
+    const TetPrep* const prep = reinterpret_cast<const TetPrep*>(A.prep);
     for (int64_t r = A.c0 + (int64_t)blockIdx.x * kAsmWarps + wib; r < A.c1; r += nwarps) {
-        // the tet's record (k_prep_p1) into shared memory
-        const Prep1& Q = prep[r - A.c0];
+        // the tet's record (k_prep_tets) into shared memory
+        const TetPrep& Q = prep[r - A.c0];
         const int nf = Q.nf;
         const bool lin = Q.lin != 0;
         const double absdet = Q.absdet;

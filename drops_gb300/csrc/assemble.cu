@@ -521,7 +521,7 @@ struct AsmArgs {
     const double* windv;  // N_P1P1 wind, xyz per vertex / edge
     const double* winde;
     double* elem_n;       // [n_active][16]: N_P1P1, row i col j
-    // P1 pair forms: the per-tet records of active tets [c0, c1) (k_prep_p1)
+    // pair forms: the per-tet records of active tets [c0, c1) (k_prep_tets)
     void* prep;
     int64_t c0, c1;
 };
@@ -1051,21 +1051,34 @@ int setup_fe_system(Context* c, unsigned forms, int rhs_kind, const double* rhs_
             TF_TRY(ensure_tables_ff(c));
             const size_t sm = sizeof(AsmPairSmem) * kAsmWarps;
             TF_CUDA(c, cudaFuncSetAttribute(k_assemble_p2_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            k_assemble_p2_pair<<<blocks, 32 * kAsmWarps, sm, c->stream>>>(A);
+            // per chunk of active tets: the per-tet records (one thread per tet), then the forms (warp per tet)
+            const int64_t chunk = std::min<int64_t>(na, kPrepChunk);
+            TF_TRY(ensure(c, c->prep1, (size_t)chunk * sizeof(TetPrep)));
+            A.prep = c->prep1.p;
+            for (int64_t c0 = 0; c0 < na; c0 += chunk) {
+                A.c0 = c0;
+                A.c1 = std::min<int64_t>(na, c0 + chunk);
+                const int64_t n = A.c1 - A.c0;
+                k_prep_tets<false><<<grid_for(c, n, 128), 128, 0, c->stream>>>(A);
+                k_assemble_p2_pair<<<grid_for(c, (n + kAsmWarps - 1) / kAsmWarps, 1, 8), 32 * kAsmWarps, sm,
+                                     c->stream>>>(A);
+                c->launches += 2;
+            }
+            --c->launches;  // counted per chunk above
         } else if (!p2 && !c->asm_fp64 && !(forms & ~((1u << TF_FORM_M) | (1u << TF_FORM_A) | (1u << TF_FORM_CN))) &&
                    (rhs_kind == TF_RHS_NONE || rhs_kind == TF_RHS_CONST || rhs_kind == TF_RHS_SPHERE_XYZ)) {
             TF_TRY(ensure_tables_ff(c));
             const size_t sm = sizeof(AsmPair1Smem) * kAsmWarps;
             TF_CUDA(c, cudaFuncSetAttribute(k_assemble_p1_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
             // per chunk of active tets: the per-tet records (one thread per tet), then the forms (warp per tet)
-            const int64_t chunk = std::min<int64_t>(na, kPrep1Chunk);
-            TF_TRY(ensure(c, c->prep1, (size_t)chunk * sizeof(Prep1)));
+            const int64_t chunk = std::min<int64_t>(na, kPrepChunk);
+            TF_TRY(ensure(c, c->prep1, (size_t)chunk * sizeof(TetPrep)));
             A.prep = c->prep1.p;
             for (int64_t c0 = 0; c0 < na; c0 += chunk) {
                 A.c0 = c0;
                 A.c1 = std::min<int64_t>(na, c0 + chunk);
                 const int64_t n = A.c1 - A.c0;
-                k_prep_p1<<<grid_for(c, n, 128), 128, 0, c->stream>>>(A);
+                k_prep_tets<true><<<grid_for(c, n, 128), 128, 0, c->stream>>>(A);
                 k_assemble_p1_pair<<<grid_for(c, (n + kAsmWarps - 1) / kAsmWarps, 1, 8), 32 * kAsmWarps, sm,
                                      c->stream>>>(A);
                 c->launches += 2;
