@@ -159,6 +159,7 @@ int tf_destroy(tf_context* t) {
     Context* c = &t->c;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    if (c->refine_pool) cudaMemPoolDestroy(c->refine_pool);
     tf::release(c->coords);
     tf::release(c->tet_v);
     tf::release(c->tet_e);

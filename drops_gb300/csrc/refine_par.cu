@@ -107,6 +107,7 @@ __global__ void k_for(int64_t n, F f) {
 struct Exec {
     bool dev = false;
     cudaStream_t s = nullptr;
+    cudaMemPool_t pool = nullptr;  // stream-ordered device allocations, when set
     int nsm = 1;
     int err = 0;  // host-side CUDA error
     template <class F>
@@ -123,11 +124,15 @@ struct Exec {
     }
 };
 
+// Device buffers come from the executor's memory pool when it has one: the
+// allocation and the free are ordered on the stream (no synchronisation), and
+// the pool keeps freed memory for the next allocation and the next call.
 template <class T>
 struct Buf {
     T* p = nullptr;
     int64_t cap = 0;
     bool dev = false;
+    bool pooled = false;  // p came from X->pool
     Exec* X = nullptr;
     // grows to at least n elements, keeping the first keep
     bool grow(int64_t n, int64_t keep) {
@@ -135,13 +140,21 @@ struct Buf {
         int64_t nc = std::max<int64_t>(n, cap + cap / 2 + 1024);
         T* q = nullptr;
         if (dev) {
-            if (cudaMalloc((void**)&q, sizeof(T) * nc) != cudaSuccess) return false;
-            if (keep > 0 && cudaMemcpyAsync(q, p, sizeof(T) * keep, cudaMemcpyDeviceToDevice, X->s) != cudaSuccess)
+            const bool from_pool = X->pool != nullptr;
+            if (from_pool) {
+                if (cudaMallocFromPoolAsync((void**)&q, sizeof(T) * nc, X->pool, X->s) != cudaSuccess) return false;
+            } else if (cudaMalloc((void**)&q, sizeof(T) * nc) != cudaSuccess) {
                 return false;
-            if (p) {
-                cudaStreamSynchronize(X->s);
-                cudaFree(p);
             }
+            if (keep > 0 && cudaMemcpyAsync(q, p, sizeof(T) * keep, cudaMemcpyDeviceToDevice, X->s) != cudaSuccess) {
+                if (from_pool)
+                    cudaFreeAsync(q, X->s);
+                else
+                    cudaFree(q);
+                return false;
+            }
+            free_dev();
+            pooled = from_pool;
         } else {
             q = (T*)std::malloc(sizeof(T) * nc);
             if (!q) return false;
@@ -152,15 +165,25 @@ struct Buf {
         cap = nc;
         return true;
     }
+    void free_dev() {
+        if (!p) return;
+        if (pooled) {
+            cudaFreeAsync(p, X->s);
+        } else {
+            cudaStreamSynchronize(X->s);
+            cudaFree(p);
+        }
+    }
     void release() {
         if (p) {
             if (dev)
-                cudaFree(p);
+                free_dev();
             else
                 std::free(p);
         }
         p = nullptr;
         cap = 0;
+        pooled = false;
     }
     void fill(int64_t n, T v) {
         T* q = p;
@@ -258,9 +281,10 @@ struct Engine {
         b.dev = X.dev;
         b.X = &X;
     }
-    Engine(bool dev, cudaStream_t s, int nsm) {
+    Engine(bool dev, cudaStream_t s, int nsm, cudaMemPool_t pool = nullptr) {
         X.dev = dev;
         X.s = s;
+        X.pool = dev ? pool : nullptr;
         X.nsm = nsm;
         setup(tv), setup(te), setup(tlev), setup(tpar), setup(tch), setup(ev), setup(elev), setup(emfr), setup(emid);
         setup(esub), setup(vlev), setup(cnt), setup(tmp32), setup(hval), setup(tmp64), setup(tnch), setup(trule);
@@ -1104,7 +1128,25 @@ int refine_band_device(Context* c, int kind, const double* par, int npar, double
         st = set_err(c, TF_ERR_CUDA, "refine: coordinates");
     if (st == TF_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) st = set_err(c, TF_ERR_CUDA, "refine: sync");
     int steps = 0;
-    Engine G(true, c->stream, c->num_sms);
+    // the context's pool for the engine's buffers: kept between calls, so a
+    // repeated refinement allocates nothing new (tf_destroy releases it)
+    if (!c->refine_pool) {
+        int pools = 0;
+        if (cudaDeviceGetAttribute(&pools, cudaDevAttrMemoryPoolsSupported, c->device) == cudaSuccess && pools) {
+            cudaMemPoolProps pp{};
+            pp.allocType = cudaMemAllocationTypePinned;
+            pp.location.type = cudaMemLocationTypeDevice;
+            pp.location.id = c->device;
+            if (cudaMemPoolCreate(&c->refine_pool, &pp) == cudaSuccess) {
+                uint64_t keep = UINT64_MAX;
+                cudaMemPoolSetAttribute(c->refine_pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            } else {
+                c->refine_pool = nullptr;
+                cudaGetLastError();
+            }
+        }
+    }
+    Engine G(true, c->stream, c->num_sms, c->refine_pool);
     if (st == TF_OK) {
         std::vector<int32_t> htv((size_t)(4 * nt0)), hte((size_t)(6 * nt0));
         cudaMemcpyAsync(htv.data(), dv.p, sizeof(int32_t) * 4 * nt0, cudaMemcpyDeviceToHost, c->stream);

@@ -350,6 +350,7 @@ struct Context {
     cudaEvent_t tune_ev[2] = {};
     int pcg_fp64_kernel = 0;    // TF_PCG_FP64_CLASSIC or TF_PCG_FP64_CG1
     int pcg_res_vcap_kb = -1;   // resident PCG: cap on the KB of matrix values kept in shared memory (-1: none)
+    cudaMemPool_t refine_pool = nullptr;  // device memory of the refinement engine, kept between calls
     double pcg_rel_update = 0.2;  // mixed resident PCG: FP64 refinement when the FP32 residual dropped by this
     double batch_rel_update = 0.2;  // mixed batched PCG: the same factor
     DBuf<float2> x_pairs;       // SpMV operand split into FP32 pairs
