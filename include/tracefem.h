@@ -127,7 +127,9 @@ int tf_mesh_download(tf_context* ctx, double* coords, int32_t* tet_v, int32_t* t
  * and edges are numbered by first touch.  The level set and everything after
  * it must be set up again.  last_level, steps: may be NULL.
  * TF_ERR_BAD_INPUT also when the mesh's tets do not list their vertices in
- * one global order (BrickBuilderCL's do; the refinement relies on it).       */
+ * one global order (BrickBuilderCL's do; the refinement relies on it).
+ * The refinement's working memory comes from a device memory pool of the
+ * context, kept for the next call and returned by tf_destroy.               */
 int tf_mesh_refine_band(tf_context* ctx, int kind, const double* par, int npar, double width, int coarse_level,
                         int fine_level, int* last_level, int* steps);
 /* The same refinement on host arrays, without a context or a device (the
