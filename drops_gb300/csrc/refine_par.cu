@@ -88,6 +88,13 @@ __host__ __device__ inline uint64_t atom_cas(uint64_t* p, uint64_t cmp, uint64_t
     return o;
 #endif
 }
+__host__ __device__ inline void atom_min(int64_t* p, int64_t v) {
+#ifdef __CUDA_ARCH__
+    atomicMin((long long*)p, (long long)v);
+#else
+    if (v < *p) *p = v;
+#endif
+}
 __host__ __device__ inline uint32_t hmix(uint64_t k) {
     k ^= k >> 33;
     k *= 0xff51afd7ed558ccdull;
@@ -1109,7 +1116,8 @@ int refine_band_parallel_host(int64_t nv, const double* coords, int64_t nt, cons
 
 // The device path: the context's (brick or uploaded) mesh refined on the
 // device and installed as an uploaded mesh; vertices and edges numbered by
-// scans over the triangulation's first touches in tet order.
+// first touch in the triangulation's order, as the sequential form numbers
+// them.
 int refine_band_device(Context* c, int kind, const double* par, int npar, double width, int clevel, int flevel,
                        int* last_level, int* steps_out) {
     using namespace rpar;
@@ -1162,7 +1170,7 @@ int refine_band_device(Context* c, int kind, const double* par, int npar, double
     release(dv);
     release(de);
     if (st != TF_OK) return st;
-    // the triangulation, first touches renumbered by scans
+    // the last triangulation level, in list order
     Buf<int32_t> tri;
     tri.dev = true;
     tri.X = &G.X;
@@ -1171,36 +1179,60 @@ int refine_band_device(Context* c, int kind, const double* par, int npar, double
         tri.release();
         return set_err(c, TF_ERR_CUDA, "refine: triangulation");
     }
-    Buf<int32_t> vnew, enew;
-    vnew.dev = enew.dev = true;
-    vnew.X = enew.X = &G.X;
-    bool okb = vnew.grow(G.nv + 1, 0) && enew.grow(G.ne + 1, 0);
-    if (!okb) {
+    // Vertices and edges numbered by first touch in the triangulation's order
+    // (tet by tet, local vertex / edge order, as the sequential form): the key
+    // of a vertex is the smallest slot 4 i + k of the triangulation holding it
+    // (6 i + j for an edge), its id the rank of that key, by a scan over the
+    // slots.  The engine's own ids come from atomic counters and are not used.
+    constexpr int64_t kNone = INT64_MAX;
+    if (6 * ntri >= (int64_t)INT32_MAX) {
         tri.release();
+        return set_err(c, TF_ERR_CAPACITY, "refine: mesh too large for 32-bit ids");
+    }
+    Buf<int64_t> vkey, ekey, voff;
+    Buf<int32_t> vslot, eslot;
+    vkey.dev = ekey.dev = voff.dev = vslot.dev = eslot.dev = true;
+    vkey.X = ekey.X = voff.X = vslot.X = eslot.X = &G.X;
+    auto release_all = [&]() {
+        tri.release(), vkey.release(), ekey.release(), voff.release(), vslot.release(), eslot.release();
+    };
+    bool okb = vkey.grow(G.nv, 0) && ekey.grow(G.ne, 0) && vslot.grow(4 * ntri + 1, 0) &&
+               eslot.grow(6 * ntri + 1, 0) && voff.grow(4 * ntri + 1, 0);
+    if (!okb) {
+        release_all();
         return set_err(c, TF_ERR_CUDA, "refine: alloc");
     }
-    vnew.fill(G.nv + 1, 0);
-    enew.fill(G.ne + 1, 0);
+    vkey.fill(G.nv, kNone);
+    ekey.fill(G.ne, kNone);
+    vslot.fill(4 * ntri, 0);
+    eslot.fill(6 * ntri, 0);
     {
         View V = G.view();
         const int32_t* tp = tri.p;
-        int32_t* vu = vnew.p;
-        int32_t* eu = enew.p;
+        int64_t* vk = vkey.p;
+        int64_t* ek = ekey.p;
+        int32_t* vs = vslot.p;
+        int32_t* es = eslot.p;
+        const int64_t nv = G.nv, ne = G.ne;
         G.X.par_for(ntri, [=] __host__ __device__(int64_t i) {
             const int32_t t = tp[i];
-            for (int k = 0; k < 4; ++k) vu[V.tv[4 * (int64_t)t + k]] = 1;
-            for (int j = 0; j < 6; ++j) eu[V.te[6 * (int64_t)t + j]] = 1;
+            for (int k = 0; k < 4; ++k) atom_min(&vk[V.tv[4 * (int64_t)t + k]], 4 * i + k);
+            for (int j = 0; j < 6; ++j) atom_min(&ek[V.te[6 * (int64_t)t + j]], 6 * i + j);
+        });
+        G.X.par_for(nv, [=] __host__ __device__(int64_t v) {
+            if (vk[v] != kNone) vs[vk[v]] = 1;
+        });
+        G.X.par_for(ne, [=] __host__ __device__(int64_t e) {
+            if (ek[e] != kNone) es[ek[e]] = 1;
         });
     }
-    const int64_t nvo = G.scan(vnew.p, G.nv);
-    Buf<int64_t> voff;
-    voff.dev = true;
-    voff.X = &G.X;
-    if (!voff.grow(G.nv + 1, 0)) okb = false;
-    if (okb) cudaMemcpyAsync(voff.p, G.tmp64.p, sizeof(int64_t) * (G.nv + 1), cudaMemcpyDeviceToDevice, c->stream);
-    const int64_t neo = G.scan(enew.p, G.ne);
+    const int64_t nvo = G.scan(vslot.p, 4 * ntri);
+    if (G.ok && cudaMemcpyAsync(voff.p, G.tmp64.p, sizeof(int64_t) * (4 * ntri + 1), cudaMemcpyDeviceToDevice,
+                                c->stream) != cudaSuccess)
+        okb = false;
+    const int64_t neo = G.scan(eslot.p, 6 * ntri);
     if (!okb || !G.ok || nvo > INT32_MAX || neo > INT32_MAX) {
-        tri.release(), vnew.release(), enew.release(), voff.release();
+        release_all();
         return set_err(c, TF_ERR_CAPACITY, "refine: mesh too large for 32-bit ids");
     }
     TF_TRY(ensure(c, c->coords, (size_t)(3 * nvo)));
@@ -1211,28 +1243,32 @@ int refine_band_device(Context* c, int kind, const double* par, int npar, double
         View V = G.view();
         const int64_t* vo = voff.p;
         const int64_t* eo = G.tmp64.p;
-        const int32_t* vu = vnew.p;
-        const int32_t* eu = enew.p;
+        const int64_t* vk = vkey.p;
+        const int64_t* ek = ekey.p;
         double* oc = c->coords.p;
         int32_t *otv = c->tet_v.p, *ote = c->tet_e.p, *oev = c->edge_v.p;
         const int32_t* tp = tri.p;
         G.X.par_for(G.nv, [=] __host__ __device__(int64_t v) {
-            if (!vu[v]) return;
-            for (int k = 0; k < 3; ++k) oc[3 * vo[v] + k] = V.vx[3 * v + k];
+            if (vk[v] == kNone) return;
+            const int64_t id = vo[vk[v]];
+            for (int k = 0; k < 3; ++k) oc[3 * id + k] = V.vx[3 * v + k];
         });
         G.X.par_for(G.ne, [=] __host__ __device__(int64_t e) {
-            if (!eu[e]) return;
-            oev[2 * eo[e]] = (int32_t)vo[V.ev[2 * e]];
-            oev[2 * eo[e] + 1] = (int32_t)vo[V.ev[2 * e + 1]];
+            if (ek[e] == kNone) return;
+            const int64_t id = eo[ek[e]];
+            // the ends of a triangulation edge are triangulation vertices
+            const int64_t ka = vk[V.ev[2 * e]], kb = vk[V.ev[2 * e + 1]];
+            oev[2 * id] = ka != kNone ? (int32_t)vo[ka] : -1;
+            oev[2 * id + 1] = kb != kNone ? (int32_t)vo[kb] : -1;
         });
         G.X.par_for(ntri, [=] __host__ __device__(int64_t i) {
             const int32_t t = tp[i];
-            for (int k = 0; k < 4; ++k) otv[4 * i + k] = (int32_t)vo[V.tv[4 * (int64_t)t + k]];
-            for (int j = 0; j < 6; ++j) ote[6 * i + j] = (int32_t)eo[V.te[6 * (int64_t)t + j]];
+            for (int k = 0; k < 4; ++k) otv[4 * i + k] = (int32_t)vo[vk[V.tv[4 * (int64_t)t + k]]];
+            for (int j = 0; j < 6; ++j) ote[6 * i + j] = (int32_t)eo[ek[V.te[6 * (int64_t)t + j]]];
         });
     }
     const cudaError_t ce = cudaStreamSynchronize(c->stream);
-    tri.release(), vnew.release(), enew.release(), voff.release();
+    release_all();
     if (ce != cudaSuccess || G.X.err) return set_err(c, TF_ERR_CUDA, "refine: output");
     MeshView& M = c->mesh;
     M = MeshView{};

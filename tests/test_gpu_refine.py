@@ -113,7 +113,8 @@ def test_device_refinement_matches_reference(ctx, golden, shape, n, a, width, cl
 ])
 def test_device_refinement_equals_sequential_form(ctx, case):
     """The device engine against the sequential form (pinned to the reference above) on other inputs: an
-    uploaded mesh, a plane, uniform refinement (coarse = fine level), a thin band at three levels."""
+    uploaded mesh, a plane, uniform refinement (coarse = fine level), a thin band at three levels.  Both number
+    vertices and edges by first touch in the triangulation's order, so all four arrays agree exactly."""
     from oracle import pyoracle as O
 
     how, kind, par, width, cl, fl = case
@@ -128,6 +129,8 @@ def test_device_refinement_equals_sequential_form(ctx, case):
     r = tf.refine_band(om.coords, om.tet_v, kind, par, width, cl, fl)
     assert last == r["last_level"] and steps == r["steps"]
     assert np.array_equal(coords[tv], r["coords"][r["tet_v"]])
+    for got, key in ((coords, "coords"), (tv, "tet_v"), (te, "tet_e"), (ev, "edge_v")):
+        assert np.array_equal(got, r[key]), key
 
 
 def test_refine_rejects_bad_input_on_device(ctx):
@@ -138,6 +141,29 @@ def test_refine_rejects_bad_input_on_device(ctx):
         ctx.mesh_refine_band(tf.LS_ELLIPSOID, [0.0] * 15, 0.1, 0, 1)
     # the context keeps its mesh after a refused call
     assert ctx.mesh_info()[2] == 6 * 27
+
+
+def test_repeated_refinement_from_the_pool(ctx, golden):
+    """The refinement's buffers come from a memory pool of the context that keeps freed memory, uncleared, for
+    the next call: after a torus band has left its data in the pool, the sphere refinement twice gives the
+    reference's mesh both times, with the same vertex and edge numbering."""
+    g = golden("refine_meshes.npz")
+    i = int(np.argmax(g["n"] * (g["shape"] == "sphere")))
+    n, a, width, cl, fl = int(g["n"][i]), float(g["a"][i]), float(g["width"][i]), int(g["clevel"][i]), int(g["flevel"][i])
+    c = tf.TraceFEM()
+    try:
+        c.brick_cube(6, 1.55)
+        c.mesh_refine_band(tf.LS_TORUS, [1.0, 0.4, 2], 0.02, 0, 3)
+        out = []
+        for _ in range(2):
+            c.brick_cube(n, a)
+            assert c.mesh_refine_band(tf.LS_SPHERE, [0.0, 0.0, 0.0, 1.0], width, cl, fl)[0] == fl
+            out.append(c.mesh_download())
+        assert sha(out[0][0][out[0][1]]) == str(g["tet_xyz_sha"][i])
+        for x, y in zip(out[0], out[1]):
+            assert np.array_equal(x, y)
+    finally:
+        c.close()
 
 
 def test_refine_then_brick_again(ctx, golden):
