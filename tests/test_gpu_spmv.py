@@ -157,19 +157,27 @@ def test_spmv_split_edges(ctxs):
 
 def test_spmv_pair_large(ctxs):
     """The pair kernel on a matrix of 9M stored entries (a few hundred blocks of 64 slices each, several chunks
-    per block) and the default kernel (FP64), bit-identical to the forced FP64 context; an unknown kernel is
-    refused."""
-    pair, native = ctxs
+    per block) and the default kernel (FP64), bit-identical to a context forced to FP64 at the same launch
+    shape; an unknown kernel is refused.  The balanced kernel's warps split a block's column work, so the
+    order in which a row's partial sums meet follows the grid: two contexts compare bit for bit only at the
+    same shape (the fixed default here, autotuning off in both), and each is checked against the FP64 bound."""
+    pair, _ = ctxs
     rng = np.random.default_rng(21)
     m = 400000
     rp, ci, v = _random_csr(rng, rng.integers(18, 26, m), m)
     assert rp[-1] >= 8 << 20
     x = rng.uniform(-1, 1, m)
     _check(_spmv(pair, rp, ci, v, x), rp, ci, v, x, PAIR_REL)
-    default = tf.TraceFEM()
+    default, native = tf.TraceFEM(), tf.TraceFEM()
     try:
         with pytest.raises(tf.TraceFEMError):
             default.spmv_options(2)
-        assert np.array_equal(_spmv(default, rp, ci, v, x), _spmv(native, rp, ci, v, x))
+        native.spmv_options(tf.SPMV_KERNEL_FP64)
+        default.autotune(False)
+        native.autotune(False)
+        y = _spmv(default, rp, ci, v, x)
+        _check(y, rp, ci, v, x, FP64_REL)
+        assert np.array_equal(y, _spmv(native, rp, ci, v, x))
     finally:
         default.close()
+        native.close()
