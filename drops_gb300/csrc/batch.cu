@@ -160,12 +160,28 @@ __device__ __forceinline__ void cta_sum(const V (&v)[NV], double* sh, F f) {
     __syncthreads();
 }
 
+// <row of A, x> by a group of G lanes (aligned inside the warp); every lane of
+// the group receives the sum.  All 32 lanes of the warp must call it.
+template <int G, class V, class F>
+__device__ __forceinline__ V group_row_dot(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                           const V* __restrict__ val, int64_t row, bool valid, int sub, F xval) {
+    V acc = V(0);
+    if (valid) {
+        const int32_t b = __ldg(rowptr + row), e = __ldg(rowptr + row + 1);
+        for (int32_t k = b + sub; k < e; k += G) acc += __ldg(val + k) * xval(__ldg(col + k));
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    return acc;
+}
+
 // Two rows at once, row0 and row1, by the same group of G lanes: both rows'
 // row pointers, then rounds of U entries of each row whose column and value
 // loads are issued together, then their x gathers.  A pass over the rows thus
 // waits for one chain of dependent loads for two rows.  Each row's products
-// are added in k order; every lane of the group receives both sums, and all
-// 32 lanes of the warp must call it.
+// are added in k order, as group_row_dot adds them; every lane of the group
+// receives both sums, and all 32 lanes of the warp must call it.  (The FP32
+// iterations use it; in FP64 it was slower than one row at a time.)
 template <int G, class V, class F>
 __device__ __forceinline__ void group_row_dot2(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                                                const V* __restrict__ val, int64_t row0, bool ok0, int64_t row1,
@@ -278,27 +294,22 @@ __device__ void batch_pcg_instance(const BatchPcgArgs& a, int inst, double* sh, 
     // r = b - A x (FP64), z = r / d (p = z the first time); sums <r,r>, <b,b>, <z,r>
     auto true_residual = [&](bool first) {
         double v[3] = {0., 0., 0.};
-        // rows base + slot and base + per_pass + slot, in that order
-        for (int64_t base = r0; base < r1; base += 2 * per_pass) {
-            const int64_t rows[2] = {base + slot, base + per_pass + slot};
-            double ax[2];
-            group_row_dot2<G, double>(a.rowptr, a.col, a.val64, rows[0], rows[0] < r1, rows[1], rows[1] < r1, sub,
-                                      [&](int32_t j) { return a.x[j]; }, ax[0], ax[1]);
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int64_t row = rows[h];
-                if (row < r1 && sub == 0) {
-                    const double bi = a.b[row];
-                    const double ri = bi - ax[h];
-                    const V rv = (V)ri;
-                    const V zv = rv / d[row];
-                    r[row] = rv;
-                    z[row] = zv;
-                    if (first) pa[row] = zv;
-                    v[0] += ri * ri;
-                    v[1] += bi * bi;
-                    v[2] += (double)(zv * rv);
-                }
+        for (int64_t base = r0; base < r1; base += per_pass) {
+            const int64_t row = base + slot;
+            const bool valid = row < r1;
+            const double ax = group_row_dot<G, double>(a.rowptr, a.col, a.val64, row, valid, sub,
+                                                       [&](int32_t j) { return a.x[j]; });
+            if (valid && sub == 0) {
+                const double bi = a.b[row];
+                const double ri = bi - ax;
+                const V rv = (V)ri;
+                const V zv = rv / d[row];
+                r[row] = rv;
+                z[row] = zv;
+                if (first) pa[row] = zv;
+                v[0] += ri * ri;
+                v[1] += bi * bi;
+                v[2] += (double)(zv * rv);
             }
         }
         if (first) {
@@ -338,20 +349,35 @@ __device__ void batch_pcg_instance(const BatchPcgArgs& a, int inst, double* sh, 
         // phase A: p_new = z + beta p_old (on the fly), q = A p_new, <q, p_new>
         {
             V v[1] = {V(0)};
-            // rows base + slot and base + per_pass + slot, in that order
-            for (int64_t base = r0; base < r1; base += 2 * per_pass) {
-                const int64_t rows[2] = {base + slot, base + per_pass + slot};
-                V acc[2];
-                group_row_dot2<G, V>(a.rowptr, a.col, val, rows[0], rows[0] < r1, rows[1], rows[1] < r1, sub,
-                                     [&](int32_t j) { return z[j] + beta * pc[j]; }, acc[0], acc[1]);
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int64_t row = rows[h];
-                    if (row < r1 && sub == 0) {
+            if constexpr (!kMixed) {
+                for (int64_t base = r0; base < r1; base += per_pass) {
+                    const int64_t row = base + slot;
+                    const bool valid = row < r1;
+                    const V acc = group_row_dot<G, V>(a.rowptr, a.col, val, row, valid, sub,
+                                                      [&](int32_t j) { return z[j] + beta * pc[j]; });
+                    if (valid && sub == 0) {
                         const V pi = z[row] + beta * pc[row];
                         pn[row] = pi;
-                        q[row] = acc[h];
-                        v[0] += acc[h] * pi;
+                        q[row] = acc;
+                        v[0] += acc * pi;
+                    }
+                }
+            } else {
+                // rows base + slot and base + per_pass + slot, in that order
+                for (int64_t base = r0; base < r1; base += 2 * per_pass) {
+                    const int64_t rows[2] = {base + slot, base + per_pass + slot};
+                    V acc[2];
+                    group_row_dot2<G, V>(a.rowptr, a.col, val, rows[0], rows[0] < r1, rows[1], rows[1] < r1, sub,
+                                         [&](int32_t j) { return z[j] + beta * pc[j]; }, acc[0], acc[1]);
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int64_t row = rows[h];
+                        if (row < r1 && sub == 0) {
+                            const V pi = z[row] + beta * pc[row];
+                            pn[row] = pi;
+                            q[row] = acc[h];
+                            v[0] += acc[h] * pi;
+                        }
                     }
                 }
             }
