@@ -293,6 +293,10 @@ struct Engine {
         X.s = s;
         X.pool = dev ? pool : nullptr;
         X.nsm = nsm;
+        if (dev && cudaMallocHost(&pin, kPinBytes) != cudaSuccess) {
+            pin = nullptr;  // unstaged copies still work
+            cudaGetLastError();
+        }
         setup(tv), setup(te), setup(tlev), setup(tpar), setup(tch), setup(ev), setup(elev), setup(emfr), setup(emid);
         setup(esub), setup(vlev), setup(cnt), setup(tmp32), setup(hval), setup(tmp64), setup(tnch), setup(trule);
         setup(sel_n);
@@ -300,6 +304,7 @@ struct Engine {
         setup(flag8), setup(vx), setup(hkey), setup(rules), setup(cub_tmp);
     }
     ~Engine() {
+        if (pin) cudaFreeHost(pin);
         tv.release(), te.release(), tlev.release(), tpar.release(), tch.release(), ev.release(), elev.release();
         emfr.release(), emid.release(), esub.release(), vlev.release(), cnt.release(), tmp32.release();
         sel_n.release();
@@ -321,19 +326,28 @@ struct Engine {
         V.cape = std::min({ev.cap / 2, elev.cap, emfr.cap, emid.cap, esub.cap / 2, erm.cap, ealive.cap, esplit.cap});
         return V;
     }
-    // host copies of small device values
+    // Host copies of device values, synchronous.  Small ones (the counts read
+    // before each creating pass) go through a pinned staging buffer: a copy
+    // from or to pageable memory would pass through the driver's own staging.
+    static constexpr size_t kPinBytes = 256;
+    void* pin = nullptr;
     void get(void* dst, const void* src, size_t bytes) {
         if (X.dev) {
-            if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, X.s) != cudaSuccess ||
+            const bool staged = pin && bytes <= kPinBytes;
+            if (cudaMemcpyAsync(staged ? pin : dst, src, bytes, cudaMemcpyDeviceToHost, X.s) != cudaSuccess ||
                 cudaStreamSynchronize(X.s) != cudaSuccess)
                 ok = false;
+            else if (staged)
+                std::memcpy(dst, pin, bytes);
         } else {
             std::memcpy(dst, src, bytes);
         }
     }
     void put(void* dst, const void* src, size_t bytes) {
         if (X.dev) {
-            if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, X.s) != cudaSuccess ||
+            const bool staged = pin && bytes <= kPinBytes;
+            if (staged) std::memcpy(pin, src, bytes);
+            if (cudaMemcpyAsync(dst, staged ? pin : src, bytes, cudaMemcpyHostToDevice, X.s) != cudaSuccess ||
                 cudaStreamSynchronize(X.s) != cudaSuccess)
                 ok = false;
         } else {
@@ -390,8 +404,7 @@ struct Engine {
         }
         int64_t total = 0;
         if (X.dev) {
-            const int32_t zero = 0;
-            if (cudaMemcpyAsync(in + n, &zero, sizeof zero, cudaMemcpyHostToDevice, X.s) != cudaSuccess) ok = false;
+            if (cudaMemsetAsync(in + n, 0, sizeof(int32_t), X.s) != cudaSuccess) ok = false;
             size_t bytes = 0;
             cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, tmp64.p, (int)(n + 1), X.s);
             if (!cub_tmp.grow((int64_t)bytes + 1, 0)) {
