@@ -123,8 +123,9 @@ constexpr int64_t kPrepChunk = 1 << 18;  // tets per prep pass (about 0.6 GB of 
 template <bool LIN>
 __global__ void __launch_bounds__(128) k_prep_tets(AsmArgs A) {
     TetPrep* const out = reinterpret_cast<TetPrep*>(A.prep);
-    for (int64_t r = A.c0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < A.c1;
-         r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t n = A.c1 - A.c0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = A.c0 + (A.prep_order ? A.prep_order[i] : i);
         TetPrep& Q = out[r - A.c0];
         const int32_t t = A.active[r];
         int32_t v[4], e[6];
@@ -244,6 +245,28 @@ __global__ void __launch_bounds__(128) k_prep_tets(AsmArgs A) {
                 Q.G[vv][c] = ff_split(g.G[vv][c]);
                 Q.X[vv][c] = ff_split(g.X[vv][c]);
             }
+    }
+}
+
+// Sort key of a tet for k_prep_tets: the signs (-, 0, +) of its 10 lattice
+// values in base 3.  They fix every branch of the prep (which lattice edges
+// are cut, each sub-tet's pattern and facets).  Signs from the bits: -0 and
+// +0 are zero, NaN counts by its sign bit (the key only orders the threads).
+constexpr int kPrepKeyBits = 16;  // 3^10 = 59,049 < 2^16
+__global__ void k_prep_key(AsmArgs A, uint32_t* __restrict__ key, int32_t* __restrict__ idx) {
+    const int64_t n = A.c1 - A.c0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int32_t v[4], e[6];
+        mesh_tet(A.M, A.active[A.c0 + i], v, e);
+        uint32_t k = 0;
+        for (int j = 0; j < 10; ++j) {
+            const unsigned long long b =
+                (unsigned long long)__double_as_longlong(j < 4 ? A.lsv[v[j]] : A.lse[e[j - 4]]);
+            const uint32_t sg = (b << 1) == 0ull ? 1u : (b >> 63) ? 0u : 2u;
+            k = 3u * k + sg;
+        }
+        key[i] = k;
+        idx[i] = (int32_t)i;
     }
 }
 

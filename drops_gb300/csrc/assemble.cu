@@ -21,6 +21,8 @@
 // reference's triangulation-order accumulation, without atomics.
 #include <climits>
 
+#include <cub/device/device_radix_sort.cuh>
+
 #include "ff.cuh"
 #include "tf_internal.cuh"
 
@@ -524,6 +526,7 @@ struct AsmArgs {
     // pair forms: the per-tet records of active tets [c0, c1) (k_prep_tets)
     void* prep;
     int64_t c0, c1;
+    const int32_t* prep_order;  // prep thread i takes active tet c0 + prep_order[i] (null: c0 + i)
 };
 
 template <int NL>
@@ -794,6 +797,30 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs A) {
 
 #include "asm_pair.cuh"
 
+// The order of the prep threads over active tets [A.c0, A.c1): by the sign
+// pattern of each tet's lattice values (k_prep_key), so that a warp's tets
+// take the same branches.  Every thread still writes its own tet's record.
+static int prep_order(Context* c, AsmArgs& A, int64_t chunk) {
+    A.prep_order = nullptr;
+    if (!c->prep_sort) return TF_OK;
+    const int64_t n = A.c1 - A.c0;
+    TF_TRY(ensure(c, c->prep_key, (size_t)(2 * chunk)));
+    TF_TRY(ensure(c, c->prep_idx, (size_t)(2 * chunk)));
+    uint32_t* key = c->prep_key.p;
+    int32_t* idx = c->prep_idx.p;
+    k_prep_key<<<grid_for(c, n, 256), 256, 0, c->stream>>>(A, key, idx);
+    ++c->launches;
+    TF_CUDA(c, cudaGetLastError());
+    size_t bytes = 0;
+    TF_CUDA(c, cub::DeviceRadixSort::SortPairs(nullptr, bytes, key, key + chunk, idx, idx + chunk, (int)n, 0,
+                                                kPrepKeyBits, c->stream));
+    TF_TRY(ensure(c, c->prep_tmp, bytes + 1));
+    TF_CUDA(c, cub::DeviceRadixSort::SortPairs(c->prep_tmp.p, bytes, key, key + chunk, idx, idx + chunk, (int)n, 0,
+                                                kPrepKeyBits, c->stream));
+    A.prep_order = idx + chunk;
+    return TF_OK;
+}
+
 // ---------------------------------------------------------------------------
 // CSR pattern: contributions bucketed by row, sorted by (column, contribution)
 // ---------------------------------------------------------------------------
@@ -1059,6 +1086,7 @@ int setup_fe_system(Context* c, unsigned forms, int rhs_kind, const double* rhs_
                 A.c0 = c0;
                 A.c1 = std::min<int64_t>(na, c0 + chunk);
                 const int64_t n = A.c1 - A.c0;
+                TF_TRY(prep_order(c, A, chunk));
                 k_prep_tets<false><<<grid_for(c, n, 128), 128, 0, c->stream>>>(A);
                 k_assemble_p2_pair<<<grid_for(c, (n + kAsmWarps - 1) / kAsmWarps, 1, 8), 32 * kAsmWarps, sm,
                                      c->stream>>>(A);
@@ -1078,6 +1106,7 @@ int setup_fe_system(Context* c, unsigned forms, int rhs_kind, const double* rhs_
                 A.c0 = c0;
                 A.c1 = std::min<int64_t>(na, c0 + chunk);
                 const int64_t n = A.c1 - A.c0;
+                TF_TRY(prep_order(c, A, chunk));
                 k_prep_tets<true><<<grid_for(c, n, 128), 128, 0, c->stream>>>(A);
                 k_assemble_p1_pair<<<grid_for(c, (n + kAsmWarps - 1) / kAsmWarps, 1, 8), 32 * kAsmWarps, sm,
                                      c->stream>>>(A);

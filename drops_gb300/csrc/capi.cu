@@ -137,6 +137,7 @@ int tf_create(tf_context** out, int device) {
     if (const char* e = std::getenv("TF_PCG_RES_VCAP_KB")) c->pcg_res_vcap_kb = std::atoi(e);
     if (const char* e = std::getenv("TF_PCG_REL_UPDATE")) c->pcg_rel_update = std::atof(e);
     if (const char* e = std::getenv("TF_BATCH_REL_UPDATE")) c->batch_rel_update = std::atof(e);
+    if (const char* e = std::getenv("TF_PREP_SORT")) c->prep_sort = std::atoi(e) != 0;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
         cudaMallocHost((void**)&c->h_status, 4 * sizeof(int)) != cudaSuccess ||
@@ -207,6 +208,9 @@ int tf_destroy(tf_context* t) {
     tf::release(c->qq_base);
     tf::release(c->qq_idx);
     tf::release(c->prep1);
+    tf::release(c->prep_key);
+    tf::release(c->prep_idx);
+    tf::release(c->prep_tmp);
     tf::release(c->tune_buf);
     tf::release(c->ch_ring);
     tf::release(c->ch_av);

@@ -397,6 +397,10 @@ struct Context {
     DBuf<double> qq_grad;  // isoparametric P2: recovered level-set gradient per interface DOF
     DBuf<double> qq_base;   // isoparametric P2: per cut tet its data, per quadrature point the base point and the point data
     DBuf<int32_t> qq_idx;   // isoparametric P2: points per tet, their offsets, each point's tet
+    DBuf<uint32_t> prep_key;      // pair forms: sort keys of the prep threads (2 x chunk)
+    DBuf<int32_t> prep_idx;       // and their tets (2 x chunk)
+    DBuf<unsigned char> prep_tmp;
+    bool prep_sort = true;        // prep threads ordered by the tets' sign patterns
     DBuf<unsigned char> prep1;  // P1 pair forms: per-tet records of one chunk of active tets
     DBuf<double> ch_prev, ch_x1, ch_x2;  // adaptive BDF1/BDF2: chi_prev, BDF1 and BDF2 states
     DBuf<float> ch_xyz, ch_nrm, ch_Y, ch_pred;
