@@ -678,3 +678,38 @@ def test_patch_topology_bitexact(ctx, golden):
         assert np.array_equal(v, g["patch_verts"][4 * vo:4 * (vo + nv)].reshape(-1, 4))
         fo += k
         vo += nv
+
+
+def _pair_forms(sort, fe, kind, par, p2ls, n):
+    """M, A, C_n values and the load vector from a fresh context whose TF_PREP_SORT is `sort`."""
+    import os
+
+    old = os.environ.get("TF_PREP_SORT")
+    os.environ["TF_PREP_SORT"] = sort
+    try:
+        c = tf.TraceFEM()
+    finally:
+        if old is None:
+            os.environ.pop("TF_PREP_SORT", None)
+        else:
+            os.environ["TF_PREP_SORT"] = old
+    try:
+        c.brick_cube(n, 5.0 / 3.0)
+        c.levelset_analytic(kind, par, p2ls)
+        c.distribute_dofs(fe)
+        c.setup_fe_system([tf.FORM_M, tf.FORM_A, tf.FORM_CN], tf.RHS_SPHERE_XYZ, [0, 0, 0, 1.0, 13.0])
+        return [c.matrix(f)[2] for f in (tf.FORM_M, tf.FORM_A, tf.FORM_CN)] + [c.vec_download(tf.VEC_RHS)]
+    finally:
+        c.close()
+
+
+@pytest.mark.parametrize("fe,kind,par,p2ls", [(tf.P2IF, tf.LS_ELLIPSOID, ELLIPSOID, True),
+                                              (tf.P1IF, tf.LS_SPHERE, [0, 0, 0, 1.0], False),
+                                              (tf.P1IF, tf.LS_TORUS, [1.0, 0.4, 2], True)])
+def test_prep_order_leaves_forms_unchanged(ctx, fe, kind, par, p2ls):
+    """The pair forms' per-tet pass runs its threads ordered by the tets' sign patterns (the default) or in tet
+    order (TF_PREP_SORT=0).  Each thread writes its own tet's record, so the forms are bit-identical."""
+    a = _pair_forms("1", fe, kind, par, p2ls, 24)
+    b = _pair_forms("0", fe, kind, par, p2ls, 24)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
