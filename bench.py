@@ -846,12 +846,14 @@ def run_refine(args):
         assert st == tf.OK and res <= 1e-10
     ctx.close()
     ms = statistics.median(ts)
-    return {"refine_ms": round(statistics.median(tr), 1), "levels": last, "steps": steps, "tets": nt, "vertices": nv,
+    return {"refine_ms": round(statistics.median(tr), 1), "refine_first_ms": round(tr[0], 1), "levels": last,
+            "steps": steps, "tets": nt, "vertices": nv,
             "cut_tets": na, "dofs": m, "path_ms": round(ms, 3), "cut_tets_per_s": round(na / (ms / 1e3), 1),
             "pcg_iters": int(statistics.median(its)),
             "note": f"{REFINE_N}^3 Kuhn cubes on [-5/3,5/3]^3 refined towards the unit sphere (width "
                     f"{REFINE_WIDTH}, levels 0..{REFINE_LEVELS}); refine_ms: tf_mesh_refine_band on the device (wall "
-                    "clock), path_ms: the P2 path with mixed PCG on the device, L2 flushed before each path"}
+                    "clock, median of 3 calls in one context; the first call, refine_first_ms, also fills the "
+                    "context's memory pool), path_ms: the P2 path with mixed PCG on the device, L2 flushed before each path"}
 
 
 def refine_cpu_sample():
